@@ -1,0 +1,177 @@
+"""ctypes mirror of ``include/dem_hotpath.h`` and ``include/dem_workloads.h``.
+
+Loads the in-tree ``libexadem_gb300.so``.  There is no fallback: if the library
+is missing the import of the compute path raises, so a GPU run can never
+silently take another path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libexadem_gb300.so"
+
+DEM_OK = 0
+ERRORS = {1: "DEM_ERR_INVALID_ARG", 2: "DEM_ERR_CUDA", 3: "DEM_ERR_OOM", 4: "DEM_ERR_UNSUPPORTED",
+          5: "DEM_ERR_OVERFLOW", 6: "DEM_ERR_TIMEOUT", 7: "DEM_ERR_STATE", 8: "DEM_ERR_NO_DEVICE"}
+
+ITYPE_VERTEX_VERTEX = 0
+ITYPE_VERTEX_EDGE = 1
+ITYPE_VERTEX_FACE = 2
+ITYPE_EDGE_EDGE = 3
+ITYPE_VERTEX_CYLINDER = 4
+ITYPE_VERTEX_SURFACE = 5
+LAW_HOOKE_NONE = 0
+LAW_HOOKE_COHESIVE = 1
+
+D = C.c_double
+PD = C.POINTER(C.c_double)
+PU64 = C.POINTER(C.c_uint64)
+PU32 = C.POINTER(C.c_uint32)
+PU16 = C.POINTER(C.c_uint16)
+PU8 = C.POINTER(C.c_uint8)
+
+
+class ContactParams(C.Structure):
+    _fields_ = [("kn", D), ("kt", D), ("kr", D), ("mu", D), ("damp_rate", D), ("fc", D), ("dncut", D)]
+
+
+class Params(C.Structure):
+    _fields_ = [("bounds_lo", D * 3), ("bounds_hi", D * 3), ("periodic", C.c_int32 * 3),
+                ("rcut_inc", D), ("cell_size", D), ("dt", D), ("gravity", D * 3),
+                ("symetric", C.c_int32), ("law", C.c_int32),
+                ("config", ContactParams), ("config_driver", ContactParams),
+                ("fp32_broad_phase", C.c_int32), ("fp32_contact_screen", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
+
+
+PARTICLE_FIELDS = ["rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz",
+                   "vrotx", "vroty", "vrotz", "arotx", "aroty", "arotz", "momx", "momy", "momz",
+                   "qw", "qx", "qy", "qz", "inertiax", "inertiay", "inertiaz", "mass", "radius", "homothety"]
+
+
+class Particles(C.Structure):
+    _fields_ = [("n", C.c_uint64)] + [(f, PD) for f in PARTICLE_FIELDS] + [
+        ("id", PU64), ("type", PU32), ("group", PU32)]
+
+
+class Surface(C.Structure):
+    _fields_ = [("offset", D), ("normal", D * 3), ("center", D * 3), ("vel", D * 3), ("vrot", D * 3)]
+
+
+class Cylinder(C.Structure):
+    _fields_ = [("radius", D), ("axis", D * 3), ("center", D * 3), ("vel", D * 3), ("vrot", D * 3)]
+
+
+class State(C.Structure):
+    _fields_ = [("kinetic_energy", D * 3), ("rotation_energy", D * 3), ("mass", D),
+                ("n_particles", C.c_uint64), ("n_interactions", C.c_uint64),
+                ("n_active_interactions", C.c_uint64)]
+
+
+class InteractionList(C.Structure):
+    _fields_ = [("capacity", C.c_uint64), ("count", C.c_uint64), ("owner_id", PU64), ("partner_id", PU64),
+                ("type", PU16), ("swap", PU8), ("owner_sub", PU32), ("partner_sub", PU32),
+                ("friction", PD), ("moment", PD)]
+
+
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 24), ("launches", C.c_uint64), ("timed", C.c_uint64), ("total_ms", D)]
+
+
+class RsaSpec(C.Structure):
+    _fields_ = [("n", C.c_uint64), ("rmin", D), ("rmax", D), ("density", D), ("lo", D * 3), ("hi", D * 3),
+                ("periodic", C.c_int32 * 3), ("grow_axis", C.c_int32), ("region", C.c_int32),
+                ("cyl_center", D * 2), ("cyl_radius", D), ("vmin", D), ("vmax", D), ("seed", C.c_uint64),
+                ("max_attempts", C.c_uint64), ("id_offset", C.c_uint64)]
+
+
+def ptr(a: np.ndarray | None, ctype=PD):
+    if a is None:
+        return C.cast(None, ctype)
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctype)
+
+
+def particles_struct(arrays: dict, n: int) -> Particles:
+    """Builds a Particles view over numpy arrays (kept alive by the caller)."""
+    p = Particles()
+    p.n = n
+    for f in PARTICLE_FIELDS:
+        setattr(p, f, ptr(arrays.get(f)))
+    p.id = ptr(arrays.get("id"), PU64)
+    p.type = ptr(arrays.get("type"), PU32)
+    p.group = ptr(arrays.get("group"), PU32)
+    return p
+
+
+# ---- function signatures shared by the library and the oracle ---------------
+_CTX = C.c_void_p
+
+
+def _sig(lib, name, args, res=C.c_int):
+    fn = getattr(lib, name)
+    fn.argtypes = args
+    fn.restype = res
+    return fn
+
+
+def declare_library(lib) -> None:
+    _sig(lib, "dem_ctx_create", [C.POINTER(Params), C.POINTER(_CTX)])
+    _sig(lib, "dem_ctx_destroy", [_CTX])
+    _sig(lib, "dem_last_error", [_CTX], C.c_char_p)
+    _sig(lib, "dem_ctx_stream", [_CTX, C.POINTER(C.c_void_p)])
+    _sig(lib, "dem_set_params", [_CTX, C.POINTER(Params)])
+    _sig(lib, "dem_set_particles", [_CTX, C.POINTER(Particles), C.c_int])
+    _sig(lib, "dem_get_particles", [_CTX, C.POINTER(Particles), C.c_int])
+    _sig(lib, "dem_register_surface", [_CTX, C.POINTER(Surface)])
+    _sig(lib, "dem_register_cylinder", [_CTX, C.POINTER(Cylinder)])
+    _sig(lib, "dem_particle_displ_over", [_CTX, C.POINTER(C.c_int)])
+    for name in ["dem_update_particle_neighbors", "dem_reset_force_moment", "dem_gravity_force",
+                 "dem_contact_sphere", "dem_force_to_accel", "dem_combined_compute_prolog",
+                 "dem_combined_compute_epilog", "dem_first_iteration"]:
+        _sig(lib, name, [_CTX])
+    _sig(lib, "dem_step", [_CTX, C.c_int])
+    _sig(lib, "dem_rebuild_count", [_CTX, PU64])
+    _sig(lib, "dem_simulation_state", [_CTX, C.POINTER(State)])
+    _sig(lib, "dem_interaction_count", [_CTX, PU64])
+    _sig(lib, "dem_get_interactions", [_CTX, C.POINTER(InteractionList)])
+    _sig(lib, "dem_packing_profile", [_CTX, C.c_int, D, D, PD])
+    _sig(lib, "dem_generate_rsa_spheres", [C.POINTER(RsaSpec), C.POINTER(Particles), PD])
+    _sig(lib, "dem_profile", [_CTX, C.c_int])
+    _sig(lib, "dem_kernel_stats", [_CTX, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)])
+    _sig(lib, "dem_reset_kernel_stats", [_CTX])
+
+
+# Symbols declared in include/dem_hotpath.h and include/dem_workloads.h.
+EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stream", "dem_set_params",
+            "dem_set_particles", "dem_get_particles", "dem_register_surface", "dem_register_cylinder",
+            "dem_particle_displ_over", "dem_update_particle_neighbors", "dem_reset_force_moment",
+            "dem_gravity_force", "dem_contact_sphere", "dem_force_to_accel", "dem_combined_compute_prolog",
+            "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
+            "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
+            "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats"]
+
+_LIB = None
+
+
+def load(path: Path | None = None):
+    """Loads (once) and returns the native library; raises if it is not built."""
+    global _LIB
+    if _LIB is None:
+        p = Path(path) if path else LIB_PATH
+        if not p.exists():
+            raise RuntimeError(f"native library missing: {p} (run exadem_gb300.build.build())")
+        lib = C.CDLL(str(p))
+        declare_library(lib)
+        _LIB = lib
+    return _LIB
+
+
+class DemError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str = ""):
+        super().__init__(f"{where}: {ERRORS.get(code, code)} {msg}".strip())
+        self.code = code

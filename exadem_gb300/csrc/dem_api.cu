@@ -1,0 +1,622 @@
+// dem_api.cu -- C ABI of the GB300 DEM hot path: context, memory, operator entry points.
+//
+// Each dem_* function stands in for one exaDEM operator (see include/dem_hotpath.h
+// for the reference citations).  Host code only orchestrates: all per-particle
+// and per-interaction work runs in the kernels of k_*.cu on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "dem_ctx.cuh"
+
+using namespace dem;
+
+namespace {
+
+int check_params(dem_ctx* c, const dem_params* p) {
+  if (!p) return c->fail(DEM_ERR_INVALID_ARG, "params is NULL");
+  for (int d = 0; d < 3; d++)
+    if (!(p->bounds_hi[d] > p->bounds_lo[d])) return c->fail(DEM_ERR_INVALID_ARG, "empty domain bounds");
+  if (!(p->rcut_inc >= 0)) return c->fail(DEM_ERR_INVALID_ARG, "rcut_inc must be >= 0");
+  if (!(p->dt > 0)) return c->fail(DEM_ERR_INVALID_ARG, "dt must be > 0");
+  if (p->symetric != 1) return c->fail(DEM_ERR_UNSUPPORTED, "only symetric: true is supported");
+  if (p->law != DEM_LAW_HOOKE_NONE && p->law != DEM_LAW_HOOKE_COHESIVE)
+    return c->fail(DEM_ERR_UNSUPPORTED, "unknown contact law");
+  if (p->law == DEM_LAW_HOOKE_NONE && (p->config.dncut > 0 || p->config_driver.dncut > 0))
+    return c->fail(DEM_ERR_INVALID_ARG,
+                   "dncut is != 0 while the cohesive force is not used (contact_force_sphere.cu.in:280-292)");
+  if (p->law == DEM_LAW_HOOKE_COHESIVE && (p->config.dncut == 0 || p->config_driver.dncut == 0))
+    return c->fail(DEM_ERR_INVALID_ARG, "cohesive law needs dncut > 0");
+  return DEM_OK;
+}
+
+void free_particles(dem_ctx* c) {
+  for (int b = 0; b < 2; b++) {
+    if (c->pblock[b]) cudaFree(c->pblock[b]);
+    c->pblock[b] = nullptr;
+    c->P[b] = PArrays{};
+  }
+  c->pcap = 0;
+}
+
+int alloc_particles(dem_ctx* c, uint64_t n) {
+  if (n <= c->pcap && c->pblock[0]) return DEM_OK;
+  free_particles(c);
+  const uint64_t cap = std::max<uint64_t>(n, 1);
+  const size_t per = NPF * sizeof(double) + sizeof(uint64_t) + 2 * sizeof(uint32_t);
+  for (int b = 0; b < 2; b++) {
+    DEM_CUDA_TRY(c, cudaMalloc(&c->pblock[b], per * cap + 1024));
+    char* base = static_cast<char*>(c->pblock[b]);
+    for (int f = 0; f < NPF; f++) c->P[b].f[f] = reinterpret_cast<double*>(base + (size_t)f * cap * sizeof(double));
+    base += (size_t)NPF * cap * sizeof(double);
+    c->P[b].id = reinterpret_cast<uint64_t*>(base);
+    base += cap * sizeof(uint64_t);
+    c->P[b].type = reinterpret_cast<uint32_t*>(base);
+    base += cap * sizeof(uint32_t);
+    c->P[b].group = reinterpret_cast<uint32_t*>(base);
+  }
+  // per-particle index arrays
+  cudaFree(c->cell_of);
+  cudaFree(c->cell_tmp);
+  cudaFree(c->perm);
+  cudaFree(c->pcnt);
+  cudaFree(c->rev_off);
+  cudaFree(c->rev_cnt);
+  cudaFree(c->own_off[0]);
+  cudaFree(c->own_off[1]);
+  DEM_CUDA_TRY(c, cudaMalloc(&c->cell_of, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->cell_tmp, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->perm, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->pcnt, (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->rev_off, (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->rev_cnt, (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->own_off[0], (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->own_off[1], (cap + 1) * 4));
+  c->pcap = cap;
+  return DEM_OK;
+}
+
+void free_iarrays(IArrays& I) {
+  cudaFree(I.owner);
+  cudaFree(I.partner);
+  cudaFree(I.pid);
+  cudaFree(I.meta);
+  for (int d = 0; d < 3; d++) {
+    cudaFree(I.ft[d]);
+    cudaFree(I.mo[d]);
+  }
+  I = IArrays{};
+}
+
+int alloc_iarrays(dem_ctx* c, int b, uint64_t need) {
+  if (need <= c->icap[b] && c->I[b].owner) return DEM_OK;
+  free_iarrays(c->I[b]);
+  c->icap[b] = 0;
+  const uint64_t cap = need + need / 4 + 4096;
+  IArrays& I = c->I[b];
+  DEM_CUDA_TRY(c, cudaMalloc(&I.owner, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&I.partner, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&I.pid, cap * 8));
+  DEM_CUDA_TRY(c, cudaMalloc(&I.meta, cap * 4));
+  for (int d = 0; d < 3; d++) {
+    DEM_CUDA_TRY(c, cudaMalloc(&I.ft[d], cap * 8));
+    DEM_CUDA_TRY(c, cudaMalloc(&I.mo[d], cap * 8));
+  }
+  c->icap[b] = cap;
+  return DEM_OK;
+}
+
+int alloc_records(dem_ctx* c, uint64_t need) {
+  if (need <= c->rcap && c->rev_idx) return DEM_OK;
+  for (int d = 0; d < 3; d++) {
+    cudaFree(c->R.f[d]);
+    cudaFree(c->R.ti[d]);
+    cudaFree(c->R.tj[d]);
+  }
+  c->R = Records{};
+  cudaFree(c->rev_idx);
+  c->rev_idx = nullptr;
+  c->rcap = 0;
+  const uint64_t cap = need + need / 4 + 4096;
+  for (int d = 0; d < 3; d++) {
+    DEM_CUDA_TRY(c, cudaMalloc(&c->R.f[d], cap * 8));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->R.ti[d], cap * 8));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->R.tj[d], cap * 8));
+  }
+  DEM_CUDA_TRY(c, cudaMalloc(&c->rev_idx, cap * 4));
+  c->rcap = cap;
+  return DEM_OK;
+}
+
+// Cell grid: cell size >= nbh_dist = 2*r_max + rcut_inc (dem_rcut_max.cpp:60, config_globals.msp:35-37).
+int setup_grid(dem_ctx* c) {
+  const dem_params& p = c->prm;
+  const double nd = 2 * c->rad_max + p.rcut_inc;
+  const double cs = std::max(p.cell_size, nd);
+  if (!(cs > 0)) return c->fail(DEM_ERR_INVALID_ARG, "cell size must be > 0");
+  GridDev g{};
+  uint64_t nc = 1;
+  for (int d = 0; d < 3; d++) {
+    g.lo[d] = p.bounds_lo[d];
+    g.hi[d] = p.bounds_hi[d];
+    g.L[d] = p.bounds_hi[d] - p.bounds_lo[d];
+    g.periodic[d] = p.periodic[d] ? 1 : 0;
+    if (g.periodic[d]) {
+      g.dims[d] = std::max(1, (int)std::floor(g.L[d] / cs));
+      if (g.dims[d] < 3) return c->fail(DEM_ERR_INVALID_ARG, "periodic dimension needs at least 3 cells");
+      g.csz[d] = g.L[d] / g.dims[d];
+    } else {
+      g.dims[d] = std::max(1, (int)std::ceil(g.L[d] / cs));
+      g.csz[d] = cs;
+    }
+    nc *= (uint64_t)g.dims[d];
+  }
+  if (nc > (1ull << 31)) return c->fail(DEM_ERR_INVALID_ARG, "cell grid too large; raise cell_size");
+  c->grid = g;
+  c->ncell = nc;
+  if (nc + 1 > c->ccap) {
+    cudaFree(c->cell_cnt);
+    cudaFree(c->cell_start);
+    c->cell_cnt = c->cell_start = nullptr;
+    c->ccap = 0;
+    DEM_CUDA_TRY(c, cudaMalloc(&c->cell_cnt, (nc + 1) * 4));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->cell_start, (nc + 1) * 4));
+    c->ccap = nc + 1;
+  }
+  return DEM_OK;
+}
+
+int update_neighbors(dem_ctx* c) {
+  if (c->n == 0) {
+    c->ni = 0;
+    c->have_list = true;
+    return DEM_OK;
+  }
+  int rc;
+  if ((rc = launch_bin_particles(c))) return rc;
+  if ((rc = launch_reorder_particles(c))) return rc;
+  if ((rc = launch_count_sphere(c))) return rc;
+  const int nw = 1 - c->icur;
+  uint32_t* new_off = c->own_off[nw];
+  if ((rc = scan_exclusive_u32(c, c->pcnt, new_off, c->n))) return rc;
+  uint32_t total = 0;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(&total, new_off + c->n, 4, cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if ((rc = alloc_iarrays(c, nw, total))) return rc;
+  if ((rc = alloc_records(c, total))) return rc;
+  if ((rc = launch_fill_sphere(c, new_off, total))) return rc;
+  c->icur = nw;
+  c->ni = total;
+  c->have_list = true;
+  c->hist_valid = true;
+  if ((rc = launch_reverse_lists(c))) return rc;
+  c->rebuilds++;
+  return DEM_OK;
+}
+
+int compute_force(dem_ctx* c) {
+  int rc;
+  if ((rc = launch_gravity(c))) return rc;
+  if ((rc = launch_contact_sphere(c))) return rc;
+  return launch_gather_forces(c);
+}
+
+int need_list(dem_ctx* c) {
+  if (!c->have_list) return c->fail(DEM_ERR_STATE, "no interaction list: call dem_update_particle_neighbors first");
+  return DEM_OK;
+}
+
+int copy_field(dem_ctx* c, double* dst, const double* src, uint64_t n, cudaMemcpyKind k) {
+  if (!dst || !src || !n) return DEM_OK;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(dst, src, n * sizeof(double), k, c->stream));
+  return DEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dem_ctx_create(const dem_params* params, dem_ctx** out) {
+  if (!out) return DEM_ERR_INVALID_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DEM_ERR_NO_DEVICE;
+  dem_ctx* c = new (std::nothrow) dem_ctx();
+  if (!c) return DEM_ERR_OOM;
+  int rc = check_params(c, params);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  c->prm = *params;
+  cudaGetDevice(&c->device);
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->d_scalars, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost(&c->h_scalars, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&c->drv_dev, DEM_MAX_DRIVERS * sizeof(DriverDev)) != cudaSuccess) {
+    dem_ctx_destroy(c);
+    return DEM_ERR_CUDA;
+  }
+  c->red_cap = std::max<uint64_t>(7ull * 2 * c->num_sms + 16, 4096);
+  if (cudaMalloc(&c->d_red, c->red_cap * sizeof(double)) != cudaSuccess) {
+    dem_ctx_destroy(c);
+    return DEM_ERR_CUDA;
+  }
+  cudaMemset(c->d_scalars, 0, 8 * sizeof(unsigned long long));
+  for (int d = 0; d < 3; d++) c->grid.L[d] = c->prm.bounds_hi[d] - c->prm.bounds_lo[d];
+  *out = c;
+  return DEM_OK;
+}
+
+int dem_ctx_destroy(dem_ctx* c) {
+  if (!c) return DEM_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->fold_events();
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  c->ev_pool.clear();
+  free_particles(c);
+  for (int b = 0; b < 2; b++) {
+    free_iarrays(c->I[b]);
+    cudaFree(c->own_off[b]);
+  }
+  for (int d = 0; d < 3; d++) {
+    cudaFree(c->R.f[d]);
+    cudaFree(c->R.ti[d]);
+    cudaFree(c->R.tj[d]);
+  }
+  cudaFree(c->rev_idx);
+  cudaFree(c->rev_off);
+  cudaFree(c->rev_cnt);
+  cudaFree(c->cell_cnt);
+  cudaFree(c->cell_start);
+  cudaFree(c->cell_of);
+  cudaFree(c->cell_tmp);
+  cudaFree(c->perm);
+  cudaFree(c->pcnt);
+  cudaFree(c->scan_blk);
+  cudaFree(c->d_scalars);
+  cudaFree(c->d_red);
+  cudaFree(c->drv_dev);
+  if (c->h_scalars) cudaFreeHost(c->h_scalars);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return DEM_OK;
+}
+
+const char* dem_last_error(const dem_ctx* c) { return c ? c->last_err.c_str() : "null context"; }
+
+int dem_ctx_stream(dem_ctx* c, void** stream) {
+  if (!c || !stream) return DEM_ERR_INVALID_ARG;
+  *stream = (void*)c->stream;
+  return DEM_OK;
+}
+
+int dem_set_params(dem_ctx* c, const dem_params* p) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  int rc = check_params(c, p);
+  if (rc) return rc;
+  const bool grid_changed = std::memcmp(p->bounds_lo, c->prm.bounds_lo, sizeof(p->bounds_lo)) ||
+                            std::memcmp(p->bounds_hi, c->prm.bounds_hi, sizeof(p->bounds_hi)) ||
+                            std::memcmp(p->periodic, c->prm.periodic, sizeof(p->periodic)) ||
+                            p->rcut_inc != c->prm.rcut_inc || p->cell_size != c->prm.cell_size;
+  c->prm = *p;
+  if (grid_changed && c->n) {
+    if ((rc = setup_grid(c))) return rc;
+    c->have_list = false;  // a new skin or domain needs a rebuild (history is kept by key)
+  }
+  return DEM_OK;
+}
+
+int dem_set_particles(dem_ctx* c, const dem_particles* p, int on_device) {
+  if (!c || !p) return DEM_ERR_INVALID_ARG;
+  if (p->n >= (1ull << 31)) return c->fail(DEM_ERR_INVALID_ARG, "too many particles");
+  if (!p->rx || !p->ry || !p->rz || !p->radius)
+    return c->fail(DEM_ERR_INVALID_ARG, "positions and radius are required");
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const uint64_t n = p->n;
+  int rc = alloc_particles(c, n);
+  if (rc) return rc;
+  c->pcur = 0;
+  PArrays& P = c->P[0];
+  const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const double* src[NPF] = {p->rx, p->ry, p->rz, p->vx, p->vy, p->vz, p->fx, p->fy, p->fz, p->vrotx, p->vroty,
+                            p->vrotz, p->arotx, p->aroty, p->arotz, p->momx, p->momy, p->momz, p->qw, p->qx,
+                            p->qy, p->qz, p->inertiax, p->inertiay, p->inertiaz, p->mass, p->radius, p->homothety,
+                            p->rx, p->ry, p->rz};
+  // defaults for absent fields: 0, except orientation w, inertia, mass and homothety = 1
+  std::vector<double> ones(n ? n : 1, 1.0);
+  for (int f = 0; f < NPF; f++) {
+    if (src[f]) {
+      if ((rc = copy_field(c, P.f[f], src[f], n, k))) return rc;
+    } else if (f == QW || f == IX || f == IY || f == IZ || f == MASS || f == HOM) {
+      if ((rc = copy_field(c, P.f[f], ones.data(), n, cudaMemcpyHostToDevice))) return rc;
+    } else if (n) {
+      DEM_CUDA_TRY(c, cudaMemsetAsync(P.f[f], 0, n * sizeof(double), c->stream));
+    }
+  }
+  std::vector<uint64_t> ids;
+  if (p->id) {
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(P.id, p->id, n * 8, k, c->stream));
+  } else if (n) {
+    ids.resize(n);
+    std::iota(ids.begin(), ids.end(), 0ull);
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(P.id, ids.data(), n * 8, cudaMemcpyHostToDevice, c->stream));
+  }
+  if (p->type) {
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(P.type, p->type, n * 4, k, c->stream));
+  } else if (n) {
+    DEM_CUDA_TRY(c, cudaMemsetAsync(P.type, 0, n * 4, c->stream));
+  }
+  if (p->group) {
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(P.group, p->group, n * 4, k, c->stream));
+  } else if (n) {
+    DEM_CUDA_TRY(c, cudaMemsetAsync(P.group, 0, n * 4, c->stream));
+  }
+  // r_max for nbh_dist (dem_rcut_max.cpp:49-66)
+  std::vector<double> rad(n);
+  if (n) {
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(rad.data(), P.f[RAD], n * 8, cudaMemcpyDeviceToHost, c->stream));
+  }
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  double rmax = 0.0;
+  for (double r : rad) rmax = std::max(rmax, r);
+  c->rad_max = rmax;
+  c->n = n;
+  c->ni = 0;
+  c->have_list = false;
+  c->hist_valid = false;
+  c->rebuilds = 0;
+  return setup_grid(c);
+}
+
+int dem_get_particles(dem_ctx* c, dem_particles* out, int on_device) {
+  if (!c || !out) return DEM_ERR_INVALID_ARG;
+  if (out->n < c->n) return c->fail(DEM_ERR_INVALID_ARG, "output arrays too small");
+  const uint64_t n = c->n;
+  const PArrays& P = c->P[c->pcur];
+  const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  double* dst[BX] = {out->rx, out->ry, out->rz, out->vx, out->vy, out->vz, out->fx, out->fy, out->fz,
+                     out->vrotx, out->vroty, out->vrotz, out->arotx, out->aroty, out->arotz, out->momx,
+                     out->momy, out->momz, out->qw, out->qx, out->qy, out->qz, out->inertiax, out->inertiay,
+                     out->inertiaz, out->mass, out->radius, out->homothety};
+  int rc;
+  for (int f = 0; f < BX; f++)
+    if ((rc = copy_field(c, dst[f], P.f[f], n, k))) return rc;
+  if (out->id && n) DEM_CUDA_TRY(c, cudaMemcpyAsync(out->id, P.id, n * 8, k, c->stream));
+  if (out->type && n) DEM_CUDA_TRY(c, cudaMemcpyAsync(out->type, P.type, n * 4, k, c->stream));
+  if (out->group && n) DEM_CUDA_TRY(c, cudaMemcpyAsync(out->group, P.group, n * 4, k, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  out->n = n;
+  return DEM_OK;
+}
+
+static int add_driver(dem_ctx* c, const DriverDev& d) {
+  if (c->ndrv >= DEM_MAX_DRIVERS) return c->fail(DEM_ERR_INVALID_ARG, "too many drivers");
+  c->drv_host[c->ndrv] = d;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->drv_dev + c->ndrv, &c->drv_host[c->ndrv], sizeof(DriverDev),
+                                  cudaMemcpyHostToDevice, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->ndrv++;
+  c->have_list = false;
+  return DEM_OK;
+}
+
+int dem_register_surface(dem_ctx* c, const dem_surface* s) {
+  if (!c || !s) return DEM_ERR_INVALID_ARG;
+  DriverDev d{};
+  d.kind = 0;
+  d.offset = s->offset;
+  for (int k = 0; k < 3; k++) {
+    d.normal[k] = s->normal[k];
+    d.vel[k] = s->vel[k];
+    d.vrot[k] = s->vrot[k];
+    d.center_proj[k] = d.offset * d.normal[k];  // Surface::initialize (surface.hpp:138)
+  }
+  const bool vrot0 = s->vrot[0] == 0.0 && s->vrot[1] == 0.0 && s->vrot[2] == 0.0;
+  const bool c0 = s->center[0] == 0.0 && s->center[1] == 0.0 && s->center[2] == 0.0;
+  for (int k = 0; k < 3; k++) d.center[k] = (vrot0 && c0) ? d.offset * d.normal[k] : s->center[k];
+  return add_driver(c, d);
+}
+
+int dem_register_cylinder(dem_ctx* c, const dem_cylinder* cy) {
+  if (!c || !cy) return DEM_ERR_INVALID_ARG;
+  if (!(cy->radius > 0)) return c->fail(DEM_ERR_INVALID_ARG, "cylinder radius must be > 0");
+  DriverDev d{};
+  d.kind = 1;
+  d.radius = cy->radius;
+  for (int k = 0; k < 3; k++) {
+    d.axis[k] = cy->axis[k];
+    d.center[k] = cy->axis[k] * cy->center[k];  // Cylinder::initialize (cylinder.hpp:89-99)
+    d.vel[k] = cy->vel[k];
+    d.vrot[k] = cy->vrot[k];
+  }
+  return add_driver(c, d);
+}
+
+int dem_particle_displ_over(dem_ctx* c, int* result) {
+  if (!c || !result) return DEM_ERR_INVALID_ARG;
+  int rc = launch_displ_over(c);
+  if (rc) return rc;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->h_scalars, c->d_scalars, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                  c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  *result = c->h_scalars[0] ? 1 : 0;
+  return DEM_OK;
+}
+
+int dem_update_particle_neighbors(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  return update_neighbors(c);
+}
+
+int dem_reset_force_moment(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  return launch_reset_force_moment(c);
+}
+
+int dem_gravity_force(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  return launch_gravity(c);
+}
+
+int dem_contact_sphere(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  int rc = need_list(c);
+  if (rc) return rc;
+  if ((rc = launch_contact_sphere(c))) return rc;
+  return launch_gather_forces(c);
+}
+
+int dem_force_to_accel(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  return launch_force_to_accel(c);
+}
+
+int dem_combined_compute_prolog(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  return launch_prolog(c);
+}
+
+int dem_combined_compute_epilog(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  return launch_epilog(c);
+}
+
+int dem_simulation_state(dem_ctx* c, dem_state* out) {
+  if (!c || !out) return DEM_ERR_INVALID_ARG;
+  return launch_state(c, out);
+}
+
+int dem_first_iteration(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  int rc;
+  if ((rc = update_neighbors(c))) return rc;
+  if ((rc = launch_reset_force_moment(c))) return rc;
+  return compute_force(c);
+}
+
+int dem_step(dem_ctx* c, int nsteps) {
+  if (!c || nsteps < 0) return DEM_ERR_INVALID_ARG;
+  int rc = need_list(c);
+  if (rc) return rc;
+  for (int s = 0; s < nsteps; s++) {
+    if ((rc = launch_prolog(c))) return rc;
+    int over = 0;
+    if ((rc = dem_particle_displ_over(c, &over))) return rc;
+    if (over && (rc = update_neighbors(c))) return rc;
+    if ((rc = launch_reset_force_moment(c))) return rc;
+    if ((rc = compute_force(c))) return rc;
+    if ((rc = launch_force_to_accel(c))) return rc;
+    if ((rc = launch_epilog(c))) return rc;
+  }
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return DEM_OK;
+}
+
+int dem_rebuild_count(dem_ctx* c, uint64_t* out) {
+  if (!c || !out) return DEM_ERR_INVALID_ARG;
+  *out = c->rebuilds;
+  return DEM_OK;
+}
+
+int dem_interaction_count(dem_ctx* c, uint64_t* out) {
+  if (!c || !out) return DEM_ERR_INVALID_ARG;
+  *out = c->ni;
+  return DEM_OK;
+}
+
+int dem_get_interactions(dem_ctx* c, dem_interaction_list* l) {
+  if (!c || !l) return DEM_ERR_INVALID_ARG;
+  l->count = c->ni;
+  if (l->capacity < c->ni) return c->fail(DEM_ERR_INVALID_ARG, "interaction list capacity too small");
+  const uint64_t ni = c->ni, n = c->n;
+  std::vector<uint32_t> owner(ni), meta(ni);
+  std::vector<uint64_t> pid(ni), id(n);
+  std::vector<double> h[6];
+  const IArrays& I = c->I[c->icur];
+  for (int k = 0; k < 6; k++) h[k].resize(ni);
+  if (ni) {
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(owner.data(), I.owner, ni * 4, cudaMemcpyDeviceToHost, c->stream));
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(meta.data(), I.meta, ni * 4, cudaMemcpyDeviceToHost, c->stream));
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(pid.data(), I.pid, ni * 8, cudaMemcpyDeviceToHost, c->stream));
+    for (int d = 0; d < 3; d++) {
+      DEM_CUDA_TRY(c, cudaMemcpyAsync(h[d].data(), I.ft[d], ni * 8, cudaMemcpyDeviceToHost, c->stream));
+      DEM_CUDA_TRY(c, cudaMemcpyAsync(h[3 + d].data(), I.mo[d], ni * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+  }
+  if (n) DEM_CUDA_TRY(c, cudaMemcpyAsync(id.data(), c->P[c->pcur].id, n * 8, cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  // owners' segments are contiguous and key-sorted inside; order the segments by owner id
+  std::vector<uint64_t> seg_start;
+  for (uint64_t k = 0; k < ni; k++)
+    if (k == 0 || owner[k] != owner[k - 1]) seg_start.push_back(k);
+  std::vector<size_t> order(seg_start.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::sort(order.begin(), order.end(),
+            [&](size_t a, size_t b) { return id[owner[seg_start[a]]] < id[owner[seg_start[b]]]; });
+  uint64_t w = 0;
+  for (size_t o : order) {
+    const uint64_t b = seg_start[o], e = (o + 1 < seg_start.size()) ? seg_start[o + 1] : ni;
+    for (uint64_t k = b; k < e; k++, w++) {
+      if (l->owner_id) l->owner_id[w] = id[owner[k]];
+      if (l->partner_id) l->partner_id[w] = pid[k];
+      if (l->type) l->type[w] = (uint16_t)meta_type(meta[k]);
+      if (l->swap) l->swap[w] = 0;
+      if (l->owner_sub) l->owner_sub[w] = 0;
+      if (l->partner_sub) l->partner_sub[w] = 0;
+      if (l->friction)
+        for (int d = 0; d < 3; d++) l->friction[3 * w + d] = h[d][k];
+      if (l->moment)
+        for (int d = 0; d < 3; d++) l->moment[3 * w + d] = h[3 + d][k];
+    }
+  }
+  return DEM_OK;
+}
+
+int dem_profile(dem_ctx* c, int enable) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  c->prof_on = enable != 0;
+  return DEM_OK;
+}
+
+int dem_kernel_stats(dem_ctx* c, dem_kernel_stat* out, int capacity, int* count) {
+  if (!c || !count) return DEM_ERR_INVALID_ARG;
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->fold_events();
+  int m = 0;
+  for (int k = 0; k < K_NCLASS; k++) {
+    if (out && m < capacity) {
+      std::memset(out[m].name, 0, sizeof(out[m].name));
+      std::strncpy(out[m].name, kDemKClassNames[k], sizeof(out[m].name) - 1);
+      out[m].launches = c->launches[k];
+      out[m].timed = c->prof_n[k];
+      out[m].total_ms = c->prof_ms[k];
+    }
+    m++;
+  }
+  *count = m;
+  return DEM_OK;
+}
+
+int dem_reset_kernel_stats(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->fold_events();
+  for (int k = 0; k < K_NCLASS; k++) {
+    c->launches[k] = 0;
+    c->prof_ms[k] = 0;
+    c->prof_n[k] = 0;
+  }
+  return DEM_OK;
+}
+
+int dem_packing_profile(dem_ctx* c, int nslabs, double zlo, double zhi, double* out) {
+  if (!c || !out || nslabs <= 0 || !(zhi > zlo)) return DEM_ERR_INVALID_ARG;
+  return launch_profile(c, nslabs, zlo, zhi, out);
+}
+
+}  // extern "C"

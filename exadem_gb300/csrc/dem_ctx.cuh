@@ -1,0 +1,160 @@
+// dem_ctx.cuh -- the library context (one simulated system) and the kernel
+// launchers shared by the translation units of the GB300 DEM hot path.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "dem_internal.cuh"
+
+// Kernel classes for the built-in profiler (dem_profile / dem_kernel_stats).
+enum DemKClass : int {
+  K_PROLOG, K_DISPL, K_BIN, K_REORDER, K_BROAD_COUNT, K_BROAD_FILL, K_REVERSE, K_SCAN,
+  K_CONTACT, K_GATHER, K_RESET, K_GRAVITY, K_F2A, K_EPILOG, K_STATE, K_NCLASS
+};
+static const char* const kDemKClassNames[K_NCLASS] = {
+    "prolog", "displ_over", "bin_cells", "reorder", "broad_count", "broad_fill", "reverse_lists", "scan",
+    "contact", "gather", "reset", "gravity", "force_to_accel", "epilog", "state"};
+
+struct dem_ctx {
+  dem_params prm{};
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int num_sms = 152;
+  std::string last_err;
+
+  // particles (double-buffered for the cell reorder)
+  uint64_t n = 0, pcap = 0;
+  dem::PArrays P[2]{};
+  void* pblock[2] = {nullptr, nullptr};
+  int pcur = 0;
+  double rad_max = 0.0;
+
+  // drivers
+  int ndrv = 0;
+  dem::DriverDev drv_host[DEM_MAX_DRIVERS]{};
+  dem::DriverDev* drv_dev = nullptr;
+
+  // cell grid
+  dem::GridDev grid{};
+  uint64_t ncell = 0, ccap = 0;
+  uint32_t* cell_cnt = nullptr;    // ncell+1 (counts, then cursor)
+  uint32_t* cell_start = nullptr;  // ncell+1
+  uint32_t* cell_of = nullptr;     // n, cell of each particle (new order after reorder)
+  uint32_t* cell_tmp = nullptr;    // n, cell of each particle in the old order
+  uint32_t* perm = nullptr;        // n, new slot -> old slot
+  uint32_t* pcnt = nullptr;        // n+1 candidate counts (then offsets)
+
+  // interactions (double-buffered for the history carry-over)
+  uint64_t ni = 0;
+  uint64_t icap[2] = {0, 0};
+  dem::IArrays I[2]{};
+  uint32_t* own_off[2] = {nullptr, nullptr};  // n+1 each
+  int icur = 0;
+  bool have_list = false;   // list valid for the current particle state
+  bool hist_valid = false;  // I[icur]/own_off[icur] usable as history for the next build
+  uint64_t rcap = 0;
+  dem::Records R{};
+  uint32_t* rev_off = nullptr;  // n+1
+  uint32_t* rev_cnt = nullptr;  // n+1
+  uint32_t* rev_idx = nullptr;  // rcap
+
+  // scan scratch
+  uint32_t* scan_blk = nullptr;
+  uint64_t scan_cap = 0;
+
+  // small device scalars: [0] displacement flag, [1] active contacts, [2] overflow
+  unsigned long long* d_scalars = nullptr;
+  unsigned long long* h_scalars = nullptr;  // pinned
+  double* d_red = nullptr;                  // reduction scratch
+  uint64_t red_cap = 0;
+
+  uint64_t rebuilds = 0;
+  uint64_t n_active = 0;
+
+  // built-in profiler: launches always counted; CUDA-event times when enabled
+  bool prof_on = false;
+  uint64_t launches[K_NCLASS] = {};
+  double prof_ms[K_NCLASS] = {};
+  uint64_t prof_n[K_NCLASS] = {};
+  struct PendingEv {
+    int k;
+    cudaEvent_t a, b;
+  };
+  std::vector<PendingEv> pending;
+  std::vector<cudaEvent_t> ev_pool;
+  cudaEvent_t get_event() {
+    if (!ev_pool.empty()) {
+      cudaEvent_t e = ev_pool.back();
+      ev_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  void fold_events() {
+    for (auto& p : pending) {
+      float ms = 0.f;
+      if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+        prof_ms[p.k] += ms;
+        prof_n[p.k]++;
+      }
+      ev_pool.push_back(p.a);
+      ev_pool.push_back(p.b);
+    }
+    pending.clear();
+  }
+
+  int fail(int code, const std::string& msg) {
+    last_err = msg;
+    return code;
+  }
+};
+
+namespace dem {
+// k_scan.cu
+int scan_exclusive_u32(dem_ctx* c, const uint32_t* in, uint32_t* out, uint64_t n);
+// k_grid.cu
+int launch_bin_particles(dem_ctx* c);
+int launch_reorder_particles(dem_ctx* c);
+// k_neigh_sphere.cu
+int launch_count_sphere(dem_ctx* c);
+int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total);
+int launch_reverse_lists(dem_ctx* c);
+// k_contact_sphere.cu
+int launch_contact_sphere(dem_ctx* c);
+int launch_gather_forces(dem_ctx* c);
+// k_particles.cu
+int launch_reset_force_moment(dem_ctx* c);
+int launch_gravity(dem_ctx* c);
+int launch_force_to_accel(dem_ctx* c);
+int launch_prolog(dem_ctx* c);
+int launch_epilog(dem_ctx* c);
+int launch_displ_over(dem_ctx* c);
+int launch_state(dem_ctx* c, dem_state* out);
+int launch_profile(dem_ctx* c, int nslabs, double zlo, double zhi, double* out);
+}  // namespace dem
+
+inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+// RAII scope around the launches of one kernel class on the ctx stream.
+struct ProfScope {
+  dem_ctx* c;
+  int k;
+  cudaEvent_t a = nullptr;
+  ProfScope(dem_ctx* ctx, int kclass, int nlaunch = 1) : c(ctx), k(kclass) {
+    c->launches[k] += (uint64_t)nlaunch;
+    if (c->prof_on) {
+      a = c->get_event();
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~ProfScope() {
+    if (a) {
+      cudaEvent_t b = c->get_event();
+      cudaEventRecord(b, c->stream);
+      c->pending.push_back({k, a, b});
+      if (c->pending.size() > 4096) c->fold_events();
+    }
+  }
+};

@@ -1,0 +1,122 @@
+// dem_internal.cuh -- device data layout and shared helpers of the GB300 DEM hot path.
+//
+// Layout in HBM (all structure-of-arrays):
+//   particles: 31 FP64 fields + id (u64) + type/group (u32), double-buffered so
+//              the cell reorder at a rebuild is a gather from one copy into the other;
+//   interactions: sorted by owner slot, and by InteractionPair key inside one
+//              owner; keys (partner slot, partner id, meta), history (6 FP64)
+//              and the per-step force record (9 FP64) in separate arrays;
+//   cells: counts/starts of the cell grid used by the broad phase.
+// All FP64 arithmetic that decides a result keeps the operation order of the
+// reference and is compiled with --fmad=false, so the results are bit-identical
+// to the CPU restatement of the reference.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/dem_hotpath.h"
+
+namespace dem {
+
+// ---------------------------------------------------------------- fields
+enum PField : int {
+  RX, RY, RZ, VX, VY, VZ, FX, FY, FZ,
+  WX, WY, WZ,   // vrot
+  AX, AY, AZ,   // arot
+  MX, MY, MZ,   // mom
+  QW, QX, QY, QZ,
+  IX, IY, IZ,   // inertia
+  MASS, RAD, HOM,
+  BX, BY, BZ,   // backup positions for the displacement trigger
+  NPF
+};
+
+struct PArrays {
+  double* f[NPF];
+  uint64_t* id;
+  uint32_t* type;
+  uint32_t* group;
+};
+
+// interaction meta word: bits 0..7 type, bits 8..13 periodic image shift of
+// the partner (2 bits per axis: 0 none, 1 = +L, 2 = -L), bit 14 owner-only
+// (partner is a periodic ghost image whose force is discarded).
+__host__ __device__ inline uint32_t meta_type(uint32_t m) { return m & 0xffu; }
+__host__ __device__ inline int meta_shift(uint32_t m, int d) {
+  uint32_t s = (m >> (8 + 2 * d)) & 3u;
+  return s == 1 ? 1 : (s == 2 ? -1 : 0);
+}
+__host__ __device__ inline bool meta_owner_only(uint32_t m) { return (m >> 14) & 1u; }
+__host__ __device__ inline uint32_t make_meta(uint32_t type, int sx, int sy, int sz, bool owner_only) {
+  auto enc = [](int s) -> uint32_t { return s == 1 ? 1u : (s == -1 ? 2u : 0u); };
+  return type | (enc(sx) << 8) | (enc(sy) << 10) | (enc(sz) << 12) | ((owner_only ? 1u : 0u) << 14);
+}
+
+struct IArrays {
+  uint32_t* owner;    // owner particle slot
+  uint32_t* partner;  // partner particle slot, or driver index
+  uint64_t* pid;      // partner id (particle id, or driver index) -- key
+  uint32_t* meta;
+  double* ft[3];      // history: attr::friction
+  double* mo[3];      // history: attr::moment
+};
+
+struct Records {  // per-interaction force record of the last force pass
+  double* f[3];
+  double* ti[3];
+  double* tj[3];
+};
+
+// drivers in device-friendly form (stationary; vrot enters the relative velocity)
+struct DriverDev {
+  int kind;  // 0 surface, 1 cylinder
+  double offset, radius;
+  double normal[3], center[3], center_proj[3], axis[3], vel[3], vrot[3];
+};
+#define DEM_MAX_DRIVERS 16
+
+struct GridDev {
+  int dims[3];
+  double lo[3];
+  double hi[3];
+  double csz[3];
+  int periodic[3];
+  double L[3];
+};
+
+// ------------------------------------------------------------- vector math
+struct V3 {
+  double x, y, z;
+};
+__host__ __device__ inline V3 mk(double x, double y, double z) { return V3{x, y, z}; }
+__host__ __device__ inline V3 operator+(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__host__ __device__ inline V3 operator-(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__host__ __device__ inline V3 operator-(V3 a) { return V3{-a.x, -a.y, -a.z}; }
+__host__ __device__ inline V3 operator*(V3 a, double s) { return V3{a.x * s, a.y * s, a.z * s}; }
+__host__ __device__ inline V3 operator*(double s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
+__host__ __device__ inline V3 operator*(V3 a, V3 b) { return V3{a.x * b.x, a.y * b.y, a.z * b.z}; }
+__host__ __device__ inline V3 operator/(V3 a, double s) { return V3{a.x / s, a.y / s, a.z / s}; }
+__host__ __device__ inline double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ inline V3 cross(V3 a, V3 b) {
+  return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__host__ __device__ inline double vnorm(V3 a) { return sqrt(dot(a, a)); }
+
+// ----------------------------------------------------------------- errors
+struct Status {
+  int code = DEM_OK;
+  std::string msg;
+};
+
+}  // namespace dem
+
+#define DEM_CUDA_TRY(ctx, call)                                                            \
+  do {                                                                                     \
+    cudaError_t _e = (call);                                                               \
+    if (_e != cudaSuccess) {                                                               \
+      return (ctx)->fail(_e == cudaErrorMemoryAllocation ? DEM_ERR_OOM : DEM_ERR_CUDA,     \
+                         std::string(#call) + ": " + cudaGetErrorString(_e));              \
+    }                                                                                      \
+  } while (0)

@@ -1,0 +1,129 @@
+// k_grid.cu -- cell binning and particle reorder at a neighbour rebuild.
+//
+// Stands in for exaNBody's move_particles / migrate_cell_particles / grid
+// (periodic wrap into the domain, particles stored cell by cell).  Steps:
+//   k_bin:       periodic wrap, cell index, cell histogram (atomics on counts)
+//   scan:        cell starts
+//   k_scatter:   slot of each particle inside its cell (atomic cursor)
+//   k_cell_sort: order inside one cell by particle id, so the layout is
+//                deterministic whatever order the atomics ran in
+//   k_reorder:   gather every field into the other particle buffer
+// All of it is integer / copy work: HBM-bound, one read and one write per field.
+#include "dem_ctx.cuh"
+
+namespace dem {
+namespace {
+
+__global__ void k_bin(PArrays P, uint64_t n, GridDev g, uint32_t* __restrict__ cell_tmp,
+                      uint32_t* __restrict__ cell_cnt) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  int k[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    double x = P.f[RX + d][s];
+    if (g.periodic[d]) {
+      const double lo = g.lo[d], hi = g.hi[d], Ld = g.L[d];
+      if (x < lo) {
+        x = x + Ld;
+        if (x >= hi) x = lo;
+      } else if (x >= hi) {
+        x = x - Ld;
+        if (x < lo) x = lo;
+      }
+      P.f[RX + d][s] = x;
+    }
+    double q = floor((x - g.lo[d]) / g.csz[d]);
+    long kk = (q < 0.0) ? 0 : (q >= (double)g.dims[d] ? g.dims[d] - 1 : (long)q);
+    if (kk < 0) kk = 0;
+    if (kk >= g.dims[d]) kk = g.dims[d] - 1;
+    k[d] = (int)kk;
+  }
+  const uint32_t c = (uint32_t)k[0] + (uint32_t)g.dims[0] * ((uint32_t)k[1] + (uint32_t)g.dims[1] * (uint32_t)k[2]);
+  cell_tmp[s] = c;
+  atomicAdd(&cell_cnt[c], 1u);
+}
+
+__global__ void k_scatter(const uint32_t* __restrict__ cell_tmp, uint64_t n, const uint32_t* __restrict__ cell_start,
+                          uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t c = cell_tmp[s];
+  const uint32_t pos = cell_start[c] + atomicAdd(&cursor[c], 1u);
+  perm[pos] = (uint32_t)s;
+}
+
+__global__ void k_cell_sort(uint64_t ncell, const uint32_t* __restrict__ cell_start, const uint64_t* __restrict__ id,
+                            uint32_t* __restrict__ perm) {
+  const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncell) return;
+  const uint32_t b = cell_start[c], e = cell_start[c + 1];
+  for (uint32_t a = b + 1; a < e; a++) {
+    const uint32_t v = perm[a];
+    const uint64_t key = id[v];
+    uint32_t q = a;
+    while (q > b && id[perm[q - 1]] > key) {
+      perm[q] = perm[q - 1];
+      q--;
+    }
+    perm[q] = v;
+  }
+}
+
+__global__ void k_reorder(PArrays src, PArrays dst, uint64_t n, const uint32_t* __restrict__ perm,
+                          const uint32_t* __restrict__ cell_tmp, uint32_t* __restrict__ cell_of) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const uint32_t o = perm[t];
+#pragma unroll
+  for (int k = 0; k < BX; k++) dst.f[k][t] = src.f[k][o];
+  // backup_r: positions at this rebuild, for the displacement trigger
+  dst.f[BX][t] = src.f[RX][o];
+  dst.f[BY][t] = src.f[RY][o];
+  dst.f[BZ][t] = src.f[RZ][o];
+  dst.id[t] = src.id[o];
+  dst.type[t] = src.type[o];
+  dst.group[t] = src.group[o];
+  cell_of[t] = cell_tmp[o];
+}
+
+__global__ void k_zero_u32(uint32_t* p, uint64_t n) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0u;
+}
+}  // namespace
+
+// Sets up the grid, wraps, bins, scans and scatters; leaves perm = new slot -> old slot.
+int launch_bin_particles(dem_ctx* c) {
+  const uint64_t n = c->n;
+  const uint64_t nc = c->ncell;
+  cudaStream_t st = c->stream;
+  int rc;
+  {
+  ProfScope ps(c, K_BIN, n ? 2 : 1);
+  k_zero_u32<<<grid_for(nc + 1, 256), 256, 0, st>>>(c->cell_cnt, nc + 1);
+  if (n) k_bin<<<grid_for(n, 256), 256, 0, st>>>(c->P[c->pcur], n, c->grid, c->cell_tmp, c->cell_cnt);
+  }
+  rc = scan_exclusive_u32(c, c->cell_cnt, c->cell_start, nc);
+  if (rc) return rc;
+  ProfScope ps(c, K_BIN, n ? 3 : 2);
+  k_zero_u32<<<grid_for(nc + 1, 256), 256, 0, st>>>(c->cell_cnt, nc + 1);
+  if (n) k_scatter<<<grid_for(n, 256), 256, 0, st>>>(c->cell_tmp, n, c->cell_start, c->cell_cnt, c->perm);
+  k_cell_sort<<<grid_for(nc, 256), 256, 0, st>>>(nc, c->cell_start, c->P[c->pcur].id, c->perm);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+// Gathers all particle fields into the other buffer in cell order and swaps.
+int launch_reorder_particles(dem_ctx* c) {
+  const uint64_t n = c->n;
+  ProfScope ps(c, K_REORDER, n ? 1 : 0);
+  if (n) {
+    k_reorder<<<grid_for(n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->P[1 - c->pcur], n, c->perm, c->cell_tmp,
+                                                        c->cell_of);
+  }
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  c->pcur = 1 - c->pcur;
+  return DEM_OK;
+}
+}  // namespace dem

@@ -1,0 +1,297 @@
+// k_neigh_sphere.cu -- sphere interaction-list rebuild (exact two-pass count / fill).
+//
+// Replaces chunk_neighbors_contact (src/grid/chunk_neighbors_contact.cpp:45-57),
+// nbh_sphere in symetric mode (src/sphere/nbh_sphere.cu:64-309) and
+// classify_interactions (src/interaction/classify_interactions.cpp:52-136):
+//   - drivers first: Surface / Cylinder filters with r + rcut_inc
+//     (nbh_sphere.cu:140-233, surface.hpp:320-324, cylinder.hpp:225-235);
+//   - particle pairs over the 27-cell stencil with the FP64 filter
+//     d2 > 0 && d2 < (r_a + r_b + rcut_inc)^2 && d2 < nbh_dist^2;
+//     a pair is owned by the smaller id, except when the partner is a periodic
+//     ghost image, which is kept from both sides (nbh_sphere.cu:244-249);
+//   - each owner's list sorted by InteractionPair order, history (friction,
+//     moment) carried over from the previous list by key equality
+//     (interaction_manager.hpp:89-112, placeholder_interaction.hpp:398-408).
+// One thread per owner particle; particles are in cell order so the stencil
+// reads of neighbouring threads hit the same cells (L1/L2 reuse).
+#include "dem_ctx.cuh"
+
+namespace dem {
+namespace {
+
+struct BPArgs {
+  PArrays P;
+  uint64_t n;
+  GridDev g;
+  const uint32_t* cell_start;
+  const uint32_t* cell_of;
+  const DriverDev* drv;
+  int ndrv;
+  double skin;
+  double rcut2;
+};
+
+__device__ inline bool driver_filter(const DriverDev& d, double rcut, V3 p) {
+  if (d.kind == 0) {
+    const V3 nrm = mk(d.normal[0], d.normal[1], d.normal[2]);
+    const V3 proj = dot(p, nrm) * nrm;
+    const double dd = vnorm(proj - mk(d.center_proj[0], d.center_proj[1], d.center_proj[2]));
+    return dd <= rcut;
+  }
+  const V3 proj = p * mk(d.axis[0], d.axis[1], d.axis[2]);
+  const V3 dir = proj - mk(d.center[0], d.center[1], d.center[2]);
+  const double dd = vnorm(dir);
+  const double dn = d.radius - (dd + rcut);
+  return dn <= 0;
+}
+
+template <class Emit>
+__device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& emit) {
+  const double* __restrict__ rx = a.P.f[RX];
+  const double* __restrict__ ry = a.P.f[RY];
+  const double* __restrict__ rz = a.P.f[RZ];
+  const double* __restrict__ rad = a.P.f[RAD];
+  const uint64_t* __restrict__ id = a.P.id;
+  const V3 ri = mk(rx[s], ry[s], rz[s]);
+  const double radi = rad[s];
+  const uint64_t idi = id[s];
+  for (int k = 0; k < a.ndrv; k++) {
+    const DriverDev& d = a.drv[k];
+    if (driver_filter(d, radi + a.skin, ri))
+      emit((uint32_t)k, (uint64_t)k,
+           make_meta(d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER, 0, 0, 0, false));
+  }
+  const uint32_t c = a.cell_of[s];
+  const int d0 = a.g.dims[0], d1 = a.g.dims[1], d2n = a.g.dims[2];
+  const int cx = (int)(c % (uint32_t)d0);
+  const int cy = (int)((c / (uint32_t)d0) % (uint32_t)d1);
+  const int cz = (int)(c / ((uint32_t)d0 * (uint32_t)d1));
+  for (int dz = -1; dz <= 1; dz++) {
+    int z = cz + dz, sz = 0;
+    if (z < 0) {
+      if (!a.g.periodic[2]) continue;
+      z += d2n;
+      sz = -1;
+    } else if (z >= d2n) {
+      if (!a.g.periodic[2]) continue;
+      z -= d2n;
+      sz = 1;
+    }
+    for (int dy = -1; dy <= 1; dy++) {
+      int y = cy + dy, sy = 0;
+      if (y < 0) {
+        if (!a.g.periodic[1]) continue;
+        y += d1;
+        sy = -1;
+      } else if (y >= d1) {
+        if (!a.g.periodic[1]) continue;
+        y -= d1;
+        sy = 1;
+      }
+      for (int dx = -1; dx <= 1; dx++) {
+        int x = cx + dx, sx = 0;
+        if (x < 0) {
+          if (!a.g.periodic[0]) continue;
+          x += d0;
+          sx = -1;
+        } else if (x >= d0) {
+          if (!a.g.periodic[0]) continue;
+          x -= d0;
+          sx = 1;
+        }
+        const uint32_t cc = (uint32_t)x + (uint32_t)d0 * ((uint32_t)y + (uint32_t)d1 * (uint32_t)z);
+        const uint32_t qb = a.cell_start[cc], qe = a.cell_start[cc + 1];
+        const bool ghost = (sx | sy | sz) != 0;
+        for (uint32_t q = qb; q < qe; q++) {
+          V3 rj = mk(rx[q], ry[q], rz[q]);
+          if (sx) rj.x = rj.x + (double)sx * a.g.L[0];
+          if (sy) rj.y = rj.y + (double)sy * a.g.L[1];
+          if (sz) rj.z = rj.z + (double)sz * a.g.L[2];
+          const double ddx = rj.x - ri.x, ddy = rj.y - ri.y, ddz = rj.z - ri.z;
+          const double d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+          const double rmax = radi + rad[q] + a.skin;
+          if (!(d2 > 0.0 && d2 < rmax * rmax && d2 < a.rcut2)) continue;
+          const uint64_t idj = id[q];
+          if (!ghost && idi >= idj) continue;
+          emit(q, idj, make_meta(DEM_ITYPE_VERTEX_VERTEX, sx, sy, sz, ghost));
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  uint32_t m = 0;
+  for_each_candidate(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t) { m++; });
+  cnt[s] = m;
+}
+
+__device__ inline bool key_less(uint64_t pa, uint32_t ta, uint64_t pb, uint32_t tb) {
+  return pa < pb || (pa == pb && ta < tb);
+}
+
+__global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, IArrays old,
+                       const uint32_t* __restrict__ old_off, const uint32_t* __restrict__ perm, int have_old) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  const uint32_t b = off[s], e = off[s + 1];
+  uint32_t w = b;
+  for_each_candidate(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta) {
+    if (w < e) {
+      dst.partner[w] = q;
+      dst.pid[w] = pid;
+      dst.meta[w] = meta;
+    }
+    w++;
+  });
+  // InteractionPair order inside the owner: (partner id, type); swap and subs are 0 for spheres
+  for (uint32_t x = b + 1; x < e; x++) {
+    const uint64_t pk = dst.pid[x];
+    const uint32_t mk_ = dst.meta[x], qk = dst.partner[x];
+    const uint32_t tk = meta_type(mk_);
+    uint32_t y = x;
+    while (y > b && key_less(pk, tk, dst.pid[y - 1], meta_type(dst.meta[y - 1]))) {
+      dst.pid[y] = dst.pid[y - 1];
+      dst.meta[y] = dst.meta[y - 1];
+      dst.partner[y] = dst.partner[y - 1];
+      y--;
+    }
+    dst.pid[y] = pk;
+    dst.meta[y] = mk_;
+    dst.partner[y] = qk;
+  }
+  // history carry-over: binary search in the previous list of the same particle
+  uint32_t ob = 0, oe = 0;
+  if (have_old) {
+    const uint32_t os = perm[s];
+    ob = old_off[os];
+    oe = old_off[os + 1];
+  }
+  for (uint32_t x = b; x < e; x++) {
+    dst.owner[x] = (uint32_t)s;
+    double h[6] = {0, 0, 0, 0, 0, 0};
+    const uint64_t pk = dst.pid[x];
+    const uint32_t tk = meta_type(dst.meta[x]);
+    uint32_t lo = ob, hi = oe;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (key_less(old.pid[mid], meta_type(old.meta[mid]), pk, tk))
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    if (lo < oe && old.pid[lo] == pk && meta_type(old.meta[lo]) == tk) {
+      h[0] = old.ft[0][lo];
+      h[1] = old.ft[1][lo];
+      h[2] = old.ft[2][lo];
+      h[3] = old.mo[0][lo];
+      h[4] = old.mo[1][lo];
+      h[5] = old.mo[2][lo];
+    }
+    dst.ft[0][x] = h[0];
+    dst.ft[1][x] = h[1];
+    dst.ft[2][x] = h[2];
+    dst.mo[0][x] = h[3];
+    dst.mo[1][x] = h[4];
+    dst.mo[2][x] = h[5];
+  }
+}
+
+__global__ void k_zero_u32(uint32_t* p, uint64_t n) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0u;
+}
+
+// partner-side lists: interactions whose partner is a real particle that receives -f
+__global__ void k_rev_count(IArrays I, uint64_t ni, uint32_t* __restrict__ cnt) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ni) return;
+  const uint32_t m = I.meta[k];
+  if (meta_type(m) == DEM_ITYPE_VERTEX_VERTEX && !meta_owner_only(m)) atomicAdd(&cnt[I.partner[k]], 1u);
+}
+__global__ void k_rev_fill(IArrays I, uint64_t ni, const uint32_t* __restrict__ off, uint32_t* __restrict__ cursor,
+                           uint32_t* __restrict__ idx) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ni) return;
+  const uint32_t m = I.meta[k];
+  if (meta_type(m) == DEM_ITYPE_VERTEX_VERTEX && !meta_owner_only(m)) {
+    const uint32_t j = I.partner[k];
+    idx[off[j] + atomicAdd(&cursor[j], 1u)] = (uint32_t)k;
+  }
+}
+// order of the partner-side contributions: InteractionPair order = (owner id, index)
+__global__ void k_rev_sort(uint64_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ owner,
+                           const uint64_t* __restrict__ id, uint32_t* __restrict__ idx) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t b = off[s], e = off[s + 1];
+  for (uint32_t x = b + 1; x < e; x++) {
+    const uint32_t k = idx[x];
+    const uint64_t ok = id[owner[k]];
+    uint32_t y = x;
+    while (y > b) {
+      const uint32_t kp = idx[y - 1];
+      const uint64_t op = id[owner[kp]];
+      if (op < ok || (op == ok && kp < k)) break;
+      idx[y] = kp;
+      y--;
+    }
+    idx[y] = k;
+  }
+}
+
+BPArgs make_args(dem_ctx* c) {
+  BPArgs a;
+  a.P = c->P[c->pcur];
+  a.n = c->n;
+  a.g = c->grid;
+  a.cell_start = c->cell_start;
+  a.cell_of = c->cell_of;
+  a.drv = c->drv_dev;
+  a.ndrv = c->ndrv;
+  a.skin = c->prm.rcut_inc;
+  const double nd = 2 * c->rad_max + c->prm.rcut_inc;
+  a.rcut2 = nd * nd;
+  return a;
+}
+}  // namespace
+
+int launch_count_sphere(dem_ctx* c) {
+  ProfScope ps(c, K_BROAD_COUNT, c->n ? 1 : 0);
+  if (c->n) k_count<<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total) {
+  (void)total;
+  const int nw = 1 - c->icur;
+  ProfScope ps(c, K_BROAD_FILL, c->n ? 1 : 0);
+  if (c->n)
+    k_fill<<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw], c->I[c->icur],
+                                                       c->own_off[c->icur], c->perm, c->hist_valid ? 1 : 0);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+int launch_reverse_lists(dem_ctx* c) {
+  const uint64_t n = c->n, ni = c->ni;
+  cudaStream_t st = c->stream;
+  const IArrays& I = c->I[c->icur];
+  {
+  ProfScope ps(c, K_REVERSE, ni ? 2 : 1);
+  k_zero_u32<<<grid_for(n + 1, 256), 256, 0, st>>>(c->rev_cnt, n + 1);
+  if (ni) k_rev_count<<<grid_for(ni, 256), 256, 0, st>>>(I, ni, c->rev_cnt);
+  }
+  int rc = scan_exclusive_u32(c, c->rev_cnt, c->rev_off, n);
+  if (rc) return rc;
+  ProfScope ps(c, K_REVERSE, 1 + (ni ? 1 : 0) + (n ? 1 : 0));
+  k_zero_u32<<<grid_for(n + 1, 256), 256, 0, st>>>(c->rev_cnt, n + 1);
+  if (ni) k_rev_fill<<<grid_for(ni, 256), 256, 0, st>>>(I, ni, c->rev_off, c->rev_cnt, c->rev_idx);
+  if (n) k_rev_sort<<<grid_for(n, 256), 256, 0, st>>>(n, c->rev_off, I.owner, c->P[c->pcur].id, c->rev_idx);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+}  // namespace dem

@@ -1,0 +1,259 @@
+// k_particles.cu -- per-particle operators of the Verlet scheme and the state reductions.
+//
+//   reset_force_moment   src/numericalscheme/reset_force_moment.cu:69-70
+//   gravity_force        src/forcefield/include/exaDEM/forcefield/gravity_force.hpp:38-46
+//   force_to_accel       src/numericalscheme/include/exaDEM/force_to_accel.hpp:26-33
+//   prolog               src/numericalscheme/combined_compute_prolog.cu:94-116,
+//                        push_to_quaternion.hpp:26-38 (x, v/2, q, w/2)
+//   epilog               src/numericalscheme/combined_compute_epilog.cu:94-113,
+//                        angular_acceleration.hpp:27-43, angular_velocity.hpp:27-33
+//   particle_displ_over  exaNBody: any |r - r_backup|^2 >= max_displ^2, max_displ = rcut_inc/2
+//   simulation_state     src/io/include/exaDEM/simulation_state.hpp:48-56 (deterministic tree sum)
+// Quaternion arithmetic restates onika's Quaternion operators following exaDEM's
+// quat type (src/shape/include/exaDEM/type/quat.hpp:79-96,233-242).
+#include "dem_ctx.cuh"
+
+namespace dem {
+namespace {
+
+struct Q4 {
+  double w, x, y, z;
+};
+__device__ inline V3 qrotate(Q4 q, V3 v) {
+  const V3 qv = mk(q.x, q.y, q.z);
+  V3 uv = cross(qv, v);
+  V3 uuv = cross(qv, uv);
+  uv = uv * (2.0 * q.w);
+  uuv = uuv * 2.0;
+  return v + uv + uuv;
+}
+
+__global__ void k_reset(PArrays P, uint64_t n) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  P.f[FX][s] = 0.0;
+  P.f[FY][s] = 0.0;
+  P.f[FZ][s] = 0.0;
+  P.f[MX][s] = 0.0;
+  P.f[MY][s] = 0.0;
+  P.f[MZ][s] = 0.0;
+}
+
+__global__ void k_gravity(PArrays P, uint64_t n, double gx, double gy, double gz) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double m = P.f[MASS][s];
+  P.f[FX][s] = P.f[FX][s] + gx * m;
+  P.f[FY][s] = P.f[FY][s] + gy * m;
+  P.f[FZ][s] = P.f[FZ][s] + gz * m;
+}
+
+__global__ void k_force_to_accel(PArrays P, uint64_t n) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double m = P.f[MASS][s];
+  P.f[FX][s] = P.f[FX][s] / m;
+  P.f[FY][s] = P.f[FY][s] / m;
+  P.f[FZ][s] = P.f[FZ][s] / m;
+}
+
+__global__ void k_prolog(PArrays P, uint64_t n, double delta_t, double half_delta_t, double delta_t2_2) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const double v = P.f[VX + d][s], a = P.f[FX + d][s];
+    P.f[RX + d][s] = P.f[RX + d][s] + (v * delta_t + a * delta_t2_2);
+    P.f[VX + d][s] = v + a * half_delta_t;
+  }
+  Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+  const V3 om = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+  Q4 d;
+  d.x = 0.5 * (om.y * Q.z - om.z * Q.y + om.x * Q.w);
+  d.y = 0.5 * (om.z * Q.x - om.x * Q.z + om.y * Q.w);
+  d.z = 0.5 * (om.x * Q.y - om.y * Q.x + om.z * Q.w);
+  d.w = -0.5 * (om.x * Q.x + om.y * Q.y + om.z * Q.z);
+  Q.w = Q.w + d.w * delta_t;
+  Q.x = Q.x + d.x * delta_t;
+  Q.y = Q.y + d.y * delta_t;
+  Q.z = Q.z + d.z * delta_t;
+  const double norm2 = Q.w * Q.w + (Q.x * Q.x + Q.y * Q.y + Q.z * Q.z);
+  if (norm2 <= 1e-9) {
+    Q = {1.0, 0.0, 0.0, 0.0};
+  } else {
+    const double inv = 1.0 / sqrt(norm2);
+    Q = {Q.w * inv, Q.x * inv, Q.y * inv, Q.z * inv};
+  }
+  P.f[QW][s] = Q.w;
+  P.f[QX][s] = Q.x;
+  P.f[QY][s] = Q.y;
+  P.f[QZ][s] = Q.z;
+  P.f[WX][s] = om.x + half_delta_t * P.f[AX][s];
+  P.f[WY][s] = om.y + half_delta_t * P.f[AY][s];
+  P.f[WZ][s] = om.z + half_delta_t * P.f[AZ][s];
+}
+
+__global__ void k_epilog(PArrays P, uint64_t n, double half_delta_t) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+  const Q4 Qinv = {Q.w, -Q.x, -Q.y, -Q.z};
+  const V3 vrot = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+  const V3 mom = mk(P.f[MX][s], P.f[MY][s], P.f[MZ][s]);
+  const V3 I = mk(P.f[IX][s], P.f[IY][s], P.f[IZ][s]);
+  const V3 omega = qrotate(Qinv, vrot);
+  const V3 M = qrotate(Qinv, mom);
+  const V3 domega = mk((M.x - (I.z - I.y) * omega.y * omega.z) / I.x, (M.y - (I.x - I.z) * omega.z * omega.x) / I.y,
+                       (M.z - (I.y - I.x) * omega.x * omega.y) / I.z);
+  const V3 arot = qrotate(Q, domega);
+  P.f[AX][s] = arot.x;
+  P.f[AY][s] = arot.y;
+  P.f[AZ][s] = arot.z;
+  P.f[WX][s] = vrot.x + arot.x * half_delta_t;
+  P.f[WY][s] = vrot.y + arot.y * half_delta_t;
+  P.f[WZ][s] = vrot.z + arot.z * half_delta_t;
+#pragma unroll
+  for (int d = 0; d < 3; d++) P.f[VX + d][s] = P.f[VX + d][s] + P.f[FX + d][s] * half_delta_t;
+}
+
+__global__ void k_displ(PArrays P, uint64_t n, double thr2, unsigned long long* flag) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (s < n) {
+    const double dx = P.f[RX][s] - P.f[BX][s], dy = P.f[RY][s] - P.f[BY][s], dz = P.f[RZ][s] - P.f[BZ][s];
+    over = dx * dx + dy * dy + dz * dz >= thr2;
+  }
+  if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+}
+
+// Deterministic two-level reduction: fixed block partition, fixed tree order.
+constexpr int RED_THREADS = 256;
+__global__ void k_state_partial(PArrays P, uint64_t n, double* __restrict__ part) {
+  __shared__ double sh[7][RED_THREADS];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (uint64_t s = (uint64_t)blockIdx.x * RED_THREADS + threadIdx.x; s < n; s += (uint64_t)gridDim.x * RED_THREADS) {
+    const double m = P.f[MASS][s];
+    acc[0] += m;
+    acc[1] += 0.5 * P.f[WX][s] * P.f[WX][s] * m;
+    acc[2] += 0.5 * P.f[WY][s] * P.f[WY][s] * m;
+    acc[3] += 0.5 * P.f[WZ][s] * P.f[WZ][s] * m;
+    acc[4] += 0.5 * P.f[VX][s] * P.f[VX][s] * m;
+    acc[5] += 0.5 * P.f[VY][s] * P.f[VY][s] * m;
+    acc[6] += 0.5 * P.f[VZ][s] * P.f[VZ][s] * m;
+  }
+#pragma unroll
+  for (int k = 0; k < 7; k++) sh[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int w = RED_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int k = 0; k < 7; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 7) part[blockIdx.x * 7 + threadIdx.x] = sh[threadIdx.x][0];
+}
+__global__ void k_state_final(const double* __restrict__ part, int nb, double* __restrict__ out) {
+  if (threadIdx.x < 7) {
+    double a = 0;
+    for (int b = 0; b < nb; b++) a += part[b * 7 + threadIdx.x];
+    out[threadIdx.x] = a;
+  }
+}
+
+__global__ void k_profile(PArrays P, uint64_t n, int nslabs, double zlo, double dz, double* __restrict__ vol) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double zc = P.f[RZ][s], r = P.f[RAD][s];
+  int a = (int)floor((zc - r - zlo) / dz), b = (int)floor((zc + r - zlo) / dz);
+  if (a < 0) a = 0;
+  if (b > nslabs - 1) b = nslabs - 1;
+  for (int k = a; k <= b; k++) {
+    const double s0 = zlo + k * dz, s1 = zlo + (k + 1) * dz;
+    const double lo = fmax(s0, zc - r), hi = fmin(s1, zc + r);
+    if (hi <= lo) continue;
+    const double ul = lo - zc, uh = hi - zc;
+    const double Fh = r * r * uh - uh * uh * uh / 3.0, Fl = r * r * ul - ul * ul * ul / 3.0;
+    atomicAdd(&vol[k], M_PI * (Fh - Fl));
+  }
+}
+}  // namespace
+
+int launch_reset_force_moment(dem_ctx* c) {
+  ProfScope ps(c, K_RESET, c->n ? 1 : 0);
+  if (c->n) k_reset<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->n);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+int launch_gravity(dem_ctx* c) {
+  ProfScope ps(c, K_GRAVITY, c->n ? 1 : 0);
+  if (c->n)
+    k_gravity<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->n, c->prm.gravity[0], c->prm.gravity[1],
+                                                            c->prm.gravity[2]);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+int launch_force_to_accel(dem_ctx* c) {
+  ProfScope ps(c, K_F2A, c->n ? 1 : 0);
+  if (c->n) k_force_to_accel<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->n);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+int launch_prolog(dem_ctx* c) {
+  const double delta_t = c->prm.dt;
+  const double half_delta_t = delta_t * 0.5;
+  const double delta_t2_2 = delta_t * delta_t * 0.5;
+  ProfScope ps(c, K_PROLOG, c->n ? 1 : 0);
+  if (c->n)
+    k_prolog<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->P[c->pcur], c->n, delta_t, half_delta_t, delta_t2_2);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+int launch_epilog(dem_ctx* c) {
+  const double half_delta_t = c->prm.dt * 0.5;
+  ProfScope ps(c, K_EPILOG, c->n ? 1 : 0);
+  if (c->n) k_epilog<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->P[c->pcur], c->n, half_delta_t);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+int launch_displ_over(dem_ctx* c) {
+  const double max_displ = c->prm.rcut_inc * 0.5;
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars, 0, sizeof(unsigned long long), c->stream));
+  ProfScope ps(c, K_DISPL, c->n ? 1 : 0);
+  if (c->n) k_displ<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->n, max_displ * max_displ, c->d_scalars);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+int launch_state(dem_ctx* c, dem_state* out) {
+  const int nb = 2 * c->num_sms;
+  double* part = c->d_red;
+  double* fin = c->d_red + 7 * nb;
+  ProfScope ps(c, K_STATE, 2);
+  k_state_partial<<<nb, RED_THREADS, 0, c->stream>>>(c->P[c->pcur], c->n, part);
+  k_state_final<<<1, 32, 0, c->stream>>>(part, nb, fin);
+  double h[7];
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(h, fin, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->h_scalars, c->d_scalars, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                  c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  out->mass = h[0];
+  for (int d = 0; d < 3; d++) {
+    out->rotation_energy[d] = h[1 + d];
+    out->kinetic_energy[d] = h[4 + d];
+  }
+  out->n_particles = c->n;
+  out->n_interactions = c->ni;
+  out->n_active_interactions = c->h_scalars[1];
+  return DEM_OK;
+}
+int launch_profile(dem_ctx* c, int nslabs, double zlo, double zhi, double* out) {
+  if ((uint64_t)nslabs > c->red_cap) return c->fail(DEM_ERR_INVALID_ARG, "nslabs too large");
+  const double dz = (zhi - zlo) / nslabs;
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_red, 0, nslabs * sizeof(double), c->stream));
+  if (c->n) k_profile<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->n, nslabs, zlo, dz, c->d_red);
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(out, c->d_red, nslabs * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const double area = c->grid.L[0] * c->grid.L[1];
+  for (int k = 0; k < nslabs; k++) out[k] = out[k] / (area * dz);
+  return DEM_OK;
+}
+}  // namespace dem

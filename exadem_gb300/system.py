@@ -1,0 +1,271 @@
+"""Host-side mirror of exaDEM's operator interface for the per-timestep hot path.
+
+``System`` owns one native context (``dem_ctx``) and exposes one method per
+reference operator, under the reference's operator name:
+
+=============================  ==================================================
+method                          reference operator (exaDEM / exaNBody)
+=============================  ==================================================
+``update_particle_neighbors``   move_particles + chunk_neighbors_contact +
+                                nbh_sphere + classify_interactions + backup_r
+``particle_displ_over``         particle_displ_over
+``reset_force_moment``          reset_force_moment
+``gravity_force``               gravity_force
+``contact_sphere``              contact_sphere / contact_singlemat_sphere_hooke_*
+``force_to_accel``              force_to_accel
+``combined_compute_prolog``     combined_compute_prolog
+``combined_compute_epilog``     combined_compute_epilog
+``simulation_state``            simulation_state
+``first_iteration``             first_iteration block of main-config.msp
+``step``                        compute_loop x n with numerical_scheme_verlet
+=============================  ==================================================
+
+Errors are raised as ``DemError`` (the reference prints and exits).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+
+
+def make_params(bounds_lo, bounds_hi, periodic=(0, 0, 0), rcut_inc=0.05, dt=1e-3, gravity=(0.0, 0.0, -9.807),
+                law=A.LAW_HOOKE_NONE, config=None, config_driver=None, cell_size=0.0, fp32_broad_phase=0,
+                fp32_contact_screen=0) -> A.Params:
+    p = A.Params()
+    p.bounds_lo[:] = list(map(float, bounds_lo))
+    p.bounds_hi[:] = list(map(float, bounds_hi))
+    p.periodic[:] = [int(bool(x)) for x in periodic]
+    p.rcut_inc = rcut_inc
+    p.cell_size = cell_size
+    p.dt = dt
+    p.gravity[:] = list(map(float, gravity))
+    p.symetric = 1
+    p.law = law
+    p.config = contact_params(**(config or {}))
+    p.config_driver = contact_params(**(config_driver or config or {}))
+    p.fp32_broad_phase = int(fp32_broad_phase)
+    p.fp32_contact_screen = int(fp32_contact_screen)
+    return p
+
+
+def contact_params(kn=1e4, kt=8e3, kr=0.0, mu=0.3, damp_rate=0.9, fc=0.0, dncut=0.0) -> A.ContactParams:
+    """ContactParams YAML keys (contact_parameters.hpp:138-190)."""
+    return A.ContactParams(kn, kt, kr, mu, damp_rate, fc, dncut)
+
+
+def empty_particles(n: int) -> dict:
+    a = {f: np.zeros(n) for f in A.PARTICLE_FIELDS}
+    a["id"] = np.zeros(n, dtype=np.uint64)
+    a["type"] = np.zeros(n, dtype=np.uint32)
+    a["group"] = np.zeros(n, dtype=np.uint32)
+    return a
+
+
+def _contig(arrays: dict) -> dict:
+    out = {}
+    for k, v in arrays.items():
+        if v is None:
+            continue
+        if k == "id":
+            out[k] = np.ascontiguousarray(v, dtype=np.uint64)
+        elif k in ("type", "group"):
+            out[k] = np.ascontiguousarray(v, dtype=np.uint32)
+        else:
+            out[k] = np.ascontiguousarray(v, dtype=np.float64)
+    return out
+
+
+class _Backend:
+    """Function table: the native library (``dem_*``).  Tests build the same
+    table over the oracle so both sides are driven by identical code."""
+
+    prefix = "dem_"
+
+    def __init__(self, lib):
+        self.lib = lib
+
+    def __getattr__(self, name):
+        return getattr(self.lib, self.prefix + name)
+
+
+class System:
+    def __init__(self, params: A.Params, backend=None):
+        self.b = backend or _Backend(A.load())
+        self.params = params
+        h = C.c_void_p()
+        self._check(self.b.ctx_create(C.byref(params), C.byref(h)), "ctx_create")
+        self.h = h
+        self.n = 0
+
+    # ------------------------------------------------------------ plumbing
+    def _check(self, rc: int, where: str) -> None:
+        if rc != A.DEM_OK:
+            msg = ""
+            if getattr(self, "h", None):
+                try:
+                    msg = (self.b.last_error(self.h) or b"").decode()
+                except Exception:  # noqa: BLE001
+                    msg = ""
+            raise A.DemError(rc, where, msg)
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.b.ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -------------------------------------------------------------- state
+    def set_params(self, params: A.Params) -> None:
+        self._check(self.b.set_params(self.h, C.byref(params)), "set_params")
+        self.params = params
+
+    def set_particles(self, arrays: dict) -> None:
+        arrays = _contig(arrays)
+        n = len(arrays["rx"])
+        st = A.particles_struct(arrays, n)
+        self._check(self.b.set_particles(self.h, C.byref(st), 0), "set_particles")
+        self.n = n
+
+    def register_surface(self, offset, normal, center=(0, 0, 0), vel=(0, 0, 0), vrot=(0, 0, 0)) -> None:
+        s = A.Surface(offset, (C.c_double * 3)(*normal), (C.c_double * 3)(*center), (C.c_double * 3)(*vel),
+                      (C.c_double * 3)(*vrot))
+        self._check(self.b.register_surface(self.h, C.byref(s)), "register_surface")
+
+    def register_cylinder(self, radius, axis, center, vel=(0, 0, 0), vrot=(0, 0, 0)) -> None:
+        c = A.Cylinder(radius, (C.c_double * 3)(*axis), (C.c_double * 3)(*center), (C.c_double * 3)(*vel),
+                       (C.c_double * 3)(*vrot))
+        self._check(self.b.register_cylinder(self.h, C.byref(c)), "register_cylinder")
+
+    def particles(self, sort_by_id: bool = True) -> dict:
+        a = {f: np.zeros(self.n) for f in A.PARTICLE_FIELDS}
+        a["id"] = np.zeros(self.n, dtype=np.uint64)
+        a["type"] = np.zeros(self.n, dtype=np.uint32)
+        a["group"] = np.zeros(self.n, dtype=np.uint32)
+        st = A.particles_struct(a, self.n)
+        self._check(self.b.get_particles(self.h, C.byref(st), 0), "get_particles")
+        if sort_by_id:
+            o = np.argsort(a["id"], kind="stable")
+            a = {k: v[o] for k, v in a.items()}
+        return a
+
+    # ---------------------------------------------------------- operators
+    def update_particle_neighbors(self) -> None:
+        self._check(self.b.update_particle_neighbors(self.h), "update_particle_neighbors")
+
+    def particle_displ_over(self) -> bool:
+        r = C.c_int()
+        self._check(self.b.particle_displ_over(self.h, C.byref(r)), "particle_displ_over")
+        return bool(r.value)
+
+    def reset_force_moment(self) -> None:
+        self._check(self.b.reset_force_moment(self.h), "reset_force_moment")
+
+    def gravity_force(self) -> None:
+        self._check(self.b.gravity_force(self.h), "gravity_force")
+
+    def contact_sphere(self) -> None:
+        self._check(self.b.contact_sphere(self.h), "contact_sphere")
+
+    def force_to_accel(self) -> None:
+        self._check(self.b.force_to_accel(self.h), "force_to_accel")
+
+    def combined_compute_prolog(self) -> None:
+        self._check(self.b.combined_compute_prolog(self.h), "combined_compute_prolog")
+
+    def combined_compute_epilog(self) -> None:
+        self._check(self.b.combined_compute_epilog(self.h), "combined_compute_epilog")
+
+    def first_iteration(self) -> None:
+        self._check(self.b.first_iteration(self.h), "first_iteration")
+
+    def step(self, nsteps: int = 1) -> None:
+        self._check(self.b.step(self.h, int(nsteps)), "step")
+
+    def rebuild_count(self) -> int:
+        v = C.c_uint64()
+        self._check(self.b.rebuild_count(self.h, C.byref(v)), "rebuild_count")
+        return int(v.value)
+
+    def simulation_state(self) -> dict:
+        s = A.State()
+        self._check(self.b.simulation_state(self.h, C.byref(s)), "simulation_state")
+        return {"kinetic_energy": np.array(s.kinetic_energy[:]), "rotation_energy": np.array(s.rotation_energy[:]),
+                "mass": s.mass, "n_particles": s.n_particles, "n_interactions": s.n_interactions,
+                "n_active_interactions": s.n_active_interactions}
+
+    def interaction_count(self) -> int:
+        v = C.c_uint64()
+        self._check(self.b.interaction_count(self.h, C.byref(v)), "interaction_count")
+        return int(v.value)
+
+    def interactions(self) -> dict:
+        m = self.interaction_count()
+        out = {"owner_id": np.zeros(m, np.uint64), "partner_id": np.zeros(m, np.uint64),
+               "type": np.zeros(m, np.uint16), "swap": np.zeros(m, np.uint8), "owner_sub": np.zeros(m, np.uint32),
+               "partner_sub": np.zeros(m, np.uint32), "friction": np.zeros(3 * m), "moment": np.zeros(3 * m)}
+        lst = A.InteractionList(m, 0, A.ptr(out["owner_id"], A.PU64), A.ptr(out["partner_id"], A.PU64),
+                                A.ptr(out["type"], A.PU16), A.ptr(out["swap"], A.PU8),
+                                A.ptr(out["owner_sub"], A.PU32), A.ptr(out["partner_sub"], A.PU32),
+                                A.ptr(out["friction"]), A.ptr(out["moment"]))
+        self._check(self.b.get_interactions(self.h, C.byref(lst)), "get_interactions")
+        out["friction"] = out["friction"].reshape(-1, 3)
+        out["moment"] = out["moment"].reshape(-1, 3)
+        return out
+
+    # ---------------------------------------------------------- profiling
+    def profile(self, enable: bool = True) -> None:
+        self._check(self.b.profile(self.h, int(enable)), "profile")
+
+    def kernel_stats(self) -> dict:
+        arr = (A.KernelStat * 64)()
+        cnt = C.c_int()
+        self._check(self.b.kernel_stats(self.h, arr, 64, C.byref(cnt)), "kernel_stats")
+        return {arr[i].name.decode(): {"launches": arr[i].launches, "timed": arr[i].timed,
+                                       "total_ms": arr[i].total_ms} for i in range(cnt.value)}
+
+    def reset_kernel_stats(self) -> None:
+        self._check(self.b.reset_kernel_stats(self.h), "reset_kernel_stats")
+
+    def stream_handle(self) -> int:
+        v = C.c_void_p()
+        self._check(self.b.ctx_stream(self.h, C.byref(v)), "ctx_stream")
+        return int(v.value or 0)
+
+    def packing_profile(self, nslabs: int, zlo: float, zhi: float) -> np.ndarray:
+        out = np.zeros(nslabs)
+        self._check(self.b.packing_profile(self.h, int(nslabs), float(zlo), float(zhi), A.ptr(out)),
+                    "packing_profile")
+        return out
+
+
+# Reference operator names -> System methods (what an .msp deck names).
+OPERATORS = {
+    "update_particle_neighbors": System.update_particle_neighbors,
+    "chunk_neighbors_contact": System.update_particle_neighbors,
+    "nbh_sphere": System.update_particle_neighbors,
+    "particle_displ_over": System.particle_displ_over,
+    "reset_force_moment": System.reset_force_moment,
+    "gravity_force": System.gravity_force,
+    "contact_sphere": System.contact_sphere,
+    "contact_singlemat_sphere_hooke": System.contact_sphere,
+    "contact_singlemat_sphere_hooke_none": System.contact_sphere,
+    "contact_singlemat_sphere_hooke_cohesive": System.contact_sphere,
+    "force_to_accel": System.force_to_accel,
+    "combined_compute_prolog": System.combined_compute_prolog,
+    "combined_compute_epilog": System.combined_compute_epilog,
+    "simulation_state": System.simulation_state,
+}

@@ -1,0 +1,247 @@
+/*
+ * dem_hotpath.h -- C ABI of the GB300-native exaDEM per-timestep hot path.
+ *
+ * Every entry point replaces one exaDEM / exaNBody operator (or a fixed
+ * sequence of them) of the default Verlet deck.  The reference interface each
+ * one stands in for is cited beside it (paths are relative to the exaDEM
+ * source tree).  The library owns its device memory; callers hand in and read
+ * back host (or device) arrays through plain pointers and sizes.
+ *
+ * Conventions
+ *   - every function returns an int status: DEM_OK (0) or a DEM_ERR_* code;
+ *     dem_last_error() returns a one-line description of the last failure.
+ *     (The reference prints and exits through color_log::error, e.g.
+ *     src/interaction/include/exaDEM/interaction/placeholder_interaction.hpp:188-193.)
+ *   - one dem_ctx is one simulated system (or one batch of systems); a ctx is
+ *     not thread-safe; all work is queued on the ctx's own CUDA stream.
+ *   - all particle state is FP64 structure-of-arrays, ids are uint64,
+ *     type/group are uint32 (include/exaDEM/fields.h:34-54).
+ */
+#ifndef DEM_HOTPATH_H
+#define DEM_HOTPATH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DEM_OK 0
+#define DEM_ERR_INVALID_ARG 1 /* bad pointer, size or parameter            */
+#define DEM_ERR_CUDA 2        /* a CUDA runtime call failed                */
+#define DEM_ERR_OOM 3         /* device allocation failed                  */
+#define DEM_ERR_UNSUPPORTED 4 /* feature outside the implemented path      */
+#define DEM_ERR_OVERFLOW 5    /* a fixed-capacity device buffer overflowed */
+#define DEM_ERR_TIMEOUT 6     /* a bounded device wait gave up             */
+#define DEM_ERR_STATE 7       /* call order violated (e.g. no particles)   */
+#define DEM_ERR_NO_DEVICE 8   /* no CUDA device visible                    */
+
+/* ---- interaction type ids (src/interaction/include/exaDEM/interaction/interaction_enum.hpp:24-57) */
+#define DEM_ITYPE_VERTEX_VERTEX 0
+#define DEM_ITYPE_VERTEX_EDGE 1
+#define DEM_ITYPE_VERTEX_FACE 2
+#define DEM_ITYPE_EDGE_EDGE 3
+#define DEM_ITYPE_VERTEX_CYLINDER 4
+#define DEM_ITYPE_VERTEX_SURFACE 5
+
+/* ---- contact law parameters -------------------------------------------
+ * Mirrors ContactParams {dncut, kn, kt, kr, fc, mu, damp_rate}
+ * (src/forcefield/include/exaDEM/forcefield/contact_parameters.hpp:32-41,138-190).
+ * dncut == 0 and fc == 0 means "no cohesion".                             */
+typedef struct dem_contact_params {
+  double kn, kt, kr, mu, damp_rate;
+  double fc, dncut;
+} dem_contact_params;
+
+/* Contact law variant, as in the operator names contact_singlemat_sphere_hooke_{none,cohesive}
+ * (src/sphere/CMakeLists.txt:63-110, contact_force.hpp:26-48).           */
+#define DEM_LAW_HOOKE_NONE 0
+#define DEM_LAW_HOOKE_COHESIVE 1
+
+/* ---- simulation / domain parameters ------------------------------------
+ * domain: bounds + periodic flags (exaNBody Domain, e.g.
+ * example/spheres/rotating-drum/rotating-drum-mini.msp "domain:" block);
+ * rcut_inc: Verlet skin (slot rcut_inc, nbh_sphere.cu:48);
+ * cell_size: 0 = deduced as max(2*r_max + rcut_inc) (config_globals.msp:35-37,
+ * src/field/dem_rcut_max.cpp:49-66).                                       */
+typedef struct dem_params {
+  double bounds_lo[3];
+  double bounds_hi[3];
+  int32_t periodic[3];
+  double rcut_inc;
+  double cell_size;
+  double dt;
+  double gravity[3];       /* gravity_force slot "gravity" (gravity_force.hpp:38-46) */
+  int32_t symetric;        /* nbh_sphere / contact_sphere slot "symetric"; only 1 is supported */
+  int32_t law;             /* DEM_LAW_* */
+  dem_contact_params config;        /* contact_sphere slot "config"        */
+  dem_contact_params config_driver; /* contact_sphere slot "config_driver" */
+  /* Split-precision switches (no effect on results, see DESIGN):
+   * fp32_broad_phase: FP32 cell-relative broad phase with a proven superset bound,
+   *                   then an exact FP64 decision in the rounding band;
+   * fp32_contact_screen: FP32 test that skips the FP64 contact law for pairs
+   *                   that are provably apart.                            */
+  int32_t fp32_broad_phase;
+  int32_t fp32_contact_screen;
+  int32_t reserved[6];
+} dem_params;
+
+/* ---- particle state view (host or device pointers) ---------------------
+ * Field names follow include/exaDEM/fields.h:34-54 and the implicit exaNBody
+ * fields rx..fz, id, type.  f holds forces after compute_force and
+ * accelerations after force_to_accel, exactly as in the reference.
+ * Pointers that are NULL in dem_get_particles are skipped.                */
+typedef struct dem_particles {
+  uint64_t n;
+  double *rx, *ry, *rz;
+  double *vx, *vy, *vz;
+  double *fx, *fy, *fz;
+  double *vrotx, *vroty, *vrotz; /* angular velocity (field vrot)      */
+  double *arotx, *aroty, *arotz; /* angular acceleration (field arot)  */
+  double *momx, *momy, *momz;    /* torque (field mom)                 */
+  double *qw, *qx, *qy, *qz;     /* orientation (field orient)         */
+  double *inertiax, *inertiay, *inertiaz;
+  double *mass, *radius, *homothety;
+  uint64_t *id;
+  uint32_t *type, *group;
+} dem_particles;
+
+/* ---- drivers (src/driver/include/exaDEM/surface.hpp:29-44, cylinder.hpp:27-36) */
+typedef struct dem_surface {
+  double offset;     /* along normal                       */
+  double normal[3];  /* unit normal                        */
+  double center[3];  /* defaults to offset*normal if vrot==0 (surface.hpp:68-76) */
+  double vel[3];
+  double vrot[3];
+} dem_surface;
+
+typedef struct dem_cylinder {
+  double radius;
+  double axis[3];    /* component mask, e.g. (1,0,1) for a y-axis drum (cylinder.hpp:255-277) */
+  double center[3];  /* stored as axis*center (cylinder.hpp:89-99)          */
+  double vel[3];
+  double vrot[3];    /* drum angular velocity                               */
+} dem_cylinder;
+
+/* ---- thermodynamic state (src/io/include/exaDEM/simulation_state.hpp:48-56) */
+typedef struct dem_state {
+  double kinetic_energy[3];  /* sum 0.5*m*v*v per component            */
+  double rotation_energy[3]; /* sum 0.5*m*w*w per component (sic)      */
+  double mass;
+  uint64_t n_particles;
+  uint64_t n_interactions;        /* candidate interactions in the list */
+  uint64_t n_active_interactions; /* with dn < 0 at the last force pass */
+} dem_state;
+
+/* ---- interaction list readback ------------------------------------------
+ * One row per interaction, sorted by InteractionPair::operator<
+ * (owner id, partner id, type, swap, owner sub, partner sub)
+ * (src/interaction/include/exaDEM/interaction/interaction_pair.hpp:222-249).
+ * For driver interactions partner_id is the driver index.  Arrays must hold
+ * `capacity` rows; NULL arrays are skipped.                               */
+typedef struct dem_interaction_list {
+  uint64_t capacity;
+  uint64_t count; /* out */
+  uint64_t *owner_id, *partner_id;
+  uint16_t *type;
+  uint8_t *swap;
+  uint32_t *owner_sub, *partner_sub;
+  double *friction;  /* 3*capacity, xyz interleaved (attr::friction) */
+  double *moment;    /* 3*capacity (attr::moment)                    */
+} dem_interaction_list;
+
+typedef struct dem_ctx dem_ctx;
+
+/* ---- lifecycle ----------------------------------------------------------- */
+/* Creates a context on the current CUDA device.  No reference counterpart:
+ * in exaDEM the operator slots own the data (onika::scg slots).           */
+int dem_ctx_create(const dem_params* params, dem_ctx** out);
+int dem_ctx_destroy(dem_ctx* ctx);
+const char* dem_last_error(const dem_ctx* ctx);
+/* The ctx's CUDA stream (cudaStream_t), as the operator's
+ * parallel_execution_context() stream (classifier_for_all.hpp:244-255).  */
+int dem_ctx_stream(dem_ctx* ctx, void** stream);
+int dem_set_params(dem_ctx* ctx, const dem_params* params);
+
+/* ---- state binding ------------------------------------------------------ */
+/* Replaces the particle set (input_data + set_fields, src/field/set_fields.cu:238-330).
+ * on_device != 0: the pointers are device pointers.                      */
+int dem_set_particles(dem_ctx* ctx, const dem_particles* p, int on_device);
+/* Reads the particle set back (in the library's internal cell order; use id). */
+int dem_get_particles(dem_ctx* ctx, dem_particles* out, int on_device);
+/* register_surface / register_cylinder (drivers.hpp:291-320).  Stationary
+ * motion only; vrot enters the relative velocity (rotating drum).         */
+int dem_register_surface(dem_ctx* ctx, const dem_surface* s);
+int dem_register_cylinder(dem_ctx* ctx, const dem_cylinder* c);
+
+/* ---- one call per reference operator ------------------------------------ */
+/* particle_displ_over (exaNBody; threshold max_displ = rcut_inc/2,
+ * config_move_particles.msp:12-15): *result = 1 if some particle moved by
+ * >= threshold since the last neighbour update.                          */
+int dem_particle_displ_over(dem_ctx* ctx, int* result);
+/* update_particle_neighbors for spheres: periodic wrap (move_particles),
+ * chunk_neighbors_contact (src/grid/chunk_neighbors_contact.cpp:45-114),
+ * nbh_sphere with history carry-over (src/sphere/nbh_sphere.cu:64-309,
+ * interaction_manager.hpp:89-112), classify_interactions
+ * (src/interaction/classify_interactions.cpp:52-136) and backup_r.      */
+int dem_update_particle_neighbors(dem_ctx* ctx);
+/* reset_force_moment (src/numericalscheme/reset_force_moment.cu:69-70) */
+int dem_reset_force_moment(dem_ctx* ctx);
+/* gravity_force (src/forcefield/gravity_force.cu:67-86), g from params */
+int dem_gravity_force(dem_ctx* ctx);
+/* contact_sphere / contact_singlemat_sphere_hooke_{none,cohesive}
+ * (src/sphere/contact_force_sphere.cu.in:133-188, contact_sphere.hpp:122-297).
+ * Adds contact forces and torques to f and mom with a deterministic
+ * per-particle gather instead of atomics.                                 */
+int dem_contact_sphere(dem_ctx* ctx);
+/* force_to_accel (src/numericalscheme/include/exaDEM/force_to_accel.hpp:26-33) */
+int dem_force_to_accel(dem_ctx* ctx);
+/* combined_compute_prolog (src/numericalscheme/combined_compute_prolog.cu:94-116) */
+int dem_combined_compute_prolog(dem_ctx* ctx);
+/* combined_compute_epilog (src/numericalscheme/combined_compute_epilog.cu:94-113) */
+int dem_combined_compute_epilog(dem_ctx* ctx);
+/* simulation_state (src/io/simulation_state.cu:121-200) */
+int dem_simulation_state(dem_ctx* ctx, dem_state* out);
+
+/* ---- fused sequences ------------------------------------------------------ */
+/* first_iteration (data/config/main-config.msp:55-65): init_particles
+ * (neighbour build), reset_force_moment, compute_force (gravity + contact).
+ * As in the reference deck, force_to_accel is NOT applied here.           */
+int dem_first_iteration(dem_ctx* ctx);
+/* nsteps iterations of compute_loop with numerical_scheme_verlet
+ * (config_numerical_schemes.msp:6-28): prolog, displacement trigger and
+ * conditional rebuild, reset, gravity, contact, force_to_accel, epilog.
+ * The device decides rebuilds; the host does not synchronise per step.  */
+int dem_step(dem_ctx* ctx, int nsteps);
+/* Number of neighbour rebuilds done so far (trigger_move_particles count). */
+int dem_rebuild_count(dem_ctx* ctx, uint64_t* out);
+
+/* ---- analysis / parity readback ------------------------------------------ */
+int dem_interaction_count(dem_ctx* ctx, uint64_t* out);
+int dem_get_interactions(dem_ctx* ctx, dem_interaction_list* out);
+/* Packing-fraction profile: solid volume fraction of the spheres in nslabs
+ * equal horizontal slabs between zlo and zhi (no reference counterpart;
+ * analytic sphere/slab volumes).  out has nslabs entries.                 */
+int dem_packing_profile(dem_ctx* ctx, int nslabs, double zlo, double zhi, double* out);
+
+/* ---- profiling ------------------------------------------------------------
+ * Stands in for onika's per-operator timers (profiling: exectime / summary,
+ * data/config/config_defaults.msp:30-33).  Kernel launches are always
+ * counted; with dem_profile(ctx, 1) each kernel class is also timed with CUDA
+ * events on the ctx stream.  dem_kernel_stats fills up to `capacity` rows.  */
+typedef struct dem_kernel_stat {
+  char name[24];
+  uint64_t launches;
+  uint64_t timed;   /* number of timed launch groups  */
+  double total_ms;  /* summed CUDA-event time          */
+} dem_kernel_stat;
+int dem_profile(dem_ctx* ctx, int enable);
+int dem_kernel_stats(dem_ctx* ctx, dem_kernel_stat* out, int capacity, int* count);
+int dem_reset_kernel_stats(dem_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DEM_HOTPATH_H */

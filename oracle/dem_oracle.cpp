@@ -1,0 +1,924 @@
+/*
+ * dem_oracle.cpp -- CPU oracle for the exaDEM per-timestep hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU library is
+ * compared against (tests/, the smoke check and the CPU baseline leg of the
+ * benchmark).  Nothing in the product links or calls it.
+ *
+ * It restates, in plain sequential C++ (OpenMP only over independent items,
+ * so results do not depend on the thread count), the arithmetic of the
+ * reference CPU path for spheres.  Each function cites the reference lines it
+ * follows (paths relative to the exaDEM source tree).  Two external libraries
+ * of the reference are not vendored and are restated from their mathematics:
+ *   - onika (Collab4exaNBody/onika, unpinned HEAD): Vec3d operators
+ *     (component-wise), dot/cross/norm, Quaternion*Vec3d rotation,
+ *     dot(Quaternion, Vec3d) time derivative and normalize().  The quaternion
+ *     formulas follow exaDEM's own quat type, which is the same lineage
+ *     (src/shape/include/exaDEM/type/quat.hpp:71-110,233-242).
+ *   - exaNBody (Collab4exaNBody/exaNBody, unpinned HEAD): the neighbour search
+ *     (all pairs with d2 > 0, d2 < (r_a+r_b+rcut_inc)^2 and d2 < nbh_dist^2,
+ *     src/grid/chunk_neighbors_contact.cpp:45-57), periodic ghost images,
+ *     PushVec3{First,Second}OrderFunctor (x += v*dt + a*dt^2/2, v += a*dt/2)
+ *     and particle_displ_over (|r - r_backup|^2 >= max_displ^2).
+ * Parity status: the reference itself cannot be compiled here (exaNBody, onika,
+ * MPI and yaml-cpp are absent) and ships no golden values for this path, so
+ * this restatement is pinned only by analytic known-answer tests.
+ *
+ * Canonical summation order (the reference sums with unordered atomics,
+ * contact_sphere.hpp:183-196): for each particle, f = g*m, then the
+ * contributions of the interactions it owns in InteractionPair order, then
+ * those where it is the partner, in InteractionPair order.
+ *
+ * Build: g++ -O2 -ffp-contract=off -fopenmp (no -ffast-math: the rolling
+ * clip below relies on IEEE NaN semantics).
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/dem_hotpath.h"
+
+namespace {
+
+struct V3 {
+  double x, y, z;
+};
+inline V3 operator+(const V3& a, const V3& b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 operator-(const V3& a, const V3& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 operator-(const V3& a) { return {-a.x, -a.y, -a.z}; }
+inline V3 operator*(const V3& a, double s) { return {a.x * s, a.y * s, a.z * s}; }
+inline V3 operator*(double s, const V3& a) { return {s * a.x, s * a.y, s * a.z}; }
+inline V3 operator*(const V3& a, const V3& b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline V3 operator/(const V3& a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+inline V3& operator+=(V3& a, const V3& b) { a.x += b.x; a.y += b.y; a.z += b.z; return a; }
+inline V3& operator-=(V3& a, const V3& b) { a.x -= b.x; a.y -= b.y; a.z -= b.z; return a; }
+inline V3& operator*=(V3& a, double s) { a.x *= s; a.y *= s; a.z *= s; return a; }
+inline double dot(const V3& a, const V3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V3 cross(const V3& a, const V3& b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline double norm(const V3& a) { return std::sqrt(dot(a, a)); }
+inline bool is_null(const V3& a) { return a.x == 0.0 && a.y == 0.0 && a.z == 0.0; }
+
+struct Quat {
+  double w, x, y, z;
+};
+// Quaternion * Vec3d rotation (type/quat.hpp:79-89).
+inline V3 rotate(const Quat& q, const V3& v) {
+  V3 qv = {q.x, q.y, q.z};
+  V3 uv = cross(qv, v);
+  V3 uuv = cross(qv, uv);
+  uv *= (2.0 * q.w);
+  uuv *= 2.0;
+  return v + uv + uuv;
+}
+// dot(Q, omega): quaternion time derivative (type/quat.hpp:91-96).
+inline Quat qdot(const Quat& q, const V3& om) {
+  Quat r;
+  r.x = 0.5 * (om.y * q.z - om.z * q.y + om.x * q.w);
+  r.y = 0.5 * (om.z * q.x - om.x * q.z + om.y * q.w);
+  r.z = 0.5 * (om.x * q.y - om.y * q.x + om.z * q.w);
+  r.w = -0.5 * (om.x * q.x + om.y * q.y + om.z * q.z);
+  return r;
+}
+// normalize (type/quat.hpp:233-242).
+inline Quat qnormalize(Quat q) {
+  double norm2 = q.w * q.w + (q.x * q.x + q.y * q.y + q.z * q.z);
+  if (norm2 <= 1e-9) return {1.0, 0.0, 0.0, 0.0};
+  double n = std::sqrt(norm2);
+  double inv = 1.0 / n;
+  return {q.w * inv, q.x * inv, q.y * inv, q.z * inv};
+}
+
+struct Surface {
+  double offset;
+  V3 normal, center, center_proj, vel, vrot;
+};
+struct Cylinder {
+  double radius;
+  V3 axis, center, vel, vrot;
+};
+struct Driver {
+  int kind;  // 0 surface, 1 cylinder
+  Surface s;
+  Cylinder c;
+};
+
+// One interaction = InteractionPair + Interaction data (interaction_pair.hpp:56-71,
+// interaction.hpp:44-49).  Sphere pairs: type 0, swap 0, subs 0.
+struct Inter {
+  uint64_t oid, pid;
+  uint16_t type;
+  uint8_t swap;
+  uint8_t owner_only;  // partner is a periodic ghost image: its force is discarded
+  uint32_t osub, psub;
+  int32_t oi, pj;      // particle indices (pj = driver index for drivers)
+  int8_t sh[3];        // periodic image of the partner: r_j + sh*L
+  V3 friction, moment;
+};
+inline bool key_less(const Inter& a, const Inter& b) {  // InteractionPair::operator< (interaction_pair.hpp:222-249)
+  if (a.oid != b.oid) return a.oid < b.oid;
+  if (a.pid != b.pid) return a.pid < b.pid;
+  if (a.type != b.type) return a.type < b.type;
+  if (a.swap != b.swap) return a.swap < b.swap;
+  if (a.osub != b.osub) return a.osub < b.osub;
+  return a.psub < b.psub;
+}
+inline bool key_eq(const Inter& a, const Inter& b) {  // interaction_pair.hpp:186-198
+  return a.oid == b.oid && a.pid == b.pid && a.osub == b.osub && a.psub == b.psub && a.swap == b.swap &&
+         a.type == b.type;
+}
+
+struct Rec {  // per-interaction force record
+  V3 f, ti, tj;
+  int active;
+};
+
+struct Oracle {
+  dem_params prm;
+  size_t n = 0;
+  std::vector<double> rx, ry, rz, vx, vy, vz, fx, fy, fz, wx, wy, wz, ax, ay, az, mx, my, mz, qw, qx, qy, qz, ix,
+      iy, iz, mass, rad, hom, bx, by, bz;
+  std::vector<uint64_t> id;
+  std::vector<uint32_t> type, group;
+  std::vector<Driver> drivers;
+  std::vector<Inter> inter;          // global InteractionPair order
+  std::vector<size_t> own_off;       // per particle: owned range (particles sorted by id index)
+  std::vector<int32_t> own_first;    // per particle index: first owned interaction or -1
+  std::vector<int32_t> own_cnt;
+  std::vector<size_t> rev_off;       // per particle: partner-side interactions
+  std::vector<int32_t> rev_idx;
+  std::vector<Rec> rec;
+  uint64_t rebuilds = 0;
+  uint64_t n_active = 0;
+  std::string err;
+};
+
+inline double L(const Oracle& o, int d) { return o.prm.bounds_hi[d] - o.prm.bounds_lo[d]; }
+
+V3 pos(const Oracle& o, size_t i) { return {o.rx[i], o.ry[i], o.rz[i]}; }
+
+// Partner position with its periodic ghost image (exaNBody ghost copy r + shift).
+V3 partner_pos(const Oracle& o, const Inter& it) {
+  V3 r = pos(o, it.pj);
+  if (it.sh[0]) r.x = r.x + (double)it.sh[0] * L(o, 0);
+  if (it.sh[1]) r.y = r.y + (double)it.sh[1] * L(o, 1);
+  if (it.sh[2]) r.z = r.z + (double)it.sh[2] * L(o, 2);
+  return r;
+}
+
+double nbh_dist(const Oracle& o) {
+  double rmax = 0.0;
+  for (size_t i = 0; i < o.n; i++) rmax = std::max(rmax, 2 * o.rad[i]);  // dem_rcut_max.cpp:49-66
+  return rmax + o.prm.rcut_inc;
+}
+
+// ---------------------------------------------------------------- drivers
+// Surface::filter / detector (src/driver/include/exaDEM/surface.hpp:320-350)
+bool surface_filter(const Surface& s, double rcut, const V3& p) {
+  V3 proj = dot(p, s.normal) * s.normal;
+  double d = norm(proj - s.center_proj);
+  return d <= rcut;
+}
+bool surface_detect(const Surface& s, double rcut, const V3& p, double& dn, V3& n, V3& cp) {
+  V3 proj = dot(p, s.normal) * s.normal;
+  V3 s2p = -(s.center_proj - proj);
+  double d = norm(s2p);
+  dn = d - rcut;
+  if (dn > 0) return false;
+  n = s2p / d;
+  cp = p - n * (rcut + 0.5 * dn);
+  return true;
+}
+// Cylinder::filter / detector (src/driver/include/exaDEM/cylinder.hpp:225-277)
+bool cylinder_filter(const Cylinder& c, double rcut, const V3& vi) {
+  V3 proj = vi * c.axis;
+  V3 dir = proj - c.center;
+  double d = norm(dir);
+  double dn = c.radius - (d + rcut);
+  return dn <= 0;
+}
+bool cylinder_detect(const Cylinder& c, double rcut, const V3& pi, double& dn, V3& n, V3& cp) {
+  V3 proj = pi * c.axis;
+  V3 dir = c.center - proj;
+  double d = norm(dir);
+  dn = c.radius - (rcut + d);
+  if (dn > 0) return false;
+  n = dir / d;
+  cp = pi - n * (rcut + 0.5 * dn);
+  return true;
+}
+
+// ---------------------------------------------------------- neighbour build
+// Periodic wrap done by move_particles before each rebuild.
+void wrap(Oracle& o) {
+  for (int d = 0; d < 3; d++) {
+    if (!o.prm.periodic[d]) continue;
+    double lo = o.prm.bounds_lo[d], hi = o.prm.bounds_hi[d], Ld = hi - lo;
+    std::vector<double>& r = d == 0 ? o.rx : (d == 1 ? o.ry : o.rz);
+    for (size_t i = 0; i < o.n; i++) {
+      double x = r[i];
+      if (x < lo) {
+        x = x + Ld;
+        if (x >= hi) x = lo;
+      } else if (x >= hi) {
+        x = x - Ld;
+        if (x < lo) x = lo;
+      }
+      r[i] = x;
+    }
+  }
+}
+
+// chunk_neighbors_contact + nbh_sphere (symetric) + classify, with history
+// carried over by InteractionPair equality (interaction_manager.hpp:89-112,
+// placeholder_interaction.hpp:398-408).
+int update_neighbors(Oracle& o) {
+  wrap(o);
+  const double skin = o.prm.rcut_inc;
+  const double nd = nbh_dist(o);
+  const double rcut2 = nd * nd;
+  double cs = std::max(o.prm.cell_size, nd);
+  int dims[3];
+  double lo[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = o.prm.bounds_lo[d];
+    dims[d] = std::max(1, (int)std::floor(L(o, d) / cs));
+    if (o.prm.periodic[d] && dims[d] < 3) {
+      o.err = "periodic dimension needs at least 3 cells";
+      return DEM_ERR_INVALID_ARG;
+    }
+  }
+  double csz[3];
+  for (int d = 0; d < 3; d++) csz[d] = o.prm.periodic[d] ? L(o, d) / dims[d] : cs;
+  if (!o.prm.periodic[0] || !o.prm.periodic[1] || !o.prm.periodic[2]) {
+    // non periodic dims: grid from bounds, particles outside clamped into border cells
+    for (int d = 0; d < 3; d++)
+      if (!o.prm.periodic[d]) dims[d] = std::max(1, (int)std::ceil(L(o, d) / cs));
+  }
+  auto cell_of = [&](size_t i, int c[3]) {
+    double r[3] = {o.rx[i], o.ry[i], o.rz[i]};
+    for (int d = 0; d < 3; d++) {
+      long k = (long)std::floor((r[d] - lo[d]) / csz[d]);
+      if (k < 0) k = 0;
+      if (k >= dims[d]) k = dims[d] - 1;
+      c[d] = (int)k;
+    }
+  };
+  size_t ncell = (size_t)dims[0] * dims[1] * dims[2];
+  std::vector<size_t> cstart(ncell + 1, 0), cidx(o.n);
+  std::vector<int> pc(3 * o.n);
+  for (size_t i = 0; i < o.n; i++) {
+    cell_of(i, &pc[3 * i]);
+    size_t c = (size_t)pc[3 * i] + dims[0] * ((size_t)pc[3 * i + 1] + (size_t)dims[1] * pc[3 * i + 2]);
+    cstart[c + 1]++;
+  }
+  for (size_t c = 0; c < ncell; c++) cstart[c + 1] += cstart[c];
+  {
+    std::vector<size_t> cur(cstart.begin(), cstart.end() - 1);
+    for (size_t i = 0; i < o.n; i++) {
+      size_t c = (size_t)pc[3 * i] + dims[0] * ((size_t)pc[3 * i + 1] + (size_t)dims[1] * pc[3 * i + 2]);
+      cidx[cur[c]++] = i;
+    }
+  }
+
+  // per owner candidate lists
+  std::vector<std::vector<Inter>> per(o.n);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (long ii = 0; ii < (long)o.n; ii++) {
+    size_t i = (size_t)ii;
+    std::vector<Inter>& lst = per[i];
+    const V3 ri = pos(o, i);
+    // drivers first (nbh_sphere.cu:140-233)
+    for (size_t k = 0; k < o.drivers.size(); k++) {
+      const Driver& dv = o.drivers[k];
+      const double rv = o.rad[i] + skin;
+      bool keep = dv.kind == 0 ? surface_filter(dv.s, rv, ri) : cylinder_filter(dv.c, rv, ri);
+      if (!keep) continue;
+      Inter it{};
+      it.oid = o.id[i];
+      it.pid = k;
+      it.type = dv.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER;
+      it.oi = (int32_t)i;
+      it.pj = (int32_t)k;
+      lst.push_back(it);
+    }
+    // particle pairs over the 27-cell stencil (nbh_sphere.cu:238-263)
+    const int* ci = &pc[3 * i];
+    for (int dz = -1; dz <= 1; dz++)
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          int c[3] = {ci[0] + dx, ci[1] + dy, ci[2] + dz};
+          int sh[3] = {0, 0, 0};
+          bool skip = false;
+          for (int d = 0; d < 3; d++) {
+            if (c[d] < 0) {
+              if (!o.prm.periodic[d]) { skip = true; break; }
+              c[d] += dims[d];
+              sh[d] = -1;
+            } else if (c[d] >= dims[d]) {
+              if (!o.prm.periodic[d]) { skip = true; break; }
+              c[d] -= dims[d];
+              sh[d] = 1;
+            }
+          }
+          if (skip) continue;
+          size_t cc = (size_t)c[0] + dims[0] * ((size_t)c[1] + (size_t)dims[1] * c[2]);
+          for (size_t q = cstart[cc]; q < cstart[cc + 1]; q++) {
+            size_t j = cidx[q];
+            V3 rj = pos(o, j);
+            if (sh[0]) rj.x = rj.x + (double)sh[0] * L(o, 0);
+            if (sh[1]) rj.y = rj.y + (double)sh[1] * L(o, 1);
+            if (sh[2]) rj.z = rj.z + (double)sh[2] * L(o, 2);
+            const double ddx = rj.x - ri.x, ddy = rj.y - ri.y, ddz = rj.z - ri.z;
+            const double d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            const double rmax = o.rad[i] + o.rad[j] + skin;  // ContactNeighborFilterFunc
+            if (!(d2 > 0.0 && d2 < rmax * rmax && d2 < rcut2)) continue;
+            const bool ghost = sh[0] || sh[1] || sh[2];
+            if (!ghost && o.id[i] >= o.id[j]) continue;
+            Inter it{};
+            it.oid = o.id[i];
+            it.pid = o.id[j];
+            it.type = DEM_ITYPE_VERTEX_VERTEX;
+            it.oi = (int32_t)i;
+            it.pj = (int32_t)j;
+            it.owner_only = ghost ? 1 : 0;
+            it.sh[0] = (int8_t)sh[0];
+            it.sh[1] = (int8_t)sh[1];
+            it.sh[2] = (int8_t)sh[2];
+            lst.push_back(it);
+          }
+        }
+    std::sort(lst.begin(), lst.end(), key_less);
+  }
+  // global InteractionPair order = owners by id
+  std::vector<size_t> by_id(o.n);
+  for (size_t i = 0; i < o.n; i++) by_id[i] = i;
+  std::sort(by_id.begin(), by_id.end(), [&](size_t a, size_t b) { return o.id[a] < o.id[b]; });
+  std::vector<Inter> fresh;
+  size_t tot = 0;
+  for (size_t i = 0; i < o.n; i++) tot += per[i].size();
+  fresh.reserve(tot);
+  for (size_t k = 0; k < o.n; k++) {
+    auto& l = per[by_id[k]];
+    fresh.insert(fresh.end(), l.begin(), l.end());
+  }
+  // history carry-over: old list is sorted by key, binary search like update()
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < (long)fresh.size(); k++) {
+    Inter& it = fresh[k];
+    auto lb = std::lower_bound(o.inter.begin(), o.inter.end(), it, key_less);
+    if (lb != o.inter.end() && key_eq(*lb, it)) {
+      it.friction = lb->friction;
+      it.moment = lb->moment;
+    }
+  }
+  o.inter.swap(fresh);
+  // owned ranges and partner lists (canonical gather order)
+  o.own_first.assign(o.n, -1);
+  o.own_cnt.assign(o.n, 0);
+  for (size_t k = 0; k < o.inter.size(); k++) {
+    const Inter& it = o.inter[k];
+    if (o.own_first[it.oi] < 0) o.own_first[it.oi] = (int32_t)k;
+    o.own_cnt[it.oi]++;
+  }
+  o.rev_off.assign(o.n + 1, 0);
+  for (const Inter& it : o.inter)
+    if (it.type == DEM_ITYPE_VERTEX_VERTEX && !it.owner_only) o.rev_off[it.pj + 1]++;
+  for (size_t i = 0; i < o.n; i++) o.rev_off[i + 1] += o.rev_off[i];
+  o.rev_idx.assign(o.rev_off[o.n], 0);
+  {
+    std::vector<size_t> cur(o.rev_off.begin(), o.rev_off.end() - 1);
+    for (size_t k = 0; k < o.inter.size(); k++) {  // k ascending = key order
+      const Inter& it = o.inter[k];
+      if (it.type == DEM_ITYPE_VERTEX_VERTEX && !it.owner_only) o.rev_idx[cur[it.pj]++] = (int32_t)k;
+    }
+  }
+  o.rec.assign(o.inter.size(), Rec{});
+  // backup_r
+  o.bx = o.rx;
+  o.by = o.ry;
+  o.bz = o.rz;
+  o.rebuilds++;
+  return DEM_OK;
+}
+
+// --------------------------------------------------------------- contact law
+// contact_force_core<Hooke, None|Cohesive> (src/forcefield/include/exaDEM/forcefield/contact_force.hpp:146-235)
+// with common_kernels.hpp:27-145.
+void contact_force_core(bool cohesive, double dn, const V3& n, double dt, const dem_contact_params& hkp, double meff,
+                        V3& ft, const V3& cp, const V3& pos_i, const V3& vel_i, V3& f_i, V3& mom_i,
+                        const V3& vrot_i, const V3& pos_j, const V3& vel_j, const V3& vrot_j) {
+  if (cohesive) {
+    if (dn >= 0) {
+      const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
+      f_i += fn_value * n;
+      ft = {0, 0, 0};
+      return;
+    }
+  }
+  const double damp = hkp.damp_rate * 2.0 * std::sqrt(hkp.kn * meff);  // compute_damp
+  // compute_relative_velocity
+  const V3 contribution_i = vel_i - cross(cp - pos_i, vrot_i);
+  const V3 contribution_j = vel_j - cross(cp - pos_j, vrot_j);
+  const V3 vel = contribution_j - contribution_i;
+  const double vn = dot(vel, n);
+  V3 fn;
+  {
+    const double fne = -hkp.kn * dn;
+    const double fnv = damp * vn;
+    double nf = (fnv + fne > 0) ? fnv + fne : 0;  // normal_force
+    if (cohesive) {
+      const double fn_norm = nf - hkp.fc;
+      nf = fn_norm < (-hkp.fc) ? -hkp.fc : fn_norm;
+    }
+    fn = nf * n;
+  }
+  {
+    const V3 vt = vel - vn * n;
+    const V3 ftd = dt * vt;
+    ft += hkp.kt * ftd;  // compute_tangential_force
+  }
+  double threshold_ft;
+  if (!cohesive) {
+    const double fne = hkp.kn * dn;
+    threshold_ft = std::fabs(hkp.mu * fne);
+  } else {
+    threshold_ft = std::fabs(hkp.mu * (dot(fn, n) + hkp.fc));
+  }
+  {
+    double ft_square = dot(ft, ft);  // fit_tangential_force
+    if (ft_square > 0.0 && ft_square > threshold_ft * threshold_ft) ft *= (threshold_ft / std::sqrt(ft_square));
+  }
+  f_i = fn + ft;
+  mom_i += hkp.kr * (vrot_j - vrot_i) * dt;
+  V3 branch = cp - pos_i;
+  double r = (dot(branch, vrot_i)) / (dot(vrot_i, vrot_i));
+  branch -= r * vrot_i;
+  constexpr double mur = 0;
+  double threshold_mom = std::fabs(mur * norm(branch) * norm(fn));
+  double mom_square = dot(mom_i, mom_i);
+  if (mom_square > 0.0 && mom_square > threshold_mom * threshold_mom)
+    mom_i = mom_i * (threshold_mom / std::sqrt(mom_square));
+}
+
+// sphere::ContactLawFunc (src/sphere/include/exaDEM/sphere/contact_sphere.hpp:122-203) and
+// ContactLawDriverFunc (contact_sphere.hpp:231-297), producing a force record.
+void contact_one(Oracle& o, size_t k) {
+  Inter& it = o.inter[k];
+  Rec& rc = o.rec[k];
+  rc = Rec{};
+  const bool cohesive = o.prm.law == DEM_LAW_HOOKE_COHESIVE;
+  const double dt = o.prm.dt;
+  const size_t i = it.oi;
+  const V3 ri = pos(o, i);
+  const V3 vrot_i = {o.wx[i], o.wy[i], o.wz[i]};
+  if (it.type == DEM_ITYPE_VERTEX_VERTEX) {
+    const size_t j = it.pj;
+    const V3 rj = partner_pos(o, it);
+    const double rad_i = o.rad[i], rad_j = o.rad[j];
+    const V3 vrot_j = {o.wx[j], o.wy[j], o.wz[j]};
+    // detection_vertex_vertex_core (src/shape/include/exaDEM/shape_detection_core.hpp:57-81)
+    const double R = rad_i + rad_j;
+    const V3 dist = ri - rj;
+    const double dist_norm = norm(dist);
+    const double inv_dist_norm = 1.0 / dist_norm;
+    double dn = dist_norm - R;
+    const V3 n = dist * inv_dist_norm;
+    const V3 cp = ri - n * (rad_i + 0.5 * dn);
+    bool contact = dn < 0;
+    const dem_contact_params& cpar = o.prm.config;
+    if (cohesive) contact = (contact || dn <= cpar.dncut);
+    if (contact) {
+      const V3 vi = {o.vx[i], o.vy[i], o.vz[i]};
+      const V3 vj = {o.vx[j], o.vy[j], o.vz[j]};
+      const double m_i = o.mass[i], m_j = o.mass[j];
+      V3 f = {0, 0, 0};
+      const double meff = (m_i * m_j) / (m_i + m_j);  // compute_effective_mass
+      contact_force_core(cohesive, dn, n, dt, cpar, meff, it.friction, cp, ri, vi, f, it.moment, vrot_i, rj, vj,
+                         vrot_j);
+      rc.f = f;
+      rc.ti = cross(cp - ri, f) + it.moment;       // compute_moments
+      rc.tj = cross(cp - rj, -f) + (-it.moment);
+      rc.active = dn < 0;
+    } else {
+      it.friction = {0, 0, 0};
+      it.moment = {0, 0, 0};
+    }
+    return;
+  }
+  // drivers
+  const Driver& dv = o.drivers[it.pj];
+  const double rad = o.rad[i];
+  double dn = 0;
+  V3 n{}, cp{};
+  bool contact;
+  V3 dpos, dvel, dvrot;
+  if (dv.kind == 0) {
+    contact = surface_detect(dv.s, rad, ri, dn, n, cp);
+    dpos = dv.s.center;
+    dvel = dv.s.vel;
+    dvrot = dv.s.vrot;
+  } else {
+    contact = cylinder_detect(dv.c, rad, ri, dn, n, cp);
+    dpos = dv.c.center;
+    dvel = dv.c.vel;
+    dvrot = dv.c.vrot;
+  }
+  const dem_contact_params& cpar = o.prm.config_driver;
+  if (cohesive) contact = (contact || dn <= cpar.dncut);
+  if (contact) {
+    const V3 v = {o.vx[i], o.vy[i], o.vz[i]};
+    const double meff = o.mass[i];
+    V3 f = {0, 0, 0};
+    contact_force_core(cohesive, dn, n, dt, cpar, meff, it.friction, cp, ri, v, f, it.moment, vrot_i, dpos, dvel,
+                       dvrot);
+    rc.f = f;
+    rc.ti = cross(cp - ri, f) + it.moment;
+    rc.active = dn < 0;
+  } else {
+    it.friction = {0, 0, 0};
+    it.moment = {0, 0, 0};
+  }
+}
+
+void contact_all(Oracle& o) {
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < (long)o.inter.size(); k++) contact_one(o, (size_t)k);
+  uint64_t na = 0;
+  for (const Rec& r : o.rec) na += r.active ? 1 : 0;
+  o.n_active = na;
+  // deterministic gather: owned contributions (key order) then partner contributions (key order)
+#pragma omp parallel for schedule(static)
+  for (long ii = 0; ii < (long)o.n; ii++) {
+    size_t i = (size_t)ii;
+    V3 f = {o.fx[i], o.fy[i], o.fz[i]};
+    V3 m = {o.mx[i], o.my[i], o.mz[i]};
+    if (o.own_first[i] >= 0) {
+      for (int32_t k = o.own_first[i]; k < o.own_first[i] + o.own_cnt[i]; k++) {
+        f += o.rec[k].f;
+        m += o.rec[k].ti;
+      }
+    }
+    for (size_t q = o.rev_off[i]; q < o.rev_off[i + 1]; q++) {
+      const Rec& r = o.rec[o.rev_idx[q]];
+      f += -r.f;
+      m += r.tj;
+    }
+    o.fx[i] = f.x;
+    o.fy[i] = f.y;
+    o.fz[i] = f.z;
+    o.mx[i] = m.x;
+    o.my[i] = m.y;
+    o.mz[i] = m.z;
+  }
+}
+
+// ------------------------------------------------------------ particle ops
+void reset_force_moment(Oracle& o) {  // reset_force_moment.cu:69-70
+  std::fill(o.fx.begin(), o.fx.end(), 0.0);
+  std::fill(o.fy.begin(), o.fy.end(), 0.0);
+  std::fill(o.fz.begin(), o.fz.end(), 0.0);
+  std::fill(o.mx.begin(), o.mx.end(), 0.0);
+  std::fill(o.my.begin(), o.my.end(), 0.0);
+  std::fill(o.mz.begin(), o.mz.end(), 0.0);
+}
+void gravity_force(Oracle& o) {  // gravity_force.hpp:38-46
+  const double* g = o.prm.gravity;
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)o.n; i++) {
+    o.fx[i] += g[0] * o.mass[i];
+    o.fy[i] += g[1] * o.mass[i];
+    o.fz[i] += g[2] * o.mass[i];
+  }
+}
+void force_to_accel(Oracle& o) {  // force_to_accel.hpp:26-33
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)o.n; i++) {
+    o.fx[i] /= o.mass[i];
+    o.fy[i] /= o.mass[i];
+    o.fz[i] /= o.mass[i];
+  }
+}
+// combined_compute_prolog (combined_compute_prolog.cu:94-116): PushVec3SecondOrder,
+// PushVec3FirstOrder, PushToQuaternion (push_to_quaternion.hpp:26-38).
+void prolog(Oracle& o) {
+  const double delta_t = o.prm.dt;
+  const double half_delta_t = delta_t * 0.5;
+  const double delta_t2_2 = delta_t * delta_t * 0.5;
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)o.n; i++) {
+    o.rx[i] += o.vx[i] * delta_t + o.fx[i] * delta_t2_2;
+    o.ry[i] += o.vy[i] * delta_t + o.fy[i] * delta_t2_2;
+    o.rz[i] += o.vz[i] * delta_t + o.fz[i] * delta_t2_2;
+    o.vx[i] += o.fx[i] * half_delta_t;
+    o.vy[i] += o.fy[i] * half_delta_t;
+    o.vz[i] += o.fz[i] * half_delta_t;
+    Quat Q = {o.qw[i], o.qx[i], o.qy[i], o.qz[i]};
+    const V3 w = {o.wx[i], o.wy[i], o.wz[i]};
+    const Quat d = qdot(Q, w);
+    Q = {Q.w + d.w * delta_t, Q.x + d.x * delta_t, Q.y + d.y * delta_t, Q.z + d.z * delta_t};
+    Q = qnormalize(Q);
+    o.qw[i] = Q.w;
+    o.qx[i] = Q.x;
+    o.qy[i] = Q.y;
+    o.qz[i] = Q.z;
+    o.wx[i] += half_delta_t * o.ax[i];
+    o.wy[i] += half_delta_t * o.ay[i];
+    o.wz[i] += half_delta_t * o.az[i];
+  }
+}
+// combined_compute_epilog (combined_compute_epilog.cu:94-113) with
+// PushToAngularAcceleration (angular_acceleration.hpp:27-43) and PushToAngularVelocity.
+void epilog(Oracle& o) {
+  const double half_delta_t = o.prm.dt * 0.5;
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < (long)o.n; i++) {
+    const Quat Q = {o.qw[i], o.qx[i], o.qy[i], o.qz[i]};
+    const Quat Qinv = {Q.w, -Q.x, -Q.y, -Q.z};
+    const V3 vrot = {o.wx[i], o.wy[i], o.wz[i]};
+    const V3 mom = {o.mx[i], o.my[i], o.mz[i]};
+    const V3 I = {o.ix[i], o.iy[i], o.iz[i]};
+    const V3 omega = rotate(Qinv, vrot);
+    const V3 M = rotate(Qinv, mom);
+    const V3 domega = {(M.x - (I.z - I.y) * omega.y * omega.z) / I.x, (M.y - (I.x - I.z) * omega.z * omega.x) / I.y,
+                       (M.z - (I.y - I.x) * omega.x * omega.y) / I.z};
+    const V3 arot = rotate(Q, domega);
+    o.ax[i] = arot.x;
+    o.ay[i] = arot.y;
+    o.az[i] = arot.z;
+    o.wx[i] += arot.x * half_delta_t;
+    o.wy[i] += arot.y * half_delta_t;
+    o.wz[i] += arot.z * half_delta_t;
+    o.vx[i] += o.fx[i] * half_delta_t;
+    o.vy[i] += o.fy[i] * half_delta_t;
+    o.vz[i] += o.fz[i] * half_delta_t;
+  }
+}
+int displ_over(const Oracle& o) {
+  const double max_displ = o.prm.rcut_inc * 0.5;
+  const double thr2 = max_displ * max_displ;
+  int over = 0;
+#pragma omp parallel for schedule(static) reduction(| : over)
+  for (long i = 0; i < (long)o.n; i++) {
+    const double dx = o.rx[i] - o.bx[i], dy = o.ry[i] - o.by[i], dz = o.rz[i] - o.bz[i];
+    if (dx * dx + dy * dy + dz * dz >= thr2) over |= 1;
+  }
+  return over;
+}
+
+void compute_force(Oracle& o) {
+  gravity_force(o);
+  contact_all(o);
+}
+
+// Profile: solid fraction of spheres in horizontal slabs (analytic cap volumes).
+double sphere_slab_volume(double zc, double r, double a, double b) {
+  double lo = std::max(a, zc - r), hi = std::min(b, zc + r);
+  if (hi <= lo) return 0.0;
+  // integral of pi*(r^2 - (z-zc)^2) dz from lo to hi
+  auto F = [&](double z) {
+    double u = z - zc;
+    return r * r * u - u * u * u / 3.0;
+  };
+  return M_PI * (F(hi) - F(lo));
+}
+
+}  // namespace
+
+// ============================================================== C interface
+extern "C" {
+
+int oracle_create(const dem_params* p, void** out) {
+  if (!p || !out) return DEM_ERR_INVALID_ARG;
+  Oracle* o = new Oracle();
+  o->prm = *p;
+  *out = o;
+  return DEM_OK;
+}
+int oracle_destroy(void* h) {
+  delete (Oracle*)h;
+  return DEM_OK;
+}
+int oracle_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+int oracle_set_particles(void* h, const dem_particles* p) {
+  Oracle& o = *(Oracle*)h;
+  size_t n = p->n;
+  o.n = n;
+  auto cp = [n](std::vector<double>& v, const double* s, double dflt) {
+    v.assign(n, dflt);
+    if (s) std::memcpy(v.data(), s, n * sizeof(double));
+  };
+  cp(o.rx, p->rx, 0); cp(o.ry, p->ry, 0); cp(o.rz, p->rz, 0);
+  cp(o.vx, p->vx, 0); cp(o.vy, p->vy, 0); cp(o.vz, p->vz, 0);
+  cp(o.fx, p->fx, 0); cp(o.fy, p->fy, 0); cp(o.fz, p->fz, 0);
+  cp(o.wx, p->vrotx, 0); cp(o.wy, p->vroty, 0); cp(o.wz, p->vrotz, 0);
+  cp(o.ax, p->arotx, 0); cp(o.ay, p->aroty, 0); cp(o.az, p->arotz, 0);
+  cp(o.mx, p->momx, 0); cp(o.my, p->momy, 0); cp(o.mz, p->momz, 0);
+  cp(o.qw, p->qw, 1); cp(o.qx, p->qx, 0); cp(o.qy, p->qy, 0); cp(o.qz, p->qz, 0);
+  cp(o.ix, p->inertiax, 1); cp(o.iy, p->inertiay, 1); cp(o.iz, p->inertiaz, 1);
+  cp(o.mass, p->mass, 1); cp(o.rad, p->radius, 0.5); cp(o.hom, p->homothety, 1);
+  o.id.assign(n, 0);
+  for (size_t i = 0; i < n; i++) o.id[i] = p->id ? p->id[i] : i;
+  o.type.assign(n, 0);
+  o.group.assign(n, 0);
+  if (p->type) std::memcpy(o.type.data(), p->type, n * 4);
+  if (p->group) std::memcpy(o.group.data(), p->group, n * 4);
+  o.bx = o.rx;
+  o.by = o.ry;
+  o.bz = o.rz;
+  o.inter.clear();
+  o.rec.clear();
+  o.own_first.assign(n, -1);
+  o.own_cnt.assign(n, 0);
+  o.rev_off.assign(n + 1, 0);
+  o.rev_idx.clear();
+  return DEM_OK;
+}
+int oracle_get_particles(void* h, dem_particles* p) {
+  Oracle& o = *(Oracle*)h;
+  if (p->n < o.n) return DEM_ERR_INVALID_ARG;
+  auto cp = [&](double* d, const std::vector<double>& v) {
+    if (d) std::memcpy(d, v.data(), o.n * sizeof(double));
+  };
+  cp(p->rx, o.rx); cp(p->ry, o.ry); cp(p->rz, o.rz);
+  cp(p->vx, o.vx); cp(p->vy, o.vy); cp(p->vz, o.vz);
+  cp(p->fx, o.fx); cp(p->fy, o.fy); cp(p->fz, o.fz);
+  cp(p->vrotx, o.wx); cp(p->vroty, o.wy); cp(p->vrotz, o.wz);
+  cp(p->arotx, o.ax); cp(p->aroty, o.ay); cp(p->arotz, o.az);
+  cp(p->momx, o.mx); cp(p->momy, o.my); cp(p->momz, o.mz);
+  cp(p->qw, o.qw); cp(p->qx, o.qx); cp(p->qy, o.qy); cp(p->qz, o.qz);
+  cp(p->inertiax, o.ix); cp(p->inertiay, o.iy); cp(p->inertiaz, o.iz);
+  cp(p->mass, o.mass); cp(p->radius, o.rad); cp(p->homothety, o.hom);
+  if (p->id) std::memcpy(p->id, o.id.data(), o.n * 8);
+  if (p->type) std::memcpy(p->type, o.type.data(), o.n * 4);
+  if (p->group) std::memcpy(p->group, o.group.data(), o.n * 4);
+  p->n = o.n;
+  return DEM_OK;
+}
+int oracle_register_surface(void* h, const dem_surface* s) {
+  Oracle& o = *(Oracle*)h;
+  Driver d{};
+  d.kind = 0;
+  d.s.offset = s->offset;
+  d.s.normal = {s->normal[0], s->normal[1], s->normal[2]};
+  d.s.vel = {s->vel[0], s->vel[1], s->vel[2]};
+  d.s.vrot = {s->vrot[0], s->vrot[1], s->vrot[2]};
+  d.s.center_proj = d.s.offset * d.s.normal;  // Surface::initialize (surface.hpp:138)
+  if (is_null(d.s.vrot) && is_null({s->center[0], s->center[1], s->center[2]}))
+    d.s.center = d.s.offset * d.s.normal;  // YAML default (surface.hpp:74)
+  else
+    d.s.center = {s->center[0], s->center[1], s->center[2]};
+  o.drivers.push_back(d);
+  return DEM_OK;
+}
+int oracle_register_cylinder(void* h, const dem_cylinder* c) {
+  Oracle& o = *(Oracle*)h;
+  Driver d{};
+  d.kind = 1;
+  d.c.radius = c->radius;
+  d.c.axis = {c->axis[0], c->axis[1], c->axis[2]};
+  d.c.center = d.c.axis * V3{c->center[0], c->center[1], c->center[2]};  // Cylinder::initialize
+  d.c.vel = {c->vel[0], c->vel[1], c->vel[2]};
+  d.c.vrot = {c->vrot[0], c->vrot[1], c->vrot[2]};
+  o.drivers.push_back(d);
+  return DEM_OK;
+}
+int oracle_update_neighbors(void* h) { return update_neighbors(*(Oracle*)h); }
+int oracle_displ_over(void* h, int* r) {
+  *r = displ_over(*(Oracle*)h);
+  return DEM_OK;
+}
+int oracle_reset_force_moment(void* h) {
+  reset_force_moment(*(Oracle*)h);
+  return DEM_OK;
+}
+int oracle_gravity_force(void* h) {
+  gravity_force(*(Oracle*)h);
+  return DEM_OK;
+}
+int oracle_contact_sphere(void* h) {
+  contact_all(*(Oracle*)h);
+  return DEM_OK;
+}
+int oracle_force_to_accel(void* h) {
+  force_to_accel(*(Oracle*)h);
+  return DEM_OK;
+}
+int oracle_prolog(void* h) {
+  prolog(*(Oracle*)h);
+  return DEM_OK;
+}
+int oracle_epilog(void* h) {
+  epilog(*(Oracle*)h);
+  return DEM_OK;
+}
+// first_iteration (main-config.msp:55-65)
+int oracle_first_iteration(void* h) {
+  Oracle& o = *(Oracle*)h;
+  int rc = update_neighbors(o);
+  if (rc) return rc;
+  reset_force_moment(o);
+  compute_force(o);
+  return DEM_OK;
+}
+// numerical_scheme_verlet (config_numerical_schemes.msp:6-28)
+int oracle_step(void* h, int nsteps) {
+  Oracle& o = *(Oracle*)h;
+  for (int s = 0; s < nsteps; s++) {
+    prolog(o);
+    if (displ_over(o)) {
+      int rc = update_neighbors(o);
+      if (rc) return rc;
+    }
+    reset_force_moment(o);
+    compute_force(o);
+    force_to_accel(o);
+    epilog(o);
+  }
+  return DEM_OK;
+}
+int oracle_rebuild_count(void* h, uint64_t* out) {
+  *out = ((Oracle*)h)->rebuilds;
+  return DEM_OK;
+}
+int oracle_state(void* h, dem_state* s) {  // ReduceSimulationStateFunctor (simulation_state.hpp:48-56)
+  Oracle& o = *(Oracle*)h;
+  std::memset(s, 0, sizeof(*s));
+  for (size_t i = 0; i < o.n; i++) {
+    const double m = o.mass[i];
+    s->mass += m;
+    s->rotation_energy[0] += 0.5 * o.wx[i] * o.wx[i] * m;
+    s->rotation_energy[1] += 0.5 * o.wy[i] * o.wy[i] * m;
+    s->rotation_energy[2] += 0.5 * o.wz[i] * o.wz[i] * m;
+    s->kinetic_energy[0] += 0.5 * o.vx[i] * o.vx[i] * m;
+    s->kinetic_energy[1] += 0.5 * o.vy[i] * o.vy[i] * m;
+    s->kinetic_energy[2] += 0.5 * o.vz[i] * o.vz[i] * m;
+  }
+  s->n_particles = o.n;
+  s->n_interactions = o.inter.size();
+  s->n_active_interactions = o.n_active;
+  return DEM_OK;
+}
+int oracle_interaction_count(void* h, uint64_t* out) {
+  *out = ((Oracle*)h)->inter.size();
+  return DEM_OK;
+}
+int oracle_get_interactions(void* h, dem_interaction_list* l) {
+  Oracle& o = *(Oracle*)h;
+  l->count = o.inter.size();
+  if (l->capacity < o.inter.size()) return DEM_ERR_INVALID_ARG;
+  for (size_t k = 0; k < o.inter.size(); k++) {
+    const Inter& it = o.inter[k];
+    if (l->owner_id) l->owner_id[k] = it.oid;
+    if (l->partner_id) l->partner_id[k] = it.pid;
+    if (l->type) l->type[k] = it.type;
+    if (l->swap) l->swap[k] = it.swap;
+    if (l->owner_sub) l->owner_sub[k] = it.osub;
+    if (l->partner_sub) l->partner_sub[k] = it.psub;
+    if (l->friction) {
+      l->friction[3 * k] = it.friction.x;
+      l->friction[3 * k + 1] = it.friction.y;
+      l->friction[3 * k + 2] = it.friction.z;
+    }
+    if (l->moment) {
+      l->moment[3 * k] = it.moment.x;
+      l->moment[3 * k + 1] = it.moment.y;
+      l->moment[3 * k + 2] = it.moment.z;
+    }
+  }
+  return DEM_OK;
+}
+int oracle_packing_profile(void* h, int nslabs, double zlo, double zhi, double* out) {
+  Oracle& o = *(Oracle*)h;
+  if (nslabs <= 0 || !(zhi > zlo)) return DEM_ERR_INVALID_ARG;
+  const double dz = (zhi - zlo) / nslabs;
+  const double area = L(o, 0) * L(o, 1);
+  std::vector<double> vol(nslabs, 0.0);
+  for (size_t i = 0; i < o.n; i++) {
+    const double zc = o.rz[i], r = o.rad[i];
+    int a = (int)std::floor((zc - r - zlo) / dz), b = (int)std::floor((zc + r - zlo) / dz);
+    a = std::max(a, 0);
+    b = std::min(b, nslabs - 1);
+    for (int s = a; s <= b; s++) vol[s] += sphere_slab_volume(zc, r, zlo + s * dz, zlo + (s + 1) * dz);
+  }
+  for (int s = 0; s < nslabs; s++) out[s] = vol[s] / (area * dz);
+  return DEM_OK;
+}
+const char* oracle_last_error(void* h) { return ((Oracle*)h)->err.c_str(); }
+}

@@ -1,0 +1,84 @@
+"""Python loader of the CPU oracle (test infrastructure only).
+
+Only tests, the smoke check and the CPU-baseline leg of the benchmark use it,
+as the checker.  It exposes the oracle's C functions through the same method
+table as the native library, so ``exadem_gb300.system.System`` drives either
+one with identical calls.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from exadem_gb300 import _abi as A
+from exadem_gb300.system import System
+
+from . import build as _build
+
+_LIB = None
+_CTX = C.c_void_p
+
+
+def load(rebuild: bool = True):
+    global _LIB
+    if _LIB is None:
+        path = _build.build() if rebuild else _build.LIB
+        lib = C.CDLL(str(path))
+        sig = lambda n, a, r=C.c_int: (setattr(getattr(lib, n), "argtypes", a), setattr(getattr(lib, n), "restype", r))
+        sig("oracle_create", [C.POINTER(A.Params), C.POINTER(_CTX)])
+        sig("oracle_destroy", [_CTX])
+        sig("oracle_set_threads", [C.c_int])
+        sig("oracle_last_error", [_CTX], C.c_char_p)
+        sig("oracle_set_particles", [_CTX, C.POINTER(A.Particles)])
+        sig("oracle_get_particles", [_CTX, C.POINTER(A.Particles)])
+        sig("oracle_register_surface", [_CTX, C.POINTER(A.Surface)])
+        sig("oracle_register_cylinder", [_CTX, C.POINTER(A.Cylinder)])
+        sig("oracle_displ_over", [_CTX, C.POINTER(C.c_int)])
+        for n in ["oracle_update_neighbors", "oracle_reset_force_moment", "oracle_gravity_force",
+                  "oracle_contact_sphere", "oracle_force_to_accel", "oracle_prolog", "oracle_epilog",
+                  "oracle_first_iteration"]:
+            sig(n, [_CTX])
+        sig("oracle_step", [_CTX, C.c_int])
+        sig("oracle_rebuild_count", [_CTX, A.PU64])
+        sig("oracle_state", [_CTX, C.POINTER(A.State)])
+        sig("oracle_interaction_count", [_CTX, A.PU64])
+        sig("oracle_get_interactions", [_CTX, C.POINTER(A.InteractionList)])
+        sig("oracle_packing_profile", [_CTX, C.c_int, C.c_double, C.c_double, A.PD])
+        _LIB = lib
+    return _LIB
+
+
+class OracleBackend:
+    _MAP = {"ctx_create": "oracle_create", "ctx_destroy": "oracle_destroy", "last_error": "oracle_last_error",
+            "register_surface": "oracle_register_surface", "register_cylinder": "oracle_register_cylinder",
+            "update_particle_neighbors": "oracle_update_neighbors", "particle_displ_over": "oracle_displ_over",
+            "reset_force_moment": "oracle_reset_force_moment", "gravity_force": "oracle_gravity_force",
+            "contact_sphere": "oracle_contact_sphere", "force_to_accel": "oracle_force_to_accel",
+            "combined_compute_prolog": "oracle_prolog", "combined_compute_epilog": "oracle_epilog",
+            "first_iteration": "oracle_first_iteration", "step": "oracle_step",
+            "rebuild_count": "oracle_rebuild_count", "simulation_state": "oracle_state",
+            "interaction_count": "oracle_interaction_count", "get_interactions": "oracle_get_interactions",
+            "packing_profile": "oracle_packing_profile"}
+
+    def __init__(self):
+        self.lib = load()
+
+    def set_particles(self, h, st, on_device=0):
+        return self.lib.oracle_set_particles(h, st)
+
+    def get_particles(self, h, st, on_device=0):
+        return self.lib.oracle_get_particles(h, st)
+
+    def set_params(self, h, p):
+        return 4  # DEM_ERR_UNSUPPORTED: the oracle takes its parameters at creation only
+
+    def __getattr__(self, name):
+        return getattr(self.lib, self._MAP[name])
+
+
+def set_threads(n: int) -> int:
+    return load().oracle_set_threads(int(n))
+
+
+def oracle_system(params: A.Params) -> System:
+    return System(params, backend=OracleBackend())
