@@ -19,22 +19,31 @@ struct Rng {
   double uniform(double a, double b) { return a + (b - a) * u01(); }
 };
 
+// Cells of at least `cell` per axis; on periodic axes the cells tile the
+// period exactly (floor(L/cell) cells of width L/dims) so the +-1 stencil with
+// wrap-around sees every neighbour across the boundary.
 struct HashGrid {
-  double lo[3], cs;
+  double lo[3], cs[3];
   int dims[3];
   std::vector<int64_t> head;
   std::vector<int64_t> next;
-  void init(const double* l, const double* h, double cell, uint64_t n) {
-    cs = cell;
+  void init(const double* l, const double* h, double cell, const int32_t* periodic, uint64_t n) {
     for (int d = 0; d < 3; d++) {
       lo[d] = l[d];
-      dims[d] = std::max(1, (int)std::ceil((h[d] - l[d]) / cs));
+      const double Ld = h[d] - l[d];
+      if (periodic[d]) {
+        dims[d] = std::max(1, (int)std::floor(Ld / cell));
+        cs[d] = Ld / dims[d];
+      } else {
+        dims[d] = std::max(1, (int)std::ceil(Ld / cell));
+        cs[d] = cell;
+      }
     }
     head.assign((size_t)dims[0] * dims[1] * dims[2], -1);
     next.assign(n, -1);
   }
   int coord(int d, double x) const {
-    int k = (int)std::floor((x - lo[d]) / cs);
+    int k = (int)std::floor((x - lo[d]) / cs[d]);
     return std::min(std::max(k, 0), dims[d] - 1);
   }
   size_t idx(int x, int y, int z) const { return (size_t)x + (size_t)dims[0] * ((size_t)y + (size_t)dims[1] * z); }
@@ -55,7 +64,7 @@ extern "C" int dem_generate_rsa_spheres(const dem_rsa_spec* sp, dem_particles* o
   double ghi[3] = {hi[0], hi[1], hi[2]};
   if (ga >= 0) ghi[ga] = hi[ga] + 8.0 * (hi[ga] - lo[ga]) + 16 * sp->rmax;
   HashGrid grid;
-  grid.init(lo, ghi, 2.0 * sp->rmax, n);
+  grid.init(lo, ghi, 2.0 * sp->rmax, sp->periodic, n);
   std::vector<double> x(n), y(n), z(n), r(n);
   const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
   const uint64_t max_att = sp->max_attempts ? sp->max_attempts : 64;
@@ -81,29 +90,31 @@ extern "C" int dem_generate_rsa_spheres(const dem_rsa_spec* sp, dem_particles* o
       }
       bool ok = ok_region;
       if (ok) {
-        int c[3];
-        for (int d = 0; d < 3; d++) c[d] = grid.coord(d, p[d]);
-        for (int dz = -1; dz <= 1 && ok; dz++)
-          for (int dy = -1; dy <= 1 && ok; dy++)
-            for (int dx = -1; dx <= 1 && ok; dx++) {
-              int q[3] = {c[0] + dx, c[1] + dy, c[2] + dz};
-              bool skip = false;
-              for (int d = 0; d < 3; d++) {
-                if (q[d] < 0 || q[d] >= grid.dims[d]) {
-                  if (!sp->periodic[d]) {
-                    skip = true;
-                    break;
-                  }
-                  q[d] = (q[d] + grid.dims[d]) % grid.dims[d];
-                }
-              }
-              if (skip) continue;
-              for (int64_t j = grid.head[grid.idx(q[0], q[1], q[2])]; j >= 0; j = grid.next[j]) {
+        // per axis: the distinct cells within +-1 (wrapped on periodic axes)
+        int cand[3][3], nc[3];
+        for (int d = 0; d < 3; d++) {
+          const int c = grid.coord(d, p[d]);
+          nc[d] = 0;
+          for (int o = -1; o <= 1; o++) {
+            int q = c + o;
+            if (q < 0 || q >= grid.dims[d]) {
+              if (!sp->periodic[d]) continue;
+              q = (q + grid.dims[d]) % grid.dims[d];
+            }
+            bool dup = false;
+            for (int m = 0; m < nc[d]; m++) dup |= cand[d][m] == q;
+            if (!dup) cand[d][nc[d]++] = q;
+          }
+        }
+        for (int a = 0; a < nc[2] && ok; a++)
+          for (int b = 0; b < nc[1] && ok; b++)
+            for (int e = 0; e < nc[0] && ok; e++) {
+              for (int64_t j = grid.head[grid.idx(cand[0][e], cand[1][b], cand[2][a])]; j >= 0; j = grid.next[j]) {
                 double dd[3] = {p[0] - x[j], p[1] - y[j], p[2] - z[j]};
                 for (int d = 0; d < 3; d++)
                   if (sp->periodic[d]) dd[d] -= L[d] * std::round(dd[d] / L[d]);
-                const double s = rk + r[j];
-                if (dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2] < s * s) {
+                const double sr = rk + r[j];
+                if (dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2] < sr * sr) {
                   ok = false;
                   break;
                 }
