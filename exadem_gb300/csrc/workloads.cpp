@@ -62,7 +62,14 @@ extern "C" int dem_generate_rsa_spheres(const dem_rsa_spec* sp, dem_particles* o
   const int ga = sp->grow_axis;
   // grid big enough for generous growth along the grow axis
   double ghi[3] = {hi[0], hi[1], hi[2]};
-  if (ga >= 0) ghi[ga] = hi[ga] + 8.0 * (hi[ga] - lo[ga]) + 16 * sp->rmax;
+  if (ga >= 0) {
+    // room for a column at a solid fraction down to 0.05 (the moving-window RSA reaches ~0.29)
+    double area = 1.0;
+    for (int d = 0; d < 3; d++)
+      if (d != ga) area *= hi[d] - lo[d];
+    const double vmax = 4.0 / 3.0 * 3.14159265358979 * sp->rmax * sp->rmax * sp->rmax;
+    ghi[ga] = hi[ga] + (double)n * vmax / (0.05 * area) + 16 * sp->rmax;
+  }
   HashGrid grid;
   grid.init(lo, ghi, 2.0 * sp->rmax, sp->periodic, n);
   std::vector<double> x(n), y(n), z(n), r(n);
