@@ -144,6 +144,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_profile", [_CTX, C.c_int])
     _sig(lib, "dem_kernel_stats", [_CTX, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)])
     _sig(lib, "dem_reset_kernel_stats", [_CTX])
+    _sig(lib, "dem_simulation_state_noalloc", [C.POINTER(Particles), PD, C.c_void_p])
 
 
 # Symbols declared in include/dem_hotpath.h and include/dem_workloads.h.
@@ -153,7 +154,8 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_gravity_force", "dem_contact_sphere", "dem_force_to_accel", "dem_combined_compute_prolog",
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
             "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
-            "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats"]
+            "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
+            "dem_simulation_state_noalloc"]
 
 _LIB = None
 

@@ -241,6 +241,24 @@ int dem_profile(dem_ctx* ctx, int enable);
 int dem_kernel_stats(dem_ctx* ctx, dem_kernel_stat* out, int capacity, int* count);
 int dem_reset_kernel_stats(dem_ctx* ctx);
 
+/* ---- state reduction without any device allocation ---------------------
+ * No counterpart in the reference.  For callers that may not call cudaMalloc
+ * (their device memory is owned by another allocator, or they must not pay
+ * the implicit synchronisation of cudaMalloc/cudaFree): the same sums as
+ * dem_simulation_state, over particle arrays already on the device.  The only
+ * scratch is a file-scope device array sized for
+ * DEM_STATE_NOALLOC_MAX_PARTICLES particles (448 KiB, held by every GPU that
+ * loads the library until exit); larger n returns DEM_ERR_INVALID_ARG.
+ *   dev:     device pointers vx, vy, vz, vrotx, vroty, vrotz, mass and n
+ *            (other fields unused);
+ *   dev_out: device array of 7 doubles, written in the order
+ *            kinetic_energy x,y,z, rotation_energy x,y,z, mass;
+ *   stream:  cudaStream_t (NULL = legacy default stream); asynchronous.
+ * The first call on a device looks up the scratch address (make it before any
+ * stream capture).  Calls share the scratch: calls that overlap on the GPU race. */
+#define DEM_STATE_NOALLOC_MAX_PARTICLES 16777216ull
+int dem_simulation_state_noalloc(const dem_particles* dev, double* dev_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
