@@ -148,7 +148,8 @@ def allsum(dist, x: float) -> float:
 def workload(args):
     from exadem_gb300 import workloads as W
 
-    return W.spheres_floor(n=args.n, fp32_contact_screen=0 if args.plain else 1)
+    opt = 0 if args.plain else 1
+    return W.spheres_floor(n=args.n, fp32_contact_screen=opt, fused_step=opt)
 
 
 def cpu_baseline(w, budget_s: float = 20.0):
@@ -271,7 +272,9 @@ def run_native(args, rank, world, local, dist):
         "config": {"workload": "spheres_floor: 2M polydisperse spheres r~U[0.4,0.6], periodic x/y, floor wall, "
                                "Hooke+cohesion(kc=1e3,dncut=0.01)+kr=100, dt=5e-4" if args.n == 2_000_000 else
                    f"spheres_floor n={args.n}",
-                   "n_particles": w.n, "path": "plain" if args.plain else "fp32-screen",
+                   "n_particles": w.n,
+                   "path": "plain FP64 operator kernels" if args.plain else
+                           "fused step, FP32 contact screen, compacted FP64 contact law, exact fast division",
                    "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "phi_achieved": round(w.info["phi_achieved"], 4)},

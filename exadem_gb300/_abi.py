@@ -45,7 +45,7 @@ class Params(C.Structure):
                 ("symetric", C.c_int32), ("law", C.c_int32),
                 ("config", ContactParams), ("config_driver", ContactParams),
                 ("fp32_broad_phase", C.c_int32), ("fp32_contact_screen", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("fused_step", C.c_int32), ("reserved", C.c_int32 * 5)]
 
 
 PARTICLE_FIELDS = ["rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz",
@@ -145,6 +145,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_kernel_stats", [_CTX, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)])
     _sig(lib, "dem_reset_kernel_stats", [_CTX])
     _sig(lib, "dem_simulation_state_noalloc", [C.POINTER(Particles), PD, C.c_void_p])
+    _sig(lib, "dem_selftest_division", [C.c_uint64, C.c_uint64, PU64, PU64])
 
 
 # Symbols declared in include/dem_hotpath.h and include/dem_workloads.h.
@@ -155,7 +156,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
             "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
-            "dem_simulation_state_noalloc"]
+            "dem_simulation_state_noalloc", "dem_selftest_division"]
 
 _LIB = None
 

@@ -109,6 +109,16 @@ int alloc_iarrays(dem_ctx* c, int b, uint64_t need) {
   return DEM_OK;
 }
 
+void free_compact(dem_ctx* c) {
+  cudaFree(c->L1);
+  cudaFree(c->L2);
+  c->L1 = c->L2 = nullptr;
+  for (int q = 0; q < 7; q++) {
+    cudaFree(c->Dscr[q]);
+    c->Dscr[q] = nullptr;
+  }
+}
+
 int alloc_records(dem_ctx* c, uint64_t need) {
   if (need <= c->rcap && c->rev_idx) return DEM_OK;
   for (int d = 0; d < 3; d++) {
@@ -119,6 +129,7 @@ int alloc_records(dem_ctx* c, uint64_t need) {
   c->R = Records{};
   cudaFree(c->rev_idx);
   c->rev_idx = nullptr;
+  free_compact(c);
   c->rcap = 0;
   const uint64_t cap = need + need / 4 + 4096;
   for (int d = 0; d < 3; d++) {
@@ -127,6 +138,9 @@ int alloc_records(dem_ctx* c, uint64_t need) {
     DEM_CUDA_TRY(c, cudaMalloc(&c->R.tj[d], cap * 8));
   }
   DEM_CUDA_TRY(c, cudaMalloc(&c->rev_idx, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->L1, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->L2, cap * 4));
+  for (int q = 0; q < 7; q++) DEM_CUDA_TRY(c, cudaMalloc(&c->Dscr[q], cap * 8));
   c->rcap = cap;
   return DEM_OK;
 }
@@ -209,6 +223,14 @@ int need_list(dem_ctx* c) {
   return DEM_OK;
 }
 
+// Copies device scalar idx to the pinned host mirror and waits.
+int read_flag(dem_ctx* c, int idx) {
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->h_scalars + idx, c->d_scalars + idx, sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return DEM_OK;
+}
+
 int copy_field(dem_ctx* c, double* dst, const double* src, uint64_t n, cudaMemcpyKind k) {
   if (!dst || !src || !n) return DEM_OK;
   DEM_CUDA_TRY(c, cudaMemcpyAsync(dst, src, n * sizeof(double), k, c->stream));
@@ -269,6 +291,7 @@ int dem_ctx_destroy(dem_ctx* c) {
     cudaFree(c->R.tj[d]);
   }
   cudaFree(c->rev_idx);
+  free_compact(c);
   cudaFree(c->rev_off);
   cudaFree(c->rev_cnt);
   cudaFree(c->cell_cnt);
@@ -326,10 +349,11 @@ int dem_set_particles(dem_ctx* c, const dem_particles* p, int on_device) {
   const double* src[NPF] = {p->rx, p->ry, p->rz, p->vx, p->vy, p->vz, p->fx, p->fy, p->fz, p->vrotx, p->vroty,
                             p->vrotz, p->arotx, p->aroty, p->arotz, p->momx, p->momy, p->momz, p->qw, p->qx,
                             p->qy, p->qz, p->inertiax, p->inertiay, p->inertiaz, p->mass, p->radius, p->homothety,
-                            p->rx, p->ry, p->rz};
+                            nullptr, nullptr, nullptr, nullptr, p->rx, p->ry, p->rz};
   // defaults for absent fields: 0, except orientation w, inertia, mass and homothety = 1
   std::vector<double> ones(n ? n : 1, 1.0);
   for (int f = 0; f < NPF; f++) {
+    if (f >= IMASS && f <= IIZ) continue;  // derived below
     if (src[f]) {
       if ((rc = copy_field(c, P.f[f], src[f], n, k))) return rc;
     } else if (f == QW || f == IX || f == IY || f == IZ || f == MASS || f == HOM) {
@@ -356,6 +380,7 @@ int dem_set_particles(dem_ctx* c, const dem_particles* p, int on_device) {
   } else if (n) {
     DEM_CUDA_TRY(c, cudaMemsetAsync(P.group, 0, n * 4, c->stream));
   }
+  if ((rc = launch_reciprocals(c, n))) return rc;
   // r_max for nbh_dist (dem_rcut_max.cpp:49-66)
   std::vector<double> rad(n);
   if (n) {
@@ -379,12 +404,12 @@ int dem_get_particles(dem_ctx* c, dem_particles* out, int on_device) {
   const uint64_t n = c->n;
   const PArrays& P = c->P[c->pcur];
   const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  double* dst[BX] = {out->rx, out->ry, out->rz, out->vx, out->vy, out->vz, out->fx, out->fy, out->fz,
+  double* dst[NUSER] = {out->rx, out->ry, out->rz, out->vx, out->vy, out->vz, out->fx, out->fy, out->fz,
                      out->vrotx, out->vroty, out->vrotz, out->arotx, out->aroty, out->arotz, out->momx,
                      out->momy, out->momz, out->qw, out->qx, out->qy, out->qz, out->inertiax, out->inertiay,
                      out->inertiaz, out->mass, out->radius, out->homothety};
   int rc;
-  for (int f = 0; f < BX; f++)
+  for (int f = 0; f < NUSER; f++)
     if ((rc = copy_field(c, dst[f], P.f[f], n, k))) return rc;
   if (out->id && n) DEM_CUDA_TRY(c, cudaMemcpyAsync(out->id, P.id, n * 8, k, c->stream));
   if (out->type && n) DEM_CUDA_TRY(c, cudaMemcpyAsync(out->type, P.type, n * 4, k, c->stream));
@@ -504,6 +529,15 @@ int dem_step(dem_ctx* c, int nsteps) {
   int rc = need_list(c);
   if (rc) return rc;
   for (int s = 0; s < nsteps; s++) {
+    if (c->prm.fused_step) {
+      // prolog + trigger; rebuild if needed; three-pass contact; gather + f2a + epilog
+      if ((rc = launch_fused_prolog(c))) return rc;
+      if ((rc = read_flag(c, 0))) return rc;
+      if (c->h_scalars[0] && (rc = update_neighbors(c))) return rc;
+      if ((rc = launch_contact_compact(c))) return rc;
+      if ((rc = launch_fused_epilog(c))) return rc;
+      continue;
+    }
     if ((rc = launch_prolog(c))) return rc;
     int over = 0;
     if ((rc = dem_particle_displ_over(c, &over))) return rc;

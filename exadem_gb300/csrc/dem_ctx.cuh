@@ -57,6 +57,10 @@ struct dem_ctx {
   uint32_t* rev_off = nullptr;  // n+1
   uint32_t* rev_cnt = nullptr;  // n+1
   uint32_t* rev_idx = nullptr;  // rcap
+  // compacted contact passes (rcap each): work lists and detection results
+  uint32_t* L1 = nullptr;
+  uint32_t* L2 = nullptr;
+  double* Dscr[7] = {};
 
   // scan scratch
   uint32_t* scan_blk = nullptr;
@@ -133,6 +137,11 @@ int launch_epilog(dem_ctx* c);
 int launch_displ_over(dem_ctx* c);
 int launch_state(dem_ctx* c, dem_state* out);
 int launch_profile(dem_ctx* c, int nslabs, double zlo, double zhi, double* out);
+int launch_reciprocals(dem_ctx* c, uint64_t n);  // on P[0] after an upload
+// k_step_fused.cu
+int launch_fused_prolog(dem_ctx* c);
+int launch_contact_compact(dem_ctx* c);
+int launch_fused_epilog(dem_ctx* c);
 }  // namespace dem
 
 inline unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }

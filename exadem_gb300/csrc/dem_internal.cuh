@@ -1,7 +1,7 @@
 // dem_internal.cuh -- device data layout and shared helpers of the GB300 DEM hot path.
 //
 // Layout in HBM (all structure-of-arrays):
-//   particles: 31 FP64 fields + id (u64) + type/group (u32), double-buffered so
+//   particles: 35 FP64 fields + id (u64) + type/group (u32), double-buffered so
 //              the cell reorder at a rebuild is a gather from one copy into the other;
 //   interactions: sorted by owner slot, and by InteractionPair key inside one
 //              owner; keys (partner slot, partner id, meta), history (6 FP64)
@@ -29,9 +29,11 @@ enum PField : int {
   QW, QX, QY, QZ,
   IX, IY, IZ,   // inertia
   MASS, RAD, HOM,
+  IMASS, IIX, IIY, IIZ,  // RN(1/mass), RN(1/inertia): exact divisions by Markstein's step
   BX, BY, BZ,   // backup positions for the displacement trigger
   NPF
 };
+constexpr int NUSER = HOM + 1;  // fields exchanged with the caller (rx .. homothety)
 
 struct PArrays {
   double* f[NPF];

@@ -11,22 +11,10 @@
 //   simulation_state     src/io/include/exaDEM/simulation_state.hpp:48-56 (deterministic tree sum)
 // Quaternion arithmetic restates onika's Quaternion operators following exaDEM's
 // quat type (src/shape/include/exaDEM/type/quat.hpp:79-96,233-242).
-#include "dem_ctx.cuh"
+#include "integrate_core.cuh"
 
 namespace dem {
 namespace {
-
-struct Q4 {
-  double w, x, y, z;
-};
-__device__ inline V3 qrotate(Q4 q, V3 v) {
-  const V3 qv = mk(q.x, q.y, q.z);
-  V3 uv = cross(qv, v);
-  V3 uuv = cross(qv, uv);
-  uv = uv * (2.0 * q.w);
-  uuv = uuv * 2.0;
-  return v + uv + uuv;
-}
 
 __global__ void k_reset(PArrays P, uint64_t n) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -60,60 +48,15 @@ __global__ void k_force_to_accel(PArrays P, uint64_t n) {
 __global__ void k_prolog(PArrays P, uint64_t n, double delta_t, double half_delta_t, double delta_t2_2) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const double v = P.f[VX + d][s], a = P.f[FX + d][s];
-    P.f[RX + d][s] = P.f[RX + d][s] + (v * delta_t + a * delta_t2_2);
-    P.f[VX + d][s] = v + a * half_delta_t;
-  }
-  Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
-  const V3 om = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
-  Q4 d;
-  d.x = 0.5 * (om.y * Q.z - om.z * Q.y + om.x * Q.w);
-  d.y = 0.5 * (om.z * Q.x - om.x * Q.z + om.y * Q.w);
-  d.z = 0.5 * (om.x * Q.y - om.y * Q.x + om.z * Q.w);
-  d.w = -0.5 * (om.x * Q.x + om.y * Q.y + om.z * Q.z);
-  Q.w = Q.w + d.w * delta_t;
-  Q.x = Q.x + d.x * delta_t;
-  Q.y = Q.y + d.y * delta_t;
-  Q.z = Q.z + d.z * delta_t;
-  const double norm2 = Q.w * Q.w + (Q.x * Q.x + Q.y * Q.y + Q.z * Q.z);
-  if (norm2 <= 1e-9) {
-    Q = {1.0, 0.0, 0.0, 0.0};
-  } else {
-    const double inv = 1.0 / sqrt(norm2);
-    Q = {Q.w * inv, Q.x * inv, Q.y * inv, Q.z * inv};
-  }
-  P.f[QW][s] = Q.w;
-  P.f[QX][s] = Q.x;
-  P.f[QY][s] = Q.y;
-  P.f[QZ][s] = Q.z;
-  P.f[WX][s] = om.x + half_delta_t * P.f[AX][s];
-  P.f[WY][s] = om.y + half_delta_t * P.f[AY][s];
-  P.f[WZ][s] = om.z + half_delta_t * P.f[AZ][s];
+  prolog_one(P, s, delta_t, half_delta_t, delta_t2_2);
 }
 
 __global__ void k_epilog(PArrays P, uint64_t n, double half_delta_t) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  const Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
-  const Q4 Qinv = {Q.w, -Q.x, -Q.y, -Q.z};
-  const V3 vrot = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+  const V3 a = mk(P.f[FX][s], P.f[FY][s], P.f[FZ][s]);
   const V3 mom = mk(P.f[MX][s], P.f[MY][s], P.f[MZ][s]);
-  const V3 I = mk(P.f[IX][s], P.f[IY][s], P.f[IZ][s]);
-  const V3 omega = qrotate(Qinv, vrot);
-  const V3 M = qrotate(Qinv, mom);
-  const V3 domega = mk((M.x - (I.z - I.y) * omega.y * omega.z) / I.x, (M.y - (I.x - I.z) * omega.z * omega.x) / I.y,
-                       (M.z - (I.y - I.x) * omega.x * omega.y) / I.z);
-  const V3 arot = qrotate(Q, domega);
-  P.f[AX][s] = arot.x;
-  P.f[AY][s] = arot.y;
-  P.f[AZ][s] = arot.z;
-  P.f[WX][s] = vrot.x + arot.x * half_delta_t;
-  P.f[WY][s] = vrot.y + arot.y * half_delta_t;
-  P.f[WZ][s] = vrot.z + arot.z * half_delta_t;
-#pragma unroll
-  for (int d = 0; d < 3; d++) P.f[VX + d][s] = P.f[VX + d][s] + P.f[FX + d][s] * half_delta_t;
+  epilog_one<false>(P, s, half_delta_t, a, mom);
 }
 
 __global__ void k_displ(PArrays P, uint64_t n, double thr2, unsigned long long* flag) {
@@ -176,7 +119,21 @@ __global__ void k_profile(PArrays P, uint64_t n, int nslabs, double zlo, double 
     atomicAdd(&vol[k], M_PI * (Fh - Fl));
   }
 }
+__global__ void k_reciprocals(PArrays P, uint64_t n) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  P.f[IMASS][s] = 1.0 / P.f[MASS][s];
+  P.f[IIX][s] = 1.0 / P.f[IX][s];
+  P.f[IIY][s] = 1.0 / P.f[IY][s];
+  P.f[IIZ][s] = 1.0 / P.f[IZ][s];
+}
 }  // namespace
+
+int launch_reciprocals(dem_ctx* c, uint64_t n) {
+  if (n) k_reciprocals<<<grid_for(n, 256), 256, 0, c->stream>>>(c->P[0], n);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
 
 int launch_reset_force_moment(dem_ctx* c) {
   ProfScope ps(c, K_RESET, c->n ? 1 : 0);

@@ -1,0 +1,341 @@
+// k_step_fused.cu -- the optimised Verlet step: fewer launches, dense FP64 warps.
+//
+// FP64 on GB300 runs at 2 thread-instructions per clock per SM (1/64 of FP32),
+// so the step is bound by the FP64 pipe, not by HBM.  Two consequences drive
+// this file, and neither changes a single result bit:
+//  * lanes that need no FP64 work must not share a warp with lanes that do:
+//    a warp instruction with one active lane costs the FP64 pipe as much as a
+//    full one.  The contact law therefore runs in three passes:
+//      k_cscreen  one thread per interaction; an FP32 test proves most pairs
+//                 apart (history reset, zero record, no FP64 at all); the others
+//                 are appended to list L1 with warp-aggregated atomics;
+//      k_cdetect  dense over L1: FP64 detection; no contact -> reset; cohesive
+//                 attraction without overlap (cheap branch) finished here;
+//                 overlapping pairs append (k, dn, n, cp) to list L2;
+//      k_chooke   dense over L2: the full Hooke law with friction and rolling.
+//  * the divisions by mass and inertia use exact reciprocal-based division
+//    (math_exact.cuh) and reset + gravity + gather + force_to_accel + epilog
+//    are one kernel, prolog + displacement trigger another.
+// Order of summation, operation order and rounding are those of the operator
+// kernels (contact_core.cuh, integrate_core.cuh).
+#include "contact_core.cuh"
+#include "integrate_core.cuh"
+
+namespace dem {
+namespace {
+
+constexpr int FT = 128;  // threads per block
+
+// All 32 lanes must call it.  Returns the slot of this lane when want is set.
+__device__ __forceinline__ uint32_t warp_append(bool want, unsigned long long* counter) {
+  const unsigned mask = __ballot_sync(0xffffffffu, want);
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+  }
+  return (uint32_t)base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+struct CArgs {
+  PArrays P;
+  IArrays I;
+  Records R;
+  uint64_t ni;
+  GridDev g;
+  const DriverDev* drv;
+  dem_contact_params cp, cpd;
+  double dt;
+  int cohesive;
+  int screen;
+  uint32_t* L1;
+  uint32_t* L2;
+  double* D[7];  // dn, n(3), cp(3) of the L2 entries
+  unsigned long long* cnt;  // [0] L1 count, [1] L2 count
+  unsigned long long* n_active;
+};
+
+__device__ __forceinline__ void write_result(const CArgs& a, uint64_t k, V3 ft, V3 mo, V3 f, V3 ti, V3 tj) {
+  a.I.ft[0][k] = ft.x;
+  a.I.ft[1][k] = ft.y;
+  a.I.ft[2][k] = ft.z;
+  a.I.mo[0][k] = mo.x;
+  a.I.mo[1][k] = mo.y;
+  a.I.mo[2][k] = mo.z;
+  a.R.f[0][k] = f.x;
+  a.R.f[1][k] = f.y;
+  a.R.f[2][k] = f.z;
+  a.R.ti[0][k] = ti.x;
+  a.R.ti[1][k] = ti.y;
+  a.R.ti[2][k] = ti.z;
+  a.R.tj[0][k] = tj.x;
+  a.R.tj[1][k] = tj.y;
+  a.R.tj[2][k] = tj.z;
+}
+
+__device__ __forceinline__ V3 partner_pos(const CArgs& a, uint32_t meta, uint32_t j) {
+  V3 rj = ldv(a.P, RX, j);
+  const int sx = meta_shift(meta, 0), sy = meta_shift(meta, 1), sz = meta_shift(meta, 2);
+  if (sx) rj.x = rj.x + (double)sx * a.g.L[0];
+  if (sy) rj.y = rj.y + (double)sy * a.g.L[1];
+  if (sz) rj.z = rj.z + (double)sz * a.g.L[2];
+  return rj;
+}
+
+__global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
+  const uint64_t k = (uint64_t)blockIdx.x * FT + threadIdx.x;
+  bool want = false;
+  if (k < a.ni) {
+    const uint32_t meta = a.I.meta[k];
+    want = true;
+    if (a.screen && meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
+      const uint32_t i = a.I.owner[k], j = a.I.partner[k];
+      const V3 ri = ldv(a.P, RX, i);
+      const V3 rj = partner_pos(a, meta, j);
+      const double rad_i = a.P.f[RAD][i], rad_j = a.P.f[RAD][j];
+      // same proof of separation as the one-pass kernel (k_contact_sphere.cu)
+      const float ex = (float)(ri.x - rj.x), ey = (float)(ri.y - rj.y), ez = (float)(ri.z - rj.z);
+      const float d2f = ex * ex + ey * ey + ez * ez;
+      const double lim = rad_i + rad_j + (a.cohesive ? fmax(a.cp.dncut, 0.0) : 0.0);
+      const float limf = (float)lim;
+      if (lim > 1e-15 && lim < 1e15 && d2f > limf * limf * 1.0000039f) {
+        want = false;
+        const V3 z = mk(0, 0, 0);
+        write_result(a, k, z, z, z, z, z);
+      }
+    }
+  }
+  const uint32_t pos = warp_append(want, a.cnt);
+  if (want) a.L1[pos] = (uint32_t)k;
+}
+
+__global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
+  const uint64_t n1 = a.cnt[0];
+  const uint64_t stride = (uint64_t)gridDim.x * FT;
+  for (uint64_t base = (uint64_t)blockIdx.x * FT; base < n1; base += stride) {
+    const uint64_t w = base + threadIdx.x;
+    bool heavy = false;
+    uint32_t k = 0;
+    double dn = 0;
+    V3 n = mk(0, 0, 0), cpos = mk(0, 0, 0);
+    if (w < n1) {
+      k = a.L1[w];
+      const uint32_t meta = a.I.meta[k];
+      const uint32_t i = a.I.owner[k], j = a.I.partner[k];
+      const V3 ri = ldv(a.P, RX, i);
+      const double rad_i = a.P.f[RAD][i];
+      bool contact;
+      bool is_vv = meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX;
+      V3 rj = mk(0, 0, 0);
+      double dncut;
+      if (is_vv) {
+        rj = partner_pos(a, meta, j);
+        const double rad_j = a.P.f[RAD][j];
+        const double R = rad_i + rad_j;
+        const V3 dist = ri - rj;
+        const double dist_norm = vnorm(dist);
+        const double inv_dist_norm = 1.0 / dist_norm;
+        dn = dist_norm - R;
+        n = dist * inv_dist_norm;
+        cpos = ri - n * (rad_i + 0.5 * dn);
+        contact = dn < 0;
+        dncut = a.cp.dncut;
+      } else {
+        const DriverDev& d = a.drv[j];
+        if (d.kind == 0) {
+          const V3 nrm = mk(d.normal[0], d.normal[1], d.normal[2]);
+          const V3 proj = dot(ri, nrm) * nrm;
+          const V3 s2p = -(mk(d.center_proj[0], d.center_proj[1], d.center_proj[2]) - proj);
+          const double dd = vnorm(s2p);
+          dn = dd - rad_i;
+          contact = !(dn > 0);
+          if (contact) {
+            n = s2p / dd;
+            cpos = ri - n * (rad_i + 0.5 * dn);
+          }
+        } else {
+          const V3 proj = ri * mk(d.axis[0], d.axis[1], d.axis[2]);
+          const V3 dir = mk(d.center[0], d.center[1], d.center[2]) - proj;
+          const double dd = vnorm(dir);
+          dn = d.radius - (rad_i + dd);
+          contact = !(dn > 0);
+          if (contact) {
+            n = dir / dd;
+            cpos = ri - n * (rad_i + 0.5 * dn);
+          }
+        }
+        dncut = a.cpd.dncut;
+      }
+      if (a.cohesive) contact = (contact || dn <= dncut);
+      const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+      if (!contact) {
+        const V3 z = mk(0, 0, 0);
+        write_result(a, k, z, z, z, z, z);
+      } else if (a.cohesive && dn >= 0) {
+        // cohesive attraction before contact (contact_force.hpp:165-173): f = fn_value n, ft = 0
+        const dem_contact_params& hkp = is_vv ? a.cp : a.cpd;
+        const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
+        const V3 f = mk(0, 0, 0) + fn_value * n;
+        const V3 ti = cross(cpos - ri, f) + mo;
+        const V3 tj = is_vv ? cross(cpos - rj, -f) + (-mo) : mk(0, 0, 0);
+        write_result(a, k, mk(0, 0, 0), mo, f, ti, tj);
+      } else {
+        heavy = true;
+      }
+    }
+    const uint32_t pos = warp_append(heavy, a.cnt + 1);
+    if (heavy) {
+      a.L2[pos] = k;
+      a.D[0][pos] = dn;
+      a.D[1][pos] = n.x;
+      a.D[2][pos] = n.y;
+      a.D[3][pos] = n.z;
+      a.D[4][pos] = cpos.x;
+      a.D[5][pos] = cpos.y;
+      a.D[6][pos] = cpos.z;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(FT) k_chooke(CArgs a) {
+  const uint64_t n2 = a.cnt[1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a.n_active = n2;  // every L2 pair overlaps (dn < 0)
+  const uint64_t stride = (uint64_t)gridDim.x * FT;
+  for (uint64_t w = (uint64_t)blockIdx.x * FT + threadIdx.x; w < n2; w += stride) {
+    const uint32_t k = a.L2[w];
+    const double dn = a.D[0][w];
+    const V3 n = mk(a.D[1][w], a.D[2][w], a.D[3][w]);
+    const V3 cpos = mk(a.D[4][w], a.D[5][w], a.D[6][w]);
+    const uint32_t meta = a.I.meta[k];
+    const uint32_t i = a.I.owner[k], j = a.I.partner[k];
+    const V3 ri = ldv(a.P, RX, i);
+    V3 ft = mk(a.I.ft[0][k], a.I.ft[1][k], a.I.ft[2][k]);
+    V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+    V3 f = mk(0, 0, 0), ti, tj = mk(0, 0, 0);
+    const V3 vi = ldv(a.P, VX, i);
+    const V3 wi = ldv(a.P, WX, i);
+    if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
+      const V3 rj = partner_pos(a, meta, j);
+      const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
+      const double m_i = a.P.f[MASS][i], m_j = a.P.f[MASS][j];
+      const double meff = (m_i * m_j) / (m_i + m_j);
+      contact_force_core(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, ri, vi, f, mo, wi, rj, vj, wj);
+      ti = cross(cpos - ri, f) + mo;
+      tj = cross(cpos - rj, -f) + (-mo);
+    } else {
+      const DriverDev& d = a.drv[j];
+      const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
+      const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
+      const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
+      const double meff = a.P.f[MASS][i];
+      contact_force_core(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, ri, vi, f, mo, wi, dpos, dvel, dvrot);
+      ti = cross(cpos - ri, f) + mo;
+    }
+    write_result(a, k, ft, mo, f, ti, tj);
+  }
+}
+
+__global__ void k_fused_prolog(PArrays P, uint64_t n, double delta_t, double half_delta_t, double delta_t2_2,
+                               double thr2, unsigned long long* flag) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (s < n) {
+    prolog_one(P, s, delta_t, half_delta_t, delta_t2_2);
+    const double dx = P.f[RX][s] - P.f[BX][s], dy = P.f[RY][s] - P.f[BY][s], dz = P.f[RZ][s] - P.f[BZ][s];
+    over = dx * dx + dy * dy + dz * dz >= thr2;
+  }
+  if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+}
+
+// reset_force_moment + gravity_force + contact gather + force_to_accel + epilog
+__global__ void __launch_bounds__(FT) k_fused_epilog(PArrays P, Records R, uint64_t n,
+                                                     const uint32_t* __restrict__ own_off,
+                                                     const uint32_t* __restrict__ rev_off,
+                                                     const uint32_t* __restrict__ rev_idx, double gx, double gy,
+                                                     double gz, double half_delta_t) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const double m = P.f[MASS][s];
+  V3 f = mk(0.0 + gx * m, 0.0 + gy * m, 0.0 + gz * m);
+  V3 mom = mk(0.0, 0.0, 0.0);
+  for (uint32_t k = own_off[s]; k < own_off[s + 1]; k++) {
+    f = f + mk(R.f[0][k], R.f[1][k], R.f[2][k]);
+    mom = mom + mk(R.ti[0][k], R.ti[1][k], R.ti[2][k]);
+  }
+  for (uint32_t q = rev_off[s]; q < rev_off[s + 1]; q++) {
+    const uint32_t k = rev_idx[q];
+    f = f + (-mk(R.f[0][k], R.f[1][k], R.f[2][k]));
+    mom = mom + mk(R.tj[0][k], R.tj[1][k], R.tj[2][k]);
+  }
+  const double im = P.f[IMASS][s];
+  const V3 acc = mk(div_rn(f.x, m, im), div_rn(f.y, m, im), div_rn(f.z, m, im));
+  P.f[FX][s] = acc.x;
+  P.f[FY][s] = acc.y;
+  P.f[FZ][s] = acc.z;
+  P.f[MX][s] = mom.x;
+  P.f[MY][s] = mom.y;
+  P.f[MZ][s] = mom.z;
+  epilog_one<true>(P, s, half_delta_t, acc, mom);
+}
+
+CArgs make_cargs(dem_ctx* c) {
+  CArgs a;
+  a.P = c->P[c->pcur];
+  a.I = c->I[c->icur];
+  a.R = c->R;
+  a.ni = c->ni;
+  a.g = c->grid;
+  a.drv = c->drv_dev;
+  a.cp = c->prm.config;
+  a.cpd = c->prm.config_driver;
+  a.dt = c->prm.dt;
+  a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
+  a.screen = c->prm.fp32_contact_screen;
+  a.L1 = c->L1;
+  a.L2 = c->L2;
+  for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];
+  a.cnt = c->d_scalars + 3;
+  a.n_active = c->d_scalars + 1;
+  return a;
+}
+}  // namespace
+
+int launch_fused_prolog(dem_ctx* c) {
+  const double delta_t = c->prm.dt;
+  const double half_delta_t = delta_t * 0.5;
+  const double delta_t2_2 = delta_t * delta_t * 0.5;
+  const double max_displ = c->prm.rcut_inc * 0.5;
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars, 0, sizeof(unsigned long long), c->stream));
+  ProfScope ps(c, K_PROLOG, c->n ? 1 : 0);
+  if (c->n)
+    k_fused_prolog<<<grid_for(c->n, FT), FT, 0, c->stream>>>(c->P[c->pcur], c->n, delta_t, half_delta_t, delta_t2_2,
+                                                              max_displ * max_displ, c->d_scalars);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+int launch_contact_compact(dem_ctx* c) {
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 3, 0, 2 * sizeof(unsigned long long), c->stream));
+  ProfScope ps(c, K_CONTACT, 3);
+  const CArgs a = make_cargs(c);
+  const unsigned persistent = (unsigned)c->num_sms * 8u;
+  if (c->ni) k_cscreen<<<grid_for(c->ni, FT), FT, 0, c->stream>>>(a);
+  k_cdetect<<<persistent, FT, 0, c->stream>>>(a);
+  k_chooke<<<persistent, FT, 0, c->stream>>>(a);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+int launch_fused_epilog(dem_ctx* c) {
+  ProfScope ps(c, K_EPILOG, c->n ? 1 : 0);
+  if (c->n)
+    k_fused_epilog<<<grid_for(c->n, FT), FT, 0, c->stream>>>(c->P[c->pcur], c->R, c->n, c->own_off[c->icur],
+                                                              c->rev_off, c->rev_idx, c->prm.gravity[0],
+                                                              c->prm.gravity[1], c->prm.gravity[2],
+                                                              c->prm.dt * 0.5);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+}  // namespace dem

@@ -1,0 +1,36 @@
+// math_exact.cuh -- FP64 helpers that return exactly the IEEE result of the
+// operation they replace, with fewer FP64 pipe instructions.
+//
+// div_rn(a, b, y): the correctly rounded quotient a/b, given y = RN(1/b)
+// precomputed once per particle (masses and inertias do not change).  Method:
+// Markstein's correction step (P. Markstein, "Computation of elementary
+// functions on the IBM RISC System/6000 processor", IBM J. Res. Dev. 34(1),
+// 1990; also Muller et al., Handbook of Floating-Point Arithmetic, 2nd ed.,
+// sec. 4.7): with y within half an ulp of 1/b and q within one ulp of a/b,
+// the remainder r = a - b*q is exact in one FMA and RN(q + r*y) = RN(a/b).
+// q = RN(a*y) is within one ulp of a/b.  The fast path is taken only where no
+// intermediate can overflow, underflow or be special (both exponents within
+// 2^+-500, a != 0); a == 0 returns a*y, the correctly signed zero; everything
+// else falls back to the hardware-compiled division a / b.
+// 3 FP64 instructions instead of a full division (~14 DFMA on sm_103a).
+#pragma once
+#include <stdint.h>
+
+namespace dem {
+
+__device__ __forceinline__ bool exp_in_safe_range(double x) {
+  const uint32_t e = (uint32_t)(__double_as_longlong(x) >> 52) & 0x7ffu;
+  return e > 1023u - 500u && e < 1023u + 500u;
+}
+
+__device__ __forceinline__ double div_rn(double a, double b, double y) {
+  if (a == 0.0) return a * y;
+  if (exp_in_safe_range(a) && exp_in_safe_range(b)) {
+    const double q = a * y;
+    const double r = fma(-q, b, a);
+    return fma(r, y, q);
+  }
+  return a / b;
+}
+
+}  // namespace dem

@@ -33,7 +33,7 @@ from . import _abi as A
 
 def make_params(bounds_lo, bounds_hi, periodic=(0, 0, 0), rcut_inc=0.05, dt=1e-3, gravity=(0.0, 0.0, -9.807),
                 law=A.LAW_HOOKE_NONE, config=None, config_driver=None, cell_size=0.0, fp32_broad_phase=0,
-                fp32_contact_screen=0) -> A.Params:
+                fp32_contact_screen=0, fused_step=0) -> A.Params:
     p = A.Params()
     p.bounds_lo[:] = list(map(float, bounds_lo))
     p.bounds_hi[:] = list(map(float, bounds_hi))
@@ -48,6 +48,7 @@ def make_params(bounds_lo, bounds_hi, periodic=(0, 0, 0), rcut_inc=0.05, dt=1e-3
     p.config_driver = contact_params(**(config_driver or config or {}))
     p.fp32_broad_phase = int(fp32_broad_phase)
     p.fp32_contact_screen = int(fp32_contact_screen)
+    p.fused_step = int(fused_step)
     return p
 
 

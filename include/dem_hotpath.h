@@ -85,7 +85,11 @@ typedef struct dem_params {
    *                   that are provably apart.                            */
   int32_t fp32_broad_phase;
   int32_t fp32_contact_screen;
-  int32_t reserved[6];
+  /* fused_step: dem_step runs the fused kernels (prolog + displacement test,
+   * compacted three-pass contact law, gather + force_to_accel + epilog) with
+   * exact reciprocal-based divisions.  Same results bit for bit.          */
+  int32_t fused_step;
+  int32_t reserved[5];
 } dem_params;
 
 /* ---- particle state view (host or device pointers) ---------------------

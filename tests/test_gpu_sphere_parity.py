@@ -117,3 +117,43 @@ def test_particles_outside_domain(native_lib):
     g, o = _first(w)
     assert_same_list(g.interactions(), o.interactions())
     assert_forces(g.particles(), o.particles())
+
+
+def test_exact_division_selftest(native_lib):
+    """Reciprocal-based division (Markstein's step) equals a / b bit for bit."""
+    import ctypes as C
+
+    bad, fast = C.c_uint64(), C.c_uint64()
+    assert native_lib.dem_selftest_division(40_000_000, 12345, C.byref(bad), C.byref(fast)) == 0
+    assert fast.value > 25_000_000
+    assert bad.value == 0
+
+
+@pytest.mark.parametrize("flags", [dict(fused_step=1), dict(fused_step=1, fp32_contact_screen=1)])
+def test_fused_step_bit_exact_with_plain(native_lib, flags):
+    w1 = W.spheres_floor(n=6000, side=24.0, phi=0.3)
+    w2 = W.spheres_floor(n=6000, side=24.0, phi=0.3, **flags)
+    a, b = w1.build(), w2.build()
+    for s in (a, b):
+        s.first_iteration()
+        s.step(80)
+    pa, pb = a.particles(), b.particles()
+    assert bit_equal_fraction(pa, pb) == 1.0
+    la, lb = a.interactions(), b.interactions()
+    assert_same_list(la, lb)
+    np.testing.assert_array_equal(la["friction"], lb["friction"])
+    np.testing.assert_array_equal(la["moment"], lb["moment"])
+    assert a.simulation_state()["n_active_interactions"] == b.simulation_state()["n_active_interactions"]
+
+
+@pytest.mark.parametrize("make", [lambda: W.spheres_box(n=4000, box=22.0, seed=9, fused_step=1, fp32_contact_screen=1),
+                                  lambda: W.spheres_drum(n=4000, fused_step=1, fp32_contact_screen=1)])
+def test_fused_step_matches_oracle(native_lib, make):
+    w = make()
+    g, o = pair(w)
+    for s in (g, o):
+        s.first_iteration()
+        s.step(100)
+    assert g.rebuild_count() == o.rebuild_count()
+    assert_same_list(g.interactions(), o.interactions())
+    assert_state(g.particles(), o.particles(), 1e-12)
