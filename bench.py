@@ -149,7 +149,7 @@ def workload(args):
     from exadem_gb300 import workloads as W
 
     opt = 0 if args.plain else 1
-    return W.spheres_floor(n=args.n, fp32_contact_screen=opt, fused_step=opt)
+    return W.spheres_floor(n=args.n, fp32_contact_screen=opt, fused_step=opt, fp32_broad_phase=opt)
 
 
 def cpu_baseline(w, budget_s: float = 20.0):
@@ -274,7 +274,7 @@ def run_native(args, rank, world, local, dist):
                    f"spheres_floor n={args.n}",
                    "n_particles": w.n,
                    "path": "plain FP64 operator kernels" if args.plain else
-                           "fused step, FP32 contact screen, compacted FP64 contact law, exact fast division",
+                           "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division",
                    "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "phi_achieved": round(w.info["phi_achieved"], 4)},

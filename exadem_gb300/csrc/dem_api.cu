@@ -75,6 +75,10 @@ int alloc_particles(dem_ctx* c, uint64_t n) {
   DEM_CUDA_TRY(c, cudaMalloc(&c->rev_cnt, (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->own_off[0], (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->own_off[1], (cap + 1) * 4));
+  for (int q = 0; q < 4; q++) {
+    cudaFree(c->crel[q]);
+    DEM_CUDA_TRY(c, cudaMalloc(&c->crel[q], cap * sizeof(float)));
+  }
   c->pcap = cap;
   return DEM_OK;
 }
@@ -300,6 +304,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   cudaFree(c->cell_tmp);
   cudaFree(c->perm);
   cudaFree(c->pcnt);
+  for (int q = 0; q < 4; q++) cudaFree(c->crel[q]);
   cudaFree(c->scan_blk);
   cudaFree(c->d_scalars);
   cudaFree(c->d_red);

@@ -71,12 +71,22 @@ __global__ void k_cell_sort(uint64_t ncell, const uint32_t* __restrict__ cell_st
 }
 
 __global__ void k_reorder(PArrays src, PArrays dst, uint64_t n, const uint32_t* __restrict__ perm,
-                          const uint32_t* __restrict__ cell_tmp, uint32_t* __restrict__ cell_of) {
+                          const uint32_t* __restrict__ cell_tmp, uint32_t* __restrict__ cell_of, GridDev g,
+                          float* __restrict__ xr, float* __restrict__ yr, float* __restrict__ zr,
+                          float* __restrict__ rf) {
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const uint32_t o = perm[t];
 #pragma unroll
   for (int k = 0; k < BX; k++) dst.f[k][t] = src.f[k][o];
+  // FP32 coordinates relative to the origin of the particle's cell, for the FP32 broad phase
+  const uint32_t c = cell_tmp[o];
+  const uint32_t kx = c % (uint32_t)g.dims[0], ky = (c / (uint32_t)g.dims[0]) % (uint32_t)g.dims[1],
+                 kz = c / ((uint32_t)g.dims[0] * (uint32_t)g.dims[1]);
+  xr[t] = (float)(src.f[RX][o] - (g.lo[0] + (double)kx * g.csz[0]));
+  yr[t] = (float)(src.f[RY][o] - (g.lo[1] + (double)ky * g.csz[1]));
+  zr[t] = (float)(src.f[RZ][o] - (g.lo[2] + (double)kz * g.csz[2]));
+  rf[t] = (float)src.f[RAD][o];
   // backup_r: positions at this rebuild, for the displacement trigger
   dst.f[BX][t] = src.f[RX][o];
   dst.f[BY][t] = src.f[RY][o];
@@ -120,7 +130,8 @@ int launch_reorder_particles(dem_ctx* c) {
   ProfScope ps(c, K_REORDER, n ? 1 : 0);
   if (n) {
     k_reorder<<<grid_for(n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->P[1 - c->pcur], n, c->perm, c->cell_tmp,
-                                                        c->cell_of);
+                                                        c->cell_of, c->grid, c->crel[0], c->crel[1], c->crel[2],
+                                                        c->crel[3]);
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
   c->pcur = 1 - c->pcur;

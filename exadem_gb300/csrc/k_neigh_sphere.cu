@@ -29,7 +29,33 @@ struct BPArgs {
   int ndrv;
   double skin;
   double rcut2;
+  // FP32 broad phase: cell-relative coordinates and radii, cell sizes, skin
+  const float* xr;
+  const float* yr;
+  const float* zr;
+  const float* rf;
+  float csz[3];
+  float skin_f;
 };
+
+// FP32 decision of the broad-phase filter d2 > 0 && d2 < (r_i + r_j + skin)^2.
+// Coordinates are relative to each particle's cell origin, so |x_rel| is
+// about one cell and the FP32 difference vector has an absolute error below
+// 2^-22 (|x_rel_i| + |x_rel_j| + cell): three roundings of magnitudes bounded by
+// that sum (conversion of each coordinate, then subtraction and addition of the
+// cell offset).  The FP32 radius sum has a relative error below 2^-22.  m is 8x
+// the sum of both bounds; outside [rm - m, rm + m] the FP32 comparison equals
+// the FP64 one; inside, and near d = 0, the caller runs the exact FP64 test.
+// Returns 1 = keep, 0 = drop, -1 = undecided.
+__device__ __forceinline__ int f32_decide(float ex, float ey, float ez, float si, float sj, float cmax, float rm) {
+  const float d2f = ex * ex + ey * ey + ez * ez;
+  const float m = (si + sj + cmax) * 1.9073486e-06f /* 2^-19 */ + rm * 9.5367432e-07f /* 2^-20 */;
+  const float hi = rm + m;
+  if (d2f > hi * hi) return 0;
+  const float lo = rm - m;
+  if (lo > 0.f && d2f < lo * lo && d2f > 4.f * m * m) return 1;
+  return -1;
+}
 
 __device__ inline bool driver_filter(const DriverDev& d, double rcut, V3 p) {
   if (d.kind == 0) {
@@ -45,7 +71,7 @@ __device__ inline bool driver_filter(const DriverDev& d, double rcut, V3 p) {
   return dn <= 0;
 }
 
-template <class Emit>
+template <bool F32, class Emit>
 __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& emit) {
   const double* __restrict__ rx = a.P.f[RX];
   const double* __restrict__ ry = a.P.f[RY];
@@ -60,6 +86,15 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
     if (driver_filter(d, radi + a.skin, ri))
       emit((uint32_t)k, (uint64_t)k,
            make_meta(d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER, 0, 0, 0, false));
+  }
+  float xri = 0.f, yri = 0.f, zri = 0.f, rfi = 0.f, si = 0.f, cmax = 0.f;
+  if (F32) {
+    xri = a.xr[s];
+    yri = a.yr[s];
+    zri = a.zr[s];
+    rfi = a.rf[s];
+    si = fmaxf(fabsf(xri), fmaxf(fabsf(yri), fabsf(zri)));
+    cmax = fmaxf(a.csz[0], fmaxf(a.csz[1], a.csz[2]));
   }
   const uint32_t c = a.cell_of[s];
   const int d0 = a.g.dims[0], d1 = a.g.dims[1], d2n = a.g.dims[2];
@@ -102,17 +137,28 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
         const uint32_t cc = (uint32_t)x + (uint32_t)d0 * ((uint32_t)y + (uint32_t)d1 * (uint32_t)z);
         const uint32_t qb = a.cell_start[cc], qe = a.cell_start[cc + 1];
         const bool ghost = (sx | sy | sz) != 0;
+        const float oxf = (float)dx * a.csz[0], oyf = (float)dy * a.csz[1], ozf = (float)dz * a.csz[2];
         for (uint32_t q = qb; q < qe; q++) {
-          V3 rj = mk(rx[q], ry[q], rz[q]);
-          if (sx) rj.x = rj.x + (double)sx * a.g.L[0];
-          if (sy) rj.y = rj.y + (double)sy * a.g.L[1];
-          if (sz) rj.z = rj.z + (double)sz * a.g.L[2];
-          const double ddx = rj.x - ri.x, ddy = rj.y - ri.y, ddz = rj.z - ri.z;
-          const double d2 = ddx * ddx + ddy * ddy + ddz * ddz;
-          const double rmax = radi + rad[q] + a.skin;
-          if (!(d2 > 0.0 && d2 < rmax * rmax && d2 < a.rcut2)) continue;
           const uint64_t idj = id[q];
-          if (!ghost && idi >= idj) continue;
+          if (!ghost && idi >= idj) continue;  // owner rule first (integer test)
+          int keep = -1;
+          if (F32) {
+            const float xj = a.xr[q], yj = a.yr[q], zj = a.zr[q];
+            const float sj = fmaxf(fabsf(xj), fmaxf(fabsf(yj), fabsf(zj)));
+            keep = f32_decide((xj - xri) + oxf, (yj - yri) + oyf, (zj - zri) + ozf, si, sj, cmax,
+                              rfi + a.rf[q] + a.skin_f);
+          }
+          if (keep < 0) {
+            V3 rj = mk(rx[q], ry[q], rz[q]);
+            if (sx) rj.x = rj.x + (double)sx * a.g.L[0];
+            if (sy) rj.y = rj.y + (double)sy * a.g.L[1];
+            if (sz) rj.z = rj.z + (double)sz * a.g.L[2];
+            const double ddx = rj.x - ri.x, ddy = rj.y - ri.y, ddz = rj.z - ri.z;
+            const double d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            const double rmax = radi + rad[q] + a.skin;
+            keep = (d2 > 0.0 && d2 < rmax * rmax && d2 < a.rcut2) ? 1 : 0;
+          }
+          if (!keep) continue;
           emit(q, idj, make_meta(DEM_ITYPE_VERTEX_VERTEX, sx, sy, sz, ghost));
         }
       }
@@ -120,11 +166,12 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
   }
 }
 
+template <bool F32>
 __global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
   uint32_t m = 0;
-  for_each_candidate(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t) { m++; });
+  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t) { m++; });
   cnt[s] = m;
 }
 
@@ -132,13 +179,14 @@ __device__ inline bool key_less(uint64_t pa, uint32_t ta, uint64_t pb, uint32_t 
   return pa < pb || (pa == pb && ta < tb);
 }
 
+template <bool F32>
 __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, IArrays old,
                        const uint32_t* __restrict__ old_off, const uint32_t* __restrict__ perm, int have_old) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
   const uint32_t b = off[s], e = off[s + 1];
   uint32_t w = b;
-  for_each_candidate(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta) {
+  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta) {
     if (w < e) {
       dst.partner[w] = q;
       dst.pid[w] = pid;
@@ -254,13 +302,24 @@ BPArgs make_args(dem_ctx* c) {
   a.skin = c->prm.rcut_inc;
   const double nd = 2 * c->rad_max + c->prm.rcut_inc;
   a.rcut2 = nd * nd;
+  a.xr = c->crel[0];
+  a.yr = c->crel[1];
+  a.zr = c->crel[2];
+  a.rf = c->crel[3];
+  for (int d = 0; d < 3; d++) a.csz[d] = (float)c->grid.csz[d];
+  a.skin_f = (float)c->prm.rcut_inc;
   return a;
 }
 }  // namespace
 
 int launch_count_sphere(dem_ctx* c) {
   ProfScope ps(c, K_BROAD_COUNT, c->n ? 1 : 0);
-  if (c->n) k_count<<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt);
+  if (c->n) {
+    if (c->prm.fp32_broad_phase)
+      k_count<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt);
+    else
+      k_count<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt);
+  }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }
@@ -269,9 +328,14 @@ int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total) {
   (void)total;
   const int nw = 1 - c->icur;
   ProfScope ps(c, K_BROAD_FILL, c->n ? 1 : 0);
-  if (c->n)
-    k_fill<<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw], c->I[c->icur],
-                                                       c->own_off[c->icur], c->perm, c->hist_valid ? 1 : 0);
+  if (c->n) {
+    if (c->prm.fp32_broad_phase)
+      k_fill<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw], c->I[c->icur],
+                                                               c->own_off[c->icur], c->perm, c->hist_valid ? 1 : 0);
+    else
+      k_fill<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw], c->I[c->icur],
+                                                                c->own_off[c->icur], c->perm, c->hist_valid ? 1 : 0);
+  }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

@@ -156,6 +156,25 @@ typedef struct dem_interaction_list {
   double *moment;    /* 3*capacity (attr::moment)                    */
 } dem_interaction_list;
 
+/* ---- convex sphero-polyhedron shapes --------------------------------------
+ * Mirrors exaDEM's shape (src/shape/include/exaDEM/shape.hpp:50-68) and the
+ * .shp file layout (example/polyhedra/rotating_drum/octahedron.shp):
+ * vertices, edges (vertex pairs), faces (vertex lists), Minkowski radius and
+ * the precomputed shape OBB (preCompDone: obb.center/e1/e2/e3/extent, the
+ * extent including the radius, shape_prepro.hpp:26-97).  Particle field
+ * `type` indexes the shape table.                                          */
+typedef struct dem_shape {
+  int32_t nv, ne, nf;
+  const double* vertices;       /* 3*nv, body frame                   */
+  const int32_t* edges;         /* 2*ne                               */
+  const int32_t* face_sizes;    /* nf                                 */
+  const int32_t* face_vertices; /* sum(face_sizes), in face order     */
+  double radius;                /* Minkowski radius                   */
+  double obb_center[3], obb_e1[3], obb_e2[3], obb_e3[3], obb_extent[3];
+} dem_shape;
+#define DEM_MAX_SHAPE_VERTICES 32
+#define DEM_MAX_SHAPE_FACE_SIZE 16
+
 typedef struct dem_ctx dem_ctx;
 
 /* ---- lifecycle ----------------------------------------------------------- */
@@ -180,6 +199,10 @@ int dem_get_particles(dem_ctx* ctx, dem_particles* out, int on_device);
 int dem_register_surface(dem_ctx* ctx, const dem_surface* s);
 int dem_register_cylinder(dem_ctx* ctx, const dem_cylinder* c);
 
+/* Switches the context to polyhedron mode (nbh_polyhedron, contact_polyhedron,
+ * vertex_displ_over, config_polyhedra.msp:6-34).  Shapes are copied.       */
+int dem_set_shapes(dem_ctx* ctx, const dem_shape* shapes, int nshapes);
+
 /* ---- one call per reference operator ------------------------------------ */
 /* particle_displ_over (exaNBody; threshold max_displ = rcut_inc/2,
  * config_move_particles.msp:12-15): *result = 1 if some particle moved by
@@ -191,6 +214,16 @@ int dem_particle_displ_over(dem_ctx* ctx, int* result);
  * interaction_manager.hpp:89-112), classify_interactions
  * (src/interaction/classify_interactions.cpp:52-136) and backup_r.      */
 int dem_update_particle_neighbors(dem_ctx* ctx);
+/* compute_vertices (src/polyhedron/compute_vertices.cu:68-108): world-space
+ * vertices v = r + q * (h * v0) of every polyhedron.                      */
+int dem_compute_vertices(dem_ctx* ctx);
+/* vertex_displ_over (src/polyhedron/vertex_displ_over.cu:74-134, backup_dem.hpp:65-110):
+ * *result = 1 if some vertex moved by >= rcut_inc/2 since the last rebuild. */
+int dem_vertex_displ_over(dem_ctx* ctx, int* result);
+/* contact_polyhedron / contact_singlemat_polyhedron_hooke[_none]
+ * (src/polyhedron/contact_force_polyhedron.cu.in:186-215,
+ * polyhedron/contact.hpp:123-303): VV, VE, VF, EE and vertex-driver contacts. */
+int dem_contact_polyhedron(dem_ctx* ctx);
 /* reset_force_moment (src/numericalscheme/reset_force_moment.cu:69-70) */
 int dem_reset_force_moment(dem_ctx* ctx);
 /* gravity_force (src/forcefield/gravity_force.cu:67-86), g from params */

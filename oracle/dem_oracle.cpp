@@ -156,6 +156,11 @@ struct Oracle {
   std::vector<size_t> rev_off;       // per particle: partner-side interactions
   std::vector<int32_t> rev_idx;
   std::vector<Rec> rec;
+  // polyhedron mode
+  bool poly = false;
+  std::vector<struct PShape> shapes;
+  std::vector<std::vector<V3>> vtx;   // world vertices per particle
+  std::vector<std::vector<V3>> bvtx;  // vertices at the last rebuild (backup_dem)
   uint64_t rebuilds = 0;
   uint64_t n_active = 0;
   std::string err;
@@ -549,9 +554,16 @@ void contact_one(Oracle& o, size_t k) {
   }
 }
 
+void contact_one_poly(Oracle& o, size_t k);
+
 void contact_all(Oracle& o) {
+  if (o.poly) {
 #pragma omp parallel for schedule(static)
-  for (long k = 0; k < (long)o.inter.size(); k++) contact_one(o, (size_t)k);
+    for (long k = 0; k < (long)o.inter.size(); k++) contact_one_poly(o, (size_t)k);
+  } else {
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < (long)o.inter.size(); k++) contact_one(o, (size_t)k);
+  }
   uint64_t na = 0;
   for (const Rec& r : o.rec) na += r.active ? 1 : 0;
   o.n_active = na;
@@ -691,6 +703,577 @@ double sphere_slab_volume(double zc, double r, double a, double b) {
   return M_PI * (F(hi) - F(lo));
 }
 
+// ======================================================= polyhedra
+// Oriented bounding box (src/shape/include/exaDEM/type/OBB.hpp).
+struct OBBr {
+  V3 c, e1, e2, e3, ext;
+};
+struct PShape {
+  std::vector<V3> v;
+  std::vector<int> e;                  // 2*ne
+  std::vector<std::vector<int>> f;     // faces
+  double r = 0;                        // Minkowski radius
+  OBBr obb;
+  int nv() const { return (int)v.size(); }
+  int ne() const { return (int)e.size() / 2; }
+  int nf() const { return (int)f.size(); }
+  double max_rcut() const {            // shape.hpp:479-489
+    double rc = 0;
+    for (const V3& x : v) rc = std::max(rc, norm(x) + r);
+    return rc;
+  }
+};
+
+inline void obb_enlarge(OBBr& o, double m) {  // OBB::enlarge
+  o.ext.x += m;
+  o.ext.y += m;
+  o.ext.z += m;
+}
+// compute_obb (src/shape/include/exaDEM/basic_types.hpp:37-48)
+OBBr compute_obb(const OBBr& in, const V3& p, const Quat& q, double h) {
+  OBBr o = in;
+  o.e1 = rotate(q, o.e1);
+  o.e2 = rotate(q, o.e2);
+  o.e3 = rotate(q, o.e3);
+  o.c = rotate(q, o.c);
+  if (h != 1.0) {
+    o.ext *= h;
+    o.c *= h;
+  }
+  o.c += p;
+  return o;
+}
+// OBB::intersect, separating axis test with tol = FLT_EPSILON (type/OBB.hpp:90-220)
+bool obb_intersect(const OBBr& A, const OBBr& B) {
+  const double tol = 1.1920928955078125e-07;
+  double ra, rb;
+  double Rxx, Rxy, Rxz, Ryx, Ryy, Ryz, Rzx, Rzy, Rzz;
+  double Axx, Axy, Axz, Ayx, Ayy, Ayz, Azx, Azy, Azz;
+  Rxx = dot(A.e1, B.e1);
+  Rxy = dot(A.e1, B.e2);
+  Rxz = dot(A.e1, B.e3);
+  Axx = std::fabs(Rxx) + tol;
+  Axy = std::fabs(Rxy) + tol;
+  Axz = std::fabs(Rxz) + tol;
+  const V3 tt = A.c - B.c;
+  const V3 t = {dot(tt, A.e1), dot(tt, A.e2), dot(tt, A.e3)};
+  ra = A.ext.x;
+  rb = B.ext.x * Axx + B.ext.y * Axy + B.ext.z * Axz;
+  if (std::fabs(t.x) > ra + rb) return false;
+  Ryx = dot(A.e2, B.e1);
+  Ayx = std::fabs(Ryx) + tol;
+  Ryy = dot(A.e2, B.e2);
+  Ayy = std::fabs(Ryy) + tol;
+  Ryz = dot(A.e2, B.e3);
+  Ayz = std::fabs(Ryz) + tol;
+  ra = A.ext.y;
+  rb = B.ext.x * Ayx + B.ext.y * Ayy + B.ext.z * Ayz;
+  if (std::fabs(t.y) > ra + rb) return false;
+  Rzx = dot(A.e3, B.e1);
+  Azx = std::fabs(Rzx) + tol;
+  Rzy = dot(A.e3, B.e2);
+  Azy = std::fabs(Rzy) + tol;
+  Rzz = dot(A.e3, B.e3);
+  Azz = std::fabs(Rzz) + tol;
+  ra = A.ext.z;
+  rb = B.ext.x * Azx + B.ext.y * Azy + B.ext.z * Azz;
+  if (std::fabs(t.z) > ra + rb) return false;
+  ra = A.ext.x * Axx + A.ext.y * Ayx + A.ext.z * Azx;
+  rb = B.ext.x;
+  if (std::fabs(t.x * Rxx + t.y * Ryx + t.z * Rzx) > ra + rb) return false;
+  ra = A.ext.x * Axy + A.ext.y * Ayy + A.ext.z * Azy;
+  rb = B.ext.y;
+  if (std::fabs(t.x * Rxy + t.y * Ryy + t.z * Rzy) > ra + rb) return false;
+  ra = A.ext.x * Axz + A.ext.y * Ayz + A.ext.z * Azz;
+  rb = B.ext.z;
+  if (std::fabs(t.x * Rxz + t.y * Ryz + t.z * Rzz) > ra + rb) return false;
+  ra = A.ext.y * Azx + A.ext.z * Ayx;
+  rb = B.ext.y * Axz + B.ext.z * Axy;
+  if (std::fabs(t.z * Ryx - t.y * Rzx) > ra + rb) return false;
+  ra = A.ext.y * Azy + A.ext.z * Ayy;
+  rb = B.ext.x * Axz + B.ext.z * Axx;
+  if (std::fabs(t.z * Ryy - t.y * Rzy) > ra + rb) return false;
+  ra = A.ext.y * Azz + A.ext.z * Ayz;
+  rb = B.ext.x * Axy + B.ext.y * Axx;
+  if (std::fabs(t.z * Ryz - t.y * Rzz) > ra + rb) return false;
+  ra = A.ext.x * Azx + A.ext.z * Axx;
+  rb = B.ext.y * Ayz + B.ext.z * Ayy;
+  if (std::fabs(t.x * Rzx - t.z * Rxx) > ra + rb) return false;
+  ra = A.ext.x * Azy + A.ext.z * Axy;
+  rb = B.ext.x * Ayz + B.ext.z * Ayx;
+  if (std::fabs(t.x * Rzy - t.z * Rxy) > ra + rb) return false;
+  ra = A.ext.x * Azz + A.ext.z * Axz;
+  rb = B.ext.x * Ayy + B.ext.y * Ayx;
+  if (std::fabs(t.x * Rzz - t.z * Rxz) > ra + rb) return false;
+  ra = A.ext.x * Ayx + A.ext.y * Axx;
+  rb = B.ext.y * Azz + B.ext.z * Azy;
+  if (std::fabs(t.y * Rxx - t.x * Ryx) > ra + rb) return false;
+  ra = A.ext.x * Ayy + A.ext.y * Axy;
+  rb = B.ext.x * Azz + B.ext.z * Azx;
+  if (std::fabs(t.y * Rxy - t.x * Ryy) > ra + rb) return false;
+  ra = A.ext.x * Ayz + A.ext.y * Axz;
+  rb = B.ext.x * Azy + B.ext.y * Azx;
+  if (std::fabs(t.y * Rxz - t.x * Ryz) > ra + rb) return false;
+  return true;
+}
+
+inline void vnormalize(V3& v) { v = v / norm(v); }  // _normalize (include/exaDEM/normalize.hpp:43-46)
+
+// ---- filters (src/shape/include/exaDEM/shape_detection_core.hpp)
+bool filter_vv(double rV, const V3& vi, double ri, const V3& vj, double rj) {  // :43-53
+  const double R = ri + rj + rV;
+  const V3 dist = vi - vj;
+  const double d2 = dot(dist, dist);
+  return d2 <= R * R;
+}
+bool filter_ve(double rV, const V3& vi, double ri, const V3& vf, const V3& vs, double rj) {  // :83-101
+  const V3 distfs = vs - vf;
+  const V3 distfi = vi - vf;
+  const double r = (dot(distfs, distfi)) / (dot(distfs, distfs));
+  if (r < -rV || r > 1.0 + rV) return false;
+  const V3 dist = distfi - distfs * r;
+  const double Rmax = ri + rj + rV;
+  return (dot(dist, dist) < (Rmax * Rmax));
+}
+// point-in-face test shared by the face filter and detection (:246-309, :398-466)
+bool vf_core(double lim, const V3& vi, const std::vector<V3>& vaj, const std::vector<int>& face, double& dist_out,
+             V3& n_out) {
+  const int nf = (int)face.size();
+  const V3& va = vaj[face[0]];
+  const V3& vb = vaj[face[1]];
+  const V3& vc = vaj[face[nf - 1]];
+  const V3 v = vi - va;
+  V3 v1 = vb - va;
+  V3 v2 = vc - va;
+  vnormalize(v1);
+  V3 n = cross(v1, v2);
+  vnormalize(n);
+  double dist = dot(n, v);
+  if (dist < 0) {
+    n = n * (-1);
+    dist = -dist;
+  }
+  dist_out = dist;
+  n_out = n;
+  if (dist > lim) return false;
+  const V3 P = vi - n * dist;
+  int ODD = 0;
+  v2 = cross(n, v1);
+  const double ori1 = dot(P, v1);
+  const double ori2 = dot(P, v2);
+  for (int iva = 0; iva < nf; ++iva) {
+    int ivb = iva + 1;
+    if (ivb == nf) ivb = 0;
+    const V3& _va = vaj[face[iva]];
+    const V3& _vb = vaj[face[ivb]];
+    const double pa1 = dot(_va, v1);
+    const double pb1 = dot(_vb, v1);
+    const double pa2 = dot(_va, v2);
+    const double pb2 = dot(_vb, v2);
+    if ((pa2 < ori2 && pb2 >= ori2) || (pb2 < ori2 && pa2 >= ori2)) {
+      if (pa1 + (ori2 - pa2) / (pb2 - pa2) * (pb1 - pa1) < ori1) ODD = 1 - ODD;
+    }
+  }
+  return ODD == 1;
+}
+bool filter_vf(double rV, const V3& vi, double ri, const std::vector<V3>& vaj, const std::vector<int>& face,
+               double rj) {
+  double dist;
+  V3 n;
+  return vf_core(ri + rj + rV, vi, vaj, face, dist, n);
+}
+bool filter_ee(double rV, const V3& vfi, const V3& vsi, double ri, const V3& vfj, const V3& vsj, double rj) {  // :468-504
+  const double R = ri + rj + rV;
+  const V3 Ei = vsi - vfi;
+  const V3 Ej = vsj - vfj;
+  const V3 v = vfi - vfj;
+  const double c = dot(Ei, Ei);
+  const double d = dot(Ej, Ej);
+  const double e = dot(Ei, Ej);
+  double f = (c * d) - (e * e);
+  if (std::fabs(f) > 1.0e-12) {
+    f = 1.0 / f;
+    const double a = dot(Ei, v);
+    const double b = dot(Ej, v);
+    const double s_ = (e * b - a * d) * f;
+    const double t_ = (c * b - e * a) * f;
+    if (s_ <= 0.0 || s_ >= 1.0 || t_ <= 0.0 || t_ >= 1.0) return false;
+    const V3 pi = vfi + Ei * s_;
+    const V3 pj = vfj + Ej * t_;
+    const V3 n = pi - pj;
+    return (dot(n, n) <= (R * R));
+  }
+  return false;
+}
+
+// ---- detection cores: {contact, dn, n, cp}; no contact returns dn = 0 like contact()
+struct Det {
+  bool c = false;
+  double dn = 0;
+  V3 n = {0, 0, 0}, cp = {0, 0, 0};
+};
+Det detect_vv(const V3& pi, double ri, const V3& pj, double rj) {  // :57-81
+  const double R = ri + rj;
+  const V3 dist = pi - pj;
+  const double dist_norm = norm(dist);
+  const double inv_dist_norm = 1.0 / dist_norm;
+  const double dn = dist_norm - R;
+  const V3 n = dist * inv_dist_norm;
+  const V3 cp = pi - n * (ri + 0.5 * dn);
+  return {dn < 0, dn, n, cp};
+}
+Det detect_ve(const V3& vi, double ri, const V3& vf, const V3& vs, double rj) {  // :122-148
+  const V3 distfs = vs - vf;
+  const V3 distfi = vi - vf;
+  const double r = (dot(distfs, distfi)) / (dot(distfs, distfs));
+  if (r <= 0 || r >= 1.0) return Det{};
+  V3 n = distfi - distfs * r;
+  const double dn = norm(n) - (ri + rj);
+  if (dn > 0) return Det{};
+  vnormalize(n);
+  const V3 cp = vi - n * (ri + 0.5 * dn);
+  return {true, dn, n, cp};
+}
+Det detect_vf(const V3& vi, double ri, const std::vector<V3>& vaj, const std::vector<int>& face, double rj) {
+  double dist;
+  V3 n;
+  const bool inside = vf_core(ri + rj, vi, vaj, face, dist, n);
+  if (dist > (ri + rj)) return Det{};
+  const double dn = dist - (ri + rj);
+  const V3 cp = vi - n * (ri + 0.5 * dn);
+  return {inside, dn, n, cp};
+}
+Det detect_ee(const V3& vfi, const V3& vsi, double ri, const V3& vfj, const V3& vsj, double rj) {  // :521-566
+  const double R = ri + rj;
+  const V3 Ei = vsi - vfi;
+  const V3 Ej = vsj - vfj;
+  const V3 v = vfi - vfj;
+  const double c = dot(Ei, Ei);
+  const double d = dot(Ej, Ej);
+  const double e = dot(Ei, Ej);
+  double f = (c * d) - (e * e);
+  if (std::fabs(f) > 1.0e-12) {
+    f = 1.0 / f;
+    const double a = dot(Ei, v);
+    const double b = dot(Ej, v);
+    const double s_ = (e * b - a * d) * f;
+    const double t_ = (c * b - e * a) * f;
+    if (s_ <= 0.0 || s_ >= 1.0 || t_ <= 0.0 || t_ >= 1.0) return Det{};
+    const V3 pi = vfi + Ei * s_;
+    const V3 pj = vfj + Ej * t_;
+    V3 n = pi - pj;
+    const double dn = norm(n) - R;
+    if (dn > 0) return Det{};
+    vnormalize(n);
+    const V3 cp = pi - n * (ri + 0.5 * dn);
+    return {dn <= 0, dn, n, cp};
+  }
+  return Det{};
+}
+
+// world vertices: shape::get_vertex = p + q * (h * v0) (shape.hpp:245-262)
+void compute_vertices(Oracle& o) {
+  o.vtx.resize(o.n);
+#pragma omp parallel for schedule(static)
+  for (long ii = 0; ii < (long)o.n; ii++) {
+    const size_t i = (size_t)ii;
+    const PShape& sh = o.shapes[o.type[i]];
+    const V3 p = pos(o, i);
+    const Quat q = {o.qw[i], o.qx[i], o.qy[i], o.qz[i]};
+    const double h = o.hom[i];
+    o.vtx[i].resize(sh.nv());
+    for (int k = 0; k < sh.nv(); k++) o.vtx[i][k] = p + rotate(q, h * sh.v[k]);
+  }
+}
+
+// nbh_polyhedron (src/polyhedron/nbh_polyhedron.cpp:75-384) + add_driver_interaction
+// (nbh_polyhedron_driver.hpp:216-238), history by key, canonical order.
+int update_neighbors_poly(Oracle& o) {
+  for (int d = 0; d < 3; d++)
+    if (o.prm.periodic[d]) {
+      o.err = "periodic boundaries are not supported for polyhedra";
+      return DEM_ERR_UNSUPPORTED;
+    }
+  compute_vertices(o);
+  const double rV = o.prm.rcut_inc;
+  const double nd = nbh_dist(o);
+  const double rcut2 = nd * nd;
+  const double cs = std::max(o.prm.cell_size, nd);
+  int dims[3];
+  for (int d = 0; d < 3; d++) dims[d] = std::max(1, (int)std::ceil(L(o, d) / cs));
+  auto cell_of = [&](size_t i, int c[3]) {
+    double r[3] = {o.rx[i], o.ry[i], o.rz[i]};
+    for (int d = 0; d < 3; d++) {
+      long k = (long)std::floor((r[d] - o.prm.bounds_lo[d]) / cs);
+      c[d] = (int)std::min<long>(std::max<long>(k, 0), dims[d] - 1);
+    }
+  };
+  const size_t ncell = (size_t)dims[0] * dims[1] * dims[2];
+  std::vector<std::vector<size_t>> cells(ncell);
+  std::vector<int> pc(3 * o.n);
+  for (size_t i = 0; i < o.n; i++) {
+    cell_of(i, &pc[3 * i]);
+    cells[(size_t)pc[3 * i] + dims[0] * ((size_t)pc[3 * i + 1] + (size_t)dims[1] * pc[3 * i + 2])].push_back(i);
+  }
+  std::vector<std::vector<Inter>> per(o.n);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (long aa = 0; aa < (long)o.n; aa++) {
+    const size_t a = (size_t)aa;
+    std::vector<Inter>& lst = per[a];
+    const PShape& sa = o.shapes[o.type[a]];
+    const double ha = o.hom[a];
+    const double ra = sa.r * ha;  // minkowski(h)
+    // drivers: each vertex against each driver
+    for (size_t k = 0; k < o.drivers.size(); k++) {
+      const Driver& dv = o.drivers[k];
+      for (int v = 0; v < sa.nv(); v++) {
+        const double rc = rV + ra;
+        const bool keep = dv.kind == 0 ? surface_filter(dv.s, rc, o.vtx[a][v]) : cylinder_filter(dv.c, rc, o.vtx[a][v]);
+        if (!keep) continue;
+        Inter it{};
+        it.oid = o.id[a];
+        it.pid = k;
+        it.type = dv.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER;
+        it.oi = (int32_t)a;
+        it.pj = (int32_t)k;
+        it.osub = (uint32_t)v;
+        it.psub = 0xffffffffu;  // DRIVER_VERTEX_SUB_IDX = -1
+        lst.push_back(it);
+      }
+    }
+    const V3 ra_pos = pos(o, a);
+    const int* ca = &pc[3 * a];
+    for (int dz = -1; dz <= 1; dz++)
+      for (int dy = -1; dy <= 1; dy++)
+        for (int dx = -1; dx <= 1; dx++) {
+          const int c[3] = {ca[0] + dx, ca[1] + dy, ca[2] + dz};
+          if (c[0] < 0 || c[1] < 0 || c[2] < 0 || c[0] >= dims[0] || c[1] >= dims[1] || c[2] >= dims[2]) continue;
+          for (size_t b : cells[(size_t)c[0] + dims[0] * ((size_t)c[1] + (size_t)dims[1] * c[2])]) {
+            const V3 rb_pos = pos(o, b);
+            const double ddx = rb_pos.x - ra_pos.x, ddy = rb_pos.y - ra_pos.y, ddz = rb_pos.z - ra_pos.z;
+            const double d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            const double rmax = o.rad[a] + o.rad[b] + rV;
+            if (!(d2 > 0.0 && d2 < rmax * rmax && d2 < rcut2)) continue;
+            if (o.id[a] >= o.id[b]) continue;
+            const PShape& sb = o.shapes[o.type[b]];
+            const double hb = o.hom[b];
+            const double rb = sb.r * hb;
+            OBBr obb_i = compute_obb(sa.obb, ra_pos, {o.qw[a], o.qx[a], o.qy[a], o.qz[a]}, ha);
+            OBBr obb_j = compute_obb(sb.obb, rb_pos, {o.qw[b], o.qx[b], o.qy[b], o.qz[b]}, hb);
+            obb_enlarge(obb_i, 0.5 * rV);
+            obb_enlarge(obb_j, 0.5 * rV);
+            if (!obb_intersect(obb_i, obb_j)) continue;
+            obb_enlarge(obb_i, 0.5 * rV);
+            obb_enlarge(obb_j, 0.5 * rV);
+            const std::vector<V3>& va = o.vtx[a];
+            const std::vector<V3>& vb = o.vtx[b];
+            auto add = [&](int type, int swap, int sub_i, int sub_j) {
+              Inter it{};
+              it.oid = o.id[a];
+              it.pid = o.id[b];
+              it.type = (uint16_t)type;
+              it.swap = (uint8_t)swap;
+              it.oi = (int32_t)a;
+              it.pj = (int32_t)b;
+              // owner() = swap ? pj_ : pi_ ; pi_.sub = sub_i
+              it.osub = (uint32_t)(swap ? sub_j : sub_i);
+              it.psub = (uint32_t)(swap ? sub_i : sub_j);
+              lst.push_back(it);
+            };
+            for (int i = 0; i < sa.nv(); i++) {
+              OBBr obbvi{};
+              obbvi.e1 = {1, 0, 0};
+              obbvi.e2 = {0, 1, 0};
+              obbvi.e3 = {0, 0, 1};
+              obbvi.c = va[i];
+              obb_enlarge(obbvi, ra);
+              if (obb_intersect(obb_j, obbvi)) {
+                for (int j = 0; j < sb.nv(); j++)
+                  if (filter_vv(rV, va[i], ra, vb[j], rb)) add(DEM_ITYPE_VERTEX_VERTEX, 0, i, j);
+                for (int j = 0; j < sb.ne(); j++)
+                  if (filter_ve(rV, va[i], ra, vb[sb.e[2 * j]], vb[sb.e[2 * j + 1]], rb)) add(DEM_ITYPE_VERTEX_EDGE, 0, i, j);
+                for (int j = 0; j < sb.nf(); j++)
+                  if (filter_vf(rV, va[i], ra, vb, sb.f[j], rb)) add(DEM_ITYPE_VERTEX_FACE, 0, i, j);
+              }
+            }
+            for (int i = 0; i < sa.ne(); i++)
+              for (int j = 0; j < sb.ne(); j++)
+                if (filter_ee(rV, va[sa.e[2 * i]], va[sa.e[2 * i + 1]], ra, vb[sb.e[2 * j]], vb[sb.e[2 * j + 1]], rb))
+                  add(DEM_ITYPE_EDGE_EDGE, 0, i, j);
+            for (int j = 0; j < sb.nv(); j++) {
+              OBBr obbvj{};
+              obbvj.e1 = {1, 0, 0};
+              obbvj.e2 = {0, 1, 0};
+              obbvj.e3 = {0, 0, 1};
+              obbvj.c = vb[j];
+              obb_enlarge(obbvj, rb);
+              if (obb_intersect(obb_i, obbvj)) {
+                for (int i = 0; i < sa.ne(); i++)
+                  if (filter_ve(rV, vb[j], rb, va[sa.e[2 * i]], va[sa.e[2 * i + 1]], ra)) add(DEM_ITYPE_VERTEX_EDGE, 1, j, i);
+                for (int i = 0; i < sa.nf(); i++)
+                  if (filter_vf(rV, vb[j], rb, va, sa.f[i], ra)) add(DEM_ITYPE_VERTEX_FACE, 1, j, i);
+              }
+            }
+          }
+        }
+    std::sort(lst.begin(), lst.end(), key_less);
+  }
+  std::vector<size_t> by_id(o.n);
+  for (size_t i = 0; i < o.n; i++) by_id[i] = i;
+  std::sort(by_id.begin(), by_id.end(), [&](size_t x, size_t y) { return o.id[x] < o.id[y]; });
+  std::vector<Inter> fresh;
+  for (size_t k = 0; k < o.n; k++) {
+    auto& l = per[by_id[k]];
+    fresh.insert(fresh.end(), l.begin(), l.end());
+  }
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < (long)fresh.size(); k++) {
+    Inter& it = fresh[k];
+    auto lb = std::lower_bound(o.inter.begin(), o.inter.end(), it, key_less);
+    if (lb != o.inter.end() && key_eq(*lb, it)) {
+      it.friction = lb->friction;
+      it.moment = lb->moment;
+    }
+  }
+  o.inter.swap(fresh);
+  o.own_first.assign(o.n, -1);
+  o.own_cnt.assign(o.n, 0);
+  for (size_t k = 0; k < o.inter.size(); k++) {
+    const Inter& it = o.inter[k];
+    if (o.own_first[it.oi] < 0) o.own_first[it.oi] = (int32_t)k;
+    o.own_cnt[it.oi]++;
+  }
+  o.rev_off.assign(o.n + 1, 0);
+  for (const Inter& it : o.inter)
+    if (it.type <= DEM_ITYPE_EDGE_EDGE) o.rev_off[it.pj + 1]++;
+  for (size_t i = 0; i < o.n; i++) o.rev_off[i + 1] += o.rev_off[i];
+  o.rev_idx.assign(o.rev_off[o.n], 0);
+  {
+    std::vector<size_t> cur(o.rev_off.begin(), o.rev_off.end() - 1);
+    for (size_t k = 0; k < o.inter.size(); k++)
+      if (o.inter[k].type <= DEM_ITYPE_EDGE_EDGE) o.rev_idx[cur[o.inter[k].pj]++] = (int32_t)k;
+  }
+  o.rec.assign(o.inter.size(), Rec{});
+  o.bx = o.rx;
+  o.by = o.ry;
+  o.bz = o.rz;
+  o.bvtx = o.vtx;  // backup_dem: vertices at this rebuild
+  o.rebuilds++;
+  return DEM_OK;
+}
+
+// polyhedron::ContactLawFunc<0..3> (polyhedron/contact.hpp:123-211) and ContactLawDriverFunc
+// (:237-303).  The record is written in the owner frame: f on the owner, torque on the
+// owner and on the partner (for swap = 1 the contact law's particle i is the partner).
+void contact_one_poly(Oracle& o, size_t k) {
+  Inter& it = o.inter[k];
+  Rec& rc = o.rec[k];
+  rc = Rec{};
+  const bool cohesive = o.prm.law == DEM_LAW_HOOKE_COHESIVE;
+  const double dt = o.prm.dt;
+  if (it.type >= DEM_ITYPE_VERTEX_CYLINDER) {
+    const size_t p = it.oi;
+    const PShape& sh = o.shapes[o.type[p]];
+    const double h = o.hom[p];
+    const V3 r = pos(o, p);
+    const Driver& dv = o.drivers[it.pj];
+    double dn = 0;
+    V3 n{}, cp{};
+    bool contact;
+    V3 dpos, dvel, dvrot;
+    const V3& vert = o.vtx[p][it.osub];
+    if (dv.kind == 0) {
+      contact = surface_detect(dv.s, sh.r * h, vert, dn, n, cp);
+      dpos = dv.s.center;
+      dvel = dv.s.vel;
+      dvrot = dv.s.vrot;
+    } else {
+      contact = cylinder_detect(dv.c, sh.r * h, vert, dn, n, cp);
+      dpos = dv.c.center;
+      dvel = dv.c.vel;
+      dvrot = dv.c.vrot;
+    }
+    const dem_contact_params& cpar = o.prm.config_driver;
+    if (cohesive) contact = (contact || dn <= cpar.dncut);
+    if (contact) {
+      const V3 v = {o.vx[p], o.vy[p], o.vz[p]};
+      const V3 vrot = {o.wx[p], o.wy[p], o.wz[p]};
+      const double meff = o.mass[p];
+      V3 f = {0, 0, 0};
+      contact_force_core(cohesive, dn, n, dt, cpar, meff, it.friction, cp, r, v, f, it.moment, vrot, dpos, dvel, dvrot);
+      rc.f = f;
+      rc.ti = cross(cp - r, f) + it.moment;
+      rc.active = dn < 0;
+    } else {
+      it.friction = {0, 0, 0};
+      it.moment = {0, 0, 0};
+    }
+    return;
+  }
+  // particle i of the contact law: pi_ (= owner unless swap)
+  const size_t ip = it.swap ? it.pj : it.oi;
+  const size_t jp = it.swap ? it.oi : it.pj;
+  const uint32_t sub_i = it.swap ? it.psub : it.osub;
+  const uint32_t sub_j = it.swap ? it.osub : it.psub;
+  const PShape& shi = o.shapes[o.type[ip]];
+  const PShape& shj = o.shapes[o.type[jp]];
+  const double ri_m = shi.r * o.hom[ip], rj_m = shj.r * o.hom[jp];
+  const std::vector<V3>& vi = o.vtx[ip];
+  const std::vector<V3>& vj = o.vtx[jp];
+  Det d;
+  switch (it.type) {
+    case DEM_ITYPE_VERTEX_VERTEX: d = detect_vv(vi[sub_i], ri_m, vj[sub_j], rj_m); break;
+    case DEM_ITYPE_VERTEX_EDGE: d = detect_ve(vi[sub_i], ri_m, vj[shj.e[2 * sub_j]], vj[shj.e[2 * sub_j + 1]], rj_m); break;
+    case DEM_ITYPE_VERTEX_FACE: d = detect_vf(vi[sub_i], ri_m, vj, shj.f[sub_j], rj_m); break;
+    default:
+      d = detect_ee(vi[shi.e[2 * sub_i]], vi[shi.e[2 * sub_i + 1]], ri_m, vj[shj.e[2 * sub_j]], vj[shj.e[2 * sub_j + 1]],
+                    rj_m);
+  }
+  bool contact = d.c;
+  const dem_contact_params& cpar = o.prm.config;
+  if (cohesive) contact = (contact || d.dn <= cpar.dncut);
+  if (contact) {
+    const V3 r_i = pos(o, ip), r_j = pos(o, jp);
+    const V3 v_i = {o.vx[ip], o.vy[ip], o.vz[ip]}, v_j = {o.vx[jp], o.vy[jp], o.vz[jp]};
+    const V3 w_i = {o.wx[ip], o.wy[ip], o.wz[ip]}, w_j = {o.wx[jp], o.wy[jp], o.wz[jp]};
+    const double meff = (o.mass[ip] * o.mass[jp]) / (o.mass[ip] + o.mass[jp]);
+    V3 f = {0, 0, 0};
+    contact_force_core(cohesive, d.dn, d.n, dt, cpar, meff, it.friction, d.cp, r_i, v_i, f, it.moment, w_i, r_j, v_j,
+                       w_j);
+    const V3 t_i = cross(d.cp - r_i, f) + it.moment;
+    const V3 t_j = cross(d.cp - r_j, -f) + (-it.moment);
+    if (!it.swap) {
+      rc.f = f;
+      rc.ti = t_i;
+      rc.tj = t_j;
+    } else {
+      rc.f = -f;
+      rc.ti = t_j;
+      rc.tj = t_i;
+    }
+    rc.active = d.dn < 0;
+  } else {
+    it.friction = {0, 0, 0};
+    it.moment = {0, 0, 0};
+  }
+}
+
+// vertex_displ_over (src/polyhedron/vertex_displ_over.cu:74-134, backup_dem.hpp:65-110)
+int vertex_displ_over(const Oracle& o) {
+  const double max_displ = o.prm.rcut_inc * 0.5;
+  const double thr2 = max_displ * max_displ;
+  int over = 0;
+#pragma omp parallel for schedule(static) reduction(| : over)
+  for (long ii = 0; ii < (long)o.n; ii++) {
+    const size_t i = (size_t)ii;
+    for (size_t v = 0; v < o.vtx[i].size(); v++) {
+      const V3 dr = o.vtx[i][v] - o.bvtx[i][v];
+      if (dot(dr, dr) >= thr2) over |= 1;
+    }
+  }
+  return over;
+}
+
 }  // namespace
 
 // ============================================================== C interface
@@ -799,9 +1382,47 @@ int oracle_register_cylinder(void* h, const dem_cylinder* c) {
   o.drivers.push_back(d);
   return DEM_OK;
 }
-int oracle_update_neighbors(void* h) { return update_neighbors(*(Oracle*)h); }
+static int rebuild(Oracle& o) { return o.poly ? update_neighbors_poly(o) : update_neighbors(o); }
+static int trigger(Oracle& o) {
+  if (o.poly) {
+    compute_vertices(o);  // compute_fast_vertices / the vertices vertex_displ_over recomputes
+    return vertex_displ_over(o);
+  }
+  return displ_over(o);
+}
+int oracle_update_neighbors(void* h) { return rebuild(*(Oracle*)h); }
 int oracle_displ_over(void* h, int* r) {
-  *r = displ_over(*(Oracle*)h);
+  *r = trigger(*(Oracle*)h);
+  return DEM_OK;
+}
+int oracle_compute_vertices(void* h) {
+  compute_vertices(*(Oracle*)h);
+  return DEM_OK;
+}
+int oracle_set_shapes(void* h, const dem_shape* shp, int nshapes) {
+  Oracle& o = *(Oracle*)h;
+  if (!shp || nshapes <= 0) return DEM_ERR_INVALID_ARG;
+  o.shapes.clear();
+  for (int s = 0; s < nshapes; s++) {
+    PShape ps;
+    for (int k = 0; k < shp[s].nv; k++)
+      ps.v.push_back({shp[s].vertices[3 * k], shp[s].vertices[3 * k + 1], shp[s].vertices[3 * k + 2]});
+    ps.e.assign(shp[s].edges, shp[s].edges + 2 * shp[s].ne);
+    int off = 0;
+    for (int f = 0; f < shp[s].nf; f++) {
+      ps.f.emplace_back(shp[s].face_vertices + off, shp[s].face_vertices + off + shp[s].face_sizes[f]);
+      off += shp[s].face_sizes[f];
+    }
+    ps.r = shp[s].radius;
+    const dem_shape& d = shp[s];
+    ps.obb.c = {d.obb_center[0], d.obb_center[1], d.obb_center[2]};
+    ps.obb.e1 = {d.obb_e1[0], d.obb_e1[1], d.obb_e1[2]};
+    ps.obb.e2 = {d.obb_e2[0], d.obb_e2[1], d.obb_e2[2]};
+    ps.obb.e3 = {d.obb_e3[0], d.obb_e3[1], d.obb_e3[2]};
+    ps.obb.ext = {d.obb_extent[0], d.obb_extent[1], d.obb_extent[2]};
+    o.shapes.push_back(ps);
+  }
+  o.poly = true;
   return DEM_OK;
 }
 int oracle_reset_force_moment(void* h) {
@@ -831,7 +1452,7 @@ int oracle_epilog(void* h) {
 // first_iteration (main-config.msp:55-65)
 int oracle_first_iteration(void* h) {
   Oracle& o = *(Oracle*)h;
-  int rc = update_neighbors(o);
+  int rc = rebuild(o);
   if (rc) return rc;
   reset_force_moment(o);
   compute_force(o);
@@ -842,8 +1463,8 @@ int oracle_step(void* h, int nsteps) {
   Oracle& o = *(Oracle*)h;
   for (int s = 0; s < nsteps; s++) {
     prolog(o);
-    if (displ_over(o)) {
-      int rc = update_neighbors(o);
+    if (trigger(o)) {
+      int rc = rebuild(o);
       if (rc) return rc;
     }
     reset_force_moment(o);

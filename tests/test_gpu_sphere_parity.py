@@ -157,3 +157,22 @@ def test_fused_step_matches_oracle(native_lib, make):
     assert g.rebuild_count() == o.rebuild_count()
     assert_same_list(g.interactions(), o.interactions())
     assert_state(g.particles(), o.particles(), 1e-12)
+
+
+@pytest.mark.parametrize("make", [
+    lambda **f: W.spheres_floor(n=8000, side=26.0, phi=0.3, **f),
+    lambda **f: W.spheres_box(n=3000, box=20.0, seed=4, **f),
+    lambda **f: W.spheres_drum(n=3000, **f)])
+def test_fp32_broad_phase_same_list(native_lib, make):
+    """The FP32 cell-relative broad phase keeps exactly the FP64 candidate set, rebuild after rebuild."""
+    a = make().build()
+    b = make(fp32_broad_phase=1, fused_step=1, fp32_contact_screen=1).build()
+    for s in (a, b):
+        s.first_iteration()
+    assert_same_list(a.interactions(), b.interactions())
+    for _ in range(4):
+        for s in (a, b):
+            s.step(25)
+            s.update_particle_neighbors()  # force a rebuild
+        assert_same_list(a.interactions(), b.interactions())
+    assert bit_equal_fraction(a.particles(), b.particles()) == 1.0
