@@ -86,7 +86,14 @@ class RsaSpec(C.Structure):
     _fields_ = [("n", C.c_uint64), ("rmin", D), ("rmax", D), ("density", D), ("lo", D * 3), ("hi", D * 3),
                 ("periodic", C.c_int32 * 3), ("grow_axis", C.c_int32), ("region", C.c_int32),
                 ("cyl_center", D * 2), ("cyl_radius", D), ("vmin", D), ("vmax", D), ("seed", C.c_uint64),
-                ("max_attempts", C.c_uint64), ("id_offset", C.c_uint64)]
+                ("max_attempts", C.c_uint64), ("id_offset", C.c_uint64), ("radii", PD)]
+
+
+class Shape(C.Structure):
+    _fields_ = [("nv", C.c_int32), ("ne", C.c_int32), ("nf", C.c_int32), ("vertices", PD),
+                ("edges", C.POINTER(C.c_int32)), ("face_sizes", C.POINTER(C.c_int32)),
+                ("face_vertices", C.POINTER(C.c_int32)), ("radius", D), ("obb_center", D * 3), ("obb_e1", D * 3),
+                ("obb_e2", D * 3), ("obb_e3", D * 3), ("obb_extent", D * 3)]
 
 
 def ptr(a: np.ndarray | None, ctype=PD):
@@ -135,6 +142,10 @@ def declare_library(lib) -> None:
                  "dem_combined_compute_epilog", "dem_first_iteration"]:
         _sig(lib, name, [_CTX])
     _sig(lib, "dem_step", [_CTX, C.c_int])
+    _sig(lib, "dem_set_shapes", [_CTX, C.POINTER(Shape), C.c_int])
+    _sig(lib, "dem_compute_vertices", [_CTX])
+    _sig(lib, "dem_contact_polyhedron", [_CTX])
+    _sig(lib, "dem_vertex_displ_over", [_CTX, C.POINTER(C.c_int)])
     _sig(lib, "dem_rebuild_count", [_CTX, PU64])
     _sig(lib, "dem_simulation_state", [_CTX, C.POINTER(State)])
     _sig(lib, "dem_interaction_count", [_CTX, PU64])
@@ -156,7 +167,8 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
             "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
-            "dem_simulation_state_noalloc", "dem_selftest_division"]
+            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_set_shapes", "dem_compute_vertices",
+            "dem_contact_polyhedron", "dem_vertex_displ_over"]
 
 _LIB = None
 

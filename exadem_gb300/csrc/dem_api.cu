@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "dem_ctx.cuh"
+#include "poly_core.cuh"
 
 using namespace dem;
 
@@ -88,6 +89,7 @@ void free_iarrays(IArrays& I) {
   cudaFree(I.partner);
   cudaFree(I.pid);
   cudaFree(I.meta);
+  cudaFree(I.sub);
   for (int d = 0; d < 3; d++) {
     cudaFree(I.ft[d]);
     cudaFree(I.mo[d]);
@@ -105,6 +107,7 @@ int alloc_iarrays(dem_ctx* c, int b, uint64_t need) {
   DEM_CUDA_TRY(c, cudaMalloc(&I.partner, cap * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&I.pid, cap * 8));
   DEM_CUDA_TRY(c, cudaMalloc(&I.meta, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&I.sub, cap * 4));
   for (int d = 0; d < 3; d++) {
     DEM_CUDA_TRY(c, cudaMalloc(&I.ft[d], cap * 8));
     DEM_CUDA_TRY(c, cudaMalloc(&I.mo[d], cap * 8));
@@ -187,7 +190,99 @@ int setup_grid(dem_ctx* c) {
   return DEM_OK;
 }
 
+void free_poly(dem_ctx* c) {
+  for (int d = 0; d < 3; d++) {
+    cudaFree(c->vtx[d]);
+    cudaFree(c->bvtx[d]);
+    c->vtx[d] = c->bvtx[d] = nullptr;
+  }
+  cudaFree(c->pobb);
+  cudaFree(c->u_off);
+  c->pobb = nullptr;
+  c->u_off = nullptr;
+  c->vcap = 0;
+}
+
+int alloc_poly(dem_ctx* c) {
+  if (!c->poly) return DEM_OK;
+  const uint64_t need = std::max<uint64_t>(c->n, 1) * (uint64_t)std::max(c->MV, 1);
+  if (need <= c->vcap && c->pobb && c->u_off) return DEM_OK;
+  free_poly(c);
+  for (int d = 0; d < 3; d++) {
+    DEM_CUDA_TRY(c, cudaMalloc(&c->vtx[d], need * 8));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->bvtx[d], need * 8));
+  }
+  DEM_CUDA_TRY(c, cudaMalloc(&c->pobb, std::max<uint64_t>(c->pcap, 1) * 15 * 8));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_off, (std::max<uint64_t>(c->pcap, 1) + 1) * 4));
+  c->vcap = need;
+  return DEM_OK;
+}
+
+void free_units(dem_ctx* c) {
+  cudaFree(c->u_owner);
+  cudaFree(c->u_partner);
+  cudaFree(c->u_pid);
+  cudaFree(c->u_kind);
+  cudaFree(c->u_pass);
+  cudaFree(c->f_cnt);
+  cudaFree(c->f_off);
+  c->u_owner = c->u_partner = c->u_kind = c->f_cnt = c->f_off = nullptr;
+  c->u_pid = nullptr;
+  c->u_pass = nullptr;
+  c->ucap = 0;
+}
+
+int grow_units(dem_ctx* c, uint64_t need) {
+  if (need <= c->ucap && c->u_owner) return DEM_OK;
+  free_units(c);
+  const uint64_t cap = need + need / 4 + 1024;
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_owner, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_partner, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_pid, cap * 8));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_kind, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_pass, cap));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->f_cnt, (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->f_off, (cap + 1) * 4));
+  c->ucap = cap;
+  return DEM_OK;
+}
+
+int alloc_records(dem_ctx* c, uint64_t need);
+int alloc_iarrays(dem_ctx* c, int b, uint64_t need);
+
+// nbh_polyhedron rebuild: bin + reorder, vertices/backup/OBBs, units, SAT, count, fill, reverse lists
+int update_neighbors_poly(dem_ctx* c) {
+  for (int d = 0; d < 3; d++)
+    if (c->prm.periodic[d]) return c->fail(DEM_ERR_UNSUPPORTED, "periodic boundaries are not supported for polyhedra");
+  if (c->n == 0) {
+    c->ni = 0;
+    c->have_list = true;
+    return DEM_OK;
+  }
+  int rc;
+  if ((rc = alloc_poly(c))) return rc;
+  if ((rc = launch_bin_particles(c))) return rc;
+  if ((rc = launch_reorder_particles(c))) return rc;
+  if ((rc = launch_poly_vertices(c, 2))) return rc;
+  uint64_t nu = 0;
+  if ((rc = launch_poly_units(c, &nu, grow_units))) return rc;
+  uint32_t total = 0;
+  if ((rc = launch_poly_feature_count(c, nu, &total))) return rc;
+  const int nw = 1 - c->icur;
+  if ((rc = alloc_iarrays(c, nw, total))) return rc;
+  if ((rc = alloc_records(c, total))) return rc;
+  if ((rc = launch_poly_feature_fill(c, nu))) return rc;
+  c->icur = nw;
+  c->ni = total;
+  c->have_list = true;
+  c->hist_valid = true;
+  if ((rc = launch_reverse_lists(c))) return rc;
+  c->rebuilds++;
+  return DEM_OK;
+}
+
 int update_neighbors(dem_ctx* c) {
+  if (c->poly) return update_neighbors_poly(c);
   if (c->n == 0) {
     c->ni = 0;
     c->have_list = true;
@@ -218,7 +313,7 @@ int update_neighbors(dem_ctx* c) {
 int compute_force(dem_ctx* c) {
   int rc;
   if ((rc = launch_gravity(c))) return rc;
-  if ((rc = launch_contact_sphere(c))) return rc;
+  if ((rc = c->poly ? launch_contact_poly(c) : launch_contact_sphere(c))) return rc;
   return launch_gather_forces(c);
 }
 
@@ -296,6 +391,9 @@ int dem_ctx_destroy(dem_ctx* c) {
   }
   cudaFree(c->rev_idx);
   free_compact(c);
+  free_poly(c);
+  free_units(c);
+  cudaFree(c->shapes_dev);
   cudaFree(c->rev_off);
   cudaFree(c->rev_cnt);
   cudaFree(c->cell_cnt);
@@ -400,6 +498,7 @@ int dem_set_particles(dem_ctx* c, const dem_particles* p, int on_device) {
   c->have_list = false;
   c->hist_valid = false;
   c->rebuilds = 0;
+  if ((rc = alloc_poly(c))) return rc;
   return setup_grid(c);
 }
 
@@ -495,10 +594,102 @@ int dem_gravity_force(dem_ctx* c) {
 
 int dem_contact_sphere(dem_ctx* c) {
   if (!c) return DEM_ERR_INVALID_ARG;
+  if (c->poly)
+    return c->fail(DEM_ERR_STATE,
+                   "The contact operator for spheres is being used, but polyhedron interactions are defined "
+                   "(contact_force_sphere.cu.in:225-233)");
   int rc = need_list(c);
   if (rc) return rc;
   if ((rc = launch_contact_sphere(c))) return rc;
   return launch_gather_forces(c);
+}
+
+int dem_contact_polyhedron(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  if (!c->poly) return c->fail(DEM_ERR_STATE, "no shapes: call dem_set_shapes first");
+  int rc = need_list(c);
+  if (rc) return rc;
+  if ((rc = launch_contact_poly(c))) return rc;
+  return launch_gather_forces(c);
+}
+
+int dem_compute_vertices(dem_ctx* c) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  if (!c->poly) return c->fail(DEM_ERR_STATE, "no shapes: call dem_set_shapes first");
+  int rc = alloc_poly(c);
+  if (rc) return rc;
+  return launch_poly_vertices(c, 0);
+}
+
+int dem_vertex_displ_over(dem_ctx* c, int* result) {
+  if (!c || !result) return DEM_ERR_INVALID_ARG;
+  if (!c->poly) return c->fail(DEM_ERR_STATE, "no shapes: call dem_set_shapes first");
+  if (!c->have_list) return c->fail(DEM_ERR_STATE, "no backup vertices: build the neighbour list first");
+  int rc = launch_poly_vertices(c, 1);
+  if (rc) return rc;
+  if ((rc = read_flag(c, 0))) return rc;
+  *result = c->h_scalars[0] ? 1 : 0;
+  return DEM_OK;
+}
+
+int dem_set_shapes(dem_ctx* c, const dem_shape* shapes, int nshapes) {
+  if (!c || !shapes || nshapes <= 0) return DEM_ERR_INVALID_ARG;
+  std::vector<ShapeDev> h(nshapes);
+  int mv = 0;
+  for (int k = 0; k < nshapes; k++) {
+    const dem_shape& d = shapes[k];
+    ShapeDev& o = h[k];
+    std::memset(&o, 0, sizeof(o));
+    if (d.nv < 1 || d.nv > SH_MAXV || d.ne < 0 || d.ne > SH_MAXE || d.nf < 0 || d.nf > SH_MAXF || !d.vertices ||
+        (d.ne && !d.edges) || (d.nf && (!d.face_sizes || !d.face_vertices)))
+      return c->fail(DEM_ERR_INVALID_ARG, "shape exceeds the supported sizes (32 vertices, 64 edges, 32 faces)");
+    o.nv = d.nv;
+    o.ne = d.ne;
+    o.nf = d.nf;
+    o.r = d.radius;
+    double mx = 0;
+    for (int i = 0; i < 3 * d.nv; i++) o.v[i] = d.vertices[i];
+    for (int i = 0; i < d.nv; i++)
+      mx = std::max(mx, std::sqrt(o.v[3 * i] * o.v[3 * i] + o.v[3 * i + 1] * o.v[3 * i + 1] + o.v[3 * i + 2] * o.v[3 * i + 2]));
+    o.maxv = mx;
+    for (int i = 0; i < 2 * d.ne; i++) {
+      if (d.edges[i] < 0 || d.edges[i] >= d.nv) return c->fail(DEM_ERR_INVALID_ARG, "edge vertex out of range");
+      o.e[i] = d.edges[i];
+    }
+    int off = 0;
+    for (int f = 0; f < d.nf; f++) {
+      o.fo[f] = off;
+      if (d.face_sizes[f] < 3 || off + d.face_sizes[f] > SH_MAXFV)
+        return c->fail(DEM_ERR_INVALID_ARG, "face needs >= 3 vertices (128 face vertices at most)");
+      for (int q = 0; q < d.face_sizes[f]; q++) {
+        const int v = d.face_vertices[off + q];
+        if (v < 0 || v >= d.nv) return c->fail(DEM_ERR_INVALID_ARG, "face vertex out of range");
+        o.fv[off + q] = v;
+      }
+      off += d.face_sizes[f];
+    }
+    o.fo[d.nf] = off;
+    for (int q = 0; q < 3; q++) {
+      o.obb[q] = d.obb_center[q];
+      o.obb[3 + q] = d.obb_e1[q];
+      o.obb[6 + q] = d.obb_e2[q];
+      o.obb[9 + q] = d.obb_e3[q];
+      o.obb[12 + q] = d.obb_extent[q];
+    }
+    mv = std::max(mv, d.nv);
+  }
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  cudaFree(c->shapes_dev);
+  c->shapes_dev = nullptr;
+  DEM_CUDA_TRY(c, cudaMalloc(&c->shapes_dev, sizeof(ShapeDev) * nshapes));
+  DEM_CUDA_TRY(c, cudaMemcpy(c->shapes_dev, h.data(), sizeof(ShapeDev) * nshapes, cudaMemcpyHostToDevice));
+  c->nshapes = nshapes;
+  if (mv != c->MV) free_poly(c);
+  c->MV = mv;
+  c->poly = true;
+  c->have_list = false;
+  c->hist_valid = false;
+  return alloc_poly(c);
 }
 
 int dem_force_to_accel(dem_ctx* c) {
@@ -534,6 +725,24 @@ int dem_step(dem_ctx* c, int nsteps) {
   int rc = need_list(c);
   if (rc) return rc;
   for (int s = 0; s < nsteps; s++) {
+    if (c->poly) {
+      // prolog, vertices + vertex_displ_over, rebuild if needed, forces, force_to_accel, epilog
+      if ((rc = launch_prolog(c))) return rc;
+      if ((rc = launch_poly_vertices(c, 1))) return rc;
+      if ((rc = read_flag(c, 0))) return rc;
+      if (c->h_scalars[0] && (rc = update_neighbors(c))) return rc;
+      if ((rc = launch_contact_poly(c))) return rc;
+      if (c->prm.fused_step) {
+        if ((rc = launch_fused_epilog(c))) return rc;
+      } else {
+        if ((rc = launch_reset_force_moment(c))) return rc;
+        if ((rc = launch_gravity(c))) return rc;
+        if ((rc = launch_gather_forces(c))) return rc;
+        if ((rc = launch_force_to_accel(c))) return rc;
+        if ((rc = launch_epilog(c))) return rc;
+      }
+      continue;
+    }
     if (c->prm.fused_step) {
       // prolog + trigger; rebuild if needed; three-pass contact; gather + f2a + epilog
       if ((rc = launch_fused_prolog(c))) return rc;
@@ -573,7 +782,7 @@ int dem_get_interactions(dem_ctx* c, dem_interaction_list* l) {
   l->count = c->ni;
   if (l->capacity < c->ni) return c->fail(DEM_ERR_INVALID_ARG, "interaction list capacity too small");
   const uint64_t ni = c->ni, n = c->n;
-  std::vector<uint32_t> owner(ni), meta(ni);
+  std::vector<uint32_t> owner(ni), meta(ni), sub(ni);
   std::vector<uint64_t> pid(ni), id(n);
   std::vector<double> h[6];
   const IArrays& I = c->I[c->icur];
@@ -581,6 +790,7 @@ int dem_get_interactions(dem_ctx* c, dem_interaction_list* l) {
   if (ni) {
     DEM_CUDA_TRY(c, cudaMemcpyAsync(owner.data(), I.owner, ni * 4, cudaMemcpyDeviceToHost, c->stream));
     DEM_CUDA_TRY(c, cudaMemcpyAsync(meta.data(), I.meta, ni * 4, cudaMemcpyDeviceToHost, c->stream));
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(sub.data(), I.sub, ni * 4, cudaMemcpyDeviceToHost, c->stream));
     DEM_CUDA_TRY(c, cudaMemcpyAsync(pid.data(), I.pid, ni * 8, cudaMemcpyDeviceToHost, c->stream));
     for (int d = 0; d < 3; d++) {
       DEM_CUDA_TRY(c, cudaMemcpyAsync(h[d].data(), I.ft[d], ni * 8, cudaMemcpyDeviceToHost, c->stream));
@@ -604,9 +814,9 @@ int dem_get_interactions(dem_ctx* c, dem_interaction_list* l) {
       if (l->owner_id) l->owner_id[w] = id[owner[k]];
       if (l->partner_id) l->partner_id[w] = pid[k];
       if (l->type) l->type[w] = (uint16_t)meta_type(meta[k]);
-      if (l->swap) l->swap[w] = 0;
-      if (l->owner_sub) l->owner_sub[w] = 0;
-      if (l->partner_sub) l->partner_sub[w] = 0;
+      if (l->swap) l->swap[w] = (uint8_t)((meta[k] >> 15) & 1u);
+      if (l->owner_sub) l->owner_sub[w] = sub[k] & 0xffffu;
+      if (l->partner_sub) l->partner_sub[w] = (sub[k] >> 16) == 0xffffu ? 0xffffffffu : (sub[k] >> 16);
       if (l->friction)
         for (int d = 0; d < 3; d++) l->friction[3 * w + d] = h[d][k];
       if (l->moment)

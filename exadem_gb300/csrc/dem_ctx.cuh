@@ -76,6 +76,25 @@ struct dem_ctx {
   uint64_t rebuilds = 0;
   uint64_t n_active = 0;
 
+  // polyhedron mode (dem_set_shapes)
+  bool poly = false;
+  int nshapes = 0;
+  int MV = 0;                         // max vertices of a shape (vertex stride)
+  void* shapes_dev = nullptr;         // dem::ShapeDev[nshapes]
+  double* vtx[3] = {};                // world vertices, n*MV each
+  double* bvtx[3] = {};               // vertices at the last rebuild
+  double* pobb = nullptr;             // world OBB per particle (15 doubles)
+  uint64_t vcap = 0;
+  uint32_t* u_off = nullptr;          // n+1 unit offsets per owner
+  uint32_t* u_owner = nullptr;        // unit arrays (ucap each)
+  uint32_t* u_partner = nullptr;
+  uint64_t* u_pid = nullptr;
+  uint32_t* u_kind = nullptr;
+  uint8_t* u_pass = nullptr;
+  uint32_t* f_cnt = nullptr;          // features per unit (ucap+1)
+  uint32_t* f_off = nullptr;          // feature offsets (ucap+1)
+  uint64_t ucap = 0;
+
   // built-in profiler: launches always counted; CUDA-event times when enabled
   bool prof_on = false;
   uint64_t launches[K_NCLASS] = {};
@@ -139,6 +158,12 @@ int launch_displ_over(dem_ctx* c);
 int launch_state(dem_ctx* c, dem_state* out);
 int launch_profile(dem_ctx* c, int nslabs, double zlo, double zhi, double* out);
 int launch_reciprocals(dem_ctx* c, uint64_t n);  // on P[0] after an upload
+// k_poly.cu
+int launch_poly_vertices(dem_ctx* c, int mode);  // 0 plain, 1 + displacement flag, 2 + backup & OBBs
+int launch_poly_units(dem_ctx* c, uint64_t* nu_out, int (*grow_units)(dem_ctx*, uint64_t));
+int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total);
+int launch_poly_feature_fill(dem_ctx* c, uint64_t nu);
+int launch_contact_poly(dem_ctx* c);
 // k_step_fused.cu
 int launch_fused_prolog(dem_ctx* c);
 int launch_contact_compact(dem_ctx* c);

@@ -44,7 +44,8 @@ struct PArrays {
 
 // interaction meta word: bits 0..7 type, bits 8..13 periodic image shift of
 // the partner (2 bits per axis: 0 none, 1 = +L, 2 = -L), bit 14 owner-only
-// (partner is a periodic ghost image whose force is discarded).
+// (partner is a periodic ghost image whose force is discarded), bit 15 swap
+// (polyhedra: the contact law's particle i is the partner).
 __host__ __device__ inline uint32_t meta_type(uint32_t m) { return m & 0xffu; }
 __host__ __device__ inline int meta_shift(uint32_t m, int d) {
   uint32_t s = (m >> (8 + 2 * d)) & 3u;
@@ -61,6 +62,7 @@ struct IArrays {
   uint32_t* partner;  // partner particle slot, or driver index
   uint64_t* pid;      // partner id (particle id, or driver index) -- key
   uint32_t* meta;
+  uint32_t* sub;      // owner sub (low 16 bits) | partner sub (high 16 bits); polyhedra
   double* ft[3];      // history: attr::friction
   double* mo[3];      // history: attr::moment
 };

@@ -219,6 +219,7 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
   }
   for (uint32_t x = b; x < e; x++) {
     dst.owner[x] = (uint32_t)s;
+    dst.sub[x] = 0u;
     double h[6] = {0, 0, 0, 0, 0, 0};
     const uint64_t pk = dst.pid[x];
     const uint32_t tk = meta_type(dst.meta[x]);
@@ -257,14 +258,14 @@ __global__ void k_rev_count(IArrays I, uint64_t ni, uint32_t* __restrict__ cnt) 
   const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ni) return;
   const uint32_t m = I.meta[k];
-  if (meta_type(m) == DEM_ITYPE_VERTEX_VERTEX && !meta_owner_only(m)) atomicAdd(&cnt[I.partner[k]], 1u);
+  if (meta_type(m) <= DEM_ITYPE_EDGE_EDGE && !meta_owner_only(m)) atomicAdd(&cnt[I.partner[k]], 1u);
 }
 __global__ void k_rev_fill(IArrays I, uint64_t ni, const uint32_t* __restrict__ off, uint32_t* __restrict__ cursor,
                            uint32_t* __restrict__ idx) {
   const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ni) return;
   const uint32_t m = I.meta[k];
-  if (meta_type(m) == DEM_ITYPE_VERTEX_VERTEX && !meta_owner_only(m)) {
+  if (meta_type(m) <= DEM_ITYPE_EDGE_EDGE && !meta_owner_only(m)) {
     const uint32_t j = I.partner[k];
     idx[off[j] + atomicAdd(&cursor[j], 1u)] = (uint32_t)k;
   }

@@ -1,0 +1,845 @@
+// k_poly.cu -- sphero-polyhedron hot path: vertices, interaction-list rebuild, contact law.
+//
+// Replaces compute_vertices (src/polyhedron/compute_vertices.cu:68-108),
+// vertex_displ_over + backup_dem (src/polyhedron/vertex_displ_over.cu:74-134,
+// backup_dem.hpp:65-110), nbh_polyhedron + add_driver_interaction
+// (src/polyhedron/nbh_polyhedron.cpp:75-384, nbh_polyhedron_driver.hpp:216-238)
+// and the contact_polyhedron operators (polyhedron/contact.hpp:123-303).
+//
+// Rebuild, exact two-pass count / fill:
+//   units   per owner A: one unit per neighbour B with id_A < id_B whose bounding
+//           spheres are within the skin (the chunk_neighbors filter), one unit per
+//           driver that can reach A; sorted by (partner id, kind);
+//   SAT     one thread per unit: OBB(A), OBB(B) enlarged by skin/2, separating axis test;
+//   features  one warp per surviving unit: per-vertex OBB gates (one lane per
+//           vertex), then every gated feature test enumerated in InteractionPair
+//           order -- VV, VE, VE(swap), VF, VF(swap), EE -- so the ballot-compacted
+//           output of the fill pass is already sorted; history by full key.
+// Contact: dense detection pass over all feature interactions (types 0-3 and
+// vertex-driver 4/5), overlapping ones appended to a list for the Hooke pass.
+// Force records are in the owner frame (for swap = 1 the contact law's particle
+// i is the partner), so the per-particle gather is the one of the sphere path.
+#include <algorithm>
+
+#include "contact_core.cuh"
+#include "poly_core.cuh"
+
+namespace dem {
+namespace {
+
+constexpr int PT = 128;
+
+struct PolyArgs {
+  PArrays P;
+  uint64_t n;
+  const ShapeDev* shapes;
+  int MV;
+  double* vx;
+  double* vy;
+  double* vz;
+  double* bx;
+  double* by;
+  double* bz;
+  double* obb;  // 15 per particle
+};
+
+// ---------------------------------------------------------------- vertices
+template <bool Displ, bool Backup>
+__global__ void k_poly_vertices(PolyArgs a, double thr2, unsigned long long* flag) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (s < a.n) {
+    const ShapeDev& sh = a.shapes[a.P.type[s]];
+    const V3 p = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
+    const Q4 q = {a.P.f[QW][s], a.P.f[QX][s], a.P.f[QY][s], a.P.f[QZ][s]};
+    const double h = a.P.f[HOM][s];
+    for (int k = 0; k < sh.nv; k++) {
+      const V3 v = world_vertex(sh, k, p, q, h);
+      const uint64_t idx = s * (uint64_t)a.MV + k;
+      a.vx[idx] = v.x;
+      a.vy[idx] = v.y;
+      a.vz[idx] = v.z;
+      if (Displ) {
+        const V3 dr = v - mk(a.bx[idx], a.by[idx], a.bz[idx]);
+        over |= dot(dr, dr) >= thr2;
+      }
+      if (Backup) {
+        a.bx[idx] = v.x;
+        a.by[idx] = v.y;
+        a.bz[idx] = v.z;
+      }
+    }
+    if (Backup) {
+      const OBBd o = compute_obb(sh, p, q, h);
+      double* w = a.obb + s * 15;
+      const double vals[15] = {o.c.x, o.c.y, o.c.z, o.e1.x, o.e1.y, o.e1.z, o.e2.x, o.e2.y, o.e2.z,
+                               o.e3.x, o.e3.y, o.e3.z, o.ext.x, o.ext.y, o.ext.z};
+#pragma unroll
+      for (int k = 0; k < 15; k++) w[k] = vals[k];
+    }
+  }
+  if (Displ) {
+    if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+  }
+}
+
+__device__ __forceinline__ OBBd load_obb(const double* o) {
+  OBBd r;
+  r.c = mk(o[0], o[1], o[2]);
+  r.e1 = mk(o[3], o[4], o[5]);
+  r.e2 = mk(o[6], o[7], o[8]);
+  r.e3 = mk(o[9], o[10], o[11]);
+  r.ext = mk(o[12], o[13], o[14]);
+  return r;
+}
+
+// ---------------------------------------------------------------- units
+struct UnitArgs {
+  PArrays P;
+  uint64_t n;
+  GridDev g;
+  const uint32_t* cell_start;
+  const uint32_t* cell_of;
+  const DriverDev* drv;
+  int ndrv;
+  const ShapeDev* shapes;
+  double rV;
+  double rcut2;
+  const float* xr;
+  const float* yr;
+  const float* zr;
+  const float* rf;
+  float csz[3];
+  float skin_f;
+  int f32;
+};
+
+__device__ __forceinline__ bool driver_reach(const DriverDev& d, double rcut, V3 p) {
+  if (d.kind == 0) {
+    const V3 nrm = mk(d.normal[0], d.normal[1], d.normal[2]);
+    const V3 proj = dot(p, nrm) * nrm;
+    const double dd = vnorm(proj - mk(d.center_proj[0], d.center_proj[1], d.center_proj[2]));
+    return dd <= rcut;
+  }
+  const V3 proj = p * mk(d.axis[0], d.axis[1], d.axis[2]);
+  const V3 dir = proj - mk(d.center[0], d.center[1], d.center[2]);
+  const double dd = vnorm(dir);
+  return d.radius - (dd + rcut) <= 0;
+}
+
+// FP32 decision of the bounding-sphere filter (same bound as the sphere broad phase).
+__device__ __forceinline__ int f32_pair(float ex, float ey, float ez, float si, float sj, float cmax, float rm) {
+  const float d2f = ex * ex + ey * ey + ez * ez;
+  const float m = (si + sj + cmax) * 1.9073486e-06f + rm * 9.5367432e-07f;
+  const float hi = rm + m;
+  if (d2f > hi * hi) return 0;
+  const float lo = rm - m;
+  if (lo > 0.f && d2f < lo * lo && d2f > 4.f * m * m) return 1;
+  return -1;
+}
+
+// emit(kind, partner, pid): kind 0 = particle, 1 = driver
+template <class Emit>
+__device__ inline void for_each_unit(const UnitArgs& a, uint32_t s, Emit&& emit) {
+  const V3 ri = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
+  const uint64_t idi = a.P.id[s];
+  if (a.ndrv) {
+    // a vertex of A can reach a driver only if the centre is within h*(max|v0| + r) + skin (+ rounding margin)
+    const ShapeDev& sh = a.shapes[a.P.type[s]];
+    const double h = a.P.f[HOM][s];
+    const double reach = h * (sh.maxv + sh.r) + a.rV;
+    const double rc = reach + 1e-9 * (1.0 + reach + fabs(ri.x) + fabs(ri.y) + fabs(ri.z));
+    for (int k = 0; k < a.ndrv; k++)
+      if (driver_reach(a.drv[k], rc, ri)) emit(1u, (uint32_t)k, (uint64_t)k);
+  }
+  float xri = 0.f, yri = 0.f, zri = 0.f, rfi = 0.f, si = 0.f, cmax = 0.f;
+  if (a.f32) {
+    xri = a.xr[s];
+    yri = a.yr[s];
+    zri = a.zr[s];
+    rfi = a.rf[s];
+    si = fmaxf(fabsf(xri), fmaxf(fabsf(yri), fabsf(zri)));
+    cmax = fmaxf(a.csz[0], fmaxf(a.csz[1], a.csz[2]));
+  }
+  const uint32_t c = a.cell_of[s];
+  const int d0 = a.g.dims[0], d1 = a.g.dims[1], d2n = a.g.dims[2];
+  const int cx = (int)(c % (uint32_t)d0);
+  const int cy = (int)((c / (uint32_t)d0) % (uint32_t)d1);
+  const int cz = (int)(c / ((uint32_t)d0 * (uint32_t)d1));
+  const double radi = a.P.f[RAD][s];
+  for (int dz = -1; dz <= 1; dz++) {
+    const int z = cz + dz;
+    if (z < 0 || z >= d2n) continue;
+    for (int dy = -1; dy <= 1; dy++) {
+      const int y = cy + dy;
+      if (y < 0 || y >= d1) continue;
+      for (int dx = -1; dx <= 1; dx++) {
+        const int x = cx + dx;
+        if (x < 0 || x >= d0) continue;
+        const uint32_t cc = (uint32_t)x + (uint32_t)d0 * ((uint32_t)y + (uint32_t)d1 * (uint32_t)z);
+        const float oxf = (float)dx * a.csz[0], oyf = (float)dy * a.csz[1], ozf = (float)dz * a.csz[2];
+        for (uint32_t q = a.cell_start[cc]; q < a.cell_start[cc + 1]; q++) {
+          const uint64_t idj = a.P.id[q];
+          if (idi >= idj) continue;
+          int keep = -1;
+          if (a.f32) {
+            const float xj = a.xr[q], yj = a.yr[q], zj = a.zr[q];
+            const float sj = fmaxf(fabsf(xj), fmaxf(fabsf(yj), fabsf(zj)));
+            keep = f32_pair((xj - xri) + oxf, (yj - yri) + oyf, (zj - zri) + ozf, si, sj, cmax,
+                            rfi + a.rf[q] + a.skin_f);
+          }
+          if (keep < 0) {
+            const double ddx = a.P.f[RX][q] - ri.x, ddy = a.P.f[RY][q] - ri.y, ddz = a.P.f[RZ][q] - ri.z;
+            const double d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+            const double rmax = radi + a.P.f[RAD][q] + a.rV;
+            keep = (d2 > 0.0 && d2 < rmax * rmax && d2 < a.rcut2) ? 1 : 0;
+          }
+          if (keep) emit(0u, q, idj);
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_unit_count(UnitArgs a, uint32_t* __restrict__ cnt) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  uint32_t m = 0;
+  for_each_unit(a, (uint32_t)s, [&](uint32_t, uint32_t, uint64_t) { m++; });
+  cnt[s] = m;
+}
+
+__global__ void k_unit_fill(UnitArgs a, const uint32_t* __restrict__ off, uint32_t* __restrict__ u_owner,
+                            uint32_t* __restrict__ u_partner, uint64_t* __restrict__ u_pid,
+                            uint32_t* __restrict__ u_kind) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  const uint32_t b = off[s], e = off[s + 1];
+  uint32_t w = b;
+  for_each_unit(a, (uint32_t)s, [&](uint32_t kind, uint32_t partner, uint64_t pid) {
+    if (w < e) {
+      u_owner[w] = (uint32_t)s;
+      u_partner[w] = partner;
+      u_pid[w] = pid;
+      u_kind[w] = kind;
+    }
+    w++;
+  });
+  // (partner id, kind): particle features (types 0-3) before driver features (types 4-5)
+  for (uint32_t x = b + 1; x < e; x++) {
+    const uint64_t pk = u_pid[x];
+    const uint32_t kk = u_kind[x], qk = u_partner[x];
+    uint32_t y = x;
+    while (y > b && (u_pid[y - 1] > pk || (u_pid[y - 1] == pk && u_kind[y - 1] > kk))) {
+      u_pid[y] = u_pid[y - 1];
+      u_kind[y] = u_kind[y - 1];
+      u_partner[y] = u_partner[y - 1];
+      y--;
+    }
+    u_pid[y] = pk;
+    u_kind[y] = kk;
+    u_partner[y] = qk;
+  }
+}
+
+// separating axis test of the two world OBBs enlarged by skin/2 (nbh_polyhedron.cpp:264-273)
+__global__ void k_unit_sat(uint64_t nu, const uint32_t* __restrict__ u_owner, const uint32_t* __restrict__ u_partner,
+                           const uint32_t* __restrict__ u_kind, const double* __restrict__ obb, double rV,
+                           uint8_t* __restrict__ pass) {
+  const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nu) return;
+  if (u_kind[u]) {
+    pass[u] = 1;
+    return;
+  }
+  OBBd A = load_obb(obb + (uint64_t)u_owner[u] * 15);
+  OBBd B = load_obb(obb + (uint64_t)u_partner[u] * 15);
+  obb_enlarge(A, 0.5 * rV);
+  obb_enlarge(B, 0.5 * rV);
+  pass[u] = obb_intersect(A, B) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------- features
+struct FeatArgs {
+  PArrays P;
+  const ShapeDev* shapes;
+  const DriverDev* drv;
+  int MV;
+  const double* vx;
+  const double* vy;
+  const double* vz;
+  const double* obb;
+  double rV;
+  uint64_t nu;
+  const uint32_t* u_owner;
+  const uint32_t* u_partner;
+  const uint64_t* u_pid;
+  const uint32_t* u_kind;
+  const uint8_t* pass;
+  uint32_t* fcnt;        // count pass: features per unit
+  const uint32_t* foff;  // fill pass: offsets (nu+1)
+  IArrays dst;
+  IArrays old;
+  const uint32_t* old_off;
+  const uint32_t* perm;
+  int have_old;
+};
+
+__device__ __forceinline__ VView vview(const FeatArgs& a, uint32_t s) {
+  const uint64_t o = (uint64_t)s * a.MV;
+  return VView{a.vx + o, a.vy + o, a.vz + o};
+}
+
+__device__ __forceinline__ int nth_bit(uint32_t mask, int r) {  // position of the r-th set bit
+  for (int k = 0; k < r; k++) mask &= mask - 1u;
+  return __ffs(mask) - 1;
+}
+
+// secondary key: type, swap, owner sub, partner sub (InteractionPair order after the partner id)
+__device__ __forceinline__ uint64_t skey(uint32_t type, uint32_t swap, uint32_t osub, uint32_t psub) {
+  return ((uint64_t)type << 48) | ((uint64_t)swap << 40) | ((uint64_t)(osub & 0xfffffu) << 20) |
+         (uint64_t)(psub & 0xfffffu);
+}
+
+__device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uint32_t partner, uint64_t pid,
+                              uint32_t type, uint32_t swap, uint32_t osub, uint32_t psub) {
+  a.dst.owner[w] = owner;
+  a.dst.partner[w] = partner;
+  a.dst.pid[w] = pid;
+  a.dst.meta[w] = type | (swap << 15);
+  a.dst.sub[w] = (osub & 0xffffu) | ((psub & 0xffffu) << 16);
+  double h[6] = {0, 0, 0, 0, 0, 0};
+  if (a.have_old) {
+    const uint32_t os = a.perm[owner];
+    uint32_t lo = a.old_off[os], hi = a.old_off[os + 1];
+    const uint32_t oe = hi;
+    const uint64_t sk = skey(type, swap, osub & 0xffffu, psub & 0xffffu);
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      const uint32_t om = a.old.meta[mid], osb = a.old.sub[mid];
+      const uint64_t ok = skey(meta_type(om), (om >> 15) & 1u, osb & 0xffffu, osb >> 16);
+      if (a.old.pid[mid] < pid || (a.old.pid[mid] == pid && ok < sk))
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    if (lo < oe && a.old.pid[lo] == pid) {
+      const uint32_t om = a.old.meta[lo], osb = a.old.sub[lo];
+      if (skey(meta_type(om), (om >> 15) & 1u, osb & 0xffffu, osb >> 16) == sk) {
+        h[0] = a.old.ft[0][lo];
+        h[1] = a.old.ft[1][lo];
+        h[2] = a.old.ft[2][lo];
+        h[3] = a.old.mo[0][lo];
+        h[4] = a.old.mo[1][lo];
+        h[5] = a.old.mo[2][lo];
+      }
+    }
+  }
+  a.dst.ft[0][w] = h[0];
+  a.dst.ft[1][w] = h[1];
+  a.dst.ft[2][w] = h[2];
+  a.dst.mo[0][w] = h[3];
+  a.dst.mo[1][w] = h[4];
+  a.dst.mo[2][w] = h[5];
+}
+
+// One warp per unit.  Fill = false: counts into fcnt; Fill = true: writes at foff.
+template <bool Fill>
+__global__ void __launch_bounds__(PT) k_features(FeatArgs a) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
+  for (uint64_t u = warp; u < a.nu; u += nwarps) {
+    uint32_t count = 0;
+    uint32_t base = Fill ? a.foff[u] : 0;
+    if (!a.pass[u]) {
+      if (!Fill && lane == 0) a.fcnt[u] = 0;
+      continue;
+    }
+    const uint32_t A = a.u_owner[u];
+    const ShapeDev& SA = a.shapes[a.P.type[A]];
+    const double ha = a.P.f[HOM][A];
+    const double ra = SA.r * ha;
+    const VView va = vview(a, A);
+    if (a.u_kind[u]) {
+      // vertex - driver (add_driver_interaction): filter(rV + minkowski(h), vertex)
+      const uint32_t k = a.u_partner[u];
+      const DriverDev& d = a.drv[k];
+      const uint32_t type = d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER;
+      const bool keep = lane < SA.nv && driver_reach(d, a.rV + ra, va[lane]);
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (Fill) {
+        if (keep) write_feature(a, base + __popc(m & ((1u << lane) - 1u)), A, k, a.u_pid[u], type, 0, lane, 0xffffu);
+      } else if (lane == 0) {
+        a.fcnt[u] = __popc(m);
+      }
+      continue;
+    }
+    const uint32_t B = a.u_partner[u];
+    const uint64_t pid = a.u_pid[u];
+    const ShapeDev& SB = a.shapes[a.P.type[B]];
+    const double hb = a.P.f[HOM][B];
+    const double rb = SB.r * hb;
+    const VView vb = vview(a, B);
+    OBBd obb_i = load_obb(a.obb + (uint64_t)A * 15);
+    OBBd obb_j = load_obb(a.obb + (uint64_t)B * 15);
+    obb_enlarge(obb_i, 0.5 * a.rV);
+    obb_enlarge(obb_j, 0.5 * a.rV);
+    obb_enlarge(obb_i, 0.5 * a.rV);
+    obb_enlarge(obb_j, 0.5 * a.rV);
+    // per-vertex OBB gates (one lane per vertex)
+    bool ga = false, gb = false;
+    if (lane < SA.nv) {
+      OBBd ov;
+      ov.c = va[lane];
+      ov.e1 = mk(1, 0, 0);
+      ov.e2 = mk(0, 1, 0);
+      ov.e3 = mk(0, 0, 1);
+      ov.ext = mk(0, 0, 0);
+      obb_enlarge(ov, ra);
+      ga = obb_intersect(obb_j, ov);
+    }
+    if (lane < SB.nv) {
+      OBBd ov;
+      ov.c = vb[lane];
+      ov.e1 = mk(1, 0, 0);
+      ov.e2 = mk(0, 1, 0);
+      ov.e3 = mk(0, 0, 1);
+      ov.ext = mk(0, 0, 0);
+      obb_enlarge(ov, rb);
+      gb = obb_intersect(obb_i, ov);
+    }
+    const uint32_t gA = __ballot_sync(0xffffffffu, ga), gB = __ballot_sync(0xffffffffu, gb);
+    const int nA = __popc(gA), nB = __popc(gB);
+    // segments in InteractionPair order: VV, VE, VE(swap), VF, VF(swap), EE
+    const uint32_t sVV = nA * SB.nv, sVE0 = nA * SB.ne, sVE1 = SA.ne * nB, sVF0 = nA * SB.nf, sVF1 = SA.nf * nB,
+                   sEE = SA.ne * SB.ne;
+    const uint32_t total = sVV + sVE0 + sVE1 + sVF0 + sVF1 + sEE;
+    for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+      const uint32_t t = t0 + lane;
+      bool keep = false;
+      uint32_t type = 0, swap = 0, osub = 0, psub = 0;
+      if (t < total) {
+        uint32_t r = t;
+        if (r < sVV) {
+          const int i = nth_bit(gA, r / SB.nv), j = r % SB.nv;
+          type = DEM_ITYPE_VERTEX_VERTEX;
+          osub = i;
+          psub = j;
+          keep = filter_vv(a.rV, va[i], ra, vb[j], rb);
+        } else if ((r -= sVV) < sVE0) {
+          const int i = nth_bit(gA, r / SB.ne), j = r % SB.ne;
+          type = DEM_ITYPE_VERTEX_EDGE;
+          osub = i;
+          psub = j;
+          keep = filter_ve(a.rV, va[i], ra, vb[SB.e[2 * j]], vb[SB.e[2 * j + 1]], rb);
+        } else if ((r -= sVE0) < sVE1) {
+          const int i = r / nB, j = nth_bit(gB, r % nB);  // A edge i, B vertex j
+          type = DEM_ITYPE_VERTEX_EDGE;
+          swap = 1;
+          osub = i;
+          psub = j;
+          keep = filter_ve(a.rV, vb[j], rb, va[SA.e[2 * i]], va[SA.e[2 * i + 1]], ra);
+        } else if ((r -= sVE1) < sVF0) {
+          const int i = nth_bit(gA, r / SB.nf), j = r % SB.nf;
+          type = DEM_ITYPE_VERTEX_FACE;
+          osub = i;
+          psub = j;
+          keep = filter_vf(a.rV, va[i], ra, vb, SB, j, rb);
+        } else if ((r -= sVF0) < sVF1) {
+          const int i = r / nB, j = nth_bit(gB, r % nB);  // A face i, B vertex j
+          type = DEM_ITYPE_VERTEX_FACE;
+          swap = 1;
+          osub = i;
+          psub = j;
+          keep = filter_vf(a.rV, vb[j], rb, va, SA, i, ra);
+        } else {
+          r -= sVF1;
+          const int i = r / SB.ne, j = r % SB.ne;
+          type = DEM_ITYPE_EDGE_EDGE;
+          osub = i;
+          psub = j;
+          keep = filter_ee(a.rV, va[SA.e[2 * i]], va[SA.e[2 * i + 1]], ra, vb[SB.e[2 * j]], vb[SB.e[2 * j + 1]], rb);
+        }
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (Fill && keep) write_feature(a, base + count + __popc(m & ((1u << lane) - 1u)), A, B, pid, type, swap, osub, psub);
+      count += __popc(m);
+    }
+    if (!Fill && lane == 0) a.fcnt[u] = count;
+  }
+}
+
+// own_off[s] = feature offset of the first unit of s
+__global__ void k_own_from_units(uint64_t n, const uint32_t* __restrict__ uoff, const uint32_t* __restrict__ foff,
+                                 uint32_t* __restrict__ own) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > n) return;
+  own[s] = foff[uoff[s]];
+}
+
+// ---------------------------------------------------------------- contact
+struct PCArgs {
+  PArrays P;
+  IArrays I;
+  Records R;
+  uint64_t ni;
+  const ShapeDev* shapes;
+  const DriverDev* drv;
+  int MV;
+  const double* vx;
+  const double* vy;
+  const double* vz;
+  dem_contact_params cp, cpd;
+  double dt;
+  int cohesive;
+  uint32_t* L2;
+  double* D[7];
+  unsigned long long* cnt;  // [1] = L2 count
+  unsigned long long* n_active;
+};
+
+__device__ __forceinline__ void pwrite(const PCArgs& a, uint64_t k, V3 ft, V3 mo, V3 f, V3 ti, V3 tj) {
+  a.I.ft[0][k] = ft.x;
+  a.I.ft[1][k] = ft.y;
+  a.I.ft[2][k] = ft.z;
+  a.I.mo[0][k] = mo.x;
+  a.I.mo[1][k] = mo.y;
+  a.I.mo[2][k] = mo.z;
+  a.R.f[0][k] = f.x;
+  a.R.f[1][k] = f.y;
+  a.R.f[2][k] = f.z;
+  a.R.ti[0][k] = ti.x;
+  a.R.ti[1][k] = ti.y;
+  a.R.ti[2][k] = ti.z;
+  a.R.tj[0][k] = tj.x;
+  a.R.tj[1][k] = tj.y;
+  a.R.tj[2][k] = tj.z;
+}
+
+__device__ __forceinline__ uint32_t warp_append2(bool want, unsigned long long* counter) {
+  const unsigned mask = __ballot_sync(0xffffffffu, want);
+  const int lane = threadIdx.x & 31;
+  unsigned long long base = 0;
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+  }
+  return (uint32_t)base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+// Roles of an interaction in the contact law: i = pi_, j = pj_ (swap exchanges owner and partner).
+struct Roles {
+  uint32_t ip, jp, sub_i, sub_j;
+};
+__device__ __forceinline__ Roles roles(const PCArgs& a, uint64_t k) {
+  const uint32_t meta = a.I.meta[k], sb = a.I.sub[k];
+  const uint32_t osub = sb & 0xffffu, psub = sb >> 16;
+  const uint32_t A = a.I.owner[k], B = a.I.partner[k];
+  if ((meta >> 15) & 1u) return Roles{B, A, psub, osub};
+  return Roles{A, B, osub, psub};
+}
+
+__device__ __forceinline__ VView pview(const PCArgs& a, uint32_t s) {
+  const uint64_t o = (uint64_t)s * a.MV;
+  return VView{a.vx + o, a.vy + o, a.vz + o};
+}
+
+__global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
+  const uint64_t k = (uint64_t)blockIdx.x * PT + threadIdx.x;
+  bool heavy = false;
+  DetD d = det_none();
+  if (k < a.ni) {
+    const uint32_t meta = a.I.meta[k];
+    const uint32_t type = meta_type(meta);
+    const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+    bool contact;
+    V3 ri, rj = mk(0, 0, 0);
+    bool is_pp = type <= DEM_ITYPE_EDGE_EDGE;
+    double dncut;
+    uint32_t swap = (meta >> 15) & 1u;
+    if (!is_pp) {
+      const uint32_t p = a.I.owner[k];
+      const ShapeDev& sh = a.shapes[a.P.type[p]];
+      const double rm = sh.r * a.P.f[HOM][p];
+      const V3 vert = pview(a, p)[a.I.sub[k] & 0xffffu];
+      const DriverDev& dv = a.drv[a.I.partner[k]];
+      d = det_none();
+      if (dv.kind == 0) {
+        const V3 nrm = mk(dv.normal[0], dv.normal[1], dv.normal[2]);
+        const V3 proj = dot(vert, nrm) * nrm;
+        const V3 s2p = -(mk(dv.center_proj[0], dv.center_proj[1], dv.center_proj[2]) - proj);
+        const double dd = vnorm(s2p);
+        d.dn = dd - rm;
+        if (!(d.dn > 0)) {
+          d.c = true;
+          d.n = s2p / dd;
+          d.cp = vert - d.n * (rm + 0.5 * d.dn);
+        }
+      } else {
+        const V3 proj = vert * mk(dv.axis[0], dv.axis[1], dv.axis[2]);
+        const V3 dir = mk(dv.center[0], dv.center[1], dv.center[2]) - proj;
+        const double dd = vnorm(dir);
+        d.dn = dv.radius - (rm + dd);
+        if (!(d.dn > 0)) {
+          d.c = true;
+          d.n = dir / dd;
+          d.cp = vert - d.n * (rm + 0.5 * d.dn);
+        }
+      }
+      ri = mk(a.P.f[RX][p], a.P.f[RY][p], a.P.f[RZ][p]);
+      dncut = a.cpd.dncut;
+    } else {
+      const Roles R = roles(a, k);
+      const ShapeDev& si = a.shapes[a.P.type[R.ip]];
+      const ShapeDev& sj = a.shapes[a.P.type[R.jp]];
+      const double rim = si.r * a.P.f[HOM][R.ip], rjm = sj.r * a.P.f[HOM][R.jp];
+      const VView vi = pview(a, R.ip), vj = pview(a, R.jp);
+      switch (type) {
+        case DEM_ITYPE_VERTEX_VERTEX:
+          d = detect_vv(vi[R.sub_i], rim, vj[R.sub_j], rjm);
+          break;
+        case DEM_ITYPE_VERTEX_EDGE:
+          d = detect_ve(vi[R.sub_i], rim, vj[sj.e[2 * R.sub_j]], vj[sj.e[2 * R.sub_j + 1]], rjm);
+          break;
+        case DEM_ITYPE_VERTEX_FACE:
+          d = detect_vf(vi[R.sub_i], rim, vj, sj, R.sub_j, rjm);
+          break;
+        default:
+          d = detect_ee(vi[si.e[2 * R.sub_i]], vi[si.e[2 * R.sub_i + 1]], rim, vj[sj.e[2 * R.sub_j]],
+                        vj[sj.e[2 * R.sub_j + 1]], rjm);
+      }
+      ri = mk(a.P.f[RX][R.ip], a.P.f[RY][R.ip], a.P.f[RZ][R.ip]);
+      rj = mk(a.P.f[RX][R.jp], a.P.f[RY][R.jp], a.P.f[RZ][R.jp]);
+      dncut = a.cp.dncut;
+    }
+    contact = d.c;
+    if (a.cohesive) contact = (contact || d.dn <= dncut);
+    if (!contact) {
+      const V3 z = mk(0, 0, 0);
+      pwrite(a, k, z, z, z, z, z);
+    } else if (a.cohesive && d.dn >= 0) {
+      const dem_contact_params& hkp = is_pp ? a.cp : a.cpd;
+      const double fn_value = (hkp.fc / hkp.dncut) * d.dn - hkp.fc;
+      const V3 f = mk(0, 0, 0) + fn_value * d.n;
+      const V3 ti = cross(d.cp - ri, f) + mo;
+      if (!is_pp) {
+        pwrite(a, k, mk(0, 0, 0), mo, f, ti, mk(0, 0, 0));
+      } else {
+        const V3 tj = cross(d.cp - rj, -f) + (-mo);
+        if (swap) pwrite(a, k, mk(0, 0, 0), mo, -f, tj, ti);
+        else pwrite(a, k, mk(0, 0, 0), mo, f, ti, tj);
+      }
+    } else {
+      heavy = true;
+    }
+  }
+  const uint32_t pos = warp_append2(heavy, a.cnt + 1);
+  if (heavy) {
+    a.L2[pos] = (uint32_t)k;
+    a.D[0][pos] = d.dn;
+    a.D[1][pos] = d.n.x;
+    a.D[2][pos] = d.n.y;
+    a.D[3][pos] = d.n.z;
+    a.D[4][pos] = d.cp.x;
+    a.D[5][pos] = d.cp.y;
+    a.D[6][pos] = d.cp.z;
+  }
+}
+
+__global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
+  const uint64_t n2 = a.cnt[1];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a.n_active = n2;
+  const uint64_t stride = (uint64_t)gridDim.x * PT;
+  for (uint64_t w = (uint64_t)blockIdx.x * PT + threadIdx.x; w < n2; w += stride) {
+    const uint32_t k = a.L2[w];
+    const double dn = a.D[0][w];
+    const V3 n = mk(a.D[1][w], a.D[2][w], a.D[3][w]);
+    const V3 cpos = mk(a.D[4][w], a.D[5][w], a.D[6][w]);
+    const uint32_t meta = a.I.meta[k];
+    V3 ft = mk(a.I.ft[0][k], a.I.ft[1][k], a.I.ft[2][k]);
+    V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+    V3 f = mk(0, 0, 0);
+    if (meta_type(meta) > DEM_ITYPE_EDGE_EDGE) {
+      const uint32_t p = a.I.owner[k];
+      const DriverDev& d = a.drv[a.I.partner[k]];
+      const V3 r = ldv(a.P, RX, p), v = ldv(a.P, VX, p), w_ = ldv(a.P, WX, p);
+      const double meff = a.P.f[MASS][p];
+      contact_force_core(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, r, v, f, mo, w_,
+                         mk(d.center[0], d.center[1], d.center[2]), mk(d.vel[0], d.vel[1], d.vel[2]),
+                         mk(d.vrot[0], d.vrot[1], d.vrot[2]));
+      pwrite(a, k, ft, mo, f, cross(cpos - r, f) + mo, mk(0, 0, 0));
+      continue;
+    }
+    const Roles R = roles(a, k);
+    const V3 r_i = ldv(a.P, RX, R.ip), r_j = ldv(a.P, RX, R.jp);
+    const V3 v_i = ldv(a.P, VX, R.ip), v_j = ldv(a.P, VX, R.jp);
+    const V3 w_i = ldv(a.P, WX, R.ip), w_j = ldv(a.P, WX, R.jp);
+    const double m_i = a.P.f[MASS][R.ip], m_j = a.P.f[MASS][R.jp];
+    const double meff = (m_i * m_j) / (m_i + m_j);
+    contact_force_core(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, r_i, v_i, f, mo, w_i, r_j, v_j, w_j);
+    const V3 t_i = cross(cpos - r_i, f) + mo;
+    const V3 t_j = cross(cpos - r_j, -f) + (-mo);
+    if ((meta >> 15) & 1u)
+      pwrite(a, k, ft, mo, -f, t_j, t_i);
+    else
+      pwrite(a, k, ft, mo, f, t_i, t_j);
+  }
+}
+
+PolyArgs make_pargs(dem_ctx* c) {
+  PolyArgs a;
+  a.P = c->P[c->pcur];
+  a.n = c->n;
+  a.shapes = (const ShapeDev*)c->shapes_dev;
+  a.MV = c->MV;
+  a.vx = c->vtx[0];
+  a.vy = c->vtx[1];
+  a.vz = c->vtx[2];
+  a.bx = c->bvtx[0];
+  a.by = c->bvtx[1];
+  a.bz = c->bvtx[2];
+  a.obb = c->pobb;
+  return a;
+}
+}  // namespace
+
+// vertices (+ displacement flag, or + backup and world OBBs at a rebuild)
+int launch_poly_vertices(dem_ctx* c, int mode) {
+  if (!c->n) return DEM_OK;
+  ProfScope ps(c, K_PROLOG, 1);
+  const PolyArgs a = make_pargs(c);
+  const double md = c->prm.rcut_inc * 0.5;
+  if (mode == 1) {
+    DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars, 0, sizeof(unsigned long long), c->stream));
+    k_poly_vertices<true, false><<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, md * md, c->d_scalars);
+  } else if (mode == 2) {
+    k_poly_vertices<false, true><<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, 0.0, nullptr);
+  } else {
+    k_poly_vertices<false, false><<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, 0.0, nullptr);
+  }
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+// Units + SAT; returns the number of units in *nu (host sync).
+int launch_poly_units(dem_ctx* c, uint64_t* nu_out, int (*grow_units)(dem_ctx*, uint64_t)) {
+  UnitArgs a;
+  a.P = c->P[c->pcur];
+  a.n = c->n;
+  a.g = c->grid;
+  a.cell_start = c->cell_start;
+  a.cell_of = c->cell_of;
+  a.drv = c->drv_dev;
+  a.ndrv = c->ndrv;
+  a.shapes = (const ShapeDev*)c->shapes_dev;
+  a.rV = c->prm.rcut_inc;
+  const double nd = 2 * c->rad_max + c->prm.rcut_inc;
+  a.rcut2 = nd * nd;
+  a.xr = c->crel[0];
+  a.yr = c->crel[1];
+  a.zr = c->crel[2];
+  a.rf = c->crel[3];
+  for (int d = 0; d < 3; d++) a.csz[d] = (float)c->grid.csz[d];
+  a.skin_f = (float)c->prm.rcut_inc;
+  a.f32 = c->prm.fp32_broad_phase;
+  {
+    ProfScope ps(c, K_BROAD_COUNT, 1);
+    k_unit_count<<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, c->pcnt);
+  }
+  int rc = scan_exclusive_u32(c, c->pcnt, c->u_off, c->n);
+  if (rc) return rc;
+  uint32_t nu = 0;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(&nu, c->u_off + c->n, 4, cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if ((rc = grow_units(c, nu))) return rc;
+  ProfScope ps(c, K_BROAD_FILL, 2);
+  k_unit_fill<<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, c->u_off, c->u_owner, c->u_partner, c->u_pid, c->u_kind);
+  if (nu)
+    k_unit_sat<<<grid_for(nu, PT), PT, 0, c->stream>>>(nu, c->u_owner, c->u_partner, c->u_kind, c->pobb,
+                                                       c->prm.rcut_inc, c->u_pass);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  *nu_out = nu;
+  return DEM_OK;
+}
+
+static FeatArgs make_fargs(dem_ctx* c, uint64_t nu) {
+  FeatArgs a;
+  a.P = c->P[c->pcur];
+  a.shapes = (const ShapeDev*)c->shapes_dev;
+  a.drv = c->drv_dev;
+  a.MV = c->MV;
+  a.vx = c->vtx[0];
+  a.vy = c->vtx[1];
+  a.vz = c->vtx[2];
+  a.obb = c->pobb;
+  a.rV = c->prm.rcut_inc;
+  a.nu = nu;
+  a.u_owner = c->u_owner;
+  a.u_partner = c->u_partner;
+  a.u_pid = c->u_pid;
+  a.u_kind = c->u_kind;
+  a.pass = c->u_pass;
+  a.fcnt = c->f_cnt;
+  a.foff = c->f_off;
+  a.dst = c->I[1 - c->icur];
+  a.old = c->I[c->icur];
+  a.old_off = c->own_off[c->icur];
+  a.perm = c->perm;
+  a.have_old = c->hist_valid ? 1 : 0;
+  return a;
+}
+
+int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total) {
+  FeatArgs a = make_fargs(c, nu);
+  const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
+  {
+    ProfScope ps(c, K_BROAD_COUNT, nu ? 1 : 0);
+    if (nu) k_features<false><<<blocks, PT, 0, c->stream>>>(a);
+  }
+  int rc = scan_exclusive_u32(c, c->f_cnt, c->f_off, nu);
+  if (rc) return rc;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(total, c->f_off + nu, 4, cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return DEM_OK;
+}
+
+int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
+  FeatArgs a = make_fargs(c, nu);
+  const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
+  ProfScope ps(c, K_BROAD_FILL, 2);
+  if (nu) k_features<true><<<blocks, PT, 0, c->stream>>>(a);
+  k_own_from_units<<<grid_for(c->n + 1, 256), 256, 0, c->stream>>>(c->n, c->u_off, c->f_off, c->own_off[1 - c->icur]);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+int launch_contact_poly(dem_ctx* c) {
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 3, 0, 2 * sizeof(unsigned long long), c->stream));
+  ProfScope ps(c, K_CONTACT, 2);
+  PCArgs a;
+  a.P = c->P[c->pcur];
+  a.I = c->I[c->icur];
+  a.R = c->R;
+  a.ni = c->ni;
+  a.shapes = (const ShapeDev*)c->shapes_dev;
+  a.drv = c->drv_dev;
+  a.MV = c->MV;
+  a.vx = c->vtx[0];
+  a.vy = c->vtx[1];
+  a.vz = c->vtx[2];
+  a.cp = c->prm.config;
+  a.cpd = c->prm.config_driver;
+  a.dt = c->prm.dt;
+  a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
+  a.L2 = c->L2;
+  for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];
+  a.cnt = c->d_scalars + 3;
+  a.n_active = c->d_scalars + 1;
+  if (c->ni) k_pdetect<<<grid_for(c->ni, PT), PT, 0, c->stream>>>(a);
+  k_phooke<<<(unsigned)c->num_sms * 8u, PT, 0, c->stream>>>(a);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+}  // namespace dem

@@ -76,7 +76,7 @@ extern "C" int dem_generate_rsa_spheres(const dem_rsa_spec* sp, dem_particles* o
   const double L[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
   const uint64_t max_att = sp->max_attempts ? sp->max_attempts : 64;
   for (uint64_t k = 0; k < n; k++) {
-    const double rk = sp->rmin == sp->rmax ? sp->rmin : rng.uniform(sp->rmin, sp->rmax);
+    const double rk = sp->radii ? sp->radii[k] : (sp->rmin == sp->rmax ? sp->rmin : rng.uniform(sp->rmin, sp->rmax));
     uint64_t att = 0;
     for (;;) {
       double p[3];

@@ -7,7 +7,12 @@ reference operator, under the reference's operator name:
 method                          reference operator (exaDEM / exaNBody)
 =============================  ==================================================
 ``update_particle_neighbors``   move_particles + chunk_neighbors_contact +
-                                nbh_sphere + classify_interactions + backup_r
+                                nbh_sphere (or nbh_polyhedron) + classify_interactions
+                                + backup_r / backup_dem
+``set_shapes``                  shape files of the deck (.shp)
+``compute_vertices``            compute_vertices
+``vertex_displ_over``           vertex_displ_over
+``contact_polyhedron``          contact_polyhedron / contact_singlemat_polyhedron_hooke*
 ``particle_displ_over``         particle_displ_over
 ``reset_force_moment``          reset_force_moment
 ``gravity_force``               gravity_force
@@ -151,6 +156,25 @@ class System:
                        (C.c_double * 3)(*vrot))
         self._check(self.b.register_cylinder(self.h, C.byref(c)), "register_cylinder")
 
+    def set_shapes(self, shapes: list) -> None:
+        """shapes: dicts with vertices (nv,3), edges (ne,2), faces (list of vertex lists), radius,
+        obb = dict(center, e1, e2, e3, extent) -- exaDEM's .shp content."""
+        keep = []
+        arr = (A.Shape * len(shapes))()
+        for k, sh in enumerate(shapes):
+            v = np.ascontiguousarray(np.asarray(sh["vertices"], dtype=np.float64).reshape(-1))
+            e = np.ascontiguousarray(np.asarray(sh["edges"], dtype=np.int32).reshape(-1))
+            fs = np.ascontiguousarray(np.array([len(f) for f in sh["faces"]], dtype=np.int32))
+            fv = np.ascontiguousarray(np.concatenate([np.asarray(f, dtype=np.int32) for f in sh["faces"]]))
+            keep += [v, e, fs, fv]
+            o = sh["obb"]
+            arr[k] = A.Shape(len(v) // 3, len(e) // 2, len(fs), A.ptr(v), A.ptr(e, C.POINTER(C.c_int32)),
+                             A.ptr(fs, C.POINTER(C.c_int32)), A.ptr(fv, C.POINTER(C.c_int32)), float(sh["radius"]),
+                             (C.c_double * 3)(*o["center"]), (C.c_double * 3)(*o["e1"]), (C.c_double * 3)(*o["e2"]),
+                             (C.c_double * 3)(*o["e3"]), (C.c_double * 3)(*o["extent"]))
+        self._check(self.b.set_shapes(self.h, arr, len(shapes)), "set_shapes")
+        self._shapes_keep = keep
+
     def particles(self, sort_by_id: bool = True) -> dict:
         a = {f: np.zeros(self.n) for f in A.PARTICLE_FIELDS}
         a["id"] = np.zeros(self.n, dtype=np.uint64)
@@ -180,6 +204,17 @@ class System:
 
     def contact_sphere(self) -> None:
         self._check(self.b.contact_sphere(self.h), "contact_sphere")
+
+    def contact_polyhedron(self) -> None:
+        self._check(self.b.contact_polyhedron(self.h), "contact_polyhedron")
+
+    def compute_vertices(self) -> None:
+        self._check(self.b.compute_vertices(self.h), "compute_vertices")
+
+    def vertex_displ_over(self) -> bool:
+        r = C.c_int()
+        self._check(self.b.vertex_displ_over(self.h, C.byref(r)), "vertex_displ_over")
+        return bool(r.value)
 
     def force_to_accel(self) -> None:
         self._check(self.b.force_to_accel(self.h), "force_to_accel")
@@ -265,6 +300,12 @@ OPERATORS = {
     "contact_singlemat_sphere_hooke": System.contact_sphere,
     "contact_singlemat_sphere_hooke_none": System.contact_sphere,
     "contact_singlemat_sphere_hooke_cohesive": System.contact_sphere,
+    "nbh_polyhedron": System.update_particle_neighbors,
+    "contact_polyhedron": System.contact_polyhedron,
+    "contact_singlemat_polyhedron_hooke": System.contact_polyhedron,
+    "contact_singlemat_polyhedron_hooke_none": System.contact_polyhedron,
+    "compute_vertices": System.compute_vertices,
+    "vertex_displ_over": System.vertex_displ_over,
     "force_to_accel": System.force_to_accel,
     "combined_compute_prolog": System.combined_compute_prolog,
     "combined_compute_epilog": System.combined_compute_epilog,

@@ -30,6 +30,7 @@ class Workload:
     cylinders: list = field(default_factory=list)  # kwargs of System.register_cylinder
     steps: int = 1000
     info: dict = field(default_factory=dict)
+    shapes: list = None  # polyhedron shapes (System.set_shapes), None for spheres
 
     @property
     def n(self) -> int:
@@ -38,6 +39,8 @@ class Workload:
     def build(self, system_factory=None) -> System:
         """Creates a System (native by default) loaded with this workload."""
         s = system_factory(self.params) if system_factory else System(self.params)
+        if self.shapes:
+            s.set_shapes(self.shapes)
         s.set_particles(self.particles)
         for kw in self.surfaces:
             s.register_surface(**kw)
@@ -47,7 +50,7 @@ class Workload:
 
 
 def rsa(n, rmin, rmax, density, lo, hi, periodic=(0, 0, 0), grow_axis=-1, seed=1, vmin=0.0, vmax=0.0,
-        region=0, cyl_center=(0.0, 0.0), cyl_radius=0.0, max_attempts=64, id_offset=0):
+        region=0, cyl_center=(0.0, 0.0), cyl_radius=0.0, max_attempts=64, id_offset=0, radii=None):
     lib = A.load()
     spec = A.RsaSpec()
     spec.n = n
@@ -63,6 +66,8 @@ def rsa(n, rmin, rmax, density, lo, hi, periodic=(0, 0, 0), grow_axis=-1, seed=1
     spec.seed = seed
     spec.max_attempts = max_attempts
     spec.id_offset = id_offset
+    if radii is not None:
+        spec.radii = A.ptr(radii)
     arr = empty_particles(n)
     st = A.particles_struct(arr, n)
     top = C.c_double(0.0)
@@ -140,3 +145,223 @@ def spheres_drum(n=20_000, rmin=0.45, rmax=0.55, fill=0.30, density=2.0, length=
                     **flags)
     cyl = dict(radius=R, axis=(1.0, 0.0, 1.0), center=(c, 0.0, c), vrot=(0.0, omega, 0.0))
     return Workload("spheres_drum", p, arr, cylinders=[cyl], steps=steps, info={"drum_radius": R, "length": length})
+
+
+# ------------------------------------------------------------------ polyhedra
+def _sym_eigen(C):
+    """Jacobi eigen decomposition of a symmetric 3x3 matrix, restating
+    mat9::sym_eigen (src/shape/include/exaDEM/type/mat9.hpp:278-376).
+    C is a flat list of 9 floats (row major); returns (V flat 9, D 3)."""
+    A = list(C)
+    V = [1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0]
+    B = [A[0], A[4], A[8]]
+    D = [A[0], A[4], A[8]]
+    Z = [0.0, 0.0, 0.0]
+    for sweep in range(1, 51):
+        sm = abs(A[1]) + abs(A[2]) + abs(A[5])
+        if abs(sm) < 1.0e-15:
+            return V, D
+        thresh = sm * 0.2 / 9.0 if sweep < 4 else 0.0
+        for p in range(2):
+            for q in range(p + 1, 3):
+                g = 100.0 * abs(A[p * 3 + q])
+                if sweep > 4 and g < 1.0e-15:
+                    A[p * 3 + q] = 0.0
+                elif abs(A[p * 3 + q]) > thresh:
+                    h = D[q] - D[p]
+                    if g < 1.0e-20:
+                        t = A[p * 3 + q] / h
+                    else:
+                        theta = 0.5 * h / A[p * 3 + q]
+                        t = 1.0 / (abs(theta) + math.sqrt(1.0 + theta * theta))
+                        if theta < 0.0:
+                            t = -t
+                    c = 1.0 / math.sqrt(1.0 + t * t)
+                    s = t * c
+                    tau = s / (1.0 + c)
+                    h = t * A[p * 3 + q]
+                    Z[p] -= h
+                    Z[q] += h
+                    D[p] -= h
+                    D[q] += h
+                    A[p * 3 + q] = 0.0
+                    for j in range(0, p):
+                        g, h = A[j * 3 + p], A[j * 3 + q]
+                        A[j * 3 + p] = g - s * (h + g * tau)
+                        A[j * 3 + q] = h + s * (g - h * tau)
+                    for j in range(p + 1, q):
+                        g, h = A[p * 3 + j], A[j * 3 + q]
+                        A[p * 3 + j] = g - s * (h - g * tau)
+                        A[j * 3 + q] = h + s * (g - h * tau)
+                    for j in range(q + 1, 3):
+                        g, h = A[p * 3 + j], A[q * 3 + j]
+                        A[p * 3 + j] = g - s * (h + g * tau)
+                        A[q * 3 + j] = h + s * (g - h * tau)
+                    for j in range(3):
+                        g, h = V[j * 3 + p], V[j * 3 + q]
+                        V[j * 3 + p] = g - s * (h + g * tau)
+                        V[j * 3 + q] = h + s * (g - h * tau)
+        B = [B[k] + Z[k] for k in range(3)]
+        D = list(B)
+        Z = [0.0, 0.0, 0.0]
+    return V, D
+
+
+def build_obb(vertices, radius):
+    """Shape OBB from the covariance of the vertices, restating build_OBB
+    (src/shape/include/exaDEM/shape_prepro.hpp:26-97); extents include the radius."""
+    vs = [tuple(map(float, v)) for v in vertices]
+    n = len(vs)
+    mu = [0.0, 0.0, 0.0]
+    for v in vs:
+        mu = [mu[0] + v[0], mu[1] + v[1], mu[2] + v[2]]
+    mu = [mu[0] / n, mu[1] / n, mu[2] / n]
+    cxx = cxy = cxz = cyy = cyz = czz = 0.0
+    for p in vs:
+        cxx += p[0] * p[0] - mu[0] * mu[0]
+        cxy += p[0] * p[1] - mu[0] * mu[1]
+        cxz += p[0] * p[2] - mu[0] * mu[2]
+        cyy += p[1] * p[1] - mu[1] * mu[1]
+        cyz += p[1] * p[2] - mu[1] * mu[2]
+        czz += p[2] * p[2] - mu[2] * mu[2]
+    V, _ = _sym_eigen([cxx, cxy, cxz, cxy, cyy, cyz, cxz, cyz, czz])
+
+    def normalized(a):  # vec3::normalize (type/vec3.hpp:257-265)
+        n2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2]
+        if n2 > 0.0:
+            inv = 1.0 / math.sqrt(n2)
+            return [a[0] * inv, a[1] * inv, a[2] * inv]
+        return list(a)
+
+    r = normalized([V[0], V[3], V[6]])
+    u = normalized([V[1], V[4], V[7]])
+    f = normalized([V[2], V[5], V[8]])
+    dot = lambda a, b: a[0] * b[0] + a[1] * b[1] + a[2] * b[2]
+    mn, mx = [1e20] * 3, [-1e20] * 3
+    for p in vs:
+        pp = [dot(r, p), dot(u, p), dot(f, p)]
+        mn = [min(mn[k], pp[k]) for k in range(3)]
+        mx = [max(mx[k], pp[k]) for k in range(3)]
+    half = [0.5 * (mx[k] + mn[k]) for k in range(3)]
+    center = [V[0] * half[0] + V[1] * half[1] + V[2] * half[2], V[3] * half[0] + V[4] * half[1] + V[5] * half[2],
+              V[6] * half[0] + V[7] * half[1] + V[8] * half[2]]
+    extent = [0.5 * (mx[k] - mn[k]) + radius for k in range(3)]
+    return {"center": center, "e1": r, "e2": u, "e3": f, "extent": extent}
+
+
+def _shape(name, vertices, edges, faces, radius, volume, i_over_m):
+    v = np.asarray(vertices, dtype=np.float64)
+    return {"name": name, "vertices": v, "edges": np.asarray(edges, dtype=np.int32), "faces": faces,
+            "radius": radius, "obb": build_obb(v, radius), "volume": volume, "i_over_m": i_over_m,
+            "max_rcut": float(max(np.linalg.norm(x) for x in v) + radius)}
+
+
+def shape_cube(a=1.0, radius=0.01):
+    h = 0.5 * a
+    v = [[-h, -h, -h], [h, -h, -h], [h, h, -h], [-h, h, -h], [-h, -h, h], [h, -h, h], [h, h, h], [-h, h, h]]
+    e = [[0, 1], [1, 2], [2, 3], [3, 0], [4, 5], [5, 6], [6, 7], [7, 4], [0, 4], [1, 5], [2, 6], [3, 7]]
+    f = [[0, 3, 2, 1], [4, 5, 6, 7], [0, 1, 5, 4], [1, 2, 6, 5], [2, 3, 7, 6], [3, 0, 4, 7]]
+    return _shape("Cube", v, e, f, radius, a ** 3, a * a / 6.0)
+
+
+def shape_tetrahedron(a=1.2, radius=0.01):
+    s = a / (2.0 * math.sqrt(2.0))
+    v = [[s, s, s], [s, -s, -s], [-s, s, -s], [-s, -s, s]]
+    e = [[0, 1], [0, 2], [0, 3], [1, 2], [1, 3], [2, 3]]
+    f = [[0, 1, 2], [0, 3, 1], [0, 2, 3], [1, 3, 2]]
+    return _shape("Tetrahedron", v, e, f, radius, a ** 3 / (6.0 * math.sqrt(2.0)), a * a / 20.0)
+
+
+def shape_octahedron(a=1.0, radius=0.01):
+    d = a / math.sqrt(2.0)
+    v = [[d, 0, 0], [-d, 0, 0], [0, d, 0], [0, -d, 0], [0, 0, d], [0, 0, -d]]
+    e = [[0, 2], [2, 1], [1, 3], [3, 0], [0, 4], [2, 4], [1, 4], [3, 4], [0, 5], [2, 5], [1, 5], [3, 5]]
+    f = [[0, 2, 4], [2, 1, 4], [1, 3, 4], [3, 0, 4], [0, 5, 2], [2, 5, 1], [1, 5, 3], [3, 5, 0]]
+    return _shape("Octahedron", v, e, f, radius, math.sqrt(2.0) / 3.0 * a ** 3, a * a / 10.0)
+
+
+def polyhedra_floor(n=200_000, side=None, phi=0.35, density=0.02, seed=3, steps=2000, dt=1e-4, skin=0.05,
+                    radius=0.01, walls=True, **flags) -> Workload:
+    """Config 3: n convex polyhedra, an equal mix of cubes (edge 1.0), regular
+    tetrahedra (edge 1.2) and octahedra (edge 1.0) with Minkowski radius 0.01;
+    orientations uniform on SU(2) (normalised 4-D Gaussian); positions by random
+    sequential addition of the circumscribed spheres (solid fraction phi of
+    those spheres, moving-window RSA as for spheres), a floor wall and four side
+    walls; Hooke kn=1e5, kt=8e4, mu=0.5, damp 0.9, dt=1e-4, gravity deposition.
+    Open values: density 0.02 (the reference's polyhedron examples), zero initial
+    velocity, skin 0.05, footprint side = (n / 14)^(1/2) * 1.0 (about 120 for 200k)."""
+    shapes = [shape_cube(1.0, radius), shape_tetrahedron(1.2, radius), shape_octahedron(1.0, radius)]
+    if side is None:
+        side = max(8.0, math.sqrt(n / 14.0))
+    types = (np.arange(n) % 3).astype(np.uint32)
+    radii = np.array([shapes[t]["max_rcut"] for t in types], dtype=np.float64)
+    rmax = float(radii.max())
+    arr, top = rsa(n, float(radii.min()), rmax, density, (0, 0, 0), (side, side, 4 * rmax), grow_axis=2, seed=seed,
+                   max_attempts=400, radii=np.ascontiguousarray(radii))
+    rng = np.random.default_rng(seed)
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1)[:, None]
+    arr["qw"], arr["qx"], arr["qy"], arr["qz"] = (np.ascontiguousarray(q[:, k]) for k in range(4))
+    arr["type"] = types
+    arr["radius"] = radii
+    vol = np.array([shapes[t]["volume"] for t in types])
+    iom = np.array([shapes[t]["i_over_m"] for t in types])
+    arr["mass"] = density * vol
+    for ax in ("inertiax", "inertiay", "inertiaz"):
+        arr[ax] = arr["mass"] * iom
+    arr["homothety"] = np.ones(n)
+    for k in ("vx", "vy", "vz"):
+        arr[k] = np.zeros(n)
+    cfg = dict(kn=1e5, kt=8e4, kr=0.0, mu=0.5, damp_rate=0.9)
+    hi = (side, side, top + 2 * rmax)
+    p = make_params((0, 0, 0), hi, (0, 0, 0), rcut_inc=skin, dt=dt, gravity=(0, 0, -9.81), config=cfg,
+                    config_driver=cfg, **flags)
+    surfaces = [dict(offset=0.0, normal=(0.0, 0.0, 1.0))]
+    if walls:
+        surfaces += [dict(offset=0.0, normal=(1.0, 0.0, 0.0)), dict(offset=side, normal=(1.0, 0.0, 0.0)),
+                     dict(offset=0.0, normal=(0.0, 1.0, 0.0)), dict(offset=side, normal=(0.0, 1.0, 0.0))]
+    sphere_vol = float(np.sum(4.0 / 3.0 * math.pi * radii ** 3))
+    w = Workload("polyhedra_floor", p, arr, surfaces=surfaces, steps=steps,
+                 info={"height": top, "phi_spheres": sphere_vol / (side * side * top), "side": side})
+    w.shapes = shapes
+    return w
+
+
+def polyhedra_lattice(nx=8, ny=8, nz=6, spacing=1.3, density=1.0, seed=7, radius=0.01, vmax=0.5, dt=1e-4,
+                      skin=0.05, kn=1e4, **flags) -> Workload:
+    """Dense test arrangement: polyhedra (cube / tetrahedron / octahedron mix) on
+    a cubic lattice whose spacing is below the circumscribed diameters, with
+    random orientations and velocities, inside a walled box.  Many vertex,
+    edge and face features are within the skin from the first step."""
+    shapes = [shape_cube(1.0, radius), shape_tetrahedron(1.2, radius), shape_octahedron(1.0, radius)]
+    rng = np.random.default_rng(seed)
+    n = nx * ny * nz
+    g = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    pos = (g + 1.0) * spacing + rng.uniform(-0.05, 0.05, (n, 3))
+    types = rng.integers(0, 3, n).astype(np.uint32)
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1)[:, None]
+    arr = empty_particles(n)
+    arr["rx"], arr["ry"], arr["rz"] = (np.ascontiguousarray(pos[:, k]) for k in range(3))
+    arr["qw"], arr["qx"], arr["qy"], arr["qz"] = (np.ascontiguousarray(q[:, k]) for k in range(4))
+    arr["vx"], arr["vy"], arr["vz"] = (rng.uniform(-vmax, vmax, n) for _ in range(3))
+    arr["vrotx"], arr["vroty"], arr["vrotz"] = (rng.uniform(-1.0, 1.0, n) for _ in range(3))
+    arr["type"] = types
+    arr["id"] = np.arange(n, dtype=np.uint64)
+    arr["radius"] = np.array([shapes[t]["max_rcut"] for t in types])
+    vol = np.array([shapes[t]["volume"] for t in types])
+    iom = np.array([shapes[t]["i_over_m"] for t in types])
+    arr["mass"] = density * vol
+    for ax in ("inertiax", "inertiay", "inertiaz"):
+        arr[ax] = arr["mass"] * iom
+    arr["homothety"] = np.ones(n)
+    hi = ((nx + 1) * spacing, (ny + 1) * spacing, (nz + 1) * spacing)
+    cfg = dict(kn=kn, kt=0.8 * kn, kr=0.0, mu=0.5, damp_rate=0.9)
+    p = make_params((0, 0, 0), hi, (0, 0, 0), rcut_inc=skin, dt=dt, gravity=(0, 0, -9.81), config=cfg,
+                    config_driver=cfg, **flags)
+    surfaces = [dict(offset=0.0, normal=(0.0, 0.0, 1.0)), dict(offset=0.0, normal=(1.0, 0.0, 0.0)),
+                dict(offset=hi[0], normal=(1.0, 0.0, 0.0)), dict(offset=0.0, normal=(0.0, 1.0, 0.0)),
+                dict(offset=hi[1], normal=(0.0, 1.0, 0.0))]
+    w = Workload("polyhedra_lattice", p, arr, surfaces=surfaces, steps=100)
+    w.shapes = shapes
+    return w

@@ -37,6 +37,7 @@ typedef struct dem_rsa_spec {
   uint64_t seed;
   uint64_t max_attempts;
   uint64_t id_offset;     /* ids are id_offset + k                           */
+  const double* radii;    /* optional: radius of sphere k (overrides rmin/rmax draws) */
 } dem_rsa_spec;
 
 /* Fills out->rx..rz, radius, mass, inertia*, vx..vz, qw (=1), id for
