@@ -44,7 +44,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
-    ap.add_argument("--n", type=int, default=2_000_000)
+    ap.add_argument("--n", type=int, default=None, help="particle count (default: the workload's)")
+    ap.add_argument("--workload", default="spheres", choices=["spheres", "polyhedra", "polyhedra_dense"],
+                    help="spheres: 2M spheres on a floor (headline); polyhedra: 200k polyhedra deposition; "
+                         "polyhedra_dense: polyhedra on a dense lattice")
     ap.add_argument("--plain", action="store_true", help="plain FP64 path (no FP32 screening)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -149,7 +152,23 @@ def workload(args):
     from exadem_gb300 import workloads as W
 
     opt = 0 if args.plain else 1
-    return W.spheres_floor(n=args.n, fp32_contact_screen=opt, fused_step=opt, fp32_broad_phase=opt)
+    flags = dict(fp32_contact_screen=opt, fused_step=opt, fp32_broad_phase=opt)
+    if args.workload == "polyhedra":
+        return W.polyhedra_floor(n=args.n or 200_000, **flags)
+    if args.workload == "polyhedra_dense":
+        side = round((args.n or 200_000) ** (1.0 / 3.0))
+        return W.polyhedra_lattice(nx=side, ny=side, nz=side, **flags)
+    return W.spheres_floor(n=args.n or 2_000_000, **flags)
+
+
+WORKLOAD_DESC = {
+    "spheres": "spheres_floor: 2M polydisperse spheres r~U[0.4,0.6], periodic x/y, floor wall, "
+               "Hooke+cohesion(kc=1e3,dncut=0.01)+kr=100, dt=5e-4",
+    "polyhedra": "polyhedra_floor: 200k cubes/tetrahedra/octahedra (Minkowski 0.01), RSA of circumscribed "
+                 "spheres at 0.35, floor + side walls, Hooke kn=1e5 kt=8e4 mu=0.5, dt=1e-4",
+    "polyhedra_dense": "polyhedra_lattice: cubes/tetrahedra/octahedra on a lattice of spacing 1.3, random "
+                       "orientations, Hooke kn=1e4, dt=1e-4",
+}
 
 
 def cpu_baseline(w, budget_s: float = 20.0):
@@ -240,8 +259,12 @@ def run_native(args, rank, world, local, dist):
         out = {k: torch.empty(v.shape, dtype=torch.from_numpy(v).dtype, pin_memory=True).numpy()
                for k, v in w.particles.items()}
         s2 = System(w.params)
+        if w.shapes:
+            s2.set_shapes(w.shapes)
         for kw in w.surfaces:
             s2.register_surface(**kw)
+        for kw in w.cylinders:
+            s2.register_cylinder(**kw)
         h2d = sum(v.nbytes for v in pinned.values())
         barrier(dist)
         t0 = time.perf_counter()
@@ -269,15 +292,13 @@ def run_native(args, rank, world, local, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded random sequential addition)",
-        "config": {"workload": "spheres_floor: 2M polydisperse spheres r~U[0.4,0.6], periodic x/y, floor wall, "
-                               "Hooke+cohesion(kc=1e3,dncut=0.01)+kr=100, dt=5e-4" if args.n == 2_000_000 else
-                   f"spheres_floor n={args.n}",
+        "config": {"workload": WORKLOAD_DESC[args.workload] if args.n is None else f"{args.workload} n={w.n}",
                    "n_particles": w.n,
                    "path": "plain FP64 operator kernels" if args.plain else
                            "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division",
                    "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
                    "parallelism": "replicas" if world > 1 else "single",
-                   "phi_achieved": round(w.info["phi_achieved"], 4)},
+                   "inputs": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in w.info.items()}},
         "roofline": {"bound": "hbm", "kernel": "contact", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni,
@@ -310,7 +331,8 @@ def run_reference(args, rank, world, local, dist):
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
             "ms_per_step": el * 1e3 / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded random sequential addition)", "impl": "reference",
-            "config": {"workload": f"spheres_floor n={w.n}", "n_particles": w.n},
+            "config": {"workload": WORKLOAD_DESC[args.workload] if args.n is None else f"{args.workload} n={w.n}",
+                       "n_particles": w.n},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": f"{steps} steps of the full workload (C++ restatement of the reference "
                                        f"CPU path; exaDEM itself cannot be built without exaNBody/onika/MPI)"},

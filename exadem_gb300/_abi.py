@@ -157,6 +157,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_reset_kernel_stats", [_CTX])
     _sig(lib, "dem_simulation_state_noalloc", [C.POINTER(Particles), PD, C.c_void_p])
     _sig(lib, "dem_selftest_division", [C.c_uint64, C.c_uint64, PU64, PU64])
+    _sig(lib, "dem_selftest_poly_decisions", [C.c_uint64, C.c_uint64, PU64])
 
 
 # Symbols declared in include/dem_hotpath.h and include/dem_workloads.h.
@@ -167,7 +168,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
             "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
-            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_set_shapes", "dem_compute_vertices",
+            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over"]
 
 _LIB = None

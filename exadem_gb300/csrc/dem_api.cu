@@ -194,7 +194,9 @@ void free_poly(dem_ctx* c) {
   for (int d = 0; d < 3; d++) {
     cudaFree(c->vtx[d]);
     cudaFree(c->bvtx[d]);
+    cudaFree(c->vrf[d]);
     c->vtx[d] = c->bvtx[d] = nullptr;
+    c->vrf[d] = nullptr;
   }
   cudaFree(c->pobb);
   cudaFree(c->u_off);
@@ -211,6 +213,7 @@ int alloc_poly(dem_ctx* c) {
   for (int d = 0; d < 3; d++) {
     DEM_CUDA_TRY(c, cudaMalloc(&c->vtx[d], need * 8));
     DEM_CUDA_TRY(c, cudaMalloc(&c->bvtx[d], need * 8));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->vrf[d], need * 4));
   }
   DEM_CUDA_TRY(c, cudaMalloc(&c->pobb, std::max<uint64_t>(c->pcap, 1) * 15 * 8));
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_off, (std::max<uint64_t>(c->pcap, 1) + 1) * 4));

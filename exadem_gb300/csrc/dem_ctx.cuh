@@ -84,6 +84,7 @@ struct dem_ctx {
   double* vtx[3] = {};                // world vertices, n*MV each
   double* bvtx[3] = {};               // vertices at the last rebuild
   double* pobb = nullptr;             // world OBB per particle (15 doubles)
+  float* vrf[3] = {};                 // FP32 vertices relative to the particle centre (rebuild time)
   uint64_t vcap = 0;
   uint32_t* u_off = nullptr;          // n+1 unit offsets per owner
   uint32_t* u_owner = nullptr;        // unit arrays (ucap each)

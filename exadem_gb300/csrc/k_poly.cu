@@ -23,6 +23,7 @@
 
 #include "contact_core.cuh"
 #include "poly_core.cuh"
+#include "poly_f32.cuh"
 
 namespace dem {
 namespace {
@@ -41,6 +42,9 @@ struct PolyArgs {
   double* by;
   double* bz;
   double* obb;  // 15 per particle
+  float* fx;    // FP32 vertices relative to the centre
+  float* fy;
+  float* fz;
 };
 
 // ---------------------------------------------------------------- vertices
@@ -67,6 +71,9 @@ __global__ void k_poly_vertices(PolyArgs a, double thr2, unsigned long long* fla
         a.bx[idx] = v.x;
         a.by[idx] = v.y;
         a.bz[idx] = v.z;
+        a.fx[idx] = (float)(v.x - p.x);
+        a.fy[idx] = (float)(v.y - p.y);
+        a.fz[idx] = (float)(v.z - p.z);
       }
     }
     if (Backup) {
@@ -283,6 +290,9 @@ struct FeatArgs {
   const uint32_t* old_off;
   const uint32_t* perm;
   int have_old;
+  const float* fvx;  // FP32 vertices relative to the particle centre
+  const float* fvy;
+  const float* fvz;
 };
 
 __device__ __forceinline__ VView vview(const FeatArgs& a, uint32_t s) {
@@ -343,15 +353,65 @@ __device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uin
   a.dst.mo[2][w] = h[5];
 }
 
+// ---------------------------------------------------------------- split precision
+// k_feat<Fill, true> decides every vertex gate and every feature test in FP32
+// first (poly_f32.cuh): a decided test has the FP64 result by construction, an
+// undecided one (its FP32 value within 8x its error bound of a threshold) runs
+// the FP64 function.  Only the rare undecided lanes touch the FP64 pipe.
+// exact FP64 filter of test (i, j) of segment seg (warp-uniform seg)
+__device__ __noinline__ bool exact_filter(int seg, int i, int j, double rV, const VView& va, double ra,
+                                          const ShapeDev& SA, const VView& vb, double rb, const ShapeDev& SB) {
+  switch (seg) {
+    case 0: return filter_vv(rV, va[i], ra, vb[j], rb);
+    case 1: return filter_ve(rV, va[i], ra, vb[SB.e[2 * j]], vb[SB.e[2 * j + 1]], rb);
+    case 2: return filter_ve(rV, vb[j], rb, va[SA.e[2 * i]], va[SA.e[2 * i + 1]], ra);
+    case 3: return filter_vf(rV, va[i], ra, vb, SB, j, rb);
+    case 4: return filter_vf(rV, vb[j], rb, va, SA, i, ra);
+    default:
+      return filter_ee(rV, va[SA.e[2 * i]], va[SA.e[2 * i + 1]], ra, vb[SB.e[2 * j]], vb[SB.e[2 * j + 1]], rb);
+  }
+}
+
+// FP32 decision of test (i, j) of segment seg (DEC_FALSE / DEC_TRUE / DEC_UNDECIDED)
+__device__ __noinline__ int decide_test(int seg, int i, int j, float R, float rV, float S, const FView& fa,
+                                        const ShapeDev& SA, const FView& fb, const ShapeDev& SB) {
+  switch (seg) {
+    case 0: return decide_vv(fa[i], fb[j], R, S);
+    case 1: return decide_ve(fa[i], fb[SB.e[2 * j]], fb[SB.e[2 * j + 1]], R, rV, S);
+    case 2: return decide_ve(fb[j], fa[SA.e[2 * i]], fa[SA.e[2 * i + 1]], R, rV, S);
+    case 3: return decide_vf(fa[i], fb, SB, j, R, S);
+    case 4: return decide_vf(fb[j], fa, SA, i, R, S);
+    default: return decide_ee(fa[SA.e[2 * i]], fa[SA.e[2 * i + 1]], fb[SB.e[2 * j]], fb[SB.e[2 * j + 1]], R, S);
+  }
+}
+
+__device__ __noinline__ int decide_gate_nf(const OBBf& o, F3 p, float rv, float S) { return decide_gate(o, p, rv, S); }
+
+__device__ __noinline__ bool vertex_gate(const OBBd& obb, V3 v, double rv) {
+  OBBd ov;
+  ov.c = v;
+  ov.e1 = mk(1, 0, 0);
+  ov.e2 = mk(0, 1, 0);
+  ov.e3 = mk(0, 0, 1);
+  ov.ext = mk(0, 0, 0);
+  obb_enlarge(ov, rv);
+  return obb_intersect(obb, ov);
+}
+
 // One warp per unit.  Fill = false: counts into fcnt; Fill = true: writes at foff.
-template <bool Fill>
-__global__ void __launch_bounds__(PT) k_features(FeatArgs a) {
+// The gated tests are processed segment by segment in InteractionPair order
+// (VV, VE, VE swap, VF, VF swap, EE) so every warp instruction runs a single
+// filter type.  F32: every gate and test is decided in FP32 first; the lanes
+// left undecided run the FP64 function.
+template <bool Fill, bool F32>
+__global__ void __launch_bounds__(PT) k_feat(FeatArgs a) {
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
   for (uint64_t u = warp; u < a.nu; u += nwarps) {
     uint32_t count = 0;
-    uint32_t base = Fill ? a.foff[u] : 0;
+    const uint32_t base = Fill ? a.foff[u] : 0;
     if (!a.pass[u]) {
       if (!Fill && lane == 0) a.fcnt[u] = 0;
       continue;
@@ -361,15 +421,14 @@ __global__ void __launch_bounds__(PT) k_features(FeatArgs a) {
     const double ha = a.P.f[HOM][A];
     const double ra = SA.r * ha;
     const VView va = vview(a, A);
-    if (a.u_kind[u]) {
-      // vertex - driver (add_driver_interaction): filter(rV + minkowski(h), vertex)
+    if (a.u_kind[u]) {  // vertex - driver (add_driver_interaction): filter(rV + minkowski(h), vertex)
       const uint32_t k = a.u_partner[u];
       const DriverDev& d = a.drv[k];
       const uint32_t type = d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER;
       const bool keep = lane < SA.nv && driver_reach(d, a.rV + ra, va[lane]);
       const unsigned m = __ballot_sync(0xffffffffu, keep);
       if (Fill) {
-        if (keep) write_feature(a, base + __popc(m & ((1u << lane) - 1u)), A, k, a.u_pid[u], type, 0, lane, 0xffffu);
+        if (keep) write_feature(a, base + __popc(m & lt), A, k, a.u_pid[u], type, 0, lane, 0xffffu);
       } else if (lane == 0) {
         a.fcnt[u] = __popc(m);
       }
@@ -387,84 +446,68 @@ __global__ void __launch_bounds__(PT) k_features(FeatArgs a) {
     obb_enlarge(obb_j, 0.5 * a.rV);
     obb_enlarge(obb_i, 0.5 * a.rV);
     obb_enlarge(obb_j, 0.5 * a.rV);
-    // per-vertex OBB gates (one lane per vertex)
+    FView fa{nullptr, nullptr, nullptr, f3(0.f, 0.f, 0.f)}, fb = fa;
+    float S = 0.f;
     bool ga = false, gb = false;
-    if (lane < SA.nv) {
-      OBBd ov;
-      ov.c = va[lane];
-      ov.e1 = mk(1, 0, 0);
-      ov.e2 = mk(0, 1, 0);
-      ov.e3 = mk(0, 0, 1);
-      ov.ext = mk(0, 0, 0);
-      obb_enlarge(ov, ra);
-      ga = obb_intersect(obb_j, ov);
-    }
-    if (lane < SB.nv) {
-      OBBd ov;
-      ov.c = vb[lane];
-      ov.e1 = mk(1, 0, 0);
-      ov.e2 = mk(0, 1, 0);
-      ov.e3 = mk(0, 0, 1);
-      ov.ext = mk(0, 0, 0);
-      obb_enlarge(ov, rb);
-      gb = obb_intersect(obb_i, ov);
+    if (F32) {
+      const V3 rA = mk(a.P.f[RX][A], a.P.f[RY][A], a.P.f[RZ][A]);
+      const V3 rB = mk(a.P.f[RX][B], a.P.f[RY][B], a.P.f[RZ][B]);
+      const F3 dR = f3((float)(rB.x - rA.x), (float)(rB.y - rA.y), (float)(rB.z - rA.z));
+      const uint64_t oA = (uint64_t)A * a.MV, oB = (uint64_t)B * a.MV;
+      fa = FView{a.fvx + oA, a.fvy + oA, a.fvz + oA, f3(0.f, 0.f, 0.f)};
+      fb = FView{a.fvx + oB, a.fvy + oB, a.fvz + oB, dR};
+      // S bounds every |coordinate| relative to A's centre: measured on the vertices
+      float sv = fmaxf(lane < SA.nv ? flen(fa[lane]) : 0.f, lane < SB.nv ? flen(fb[lane]) : 0.f);
+#pragma unroll
+      for (int o = 16; o; o >>= 1) sv = fmaxf(sv, __shfl_xor_sync(0xffffffffu, sv, o));
+      S = sv * 1.001f + (float)(ra + rb + a.rV);
+      const OBBf fi = obb_f32(obb_i, rA), fj = obb_f32(obb_j, rA);
+      const int da = lane < SA.nv ? decide_gate_nf(fj, fa[lane], (float)ra, S) : DEC_FALSE;
+      const int db = lane < SB.nv ? decide_gate_nf(fi, fb[lane], (float)rb, S) : DEC_FALSE;
+      ga = da == DEC_TRUE;
+      gb = db == DEC_TRUE;
+      if (da == DEC_UNDECIDED) ga = vertex_gate(obb_j, va[lane], ra);
+      if (db == DEC_UNDECIDED) gb = vertex_gate(obb_i, vb[lane], rb);
+    } else {
+      if (lane < SA.nv) ga = vertex_gate(obb_j, va[lane], ra);
+      if (lane < SB.nv) gb = vertex_gate(obb_i, vb[lane], rb);
     }
     const uint32_t gA = __ballot_sync(0xffffffffu, ga), gB = __ballot_sync(0xffffffffu, gb);
     const int nA = __popc(gA), nB = __popc(gB);
-    // segments in InteractionPair order: VV, VE, VE(swap), VF, VF(swap), EE
-    const uint32_t sVV = nA * SB.nv, sVE0 = nA * SB.ne, sVE1 = SA.ne * nB, sVF0 = nA * SB.nf, sVF1 = SA.nf * nB,
-                   sEE = SA.ne * SB.ne;
-    const uint32_t total = sVV + sVE0 + sVE1 + sVF0 + sVF1 + sEE;
-    for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-      const uint32_t t = t0 + lane;
-      bool keep = false;
-      uint32_t type = 0, swap = 0, osub = 0, psub = 0;
-      if (t < total) {
-        uint32_t r = t;
-        if (r < sVV) {
-          const int i = nth_bit(gA, r / SB.nv), j = r % SB.nv;
-          type = DEM_ITYPE_VERTEX_VERTEX;
-          osub = i;
-          psub = j;
-          keep = filter_vv(a.rV, va[i], ra, vb[j], rb);
-        } else if ((r -= sVV) < sVE0) {
-          const int i = nth_bit(gA, r / SB.ne), j = r % SB.ne;
-          type = DEM_ITYPE_VERTEX_EDGE;
-          osub = i;
-          psub = j;
-          keep = filter_ve(a.rV, va[i], ra, vb[SB.e[2 * j]], vb[SB.e[2 * j + 1]], rb);
-        } else if ((r -= sVE0) < sVE1) {
-          const int i = r / nB, j = nth_bit(gB, r % nB);  // A edge i, B vertex j
-          type = DEM_ITYPE_VERTEX_EDGE;
-          swap = 1;
-          osub = i;
-          psub = j;
-          keep = filter_ve(a.rV, vb[j], rb, va[SA.e[2 * i]], va[SA.e[2 * i + 1]], ra);
-        } else if ((r -= sVE1) < sVF0) {
-          const int i = nth_bit(gA, r / SB.nf), j = r % SB.nf;
-          type = DEM_ITYPE_VERTEX_FACE;
-          osub = i;
-          psub = j;
-          keep = filter_vf(a.rV, va[i], ra, vb, SB, j, rb);
-        } else if ((r -= sVF0) < sVF1) {
-          const int i = r / nB, j = nth_bit(gB, r % nB);  // A face i, B vertex j
-          type = DEM_ITYPE_VERTEX_FACE;
-          swap = 1;
-          osub = i;
-          psub = j;
-          keep = filter_vf(a.rV, vb[j], rb, va, SA, i, ra);
-        } else {
-          r -= sVF1;
-          const int i = r / SB.ne, j = r % SB.ne;
-          type = DEM_ITYPE_EDGE_EDGE;
-          osub = i;
-          psub = j;
-          keep = filter_ee(a.rV, va[SA.e[2 * i]], va[SA.e[2 * i + 1]], ra, vb[SB.e[2 * j]], vb[SB.e[2 * j + 1]], rb);
-        }
+    const float Rf = (float)(ra + rb + a.rV), rVf = (float)a.rV;
+#pragma unroll 1
+    for (int seg = 0; seg < 6; seg++) {
+      // rows x cols of the segment; rows of VV/VE/VF are gated A vertices, cols of VE/VF swap gated B vertices
+      int rows, cols;
+      switch (seg) {
+        case 0: rows = nA; cols = SB.nv; break;
+        case 1: rows = nA; cols = SB.ne; break;
+        case 2: rows = SA.ne; cols = nB; break;
+        case 3: rows = nA; cols = SB.nf; break;
+        case 4: rows = SA.nf; cols = nB; break;
+        default: rows = SA.ne; cols = SB.ne;
       }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (Fill && keep) write_feature(a, base + count + __popc(m & ((1u << lane) - 1u)), A, B, pid, type, swap, osub, psub);
-      count += __popc(m);
+      const uint32_t ns = (uint32_t)rows * (uint32_t)cols;
+      const uint32_t type = seg == 0 ? DEM_ITYPE_VERTEX_VERTEX
+                                     : (seg <= 2 ? DEM_ITYPE_VERTEX_EDGE : (seg <= 4 ? DEM_ITYPE_VERTEX_FACE
+                                                                                     : DEM_ITYPE_EDGE_EDGE));
+      const uint32_t swap = (seg == 2 || seg == 4) ? 1u : 0u;
+      for (uint32_t t0 = 0; t0 < ns; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        int i = 0, j = 0;
+        bool keep = false;
+        if (t < ns) {
+          const int r = (int)(t / (uint32_t)cols), c = (int)(t % (uint32_t)cols);
+          i = (seg == 0 || seg == 1 || seg == 3) ? nth_bit(gA, r) : r;
+          j = (seg == 2 || seg == 4) ? nth_bit(gB, c) : c;
+          const int d = F32 ? decide_test(seg, i, j, Rf, rVf, S, fa, SA, fb, SB) : DEC_UNDECIDED;
+          keep = d == DEC_TRUE;
+          if (d == DEC_UNDECIDED) keep = exact_filter(seg, i, j, a.rV, va, ra, SA, vb, rb, SB);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (Fill && keep) write_feature(a, base + count + __popc(m & lt), A, B, pid, type, swap, i, j);
+        count += __popc(m);
+      }
     }
     if (!Fill && lane == 0) a.fcnt[u] = count;
   }
@@ -701,6 +744,9 @@ PolyArgs make_pargs(dem_ctx* c) {
   a.by = c->bvtx[1];
   a.bz = c->bvtx[2];
   a.obb = c->pobb;
+  a.fx = c->vrf[0];
+  a.fy = c->vrf[1];
+  a.fz = c->vrf[2];
   return a;
 }
 }  // namespace
@@ -788,6 +834,9 @@ static FeatArgs make_fargs(dem_ctx* c, uint64_t nu) {
   a.old_off = c->own_off[c->icur];
   a.perm = c->perm;
   a.have_old = c->hist_valid ? 1 : 0;
+  a.fvx = c->vrf[0];
+  a.fvy = c->vrf[1];
+  a.fvz = c->vrf[2];
   return a;
 }
 
@@ -796,7 +845,10 @@ int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total) {
   const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
   {
     ProfScope ps(c, K_BROAD_COUNT, nu ? 1 : 0);
-    if (nu) k_features<false><<<blocks, PT, 0, c->stream>>>(a);
+    if (nu && c->prm.fp32_broad_phase)
+      k_feat<false, true><<<blocks, PT, 0, c->stream>>>(a);
+    else if (nu)
+      k_feat<false, false><<<blocks, PT, 0, c->stream>>>(a);
   }
   int rc = scan_exclusive_u32(c, c->f_cnt, c->f_off, nu);
   if (rc) return rc;
@@ -809,7 +861,10 @@ int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
   FeatArgs a = make_fargs(c, nu);
   const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
   ProfScope ps(c, K_BROAD_FILL, 2);
-  if (nu) k_features<true><<<blocks, PT, 0, c->stream>>>(a);
+  if (nu && c->prm.fp32_broad_phase)
+    k_feat<true, true><<<blocks, PT, 0, c->stream>>>(a);
+  else if (nu)
+    k_feat<true, false><<<blocks, PT, 0, c->stream>>>(a);
   k_own_from_units<<<grid_for(c->n + 1, 256), 256, 0, c->stream>>>(c->n, c->u_off, c->f_off, c->own_off[1 - c->icur]);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;

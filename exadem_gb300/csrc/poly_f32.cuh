@@ -1,0 +1,268 @@
+// poly_f32.cuh -- FP32 decisions of the polyhedron broad-phase tests.
+//
+// Each function evaluates the same formula as its FP64 counterpart in
+// poly_core.cuh (OBB::intersect, filter_vv/ve/vf/ee, which follow
+// src/polyhedra/include/exaDEM/shape/shape_detection.hpp) in FP32, together
+// with a first-order bound of the FP32 error, and returns
+//   DEC_FALSE / DEC_TRUE  when every comparison of the formula is further from
+//                         its threshold than 8x the error bound, so that the
+//                         FP64 evaluation takes the same branch;
+//   DEC_UNDECIDED         otherwise: the caller runs the FP64 function.
+// The result of a decided test is therefore the FP64 result, bit for bit.
+//
+// Inputs: coordinates relative to the centre of the owner particle A, as FP32.
+// With S a bound of every |coordinate| (S = |r_B - r_A| + both particles'
+// max vertex radii and Minkowski radii + skin), each input coordinate carries
+// an error of at most 3 u S (conversion of v - r, of r_B - r_A and their sum,
+// u = 2^-24); vector differences of inputs therefore carry at most
+// ETA = 2^-19 S (a factor 3 above 2 * sqrt(3) * 3 u S).
+#pragma once
+#include <cstdint>
+
+#include "poly_core.cuh"
+
+namespace dem {
+
+struct F3 {
+  float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 operator+(F3 a, F3 b) { return F3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ F3 operator-(F3 a, F3 b) { return F3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ F3 operator*(F3 a, float s) { return F3{a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ float fdot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float flen(F3 a) { return sqrtf(fdot(a, a)); }
+__device__ __forceinline__ F3 fcross(F3 a, F3 b) {
+  return F3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// FP32 vertices of one particle (relative to the centre of A) in SoA layout
+struct FView {
+  const float* x;
+  const float* y;
+  const float* z;
+  F3 off;
+  __device__ __forceinline__ F3 operator[](int k) const { return F3{x[k] + off.x, y[k] + off.y, z[k] + off.z}; }
+};
+
+struct OBBf {
+  F3 c, e[3];
+  float ext[3];
+};
+
+__device__ __forceinline__ OBBf obb_f32(const OBBd& o, V3 origin) {
+  OBBf r;
+  r.c = f3((float)(o.c.x - origin.x), (float)(o.c.y - origin.y), (float)(o.c.z - origin.z));
+  r.e[0] = f3((float)o.e1.x, (float)o.e1.y, (float)o.e1.z);
+  r.e[1] = f3((float)o.e2.x, (float)o.e2.y, (float)o.e2.z);
+  r.e[2] = f3((float)o.e3.x, (float)o.e3.y, (float)o.e3.z);
+  r.ext[0] = (float)o.ext.x;
+  r.ext[1] = (float)o.ext.y;
+  r.ext[2] = (float)o.ext.z;
+  return r;
+}
+
+enum : int { DEC_FALSE = 0, DEC_TRUE = 1, DEC_UNDECIDED = 2 };
+
+constexpr float F32_U = 5.9604645e-08f;  // 2^-24
+constexpr float F32_ETA = 1.9073486e-06f;  // 2^-19: ETA / S
+constexpr float F32_SAFE = 8.f;             // decided only beyond 8x the bound
+
+// one comparison "x > thr" with error bound e: +1 surely greater, -1 surely not, 0 unknown
+__device__ __forceinline__ int cmp_gt(float x, float thr, float e) {
+  const float m = F32_SAFE * e;
+  return x > thr + m ? 1 : (x < thr - m ? -1 : 0);
+}
+
+// Vertex gate: OBB::intersect(obb, box(p, rv)) with the box's axes the world axes.
+// The FP64 test returns false at the first of 15 axes with |t_L| > ra_L + rb_L.
+// Error of every axis test, with T = |c - p| + sum(ext) + rv + S:
+// obb centre and extents are FP32 roundings of the FP64 values (u T), axes
+// u per component, p carries ETA; every |t_L| and radius sum is a sum of at most
+// 6 products of magnitude <= 2T with |factor| <= 1 + tol.  Bound: 2^-17 T.
+__device__ __forceinline__ int decide_gate(const OBBf& o, F3 p, float rv, float S) {
+  const float tol = 1.1920929e-07f;
+  const F3 tt = o.c - p;
+  const float T = flen(tt) + o.ext[0] + o.ext[1] + o.ext[2] + rv + S;
+  const float e = 7.6293945e-06f * T;  // 2^-17 T
+  // rows: A axes; B axes are the world axes, so R[k][l] = component l of e_k
+  float R[3][3], Ab[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    R[k][0] = o.e[k].x;
+    R[k][1] = o.e[k].y;
+    R[k][2] = o.e[k].z;
+#pragma unroll
+    for (int l = 0; l < 3; l++) Ab[k][l] = fabsf(R[k][l]) + tol;
+  }
+  const float t[3] = {fdot(tt, o.e[0]), fdot(tt, o.e[1]), fdot(tt, o.e[2])};
+  bool undecided = false;
+  // A's axes
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int c = cmp_gt(fabsf(t[k]), o.ext[k] + rv * (Ab[k][0] + Ab[k][1] + Ab[k][2]), e);
+    if (c > 0) return DEC_FALSE;
+    undecided |= c == 0;
+  }
+  // B's (world) axes
+#pragma unroll
+  for (int l = 0; l < 3; l++) {
+    const float ra = o.ext[0] * Ab[0][l] + o.ext[1] * Ab[1][l] + o.ext[2] * Ab[2][l];
+    const int c = cmp_gt(fabsf(t[0] * R[0][l] + t[1] * R[1][l] + t[2] * R[2][l]), ra + rv, e);
+    if (c > 0) return DEC_FALSE;
+    undecided |= c == 0;
+  }
+  // cross axes A_k x B_l, with (k1, k2) the other two A axes
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const int k1 = (k + 1) % 3, k2 = (k + 2) % 3;
+#pragma unroll
+    for (int l = 0; l < 3; l++) {
+      const int l1 = (l + 1) % 3, l2 = (l + 2) % 3;
+      const float ra = o.ext[k1] * Ab[k2][l] + o.ext[k2] * Ab[k1][l];
+      const float rb = rv * (Ab[k][l2] + Ab[k][l1]);
+      const int c = cmp_gt(fabsf(t[k2] * R[k1][l] - t[k1] * R[k2][l]), ra + rb, e);
+      if (c > 0) return DEC_FALSE;
+      undecided |= c == 0;
+    }
+  }
+  return undecided ? DEC_UNDECIDED : DEC_TRUE;
+}
+
+// filter_vv: |vi - vj|^2 <= R^2.  |d| carries 2 ETA + 4u|d|.
+__device__ __forceinline__ int decide_vv(F3 vi, F3 vj, float R, float S) {
+  const float d = flen(vi - vj);
+  const int c = cmp_gt(d, R, 2.f * F32_ETA * S + 4.f * F32_U * (d + R));
+  return c > 0 ? DEC_FALSE : (c < 0 ? DEC_TRUE : DEC_UNDECIDED);
+}
+
+// filter_ve: r = E.w / E.E in [-rV, 1 + rV] and |w - E r|^2 < R^2.
+__device__ __forceinline__ int decide_ve(F3 vi, F3 vf, F3 vs, float R, float rV, float S) {
+  const float eta = F32_ETA * S;
+  const F3 E = vs - vf, w = vi - vf;
+  const float L2 = fdot(E, E), L = sqrtf(L2), W = flen(w);
+  if (!(L2 > 0.f)) return DEC_UNDECIDED;
+  const float r = fdot(E, w) / L2;
+  const float ar = fabsf(r);
+  // |d(E.w)| <= eta (W + L) + 4u L W ; |d(E.E)| <= 2 eta L + 4u L^2 ; plus 2u |r| for the division
+  const float er = (eta * (W + L) + 4.f * F32_U * L * W + ar * (2.f * eta * L + 4.f * F32_U * L2)) / L2 +
+                   2.f * F32_U * ar;
+  const int c0 = cmp_gt(-rV, r, er);  // r < -rV
+  const int c1 = cmp_gt(r, 1.f + rV, er + F32_U * (1.f + rV));
+  if (c0 > 0 || c1 > 0) return DEC_FALSE;
+  if (c0 == 0 || c1 == 0) return DEC_UNDECIDED;
+  const F3 dv = w - E * r;
+  const float d = flen(dv);
+  // |d(w - E r)| <= eta + eta |r| + L er + 4u (W + L |r|)
+  const float ed = eta * (1.f + ar) + L * er + 4.f * F32_U * (W + L * ar) + 4.f * F32_U * (d + R);
+  const int c = cmp_gt(d, R, ed);
+  return c < 0 ? DEC_TRUE : (c > 0 ? DEC_FALSE : DEC_UNDECIDED);
+}
+
+// filter_vf (vf_core): vertex vi against face `face` of the shape with vertices vf.
+// The frame (v1, n, v2 = n x v1) is built from the face's first, second and last
+// vertices as in the FP64 code.  Decided when the plane distance and every
+// comparison of the crossing-parity test are beyond their bounds.
+__device__ inline int decide_vf(F3 vi, const FView& vf, const ShapeDev& sf, int face, float lim, float S) {
+  const float eta = F32_ETA * S;
+  const int b = sf.fo[face], nf = sf.fo[face + 1] - sf.fo[face];
+  const F3 va = vf[sf.fv[b]];
+  const F3 e1 = vf[sf.fv[b + 1]] - va;
+  const F3 e2 = vf[sf.fv[b + nf - 1]] - va;
+  const float L1 = flen(e1), L2 = flen(e2);
+  if (!(L1 > 0.f)) return DEC_UNDECIDED;
+  const F3 v1 = e1 * (1.f / L1);
+  const F3 cr = fcross(v1, e2);
+  const float lc = flen(cr);
+  if (!(lc > 1e-3f * L2)) return DEC_UNDECIDED;  // face frame ill-conditioned in FP32
+  const F3 n = cr * (1.f / lc);
+  // direction errors: v1 <= 2 eta / L1 + 3u ; n <= 2 (|dv1| L2 + eta + 4u L2) / lc + 3u
+  const float ev1 = 2.f * eta / L1 + 3.f * F32_U;
+  const float en = 2.f * (ev1 * L2 + eta + 4.f * F32_U * L2) / lc + 3.f * F32_U;
+  const float ef = ev1 + en + 3.f * F32_U;  // frame error (v2 included)
+  const F3 v = vi - va;
+  const float V = flen(v);
+  const float dist = fabsf(fdot(n, v));
+  const float edist = en * V + eta + 4.f * F32_U * V;
+  const int cd = cmp_gt(dist, lim, edist + F32_U * lim);
+  if (cd > 0) return DEC_FALSE;
+  if (cd == 0) return DEC_UNDECIDED;
+  const F3 v2 = fcross(n, v1);
+  // in-plane coordinates of the face vertices relative to the projection P of vi:
+  // D1 = (v_k - vi).v1 + dist n.v1 ; D2 likewise with v2 (n.v1, n.v2 are O(ef))
+  const float eD = ef * (2.f * S + dist) + eta + 6.f * F32_U * 2.f * S;
+  int odd = 0;
+  F3 pa = vf[sf.fv[b]] - vi;
+  float a1 = fdot(pa, v1), a2 = fdot(pa, v2);
+  const int s_first = cmp_gt(a2, 0.f, eD);
+  if (s_first == 0) return DEC_UNDECIDED;
+  int sa = s_first;
+  for (int k = 0; k < nf; k++) {
+    float b1, b2;
+    int sb;
+    if (k + 1 == nf) {
+      const F3 pb = vf[sf.fv[b]] - vi;
+      b1 = fdot(pb, v1);
+      b2 = fdot(pb, v2);
+      sb = s_first;
+    } else {
+      const F3 pb = vf[sf.fv[b + k + 1]] - vi;
+      b1 = fdot(pb, v1);
+      b2 = fdot(pb, v2);
+      sb = cmp_gt(b2, 0.f, eD);
+      if (sb == 0) return DEC_UNDECIDED;
+    }
+    if (sa != sb) {  // the edge straddles the line through P along v1
+      // crossing abscissa relative to P: X = a1 + t (b1 - a1), t = -a2 / (b2 - a2) in [0, 1]
+      const float den = b2 - a2;
+      const float t = -a2 / den;
+      const float X = a1 + t * (b1 - a1);
+      const float et = 3.f * eD / fabsf(den) + 2.f * F32_U;
+      const float eX = eD + et * fabsf(b1 - a1) + 2.f * eD + 3.f * F32_U * (fabsf(a1) + fabsf(b1 - a1));
+      const int cx = cmp_gt(0.f, X, eX);  // X < 0
+      if (cx == 0) return DEC_UNDECIDED;
+      if (cx > 0) odd ^= 1;
+    }
+    a1 = b1;
+    a2 = b2;
+    sa = sb;
+  }
+  return odd ? DEC_TRUE : DEC_FALSE;
+}
+
+// filter_ee: closest points of the two lines at s, t strictly inside (0, 1) and
+// |pi - pj|^2 <= R^2; near-parallel edges (|f| within 8x its bound of 1e-12) are undecided.
+__device__ inline int decide_ee(F3 vfi, F3 vsi, F3 vfj, F3 vsj, float R, float S) {
+  const float eta = F32_ETA * S, u = F32_U;
+  const F3 Ei = vsi - vfi, Ej = vsj - vfj, v = vfi - vfj;
+  const float c = fdot(Ei, Ei), d = fdot(Ej, Ej), e = fdot(Ei, Ej);
+  const float Li = sqrtf(c), Lj = sqrtf(d), V = flen(v);
+  const float f = c * d - e * e;
+  const float ae = fabsf(e);
+  const float dc = 2.f * Li * eta + 4.f * u * c, dd = 2.f * Lj * eta + 4.f * u * d;
+  const float de = (Li + Lj) * eta + 4.f * u * Li * Lj;
+  const float df = dc * d + c * dd + 2.f * ae * de + 3.f * u * (c * d + e * e);
+  const int cf = cmp_gt(fabsf(f), 1.0e-12f, df);
+  if (cf < 0) return DEC_FALSE;
+  if (cf == 0) return DEC_UNDECIDED;
+  const float a = fdot(Ei, v), bb = fdot(Ej, v);
+  const float aa = fabsf(a), ab = fabsf(bb);
+  const float da = (Li + V) * eta + 4.f * u * Li * V, db = (Lj + V) * eta + 4.f * u * Lj * V;
+  const float inv = 1.f / f, af = fabsf(f);
+  const float s = (e * bb - a * d) * inv;
+  const float t = (c * bb - e * a) * inv;
+  const float as = fabsf(s), at = fabsf(t);
+  const float ds = (de * ab + ae * db + da * d + aa * dd + 3.f * u * (ae * ab + aa * d) + as * df) / af + 3.f * u * as;
+  const float dt = (dc * ab + c * db + de * aa + ae * da + 3.f * u * (c * ab + ae * aa) + at * df) / af + 3.f * u * at;
+  const int s0 = cmp_gt(s, 0.f, ds), s1 = cmp_gt(1.f, s, ds + u);
+  const int t0 = cmp_gt(t, 0.f, dt), t1 = cmp_gt(1.f, t, dt + u);
+  if (s0 < 0 || s1 < 0 || t0 < 0 || t1 < 0) return DEC_FALSE;
+  if (s0 == 0 || s1 == 0 || t0 == 0 || t1 == 0) return DEC_UNDECIDED;
+  const F3 nv = v + Ei * s - Ej * t;
+  const float dn = flen(nv);
+  const float edn = eta * (1.f + as + at) + Li * ds + Lj * dt + 5.f * u * (V + Li * as + Lj * at) + 4.f * u * (dn + R);
+  const int cn = cmp_gt(dn, R, edn);
+  return cn < 0 ? DEC_TRUE : (cn > 0 ? DEC_FALSE : DEC_UNDECIDED);
+}
+
+}  // namespace dem

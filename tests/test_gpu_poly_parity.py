@@ -65,3 +65,36 @@ def test_forced_rebuilds_keep_history(native_lib):
         assert_same_list(lg, lo)
         np.testing.assert_array_equal(lg["friction"], lo["friction"])
         np.testing.assert_array_equal(lg["moment"], lo["moment"])
+
+
+@pytest.mark.parametrize("seed", [5, 6])
+def test_fp32_prefilters_same_list(native_lib, seed):
+    """FP32 rejection tests (vertex gates and feature bounding spheres) keep exactly the FP64 list."""
+    a = W.polyhedra_lattice(nx=9, ny=9, nz=6, seed=seed).build()
+    b = W.polyhedra_lattice(nx=9, ny=9, nz=6, seed=seed, fp32_broad_phase=1, fused_step=1).build()
+    for s in (a, b):
+        s.first_iteration()
+    assert_same_list(a.interactions(), b.interactions())
+    for _ in range(3):
+        for s in (a, b):
+            s.step(30)
+            s.update_particle_neighbors()
+        assert_same_list(a.interactions(), b.interactions())
+    assert bit_equal_fraction(a.particles(), b.particles()) == 1.0
+
+
+def test_fp32_decisions_selftest(native_lib):
+    """The FP32 decisions of the broad-phase tests agree with FP64 whenever they decide."""
+    import ctypes as C
+
+    counts = (C.c_uint64 * 20)()
+    n = 20_000_000
+    assert native_lib.dem_selftest_poly_decisions(n, 2024, counts) == 0
+    names = ["gate", "vv", "ve", "vf", "ee"]
+    for k, name in enumerate(names):
+        bad, undecided, dec_true, exact_true = counts[4 * k: 4 * k + 4]
+        assert bad == 0, (name, bad)
+        # every draw sits near a threshold (offsets log-uniform in [1e-10, 1e-1]
+        # of the particle size), so a large share stays undecided by design
+        assert undecided < 0.8 * (n // 5), (name, undecided)
+        assert 0 < dec_true <= exact_true, name
