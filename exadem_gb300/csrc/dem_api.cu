@@ -199,8 +199,10 @@ void free_poly(dem_ctx* c) {
     c->vrf[d] = nullptr;
   }
   cudaFree(c->pobb);
+  cudaFree(c->pfbox);
   cudaFree(c->u_off);
   c->pobb = nullptr;
+  c->pfbox = nullptr;
   c->u_off = nullptr;
   c->vcap = 0;
 }
@@ -216,6 +218,7 @@ int alloc_poly(dem_ctx* c) {
     DEM_CUDA_TRY(c, cudaMalloc(&c->vrf[d], need * 4));
   }
   DEM_CUDA_TRY(c, cudaMalloc(&c->pobb, std::max<uint64_t>(c->pcap, 1) * 15 * 8));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->pfbox, std::max<uint64_t>(c->pcap, 1) * 32 * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_off, (std::max<uint64_t>(c->pcap, 1) + 1) * 4));
   c->vcap = need;
   return DEM_OK;
@@ -227,11 +230,13 @@ void free_units(dem_ctx* c) {
   cudaFree(c->u_pid);
   cudaFree(c->u_kind);
   cudaFree(c->u_pass);
+  cudaFree(c->u_slots);
   cudaFree(c->f_cnt);
   cudaFree(c->f_off);
   c->u_owner = c->u_partner = c->u_kind = c->f_cnt = c->f_off = nullptr;
   c->u_pid = nullptr;
   c->u_pass = nullptr;
+  c->u_slots = nullptr;
   c->ucap = 0;
 }
 
@@ -244,6 +249,7 @@ int grow_units(dem_ctx* c, uint64_t need) {
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_pid, cap * 8));
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_kind, cap * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_pass, cap));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_slots, cap * FEAT_SLOTS * sizeof(uint16_t)));
   DEM_CUDA_TRY(c, cudaMalloc(&c->f_cnt, (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->f_off, (cap + 1) * 4));
   c->ucap = cap;

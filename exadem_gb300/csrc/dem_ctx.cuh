@@ -15,6 +15,10 @@ static const char* const kDemKClassNames[K_NCLASS] = {
     "prolog", "displ_over", "bin_cells", "reorder", "broad_count", "broad_fill", "reverse_lists", "scan",
     "contact", "gather", "reset", "gravity", "force_to_accel", "epilog", "state"};
 
+// features recorded per polyhedron unit by the count pass of the FP32-decided
+// enumeration; the fill pass copies them instead of deciding again
+constexpr int FEAT_SLOTS = 16;
+
 struct dem_ctx {
   dem_params prm{};
   cudaStream_t stream = nullptr;
@@ -85,6 +89,7 @@ struct dem_ctx {
   double* bvtx[3] = {};               // vertices at the last rebuild
   double* pobb = nullptr;             // world OBB per particle (15 doubles)
   float* vrf[3] = {};                 // FP32 vertices relative to the particle centre (rebuild time)
+  float* pfbox = nullptr;             // FP32 gate OBB + vertex slabs per particle (rebuild time)
   uint64_t vcap = 0;
   uint32_t* u_off = nullptr;          // n+1 unit offsets per owner
   uint32_t* u_owner = nullptr;        // unit arrays (ucap each)
@@ -92,6 +97,7 @@ struct dem_ctx {
   uint64_t* u_pid = nullptr;
   uint32_t* u_kind = nullptr;
   uint8_t* u_pass = nullptr;
+  uint16_t* u_slots = nullptr;        // FEAT_SLOTS features per unit recorded by the count pass
   uint32_t* f_cnt = nullptr;          // features per unit (ucap+1)
   uint32_t* f_off = nullptr;          // feature offsets (ucap+1)
   uint64_t ucap = 0;

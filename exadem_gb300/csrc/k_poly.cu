@@ -45,6 +45,8 @@ struct PolyArgs {
   float* fx;    // FP32 vertices relative to the centre
   float* fy;
   float* fz;
+  float* fbox;  // FBOX_STRIDE per particle: FP32 gate OBB and vertex slabs (rebuild time)
+  double rV;
 };
 
 // ---------------------------------------------------------------- vertices
@@ -83,6 +85,32 @@ __global__ void k_poly_vertices(PolyArgs a, double thr2, unsigned long long* fla
                                o.e3.x, o.e3.y, o.e3.z, o.ext.x, o.ext.y, o.ext.z};
 #pragma unroll
       for (int k = 0; k < 15; k++) w[k] = vals[k];
+      // FP32 copy of the gate OBB (relative to the centre, enlarged by 0.5 rV twice as
+      // in the feature enumeration) and vertex slabs along its normalised axes
+      float* fb = a.fbox + s * FBOX_STRIDE;
+      OBBd g = o;
+      obb_enlarge(g, 0.5 * a.rV);
+      obb_enlarge(g, 0.5 * a.rV);
+      const OBBf gf = obb_f32(g, p);
+      store_obbf(fb, gf);
+      const uint64_t base = s * (uint64_t)a.MV;
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        F3 d = gf.e[k];
+        const float dl = flen(d);
+        d = dl > 0.f ? d * (1.f / dl) : f3(k == 0, k == 1, k == 2);
+        float lo = 3.4e38f, hi = -3.4e38f;
+        for (int m = 0; m < sh.nv; m++) {
+          const float pr = fdot(f3(a.fx[base + m], a.fy[base + m], a.fz[base + m]), d);
+          lo = fminf(lo, pr);
+          hi = fmaxf(hi, pr);
+        }
+        fb[15 + 3 * k] = d.x;
+        fb[16 + 3 * k] = d.y;
+        fb[17 + 3 * k] = d.z;
+        fb[24 + k] = 0.5f * (lo + hi);
+        fb[27 + k] = 0.5f * (hi - lo);
+      }
     }
   }
   if (Displ) {
@@ -293,6 +321,8 @@ struct FeatArgs {
   const float* fvx;  // FP32 vertices relative to the particle centre
   const float* fvy;
   const float* fvz;
+  const float* fbox;  // FP32 gate OBBs and vertex slabs
+  uint16_t* slots;    // FEAT_SLOTS per unit: (segment, i, j) of the features found by the count pass
 };
 
 __device__ __forceinline__ VView vview(const FeatArgs& a, uint32_t s) {
@@ -358,6 +388,28 @@ __device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uin
 // first (poly_f32.cuh): a decided test has the FP64 result by construction, an
 // undecided one (its FP32 value within 8x its error bound of a threshold) runs
 // the FP64 function.  Only the rare undecided lanes touch the FP64 pipe.
+__device__ __forceinline__ uint32_t seg_type(int seg) {
+  return seg == 0 ? DEM_ITYPE_VERTEX_VERTEX
+                  : (seg <= 2 ? DEM_ITYPE_VERTEX_EDGE : (seg <= 4 ? DEM_ITYPE_VERTEX_FACE : DEM_ITYPE_EDGE_EDGE));
+}
+__device__ __forceinline__ uint32_t seg_swap(int seg) { return (seg == 2 || seg == 4) ? 1u : 0u; }
+
+// vertex - driver unit (add_driver_interaction): filter(rV + minkowski(h), vertex)
+template <bool Fill>
+__device__ __forceinline__ void driver_unit(const FeatArgs& a, uint64_t u, uint32_t A, const ShapeDev& SA, double ra,
+                                            const VView& va, uint32_t base, int lane, uint32_t lt) {
+  const uint32_t k = a.u_partner[u];
+  const DriverDev& d = a.drv[k];
+  const uint32_t type = d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER;
+  const bool keep = lane < SA.nv && driver_reach(d, a.rV + ra, va[lane]);
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  if (Fill) {
+    if (keep) write_feature(a, base + __popc(m & lt), A, k, a.u_pid[u], type, 0, lane, 0xffffu);
+  } else if (lane == 0) {
+    a.fcnt[u] = __popc(m);
+  }
+}
+
 // exact FP64 filter of test (i, j) of segment seg (warp-uniform seg)
 __device__ __noinline__ bool exact_filter(int seg, int i, int j, double rV, const VView& va, double ra,
                                           const ShapeDev& SA, const VView& vb, double rb, const ShapeDev& SB) {
@@ -372,21 +424,6 @@ __device__ __noinline__ bool exact_filter(int seg, int i, int j, double rV, cons
   }
 }
 
-// FP32 decision of test (i, j) of segment seg (DEC_FALSE / DEC_TRUE / DEC_UNDECIDED)
-__device__ __noinline__ int decide_test(int seg, int i, int j, float R, float rV, float S, const FView& fa,
-                                        const ShapeDev& SA, const FView& fb, const ShapeDev& SB) {
-  switch (seg) {
-    case 0: return decide_vv(fa[i], fb[j], R, S);
-    case 1: return decide_ve(fa[i], fb[SB.e[2 * j]], fb[SB.e[2 * j + 1]], R, rV, S);
-    case 2: return decide_ve(fb[j], fa[SA.e[2 * i]], fa[SA.e[2 * i + 1]], R, rV, S);
-    case 3: return decide_vf(fa[i], fb, SB, j, R, S);
-    case 4: return decide_vf(fb[j], fa, SA, i, R, S);
-    default: return decide_ee(fa[SA.e[2 * i]], fa[SA.e[2 * i + 1]], fb[SB.e[2 * j]], fb[SB.e[2 * j + 1]], R, S);
-  }
-}
-
-__device__ __noinline__ int decide_gate_nf(const OBBf& o, F3 p, float rv, float S) { return decide_gate(o, p, rv, S); }
-
 __device__ __noinline__ bool vertex_gate(const OBBd& obb, V3 v, double rv) {
   OBBd ov;
   ov.c = v;
@@ -399,11 +436,11 @@ __device__ __noinline__ bool vertex_gate(const OBBd& obb, V3 v, double rv) {
 }
 
 // One warp per unit.  Fill = false: counts into fcnt; Fill = true: writes at foff.
-// The gated tests are processed segment by segment in InteractionPair order
-// (VV, VE, VE swap, VF, VF swap, EE) so every warp instruction runs a single
-// filter type.  F32: every gate and test is decided in FP32 first; the lanes
-// left undecided run the FP64 function.
-template <bool Fill, bool F32>
+// Plain FP64 enumeration in InteractionPair order: gated A vertices against all
+// B vertices (VV), edges (VE) and faces (VF), all A edges (VE swap) and faces
+// (VF swap) against gated B vertices, all edge pairs (EE), one segment (one
+// filter type) at a time.
+template <bool Fill>
 __global__ void __launch_bounds__(PT) k_feat(FeatArgs a) {
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
@@ -418,27 +455,16 @@ __global__ void __launch_bounds__(PT) k_feat(FeatArgs a) {
     }
     const uint32_t A = a.u_owner[u];
     const ShapeDev& SA = a.shapes[a.P.type[A]];
-    const double ha = a.P.f[HOM][A];
-    const double ra = SA.r * ha;
+    const double ra = SA.r * a.P.f[HOM][A];
     const VView va = vview(a, A);
-    if (a.u_kind[u]) {  // vertex - driver (add_driver_interaction): filter(rV + minkowski(h), vertex)
-      const uint32_t k = a.u_partner[u];
-      const DriverDev& d = a.drv[k];
-      const uint32_t type = d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER;
-      const bool keep = lane < SA.nv && driver_reach(d, a.rV + ra, va[lane]);
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (Fill) {
-        if (keep) write_feature(a, base + __popc(m & lt), A, k, a.u_pid[u], type, 0, lane, 0xffffu);
-      } else if (lane == 0) {
-        a.fcnt[u] = __popc(m);
-      }
+    if (a.u_kind[u]) {
+      driver_unit<Fill>(a, u, A, SA, ra, va, base, lane, lt);
       continue;
     }
     const uint32_t B = a.u_partner[u];
     const uint64_t pid = a.u_pid[u];
     const ShapeDev& SB = a.shapes[a.P.type[B]];
-    const double hb = a.P.f[HOM][B];
-    const double rb = SB.r * hb;
+    const double rb = SB.r * a.P.f[HOM][B];
     const VView vb = vview(a, B);
     OBBd obb_i = load_obb(a.obb + (uint64_t)A * 15);
     OBBd obb_j = load_obb(a.obb + (uint64_t)B * 15);
@@ -446,38 +472,12 @@ __global__ void __launch_bounds__(PT) k_feat(FeatArgs a) {
     obb_enlarge(obb_j, 0.5 * a.rV);
     obb_enlarge(obb_i, 0.5 * a.rV);
     obb_enlarge(obb_j, 0.5 * a.rV);
-    FView fa{nullptr, nullptr, nullptr, f3(0.f, 0.f, 0.f)}, fb = fa;
-    float S = 0.f;
-    bool ga = false, gb = false;
-    if (F32) {
-      const V3 rA = mk(a.P.f[RX][A], a.P.f[RY][A], a.P.f[RZ][A]);
-      const V3 rB = mk(a.P.f[RX][B], a.P.f[RY][B], a.P.f[RZ][B]);
-      const F3 dR = f3((float)(rB.x - rA.x), (float)(rB.y - rA.y), (float)(rB.z - rA.z));
-      const uint64_t oA = (uint64_t)A * a.MV, oB = (uint64_t)B * a.MV;
-      fa = FView{a.fvx + oA, a.fvy + oA, a.fvz + oA, f3(0.f, 0.f, 0.f)};
-      fb = FView{a.fvx + oB, a.fvy + oB, a.fvz + oB, dR};
-      // S bounds every |coordinate| relative to A's centre: measured on the vertices
-      float sv = fmaxf(lane < SA.nv ? flen(fa[lane]) : 0.f, lane < SB.nv ? flen(fb[lane]) : 0.f);
-#pragma unroll
-      for (int o = 16; o; o >>= 1) sv = fmaxf(sv, __shfl_xor_sync(0xffffffffu, sv, o));
-      S = sv * 1.001f + (float)(ra + rb + a.rV);
-      const OBBf fi = obb_f32(obb_i, rA), fj = obb_f32(obb_j, rA);
-      const int da = lane < SA.nv ? decide_gate_nf(fj, fa[lane], (float)ra, S) : DEC_FALSE;
-      const int db = lane < SB.nv ? decide_gate_nf(fi, fb[lane], (float)rb, S) : DEC_FALSE;
-      ga = da == DEC_TRUE;
-      gb = db == DEC_TRUE;
-      if (da == DEC_UNDECIDED) ga = vertex_gate(obb_j, va[lane], ra);
-      if (db == DEC_UNDECIDED) gb = vertex_gate(obb_i, vb[lane], rb);
-    } else {
-      if (lane < SA.nv) ga = vertex_gate(obb_j, va[lane], ra);
-      if (lane < SB.nv) gb = vertex_gate(obb_i, vb[lane], rb);
-    }
+    const bool ga = lane < SA.nv && vertex_gate(obb_j, va[lane], ra);
+    const bool gb = lane < SB.nv && vertex_gate(obb_i, vb[lane], rb);
     const uint32_t gA = __ballot_sync(0xffffffffu, ga), gB = __ballot_sync(0xffffffffu, gb);
     const int nA = __popc(gA), nB = __popc(gB);
-    const float Rf = (float)(ra + rb + a.rV), rVf = (float)a.rV;
 #pragma unroll 1
     for (int seg = 0; seg < 6; seg++) {
-      // rows x cols of the segment; rows of VV/VE/VF are gated A vertices, cols of VE/VF swap gated B vertices
       int rows, cols;
       switch (seg) {
         case 0: rows = nA; cols = SB.nv; break;
@@ -488,10 +488,6 @@ __global__ void __launch_bounds__(PT) k_feat(FeatArgs a) {
         default: rows = SA.ne; cols = SB.ne;
       }
       const uint32_t ns = (uint32_t)rows * (uint32_t)cols;
-      const uint32_t type = seg == 0 ? DEM_ITYPE_VERTEX_VERTEX
-                                     : (seg <= 2 ? DEM_ITYPE_VERTEX_EDGE : (seg <= 4 ? DEM_ITYPE_VERTEX_FACE
-                                                                                     : DEM_ITYPE_EDGE_EDGE));
-      const uint32_t swap = (seg == 2 || seg == 4) ? 1u : 0u;
       for (uint32_t t0 = 0; t0 < ns; t0 += 32) {
         const uint32_t t = t0 + lane;
         int i = 0, j = 0;
@@ -500,15 +496,225 @@ __global__ void __launch_bounds__(PT) k_feat(FeatArgs a) {
           const int r = (int)(t / (uint32_t)cols), c = (int)(t % (uint32_t)cols);
           i = (seg == 0 || seg == 1 || seg == 3) ? nth_bit(gA, r) : r;
           j = (seg == 2 || seg == 4) ? nth_bit(gB, c) : c;
-          const int d = F32 ? decide_test(seg, i, j, Rf, rVf, S, fa, SA, fb, SB) : DEC_UNDECIDED;
-          keep = d == DEC_TRUE;
-          if (d == DEC_UNDECIDED) keep = exact_filter(seg, i, j, a.rV, va, ra, SA, vb, rb, SB);
+          keep = exact_filter(seg, i, j, a.rV, va, ra, SA, vb, rb, SB);
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (Fill && keep) write_feature(a, base + count + __popc(m & lt), A, B, pid, type, swap, i, j);
+        if (Fill && keep)
+          write_feature(a, base + count + __popc(m & lt), A, B, pid, seg_type(seg), seg_swap(seg), i, j);
         count += __popc(m);
       }
     }
+    if (!Fill && lane == 0) a.fcnt[u] = count;
+  }
+}
+
+// ---- FP32-decided enumeration
+// The same feature tests as k_feat, restricted by necessary conditions and
+// decided in FP32 (poly_f32.cuh):
+//   * vertex gates decided in FP32 (FP64 OBB::intersect only when undecided);
+//   * a B vertex can pass filter_vv only within R of A's vertex hull, a face
+//     (VF) only within R of the other particle's hull, an edge (VE, EE) only
+//     when the edge, extended by rV times its length at both ends (VE accepts
+//     r in [-rV, 1 + rV]), comes within R of it; the hulls are bounded by the
+//     per-particle vertex slabs, so the other features are skipped;
+//   * every remaining test is decided in FP32; undecided lanes run the FP64 filter.
+// Enumeration order, and therefore the written list, is that of k_feat.
+struct DecUnit {
+  uint64_t u;
+  uint32_t A, B;
+  uint64_t pid;
+  const ShapeDev* SA;
+  const ShapeDev* SB;
+  double ra, rb;
+  VView va, vb;
+  FView fa, fb;
+  float R, rV, S;
+};
+
+__device__ __noinline__ int decide_vf_nf(F3 vi, const FView& vf, const ShapeDev& sf, int face, float lim, float S) {
+  return decide_vf(vi, vf, sf, face, lim, S);
+}
+
+template <int SEG, bool Fill>
+__device__ __forceinline__ void dec_segment(const FeatArgs& a, const DecUnit& x, const uint8_t* Lr, int nr,
+                                            const uint8_t* Lc, int nc, uint32_t& count, uint32_t base, int lane,
+                                            uint32_t lt) {
+  const uint32_t ns = (uint32_t)nr * (uint32_t)nc;
+  for (uint32_t t0 = 0; t0 < ns; t0 += 32) {
+    const uint32_t t = t0 + lane;
+    int i = 0, j = 0;
+    bool keep = false;
+    if (t < ns) {
+      const uint32_t r = t / (uint32_t)nc;
+      i = Lr[r];
+      j = Lc[t - r * (uint32_t)nc];
+      int d;
+      if (SEG == 0) {
+        d = decide_vv(x.fa[i], x.fb[j], x.R, x.S);
+      } else if (SEG == 1) {
+        d = decide_ve(x.fa[i], x.fb[x.SB->e[2 * j]], x.fb[x.SB->e[2 * j + 1]], x.R, x.rV, x.S);
+      } else if (SEG == 2) {
+        d = decide_ve(x.fb[j], x.fa[x.SA->e[2 * i]], x.fa[x.SA->e[2 * i + 1]], x.R, x.rV, x.S);
+      } else if (SEG == 3) {
+        d = decide_vf_nf(x.fa[i], x.fb, *x.SB, j, x.R, x.S);
+      } else if (SEG == 4) {
+        d = decide_vf_nf(x.fb[j], x.fa, *x.SA, i, x.R, x.S);
+      } else {
+        d = decide_ee(x.fa[x.SA->e[2 * i]], x.fa[x.SA->e[2 * i + 1]], x.fb[x.SB->e[2 * j]],
+                      x.fb[x.SB->e[2 * j + 1]], x.R, x.S);
+      }
+      keep = d == DEC_TRUE;
+      if (d == DEC_UNDECIDED) keep = exact_filter(SEG, i, j, a.rV, x.va, x.ra, *x.SA, x.vb, x.rb, *x.SB);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) {
+      const uint32_t pos = count + __popc(m & lt);
+      if (Fill)
+        write_feature(a, base + pos, x.A, x.B, x.pid, seg_type(SEG), seg_swap(SEG), i, j);
+      else if (pos < FEAT_SLOTS)
+        a.slots[x.u * FEAT_SLOTS + pos] = (uint16_t)((SEG << 12) | (i << 6) | j);
+    }
+    count += __popc(m);
+  }
+}
+
+// appends the lanes with keep set (index idx0 + lane) to L at off; returns the new length
+__device__ __forceinline__ int list_append(uint8_t* L, int off, bool keep, int idx0, int lane, uint32_t lt) {
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  if (keep) L[off + __popc(m & lt)] = (uint8_t)(idx0 + lane);
+  return off + __popc(m);
+}
+
+template <bool Fill>
+__global__ void __launch_bounds__(PT, 4) k_feat_dec(FeatArgs a) {
+  // per warp: gated A vertices, gated B vertices, B vertices near A, A edges near B,
+  // B edges near A, A faces near B, B faces near A
+  __shared__ uint8_t lists[PT / 32][288];
+  const int lane = threadIdx.x & 31;
+  uint8_t* LgA = lists[threadIdx.x >> 5];
+  uint8_t* LgB = LgA + 32;
+  uint8_t* LvB = LgA + 64;
+  uint8_t* LeA = LgA + 96;
+  uint8_t* LeB = LgA + 160;
+  uint8_t* LfA = LgA + 224;
+  uint8_t* LfB = LgA + 256;
+  const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (uint64_t u = warp; u < a.nu; u += nwarps) {
+    uint32_t count = 0;
+    const uint32_t base = Fill ? a.foff[u] : 0;
+    if (!a.pass[u]) {
+      if (!Fill && lane == 0) a.fcnt[u] = 0;
+      continue;
+    }
+    DecUnit x;
+    x.u = u;
+    x.A = a.u_owner[u];
+    x.SA = &a.shapes[a.P.type[x.A]];
+    x.ra = x.SA->r * a.P.f[HOM][x.A];
+    x.va = vview(a, x.A);
+    if (a.u_kind[u]) {
+      driver_unit<Fill>(a, u, x.A, *x.SA, x.ra, x.va, base, lane, lt);
+      continue;
+    }
+    const ShapeDev& SA = *x.SA;
+    x.B = a.u_partner[u];
+    x.pid = a.u_pid[u];
+    x.SB = &a.shapes[a.P.type[x.B]];
+    const ShapeDev& SB = *x.SB;
+    x.rb = SB.r * a.P.f[HOM][x.B];
+    x.vb = vview(a, x.B);
+    const uint32_t A = x.A, B = x.B;
+    if (Fill) {  // the count pass recorded the features of this unit unless they overflowed the slots
+      const uint32_t cnt = a.foff[u + 1] - base;
+      if (cnt <= FEAT_SLOTS) {
+        if ((uint32_t)lane < cnt) {
+          const uint32_t w = a.slots[u * FEAT_SLOTS + lane];
+          const int seg = (int)(w >> 12);
+          write_feature(a, base + lane, A, B, x.pid, seg_type(seg), seg_swap(seg), (w >> 6) & 63u, w & 63u);
+        }
+        continue;
+      }
+    }
+    const F3 dR = f3((float)(a.P.f[RX][B] - a.P.f[RX][A]), (float)(a.P.f[RY][B] - a.P.f[RY][A]),
+                     (float)(a.P.f[RZ][B] - a.P.f[RZ][A]));
+    const F3 zero = f3(0.f, 0.f, 0.f);
+    const uint64_t oA = (uint64_t)A * a.MV, oB = (uint64_t)B * a.MV;
+    x.fa = FView{a.fvx + oA, a.fvy + oA, a.fvz + oA, zero};
+    x.fb = FView{a.fvx + oB, a.fvy + oB, a.fvz + oB, dR};
+    // S bounds every |coordinate| relative to A's centre: measured on the vertices
+    float sv = fmaxf(lane < SA.nv ? flen(x.fa[lane]) : 0.f, lane < SB.nv ? flen(x.fb[lane]) : 0.f);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) sv = fmaxf(sv, __shfl_xor_sync(0xffffffffu, sv, o));
+    x.S = sv * 1.001f + (float)(x.ra + x.rb + a.rV);
+    x.R = (float)(x.ra + x.rb + a.rV);
+    x.rV = (float)a.rV;
+    const float lim = x.R + x.S * 6.1035156e-05f;  // R + 2^-14 S
+    const float* bA = a.fbox + (uint64_t)A * FBOX_STRIDE;
+    const float* bB = a.fbox + (uint64_t)B * FBOX_STRIDE;
+    // Lanes are packed over both particles' features, A's first: a lane of side A
+    // tests its feature against B's boxes, a lane of side B against A's.
+    int nA = 0, nB = 0, nvB = 0, neA = 0, neB = 0, nfA = 0, nfB = 0;
+    // vertex gates (OBB::intersect of the vertex box with the other particle's OBB) and
+    // B vertices near A (VV columns)
+    for (int k0 = 0; k0 < SA.nv + SB.nv; k0 += 32) {
+      const int k = k0 + lane;
+      const bool sideA = k < SA.nv, valid = k < SA.nv + SB.nv;
+      const int vi = sideA ? k : k - SA.nv;
+      int d = DEC_FALSE;
+      bool near = false;
+      F3 p = zero;
+      if (valid) {
+        p = sideA ? x.fa[vi] : x.fb[vi];
+        d = decide_gate(load_obbf(sideA ? bB : bA, sideA ? dR : zero), p, (float)(sideA ? x.ra : x.rb), x.S);
+        if (!sideA) near = slab_near_point(load_slabs(bA, zero), p, lim);
+      }
+      bool g = d == DEC_TRUE;
+      if (__any_sync(0xffffffffu, d == DEC_UNDECIDED) && d == DEC_UNDECIDED) {
+        OBBd o = load_obb(a.obb + (uint64_t)(sideA ? B : A) * 15);
+        obb_enlarge(o, 0.5 * a.rV);
+        obb_enlarge(o, 0.5 * a.rV);
+        g = vertex_gate(o, sideA ? x.va[vi] : x.vb[vi], sideA ? x.ra : x.rb);
+      }
+      nA = list_append(LgA, nA, g && sideA, vi - lane, lane, lt);
+      nB = list_append(LgB, nB, g && valid && !sideA, vi - lane, lane, lt);
+      nvB = list_append(LvB, nvB, near, vi - lane, lane, lt);
+    }
+    // edges (extended by rV times their length) and faces near the other particle
+    for (int k0 = 0; k0 < SA.ne + SB.ne; k0 += 32) {
+      const int k = k0 + lane;
+      const bool sideA = k < SA.ne, valid = k < SA.ne + SB.ne;
+      const int e = sideA ? k : k - SA.ne;
+      bool near = false;
+      if (valid) {
+        const FView& fv = sideA ? x.fa : x.fb;
+        const int* ev = sideA ? SA.e : SB.e;
+        near = slab_near_segment(load_slabs(sideA ? bB : bA, sideA ? dR : zero), fv[ev[2 * e]], fv[ev[2 * e + 1]],
+                                 x.rV, lim);
+      }
+      neA = list_append(LeA, neA, near && sideA, e - lane, lane, lt);
+      neB = list_append(LeB, neB, near && !sideA, e - lane, lane, lt);
+    }
+    for (int k0 = 0; k0 < SA.nf + SB.nf; k0 += 32) {
+      const int k = k0 + lane;
+      const bool sideA = k < SA.nf, valid = k < SA.nf + SB.nf;
+      const int f = sideA ? k : k - SA.nf;
+      bool near = false;
+      if (valid)
+        near = slab_near_face(load_slabs(sideA ? bB : bA, sideA ? dR : zero), sideA ? x.fa : x.fb,
+                              sideA ? SA : SB, f, lim);
+      nfA = list_append(LfA, nfA, near && sideA, f - lane, lane, lt);
+      nfB = list_append(LfB, nfB, near && !sideA, f - lane, lane, lt);
+    }
+    __syncwarp();
+    dec_segment<0, Fill>(a, x, LgA, nA, LvB, nvB, count, base, lane, lt);
+    dec_segment<1, Fill>(a, x, LgA, nA, LeB, neB, count, base, lane, lt);
+    dec_segment<2, Fill>(a, x, LeA, neA, LgB, nB, count, base, lane, lt);
+    dec_segment<3, Fill>(a, x, LgA, nA, LfB, nfB, count, base, lane, lt);
+    dec_segment<4, Fill>(a, x, LfA, nfA, LgB, nB, count, base, lane, lt);
+    dec_segment<5, Fill>(a, x, LeA, neA, LeB, neB, count, base, lane, lt);
+    __syncwarp();
     if (!Fill && lane == 0) a.fcnt[u] = count;
   }
 }
@@ -747,6 +953,8 @@ PolyArgs make_pargs(dem_ctx* c) {
   a.fx = c->vrf[0];
   a.fy = c->vrf[1];
   a.fz = c->vrf[2];
+  a.fbox = c->pfbox;
+  a.rV = c->prm.rcut_inc;
   return a;
 }
 }  // namespace
@@ -837,6 +1045,8 @@ static FeatArgs make_fargs(dem_ctx* c, uint64_t nu) {
   a.fvx = c->vrf[0];
   a.fvy = c->vrf[1];
   a.fvz = c->vrf[2];
+  a.fbox = c->pfbox;
+  a.slots = c->u_slots;
   return a;
 }
 
@@ -846,9 +1056,9 @@ int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total) {
   {
     ProfScope ps(c, K_BROAD_COUNT, nu ? 1 : 0);
     if (nu && c->prm.fp32_broad_phase)
-      k_feat<false, true><<<blocks, PT, 0, c->stream>>>(a);
+      k_feat_dec<false><<<blocks, PT, 0, c->stream>>>(a);
     else if (nu)
-      k_feat<false, false><<<blocks, PT, 0, c->stream>>>(a);
+      k_feat<false><<<blocks, PT, 0, c->stream>>>(a);
   }
   int rc = scan_exclusive_u32(c, c->f_cnt, c->f_off, nu);
   if (rc) return rc;
@@ -862,9 +1072,9 @@ int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
   const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
   ProfScope ps(c, K_BROAD_FILL, 2);
   if (nu && c->prm.fp32_broad_phase)
-    k_feat<true, true><<<blocks, PT, 0, c->stream>>>(a);
+    k_feat_dec<true><<<blocks, PT, 0, c->stream>>>(a);
   else if (nu)
-    k_feat<true, false><<<blocks, PT, 0, c->stream>>>(a);
+    k_feat<true><<<blocks, PT, 0, c->stream>>>(a);
   k_own_from_units<<<grid_for(c->n + 1, 256), 256, 0, c->stream>>>(c->n, c->u_off, c->f_off, c->own_off[1 - c->icur]);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;

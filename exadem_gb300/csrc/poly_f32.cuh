@@ -62,6 +62,90 @@ __device__ __forceinline__ OBBf obb_f32(const OBBd& o, V3 origin) {
   return r;
 }
 
+// Per-particle FP32 boxes written at a rebuild (floats, stride FBOX_STRIDE):
+//   [0, 15)  gate OBB as OBBf (centre relative to the particle centre, axes, extents)
+//   [15, 24) three unit slab directions d_k
+//   [24, 27) slab centres c_k and [27, 30) half widths h_k: every vertex v of the
+//            particle (relative to its centre) has |v.d_k - c_k| <= h_k
+constexpr int FBOX_STRIDE = 32;
+
+__device__ __forceinline__ void store_obbf(float* w, const OBBf& o) {
+  w[0] = o.c.x;
+  w[1] = o.c.y;
+  w[2] = o.c.z;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    w[3 + 3 * k] = o.e[k].x;
+    w[4 + 3 * k] = o.e[k].y;
+    w[5 + 3 * k] = o.e[k].z;
+    w[12 + k] = o.ext[k];
+  }
+}
+
+__device__ __forceinline__ OBBf load_obbf(const float* w, F3 off) {
+  OBBf o;
+  o.c = f3(w[0], w[1], w[2]) + off;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    o.e[k] = f3(w[3 + 3 * k], w[4 + 3 * k], w[5 + 3 * k]);
+    o.ext[k] = w[12 + k];
+  }
+  return o;
+}
+
+// Vertex slabs of a particle moved to another origin (off = centre - origin)
+struct Slabs {
+  F3 d[3];
+  float c[3], h[3];
+};
+
+__device__ __forceinline__ Slabs load_slabs(const float* w, F3 off) {
+  Slabs s;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    s.d[k] = f3(w[15 + 3 * k], w[16 + 3 * k], w[17 + 3 * k]);
+    s.c[k] = w[24 + k] + fdot(off, s.d[k]);
+    s.h[k] = w[27 + k];
+  }
+  return s;
+}
+
+// Necessary conditions for a feature to lie within distance lim of the other
+// particle's vertex hull (which the slabs contain): false when some slab,
+// widened by lim, misses the feature.  lim includes a margin m >= 2^-14 S, far
+// above the FP32 error of the projections (about 2^-20 S).
+__device__ __forceinline__ bool slab_near_point(const Slabs& s, F3 p, float lim) {
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    if (fabsf(fdot(p, s.d[k]) - s.c[k]) > s.h[k] + lim) return false;
+  return true;
+}
+// segment p0-p1 extended by ext * |p1 - p0| at both ends
+__device__ __forceinline__ bool slab_near_segment(const Slabs& s, F3 p0, F3 p1, float ext, float lim) {
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const float a = fdot(p0, s.d[k]) - s.c[k], b = fdot(p1, s.d[k]) - s.c[k];
+    const float x = ext * fabsf(b - a);
+    if (fminf(a, b) - x > s.h[k] + lim || fmaxf(a, b) + x < -(s.h[k] + lim)) return false;
+  }
+  return true;
+}
+__device__ __forceinline__ bool slab_near_face(const Slabs& s, const FView& v, const ShapeDev& sh, int face,
+                                               float lim) {
+  const int b = sh.fo[face], nf = sh.fo[face + 1] - b;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float lo = 3.4e38f, hi = -3.4e38f;
+    for (int q = 0; q < nf; q++) {
+      const float pr = fdot(v[sh.fv[b + q]], s.d[k]) - s.c[k];
+      lo = fminf(lo, pr);
+      hi = fmaxf(hi, pr);
+    }
+    if (lo > s.h[k] + lim || hi < -(s.h[k] + lim)) return false;
+  }
+  return true;
+}
+
 enum : int { DEC_FALSE = 0, DEC_TRUE = 1, DEC_UNDECIDED = 2 };
 
 constexpr float F32_U = 5.9604645e-08f;  // 2^-24

@@ -83,6 +83,27 @@ def test_fp32_prefilters_same_list(native_lib, seed):
     assert bit_equal_fraction(a.particles(), b.particles()) == 1.0
 
 
+@pytest.mark.parametrize("distort", [False, True])
+def test_fp32_broad_phase_same_list_large(native_lib, distort):
+    """64k polyhedra: the FP32-decided, slab-gated enumeration writes the FP64 list.
+    distort: homothety in [0.8, 1.2] and quaternions 2 % off unit norm (qrotate is
+    then not a rotation), which the per-particle vertex slabs must still bound."""
+    w = [W.polyhedra_lattice(nx=40, ny=40, nz=40, seed=11, **f) for f in ({}, dict(fp32_broad_phase=1))]
+    if distort:
+        rng = np.random.default_rng(3)
+        h = rng.uniform(0.8, 1.2, 64000)
+        for x in w:
+            x.particles["homothety"] = h.copy()
+            for k in ("qw", "qx", "qy", "qz"):
+                x.particles[k] = x.particles[k] * 1.02
+    a, b = (x.build() for x in w)
+    for s in (a, b):
+        s.update_particle_neighbors()
+    la, lb = a.interactions(), b.interactions()
+    assert len(la["type"]) > 100_000
+    assert_same_list(la, lb)
+
+
 def test_fp32_decisions_selftest(native_lib):
     """The FP32 decisions of the broad-phase tests agree with FP64 whenever they decide."""
     import ctypes as C
