@@ -200,9 +200,16 @@ void free_poly(dem_ctx* c) {
   }
   cudaFree(c->pobb);
   cudaFree(c->pfbox);
+  cudaFree(c->pqb);
+  cudaFree(c->vneed);
+  cudaFree(c->vneed_off);
+  cudaFree(c->vlist);
   cudaFree(c->u_off);
   c->pobb = nullptr;
   c->pfbox = nullptr;
+  c->pqb = nullptr;
+  c->vneed = c->vneed_off = c->vlist = nullptr;
+  c->nvlist = 0;
   c->u_off = nullptr;
   c->vcap = 0;
 }
@@ -219,6 +226,10 @@ int alloc_poly(dem_ctx* c) {
   }
   DEM_CUDA_TRY(c, cudaMalloc(&c->pobb, std::max<uint64_t>(c->pcap, 1) * 15 * 8));
   DEM_CUDA_TRY(c, cudaMalloc(&c->pfbox, std::max<uint64_t>(c->pcap, 1) * 32 * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->pqb, std::max<uint64_t>(c->pcap, 1) * sizeof(float4)));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->vneed, (std::max<uint64_t>(c->pcap, 1) + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->vneed_off, (std::max<uint64_t>(c->pcap, 1) + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->vlist, std::max<uint64_t>(c->pcap, 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_off, (std::max<uint64_t>(c->pcap, 1) + 1) * 4));
   c->vcap = need;
   return DEM_OK;
@@ -286,6 +297,7 @@ int update_neighbors_poly(dem_ctx* c) {
   c->have_list = true;
   c->hist_valid = true;
   if ((rc = launch_reverse_lists(c))) return rc;
+  if ((rc = launch_vertex_list(c))) return rc;
   c->rebuilds++;
   return DEM_OK;
 }
@@ -657,7 +669,10 @@ int dem_set_shapes(dem_ctx* c, const dem_shape* shapes, int nshapes) {
     o.nf = d.nf;
     o.r = d.radius;
     double mx = 0;
-    for (int i = 0; i < 3 * d.nv; i++) o.v[i] = d.vertices[i];
+    for (int i = 0; i < 3 * d.nv; i++) {
+      o.v[i] = d.vertices[i];
+      o.vf[i] = (float)d.vertices[i];
+    }
     for (int i = 0; i < d.nv; i++)
       mx = std::max(mx, std::sqrt(o.v[3 * i] * o.v[3 * i] + o.v[3 * i + 1] * o.v[3 * i + 1] + o.v[3 * i + 2] * o.v[3 * i + 2]));
     o.maxv = mx;
@@ -734,6 +749,20 @@ int dem_step(dem_ctx* c, int nsteps) {
   int rc = need_list(c);
   if (rc) return rc;
   for (int s = 0; s < nsteps; s++) {
+    if (c->poly && c->prm.fused_step) {
+      // prolog + vertex_displ_over decided in FP32; rebuild (all vertices) or the
+      // vertices of the particles in the list; contact; gather + f2a + epilog
+      if ((rc = launch_poly_fused_prolog(c))) return rc;
+      if ((rc = read_flag(c, 0))) return rc;
+      if (c->h_scalars[0]) {
+        if ((rc = update_neighbors(c))) return rc;
+      } else if ((rc = launch_poly_vertices_listed(c))) {
+        return rc;
+      }
+      if ((rc = launch_contact_poly(c))) return rc;
+      if ((rc = launch_fused_epilog(c))) return rc;
+      continue;
+    }
     if (c->poly) {
       // prolog, vertices + vertex_displ_over, rebuild if needed, forces, force_to_accel, epilog
       if ((rc = launch_prolog(c))) return rc;

@@ -90,6 +90,11 @@ struct dem_ctx {
   double* pobb = nullptr;             // world OBB per particle (15 doubles)
   float* vrf[3] = {};                 // FP32 vertices relative to the particle centre (rebuild time)
   float* pfbox = nullptr;             // FP32 gate OBB + vertex slabs per particle (rebuild time)
+  float4* pqb = nullptr;              // FP32 orientation backup (w, x, y, z) at the last rebuild
+  uint32_t* vneed = nullptr;          // 1 for particles whose vertices the interaction list uses (n+1)
+  uint32_t* vneed_off = nullptr;      // exclusive scan of vneed (n+1)
+  uint32_t* vlist = nullptr;          // those particles, ascending
+  uint64_t nvlist = 0;
   uint64_t vcap = 0;
   uint32_t* u_off = nullptr;          // n+1 unit offsets per owner
   uint32_t* u_owner = nullptr;        // unit arrays (ucap each)
@@ -171,6 +176,9 @@ int launch_poly_units(dem_ctx* c, uint64_t* nu_out, int (*grow_units)(dem_ctx*, 
 int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total);
 int launch_poly_feature_fill(dem_ctx* c, uint64_t nu);
 int launch_contact_poly(dem_ctx* c);
+int launch_poly_fused_prolog(dem_ctx* c);     // prolog + FP32-decided vertex_displ_over flag
+int launch_vertex_list(dem_ctx* c);           // particles whose vertices the list uses (host sync)
+int launch_poly_vertices_listed(dem_ctx* c);  // FP64 vertices of those particles
 // k_step_fused.cu
 int launch_fused_prolog(dem_ctx* c);
 int launch_contact_compact(dem_ctx* c);

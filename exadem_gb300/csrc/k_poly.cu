@@ -22,6 +22,7 @@
 #include <algorithm>
 
 #include "contact_core.cuh"
+#include "integrate_core.cuh"
 #include "poly_core.cuh"
 #include "poly_f32.cuh"
 
@@ -46,6 +47,7 @@ struct PolyArgs {
   float* fy;
   float* fz;
   float* fbox;  // FBOX_STRIDE per particle: FP32 gate OBB and vertex slabs (rebuild time)
+  float4* qb;   // FP32 orientation at the last rebuild
   double rV;
 };
 
@@ -85,6 +87,7 @@ __global__ void k_poly_vertices(PolyArgs a, double thr2, unsigned long long* fla
                                o.e3.x, o.e3.y, o.e3.z, o.ext.x, o.ext.y, o.ext.z};
 #pragma unroll
       for (int k = 0; k < 15; k++) w[k] = vals[k];
+      a.qb[s] = make_float4((float)q.w, (float)q.x, (float)q.y, (float)q.z);
       // FP32 copy of the gate OBB (relative to the centre, enlarged by 0.5 rV twice as
       // in the feature enumeration) and vertex slabs along its normalised axes
       float* fb = a.fbox + s * FBOX_STRIDE;
@@ -116,6 +119,77 @@ __global__ void k_poly_vertices(PolyArgs a, double thr2, unsigned long long* fla
   if (Displ) {
     if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
   }
+}
+
+// prolog (integration) + vertex_displ_over (backup_dem.hpp:65-110) decided in
+// FP32 per vertex (decide_displ); an undecided vertex is recomputed in FP64
+// exactly as the reference does (world vertex minus the stored backup vertex).
+// No vertex is written.
+__global__ void k_poly_fused_prolog(PolyArgs a, double delta_t, double half_delta_t, double delta_t2_2,
+                                    double thr2, float thr, unsigned long long* flag) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool over = false;
+  if (s < a.n) {
+    prolog_one(a.P, s, delta_t, half_delta_t, delta_t2_2);
+    const ShapeDev& sh = a.shapes[a.P.type[s]];
+    const double h = a.P.f[HOM][s];
+    const V3 p = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
+    const Q4 q = {a.P.f[QW][s], a.P.f[QX][s], a.P.f[QY][s], a.P.f[QZ][s]};
+    const F3 dp = f3((float)(p.x - a.P.f[BX][s]), (float)(p.y - a.P.f[BY][s]), (float)(p.z - a.P.f[BZ][s]));
+    const float4 qn = make_float4((float)q.w, (float)q.x, (float)q.y, (float)q.z);
+    const float4 qb = a.qb[s];
+    const float hf = (float)h;
+    const float q2 = fmaxf(fmaxf(qn.x * qn.x + qn.y * qn.y + qn.z * qn.z + qn.w * qn.w,
+                                 qb.x * qb.x + qb.y * qb.y + qb.z * qb.z + qb.w * qb.w),
+                           1.f);
+    const float pabs = (float)(fabs(p.x) + fabs(p.y) + fabs(p.z));
+    for (int k = 0; k < sh.nv && !over; k++) {
+      const F3 v0 = f3(sh.vf[3 * k], sh.vf[3 * k + 1], sh.vf[3 * k + 2]) * hf;
+      const int d = decide_displ(dp, qn, qb, v0, q2, pabs, thr);
+      if (d == DEC_UNDECIDED) {
+        const V3 v = world_vertex(sh, k, p, q, h);
+        const uint64_t idx = s * (uint64_t)a.MV + k;
+        const V3 dr = v - mk(a.bx[idx], a.by[idx], a.bz[idx]);
+        over = dot(dr, dr) >= thr2;
+      } else {
+        over = d == DEC_TRUE;
+      }
+    }
+  }
+  if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+}
+
+// vertices of the listed particles (those in the interaction list), FP64
+__global__ void k_poly_vertices_listed(PolyArgs a, const uint32_t* __restrict__ list, uint64_t count) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const uint32_t s = list[t];
+  const ShapeDev& sh = a.shapes[a.P.type[s]];
+  const V3 p = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
+  const Q4 q = {a.P.f[QW][s], a.P.f[QX][s], a.P.f[QY][s], a.P.f[QZ][s]};
+  const double h = a.P.f[HOM][s];
+  for (int k = 0; k < sh.nv; k++) {
+    const V3 v = world_vertex(sh, k, p, q, h);
+    const uint64_t idx = (uint64_t)s * a.MV + k;
+    a.vx[idx] = v.x;
+    a.vy[idx] = v.y;
+    a.vz[idx] = v.z;
+  }
+}
+
+// marks the particles whose vertices the interaction list uses: both sides of the
+// vertex/edge/face types, the owner of the driver types
+__global__ void k_vertex_needs(IArrays I, uint64_t ni, uint32_t* __restrict__ need) {
+  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ni) return;
+  need[I.owner[k]] = 1u;
+  if (meta_type(I.meta[k]) <= DEM_ITYPE_EDGE_EDGE) need[I.partner[k]] = 1u;
+}
+
+__global__ void k_vertex_compact(const uint32_t* __restrict__ need, const uint32_t* __restrict__ off, uint64_t n,
+                                 uint32_t* __restrict__ list) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < n && need[s]) list[off[s]] = (uint32_t)s;
 }
 
 __device__ __forceinline__ OBBd load_obb(const double* o) {
@@ -954,10 +1028,49 @@ PolyArgs make_pargs(dem_ctx* c) {
   a.fy = c->vrf[1];
   a.fz = c->vrf[2];
   a.fbox = c->pfbox;
+  a.qb = c->pqb;
   a.rV = c->prm.rcut_inc;
   return a;
 }
 }  // namespace
+
+int launch_poly_fused_prolog(dem_ctx* c) {
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars, 0, sizeof(unsigned long long), c->stream));
+  ProfScope ps(c, K_PROLOG, c->n ? 1 : 0);
+  if (!c->n) return DEM_OK;
+  const PolyArgs a = make_pargs(c);
+  const double dt = c->prm.dt;
+  const double md = c->prm.rcut_inc * 0.5;
+  k_poly_fused_prolog<<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, dt, dt * 0.5, dt * dt * 0.5, md * md, (float)md,
+                                                                 c->d_scalars);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+int launch_vertex_list(dem_ctx* c) {
+  c->nvlist = 0;
+  if (!c->n) return DEM_OK;
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->vneed, 0, (c->n + 1) * 4, c->stream));
+  if (c->ni)
+    k_vertex_needs<<<grid_for(c->ni, 256), 256, 0, c->stream>>>(c->I[c->icur], c->ni, c->vneed);
+  int rc = scan_exclusive_u32(c, c->vneed, c->vneed_off, c->n);
+  if (rc) return rc;
+  k_vertex_compact<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->vneed, c->vneed_off, c->n, c->vlist);
+  uint32_t cnt = 0;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(&cnt, c->vneed_off + c->n, 4, cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->nvlist = cnt;
+  return DEM_OK;
+}
+
+int launch_poly_vertices_listed(dem_ctx* c) {
+  ProfScope ps(c, K_PROLOG, c->nvlist ? 1 : 0);
+  if (!c->nvlist) return DEM_OK;
+  const PolyArgs a = make_pargs(c);
+  k_poly_vertices_listed<<<grid_for(c->nvlist, PT), PT, 0, c->stream>>>(a, c->vlist, c->nvlist);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
 
 // vertices (+ displacement flag, or + backup and world OBBs at a rebuild)
 int launch_poly_vertices(dem_ctx* c, int mode) {

@@ -57,7 +57,7 @@ struct Case {
 __device__ Case run_case(uint64_t seed, uint64_t t) {
   Rng g{seed * 0x2545f4914f6cdd1dull + t * 0x9e3779b97f4a7c15ull};
   g.next();
-  const int kind = (int)(t % 5);
+  const int kind = (int)(t % 6);
   const double sc = pow(10.0, g.uni(-3.0, 1.0));  // particle size
   const V3 pA = g.vec(100.0 * sc);
   const V3 pB = pA + g.unit() * (g.uni(0.0, 3.0) * sc);
@@ -191,6 +191,37 @@ __device__ Case run_case(uint64_t seed, uint64_t t) {
       out.dec = decide_vf(a, fv, sf, 0, Rf, S);
       break;
     }
+    case 5: {  // vertex displacement since the last rebuild against max_displ
+      const V3 p = pA;
+      const double h = g.uni(0.5, 2.0);
+      const V3 v0 = g.vec(sc);
+      Q4 q = {g.uni(-1, 1), g.uni(-1, 1), g.uni(-1, 1), g.uni(-1, 1)};
+      const double qs = (g.next() % 4 == 0 ? g.uni(0.98, 1.02) : 1.0) /
+                        sqrt(q.w * q.w + q.x * q.x + q.y * q.y + q.z * q.z);
+      q = {q.w * qs, q.x * qs, q.y * qs, q.z * qs};
+      // backup orientation: q turned by a small angle about a random axis
+      const V3 ax = g.unit();
+      const double an = g.uni(0.0, 0.2) * ((g.next() & 1) ? 1.0 : 1e-3);
+      const Q4 dq = {cos(0.5 * an), ax.x * sin(0.5 * an), ax.y * sin(0.5 * an), ax.z * sin(0.5 * an)};
+      const Q4 qb = {dq.w * q.w - dq.x * q.x - dq.y * q.y - dq.z * q.z, dq.w * q.x + dq.x * q.w + dq.y * q.z - dq.z * q.y,
+                     dq.w * q.y - dq.x * q.z + dq.y * q.w + dq.z * q.x, dq.w * q.z + dq.x * q.y - dq.y * q.x + dq.z * q.w};
+      const double md = g.uni(0.001, 0.1) * sc;
+      // backup centre placing the backup vertex at md (+ a small offset) from the current one
+      const V3 v = p + qrotate(q, h * v0);
+      const V3 pb = v - qrotate(qb, h * v0) - g.unit() * (md + g.eps(sc));
+      const V3 b = pb + qrotate(qb, h * v0);
+      const V3 dr = v - b;
+      out.exact = dot(dr, dr) >= md * md;
+      const float4 qn = make_float4((float)q.w, (float)q.x, (float)q.y, (float)q.z);
+      const float4 qbf = make_float4((float)qb.w, (float)qb.x, (float)qb.y, (float)qb.z);
+      const float q2 = fmaxf(fmaxf(qn.x * qn.x + qn.y * qn.y + qn.z * qn.z + qn.w * qn.w,
+                                   qbf.x * qbf.x + qbf.y * qbf.y + qbf.z * qbf.z + qbf.w * qbf.w),
+                             1.f);
+      const F3 dp = f3((float)(p.x - pb.x), (float)(p.y - pb.y), (float)(p.z - pb.z));
+      const F3 v0h = f3((float)v0.x, (float)v0.y, (float)v0.z) * (float)h;
+      out.dec = decide_displ(dp, qn, qbf, v0h, q2, (float)(fabs(p.x) + fabs(p.y) + fabs(p.z)), (float)md);
+      break;
+    }
     default: {  // edge - edge
       const V3 di = g.unit();
       V3 dj;
@@ -235,8 +266,8 @@ __device__ Case run_case(uint64_t seed, uint64_t t) {
 
 // counters: [kind][0] mismatches, [1] undecided, [2] decided true, [3] exact true
 __global__ void k_poly_dec_test(uint64_t n, uint64_t seed, unsigned long long* cnt) {
-  __shared__ unsigned long long sc[20];
-  if (threadIdx.x < 20) sc[threadIdx.x] = 0;
+  __shared__ unsigned long long sc[24];
+  if (threadIdx.x < 24) sc[threadIdx.x] = 0;
   __syncthreads();
   for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
     const Case c = run_case(seed, t);
@@ -246,7 +277,7 @@ __global__ void k_poly_dec_test(uint64_t n, uint64_t seed, unsigned long long* c
     if (c.exact) atomicAdd(&sc[c.kind * 4 + 3], 1ull);
   }
   __syncthreads();
-  if (threadIdx.x < 20) atomicAdd(&cnt[threadIdx.x], sc[threadIdx.x]);
+  if (threadIdx.x < 24) atomicAdd(&cnt[threadIdx.x], sc[threadIdx.x]);
 }
 }  // namespace
 }  // namespace dem
@@ -254,13 +285,13 @@ __global__ void k_poly_dec_test(uint64_t n, uint64_t seed, unsigned long long* c
 extern "C" int dem_selftest_poly_decisions(uint64_t n, uint64_t seed, uint64_t* counts) {
   if (!counts) return DEM_ERR_INVALID_ARG;
   unsigned long long* d = nullptr;
-  if (cudaMalloc(&d, 20 * sizeof(unsigned long long)) != cudaSuccess) return DEM_ERR_CUDA;
-  cudaMemset(d, 0, 20 * sizeof(unsigned long long));
+  if (cudaMalloc(&d, 24 * sizeof(unsigned long long)) != cudaSuccess) return DEM_ERR_CUDA;
+  cudaMemset(d, 0, 24 * sizeof(unsigned long long));
   dem::k_poly_dec_test<<<608, 128>>>(n, seed, d);
-  unsigned long long h[20];
+  unsigned long long h[24];
   const bool ok = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess;
   cudaFree(d);
   if (!ok || cudaGetLastError() != cudaSuccess) return DEM_ERR_CUDA;
-  for (int k = 0; k < 20; k++) counts[k] = h[k];
+  for (int k = 0; k < 24; k++) counts[k] = h[k];
   return DEM_OK;
 }

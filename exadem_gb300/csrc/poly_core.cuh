@@ -27,6 +27,7 @@ struct ShapeDev {
   int e[2 * SH_MAXE];
   int fo[SH_MAXF + 1];  // face offsets into fv
   int fv[SH_MAXFV];
+  float vf[3 * SH_MAXV];  // FP32 copy of v (split-precision displacement test)
 };
 
 struct OBBd {

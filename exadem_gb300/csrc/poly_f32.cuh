@@ -152,6 +152,33 @@ constexpr float F32_U = 5.9604645e-08f;  // 2^-24
 constexpr float F32_ETA = 1.9073486e-06f;  // 2^-19: ETA / S
 constexpr float F32_SAFE = 8.f;             // decided only beyond 8x the bound
 
+
+// FP32 rotation by a quaternion (w, x, y, z), the formula of qrotate: v + 2w (u x v) + 2 u x (u x v)
+__device__ __forceinline__ F3 qrotate_f32(float4 q, F3 v) {
+  const F3 u = f3(q.y, q.z, q.w);
+  F3 uv = fcross(u, v);
+  F3 uuv = fcross(u, uv);
+  uv = uv * (2.0f * q.x);
+  uuv = uuv * 2.0f;
+  return v + uv + uuv;
+}
+
+// vertex_displ_over for one vertex (backup_dem.hpp:65-110): over when
+// |v - v_backup|^2 >= thr^2.  FP32 displacement (r - r_b) + (q v0' - q_b v0'),
+// v0' = h v0; dp = FP32 rounding of r - r_b (FP64 difference), qn, qb = FP32
+// roundings of the quaternions, q2 = max(1, |qn|^2, |qb|^2), pabs = |r|_1.
+// Error bound E = 2u|dp| + 26u |v0'| q2 + 2u|d| + 2^-51 (pabs + |v0'|) + u thr
+// (FP32 rounding of each term and of the quaternions, and the FP64 rounding of
+// the reference's absolute vertices); decided beyond 8 E of thr.
+__device__ __forceinline__ int decide_displ(F3 dp, float4 qn, float4 qb, F3 v0h, float q2, float pabs, float thr) {
+  const float u = F32_U;
+  const F3 d = dp + (qrotate_f32(qn, v0h) - qrotate_f32(qb, v0h));
+  const float dl = flen(d), lv = flen(v0h);
+  const float E = 2.f * u * flen(dp) + 26.f * u * lv * q2 + 2.f * u * dl + 4.440892e-16f * (pabs + lv) + u * thr;
+  return dl > thr + F32_SAFE * E ? DEC_TRUE : (dl < thr - F32_SAFE * E ? DEC_FALSE : DEC_UNDECIDED);
+}
+
+
 // one comparison "x > thr" with error bound e: +1 surely greater, -1 surely not, 0 unknown
 __device__ __forceinline__ int cmp_gt(float x, float thr, float e) {
   const float m = F32_SAFE * e;

@@ -15,10 +15,11 @@ extern "C" {
 int dem_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches, uint64_t* fast_path_taken);
 
 /* Draws n seeded near-threshold cases of the polyhedron broad-phase tests
- * (kind = case % 5: 0 vertex gate / OBB::intersect, 1 filter_vv, 2 filter_ve,
- * 3 filter_vf, 4 filter_ee) and evaluates each with its FP32 decision and its
- * FP64 test.  counts[4 * kind + k], k = 0: decided cases whose result differs
- * from FP64 (must be 0), 1: undecided cases, 2: decided true, 3: FP64 true. */
+ * (kind = case % 6: 0 vertex gate / OBB::intersect, 1 filter_vv, 2 filter_ve,
+ * 3 filter_vf, 4 filter_ee, 5 vertex displacement against max_displ) and
+ * evaluates each with its FP32 decision and its FP64 test.
+ * counts[4 * kind + k] (24 entries), k = 0: decided cases whose result differs
+ * from FP64 (must be 0), 1: undecided cases, 2: decided true, 3: FP64 true.  */
 int dem_selftest_poly_decisions(uint64_t n, uint64_t seed, uint64_t* counts);
 #ifdef __cplusplus
 }

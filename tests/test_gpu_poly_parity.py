@@ -41,6 +41,27 @@ def test_lattice_100_steps(native_lib, flags):
     assert g.simulation_state()["n_active_interactions"] == o.simulation_state()["n_active_interactions"]
 
 
+def test_spinning_lattice_rebuild_steps(native_lib):
+    """Fast rotation (vertex speeds ~25 m/s, max_displ reached every ~10 steps):
+    the FP32-decided vertex_displ_over of the fused step rebuilds on the same
+    steps as the oracle, and the state stays on the oracle's."""
+    w = W.polyhedra_lattice(nx=8, ny=8, nz=4, seed=21, fused_step=1, fp32_broad_phase=1)
+    rng = np.random.default_rng(21)
+    n = w.n
+    for k in ("vrotx", "vroty", "vrotz"):
+        w.particles[k] = rng.uniform(-30.0, 30.0, n)
+    g, o = pair(w)
+    for s in (g, o):
+        s.first_iteration()
+    for _ in range(6):
+        for s in (g, o):
+            s.step(10)
+        assert g.rebuild_count() == o.rebuild_count()
+        assert_same_list(g.interactions(), o.interactions())
+    assert g.rebuild_count() >= 4
+    assert_state(g.particles(), o.particles(), 1e-12)
+
+
 def test_floor_deposition(native_lib):
     """Config 3 physics on a small column: polyhedra falling onto a floor between walls."""
     w = W.polyhedra_floor(n=2400, side=12.0)
@@ -108,14 +129,14 @@ def test_fp32_decisions_selftest(native_lib):
     """The FP32 decisions of the broad-phase tests agree with FP64 whenever they decide."""
     import ctypes as C
 
-    counts = (C.c_uint64 * 20)()
-    n = 20_000_000
+    counts = (C.c_uint64 * 24)()
+    n = 24_000_000
     assert native_lib.dem_selftest_poly_decisions(n, 2024, counts) == 0
-    names = ["gate", "vv", "ve", "vf", "ee"]
+    names = ["gate", "vv", "ve", "vf", "ee", "displacement"]
     for k, name in enumerate(names):
         bad, undecided, dec_true, exact_true = counts[4 * k: 4 * k + 4]
         assert bad == 0, (name, bad)
         # every draw sits near a threshold (offsets log-uniform in [1e-10, 1e-1]
         # of the particle size), so a large share stays undecided by design
-        assert undecided < 0.8 * (n // 5), (name, undecided)
+        assert undecided < 0.8 * (n // 6), (name, undecided)
         assert 0 < dec_true <= exact_true, name
