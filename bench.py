@@ -45,9 +45,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--n", type=int, default=None, help="particle count (default: the workload's)")
-    ap.add_argument("--workload", default="spheres", choices=["spheres", "polyhedra", "polyhedra_dense"],
+    ap.add_argument("--workload", default="spheres", choices=["spheres", "polyhedra", "polyhedra_dense", "drums"],
                     help="spheres: 2M spheres on a floor (headline); polyhedra: 200k polyhedra deposition; "
-                         "polyhedra_dense: polyhedra on a dense lattice")
+                         "polyhedra_dense: polyhedra on a dense lattice; drums: 256 rotating drums batched")
+    ap.add_argument("--systems", type=int, default=256, help="drums: number of drums")
     ap.add_argument("--plain", action="store_true", help="plain FP64 path (no FP32 screening)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -158,7 +159,37 @@ def workload(args):
     if args.workload == "polyhedra_dense":
         side = round((args.n or 200_000) ** (1.0 / 3.0))
         return W.polyhedra_lattice(nx=side, ny=side, nz=side, **flags)
+    if args.workload == "drums":
+        return W.drums_batch(nsys=args.systems, nmax=args.n or 200_000, **flags)
     return W.spheres_floor(n=args.n or 2_000_000, **flags)
+
+
+def is_batch(w) -> bool:
+    return hasattr(w, "members")
+
+
+def build_from_host(w, arrays):
+    """The workload's System, with the particle arrays `arrays` (host buffers)."""
+    from exadem_gb300 import System
+
+    s = System(w.params)
+    if is_batch(w):
+        s.set_particles(arrays)
+        for m in w.members:
+            for kw in m.surfaces:
+                s.register_surface(**kw)
+            for kw in m.cylinders:
+                s.register_cylinder(**kw)
+        s.set_systems(w.systems())
+        return s
+    if w.shapes:
+        s.set_shapes(w.shapes)
+    for kw in w.surfaces:
+        s.register_surface(**kw)
+    for kw in w.cylinders:
+        s.register_cylinder(**kw)
+    s.set_particles(arrays)
+    return s
 
 
 WORKLOAD_DESC = {
@@ -168,6 +199,8 @@ WORKLOAD_DESC = {
                  "spheres at 0.35, floor + side walls, Hooke kn=1e5 kt=8e4 mu=0.5, dt=1e-4",
     "polyhedra_dense": "polyhedra_lattice: cubes/tetrahedra/octahedra on a lattice of spacing 1.3, random "
                        "orientations, Hooke kn=1e4, dt=1e-4",
+    "drums": "drums_batch: 256 rotating drums (spheres r~U[0.45,0.55], counts log-uniform in [2e3, 2e5], "
+             "30% fill, 2 rad/s, periodic along the axis), Hooke kn=1e4 kt=8e3 mu=0.4, dt=5e-4",
 }
 
 
@@ -176,6 +209,24 @@ def cpu_baseline(w, budget_s: float = 20.0):
     from oracle.oracle import oracle_system, set_threads
 
     cores = set_threads(os.cpu_count() or 1)
+    if is_batch(w):  # the drums one after another (the oracle runs one system per context)
+        done = 0.0
+        t_all = 0.0
+        nd = 0
+        for m in w.members:
+            o = m.build(oracle_system)
+            o.first_iteration()
+            t0 = time.perf_counter()
+            o.step(10)
+            t_all += time.perf_counter() - t0
+            done += m.n * 10
+            nd += 1
+            o.close()
+            if t_all > budget_s:
+                break
+        return {"value": done / t_all, "unit": UNIT, "cores": cores, "kind": "port",
+                "sample": f"10 Verlet steps of each of the first {nd} drums ({int(done / 10)} spheres), "
+                          f"{t_all:.1f} s"}
     o = w.build(oracle_system)
     t0 = time.perf_counter()
     o.first_iteration()
@@ -194,6 +245,47 @@ def cpu_baseline(w, budget_s: float = 20.0):
                       f"({t_first:.1f} s), {el:.1f} s"}
 
 
+def run_drums_separate(args, w, rank, world, local, dist):
+    """Own plain FP64 GPU path on the batched workload: one context per drum,
+    plain operator kernels, the drums stepped one after another (each dem_step
+    ends with a stream synchronisation).  Wall-clock timing of the K steps."""
+    import torch
+
+    systems = [m.build() for m in w.members]
+    for s in systems:
+        s.first_iteration()
+        s.step(args.warmup)
+        s.reset_kernel_stats()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        barrier(dist)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for s in systems:
+                s.step(1)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        barrier(dist)
+    launches = sum(sum(v["launches"] for v in s.kernel_stats().values()) for s in systems)
+    rebuilds = sum(s.rebuild_count() for s in systems)
+    for s in systems:
+        s.close()
+    el = allmax(dist, el)
+    total = allsum(dist, float(w.n * args.steps))
+    line = {"metric": METRIC, "value": total / el, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random sequential addition)",
+            "config": {"workload": WORKLOAD_DESC["drums"] if args.n is None and args.systems == 256 else
+                       f"drums n_systems={args.systems} nmax={args.n or 200000}", "n_particles": w.n,
+                       "path": "plain FP64 operator kernels, one context per drum, drums stepped in turn",
+                       "timing": "wall clock around K steps of all drums, synchronised on both sides",
+                       "parallelism": "replicas" if world > 1 else "single"},
+            "gpu_launches": launches, "rebuilds_total": rebuilds, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def run_native(args, rank, world, local, dist):
     import numpy as np
     import torch
@@ -203,6 +295,8 @@ def run_native(args, rank, world, local, dist):
     B.build()
     torch.cuda.set_device(local)
     w = workload(args)
+    if is_batch(w) and args.plain:
+        return run_drums_separate(args, w, rank, world, local, dist)
     s = w.build()
     ext = torch.cuda.ExternalStream(s.stream_handle())
     s.first_iteration()
@@ -252,23 +346,17 @@ def run_native(args, rank, world, local, dist):
         from exadem_gb300 import System
 
         pinned = {}
-        for k, v in w.particles.items():
+        host = w.particles() if is_batch(w) else w.particles
+        for k, v in host.items():
             t = torch.empty(v.shape, dtype=torch.from_numpy(v).dtype, pin_memory=True)
             t.numpy()[:] = v
             pinned[k] = t.numpy()
         out = {k: torch.empty(v.shape, dtype=torch.from_numpy(v).dtype, pin_memory=True).numpy()
-               for k, v in w.particles.items()}
-        s2 = System(w.params)
-        if w.shapes:
-            s2.set_shapes(w.shapes)
-        for kw in w.surfaces:
-            s2.register_surface(**kw)
-        for kw in w.cylinders:
-            s2.register_cylinder(**kw)
+               for k, v in host.items()}
         h2d = sum(v.nbytes for v in pinned.values())
         barrier(dist)
         t0 = time.perf_counter()
-        s2.set_particles(pinned)
+        s2 = build_from_host(w, pinned)
         s2.first_iteration()
         s2.step(args.steps)
         from exadem_gb300 import _abi as A
@@ -282,7 +370,8 @@ def run_native(args, rank, world, local, dist):
         el = allmax(dist, el)
         e2e = {"value": total / el, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                "d2h_bytes_per_step": d2h / args.steps,
-               "note": "initial state uploaded, first_iteration, K steps, final state read back; all timed"}
+               "note": "context setup, initial state uploaded, first_iteration, K steps, final state read back; "
+                       "all timed"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -292,13 +381,16 @@ def run_native(args, rank, world, local, dist):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded random sequential addition)",
-        "config": {"workload": WORKLOAD_DESC[args.workload] if args.n is None else f"{args.workload} n={w.n}",
+        "config": {"workload": WORKLOAD_DESC[args.workload] if args.n is None and args.systems == 256
+                   else f"{args.workload} n={w.n}",
                    "n_particles": w.n,
                    "path": "plain FP64 operator kernels" if args.plain else
-                           "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division",
+                           "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division"
+                           + (f", {w.info['systems']} systems in one context" if is_batch(w) else ""),
                    "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
                    "parallelism": "replicas" if world > 1 else "single",
-                   "inputs": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in w.info.items()}},
+                   "inputs": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in w.info.items()
+                              if k != "counts"}},
         "roofline": {"bound": "hbm", "kernel": "contact", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni,
@@ -320,22 +412,28 @@ def run_reference(args, rank, world, local, dist):
 
     cores = set_threads(os.cpu_count() or 1)
     w = workload(args)
-    o = w.build(oracle_system)
-    o.first_iteration()
-    o.step(max(1, min(args.warmup, 3)))
-    steps = max(1, min(args.steps, 20))
-    t0 = time.perf_counter()
-    o.step(steps)
-    el = time.perf_counter() - t0
-    v = w.n * steps / el
+    if is_batch(w):
+        cb = cpu_baseline(w, budget_s=60.0)
+        steps, v = 10, cb["value"]
+        el = w.n * steps / v
+        sample = cb["sample"] + " (C++ restatement of the reference CPU path, one drum at a time)"
+    else:
+        o = w.build(oracle_system)
+        o.first_iteration()
+        o.step(max(1, min(args.warmup, 3)))
+        steps = max(1, min(args.steps, 20))
+        t0 = time.perf_counter()
+        o.step(steps)
+        el = time.perf_counter() - t0
+        v = w.n * steps / el
+        sample = (f"{steps} steps of the full workload (C++ restatement of the reference "
+                  f"CPU path; exaDEM itself cannot be built without exaNBody/onika/MPI)")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
             "ms_per_step": el * 1e3 / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded random sequential addition)", "impl": "reference",
             "config": {"workload": WORKLOAD_DESC[args.workload] if args.n is None else f"{args.workload} n={w.n}",
                        "n_particles": w.n},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{steps} steps of the full workload (C++ restatement of the reference "
-                                       f"CPU path; exaDEM itself cannot be built without exaNBody/onika/MPI)"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

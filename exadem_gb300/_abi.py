@@ -72,6 +72,12 @@ class State(C.Structure):
                 ("n_active_interactions", C.c_uint64)]
 
 
+class SystemDesc(C.Structure):
+    """dem_system: one independent system of a batched context."""
+    _fields_ = [("first", C.c_uint64), ("count", C.c_uint64), ("bounds_lo", D * 3), ("bounds_hi", D * 3),
+                ("periodic", C.c_int32 * 3), ("driver_first", C.c_int32), ("driver_count", C.c_int32)]
+
+
 class InteractionList(C.Structure):
     _fields_ = [("capacity", C.c_uint64), ("count", C.c_uint64), ("owner_id", PU64), ("partner_id", PU64),
                 ("type", PU16), ("swap", PU8), ("owner_sub", PU32), ("partner_sub", PU32),
@@ -148,6 +154,9 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_vertex_displ_over", [_CTX, C.POINTER(C.c_int)])
     _sig(lib, "dem_rebuild_count", [_CTX, PU64])
     _sig(lib, "dem_simulation_state", [_CTX, C.POINTER(State)])
+    _sig(lib, "dem_set_systems", [_CTX, C.POINTER(SystemDesc), C.c_int])
+    _sig(lib, "dem_system_count", [_CTX, C.POINTER(C.c_int)])
+    _sig(lib, "dem_simulation_state_systems", [_CTX, C.POINTER(State), C.c_int])
     _sig(lib, "dem_interaction_count", [_CTX, PU64])
     _sig(lib, "dem_get_interactions", [_CTX, C.POINTER(InteractionList)])
     _sig(lib, "dem_packing_profile", [_CTX, C.c_int, D, D, PD])
@@ -169,7 +178,8 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
             "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_set_shapes", "dem_compute_vertices",
-            "dem_contact_polyhedron", "dem_vertex_displ_over"]
+            "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
+            "dem_simulation_state_systems"]
 
 _LIB = None
 

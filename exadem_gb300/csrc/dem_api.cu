@@ -153,18 +153,23 @@ int alloc_records(dem_ctx* c, uint64_t need) {
 }
 
 // Cell grid: cell size >= nbh_dist = 2*r_max + rcut_inc (dem_rcut_max.cpp:60, config_globals.msp:35-37).
-int setup_grid(dem_ctx* c) {
+// Cell grid of one system: cs = max(cell_size, nbh_dist) with nbh_dist =
+// 2 r_max + rcut_inc (dem_rcut_max.cpp:60, config_globals.msp:35-37);
+// periodic axes get floor(L / cs) cells of L / dims, the others ceil(L / cs).
+static int make_grid(dem_ctx* c, const double* lo, const double* hi, const int32_t* periodic, GridDev& g,
+                     uint64_t& nc) {
   const dem_params& p = c->prm;
   const double nd = 2 * c->rad_max + p.rcut_inc;
   const double cs = std::max(p.cell_size, nd);
   if (!(cs > 0)) return c->fail(DEM_ERR_INVALID_ARG, "cell size must be > 0");
-  GridDev g{};
-  uint64_t nc = 1;
+  g = GridDev{};
+  nc = 1;
   for (int d = 0; d < 3; d++) {
-    g.lo[d] = p.bounds_lo[d];
-    g.hi[d] = p.bounds_hi[d];
-    g.L[d] = p.bounds_hi[d] - p.bounds_lo[d];
-    g.periodic[d] = p.periodic[d] ? 1 : 0;
+    g.lo[d] = lo[d];
+    g.hi[d] = hi[d];
+    g.L[d] = hi[d] - lo[d];
+    if (!(g.L[d] > 0)) return c->fail(DEM_ERR_INVALID_ARG, "empty domain");
+    g.periodic[d] = periodic[d] ? 1 : 0;
     if (g.periodic[d]) {
       g.dims[d] = std::max(1, (int)std::floor(g.L[d] / cs));
       if (g.dims[d] < 3) return c->fail(DEM_ERR_INVALID_ARG, "periodic dimension needs at least 3 cells");
@@ -175,8 +180,67 @@ int setup_grid(dem_ctx* c) {
     }
     nc *= (uint64_t)g.dims[d];
   }
-  if (nc > (1ull << 31)) return c->fail(DEM_ERR_INVALID_ARG, "cell grid too large; raise cell_size");
-  c->grid = g;
+  return DEM_OK;
+}
+
+// Grids of all systems, their cell offsets, particle and driver ranges, uploaded.
+int setup_grid(dem_ctx* c) {
+  const dem_params& p = c->prm;
+  std::vector<dem_system> sys = c->systems;
+  if (sys.empty()) {
+    dem_system one{};
+    one.first = 0;
+    one.count = c->n;
+    for (int d = 0; d < 3; d++) {
+      one.bounds_lo[d] = p.bounds_lo[d];
+      one.bounds_hi[d] = p.bounds_hi[d];
+      one.periodic[d] = p.periodic[d];
+    }
+    one.driver_first = 0;
+    one.driver_count = c->ndrv;
+    sys.push_back(one);
+  }
+  const int ns = (int)sys.size();
+  std::vector<GridDev> g(ns);
+  std::vector<uint32_t> coff(ns + 1);
+  std::vector<uint64_t> pfirst(ns + 1);
+  std::vector<int2> dr(ns);
+  uint64_t nc = 0;
+  for (int k = 0; k < ns; k++) {
+    uint64_t nck = 0;
+    int rc = make_grid(c, sys[k].bounds_lo, sys[k].bounds_hi, sys[k].periodic, g[k], nck);
+    if (rc) return rc;
+    coff[k] = (uint32_t)nc;
+    nc += nck;
+    if (nc > (1ull << 31)) return c->fail(DEM_ERR_INVALID_ARG, "cell grid too large; raise cell_size");
+    pfirst[k] = sys[k].first;
+    dr[k] = make_int2(sys[k].driver_first, sys[k].driver_count);
+  }
+  coff[ns] = (uint32_t)nc;
+  pfirst[ns] = c->n;
+  if (ns > c->sys_cap) {
+    cudaFree(c->grids_dev);
+    cudaFree(c->coff_dev);
+    cudaFree(c->pfirst_dev);
+    cudaFree(c->drange_dev);
+    c->grids_dev = nullptr;
+    c->coff_dev = nullptr;
+    c->pfirst_dev = nullptr;
+    c->drange_dev = nullptr;
+    c->sys_cap = 0;
+    DEM_CUDA_TRY(c, cudaMalloc(&c->grids_dev, ns * sizeof(GridDev)));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->coff_dev, (ns + 1) * sizeof(uint32_t)));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->pfirst_dev, (ns + 1) * sizeof(uint64_t)));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->drange_dev, ns * sizeof(int2)));
+    c->sys_cap = ns;
+  }
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->grids_dev, g.data(), ns * sizeof(GridDev), cudaMemcpyHostToDevice, c->stream));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->coff_dev, coff.data(), (ns + 1) * 4, cudaMemcpyHostToDevice, c->stream));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->pfirst_dev, pfirst.data(), (ns + 1) * 8, cudaMemcpyHostToDevice, c->stream));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->drange_dev, dr.data(), ns * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->nsys = ns;
+  c->grid = g[0];
   c->ncell = nc;
   if (nc + 1 > c->ccap) {
     cudaFree(c->cell_cnt);
@@ -272,6 +336,7 @@ int alloc_iarrays(dem_ctx* c, int b, uint64_t need);
 
 // nbh_polyhedron rebuild: bin + reorder, vertices/backup/OBBs, units, SAT, count, fill, reverse lists
 int update_neighbors_poly(dem_ctx* c) {
+  if (c->nsys != 1) return c->fail(DEM_ERR_UNSUPPORTED, "batched systems are implemented for spheres only");
   for (int d = 0; d < 3; d++)
     if (c->prm.periodic[d]) return c->fail(DEM_ERR_UNSUPPORTED, "periodic boundaries are not supported for polyhedra");
   if (c->n == 0) {
@@ -361,6 +426,46 @@ int copy_field(dem_ctx* c, double* dst, const double* src, uint64_t n, cudaMemcp
 
 extern "C" {
 
+int dem_set_systems(dem_ctx* c, const dem_system* systems, int nsystems) {
+  if (!c || !systems || nsystems < 1 || nsystems > DEM_MAX_SYSTEMS) return DEM_ERR_INVALID_ARG;
+  if (c->poly) return c->fail(DEM_ERR_UNSUPPORTED, "batched systems are implemented for spheres only");
+  uint64_t next = 0;
+  for (int k = 0; k < nsystems; k++) {
+    const dem_system& q = systems[k];
+    if (q.first != next || q.count == 0)
+      return c->fail(DEM_ERR_INVALID_ARG, "systems must be non-empty consecutive particle ranges from 0");
+    next += q.count;
+    if (q.driver_first < 0 || q.driver_count < 0 || q.driver_first + q.driver_count > c->ndrv)
+      return c->fail(DEM_ERR_INVALID_ARG, "system driver range outside the registered drivers");
+    for (int d = 0; d < 3; d++)
+      if (!(q.bounds_hi[d] > q.bounds_lo[d])) return c->fail(DEM_ERR_INVALID_ARG, "system with an empty domain");
+  }
+  if (next != c->n) return c->fail(DEM_ERR_INVALID_ARG, "systems must cover all particles");
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const std::vector<dem_system> keep = c->systems;
+  c->systems.assign(systems, systems + nsystems);
+  int rc = setup_grid(c);
+  if (rc) {
+    c->systems = keep;
+    return rc;
+  }
+  c->have_list = false;
+  c->hist_valid = false;
+  return DEM_OK;
+}
+
+int dem_system_count(dem_ctx* c, int* out) {
+  if (!c || !out) return DEM_ERR_INVALID_ARG;
+  *out = c->nsys;
+  return DEM_OK;
+}
+
+int dem_simulation_state_systems(dem_ctx* c, dem_state* out, int nsystems) {
+  if (!c || !out || nsystems != c->nsys) return DEM_ERR_INVALID_ARG;
+  return launch_state_systems(c, out);
+}
+
+
 int dem_ctx_create(const dem_params* params, dem_ctx** out) {
   if (!out) return DEM_ERR_INVALID_ARG;
   *out = nullptr;
@@ -428,6 +533,10 @@ int dem_ctx_destroy(dem_ctx* c) {
   cudaFree(c->d_scalars);
   cudaFree(c->d_red);
   cudaFree(c->drv_dev);
+  cudaFree(c->grids_dev);
+  cudaFree(c->coff_dev);
+  cudaFree(c->pfirst_dev);
+  cudaFree(c->drange_dev);
   if (c->h_scalars) cudaFreeHost(c->h_scalars);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -515,6 +624,7 @@ int dem_set_particles(dem_ctx* c, const dem_particles* p, int on_device) {
   for (double r : rad) rmax = std::max(rmax, r);
   c->rad_max = rmax;
   c->n = n;
+  c->systems.clear();
   c->ni = 0;
   c->have_list = false;
   c->hist_valid = false;
@@ -552,6 +662,7 @@ static int add_driver(dem_ctx* c, const DriverDev& d) {
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   c->ndrv++;
   c->have_list = false;
+  if (c->systems.empty() && c->n) return setup_grid(c);  // single system: all drivers
   return DEM_OK;
 }
 
@@ -655,6 +766,7 @@ int dem_vertex_displ_over(dem_ctx* c, int* result) {
 
 int dem_set_shapes(dem_ctx* c, const dem_shape* shapes, int nshapes) {
   if (!c || !shapes || nshapes <= 0) return DEM_ERR_INVALID_ARG;
+  if (!c->systems.empty()) return c->fail(DEM_ERR_UNSUPPORTED, "batched systems are implemented for spheres only");
   std::vector<ShapeDev> h(nshapes);
   int mv = 0;
   for (int k = 0; k < nshapes; k++) {
@@ -845,12 +957,30 @@ int dem_get_interactions(dem_ctx* c, dem_interaction_list* l) {
   std::iota(order.begin(), order.end(), 0);
   std::sort(order.begin(), order.end(),
             [&](size_t a, size_t b) { return id[owner[seg_start[a]]] < id[owner[seg_start[b]]]; });
+  // driver partners are stored by global driver index; report the index inside
+  // the owner's system (each system numbers its drivers from 0, as a run of its own)
+  auto driver_base = [&](uint32_t slot) -> uint64_t {
+    if (c->systems.empty()) return 0;
+    size_t lo = 0, hi = c->systems.size() - 1;
+    while (lo < hi) {
+      const size_t mid = (lo + hi + 1) / 2;
+      if (c->systems[mid].first <= slot)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    return (uint64_t)c->systems[lo].driver_first;
+  };
   uint64_t w = 0;
   for (size_t o : order) {
     const uint64_t b = seg_start[o], e = (o + 1 < seg_start.size()) ? seg_start[o + 1] : ni;
     for (uint64_t k = b; k < e; k++, w++) {
       if (l->owner_id) l->owner_id[w] = id[owner[k]];
-      if (l->partner_id) l->partner_id[w] = pid[k];
+      if (l->partner_id) {
+        const uint32_t t = meta_type(meta[k]);
+        const bool drv = t == DEM_ITYPE_VERTEX_CYLINDER || t == DEM_ITYPE_VERTEX_SURFACE;
+        l->partner_id[w] = drv ? pid[k] - driver_base(owner[k]) : pid[k];
+      }
       if (l->type) l->type[w] = (uint16_t)meta_type(meta[k]);
       if (l->swap) l->swap[w] = (uint8_t)((meta[k] >> 15) & 1u);
       if (l->owner_sub) l->owner_sub[w] = sub[k] & 0xffffu;

@@ -38,7 +38,17 @@ struct dem_ctx {
   dem::DriverDev drv_host[DEM_MAX_DRIVERS]{};
   dem::DriverDev* drv_dev = nullptr;
 
-  // cell grid
+  // systems (batched context); one system spanning prm's domain otherwise
+  std::vector<dem_system> systems;   // empty: single system from prm
+  int nsys = 1;
+  dem::GridDev* grids_dev = nullptr;  // nsys each
+  uint32_t* coff_dev = nullptr;       // nsys + 1
+  uint64_t* pfirst_dev = nullptr;     // nsys + 1
+  int2* drange_dev = nullptr;         // nsys
+  int sys_cap = 0;
+  dem::SysView sysview() const { return dem::SysView{grids_dev, coff_dev, pfirst_dev, drange_dev, nsys}; }
+
+  // cell grid (grid = system 0's, used by the single-system polyhedron path)
   dem::GridDev grid{};
   uint64_t ncell = 0, ccap = 0;
   uint32_t* cell_cnt = nullptr;    // ncell+1 (counts, then cursor)
@@ -176,6 +186,7 @@ int launch_poly_units(dem_ctx* c, uint64_t* nu_out, int (*grow_units)(dem_ctx*, 
 int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total);
 int launch_poly_feature_fill(dem_ctx* c, uint64_t nu);
 int launch_contact_poly(dem_ctx* c);
+int launch_state_systems(dem_ctx* c, dem_state* out);  // one state per system
 int launch_poly_fused_prolog(dem_ctx* c);     // prolog + FP32-decided vertex_displ_over flag
 int launch_vertex_list(dem_ctx* c);           // particles whose vertices the list uses (host sync)
 int launch_poly_vertices_listed(dem_ctx* c);  // FP64 vertices of those particles

@@ -79,8 +79,6 @@ struct DriverDev {
   double offset, radius;
   double normal[3], center[3], center_proj[3], axis[3], vel[3], vrot[3];
 };
-#define DEM_MAX_DRIVERS 16
-
 struct GridDev {
   int dims[3];
   double lo[3];
@@ -88,6 +86,29 @@ struct GridDev {
   double csz[3];
   int periodic[3];
   double L[3];
+};
+
+// Systems of a batched context (one system when not batched).  System k owns
+// particles [pfirst[k], pfirst[k+1]) (the cell sort keeps particles inside
+// their system's range), cells [coff[k], coff[k+1]) of the global cell index
+// space, and drivers [drange[k].x, drange[k].x + drange[k].y).
+struct SysView {
+  const GridDev* g;
+  const uint32_t* coff;
+  const uint64_t* pfirst;  // nsys + 1 entries
+  const int2* drange;
+  int nsys;
+  __device__ __forceinline__ int of(uint64_t s) const {
+    int lo = 0, hi = nsys - 1;
+    while (lo < hi) {  // last k with pfirst[k] <= s
+      const int mid = (lo + hi + 1) >> 1;
+      if (pfirst[mid] <= s)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    return lo;
+  }
 };
 
 // ------------------------------------------------------------- vector math

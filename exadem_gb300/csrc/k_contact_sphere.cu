@@ -26,7 +26,7 @@ struct ContactArgs {
   IArrays I;
   Records R;
   uint64_t ni;
-  GridDev g;
+  SysView sv;  // periodic lengths of the owner's system
   const DriverDev* drv;
   dem_contact_params cp;   // particle-particle
   dem_contact_params cpd;  // particle-driver
@@ -53,9 +53,12 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
     if (type == DEM_ITYPE_VERTEX_VERTEX) {
       V3 rj = ldv(a.P, RX, j);
       const int sx = meta_shift(meta, 0), sy = meta_shift(meta, 1), sz = meta_shift(meta, 2);
-      if (sx) rj.x = rj.x + (double)sx * a.g.L[0];
-      if (sy) rj.y = rj.y + (double)sy * a.g.L[1];
-      if (sz) rj.z = rj.z + (double)sz * a.g.L[2];
+      if (sx | sy | sz) {
+        const GridDev& g = a.sv.g[a.sv.of(i)];
+        if (sx) rj.x = rj.x + (double)sx * g.L[0];
+        if (sy) rj.y = rj.y + (double)sy * g.L[1];
+        if (sz) rj.z = rj.z + (double)sz * g.L[2];
+      }
       const double rad_j = a.P.f[RAD][j];
       bool skip = false;
       if (a.screen) {
@@ -183,7 +186,7 @@ int launch_contact_sphere(dem_ctx* c) {
   a.I = c->I[c->icur];
   a.R = c->R;
   a.ni = c->ni;
-  a.g = c->grid;
+  a.sv = c->sysview();
   a.drv = c->drv_dev;
   a.cp = c->prm.config;
   a.cpd = c->prm.config_driver;

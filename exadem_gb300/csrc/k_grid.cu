@@ -9,15 +9,19 @@
 //                deterministic whatever order the atomics ran in
 //   k_reorder:   gather every field into the other particle buffer
 // All of it is integer / copy work: HBM-bound, one read and one write per field.
+// Batched contexts: each system bins into its own block of the cell index
+// space, so the sort keeps every particle inside its system's slot range.
 #include "dem_ctx.cuh"
 
 namespace dem {
 namespace {
 
-__global__ void k_bin(PArrays P, uint64_t n, GridDev g, uint32_t* __restrict__ cell_tmp,
+__global__ void k_bin(PArrays P, uint64_t n, SysView sv, uint32_t* __restrict__ cell_tmp,
                       uint32_t* __restrict__ cell_cnt) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
+  const int sys = sv.of(s);
+  const GridDev& g = sv.g[sys];
   int k[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
@@ -39,7 +43,8 @@ __global__ void k_bin(PArrays P, uint64_t n, GridDev g, uint32_t* __restrict__ c
     if (kk >= g.dims[d]) kk = g.dims[d] - 1;
     k[d] = (int)kk;
   }
-  const uint32_t c = (uint32_t)k[0] + (uint32_t)g.dims[0] * ((uint32_t)k[1] + (uint32_t)g.dims[1] * (uint32_t)k[2]);
+  const uint32_t c =
+      sv.coff[sys] + (uint32_t)k[0] + (uint32_t)g.dims[0] * ((uint32_t)k[1] + (uint32_t)g.dims[1] * (uint32_t)k[2]);
   cell_tmp[s] = c;
   atomicAdd(&cell_cnt[c], 1u);
 }
@@ -71,7 +76,7 @@ __global__ void k_cell_sort(uint64_t ncell, const uint32_t* __restrict__ cell_st
 }
 
 __global__ void k_reorder(PArrays src, PArrays dst, uint64_t n, const uint32_t* __restrict__ perm,
-                          const uint32_t* __restrict__ cell_tmp, uint32_t* __restrict__ cell_of, GridDev g,
+                          const uint32_t* __restrict__ cell_tmp, uint32_t* __restrict__ cell_of, SysView sv,
                           float* __restrict__ xr, float* __restrict__ yr, float* __restrict__ zr,
                           float* __restrict__ rf) {
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -80,7 +85,9 @@ __global__ void k_reorder(PArrays src, PArrays dst, uint64_t n, const uint32_t* 
 #pragma unroll
   for (int k = 0; k < BX; k++) dst.f[k][t] = src.f[k][o];
   // FP32 coordinates relative to the origin of the particle's cell, for the FP32 broad phase
-  const uint32_t c = cell_tmp[o];
+  const int sys = sv.of(t);  // the slot stays in the particle's system range
+  const GridDev& g = sv.g[sys];
+  const uint32_t c = cell_tmp[o] - sv.coff[sys];
   const uint32_t kx = c % (uint32_t)g.dims[0], ky = (c / (uint32_t)g.dims[0]) % (uint32_t)g.dims[1],
                  kz = c / ((uint32_t)g.dims[0] * (uint32_t)g.dims[1]);
   xr[t] = (float)(src.f[RX][o] - (g.lo[0] + (double)kx * g.csz[0]));
@@ -112,7 +119,7 @@ int launch_bin_particles(dem_ctx* c) {
   {
   ProfScope ps(c, K_BIN, n ? 2 : 1);
   k_zero_u32<<<grid_for(nc + 1, 256), 256, 0, st>>>(c->cell_cnt, nc + 1);
-  if (n) k_bin<<<grid_for(n, 256), 256, 0, st>>>(c->P[c->pcur], n, c->grid, c->cell_tmp, c->cell_cnt);
+  if (n) k_bin<<<grid_for(n, 256), 256, 0, st>>>(c->P[c->pcur], n, c->sysview(), c->cell_tmp, c->cell_cnt);
   }
   rc = scan_exclusive_u32(c, c->cell_cnt, c->cell_start, nc);
   if (rc) return rc;
@@ -130,7 +137,7 @@ int launch_reorder_particles(dem_ctx* c) {
   ProfScope ps(c, K_REORDER, n ? 1 : 0);
   if (n) {
     k_reorder<<<grid_for(n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->P[1 - c->pcur], n, c->perm, c->cell_tmp,
-                                                        c->cell_of, c->grid, c->crel[0], c->crel[1], c->crel[2],
+                                                        c->cell_of, c->sysview(), c->crel[0], c->crel[1], c->crel[2],
                                                         c->crel[3]);
   }
   DEM_CUDA_TRY(c, cudaGetLastError());

@@ -13,7 +13,9 @@
 //     moment) carried over from the previous list by key equality
 //     (interaction_manager.hpp:89-112, placeholder_interaction.hpp:398-408).
 // One thread per owner particle; particles are in cell order so the stencil
-// reads of neighbouring threads hit the same cells (L1/L2 reuse).
+// reads of neighbouring threads hit the same cells (L1/L2 reuse).  In a
+// batched context the particle's system gives the grid, its cell block and
+// its drivers.
 #include "dem_ctx.cuh"
 
 namespace dem {
@@ -22,7 +24,7 @@ namespace {
 struct BPArgs {
   PArrays P;
   uint64_t n;
-  GridDev g;
+  SysView sv;
   const uint32_t* cell_start;
   const uint32_t* cell_of;
   const DriverDev* drv;
@@ -34,7 +36,6 @@ struct BPArgs {
   const float* yr;
   const float* zr;
   const float* rf;
-  float csz[3];
   float skin_f;
 };
 
@@ -81,63 +82,68 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
   const V3 ri = mk(rx[s], ry[s], rz[s]);
   const double radi = rad[s];
   const uint64_t idi = id[s];
-  for (int k = 0; k < a.ndrv; k++) {
+  const int sys = a.sv.of(s);
+  const GridDev& g = a.sv.g[sys];
+  const uint32_t coff = a.sv.coff[sys];
+  const int2 dr = a.sv.drange[sys];
+  for (int k = dr.x; k < dr.x + dr.y; k++) {
     const DriverDev& d = a.drv[k];
     if (driver_filter(d, radi + a.skin, ri))
       emit((uint32_t)k, (uint64_t)k,
            make_meta(d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER, 0, 0, 0, false));
   }
   float xri = 0.f, yri = 0.f, zri = 0.f, rfi = 0.f, si = 0.f, cmax = 0.f;
+  const float csx = (float)g.csz[0], csy = (float)g.csz[1], csz = (float)g.csz[2];
   if (F32) {
     xri = a.xr[s];
     yri = a.yr[s];
     zri = a.zr[s];
     rfi = a.rf[s];
     si = fmaxf(fabsf(xri), fmaxf(fabsf(yri), fabsf(zri)));
-    cmax = fmaxf(a.csz[0], fmaxf(a.csz[1], a.csz[2]));
+    cmax = fmaxf(csx, fmaxf(csy, csz));
   }
-  const uint32_t c = a.cell_of[s];
-  const int d0 = a.g.dims[0], d1 = a.g.dims[1], d2n = a.g.dims[2];
+  const uint32_t c = a.cell_of[s] - coff;
+  const int d0 = g.dims[0], d1 = g.dims[1], d2n = g.dims[2];
   const int cx = (int)(c % (uint32_t)d0);
   const int cy = (int)((c / (uint32_t)d0) % (uint32_t)d1);
   const int cz = (int)(c / ((uint32_t)d0 * (uint32_t)d1));
   for (int dz = -1; dz <= 1; dz++) {
     int z = cz + dz, sz = 0;
     if (z < 0) {
-      if (!a.g.periodic[2]) continue;
+      if (!g.periodic[2]) continue;
       z += d2n;
       sz = -1;
     } else if (z >= d2n) {
-      if (!a.g.periodic[2]) continue;
+      if (!g.periodic[2]) continue;
       z -= d2n;
       sz = 1;
     }
     for (int dy = -1; dy <= 1; dy++) {
       int y = cy + dy, sy = 0;
       if (y < 0) {
-        if (!a.g.periodic[1]) continue;
+        if (!g.periodic[1]) continue;
         y += d1;
         sy = -1;
       } else if (y >= d1) {
-        if (!a.g.periodic[1]) continue;
+        if (!g.periodic[1]) continue;
         y -= d1;
         sy = 1;
       }
       for (int dx = -1; dx <= 1; dx++) {
         int x = cx + dx, sx = 0;
         if (x < 0) {
-          if (!a.g.periodic[0]) continue;
+          if (!g.periodic[0]) continue;
           x += d0;
           sx = -1;
         } else if (x >= d0) {
-          if (!a.g.periodic[0]) continue;
+          if (!g.periodic[0]) continue;
           x -= d0;
           sx = 1;
         }
-        const uint32_t cc = (uint32_t)x + (uint32_t)d0 * ((uint32_t)y + (uint32_t)d1 * (uint32_t)z);
+        const uint32_t cc = coff + (uint32_t)x + (uint32_t)d0 * ((uint32_t)y + (uint32_t)d1 * (uint32_t)z);
         const uint32_t qb = a.cell_start[cc], qe = a.cell_start[cc + 1];
         const bool ghost = (sx | sy | sz) != 0;
-        const float oxf = (float)dx * a.csz[0], oyf = (float)dy * a.csz[1], ozf = (float)dz * a.csz[2];
+        const float oxf = (float)dx * csx, oyf = (float)dy * csy, ozf = (float)dz * csz;
         for (uint32_t q = qb; q < qe; q++) {
           const uint64_t idj = id[q];
           if (!ghost && idi >= idj) continue;  // owner rule first (integer test)
@@ -150,9 +156,9 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
           }
           if (keep < 0) {
             V3 rj = mk(rx[q], ry[q], rz[q]);
-            if (sx) rj.x = rj.x + (double)sx * a.g.L[0];
-            if (sy) rj.y = rj.y + (double)sy * a.g.L[1];
-            if (sz) rj.z = rj.z + (double)sz * a.g.L[2];
+            if (sx) rj.x = rj.x + (double)sx * g.L[0];
+            if (sy) rj.y = rj.y + (double)sy * g.L[1];
+            if (sz) rj.z = rj.z + (double)sz * g.L[2];
             const double ddx = rj.x - ri.x, ddy = rj.y - ri.y, ddz = rj.z - ri.z;
             const double d2 = ddx * ddx + ddy * ddy + ddz * ddz;
             const double rmax = radi + rad[q] + a.skin;
@@ -295,7 +301,7 @@ BPArgs make_args(dem_ctx* c) {
   BPArgs a;
   a.P = c->P[c->pcur];
   a.n = c->n;
-  a.g = c->grid;
+  a.sv = c->sysview();
   a.cell_start = c->cell_start;
   a.cell_of = c->cell_of;
   a.drv = c->drv_dev;
@@ -307,7 +313,6 @@ BPArgs make_args(dem_ctx* c) {
   a.yr = c->crel[1];
   a.zr = c->crel[2];
   a.rf = c->crel[3];
-  for (int d = 0; d < 3; d++) a.csz[d] = (float)c->grid.csz[d];
   a.skin_f = (float)c->prm.rcut_inc;
   return a;
 }

@@ -103,6 +103,57 @@ __global__ void k_state_final(const double* __restrict__ part, int nb, double* _
   }
 }
 
+// One block per system: the sums of k_state_partial over the system's
+// particles, and its interactions (owned by its particles; sorted by owner, so
+// the range own_off[first] .. own_off[last + 1]), counting those with a
+// non-zero friction or moment history (Interaction::active, interaction.hpp:129-136).
+__global__ void k_state_sys(PArrays P, SysView sv, IArrays I, const uint32_t* __restrict__ own_off, int have_list,
+                            double* __restrict__ out, unsigned long long* __restrict__ cnt) {
+  __shared__ double sh[7][RED_THREADS];
+  __shared__ unsigned long long sa[RED_THREADS];
+  const int k = blockIdx.x;
+  const uint64_t b = sv.pfirst[k], e = sv.pfirst[k + 1];
+  double acc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (uint64_t s = b + threadIdx.x; s < e; s += RED_THREADS) {
+    const double m = P.f[MASS][s];
+    acc[0] += m;
+    acc[1] += 0.5 * P.f[WX][s] * P.f[WX][s] * m;
+    acc[2] += 0.5 * P.f[WY][s] * P.f[WY][s] * m;
+    acc[3] += 0.5 * P.f[WZ][s] * P.f[WZ][s] * m;
+    acc[4] += 0.5 * P.f[VX][s] * P.f[VX][s] * m;
+    acc[5] += 0.5 * P.f[VY][s] * P.f[VY][s] * m;
+    acc[6] += 0.5 * P.f[VZ][s] * P.f[VZ][s] * m;
+  }
+  unsigned long long act = 0;
+  uint64_t ib = 0, ie = 0;
+  if (have_list) {
+    ib = own_off[b];
+    ie = own_off[e];
+    for (uint64_t q = ib + threadIdx.x; q < ie; q += RED_THREADS)
+      act += (I.ft[0][q] != 0.0 || I.ft[1][q] != 0.0 || I.ft[2][q] != 0.0 || I.mo[0][q] != 0.0 ||
+              I.mo[1][q] != 0.0 || I.mo[2][q] != 0.0)
+                 ? 1
+                 : 0;
+  }
+#pragma unroll
+  for (int q = 0; q < 7; q++) sh[q][threadIdx.x] = acc[q];
+  sa[threadIdx.x] = act;
+  __syncthreads();
+  for (int w = RED_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+#pragma unroll
+      for (int q = 0; q < 7; q++) sh[q][threadIdx.x] += sh[q][threadIdx.x + w];
+      sa[threadIdx.x] += sa[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 7) out[k * 7 + threadIdx.x] = sh[threadIdx.x][0];
+  if (threadIdx.x == 0) {
+    cnt[2 * k] = ie - ib;
+    cnt[2 * k + 1] = sa[0];
+  }
+}
+
 __global__ void k_profile(PArrays P, uint64_t n, int nslabs, double zlo, double dz, double* __restrict__ vol) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
@@ -202,6 +253,40 @@ int launch_state(dem_ctx* c, dem_state* out) {
   out->n_active_interactions = c->h_scalars[1];
   return DEM_OK;
 }
+int launch_state_systems(dem_ctx* c, dem_state* out) {
+  const int ns = c->nsys;
+  double* d_out = nullptr;
+  unsigned long long* d_cnt = nullptr;
+  DEM_CUDA_TRY(c, cudaMallocAsync(&d_out, (size_t)ns * 7 * sizeof(double), c->stream));
+  DEM_CUDA_TRY(c, cudaMallocAsync(&d_cnt, (size_t)ns * 2 * sizeof(unsigned long long), c->stream));
+  {
+    ProfScope ps(c, K_STATE, 1);
+    k_state_sys<<<ns, RED_THREADS, 0, c->stream>>>(c->P[c->pcur], c->sysview(), c->I[c->icur], c->own_off[c->icur],
+                                                   (c->have_list && c->ni) ? 1 : 0, d_out, d_cnt);
+  }
+  std::vector<double> h((size_t)ns * 7);
+  std::vector<unsigned long long> hc((size_t)ns * 2);
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(h.data(), d_out, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(hc.data(), d_cnt, hc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                  c->stream));
+  DEM_CUDA_TRY(c, cudaFreeAsync(d_out, c->stream));
+  DEM_CUDA_TRY(c, cudaFreeAsync(d_cnt, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  const std::vector<dem_system>& sys = c->systems;
+  for (int k = 0; k < ns; k++) {
+    dem_state& o = out[k];
+    o.mass = h[k * 7];
+    for (int d = 0; d < 3; d++) {
+      o.rotation_energy[d] = h[k * 7 + 1 + d];
+      o.kinetic_energy[d] = h[k * 7 + 4 + d];
+    }
+    o.n_particles = sys.empty() ? c->n : sys[k].count;
+    o.n_interactions = hc[2 * k];
+    o.n_active_interactions = hc[2 * k + 1];
+  }
+  return DEM_OK;
+}
+
 int launch_profile(dem_ctx* c, int nslabs, double zlo, double zhi, double* out) {
   if ((uint64_t)nslabs > c->red_cap) return c->fail(DEM_ERR_INVALID_ARG, "nslabs too large");
   const double dz = (zhi - zlo) / nslabs;

@@ -44,7 +44,7 @@ struct CArgs {
   IArrays I;
   Records R;
   uint64_t ni;
-  GridDev g;
+  SysView sv;  // periodic lengths of the owner's system
   const DriverDev* drv;
   dem_contact_params cp, cpd;
   double dt;
@@ -75,12 +75,16 @@ __device__ __forceinline__ void write_result(const CArgs& a, uint64_t k, V3 ft, 
   a.R.tj[2][k] = tj.z;
 }
 
-__device__ __forceinline__ V3 partner_pos(const CArgs& a, uint32_t meta, uint32_t j) {
+// partner position, moved by the periodic lengths of the owner i's system for an image
+__device__ __forceinline__ V3 partner_pos(const CArgs& a, uint32_t meta, uint32_t i, uint32_t j) {
   V3 rj = ldv(a.P, RX, j);
   const int sx = meta_shift(meta, 0), sy = meta_shift(meta, 1), sz = meta_shift(meta, 2);
-  if (sx) rj.x = rj.x + (double)sx * a.g.L[0];
-  if (sy) rj.y = rj.y + (double)sy * a.g.L[1];
-  if (sz) rj.z = rj.z + (double)sz * a.g.L[2];
+  if (sx | sy | sz) {
+    const GridDev& g = a.sv.g[a.sv.of(i)];
+    if (sx) rj.x = rj.x + (double)sx * g.L[0];
+    if (sy) rj.y = rj.y + (double)sy * g.L[1];
+    if (sz) rj.z = rj.z + (double)sz * g.L[2];
+  }
   return rj;
 }
 
@@ -93,7 +97,7 @@ __global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
     if (a.screen && meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
       const uint32_t i = a.I.owner[k], j = a.I.partner[k];
       const V3 ri = ldv(a.P, RX, i);
-      const V3 rj = partner_pos(a, meta, j);
+      const V3 rj = partner_pos(a, meta, i, j);
       const double rad_i = a.P.f[RAD][i], rad_j = a.P.f[RAD][j];
       // same proof of separation as the one-pass kernel (k_contact_sphere.cu)
       const float ex = (float)(ri.x - rj.x), ey = (float)(ri.y - rj.y), ez = (float)(ri.z - rj.z);
@@ -131,7 +135,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
       V3 rj = mk(0, 0, 0);
       double dncut;
       if (is_vv) {
-        rj = partner_pos(a, meta, j);
+        rj = partner_pos(a, meta, i, j);
         const double rad_j = a.P.f[RAD][j];
         const double R = rad_i + rad_j;
         const V3 dist = ri - rj;
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(FT) k_chooke(CArgs a) {
     const V3 vi = ldv(a.P, VX, i);
     const V3 wi = ldv(a.P, WX, i);
     if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
-      const V3 rj = partner_pos(a, meta, j);
+      const V3 rj = partner_pos(a, meta, i, j);
       const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
       const double m_i = a.P.f[MASS][i], m_j = a.P.f[MASS][j];
       const double meff = (m_i * m_j) / (m_i + m_j);
@@ -286,7 +290,7 @@ CArgs make_cargs(dem_ctx* c) {
   a.I = c->I[c->icur];
   a.R = c->R;
   a.ni = c->ni;
-  a.g = c->grid;
+  a.sv = c->sysview();
   a.drv = c->drv_dev;
   a.cp = c->prm.config;
   a.cpd = c->prm.config_driver;

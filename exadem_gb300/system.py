@@ -243,6 +243,34 @@ class System:
                 "mass": s.mass, "n_particles": s.n_particles, "n_interactions": s.n_interactions,
                 "n_active_interactions": s.n_active_interactions}
 
+    # ------------------------------------------------------------ batching
+    def set_systems(self, systems: list) -> None:
+        """Independent systems in one context (dem_set_systems).  Each entry:
+        dict(first, count, bounds_lo, bounds_hi, periodic, driver_first, driver_count)."""
+        arr = (A.SystemDesc * len(systems))()
+        for k, d in enumerate(systems):
+            q = arr[k]
+            q.first, q.count = int(d["first"]), int(d["count"])
+            q.bounds_lo[:] = list(map(float, d["bounds_lo"]))
+            q.bounds_hi[:] = list(map(float, d["bounds_hi"]))
+            q.periodic[:] = [int(bool(x)) for x in d.get("periodic", (0, 0, 0))]
+            q.driver_first = int(d.get("driver_first", 0))
+            q.driver_count = int(d.get("driver_count", 0))
+        self._check(self.b.set_systems(self.h, arr, len(systems)), "set_systems")
+
+    def system_count(self) -> int:
+        v = C.c_int()
+        self._check(self.b.system_count(self.h, C.byref(v)), "system_count")
+        return int(v.value)
+
+    def system_states(self) -> list:
+        ns = self.system_count()
+        arr = (A.State * ns)()
+        self._check(self.b.simulation_state_systems(self.h, arr, ns), "simulation_state_systems")
+        return [{"kinetic_energy": np.array(s.kinetic_energy[:]), "rotation_energy": np.array(s.rotation_energy[:]),
+                 "mass": s.mass, "n_particles": s.n_particles, "n_interactions": s.n_interactions,
+                 "n_active_interactions": s.n_active_interactions} for s in arr]
+
     def interaction_count(self) -> int:
         v = C.c_uint64()
         self._check(self.b.interaction_count(self.h, C.byref(v)), "interaction_count")

@@ -123,7 +123,7 @@ def spheres_floor(n=2_000_000, side=400.0, rmin=0.4, rmax=0.6, phi=0.55, density
 
 
 def spheres_drum(n=20_000, rmin=0.45, rmax=0.55, fill=0.30, density=2.0, length=None, omega=2.0, seed=5,
-                 steps=2000, dt=5e-4, skin=0.05, **flags) -> Workload:
+                 steps=2000, dt=5e-4, skin=0.05, id_offset=0, **flags) -> Workload:
     """One drum of config 5: n spheres, radii uniform in [0.45, 0.55], in a
     cylinder (axis y) whose radius is set so the solid volume is `fill` of the
     drum volume; the drum turns at `omega` rad/s (Cylinder vrot); Hooke
@@ -140,12 +140,73 @@ def spheres_drum(n=20_000, rmin=0.45, rmax=0.55, fill=0.30, density=2.0, length=
     c = R + 1.0
     lo, hi = (0.0, 0.0, 0.0), (2 * c, length, 2 * c)
     arr, _ = rsa(n, rmin, rmax, density, lo, hi, periodic=(0, 1, 0), seed=seed, region=1, cyl_center=(c, c),
-                 cyl_radius=R, max_attempts=100000)
+                 cyl_radius=R, max_attempts=100000, id_offset=id_offset)
     cfg = dict(kn=1e4, kt=8e3, kr=0.0, mu=0.4, damp_rate=0.9)
     p = make_params(lo, hi, (0, 1, 0), rcut_inc=skin, dt=dt, gravity=(0, 0, -9.81), config=cfg, config_driver=cfg,
                     **flags)
     cyl = dict(radius=R, axis=(1.0, 0.0, 1.0), center=(c, 0.0, c), vrot=(0.0, omega, 0.0))
     return Workload("spheres_drum", p, arr, cylinders=[cyl], steps=steps, info={"drum_radius": R, "length": length})
+
+
+@dataclass
+class BatchWorkload:
+    """Independent systems run in one context (dem_set_systems): the particle
+    arrays are concatenated system after system, each system keeps its own
+    domain and drivers; `members` are the systems as standalone workloads."""
+    name: str
+    params: A.Params
+    members: list
+    steps: int = 1000
+    info: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return sum(m.n for m in self.members)
+
+    def particles(self) -> dict:
+        keys = self.members[0].particles.keys()
+        return {k: np.concatenate([m.particles[k] for m in self.members]) for k in keys}
+
+    def systems(self) -> list:
+        out, first, dfirst = [], 0, 0
+        for m in self.members:
+            nd = len(m.surfaces) + len(m.cylinders)
+            p = m.params
+            out.append(dict(first=first, count=m.n, bounds_lo=list(p.bounds_lo), bounds_hi=list(p.bounds_hi),
+                            periodic=list(p.periodic), driver_first=dfirst, driver_count=nd))
+            first += m.n
+            dfirst += nd
+        return out
+
+    def build(self, system_factory=None) -> System:
+        s = system_factory(self.params) if system_factory else System(self.params)
+        s.set_particles(self.particles())
+        for m in self.members:
+            for kw in m.surfaces:
+                s.register_surface(**kw)
+            for kw in m.cylinders:
+                s.register_cylinder(**kw)
+        s.set_systems(self.systems())
+        return s
+
+
+def drums_batch(nsys=256, nmin=2_000, nmax=200_000, seed=5, steps=2000, **kw) -> BatchWorkload:
+    """Config 5: nsys rotating drums (spheres_drum) with sphere counts
+    log-uniform in [nmin, nmax] (seeded), each drum its own system with its
+    own domain (periodic along its axis) and its own rotating cylinder.
+    Drum k uses seed seed * 1000 + k and ids offset by the spheres before it."""
+    import concurrent.futures as cf
+    import os
+
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(math.log(nmin), math.log(nmax), nsys)).astype(np.int64)
+    offsets = np.concatenate([[0], np.cumsum(counts)[:-1]])
+    # the drums are independent: generate them in parallel (the C generator releases the GIL)
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(nsys, os.cpu_count() or 1))) as ex:
+        members = list(ex.map(lambda k: spheres_drum(n=int(counts[k]), seed=seed * 1000 + k, steps=steps,
+                                                     id_offset=int(offsets[k]), **kw), range(nsys)))
+    return BatchWorkload("drums_batch", members[0].params, members, steps=steps,
+                         info={"systems": nsys, "counts": counts.tolist()})
 
 
 # ------------------------------------------------------------------ polyhedra

@@ -143,7 +143,8 @@ typedef struct dem_state {
  * One row per interaction, sorted by InteractionPair::operator<
  * (owner id, partner id, type, swap, owner sub, partner sub)
  * (src/interaction/include/exaDEM/interaction/interaction_pair.hpp:222-249).
- * For driver interactions partner_id is the driver index.  Arrays must hold
+ * For driver interactions partner_id is the driver index (in a batched
+ * context, the index within the owner's system).  Arrays must hold
  * `capacity` rows; NULL arrays are skipped.                               */
 typedef struct dem_interaction_list {
   uint64_t capacity;
@@ -198,6 +199,35 @@ int dem_get_particles(dem_ctx* ctx, dem_particles* out, int on_device);
  * motion only; vrot enters the relative velocity (rotating drum).         */
 int dem_register_surface(dem_ctx* ctx, const dem_surface* s);
 int dem_register_cylinder(dem_ctx* ctx, const dem_cylinder* c);
+
+/* ---- batching: many independent systems in one context -------------------
+ * No reference counterpart (one exaDEM run is one system).  Each system is a
+ * contiguous range of the particles given to dem_set_particles, with its own
+ * domain (bounds, periodicity; cell grid of the shared cell size) and its own
+ * drivers (a range of the registration order).  Particles of different
+ * systems never interact, every system evolves exactly as it would alone, and
+ * every kernel of a step covers all systems in one launch.  Spheres only.
+ * Ids must be unique over all systems.  A rebuild is triggered when any
+ * system's trigger fires and rebuilds all systems (a rebuild does not change
+ * the trajectory: only pairs within the skin are added or dropped, and the
+ * history is carried by key).  Call after dem_set_particles (which resets the
+ * context to a single system spanning the params' domain) and after the
+ * drivers are registered.                                                  */
+typedef struct dem_system {
+  uint64_t first;         /* first particle of the system                    */
+  uint64_t count;         /* number of particles                             */
+  double bounds_lo[3], bounds_hi[3];
+  int32_t periodic[3];
+  int32_t driver_first;   /* drivers [driver_first, driver_first + driver_count) */
+  int32_t driver_count;
+} dem_system;
+#define DEM_MAX_SYSTEMS 65536
+#define DEM_MAX_DRIVERS 1024
+int dem_set_systems(dem_ctx* ctx, const dem_system* systems, int nsystems);
+int dem_system_count(dem_ctx* ctx, int* out);
+/* simulation_state of each system: out[k] for system k (nsystems entries).
+ * n_interactions / n_active_interactions are those owned by the system.  */
+int dem_simulation_state_systems(dem_ctx* ctx, dem_state* out, int nsystems);
 
 /* Switches the context to polyhedron mode (nbh_polyhedron, contact_polyhedron,
  * vertex_displ_over, config_polyhedra.msp:6-34).  Shapes are copied.       */
