@@ -50,6 +50,7 @@ def parse():
                          "polyhedra_dense: polyhedra on a dense lattice; drums: 256 rotating drums batched")
     ap.add_argument("--systems", type=int, default=256, help="drums: number of drums")
     ap.add_argument("--plain", action="store_true", help="plain FP64 path (no FP32 screening)")
+    ap.add_argument("--no-graph", action="store_true", help="fused step launched from the host, no CUDA graph")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -154,6 +155,8 @@ def workload(args):
 
     opt = 0 if args.plain else 1
     flags = dict(fp32_contact_screen=opt, fused_step=opt, fp32_broad_phase=opt)
+    if args.workload in ("spheres", "drums"):
+        flags["graph_step"] = opt and not args.no_graph
     if args.workload == "polyhedra":
         return W.polyhedra_floor(n=args.n or 200_000, **flags)
     if args.workload == "polyhedra_dense":
@@ -386,6 +389,7 @@ def run_native(args, rank, world, local, dist):
                    "n_particles": w.n,
                    "path": "plain FP64 operator kernels" if args.plain else
                            "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division"
+                           + (", whole step replayed as one CUDA graph" if getattr(w.params, "graph_step", 0) else "")
                            + (f", {w.info['systems']} systems in one context" if is_batch(w) else ""),
                    "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
                    "parallelism": "replicas" if world > 1 else "single",

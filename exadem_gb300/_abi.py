@@ -45,7 +45,7 @@ class Params(C.Structure):
                 ("symetric", C.c_int32), ("law", C.c_int32),
                 ("config", ContactParams), ("config_driver", ContactParams),
                 ("fp32_broad_phase", C.c_int32), ("fp32_contact_screen", C.c_int32),
-                ("fused_step", C.c_int32), ("reserved", C.c_int32 * 5)]
+                ("fused_step", C.c_int32), ("graph_step", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 PARTICLE_FIELDS = ["rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz",
@@ -155,6 +155,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_rebuild_count", [_CTX, PU64])
     _sig(lib, "dem_simulation_state", [_CTX, C.POINTER(State)])
     _sig(lib, "dem_set_systems", [_CTX, C.POINTER(SystemDesc), C.c_int])
+    _sig(lib, "dem_set_graph_capacity", [_CTX, C.c_uint64])
     _sig(lib, "dem_system_count", [_CTX, C.POINTER(C.c_int)])
     _sig(lib, "dem_simulation_state_systems", [_CTX, C.POINTER(State), C.c_int])
     _sig(lib, "dem_interaction_count", [_CTX, PU64])
@@ -179,7 +180,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
             "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
-            "dem_simulation_state_systems"]
+            "dem_simulation_state_systems", "dem_set_graph_capacity"]
 
 _LIB = None
 

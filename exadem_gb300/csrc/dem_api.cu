@@ -368,6 +368,7 @@ int update_neighbors_poly(dem_ctx* c) {
 }
 
 int update_neighbors(dem_ctx* c) {
+  c->gen++;  // buffers may move: a captured step graph is stale
   if (c->poly) return update_neighbors_poly(c);
   if (c->n == 0) {
     c->ni = 0;
@@ -424,6 +425,12 @@ int copy_field(dem_ctx* c, double* dst, const double* src, uint64_t n, cudaMemcp
 
 }  // namespace
 
+namespace dem {
+int ext_alloc_iarrays(dem_ctx* c, int b, uint64_t need) { return alloc_iarrays(c, b, need); }
+int ext_alloc_records(dem_ctx* c, uint64_t need) { return alloc_records(c, need); }
+void ext_free_iarrays(IArrays& I) { free_iarrays(I); }
+}  // namespace dem
+
 extern "C" {
 
 int dem_set_systems(dem_ctx* c, const dem_system* systems, int nsystems) {
@@ -442,6 +449,7 @@ int dem_set_systems(dem_ctx* c, const dem_system* systems, int nsystems) {
   }
   if (next != c->n) return c->fail(DEM_ERR_INVALID_ARG, "systems must cover all particles");
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->gen++;
   const std::vector<dem_system> keep = c->systems;
   c->systems.assign(systems, systems + nsystems);
   int rc = setup_grid(c);
@@ -532,6 +540,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   cudaFree(c->scan_blk);
   cudaFree(c->d_scalars);
   cudaFree(c->d_red);
+  free_graph(c);
   cudaFree(c->drv_dev);
   cudaFree(c->grids_dev);
   cudaFree(c->coff_dev);
@@ -553,6 +562,7 @@ int dem_ctx_stream(dem_ctx* c, void** stream) {
 
 int dem_set_params(dem_ctx* c, const dem_params* p) {
   if (!c) return DEM_ERR_INVALID_ARG;
+  c->gen++;
   int rc = check_params(c, p);
   if (rc) return rc;
   const bool grid_changed = std::memcmp(p->bounds_lo, c->prm.bounds_lo, sizeof(p->bounds_lo)) ||
@@ -573,6 +583,7 @@ int dem_set_particles(dem_ctx* c, const dem_particles* p, int on_device) {
   if (!p->rx || !p->ry || !p->rz || !p->radius)
     return c->fail(DEM_ERR_INVALID_ARG, "positions and radius are required");
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->gen++;
   const uint64_t n = p->n;
   int rc = alloc_particles(c, n);
   if (rc) return rc;
@@ -656,6 +667,7 @@ int dem_get_particles(dem_ctx* c, dem_particles* out, int on_device) {
 
 static int add_driver(dem_ctx* c, const DriverDev& d) {
   if (c->ndrv >= DEM_MAX_DRIVERS) return c->fail(DEM_ERR_INVALID_ARG, "too many drivers");
+  c->gen++;
   c->drv_host[c->ndrv] = d;
   DEM_CUDA_TRY(c, cudaMemcpyAsync(c->drv_dev + c->ndrv, &c->drv_host[c->ndrv], sizeof(DriverDev),
                                   cudaMemcpyHostToDevice, c->stream));
@@ -767,6 +779,7 @@ int dem_vertex_displ_over(dem_ctx* c, int* result) {
 int dem_set_shapes(dem_ctx* c, const dem_shape* shapes, int nshapes) {
   if (!c || !shapes || nshapes <= 0) return DEM_ERR_INVALID_ARG;
   if (!c->systems.empty()) return c->fail(DEM_ERR_UNSUPPORTED, "batched systems are implemented for spheres only");
+  c->gen++;
   std::vector<ShapeDev> h(nshapes);
   int mv = 0;
   for (int k = 0; k < nshapes; k++) {
@@ -860,6 +873,8 @@ int dem_step(dem_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return DEM_ERR_INVALID_ARG;
   int rc = need_list(c);
   if (rc) return rc;
+  // graph replay unless per-kernel timing is on (events cannot be recorded inside a graph)
+  if (c->prm.graph_step && c->prm.fused_step && !c->poly && nsteps > 0 && !c->prof_on) return step_graph(c, nsteps);
   for (int s = 0; s < nsteps; s++) {
     if (c->poly && c->prm.fused_step) {
       // prolog + vertex_displ_over decided in FP32; rebuild (all vertices) or the
@@ -912,6 +927,13 @@ int dem_step(dem_ctx* c, int nsteps) {
     if ((rc = launch_epilog(c))) return rc;
   }
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return DEM_OK;
+}
+
+int dem_set_graph_capacity(dem_ctx* c, uint64_t capacity) {
+  if (!c || capacity == 0) return DEM_ERR_INVALID_ARG;
+  c->gcap = capacity;
+  c->gen++;  // recapture with the new capacity
   return DEM_OK;
 }
 

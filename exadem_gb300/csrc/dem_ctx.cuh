@@ -48,6 +48,21 @@ struct dem_ctx {
   int sys_cap = 0;
   dem::SysView sysview() const { return dem::SysView{grids_dev, coff_dev, pfirst_dev, drange_dev, nsys}; }
 
+  // graph step (dem_graph.cu)
+  bool capturing = false;                  // kernels launched now go into a graph
+  unsigned long long* d_gs = nullptr;      // [0] ni, [1] overflow, [2] rebuilds, [3] capacity
+  unsigned long long* d_ni = nullptr;      // = d_gs
+  uint64_t gcap = 0;                       // interaction capacity the graph was captured with
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool capturing_body = false;             // capturing the conditional rebuild
+  uint64_t graph_launches_per_step[16] = {};     // kernel launches of one replay, per class
+  uint64_t graph_launches_per_rebuild[16] = {};  // and of the conditional rebuild
+  uint64_t gen = 0;        // bumped by every host-side change a captured graph depends on
+  uint64_t graph_gen = ~0ull;
+  void* snap = nullptr;                    // state snapshot for the overflow rollback
+  uint64_t snap_bytes = 0;
+
   // cell grid (grid = system 0's, used by the single-system polyhedron path)
   dem::GridDev grid{};
   uint64_t ncell = 0, ccap = 0;
@@ -187,6 +202,13 @@ int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total);
 int launch_poly_feature_fill(dem_ctx* c, uint64_t nu);
 int launch_contact_poly(dem_ctx* c);
 int launch_state_systems(dem_ctx* c, dem_state* out);  // one state per system
+int scan_reserve(dem_ctx* c, uint64_t n);
+// graph step (dem_graph.cu) and the allocators it uses (dem_api.cu)
+int step_graph(dem_ctx* c, int nsteps);
+void free_graph(dem_ctx* c);
+int ext_alloc_iarrays(dem_ctx* c, int b, uint64_t need);
+int ext_alloc_records(dem_ctx* c, uint64_t need);
+void ext_free_iarrays(IArrays& I);
 int launch_poly_fused_prolog(dem_ctx* c);     // prolog + FP32-decided vertex_displ_over flag
 int launch_vertex_list(dem_ctx* c);           // particles whose vertices the list uses (host sync)
 int launch_poly_vertices_listed(dem_ctx* c);  // FP64 vertices of those particles
@@ -204,6 +226,10 @@ struct ProfScope {
   int k;
   cudaEvent_t a = nullptr;
   ProfScope(dem_ctx* ctx, int kclass, int nlaunch = 1) : c(ctx), k(kclass) {
+    if (c->capturing) {  // counted per replay; no events inside a graph
+      (c->capturing_body ? c->graph_launches_per_rebuild : c->graph_launches_per_step)[k] += (uint64_t)nlaunch;
+      return;
+    }
     c->launches[k] += (uint64_t)nlaunch;
     if (c->prof_on) {
       a = c->get_event();

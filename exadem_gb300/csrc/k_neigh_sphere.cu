@@ -37,6 +37,7 @@ struct BPArgs {
   const float* zr;
   const float* rf;
   float skin_f;
+  uint64_t cap;  // interaction buffer capacity (graph step): a fill beyond it writes nothing
 };
 
 // FP32 decision of the broad-phase filter d2 > 0 && d2 < (r_i + r_j + skin)^2.
@@ -191,6 +192,7 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
   const uint32_t b = off[s], e = off[s + 1];
+  if (e > a.cap) return;
   uint32_t w = b;
   for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta) {
     if (w < e) {
@@ -260,20 +262,23 @@ __global__ void k_zero_u32(uint32_t* p, uint64_t n) {
 }
 
 // partner-side lists: interactions whose partner is a real particle that receives -f
-__global__ void k_rev_count(IArrays I, uint64_t ni, uint32_t* __restrict__ cnt) {
-  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= ni) return;
-  const uint32_t m = I.meta[k];
-  if (meta_type(m) <= DEM_ITYPE_EDGE_EDGE && !meta_owner_only(m)) atomicAdd(&cnt[I.partner[k]], 1u);
+// ni_dev != nullptr: the interaction count is read on the device (graph step)
+__global__ void k_rev_count(IArrays I, uint64_t ni, const unsigned long long* ni_dev, uint32_t* __restrict__ cnt) {
+  const uint64_t nn = ni_dev ? *ni_dev : ni;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t m = I.meta[k];
+    if (meta_type(m) <= DEM_ITYPE_EDGE_EDGE && !meta_owner_only(m)) atomicAdd(&cnt[I.partner[k]], 1u);
+  }
 }
-__global__ void k_rev_fill(IArrays I, uint64_t ni, const uint32_t* __restrict__ off, uint32_t* __restrict__ cursor,
-                           uint32_t* __restrict__ idx) {
-  const uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= ni) return;
-  const uint32_t m = I.meta[k];
-  if (meta_type(m) <= DEM_ITYPE_EDGE_EDGE && !meta_owner_only(m)) {
-    const uint32_t j = I.partner[k];
-    idx[off[j] + atomicAdd(&cursor[j], 1u)] = (uint32_t)k;
+__global__ void k_rev_fill(IArrays I, uint64_t ni, const unsigned long long* ni_dev, const uint32_t* __restrict__ off,
+                           uint32_t* __restrict__ cursor, uint32_t* __restrict__ idx) {
+  const uint64_t nn = ni_dev ? *ni_dev : ni;
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t m = I.meta[k];
+    if (meta_type(m) <= DEM_ITYPE_EDGE_EDGE && !meta_owner_only(m)) {
+      const uint32_t j = I.partner[k];
+      idx[off[j] + atomicAdd(&cursor[j], 1u)] = (uint32_t)k;
+    }
   }
 }
 // order of the partner-side contributions: InteractionPair order = (owner id, index)
@@ -314,6 +319,7 @@ BPArgs make_args(dem_ctx* c) {
   a.zr = c->crel[2];
   a.rf = c->crel[3];
   a.skin_f = (float)c->prm.rcut_inc;
+  a.cap = c->capturing ? c->gcap : ~0ull;
   return a;
 }
 }  // namespace
@@ -350,16 +356,20 @@ int launch_reverse_lists(dem_ctx* c) {
   const uint64_t n = c->n, ni = c->ni;
   cudaStream_t st = c->stream;
   const IArrays& I = c->I[c->icur];
+  // in a graph capture the count is on the device: persistent grids over d_ni
+  const unsigned long long* nd = c->capturing ? c->d_ni : nullptr;
+  const bool go = c->capturing || ni;
+  const unsigned gi = c->capturing ? (unsigned)c->num_sms * 8u : grid_for(ni, 256);
   {
-  ProfScope ps(c, K_REVERSE, ni ? 2 : 1);
+  ProfScope ps(c, K_REVERSE, go ? 2 : 1);
   k_zero_u32<<<grid_for(n + 1, 256), 256, 0, st>>>(c->rev_cnt, n + 1);
-  if (ni) k_rev_count<<<grid_for(ni, 256), 256, 0, st>>>(I, ni, c->rev_cnt);
+  if (go) k_rev_count<<<gi, 256, 0, st>>>(I, ni, nd, c->rev_cnt);
   }
   int rc = scan_exclusive_u32(c, c->rev_cnt, c->rev_off, n);
   if (rc) return rc;
-  ProfScope ps(c, K_REVERSE, 1 + (ni ? 1 : 0) + (n ? 1 : 0));
+  ProfScope ps(c, K_REVERSE, 1 + (go ? 1 : 0) + (n ? 1 : 0));
   k_zero_u32<<<grid_for(n + 1, 256), 256, 0, st>>>(c->rev_cnt, n + 1);
-  if (ni) k_rev_fill<<<grid_for(ni, 256), 256, 0, st>>>(I, ni, c->rev_off, c->rev_cnt, c->rev_idx);
+  if (go) k_rev_fill<<<gi, 256, 0, st>>>(I, ni, nd, c->rev_off, c->rev_cnt, c->rev_idx);
   if (n) k_rev_sort<<<grid_for(n, 256), 256, 0, st>>>(n, c->rev_off, I.owner, c->P[c->pcur].id, c->rev_idx);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;

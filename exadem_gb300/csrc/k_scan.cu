@@ -91,6 +91,18 @@ __global__ void k_scan_apply(const uint32_t* __restrict__ in, uint64_t n, const 
 }  // namespace
 
 // out has n+1 entries; out[n] = total.  in and out may not alias.
+// scratch for scans of up to n elements (called before a graph capture)
+int scan_reserve(dem_ctx* c, uint64_t n) {
+  const uint64_t ntiles = n == 0 ? 1 : (n + SCAN_TILE - 1) / SCAN_TILE;
+  if (ntiles <= c->scan_cap) return DEM_OK;
+  if (c->scan_blk) cudaFree(c->scan_blk);
+  c->scan_blk = nullptr;
+  c->scan_cap = 0;
+  DEM_CUDA_TRY(c, cudaMalloc(&c->scan_blk, ntiles * sizeof(uint32_t)));
+  c->scan_cap = ntiles;
+  return DEM_OK;
+}
+
 int scan_exclusive_u32(dem_ctx* c, const uint32_t* in, uint32_t* out, uint64_t n) {
   const uint64_t ntiles = n == 0 ? 1 : (n + SCAN_TILE - 1) / SCAN_TILE;
   if (ntiles > c->scan_cap) {

@@ -44,6 +44,7 @@ struct CArgs {
   IArrays I;
   Records R;
   uint64_t ni;
+  const unsigned long long* ni_dev;  // graph step: the count lives on the device
   SysView sv;  // periodic lengths of the owner's system
   const DriverDev* drv;
   dem_contact_params cp, cpd;
@@ -89,9 +90,12 @@ __device__ __forceinline__ V3 partner_pos(const CArgs& a, uint32_t meta, uint32_
 }
 
 __global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
-  const uint64_t k = (uint64_t)blockIdx.x * FT + threadIdx.x;
+  const uint64_t ni = a.ni_dev ? *a.ni_dev : a.ni;
+  const uint64_t stride = (uint64_t)gridDim.x * FT;
+  for (uint64_t base = (uint64_t)blockIdx.x * FT; base < ni; base += stride) {
+  const uint64_t k = base + threadIdx.x;
   bool want = false;
-  if (k < a.ni) {
+  if (k < ni) {
     const uint32_t meta = a.I.meta[k];
     want = true;
     if (a.screen && meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
@@ -113,6 +117,7 @@ __global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
   }
   const uint32_t pos = warp_append(want, a.cnt);
   if (want) a.L1[pos] = (uint32_t)k;
+  }
 }
 
 __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
@@ -290,6 +295,7 @@ CArgs make_cargs(dem_ctx* c) {
   a.I = c->I[c->icur];
   a.R = c->R;
   a.ni = c->ni;
+  a.ni_dev = c->capturing ? c->d_ni : nullptr;
   a.sv = c->sysview();
   a.drv = c->drv_dev;
   a.cp = c->prm.config;
@@ -325,7 +331,10 @@ int launch_contact_compact(dem_ctx* c) {
   ProfScope ps(c, K_CONTACT, 3);
   const CArgs a = make_cargs(c);
   const unsigned persistent = (unsigned)c->num_sms * 8u;
-  if (c->ni) k_cscreen<<<grid_for(c->ni, FT), FT, 0, c->stream>>>(a);
+  if (c->capturing)
+    k_cscreen<<<persistent, FT, 0, c->stream>>>(a);
+  else if (c->ni)
+    k_cscreen<<<grid_for(c->ni, FT), FT, 0, c->stream>>>(a);
   k_cdetect<<<persistent, FT, 0, c->stream>>>(a);
   k_chooke<<<persistent, FT, 0, c->stream>>>(a);
   DEM_CUDA_TRY(c, cudaGetLastError());

@@ -38,7 +38,7 @@ from . import _abi as A
 
 def make_params(bounds_lo, bounds_hi, periodic=(0, 0, 0), rcut_inc=0.05, dt=1e-3, gravity=(0.0, 0.0, -9.807),
                 law=A.LAW_HOOKE_NONE, config=None, config_driver=None, cell_size=0.0, fp32_broad_phase=0,
-                fp32_contact_screen=0, fused_step=0) -> A.Params:
+                fp32_contact_screen=0, fused_step=0, graph_step=0) -> A.Params:
     p = A.Params()
     p.bounds_lo[:] = list(map(float, bounds_lo))
     p.bounds_hi[:] = list(map(float, bounds_hi))
@@ -54,6 +54,7 @@ def make_params(bounds_lo, bounds_hi, periodic=(0, 0, 0), rcut_inc=0.05, dt=1e-3
     p.fp32_broad_phase = int(fp32_broad_phase)
     p.fp32_contact_screen = int(fp32_contact_screen)
     p.fused_step = int(fused_step)
+    p.graph_step = int(graph_step)
     return p
 
 
@@ -257,6 +258,9 @@ class System:
             q.driver_first = int(d.get("driver_first", 0))
             q.driver_count = int(d.get("driver_count", 0))
         self._check(self.b.set_systems(self.h, arr, len(systems)), "set_systems")
+
+    def set_graph_capacity(self, capacity: int) -> None:
+        self._check(self.b.set_graph_capacity(self.h, int(capacity)), "set_graph_capacity")
 
     def system_count(self) -> int:
         v = C.c_int()

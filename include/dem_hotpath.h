@@ -89,7 +89,13 @@ typedef struct dem_params {
    * compacted three-pass contact law, gather + force_to_accel + epilog) with
    * exact reciprocal-based divisions.  Same results bit for bit.          */
   int32_t fused_step;
-  int32_t reserved[5];
+  /* graph_step (with fused_step, spheres): dem_step replays the whole step as
+   * one CUDA graph; the neighbour rebuild is a conditional node that the
+   * device enables from its displacement trigger, with fixed-capacity
+   * interaction buffers (on overflow the call restores its starting state,
+   * doubles the capacity and runs again).  Same results bit for bit.       */
+  int32_t graph_step;
+  int32_t reserved[4];
 } dem_params;
 
 /* ---- particle state view (host or device pointers) ---------------------
@@ -282,6 +288,10 @@ int dem_first_iteration(dem_ctx* ctx);
  * conditional rebuild, reset, gravity, contact, force_to_accel, epilog.
  * The device decides rebuilds; the host does not synchronise per step.  */
 int dem_step(dem_ctx* ctx, int nsteps);
+/* Initial interaction capacity of the graph step (graph_step; default twice
+ * the current list + 4096).  It only sizes buffers: an overflow is recovered
+ * by rerunning the call's steps with twice the capacity.                  */
+int dem_set_graph_capacity(dem_ctx* ctx, uint64_t capacity);
 /* Number of neighbour rebuilds done so far (trigger_move_particles count). */
 int dem_rebuild_count(dem_ctx* ctx, uint64_t* out);
 
