@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--systems", type=int, default=256, help="drums: number of drums")
     ap.add_argument("--plain", action="store_true", help="plain FP64 path (no FP32 screening)")
     ap.add_argument("--no-graph", action="store_true", help="fused step launched from the host, no CUDA graph")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (cell size, launch shapes)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -303,6 +304,10 @@ def run_native(args, rank, world, local, dist):
     s = w.build()
     ext = torch.cuda.ExternalStream(s.stream_handle())
     s.first_iteration()
+    tune = None
+    if not args.plain and not args.no_tune and args.workload in ("spheres", "drums"):
+        # cell size and launch shapes; the skin only where it cannot change a bit
+        tune = s.autotune(steps_per_trial=3, skin_policy=1)
     s.step(args.warmup)
     torch.cuda.synchronize()
     s.reset_kernel_stats()
@@ -400,6 +405,8 @@ def run_native(args, rank, world, local, dist):
                      "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni,
                      "interactions": ni, "avg_launch_ms": t_contact * 1e3,
                      "note": "FP64-ALU bound in practice; see DESIGN roofline"},
+        "autotune": ({k: (round(v, 6) if isinstance(v, float) else v) for k, v in tune.items()}
+                     if tune else None),
         "kernel_shares": shares, "profiled_ms_per_step": step_ms_prof,
         "rebuilds_in_timed_region": rebuilds, "gpu_launches": launches,
         "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu,

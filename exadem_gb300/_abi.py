@@ -78,6 +78,11 @@ class SystemDesc(C.Structure):
                 ("periodic", C.c_int32 * 3), ("driver_first", C.c_int32), ("driver_count", C.c_int32)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("rcut_inc", D), ("cell_size", D), ("block", C.c_int32), ("contact_blocks_per_sm", C.c_int32),
+                ("ms_per_step", D), ("ms_per_step_before", D), ("trials", C.c_int32), ("vmax", C.c_float)]
+
+
 class InteractionList(C.Structure):
     _fields_ = [("capacity", C.c_uint64), ("count", C.c_uint64), ("owner_id", PU64), ("partner_id", PU64),
                 ("type", PU16), ("swap", PU8), ("owner_sub", PU32), ("partner_sub", PU32),
@@ -156,6 +161,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_simulation_state", [_CTX, C.POINTER(State)])
     _sig(lib, "dem_set_systems", [_CTX, C.POINTER(SystemDesc), C.c_int])
     _sig(lib, "dem_set_graph_capacity", [_CTX, C.c_uint64])
+    _sig(lib, "dem_autotune", [_CTX, C.c_int, C.c_int, C.POINTER(TuneResult)])
     _sig(lib, "dem_system_count", [_CTX, C.POINTER(C.c_int)])
     _sig(lib, "dem_simulation_state_systems", [_CTX, C.POINTER(State), C.c_int])
     _sig(lib, "dem_interaction_count", [_CTX, PU64])
@@ -180,7 +186,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
             "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
-            "dem_simulation_state_systems", "dem_set_graph_capacity"]
+            "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune"]
 
 _LIB = None
 

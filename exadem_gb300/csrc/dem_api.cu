@@ -223,17 +223,21 @@ int setup_grid(dem_ctx* c) {
     cudaFree(c->coff_dev);
     cudaFree(c->pfirst_dev);
     cudaFree(c->drange_dev);
+    cudaFree(c->trig_dev);
     c->grids_dev = nullptr;
     c->coff_dev = nullptr;
     c->pfirst_dev = nullptr;
     c->drange_dev = nullptr;
+    c->trig_dev = nullptr;
     c->sys_cap = 0;
     DEM_CUDA_TRY(c, cudaMalloc(&c->grids_dev, ns * sizeof(GridDev)));
     DEM_CUDA_TRY(c, cudaMalloc(&c->coff_dev, (ns + 1) * sizeof(uint32_t)));
     DEM_CUDA_TRY(c, cudaMalloc(&c->pfirst_dev, (ns + 1) * sizeof(uint64_t)));
     DEM_CUDA_TRY(c, cudaMalloc(&c->drange_dev, ns * sizeof(int2)));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->trig_dev, ns * sizeof(uint32_t)));
     c->sys_cap = ns;
   }
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->trig_dev, 0xff, ns * sizeof(uint32_t), c->stream));  // next rebuild: all
   DEM_CUDA_TRY(c, cudaMemcpyAsync(c->grids_dev, g.data(), ns * sizeof(GridDev), cudaMemcpyHostToDevice, c->stream));
   DEM_CUDA_TRY(c, cudaMemcpyAsync(c->coff_dev, coff.data(), (ns + 1) * 4, cudaMemcpyHostToDevice, c->stream));
   DEM_CUDA_TRY(c, cudaMemcpyAsync(c->pfirst_dev, pfirst.data(), (ns + 1) * 8, cudaMemcpyHostToDevice, c->stream));
@@ -367,6 +371,12 @@ int update_neighbors_poly(dem_ctx* c) {
   return DEM_OK;
 }
 
+// every system rebuilds as if its own trigger fired (explicit neighbour updates)
+int mark_all_triggered(dem_ctx* c) {
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->trig_dev, 0xff, c->nsys * sizeof(uint32_t), c->stream));
+  return DEM_OK;
+}
+
 int update_neighbors(dem_ctx* c) {
   c->gen++;  // buffers may move: a captured step graph is stale
   if (c->poly) return update_neighbors_poly(c);
@@ -393,6 +403,7 @@ int update_neighbors(dem_ctx* c) {
   c->have_list = true;
   c->hist_valid = true;
   if ((rc = launch_reverse_lists(c))) return rc;
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->trig_dev, 0, c->nsys * sizeof(uint32_t), c->stream));
   c->rebuilds++;
   return DEM_OK;
 }
@@ -429,6 +440,11 @@ namespace dem {
 int ext_alloc_iarrays(dem_ctx* c, int b, uint64_t need) { return alloc_iarrays(c, b, need); }
 int ext_alloc_records(dem_ctx* c, uint64_t need) { return alloc_records(c, need); }
 void ext_free_iarrays(IArrays& I) { free_iarrays(I); }
+int ext_update_neighbors(dem_ctx* c) {
+  int rc = mark_all_triggered(c);
+  return rc ? rc : update_neighbors(c);
+}
+int ext_setup_grid(dem_ctx* c) { return setup_grid(c); }
 }  // namespace dem
 
 extern "C" {
@@ -436,6 +452,10 @@ extern "C" {
 int dem_set_systems(dem_ctx* c, const dem_system* systems, int nsystems) {
   if (!c || !systems || nsystems < 1 || nsystems > DEM_MAX_SYSTEMS) return DEM_ERR_INVALID_ARG;
   if (c->poly) return c->fail(DEM_ERR_UNSUPPORTED, "batched systems are implemented for spheres only");
+  // all systems rebuild when one triggers; with cohesion a rebuild off a system's
+  // own schedule adds attracting pairs earlier than the system alone would
+  if (nsystems > 1 && c->prm.law == DEM_LAW_HOOKE_COHESIVE)
+    return c->fail(DEM_ERR_UNSUPPORTED, "batched systems need a law without cohesion");
   uint64_t next = 0;
   for (int k = 0; k < nsystems; k++) {
     const dem_system& q = systems[k];
@@ -546,6 +566,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   cudaFree(c->coff_dev);
   cudaFree(c->pfirst_dev);
   cudaFree(c->drange_dev);
+  cudaFree(c->trig_dev);
   if (c->h_scalars) cudaFreeHost(c->h_scalars);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -561,7 +582,9 @@ int dem_ctx_stream(dem_ctx* c, void** stream) {
 }
 
 int dem_set_params(dem_ctx* c, const dem_params* p) {
-  if (!c) return DEM_ERR_INVALID_ARG;
+  if (!c || !p) return DEM_ERR_INVALID_ARG;
+  if (c->systems.size() > 1 && p->law == DEM_LAW_HOOKE_COHESIVE)
+    return c->fail(DEM_ERR_UNSUPPORTED, "batched systems need a law without cohesion");
   c->gen++;
   int rc = check_params(c, p);
   if (rc) return rc;
@@ -723,6 +746,8 @@ int dem_particle_displ_over(dem_ctx* c, int* result) {
 
 int dem_update_particle_neighbors(dem_ctx* c) {
   if (!c) return DEM_ERR_INVALID_ARG;
+  int rc = mark_all_triggered(c);
+  if (rc) return rc;
   return update_neighbors(c);
 }
 
@@ -864,6 +889,7 @@ int dem_simulation_state(dem_ctx* c, dem_state* out) {
 int dem_first_iteration(dem_ctx* c) {
   if (!c) return DEM_ERR_INVALID_ARG;
   int rc;
+  if ((rc = mark_all_triggered(c))) return rc;
   if ((rc = update_neighbors(c))) return rc;
   if ((rc = launch_reset_force_moment(c))) return rc;
   return compute_force(c);

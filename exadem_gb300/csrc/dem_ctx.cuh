@@ -45,8 +45,13 @@ struct dem_ctx {
   uint32_t* coff_dev = nullptr;       // nsys + 1
   uint64_t* pfirst_dev = nullptr;     // nsys + 1
   int2* drange_dev = nullptr;         // nsys
+  uint32_t* trig_dev = nullptr;       // nsys: own trigger fired since the last rebuild
   int sys_cap = 0;
-  dem::SysView sysview() const { return dem::SysView{grids_dev, coff_dev, pfirst_dev, drange_dev, nsys}; }
+  dem::SysView sysview() const { return dem::SysView{grids_dev, coff_dev, pfirst_dev, drange_dev, trig_dev, nsys}; }
+
+  // launch shapes chosen by dem_autotune (no effect on results)
+  int tune_block = 128;      // threads per block of the fused prolog / epilog (64..256)
+  int tune_contact_bps = 8;  // persistent blocks per SM of the compacted contact law
 
   // graph step (dem_graph.cu)
   bool capturing = false;                  // kernels launched now go into a graph

@@ -125,7 +125,9 @@ int rebuild_body(dem_ctx* c) {
   k_graph_copy_list<<<(unsigned)c->num_sms * 4u, 256, 0, c->stream>>>(c->I[0], c->I[1], c->own_off[1], c->own_off[0],
                                                                        n, c->d_gs);
   DEM_CUDA_TRY(c, cudaGetLastError());
-  return launch_reverse_lists(c);
+  if ((rc = launch_reverse_lists(c))) return rc;
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->trig_dev, 0, c->nsys * sizeof(uint32_t), c->stream));
+  return DEM_OK;
 }
 
 void destroy_graph(dem_ctx* c) {

@@ -91,13 +91,18 @@ struct GridDev {
 // Systems of a batched context (one system when not batched).  System k owns
 // particles [pfirst[k], pfirst[k+1]) (the cell sort keeps particles inside
 // their system's range), cells [coff[k], coff[k+1]) of the global cell index
-// space, and drivers [drange[k].x, drange[k].x + drange[k].y).
+// space, and drivers [drange[k].x, drange[k].x + drange[k].y).  trig[k] is set
+// when system k's own displacement trigger fired: a rebuild wraps the periodic
+// positions and resets the displacement backups of those systems only, so
+// every system keeps the wrap times and trigger steps it has when run alone.
 struct SysView {
   const GridDev* g;
   const uint32_t* coff;
   const uint64_t* pfirst;  // nsys + 1 entries
   const int2* drange;
+  uint32_t* trig;          // nsys entries: the system's own rebuild trigger fired
   int nsys;
+  __device__ __forceinline__ bool triggered(int k) const { return nsys == 1 || trig[k] != 0u; }
   __device__ __forceinline__ int of(uint64_t s) const {
     int lo = 0, hi = nsys - 1;
     while (lo < hi) {  // last k with pfirst[k] <= s

@@ -22,11 +22,12 @@ __global__ void k_bin(PArrays P, uint64_t n, SysView sv, uint32_t* __restrict__ 
   if (s >= n) return;
   const int sys = sv.of(s);
   const GridDev& g = sv.g[sys];
+  const bool wrap = sv.triggered(sys);  // other systems keep their positions (clamped to edge cells)
   int k[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     double x = P.f[RX + d][s];
-    if (g.periodic[d]) {
+    if (g.periodic[d] && wrap) {
       const double lo = g.lo[d], hi = g.hi[d], Ld = g.L[d];
       if (x < lo) {
         x = x + Ld;
@@ -59,9 +60,20 @@ __global__ void k_scatter(const uint32_t* __restrict__ cell_tmp, uint64_t n, con
 }
 
 __global__ void k_cell_sort(uint64_t ncell, const uint32_t* __restrict__ cell_start, const uint64_t* __restrict__ id,
-                            uint32_t* __restrict__ perm) {
+                            uint32_t* __restrict__ perm, SysView sv) {
   const uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncell) return;
+  if (sv.nsys > 1) {  // cells of systems rebuilt without their own trigger are not used
+    int lo = 0, hi = sv.nsys - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sv.coff[mid] <= c)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    if (!sv.triggered(lo)) return;
+  }
   const uint32_t b = cell_start[c], e = cell_start[c + 1];
   for (uint32_t a = b + 1; a < e; a++) {
     const uint32_t v = perm[a];
@@ -94,14 +106,24 @@ __global__ void k_reorder(PArrays src, PArrays dst, uint64_t n, const uint32_t* 
   yr[t] = (float)(src.f[RY][o] - (g.lo[1] + (double)ky * g.csz[1]));
   zr[t] = (float)(src.f[RZ][o] - (g.lo[2] + (double)kz * g.csz[2]));
   rf[t] = (float)src.f[RAD][o];
-  // backup_r: positions at this rebuild, for the displacement trigger
-  dst.f[BX][t] = src.f[RX][o];
-  dst.f[BY][t] = src.f[RY][o];
-  dst.f[BZ][t] = src.f[RZ][o];
+  // backup_r: positions at this rebuild, for the displacement trigger (systems
+  // rebuilt without their own trigger keep their backups)
+  const bool own = sv.triggered(sys);
+  dst.f[BX][t] = own ? src.f[RX][o] : src.f[BX][o];
+  dst.f[BY][t] = own ? src.f[RY][o] : src.f[BY][o];
+  dst.f[BZ][t] = own ? src.f[RZ][o] : src.f[BZ][o];
   dst.id[t] = src.id[o];
   dst.type[t] = src.type[o];
   dst.group[t] = src.group[o];
   cell_of[t] = cell_tmp[o];
+}
+
+// Systems rebuilt without their own trigger keep every particle in its slot
+// (their interaction lists are then copied unchanged).
+__global__ void k_perm_keep(uint32_t* __restrict__ perm, uint64_t n, SysView sv) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  if (!sv.triggered(sv.of(t))) perm[t] = (uint32_t)t;
 }
 
 __global__ void k_zero_u32(uint32_t* p, uint64_t n) {
@@ -126,7 +148,8 @@ int launch_bin_particles(dem_ctx* c) {
   ProfScope ps(c, K_BIN, n ? 3 : 2);
   k_zero_u32<<<grid_for(nc + 1, 256), 256, 0, st>>>(c->cell_cnt, nc + 1);
   if (n) k_scatter<<<grid_for(n, 256), 256, 0, st>>>(c->cell_tmp, n, c->cell_start, c->cell_cnt, c->perm);
-  k_cell_sort<<<grid_for(nc, 256), 256, 0, st>>>(nc, c->cell_start, c->P[c->pcur].id, c->perm);
+  k_cell_sort<<<grid_for(nc, 256), 256, 0, st>>>(nc, c->cell_start, c->P[c->pcur].id, c->perm, c->sysview());
+  if (c->nsys > 1 && n) k_perm_keep<<<grid_for(n, 256), 256, 0, st>>>(c->perm, n, c->sysview());
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

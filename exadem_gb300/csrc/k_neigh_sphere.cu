@@ -15,7 +15,8 @@
 // One thread per owner particle; particles are in cell order so the stencil
 // reads of neighbouring threads hit the same cells (L1/L2 reuse).  In a
 // batched context the particle's system gives the grid, its cell block and
-// its drivers.
+// its drivers; a system rebuilt without its own trigger kept its slots, and
+// its previous list is copied as is (so its list is the one it has alone).
 #include "dem_ctx.cuh"
 
 namespace dem {
@@ -174,9 +175,13 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
 }
 
 template <bool F32>
-__global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt) {
+__global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ old_off) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
+  if (!a.sv.triggered(a.sv.of(s))) {  // slot kept (k_perm_keep): the previous list is copied
+    cnt[s] = old_off[s + 1] - old_off[s];
+    return;
+  }
   uint32_t m = 0;
   for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t) { m++; });
   cnt[s] = m;
@@ -193,6 +198,23 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
   if (s >= a.n) return;
   const uint32_t b = off[s], e = off[s + 1];
   if (e > a.cap) return;
+  if (!a.sv.triggered(a.sv.of(s))) {  // slot kept, partners of the same system kept: copy
+    const uint32_t ob = old_off[s];
+    for (uint32_t x = b; x < e; x++) {
+      const uint32_t y = ob + (x - b);
+      dst.owner[x] = (uint32_t)s;
+      dst.partner[x] = old.partner[y];
+      dst.pid[x] = old.pid[y];
+      dst.meta[x] = old.meta[y];
+      dst.sub[x] = old.sub[y];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        dst.ft[d][x] = old.ft[d][y];
+        dst.mo[d][x] = old.mo[d][y];
+      }
+    }
+    return;
+  }
   uint32_t w = b;
   for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta) {
     if (w < e) {
@@ -328,9 +350,9 @@ int launch_count_sphere(dem_ctx* c) {
   ProfScope ps(c, K_BROAD_COUNT, c->n ? 1 : 0);
   if (c->n) {
     if (c->prm.fp32_broad_phase)
-      k_count<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt);
+      k_count<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt, c->own_off[c->icur]);
     else
-      k_count<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt);
+      k_count<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt, c->own_off[c->icur]);
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;

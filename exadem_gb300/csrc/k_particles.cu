@@ -59,12 +59,13 @@ __global__ void k_epilog(PArrays P, uint64_t n, double half_delta_t) {
   epilog_one<false>(P, s, half_delta_t, a, mom);
 }
 
-__global__ void k_displ(PArrays P, uint64_t n, double thr2, unsigned long long* flag) {
+__global__ void k_displ(PArrays P, uint64_t n, double thr2, unsigned long long* flag, SysView sv) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;
   if (s < n) {
     const double dx = P.f[RX][s] - P.f[BX][s], dy = P.f[RY][s] - P.f[BY][s], dz = P.f[RZ][s] - P.f[BZ][s];
     over = dx * dx + dy * dy + dz * dz >= thr2;
+    if (over && sv.nsys > 1) atomicOr(&sv.trig[sv.of(s)], 1u);  // this system's own trigger
   }
   if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
 }
@@ -227,7 +228,9 @@ int launch_displ_over(dem_ctx* c) {
   const double max_displ = c->prm.rcut_inc * 0.5;
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars, 0, sizeof(unsigned long long), c->stream));
   ProfScope ps(c, K_DISPL, c->n ? 1 : 0);
-  if (c->n) k_displ<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->n, max_displ * max_displ, c->d_scalars);
+  if (c->n)
+    k_displ<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->n, max_displ * max_displ, c->d_scalars,
+                                                         c->sysview());
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

@@ -247,19 +247,20 @@ __global__ void __launch_bounds__(FT) k_chooke(CArgs a) {
 }
 
 __global__ void k_fused_prolog(PArrays P, uint64_t n, double delta_t, double half_delta_t, double delta_t2_2,
-                               double thr2, unsigned long long* flag) {
+                               double thr2, unsigned long long* flag, SysView sv) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;
   if (s < n) {
     prolog_one(P, s, delta_t, half_delta_t, delta_t2_2);
     const double dx = P.f[RX][s] - P.f[BX][s], dy = P.f[RY][s] - P.f[BY][s], dz = P.f[RZ][s] - P.f[BZ][s];
     over = dx * dx + dy * dy + dz * dz >= thr2;
+    if (over && sv.nsys > 1) atomicOr(&sv.trig[sv.of(s)], 1u);  // this system's own trigger
   }
   if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
 }
 
 // reset_force_moment + gravity_force + contact gather + force_to_accel + epilog
-__global__ void __launch_bounds__(FT) k_fused_epilog(PArrays P, Records R, uint64_t n,
+__global__ void __launch_bounds__(256) k_fused_epilog(PArrays P, Records R, uint64_t n,
                                                      const uint32_t* __restrict__ own_off,
                                                      const uint32_t* __restrict__ rev_off,
                                                      const uint32_t* __restrict__ rev_idx, double gx, double gy,
@@ -320,8 +321,9 @@ int launch_fused_prolog(dem_ctx* c) {
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars, 0, sizeof(unsigned long long), c->stream));
   ProfScope ps(c, K_PROLOG, c->n ? 1 : 0);
   if (c->n)
-    k_fused_prolog<<<grid_for(c->n, FT), FT, 0, c->stream>>>(c->P[c->pcur], c->n, delta_t, half_delta_t, delta_t2_2,
-                                                              max_displ * max_displ, c->d_scalars);
+    k_fused_prolog<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(c->P[c->pcur], c->n, delta_t,
+                                                                                   half_delta_t, delta_t2_2,
+                                                              max_displ * max_displ, c->d_scalars, c->sysview());
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }
@@ -330,7 +332,7 @@ int launch_contact_compact(dem_ctx* c) {
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 3, 0, 2 * sizeof(unsigned long long), c->stream));
   ProfScope ps(c, K_CONTACT, 3);
   const CArgs a = make_cargs(c);
-  const unsigned persistent = (unsigned)c->num_sms * 8u;
+  const unsigned persistent = (unsigned)c->num_sms * (unsigned)c->tune_contact_bps;
   if (c->capturing)
     k_cscreen<<<persistent, FT, 0, c->stream>>>(a);
   else if (c->ni)
@@ -344,7 +346,8 @@ int launch_contact_compact(dem_ctx* c) {
 int launch_fused_epilog(dem_ctx* c) {
   ProfScope ps(c, K_EPILOG, c->n ? 1 : 0);
   if (c->n)
-    k_fused_epilog<<<grid_for(c->n, FT), FT, 0, c->stream>>>(c->P[c->pcur], c->R, c->n, c->own_off[c->icur],
+    k_fused_epilog<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(c->P[c->pcur], c->R, c->n,
+                                                                                   c->own_off[c->icur],
                                                               c->rev_off, c->rev_idx, c->prm.gravity[0],
                                                               c->prm.gravity[1], c->prm.gravity[2],
                                                               c->prm.dt * 0.5);

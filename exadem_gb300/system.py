@@ -259,6 +259,12 @@ class System:
             q.driver_count = int(d.get("driver_count", 0))
         self._check(self.b.set_systems(self.h, arr, len(systems)), "set_systems")
 
+    def autotune(self, steps_per_trial: int = 5, skin_policy: int = 1) -> dict:
+        """dem_autotune: cell size, launch shapes and (skin_policy) the skin."""
+        r = A.TuneResult()
+        self._check(self.b.autotune(self.h, int(steps_per_trial), int(skin_policy), C.byref(r)), "autotune")
+        return {f: getattr(r, f) for f, _ in A.TuneResult._fields_}
+
     def set_graph_capacity(self, capacity: int) -> None:
         self._check(self.b.set_graph_capacity(self.h, int(capacity)), "set_graph_capacity")
 

@@ -213,10 +213,12 @@ int dem_register_cylinder(dem_ctx* ctx, const dem_cylinder* c);
  * drivers (a range of the registration order).  Particles of different
  * systems never interact, every system evolves exactly as it would alone, and
  * every kernel of a step covers all systems in one launch.  Spheres only.
- * Ids must be unique over all systems.  A rebuild is triggered when any
- * system's trigger fires and rebuilds all systems (a rebuild does not change
- * the trajectory: only pairs within the skin are added or dropped, and the
- * history is carried by key).  Call after dem_set_particles (which resets the
+ * Ids must be unique over all systems.  Each system rebuilds on its own
+ * displacement trigger: a rebuild launch covers all systems, but systems whose
+ * trigger did not fire keep their particle slots, positions, backups and
+ * interaction list unchanged (the list is copied), so every system evolves
+ * bit for bit as it does alone, list included.  The cohesive law is accepted
+ * for a single system only.  Call after dem_set_particles (which resets the
  * context to a single system spanning the params' domain) and after the
  * drivers are registered.                                                  */
 typedef struct dem_system {
@@ -292,6 +294,31 @@ int dem_step(dem_ctx* ctx, int nsteps);
  * the current list + 4096).  It only sizes buffers: an overflow is recovered
  * by rerunning the call's steps with twice the capacity.                  */
 int dem_set_graph_capacity(dem_ctx* ctx, uint64_t capacity);
+
+/* Autotuner of the fused sphere step (no reference counterpart; exaDEM takes
+ * cell_size and rcut_inc from the deck).  It times, on a copy of the state
+ * restored after each trial, a forced rebuild and steps_per_trial steps of
+ * candidate cell sizes (1, 1.25, 1.5 x (2 r_max + skin)), skins (0.5 to 3 x the
+ * current one) and launch shapes, and keeps the one with the lowest
+ * t_step + t_rebuild / ((skin/2) / (v_max dt)).  Cell size and launch shapes
+ * never change the list or the arithmetic.  The skin is tuned
+ *   skin_policy 0: never;
+ *   skin_policy 1: only without cohesion and without periodic axes, where a
+ *                  pair outside the list is apart and no result bit changes;
+ *   skin_policy 2: also with periodic axes (a rebuild wraps positions, so the
+ *                  rebuild steps reach the low bits: the run then equals the
+ *                  reference run with the chosen skin).  Never with cohesion. */
+typedef struct dem_tune_result {
+  double rcut_inc;               /* chosen skin (unchanged with cohesion)        */
+  double cell_size;              /* chosen cell_size parameter                   */
+  int32_t block;                 /* threads per block, fused prolog / epilog     */
+  int32_t contact_blocks_per_sm; /* persistent grid of the compacted contact law */
+  double ms_per_step;            /* model cost of the choice                     */
+  double ms_per_step_before;     /* model cost of the configuration before       */
+  int32_t trials;
+  float vmax;                    /* fastest particle speed used by the model     */
+} dem_tune_result;
+int dem_autotune(dem_ctx* ctx, int steps_per_trial, int skin_policy, dem_tune_result* out);
 /* Number of neighbour rebuilds done so far (trigger_move_particles count). */
 int dem_rebuild_count(dem_ctx* ctx, uint64_t* out);
 
