@@ -45,7 +45,8 @@ class Params(C.Structure):
                 ("symetric", C.c_int32), ("law", C.c_int32),
                 ("config", ContactParams), ("config_driver", ContactParams),
                 ("fp32_broad_phase", C.c_int32), ("fp32_contact_screen", C.c_int32),
-                ("fused_step", C.c_int32), ("graph_step", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("fused_step", C.c_int32), ("graph_step", C.c_int32), ("learned_sizing", C.c_int32),
+                ("reserved", C.c_int32 * 3)]
 
 
 PARTICLE_FIELDS = ["rx", "ry", "rz", "vx", "vy", "vz", "fx", "fy", "fz",
@@ -162,6 +163,15 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_set_systems", [_CTX, C.POINTER(SystemDesc), C.c_int])
     _sig(lib, "dem_set_graph_capacity", [_CTX, C.c_uint64])
     _sig(lib, "dem_autotune", [_CTX, C.c_int, C.c_int, C.POINTER(TuneResult)])
+    VP = C.c_void_p
+    _sig(lib, "dem_mlp_harvest", [_CTX, VP, VP, C.c_uint64, PU64, PU64])
+    _sig(lib, "dem_mlp_init", [_CTX, C.c_uint64, C.POINTER(C.c_float)])
+    _sig(lib, "dem_mlp_set_params", [_CTX, C.POINTER(C.c_float)])
+    _sig(lib, "dem_mlp_get_params", [_CTX, C.POINTER(C.c_float)])
+    _sig(lib, "dem_mlp_forward", [_CTX, VP, C.c_uint64, VP])
+    _sig(lib, "dem_mlp_loss_grad", [_CTX, VP, VP, C.c_uint64, C.POINTER(C.c_float), PD])
+    _sig(lib, "dem_mlp_train", [_CTX, VP, VP, C.c_uint64, C.c_int, C.c_uint64, C.c_float, C.c_uint64, PD])
+    _sig(lib, "dem_learned_stats", [_CTX, PU64, PU64, PU64])
     _sig(lib, "dem_system_count", [_CTX, C.POINTER(C.c_int)])
     _sig(lib, "dem_simulation_state_systems", [_CTX, C.POINTER(State), C.c_int])
     _sig(lib, "dem_interaction_count", [_CTX, PU64])
@@ -176,7 +186,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_selftest_poly_decisions", [C.c_uint64, C.c_uint64, PU64])
 
 
-# Symbols declared in include/dem_hotpath.h and include/dem_workloads.h.
+# Symbols declared in include/dem_hotpath.h, dem_workloads.h, dem_selftest.h and dem_learned.h.
 EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stream", "dem_set_params",
             "dem_set_particles", "dem_get_particles", "dem_register_surface", "dem_register_cylinder",
             "dem_particle_displ_over", "dem_update_particle_neighbors", "dem_reset_force_moment",
@@ -186,7 +196,9 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
             "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
-            "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune"]
+            "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune", "dem_mlp_harvest",
+            "dem_mlp_init", "dem_mlp_set_params", "dem_mlp_get_params", "dem_mlp_forward", "dem_mlp_loss_grad",
+            "dem_mlp_train", "dem_learned_stats"]
 
 _LIB = None
 

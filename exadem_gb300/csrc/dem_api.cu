@@ -10,6 +10,7 @@
 #include <numeric>
 #include <vector>
 
+#include "../../include/dem_learned.h"
 #include "dem_ctx.cuh"
 #include "poly_core.cuh"
 
@@ -310,6 +311,14 @@ void free_units(dem_ctx* c) {
   cudaFree(c->u_kind);
   cudaFree(c->u_pass);
   cudaFree(c->u_slots);
+  cudaFree(c->u_types);
+  cudaFree(c->u_slotoff);
+  cudaFree(c->u_order);
+  cudaFree(c->u_x);
+  cudaFree(c->u_rates);
+  c->u_types = c->u_slotoff = c->u_order = nullptr;
+  c->u_x = c->u_rates = nullptr;
+  c->slot_cap = 0;
   cudaFree(c->f_cnt);
   cudaFree(c->f_off);
   c->u_owner = c->u_partner = c->u_kind = c->f_cnt = c->f_off = nullptr;
@@ -329,6 +338,12 @@ int grow_units(dem_ctx* c, uint64_t need) {
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_kind, cap * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_pass, cap));
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_slots, cap * FEAT_SLOTS * sizeof(uint16_t)));
+  c->slot_cap = cap * FEAT_SLOTS;
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_types, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_slotoff, (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_order, cap * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_x, cap * DEM_MLP_IN * sizeof(float)));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_rates, cap * DEM_MLP_OUT * sizeof(float)));
   DEM_CUDA_TRY(c, cudaMalloc(&c->f_cnt, (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->f_off, (cap + 1) * 4));
   c->ucap = cap;
@@ -355,6 +370,11 @@ int update_neighbors_poly(dem_ctx* c) {
   if ((rc = launch_poly_vertices(c, 2))) return rc;
   uint64_t nu = 0;
   if ((rc = launch_poly_units(c, &nu, grow_units))) return rc;
+  c->learned_slots = false;
+  if (c->prm.learned_sizing && c->prm.fp32_broad_phase && mlp_ready(c) && nu) {
+    if ((rc = launch_unit_features(c, nu))) return rc;
+    if ((rc = launch_learned_sizing(c, nu))) return rc;  // sets learned_slots
+  }
   uint32_t total = 0;
   if ((rc = launch_poly_feature_count(c, nu, &total))) return rc;
   const int nw = 1 - c->icur;
@@ -510,7 +530,7 @@ int dem_ctx_create(const dem_params* params, dem_ctx** out) {
   cudaGetDevice(&c->device);
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device);
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&c->d_scalars, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&c->d_scalars, DEM_NSCALARS * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMallocHost(&c->h_scalars, 8 * sizeof(unsigned long long)) != cudaSuccess ||
       cudaMalloc(&c->drv_dev, DEM_MAX_DRIVERS * sizeof(DriverDev)) != cudaSuccess) {
     dem_ctx_destroy(c);
@@ -521,7 +541,7 @@ int dem_ctx_create(const dem_params* params, dem_ctx** out) {
     dem_ctx_destroy(c);
     return DEM_ERR_CUDA;
   }
-  cudaMemset(c->d_scalars, 0, 8 * sizeof(unsigned long long));
+  cudaMemset(c->d_scalars, 0, DEM_NSCALARS * sizeof(unsigned long long));
   for (int d = 0; d < 3; d++) c->grid.L[d] = c->prm.bounds_hi[d] - c->prm.bounds_lo[d];
   *out = c;
   return DEM_OK;
@@ -561,6 +581,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   cudaFree(c->d_scalars);
   cudaFree(c->d_red);
   free_graph(c);
+  mlp_free(c);
   cudaFree(c->drv_dev);
   cudaFree(c->grids_dev);
   cudaFree(c->coff_dev);

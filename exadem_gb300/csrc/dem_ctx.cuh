@@ -15,6 +15,16 @@ static const char* const kDemKClassNames[K_NCLASS] = {
     "prolog", "displ_over", "bin_cells", "reorder", "broad_count", "broad_fill", "reverse_lists", "scan",
     "contact", "gather", "reset", "gravity", "force_to_accel", "epilog", "state"};
 
+namespace dem {
+struct MlpState;  // k_mlp.cu
+}
+
+// device scalars (d_scalars, u64): [0] rebuild trigger, [1] active contacts,
+// [3..4] compaction list counts, [8] learned-record overflows,
+// [16..23] learned bin counters and cursors (14 u32)
+constexpr int DEM_NSCALARS = 32;
+constexpr int SC_LEARNED_OVF = 8, SC_LEARNED_BINS = 16;
+
 // features recorded per polyhedron unit by the count pass of the FP32-decided
 // enumeration; the fill pass copies them instead of deciding again
 constexpr int FEAT_SLOTS = 16;
@@ -48,6 +58,9 @@ struct dem_ctx {
   uint32_t* trig_dev = nullptr;       // nsys: own trigger fired since the last rebuild
   int sys_cap = 0;
   dem::SysView sysview() const { return dem::SysView{grids_dev, coff_dev, pfirst_dev, drange_dev, trig_dev, nsys}; }
+
+  // learned part (k_mlp.cu): MLP weights and training scratch
+  dem::MlpState* mlp = nullptr;
 
   // launch shapes chosen by dem_autotune (no effect on results)
   int tune_block = 128;      // threads per block of the fused prolog / epilog (64..256)
@@ -132,7 +145,18 @@ struct dem_ctx {
   uint64_t* u_pid = nullptr;
   uint32_t* u_kind = nullptr;
   uint8_t* u_pass = nullptr;
-  uint16_t* u_slots = nullptr;        // FEAT_SLOTS features per unit recorded by the count pass
+  uint16_t* u_slots = nullptr;        // features recorded by the count pass (FEAT_SLOTS per unit, or learned)
+  uint64_t slot_cap = 0;              // entries of u_slots
+  uint32_t* u_types = nullptr;        // exact VV, VE, VF, EE counts per unit (u8 x 4), count pass
+  uint32_t* u_slotoff = nullptr;      // learned sizing: record offsets (ucap + 1)
+  uint32_t* u_order = nullptr;        // learned sizing: count-pass order (warp bins)
+  float* u_x = nullptr;               // MLP inputs per unit (16 floats)
+  float* u_rates = nullptr;           // MLP rates per unit (4 floats)
+  bool learned_slots = false;         // the current rebuild uses u_slotoff / u_order
+  uint64_t learned_overflow = 0;      // units whose features overflowed the predicted record (last rebuild)
+  uint64_t learned_units = 0;
+  uint64_t nu_last = 0;               // units of the last polyhedron rebuild
+  bool labels_valid = false;          // u_types holds the last rebuild's exact counts
   uint32_t* f_cnt = nullptr;          // features per unit (ucap+1)
   uint32_t* f_off = nullptr;          // feature offsets (ucap+1)
   uint64_t ucap = 0;
@@ -207,6 +231,12 @@ int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total);
 int launch_poly_feature_fill(dem_ctx* c, uint64_t nu);
 int launch_contact_poly(dem_ctx* c);
 int launch_state_systems(dem_ctx* c, dem_state* out);  // one state per system
+void mlp_free(dem_ctx* c);
+int mlp_rates(dem_ctx* c, const float* dev_x, uint64_t n, float* dev_rates);
+bool mlp_ready(const dem_ctx* c);
+int launch_unit_features(dem_ctx* c, uint64_t nu);       // u_x of every unit
+int launch_learned_sizing(dem_ctx* c, uint64_t nu);      // rates -> records, bins (host sync)
+int launch_harvest(dem_ctx* c, float* x, uint8_t* y, uint64_t capacity, uint64_t* count, uint64_t* available);
 int scan_reserve(dem_ctx* c, uint64_t n);
 // graph step (dem_graph.cu) and the allocators it uses (dem_api.cu)
 int step_graph(dem_ctx* c, int nsteps);

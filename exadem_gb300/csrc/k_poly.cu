@@ -396,7 +396,10 @@ struct FeatArgs {
   const float* fvy;
   const float* fvz;
   const float* fbox;  // FP32 gate OBBs and vertex slabs
-  uint16_t* slots;    // FEAT_SLOTS per unit: (segment, i, j) of the features found by the count pass
+  uint16_t* slots;    // per unit: (segment, i, j) of the features found by the count pass
+  const uint32_t* slot_off;  // learned sizing: record of unit u = [slot_off[u], slot_off[u+1]); else FEAT_SLOTS each
+  const uint32_t* order;     // warp bins: the count pass visits units in this order (else 0, 1, ...)
+  uint32_t* utypes;          // count pass: VV, VE, VF, EE counts of each unit (u8 x 4, saturated)
 };
 
 __device__ __forceinline__ VView vview(const FeatArgs& a, uint32_t s) {
@@ -595,6 +598,7 @@ __global__ void __launch_bounds__(PT) k_feat(FeatArgs a) {
 // Enumeration order, and therefore the written list, is that of k_feat.
 struct DecUnit {
   uint64_t u;
+  uint32_t sbase, scap;  // feature record of the unit
   uint32_t A, B;
   uint64_t pid;
   const ShapeDev* SA;
@@ -645,8 +649,8 @@ __device__ __forceinline__ void dec_segment(const FeatArgs& a, const DecUnit& x,
       const uint32_t pos = count + __popc(m & lt);
       if (Fill)
         write_feature(a, base + pos, x.A, x.B, x.pid, seg_type(SEG), seg_swap(SEG), i, j);
-      else if (pos < FEAT_SLOTS)
-        a.slots[x.u * FEAT_SLOTS + pos] = (uint16_t)((SEG << 12) | (i << 6) | j);
+      else if (pos < x.scap)
+        a.slots[x.sbase + pos] = (uint16_t)((SEG << 12) | (i << 6) | j);
     }
     count += __popc(m);
   }
@@ -675,21 +679,28 @@ __global__ void __launch_bounds__(PT, 4) k_feat_dec(FeatArgs a) {
   const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
   const uint32_t lt = (1u << lane) - 1u;
-  for (uint64_t u = warp; u < a.nu; u += nwarps) {
+  for (uint64_t tt = warp; tt < a.nu; tt += nwarps) {
+    const uint64_t u = (!Fill && a.order) ? a.order[tt] : tt;
     uint32_t count = 0;
     const uint32_t base = Fill ? a.foff[u] : 0;
     if (!a.pass[u]) {
-      if (!Fill && lane == 0) a.fcnt[u] = 0;
+      if (!Fill && lane == 0) {
+        a.fcnt[u] = 0;
+        a.utypes[u] = 0u;
+      }
       continue;
     }
     DecUnit x;
     x.u = u;
+    x.sbase = a.slot_off ? a.slot_off[u] : (uint32_t)(u * FEAT_SLOTS);
+    x.scap = a.slot_off ? a.slot_off[u + 1] - x.sbase : (uint32_t)FEAT_SLOTS;
     x.A = a.u_owner[u];
     x.SA = &a.shapes[a.P.type[x.A]];
     x.ra = x.SA->r * a.P.f[HOM][x.A];
     x.va = vview(a, x.A);
     if (a.u_kind[u]) {
       driver_unit<Fill>(a, u, x.A, *x.SA, x.ra, x.va, base, lane, lt);
+      if (!Fill && lane == 0) a.utypes[u] = 0u;
       continue;
     }
     const ShapeDev& SA = *x.SA;
@@ -700,13 +711,13 @@ __global__ void __launch_bounds__(PT, 4) k_feat_dec(FeatArgs a) {
     x.rb = SB.r * a.P.f[HOM][x.B];
     x.vb = vview(a, x.B);
     const uint32_t A = x.A, B = x.B;
-    if (Fill) {  // the count pass recorded the features of this unit unless they overflowed the slots
+    if (Fill) {  // the count pass recorded the features of this unit unless they overflowed its record
       const uint32_t cnt = a.foff[u + 1] - base;
-      if (cnt <= FEAT_SLOTS) {
-        if ((uint32_t)lane < cnt) {
-          const uint32_t w = a.slots[u * FEAT_SLOTS + lane];
+      if (cnt <= x.scap) {
+        for (uint32_t q = lane; q < cnt; q += 32) {
+          const uint32_t w = a.slots[x.sbase + q];
           const int seg = (int)(w >> 12);
-          write_feature(a, base + lane, A, B, x.pid, seg_type(seg), seg_swap(seg), (w >> 6) & 63u, w & 63u);
+          write_feature(a, base + q, A, B, x.pid, seg_type(seg), seg_swap(seg), (w >> 6) & 63u, w & 63u);
         }
         continue;
       }
@@ -783,14 +794,143 @@ __global__ void __launch_bounds__(PT, 4) k_feat_dec(FeatArgs a) {
     }
     __syncwarp();
     dec_segment<0, Fill>(a, x, LgA, nA, LvB, nvB, count, base, lane, lt);
+    const uint32_t c_vv = count;
     dec_segment<1, Fill>(a, x, LgA, nA, LeB, neB, count, base, lane, lt);
     dec_segment<2, Fill>(a, x, LeA, neA, LgB, nB, count, base, lane, lt);
+    const uint32_t c_ve = count;
     dec_segment<3, Fill>(a, x, LgA, nA, LfB, nfB, count, base, lane, lt);
     dec_segment<4, Fill>(a, x, LfA, nfA, LgB, nB, count, base, lane, lt);
+    const uint32_t c_vf = count;
     dec_segment<5, Fill>(a, x, LeA, neA, LeB, neB, count, base, lane, lt);
     __syncwarp();
-    if (!Fill && lane == 0) a.fcnt[u] = count;
+    if (!Fill && lane == 0) {
+      a.fcnt[u] = count;
+      auto sat = [](uint32_t v) { return v > 255u ? 255u : v; };
+      a.utypes[u] = sat(c_vv) | (sat(c_ve - c_vv) << 8) | (sat(c_vf - c_ve) << 16) | (sat(count - c_vf) << 24);
+    }
   }
+}
+
+// ---------------------------------------------------------------- learned part
+// MLP inputs of unit u (dem_learned.h): B's centre in A's body frame / (r_A + r_B),
+// q_A^-1 q_B (w >= 0), one-hot of the unordered shape pair (types mod 3), and
+// OBB overlap with each OBB enlarged by 0, skin/4, skin/2 (the last is the unit test).
+__global__ void k_unit_features(uint64_t nu, PArrays P, const uint32_t* __restrict__ u_owner,
+                                const uint32_t* __restrict__ u_partner, const uint32_t* __restrict__ u_kind,
+                                const uint8_t* __restrict__ pass, const double* __restrict__ obb, double rV,
+                                float* __restrict__ X) {
+  const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nu) return;
+  float x[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) x[k] = 0.f;
+  if (!u_kind[u] && pass[u]) {
+    const uint32_t A = u_owner[u], B = u_partner[u];
+    const V3 d = mk(P.f[RX][B] - P.f[RX][A], P.f[RY][B] - P.f[RY][A], P.f[RZ][B] - P.f[RZ][A]);
+    const Q4 qa = {P.f[QW][A], P.f[QX][A], P.f[QY][A], P.f[QZ][A]};
+    const Q4 qb = {P.f[QW][B], P.f[QX][B], P.f[QY][B], P.f[QZ][B]};
+    const Q4 qc = {qa.w, -qa.x, -qa.y, -qa.z};
+    const V3 dl = qrotate(qc, d);
+    const double sc = 1.0 / (P.f[RAD][A] + P.f[RAD][B]);
+    x[0] = (float)(dl.x * sc);
+    x[1] = (float)(dl.y * sc);
+    x[2] = (float)(dl.z * sc);
+    // q_A^-1 q_B
+    double w = qc.w * qb.w - qc.x * qb.x - qc.y * qb.y - qc.z * qb.z;
+    double qx = qc.w * qb.x + qc.x * qb.w + qc.y * qb.z - qc.z * qb.y;
+    double qy = qc.w * qb.y - qc.x * qb.z + qc.y * qb.w + qc.z * qb.x;
+    double qz = qc.w * qb.z + qc.x * qb.y - qc.y * qb.x + qc.z * qb.w;
+    if (w < 0) w = -w, qx = -qx, qy = -qy, qz = -qz;
+    x[3] = (float)w;
+    x[4] = (float)qx;
+    x[5] = (float)qy;
+    x[6] = (float)qz;
+    const uint32_t ta = P.type[A] % 3u, tb = P.type[B] % 3u;
+    const uint32_t lo = ta < tb ? ta : tb, hi = ta < tb ? tb : ta;
+    const int pair = lo == 0 ? (int)hi : (lo == 1 ? 2 + (int)hi : 5);  // (0,0) (0,1) (0,2) (1,1) (1,2) (2,2)
+    x[7 + pair] = 1.f;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      OBBd oa = load_obb(obb + (uint64_t)A * 15), ob = load_obb(obb + (uint64_t)B * 15);
+      obb_enlarge(oa, 0.25 * q * rV);
+      obb_enlarge(ob, 0.25 * q * rV);
+      x[13 + q] = obb_intersect(oa, ob) ? 1.f : 0.f;
+    }
+  }
+  float* o = X + u * 16;
+#pragma unroll
+  for (int k = 0; k < 16; k++) o[k] = x[k];
+}
+
+// record size from the predicted rates (mean + 2 sd + 1 of the Poisson total,
+// capped at 64), exact bound nv_A for driver units; bin = predicted dominant
+// contact type (1..4), 0 for near-empty pairs, 5 for drivers, 6 for no-pass
+__global__ void k_learned_caps(uint64_t nu, PArrays P, const ShapeDev* __restrict__ shapes,
+                               const uint32_t* __restrict__ u_owner, const uint32_t* __restrict__ u_kind,
+                               const uint8_t* __restrict__ pass, const float* __restrict__ rates,
+                               uint32_t* __restrict__ cap, uint32_t* __restrict__ bin,
+                               unsigned int* __restrict__ bin_cnt) {
+  const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nu) return;
+  uint32_t cp = 0, b = 6;
+  if (pass[u]) {
+    if (u_kind[u]) {
+      cp = (uint32_t)shapes[P.type[u_owner[u]]].nv;
+      b = 5;
+    } else {
+      const float* r = rates + u * 4;
+      const float tot = r[0] + r[1] + r[2] + r[3];
+      const float c = ceilf(tot + 2.f * sqrtf(tot) + 1.f);
+      cp = c >= 64.f ? 64u : (c < 1.f ? 1u : (uint32_t)c);
+      if (tot < 0.5f) {
+        b = 0;
+      } else {
+        int k = 0;
+        for (int q = 1; q < 4; q++)
+          if (r[q] > r[k]) k = q;
+        b = 1 + k;
+      }
+    }
+  }
+  cap[u] = cp;
+  bin[u] = b;
+  atomicAdd(&bin_cnt[b], 1u);
+}
+
+// counting sort of the units by bin (order inside a bin is free: the count
+// pass writes each unit's results at the unit's own index)
+__global__ void k_learned_order(uint64_t nu, const uint32_t* __restrict__ bin, unsigned int* __restrict__ cursor,
+                                uint32_t* __restrict__ order) {
+  const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nu) return;
+  order[atomicAdd(&cursor[bin[u]], 1u)] = (uint32_t)u;
+}
+
+__global__ void k_learned_overflow(uint64_t nu, const uint32_t* __restrict__ fcnt, const uint32_t* __restrict__ off,
+                                   unsigned long long* __restrict__ over) {
+  const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nu) return;
+  if (fcnt[u] > off[u + 1] - off[u]) atomicAdd(over, 1ull);
+}
+
+// harvest: particle-pair units that pass the OBB test, in unit order
+__global__ void k_harvest_flags(uint64_t nu, const uint32_t* __restrict__ u_kind, const uint8_t* __restrict__ pass,
+                                uint32_t* __restrict__ flag) {
+  const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u < nu) flag[u] = (!u_kind[u] && pass[u]) ? 1u : 0u;
+}
+__global__ void k_harvest_write(uint64_t nu, const uint32_t* __restrict__ flag, const uint32_t* __restrict__ pos,
+                                const float* __restrict__ X, const uint32_t* __restrict__ types, uint64_t capacity,
+                                float* __restrict__ xo, uint8_t* __restrict__ yo) {
+  const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nu || !flag[u]) return;
+  const uint64_t p = pos[u];
+  if (p >= capacity) return;
+#pragma unroll
+  for (int k = 0; k < 16; k++) xo[p * 16 + k] = X[u * 16 + k];
+  const uint32_t t = types[u];
+#pragma unroll
+  for (int k = 0; k < 4; k++) yo[p * 4 + k] = (uint8_t)((t >> (8 * k)) & 255u);
 }
 
 // own_off[s] = feature offset of the first unit of s
@@ -1160,6 +1300,9 @@ static FeatArgs make_fargs(dem_ctx* c, uint64_t nu) {
   a.fvz = c->vrf[2];
   a.fbox = c->pfbox;
   a.slots = c->u_slots;
+  a.slot_off = c->learned_slots ? c->u_slotoff : nullptr;
+  a.order = c->learned_slots ? c->u_order : nullptr;
+  a.utypes = c->u_types;
   return a;
 }
 
@@ -1175,8 +1318,18 @@ int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total) {
   }
   int rc = scan_exclusive_u32(c, c->f_cnt, c->f_off, nu);
   if (rc) return rc;
+  if (c->learned_slots && nu) {  // pairs whose features overflowed the predicted record
+    DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + SC_LEARNED_OVF, 0, sizeof(unsigned long long), c->stream));
+    k_learned_overflow<<<grid_for(nu, 256), 256, 0, c->stream>>>(nu, c->f_cnt, c->u_slotoff, c->d_scalars + SC_LEARNED_OVF);
+  }
+  unsigned long long ovf = 0;
   DEM_CUDA_TRY(c, cudaMemcpyAsync(total, c->f_off + nu, 4, cudaMemcpyDeviceToHost, c->stream));
+  if (c->learned_slots)
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(&ovf, c->d_scalars + SC_LEARNED_OVF, 8, cudaMemcpyDeviceToHost, c->stream));
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  c->learned_overflow = ovf;
+  c->nu_last = nu;
+  c->labels_valid = c->prm.fp32_broad_phase != 0;  // the FP32-decided count pass writes the labels
   return DEM_OK;
 }
 
@@ -1190,6 +1343,72 @@ int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
     k_feat<true><<<blocks, PT, 0, c->stream>>>(a);
   k_own_from_units<<<grid_for(c->n + 1, 256), 256, 0, c->stream>>>(c->n, c->u_off, c->f_off, c->own_off[1 - c->icur]);
   DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+int launch_unit_features(dem_ctx* c, uint64_t nu) {
+  if (!nu) return DEM_OK;
+  k_unit_features<<<grid_for(nu, 128), 128, 0, c->stream>>>(nu, c->P[c->pcur], c->u_owner, c->u_partner, c->u_kind,
+                                                             c->u_pass, c->pobb, c->prm.rcut_inc, c->u_x);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+// MLP rates -> per-unit feature records (scan) and the bin order of the count pass
+int launch_learned_sizing(dem_ctx* c, uint64_t nu) {
+  int rc = mlp_rates(c, c->u_x, nu, c->u_rates);
+  if (rc) return rc;
+  unsigned int* d_bins = reinterpret_cast<unsigned int*>(c->d_scalars + SC_LEARNED_BINS);  // 7 counters, 7 cursors
+  DEM_CUDA_TRY(c, cudaMemsetAsync(d_bins, 0, 14 * sizeof(unsigned int), c->stream));
+  k_learned_caps<<<grid_for(nu, 256), 256, 0, c->stream>>>(nu, c->P[c->pcur], (const ShapeDev*)c->shapes_dev,
+                                                            c->u_owner, c->u_kind, c->u_pass, c->u_rates, c->f_cnt,
+                                                            c->u_order, d_bins);
+  if ((rc = scan_exclusive_u32(c, c->f_cnt, c->u_slotoff, nu))) return rc;
+  unsigned int bins[7];
+  uint32_t total = 0;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(bins, d_bins, sizeof(bins), cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(&total, c->u_slotoff + nu, 4, cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (total > c->slot_cap) {
+    cudaFree(c->u_slots);
+    c->u_slots = nullptr;
+    c->slot_cap = 0;
+    DEM_CUDA_TRY(c, cudaMalloc(&c->u_slots, ((uint64_t)total + total / 4 + 1024) * sizeof(uint16_t)));
+    c->slot_cap = (uint64_t)total + total / 4 + 1024;
+  }
+  unsigned int cursor[7];
+  unsigned int acc = 0;
+  for (int b = 0; b < 7; b++) {
+    cursor[b] = acc;
+    acc += bins[b];
+  }
+  // the bins were written into u_order by k_learned_caps: copy them out, then sort
+  uint32_t* bin_of = c->u_types;  // free until the count pass writes the labels
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(bin_of, c->u_order, nu * 4, cudaMemcpyDeviceToDevice, c->stream));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(d_bins + 7, cursor, sizeof(cursor), cudaMemcpyHostToDevice, c->stream));
+  k_learned_order<<<grid_for(nu, 256), 256, 0, c->stream>>>(nu, bin_of, d_bins + 7, c->u_order);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  c->learned_slots = true;
+  c->learned_units = nu;
+  return DEM_OK;
+}
+
+int launch_harvest(dem_ctx* c, float* x, uint8_t* y, uint64_t capacity, uint64_t* count, uint64_t* available) {
+  const uint64_t nu = c->nu_last;
+  *count = *available = 0;
+  if (!nu) return DEM_OK;
+  int rc = launch_unit_features(c, nu);
+  if (rc) return rc;
+  uint32_t* flag = c->u_slotoff;  // scratch: flags, then positions in u_order
+  k_harvest_flags<<<grid_for(nu, 256), 256, 0, c->stream>>>(nu, c->u_kind, c->u_pass, flag);
+  if ((rc = scan_exclusive_u32(c, flag, c->u_order, nu))) return rc;
+  uint32_t tot = 0;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(&tot, c->u_order + nu, 4, cudaMemcpyDeviceToHost, c->stream));
+  k_harvest_write<<<grid_for(nu, 256), 256, 0, c->stream>>>(nu, flag, c->u_order, c->u_x, c->u_types, capacity, x, y);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  *available = tot;
+  *count = std::min<uint64_t>(tot, capacity);
   return DEM_OK;
 }
 

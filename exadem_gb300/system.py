@@ -38,7 +38,7 @@ from . import _abi as A
 
 def make_params(bounds_lo, bounds_hi, periodic=(0, 0, 0), rcut_inc=0.05, dt=1e-3, gravity=(0.0, 0.0, -9.807),
                 law=A.LAW_HOOKE_NONE, config=None, config_driver=None, cell_size=0.0, fp32_broad_phase=0,
-                fp32_contact_screen=0, fused_step=0, graph_step=0) -> A.Params:
+                fp32_contact_screen=0, fused_step=0, graph_step=0, learned_sizing=0) -> A.Params:
     p = A.Params()
     p.bounds_lo[:] = list(map(float, bounds_lo))
     p.bounds_hi[:] = list(map(float, bounds_hi))
@@ -55,6 +55,7 @@ def make_params(bounds_lo, bounds_hi, periodic=(0, 0, 0), rcut_inc=0.05, dt=1e-3
     p.fp32_contact_screen = int(fp32_contact_screen)
     p.fused_step = int(fused_step)
     p.graph_step = int(graph_step)
+    p.learned_sizing = int(learned_sizing)
     return p
 
 

@@ -95,7 +95,13 @@ typedef struct dem_params {
    * interaction buffers (on overflow the call restores its starting state,
    * doubles the capacity and runs again).  Same results bit for bit.       */
   int32_t graph_step;
-  int32_t reserved[4];
+  /* learned_sizing (polyhedra, with fp32_broad_phase and trained weights,
+   * dem_learned.h): the MLP's predicted feature counts size each candidate
+   * pair's feature record in the count pass and order the pairs into warp
+   * bins by predicted contact type; a pair whose features overflow its record
+   * is enumerated again exactly.  Same results bit for bit.                */
+  int32_t learned_sizing;
+  int32_t reserved[3];
 } dem_params;
 
 /* ---- particle state view (host or device pointers) ---------------------

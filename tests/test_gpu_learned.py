@@ -1,0 +1,90 @@
+"""The learned part on the GPU: gradients of the library's BF16/FP32 training
+kernels against the CPU restatement, harvesting of exact labels, training, and
+the ablation that learned sizing changes no result."""
+import numpy as np
+import pytest
+
+from exadem_gb300 import workloads as W
+from exadem_gb300.learned import Learned
+from tests.helpers import assert_same_list, bit_equal_fraction
+
+pytestmark = pytest.mark.gpu
+
+FAST = dict(fused_step=1, fp32_broad_phase=1, fp32_contact_screen=1)
+
+
+def _lattice(side=22, seed=31, **kw):
+    return W.polyhedra_lattice(nx=side, ny=side, nz=side, seed=seed, **FAST, **kw)
+
+
+def test_gradients_match_cpu_restatement(native_lib):
+    import torch
+    from oracle import mlp_oracle as M
+
+    s = _lattice(side=6).build()
+    L = Learned(s)
+    L.init(seed=3, label_means=[0.05, 0.2, 0.3, 0.5])
+    rng = np.random.default_rng(5)
+    n = 3000  # not a multiple of 16: exercises the tail tile
+    x = rng.normal(0, 1, (n, 16)).astype(np.float32)
+    x[:, 7:] = rng.integers(0, 2, (n, 9))
+    y = rng.poisson(0.8, (n, 4)).astype(np.uint8)
+    xg, yg = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    loss, g = L.loss_grad(xg, yg)
+    p = L.params()
+    loss_c, g_c = M.loss_grad(p, x, y.astype(np.float32))
+    assert abs(loss - loss_c) <= 1e-5 * abs(loss_c)
+    assert np.linalg.norm(g - g_c) <= 2e-3 * np.linalg.norm(g_c)
+    assert np.allclose(g, g_c, rtol=2e-2, atol=2e-3 * np.abs(g_c).max())
+    r = L.rates(xg).cpu().numpy()
+    assert np.allclose(r, M.rates(p, x), rtol=1e-4, atol=1e-6)
+
+
+def test_harvest_labels_are_the_exact_counts(native_lib):
+    s = _lattice(side=12).build()
+    s.update_particle_neighbors()
+    x, y, avail = Learned(s).harvest(1 << 20)
+    assert avail == x.shape[0] > 1000
+    lst = s.interactions()
+    assert int(y.sum().item()) == int(np.sum(lst["type"] <= 3))
+    per_type = y.sum(0).cpu().numpy()
+    assert per_type[3] == np.sum(lst["type"] == 3) and per_type[0] == np.sum(lst["type"] == 0)
+
+
+def test_training_reduces_the_loss(native_lib):
+    s = _lattice(side=20).build()
+    s.update_particle_neighbors()
+    L = Learned(s)
+    x, y, _ = L.harvest(1 << 22)
+    L.init(seed=4, label_means=y.float().mean(0).tolist())
+    l0, _ = L.loss_grad(x, y)
+    losses = L.train(x, y, epochs=30, batch=4096, lr=3e-3, seed=4)
+    assert losses[-1] < 0.9 * l0
+    rates = L.rates(x)
+    tot_pred, tot_true = rates.sum(1), y.float().sum(1)
+    corr = np.corrcoef(tot_pred.cpu().numpy(), tot_true.cpu().numpy())[0, 1]
+    assert corr > 0.3  # learning on a small harvest; the full dataset is the bench's
+
+
+def test_learned_sizing_changes_no_result(native_lib):
+    base = _lattice(side=20).build()
+    base.update_particle_neighbors()
+    L = Learned(base)
+    x, y, _ = L.harvest(1 << 22)
+    L.init(seed=4, label_means=y.float().mean(0).tolist())
+    L.train(x, y, epochs=20, batch=4096, lr=3e-3, seed=4)
+    params = L.params()
+    a, b = _lattice(side=20).build(), _lattice(side=20, learned_sizing=1).build()
+    Learned(b).set_params(params)
+    for s in (a, b):
+        s.first_iteration()
+    st = Learned(b).stats()
+    assert st["units"] > 0 and st["record_entries"] < 16 * st["units"]
+    for _ in range(3):
+        for s in (a, b):
+            s.step(20)
+            s.update_particle_neighbors()
+        assert_same_list(a.interactions(), b.interactions())
+    assert bit_equal_fraction(a.particles(), b.particles()) == 1.0
+    st = Learned(b).stats()
+    assert st["overflow"] < 0.05 * st["units"]
