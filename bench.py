@@ -52,6 +52,13 @@ def parse():
     ap.add_argument("--plain", action="store_true", help="plain FP64 path (no FP32 screening)")
     ap.add_argument("--no-graph", action="store_true", help="fused step launched from the host, no CUDA graph")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (cell size, launch shapes)")
+    ap.add_argument("--learned", action="store_true",
+                    help="polyhedra: harvest candidate pairs, train the MLP, time with learned sizing "
+                         "and without it")
+    ap.add_argument("--harvest", type=int, default=5_000_000, help="learned: candidate pairs to harvest")
+    ap.add_argument("--learned-mode", type=int, default=1, choices=[1, 2],
+                    help="learned: 1 predicted record sizes, 2 also warp bins by predicted contact type")
+    ap.add_argument("--epochs", type=int, default=20, help="learned: training epochs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     return ap.parse_args()
@@ -158,6 +165,8 @@ def workload(args):
     flags = dict(fp32_contact_screen=opt, fused_step=opt, fp32_broad_phase=opt)
     if args.workload in ("spheres", "drums"):
         flags["graph_step"] = opt and not args.no_graph
+    if args.learned and args.workload in ("polyhedra", "polyhedra_dense"):
+        flags["learned_sizing"] = args.learned_mode
     if args.workload == "polyhedra":
         return W.polyhedra_floor(n=args.n or 200_000, **flags)
     if args.workload == "polyhedra_dense":
@@ -290,6 +299,49 @@ def run_drums_separate(args, w, rank, world, local, dist):
         print(json.dumps(line))
 
 
+def train_learned(args):
+    """Harvests candidate polyhedron pairs with their exact contact counts from
+    forced rebuilds of the dense lattice (config 3's shapes and contact law),
+    trains the MLP on the GPU, and returns its parameters and a summary."""
+    import torch
+
+    from exadem_gb300 import workloads as W
+    from exadem_gb300.learned import Learned
+
+    side = round((args.n or 200_000) ** (1.0 / 3.0))
+    s = W.polyhedra_lattice(nx=side, ny=side, nz=side, seed=41, fused_step=1, fp32_broad_phase=1,
+                            fp32_contact_screen=1).build()
+    s.first_iteration()
+    L = Learned(s)
+    xs, ys, rebuilds = [], [], 0
+    t0 = time.perf_counter()
+    while sum(x.shape[0] for x in xs) < args.harvest and rebuilds < 40:
+        s.update_particle_neighbors()
+        x, y, _ = L.harvest(1 << 24)
+        xs.append(x.clone())
+        ys.append(y.clone())
+        rebuilds += 1
+        s.step(25)
+    x = torch.cat(xs)[: args.harvest].contiguous()
+    y = torch.cat(ys)[: args.harvest].contiguous()
+    t_harvest = time.perf_counter() - t0
+    L.init(seed=4, label_means=y.float().mean(0).tolist())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = L.train(x, y, epochs=args.epochs, batch=65536, lr=1e-3, seed=4)
+    t_train = time.perf_counter() - t0
+    rates = L.rates(x)
+    tot = y.float().sum(1)
+    corr = float(torch.corrcoef(torch.stack([rates.sum(1), tot]))[0, 1])
+    params = L.params()
+    s.close()
+    return params, {"samples": int(x.shape[0]), "harvest_rebuilds": rebuilds, "harvest_s": round(t_harvest, 2),
+                    "epochs": args.epochs, "batch": 65536, "lr": 1e-3, "train_s": round(t_train, 2),
+                    "loss_first_epoch": losses[0], "loss_last_epoch": losses[-1],
+                    "corr_total_count": round(corr, 4),
+                    "label_means": [round(v, 4) for v in y.float().mean(0).tolist()]}
+
+
 def run_native(args, rank, world, local, dist):
     import numpy as np
     import torch
@@ -301,7 +353,14 @@ def run_native(args, rank, world, local, dist):
     w = workload(args)
     if is_batch(w) and args.plain:
         return run_drums_separate(args, w, rank, world, local, dist)
+    learned = None
+    if args.learned and args.workload in ("polyhedra", "polyhedra_dense"):
+        params, learned = train_learned(args)
     s = w.build()
+    if learned is not None:
+        from exadem_gb300.learned import Learned
+
+        Learned(s).set_params(params)
     ext = torch.cuda.ExternalStream(s.stream_handle())
     s.first_iteration()
     tune = None
@@ -324,6 +383,28 @@ def run_native(args, rank, world, local, dist):
         barrier(dist)
     ms = ev0.elapsed_time(ev1)
     rebuilds = s.rebuild_count() - r0
+    if learned is not None:
+        from exadem_gb300.learned import Learned
+
+        learned["last_rebuild"] = Learned(s).stats()
+        # the same step without the learned part (the exact two-pass sizing)
+        w0 = workload(argparse.Namespace(**{**vars(args), "learned": False}))
+        s0 = w0.build()
+        s0.first_iteration()
+        s0.step(args.warmup)
+        ext0 = torch.cuda.ExternalStream(s0.stream_handle())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext0)
+        s0.step(args.steps)
+        e1.record(ext0)
+        e1.synchronize()
+        learned["ms_per_step_without"] = e0.elapsed_time(e1) / args.steps
+        learned["ms_per_step_with"] = ms / args.steps
+        learned["rebuilds_without"] = s0.rebuild_count()
+        learned["same_state"] = bool(s0.simulation_state()["kinetic_energy"].tolist()
+                                     == s.simulation_state()["kinetic_energy"].tolist())
+        s0.close()
     stats = s.kernel_stats()
     launches = sum(v["launches"] for v in stats.values())
     ms = allmax(dist, ms)
@@ -407,6 +488,7 @@ def run_native(args, rank, world, local, dist):
                      "note": "FP64-ALU bound in practice; see DESIGN roofline"},
         "autotune": ({k: (round(v, 6) if isinstance(v, float) else v) for k, v in tune.items()}
                      if tune else None),
+        "learned": learned,
         "kernel_shares": shares, "profiled_ms_per_step": step_ms_prof,
         "rebuilds_in_timed_region": rebuilds, "gpu_launches": launches,
         "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu,

@@ -814,10 +814,47 @@ __global__ void __launch_bounds__(PT, 4) k_feat_dec(FeatArgs a) {
 // ---------------------------------------------------------------- learned part
 // MLP inputs of unit u (dem_learned.h): B's centre in A's body frame / (r_A + r_B),
 // q_A^-1 q_B (w >= 0), one-hot of the unordered shape pair (types mod 3), and
-// OBB overlap with each OBB enlarged by 0, skin/4, skin/2 (the last is the unit test).
+// OBB overlap with each OBB enlarged by 0, skin/4, skin/2.  Inputs need no
+// exactness: all in FP32, from the FP32 gate OBBs of the rebuild (which carry
+// the skin/2 + skin/2 enlargement of the enumeration, taken off here).
+__device__ __forceinline__ bool obb_overlap_f32(const OBBf& A, const OBBf& B, float grow) {
+  float R[3][3], AR[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      R[i][j] = fdot(A.e[i], B.e[j]);
+      AR[i][j] = fabsf(R[i][j]) + 1e-6f;
+    }
+  const F3 d = B.c - A.c;
+  const float t[3] = {fdot(d, A.e[0]), fdot(d, A.e[1]), fdot(d, A.e[2])};
+  const float ea[3] = {A.ext[0] + grow, A.ext[1] + grow, A.ext[2] + grow};
+  const float eb[3] = {B.ext[0] + grow, B.ext[1] + grow, B.ext[2] + grow};
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+    if (fabsf(t[i]) > ea[i] + eb[0] * AR[i][0] + eb[1] * AR[i][1] + eb[2] * AR[i][2]) return false;
+#pragma unroll
+  for (int j = 0; j < 3; j++)
+    if (fabsf(t[0] * R[0][j] + t[1] * R[1][j] + t[2] * R[2][j]) >
+        eb[j] + ea[0] * AR[0][j] + ea[1] * AR[1][j] + ea[2] * AR[2][j])
+      return false;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    const int i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int j1 = (j + 1) % 3, j2 = (j + 2) % 3;
+      const float ra = ea[i1] * AR[i2][j] + ea[i2] * AR[i1][j];
+      const float rb = eb[j1] * AR[i][j2] + eb[j2] * AR[i][j1];
+      if (fabsf(t[i2] * R[i1][j] - t[i1] * R[i2][j]) > ra + rb) return false;
+    }
+  }
+  return true;
+}
+
 __global__ void k_unit_features(uint64_t nu, PArrays P, const uint32_t* __restrict__ u_owner,
                                 const uint32_t* __restrict__ u_partner, const uint32_t* __restrict__ u_kind,
-                                const uint8_t* __restrict__ pass, const double* __restrict__ obb, double rV,
+                                const uint8_t* __restrict__ pass, const float* __restrict__ fbox, float rV,
                                 float* __restrict__ X) {
   const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (u >= nu) return;
@@ -826,43 +863,41 @@ __global__ void k_unit_features(uint64_t nu, PArrays P, const uint32_t* __restri
   for (int k = 0; k < 16; k++) x[k] = 0.f;
   if (!u_kind[u] && pass[u]) {
     const uint32_t A = u_owner[u], B = u_partner[u];
-    const V3 d = mk(P.f[RX][B] - P.f[RX][A], P.f[RY][B] - P.f[RY][A], P.f[RZ][B] - P.f[RZ][A]);
-    const Q4 qa = {P.f[QW][A], P.f[QX][A], P.f[QY][A], P.f[QZ][A]};
-    const Q4 qb = {P.f[QW][B], P.f[QX][B], P.f[QY][B], P.f[QZ][B]};
-    const Q4 qc = {qa.w, -qa.x, -qa.y, -qa.z};
-    const V3 dl = qrotate(qc, d);
-    const double sc = 1.0 / (P.f[RAD][A] + P.f[RAD][B]);
-    x[0] = (float)(dl.x * sc);
-    x[1] = (float)(dl.y * sc);
-    x[2] = (float)(dl.z * sc);
-    // q_A^-1 q_B
-    double w = qc.w * qb.w - qc.x * qb.x - qc.y * qb.y - qc.z * qb.z;
-    double qx = qc.w * qb.x + qc.x * qb.w + qc.y * qb.z - qc.z * qb.y;
-    double qy = qc.w * qb.y - qc.x * qb.z + qc.y * qb.w + qc.z * qb.x;
-    double qz = qc.w * qb.z + qc.x * qb.y - qc.y * qb.x + qc.z * qb.w;
-    if (w < 0) w = -w, qx = -qx, qy = -qy, qz = -qz;
-    x[3] = (float)w;
-    x[4] = (float)qx;
-    x[5] = (float)qy;
-    x[6] = (float)qz;
+    const F3 d = f3((float)(P.f[RX][B] - P.f[RX][A]), (float)(P.f[RY][B] - P.f[RY][A]),
+                    (float)(P.f[RZ][B] - P.f[RZ][A]));
+    const float4 qa = make_float4((float)P.f[QW][A], (float)P.f[QX][A], (float)P.f[QY][A], (float)P.f[QZ][A]);
+    const float4 qb = make_float4((float)P.f[QW][B], (float)P.f[QX][B], (float)P.f[QY][B], (float)P.f[QZ][B]);
+    const float4 qc = make_float4(qa.x, -qa.y, -qa.z, -qa.w);  // (w, x, y, z) conjugate
+    const F3 dl = qrotate_f32(qc, d);
+    const float sc = 1.f / (float)(P.f[RAD][A] + P.f[RAD][B]);
+    x[0] = dl.x * sc;
+    x[1] = dl.y * sc;
+    x[2] = dl.z * sc;
+    // q_A^-1 q_B, components (w, x, y, z) = (.x, .y, .z, .w)
+    float w = qc.x * qb.x - qc.y * qb.y - qc.z * qb.z - qc.w * qb.w;
+    float qx = qc.x * qb.y + qc.y * qb.x + qc.z * qb.w - qc.w * qb.z;
+    float qy = qc.x * qb.z - qc.y * qb.w + qc.z * qb.x + qc.w * qb.y;
+    float qz = qc.x * qb.w + qc.y * qb.z - qc.z * qb.y + qc.w * qb.x;
+    if (w < 0.f) w = -w, qx = -qx, qy = -qy, qz = -qz;
+    x[3] = w;
+    x[4] = qx;
+    x[5] = qy;
+    x[6] = qz;
     const uint32_t ta = P.type[A] % 3u, tb = P.type[B] % 3u;
     const uint32_t lo = ta < tb ? ta : tb, hi = ta < tb ? tb : ta;
     const int pair = lo == 0 ? (int)hi : (lo == 1 ? 2 + (int)hi : 5);  // (0,0) (0,1) (0,2) (1,1) (1,2) (2,2)
     x[7 + pair] = 1.f;
+    const OBBf oa = load_obbf(fbox + (uint64_t)A * FBOX_STRIDE, f3(0.f, 0.f, 0.f));
+    const OBBf ob = load_obbf(fbox + (uint64_t)B * FBOX_STRIDE, d);
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-      OBBd oa = load_obb(obb + (uint64_t)A * 15), ob = load_obb(obb + (uint64_t)B * 15);
-      obb_enlarge(oa, 0.25 * q * rV);
-      obb_enlarge(ob, 0.25 * q * rV);
-      x[13 + q] = obb_intersect(oa, ob) ? 1.f : 0.f;
-    }
+    for (int q = 0; q < 3; q++) x[13 + q] = obb_overlap_f32(oa, ob, (0.25f * q - 1.f) * rV) ? 1.f : 0.f;
   }
   float* o = X + u * 16;
 #pragma unroll
   for (int k = 0; k < 16; k++) o[k] = x[k];
 }
 
-// record size from the predicted rates (mean + 2 sd + 1 of the Poisson total,
+// record size from the predicted rates (mean + 3 sd + 2 of the Poisson total,
 // capped at 64), exact bound nv_A for driver units; bin = predicted dominant
 // contact type (1..4), 0 for near-empty pairs, 5 for drivers, 6 for no-pass
 __global__ void k_learned_caps(uint64_t nu, PArrays P, const ShapeDev* __restrict__ shapes,
@@ -880,7 +915,7 @@ __global__ void k_learned_caps(uint64_t nu, PArrays P, const ShapeDev* __restric
     } else {
       const float* r = rates + u * 4;
       const float tot = r[0] + r[1] + r[2] + r[3];
-      const float c = ceilf(tot + 2.f * sqrtf(tot) + 1.f);
+      const float c = ceilf(tot + 3.f * sqrtf(tot) + 2.f);
       cp = c >= 64.f ? 64u : (c < 1.f ? 1u : (uint32_t)c);
       if (tot < 0.5f) {
         b = 0;
@@ -1301,7 +1336,7 @@ static FeatArgs make_fargs(dem_ctx* c, uint64_t nu) {
   a.fbox = c->pfbox;
   a.slots = c->u_slots;
   a.slot_off = c->learned_slots ? c->u_slotoff : nullptr;
-  a.order = c->learned_slots ? c->u_order : nullptr;
+  a.order = (c->learned_slots && c->prm.learned_sizing >= 2) ? c->u_order : nullptr;
   a.utypes = c->u_types;
   return a;
 }
@@ -1349,7 +1384,7 @@ int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
 int launch_unit_features(dem_ctx* c, uint64_t nu) {
   if (!nu) return DEM_OK;
   k_unit_features<<<grid_for(nu, 128), 128, 0, c->stream>>>(nu, c->P[c->pcur], c->u_owner, c->u_partner, c->u_kind,
-                                                             c->u_pass, c->pobb, c->prm.rcut_inc, c->u_x);
+                                                             c->u_pass, c->pfbox, (float)c->prm.rcut_inc, c->u_x);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

@@ -96,10 +96,10 @@ typedef struct dem_params {
    * doubles the capacity and runs again).  Same results bit for bit.       */
   int32_t graph_step;
   /* learned_sizing (polyhedra, with fp32_broad_phase and trained weights,
-   * dem_learned.h): the MLP's predicted feature counts size each candidate
-   * pair's feature record in the count pass and order the pairs into warp
-   * bins by predicted contact type; a pair whose features overflow its record
-   * is enumerated again exactly.  Same results bit for bit.                */
+   * dem_learned.h): 1: the MLP's predicted feature counts size each candidate
+   * pair's feature record in the count pass; 2: and the count pass visits the
+   * pairs in warp bins by predicted contact type.  A pair whose features
+   * overflow its record is enumerated again exactly.  Same results bit for bit. */
   int32_t learned_sizing;
   int32_t reserved[3];
 } dem_params;

@@ -13,7 +13,8 @@
  *   [0..3)   position of B's centre in A's body frame / (r_A + r_B)
  *   [3..7)   relative orientation q_A^-1 q_B (w >= 0)
  *   [7..13)  one-hot of the unordered shape-type pair (types mod 3)
- *   [13..16) OBB(A) and OBB(B) intersect when enlarged by 0, skin/2, skin
+ *   [13..16) OBB(A) and OBB(B) overlap, each enlarged by 0, skin/4, skin/2 (the
+ *            last is the candidate test); all inputs in FP32
  * Labels (uint8 x 4): exact VV, VE (+swap), VF (+swap), EE counts (saturated at 255).
  */
 #ifndef DEM_LEARNED_H
