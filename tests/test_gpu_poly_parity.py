@@ -26,7 +26,7 @@ def test_lattice_first_iteration(native_lib):
     assert bit_equal_fraction(pg, po, ["fx", "fy", "fz", "momx", "momy", "momz"]) == 1.0
 
 
-@pytest.mark.parametrize("flags", [{}, dict(fused_step=1, fp32_broad_phase=1)])
+@pytest.mark.parametrize("flags", [{}, dict(fused_step=1, fp32_broad_phase=1, fp32_contact_screen=1)])
 def test_lattice_100_steps(native_lib, flags):
     w = W.polyhedra_lattice(seed=11, **flags)
     g, o = pair(w)
@@ -45,7 +45,7 @@ def test_spinning_lattice_rebuild_steps(native_lib):
     """Fast rotation (vertex speeds ~25 m/s, max_displ reached every ~10 steps):
     the FP32-decided vertex_displ_over of the fused step rebuilds on the same
     steps as the oracle, and the state stays on the oracle's."""
-    w = W.polyhedra_lattice(nx=8, ny=8, nz=4, seed=21, fused_step=1, fp32_broad_phase=1)
+    w = W.polyhedra_lattice(nx=8, ny=8, nz=4, seed=21, fused_step=1, fp32_broad_phase=1, fp32_contact_screen=1)
     rng = np.random.default_rng(21)
     n = w.n
     for k in ("vrotx", "vroty", "vrotz"):
