@@ -114,10 +114,12 @@ int rebuild_body(dem_ctx* c) {
   const uint64_t n = c->n;
   int rc;
   if ((rc = launch_bin_particles(c))) return rc;
-  if ((rc = launch_reorder_particles(c))) return rc;  // P[0] -> P[1]
-  DEM_CUDA_TRY(c, cudaMemcpyAsync(c->pblock[0], c->pblock[1], particle_block_bytes(c), cudaMemcpyDeviceToDevice,
-                                  c->stream));
-  c->pcur = 0;
+  if ((rc = launch_reorder_particles(c))) return rc;  // one system: P[0] -> P[1], swapped
+  if (c->pcur != 0) {                                   // (several systems reorder in place)
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(c->pblock[0], c->pblock[1], particle_block_bytes(c), cudaMemcpyDeviceToDevice,
+                                    c->stream));
+    c->pcur = 0;
+  }
   if ((rc = launch_count_sphere(c))) return rc;
   if ((rc = scan_exclusive_u32(c, c->pcnt, c->own_off[1], n))) return rc;
   k_graph_total<<<1, 1, 0, c->stream>>>(c->own_off[1], n, c->d_gs);

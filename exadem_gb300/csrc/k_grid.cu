@@ -21,13 +21,13 @@ __global__ void k_bin(PArrays P, uint64_t n, SysView sv, uint32_t* __restrict__ 
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const int sys = sv.of(s);
+  if (!sv.triggered(sys)) return;  // kept in place (k_sys_block counts it)
   const GridDev& g = sv.g[sys];
-  const bool wrap = sv.triggered(sys);  // other systems keep their positions (clamped to edge cells)
   int k[3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     double x = P.f[RX + d][s];
-    if (g.periodic[d] && wrap) {
+    if (g.periodic[d]) {
       const double lo = g.lo[d], hi = g.hi[d], Ld = g.L[d];
       if (x < lo) {
         x = x + Ld;
@@ -51,9 +51,10 @@ __global__ void k_bin(PArrays P, uint64_t n, SysView sv, uint32_t* __restrict__ 
 }
 
 __global__ void k_scatter(const uint32_t* __restrict__ cell_tmp, uint64_t n, const uint32_t* __restrict__ cell_start,
-                          uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm) {
+                          uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm, SysView sv) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
+  if (!sv.triggered(sv.of(s))) return;  // slot kept (k_perm_keep)
   const uint32_t c = cell_tmp[s];
   const uint32_t pos = cell_start[c] + atomicAdd(&cursor[c], 1u);
   perm[pos] = (uint32_t)s;
@@ -87,17 +88,26 @@ __global__ void k_cell_sort(uint64_t ncell, const uint32_t* __restrict__ cell_st
   }
 }
 
+// A system rebuilt without its own trigger is one block of its particle count
+// in its first cell, so that every system's cells start at its first slot.
+__global__ void k_sys_block(SysView sv, uint32_t* __restrict__ cell_cnt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sv.nsys || sv.triggered(k)) return;
+  atomicAdd(&cell_cnt[sv.coff[k]], (uint32_t)(sv.pfirst[k + 1] - sv.pfirst[k]));
+}
+
 __global__ void k_reorder(PArrays src, PArrays dst, uint64_t n, const uint32_t* __restrict__ perm,
                           const uint32_t* __restrict__ cell_tmp, uint32_t* __restrict__ cell_of, SysView sv,
                           float* __restrict__ xr, float* __restrict__ yr, float* __restrict__ zr,
                           float* __restrict__ rf) {
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
+  const int sys = sv.of(t);  // the slot stays in the particle's system range
+  if (!sv.triggered(sys)) return;  // kept in place
   const uint32_t o = perm[t];
 #pragma unroll
   for (int k = 0; k < BX; k++) dst.f[k][t] = src.f[k][o];
   // FP32 coordinates relative to the origin of the particle's cell, for the FP32 broad phase
-  const int sys = sv.of(t);  // the slot stays in the particle's system range
   const GridDev& g = sv.g[sys];
   const uint32_t c = cell_tmp[o] - sv.coff[sys];
   const uint32_t kx = c % (uint32_t)g.dims[0], ky = (c / (uint32_t)g.dims[0]) % (uint32_t)g.dims[1],
@@ -106,16 +116,26 @@ __global__ void k_reorder(PArrays src, PArrays dst, uint64_t n, const uint32_t* 
   yr[t] = (float)(src.f[RY][o] - (g.lo[1] + (double)ky * g.csz[1]));
   zr[t] = (float)(src.f[RZ][o] - (g.lo[2] + (double)kz * g.csz[2]));
   rf[t] = (float)src.f[RAD][o];
-  // backup_r: positions at this rebuild, for the displacement trigger (systems
-  // rebuilt without their own trigger keep their backups)
-  const bool own = sv.triggered(sys);
-  dst.f[BX][t] = own ? src.f[RX][o] : src.f[BX][o];
-  dst.f[BY][t] = own ? src.f[RY][o] : src.f[BY][o];
-  dst.f[BZ][t] = own ? src.f[RZ][o] : src.f[BZ][o];
+  // backup_r: positions at this rebuild, for the displacement trigger
+  dst.f[BX][t] = src.f[RX][o];
+  dst.f[BY][t] = src.f[RY][o];
+  dst.f[BZ][t] = src.f[RZ][o];
   dst.id[t] = src.id[o];
   dst.type[t] = src.type[o];
   dst.group[t] = src.group[o];
   cell_of[t] = cell_tmp[o];
+}
+
+// several systems: the reordered slots of the triggered systems back into the
+// current buffer (the others were not touched, so the buffers do not swap)
+__global__ void k_copy_back(PArrays from, PArrays to, uint64_t n, SysView sv) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n || !sv.triggered(sv.of(t))) return;
+#pragma unroll
+  for (int k = 0; k < NPF; k++) to.f[k][t] = from.f[k][t];
+  to.id[t] = from.id[t];
+  to.type[t] = from.type[t];
+  to.group[t] = from.group[t];
 }
 
 // Systems rebuilt without their own trigger keep every particle in its slot
@@ -142,12 +162,14 @@ int launch_bin_particles(dem_ctx* c) {
   ProfScope ps(c, K_BIN, n ? 2 : 1);
   k_zero_u32<<<grid_for(nc + 1, 256), 256, 0, st>>>(c->cell_cnt, nc + 1);
   if (n) k_bin<<<grid_for(n, 256), 256, 0, st>>>(c->P[c->pcur], n, c->sysview(), c->cell_tmp, c->cell_cnt);
+  if (c->nsys > 1) k_sys_block<<<(c->nsys + 255) / 256, 256, 0, st>>>(c->sysview(), c->cell_cnt);
   }
   rc = scan_exclusive_u32(c, c->cell_cnt, c->cell_start, nc);
   if (rc) return rc;
   ProfScope ps(c, K_BIN, n ? 3 : 2);
   k_zero_u32<<<grid_for(nc + 1, 256), 256, 0, st>>>(c->cell_cnt, nc + 1);
-  if (n) k_scatter<<<grid_for(n, 256), 256, 0, st>>>(c->cell_tmp, n, c->cell_start, c->cell_cnt, c->perm);
+  if (n)
+    k_scatter<<<grid_for(n, 256), 256, 0, st>>>(c->cell_tmp, n, c->cell_start, c->cell_cnt, c->perm, c->sysview());
   k_cell_sort<<<grid_for(nc, 256), 256, 0, st>>>(nc, c->cell_start, c->P[c->pcur].id, c->perm, c->sysview());
   if (c->nsys > 1 && n) k_perm_keep<<<grid_for(n, 256), 256, 0, st>>>(c->perm, n, c->sysview());
   DEM_CUDA_TRY(c, cudaGetLastError());
@@ -155,16 +177,20 @@ int launch_bin_particles(dem_ctx* c) {
 }
 
 // Gathers all particle fields into the other buffer in cell order and swaps.
+// Several systems: only the triggered systems' slots are gathered, then copied
+// back, and the buffers do not swap.
 int launch_reorder_particles(dem_ctx* c) {
   const uint64_t n = c->n;
-  ProfScope ps(c, K_REORDER, n ? 1 : 0);
+  const bool part = c->nsys > 1;
+  ProfScope ps(c, K_REORDER, n ? (part ? 2 : 1) : 0);
   if (n) {
     k_reorder<<<grid_for(n, 256), 256, 0, c->stream>>>(c->P[c->pcur], c->P[1 - c->pcur], n, c->perm, c->cell_tmp,
                                                         c->cell_of, c->sysview(), c->crel[0], c->crel[1], c->crel[2],
                                                         c->crel[3]);
+    if (part) k_copy_back<<<grid_for(n, 256), 256, 0, c->stream>>>(c->P[1 - c->pcur], c->P[c->pcur], n, c->sysview());
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
-  c->pcur = 1 - c->pcur;
+  if (!part) c->pcur = 1 - c->pcur;
   return DEM_OK;
 }
 }  // namespace dem

@@ -142,8 +142,22 @@ __global__ void k_poly_fused_prolog(PolyArgs a, double delta_t, double half_delt
     const float q2 = fmaxf(fmaxf(qn.x * qn.x + qn.y * qn.y + qn.z * qn.z + qn.w * qn.w,
                                  qb.x * qb.x + qb.y * qb.y + qb.z * qb.z + qb.w * qb.w),
                            1.f);
+    bool k_skip_vertices = false;
     const float pabs = (float)(fabs(p.x) + fabs(p.y) + fabs(p.z));
-    for (int k = 0; k < sh.nv && !over; k++) {
+    // Rigid-body bound on every vertex displacement: with F(q) = q v q* in the
+    // form v + 2w (u x v) + 2 u x (u x v), |dF/dq| <= 6 |q| |v| |dq|, so
+    // |F(q) v0' - F(q_b) v0'| <= 6 max(|q|, |q_b|) |q - q_b| |v0'|.  The FP32
+    // |q - q_b| carries at most 4u max|q| of rounding (both quaternions rounded
+    // to FP32), the other terms a relative 1e-5; below thr (1 - 1e-4) no vertex
+    // can reach the threshold and the per-vertex test is skipped.
+    {
+      const float qm = sqrtf(q2);
+      const float dqx = qn.x - qb.x, dqy = qn.y - qb.y, dqz = qn.z - qb.z, dqw = qn.w - qb.w;
+      const float dq = sqrtf(dqx * dqx + dqy * dqy + dqz * dqz + dqw * dqw) + 8.f * 5.9604645e-08f * qm;
+      const float bound = (flen(dp) + 6.f * qm * dq * hf * (float)sh.maxv) * 1.00001f + 4.440892e-16f * pabs;
+      if (bound < thr * 0.9999f) over = false, k_skip_vertices = true;
+    }
+    for (int k = 0; k < sh.nv && !over && !k_skip_vertices; k++) {
       const F3 v0 = f3(sh.vf[3 * k], sh.vf[3 * k + 1], sh.vf[3 * k + 2]) * hf;
       const int d = decide_displ(dp, qn, qb, v0, q2, pabs, thr);
       if (d == DEC_UNDECIDED) {
