@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--plain", action="store_true", help="plain FP64 path (no FP32 screening)")
     ap.add_argument("--no-graph", action="store_true", help="fused step launched from the host, no CUDA graph")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (cell size, launch shapes)")
+    ap.add_argument("--mul-mode", type=int, default=None, choices=[0, 1, 2, 3],
+                    help="integration multiplies on the integer pipe: 0 none, 1 rotations, 2 the rest, 3 all "
+                         "(default: the autotuner's choice, else 1)")
     ap.add_argument("--learned", action="store_true",
                     help="polyhedra: harvest candidate pairs, train the MLP, time with learned sizing "
                          "and without it")
@@ -367,6 +370,8 @@ def run_native(args, rank, world, local, dist):
     if not args.plain and not args.no_tune and args.workload in ("spheres", "drums"):
         # cell size and launch shapes; the skin only where it cannot change a bit
         tune = s.autotune(steps_per_trial=3, skin_policy=1)
+    if args.mul_mode is not None:
+        s.set_mul_mode(args.mul_mode)
     s.step(args.warmup)
     torch.cuda.synchronize()
     s.reset_kernel_stats()
@@ -427,6 +432,7 @@ def run_native(args, rank, world, local, dist):
     shares = {k: round(v["total_ms"] / max(sum(x["total_ms"] for x in prof.values()), 1e-9), 4)
               for k, v in prof.items() if v["total_ms"] > 0}
     state = s.simulation_state()
+    mul_mode = s.mul_mode()
     s.close()
 
     # end to end through the C ABI from pinned host buffers
@@ -477,6 +483,7 @@ def run_native(args, rank, world, local, dist):
                            "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division"
                            + (", whole step replayed as one CUDA graph" if getattr(w.params, "graph_step", 0) else "")
                            + (f", {w.info['systems']} systems in one context" if is_batch(w) else ""),
+                   "mul_mode": None if args.plain else mul_mode,
                    "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "inputs": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in w.info.items()
@@ -485,7 +492,7 @@ def run_native(args, rank, world, local, dist):
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni,
                      "interactions": ni, "avg_launch_ms": t_contact * 1e3,
-                     "note": "FP64-ALU bound in practice; see DESIGN roofline"},
+                     "note": "FP64-pipe bound in practice (per-kernel rooflines under profiles/)"},
         "autotune": ({k: (round(v, 6) if isinstance(v, float) else v) for k, v in tune.items()}
                      if tune else None),
         "learned": learned,

@@ -81,7 +81,8 @@ class SystemDesc(C.Structure):
 
 class TuneResult(C.Structure):
     _fields_ = [("rcut_inc", D), ("cell_size", D), ("block", C.c_int32), ("contact_blocks_per_sm", C.c_int32),
-                ("ms_per_step", D), ("ms_per_step_before", D), ("trials", C.c_int32), ("vmax", C.c_float)]
+                ("ms_per_step", D), ("ms_per_step_before", D), ("trials", C.c_int32), ("vmax", C.c_float),
+                ("mul_mode", C.c_int32)]
 
 
 class InteractionList(C.Structure):
@@ -163,6 +164,8 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_set_systems", [_CTX, C.POINTER(SystemDesc), C.c_int])
     _sig(lib, "dem_set_graph_capacity", [_CTX, C.c_uint64])
     _sig(lib, "dem_autotune", [_CTX, C.c_int, C.c_int, C.POINTER(TuneResult)])
+    _sig(lib, "dem_set_mul_mode", [_CTX, C.c_int])
+    _sig(lib, "dem_get_mul_mode", [_CTX, C.POINTER(C.c_int)])
     VP = C.c_void_p
     _sig(lib, "dem_mlp_harvest", [_CTX, VP, VP, C.c_uint64, PU64, PU64])
     _sig(lib, "dem_mlp_init", [_CTX, C.c_uint64, C.POINTER(C.c_float)])
@@ -184,6 +187,8 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_simulation_state_noalloc", [C.POINTER(Particles), PD, C.c_void_p])
     _sig(lib, "dem_selftest_division", [C.c_uint64, C.c_uint64, PU64, PU64])
     _sig(lib, "dem_selftest_poly_decisions", [C.c_uint64, C.c_uint64, PU64])
+    _sig(lib, "dem_selftest_emu_mul", [C.c_uint64, C.c_uint64, PU64])
+    _sig(lib, "dem_probe_mul_rates", [C.c_int, C.POINTER(C.c_double)])
 
 
 # Symbols declared in include/dem_hotpath.h, dem_workloads.h, dem_selftest.h and dem_learned.h.
@@ -194,9 +199,9 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
             "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
-            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_set_shapes", "dem_compute_vertices",
+            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_selftest_emu_mul", "dem_probe_mul_rates", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
-            "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune", "dem_mlp_harvest",
+            "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune", "dem_set_mul_mode", "dem_get_mul_mode", "dem_mlp_harvest",
             "dem_mlp_init", "dem_mlp_set_params", "dem_mlp_get_params", "dem_mlp_forward", "dem_mlp_loss_grad",
             "dem_mlp_train", "dem_learned_stats"]
 

@@ -984,6 +984,19 @@ int dem_set_graph_capacity(dem_ctx* c, uint64_t capacity) {
   return DEM_OK;
 }
 
+int dem_set_mul_mode(dem_ctx* c, int mode) {
+  if (!c || mode < 0 || mode > 3) return DEM_ERR_INVALID_ARG;
+  c->mul_mode = mode;
+  c->gen++;  // a captured step holds the kernel instance of the old mode
+  return DEM_OK;
+}
+
+int dem_get_mul_mode(dem_ctx* c, int* mode) {
+  if (!c || !mode) return DEM_ERR_INVALID_ARG;
+  *mode = c->mul_mode;
+  return DEM_OK;
+}
+
 int dem_rebuild_count(dem_ctx* c, uint64_t* out) {
   if (!c || !out) return DEM_ERR_INVALID_ARG;
   *out = c->rebuilds;

@@ -51,7 +51,7 @@ struct Saved {
   uint64_t ni, rebuilds;
   bool have_list, hist_valid;
   dem_params prm;
-  int tune_block, tune_contact_bps;
+  int tune_block, tune_contact_bps, mul_mode;
 };
 
 int save_state(dem_ctx* c, Saved& s) {
@@ -64,6 +64,7 @@ int save_state(dem_ctx* c, Saved& s) {
   s.prm = c->prm;
   s.tune_block = c->tune_block;
   s.tune_contact_bps = c->tune_contact_bps;
+  s.mul_mode = c->mul_mode;
   const size_t bytes = pblock_bytes(c) + (c->n + 1) * 4 + c->ni * 72 + 1024;
   DEM_CUDA_TRY(c, cudaMalloc(&s.dev, bytes));
   char* p = static_cast<char*>(s.dev);
@@ -96,6 +97,7 @@ int restore_state(dem_ctx* c, const Saved& s) {
   c->hist_valid = s.hist_valid;
   c->tune_block = s.tune_block;
   c->tune_contact_bps = s.tune_contact_bps;
+  c->mul_mode = s.mul_mode;
   if (std::memcmp(&c->prm, &s.prm, sizeof(dem_params))) {
     c->prm = s.prm;
     int rc = ext_setup_grid(c);
@@ -200,11 +202,12 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
   int trials = 0;
 
   // one trial: forced rebuild (timed), then steps (timed); the state is restored after
-  auto trial = [&](double skin, double cell, int block, int bps, double* cost) -> int {
+  auto trial = [&](double skin, double cell, int block, int bps, int mode, double* cost) -> int {
     c->prm.rcut_inc = skin;
     c->prm.cell_size = cell;
     c->tune_block = block;
     c->tune_contact_bps = bps;
+    c->mul_mode = mode;
     int r = ext_setup_grid(c);
     if (r) return r;
     tm.start();
@@ -224,13 +227,14 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
 
   double best = 1e300, before = 0;
   double best_skin = skin0, best_cell = c->prm.cell_size;
-  if ((rc = trial(skin0, c->prm.cell_size, c->tune_block, c->tune_contact_bps, &before))) return rc;
+  const int mode0 = c->mul_mode;
+  if ((rc = trial(skin0, c->prm.cell_size, c->tune_block, c->tune_contact_bps, mode0, &before))) return rc;
   best = before;
   for (double sk : skins)
     for (double f : cell_factors) {
       const double cell = f * (nd0 + sk);
       double cost;
-      if ((rc = trial(sk, cell, c->tune_block, c->tune_contact_bps, &cost))) return rc;
+      if ((rc = trial(sk, cell, c->tune_block, c->tune_contact_bps, mode0, &cost))) return rc;
       if (cost < best) {
         best = cost;
         best_skin = sk;
@@ -241,19 +245,31 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
   for (int block : {64, 128, 256})
     for (int bps : {4, 8, 16}) {
       double cost;
-      if ((rc = trial(best_skin, best_cell, block, bps, &cost))) return rc;
+      if ((rc = trial(best_skin, best_cell, block, bps, mode0, &cost))) return rc;
       if (cost < best) {
         best = cost;
         best_block = block;
         best_bps = bps;
       }
     }
+  // multiply placement of the integration kernels (same bits in every mode)
+  int best_mode = mode0;
+  for (int mode : {0, 1, 2, 3}) {
+    if (mode == mode0) continue;
+    double cost;
+    if ((rc = trial(best_skin, best_cell, best_block, best_bps, mode, &cost))) return rc;
+    if (cost < best) {
+      best = cost;
+      best_mode = mode;
+    }
+  }
   cudaFree(base.dev);
 
   // apply: launch shapes and cell size keep the current list (they take effect at the
   // next rebuild); a new skin rebuilds now (no effect on any result without cohesion)
   c->tune_block = best_block;
   c->tune_contact_bps = best_bps;
+  c->mul_mode = best_mode;
   const bool skin_changed = best_skin != skin0;
   c->prm.cell_size = best_cell;
   c->prm.rcut_inc = best_skin;
@@ -270,5 +286,6 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
   out->ms_per_step_before = before;
   out->trials = trials;
   out->vmax = vmax;
+  out->mul_mode = best_mode;
   return DEM_OK;
 }

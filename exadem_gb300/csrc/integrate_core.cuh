@@ -8,11 +8,70 @@
 //           angular_velocity.hpp:27-33.
 // Quaternion arithmetic restates onika's operators following exaDEM's quat type
 // (src/shape/include/exaDEM/type/quat.hpp:79-96,233-242).
+//
+// Multiply placement (Mode, fused kernels only).  Every multiply below goes
+// through a policy: MulFP64 is the FP64 pipe, MulInt the integer-pipe IEEE
+// multiply of emu64.cuh.  Both return the same bits, so the mode changes only
+// which pipe does the work.  Mode bit 0 places the rotation multiplies
+// (quaternion rotations, quaternion derivative, normalisation, Euler terms),
+// bit 1 the rest (Verlet pushes, gravity, quotient estimates).  Additions,
+// the FMAs of div_rn, the square root and the division stay on the FP64 pipe,
+// so with both bits set the two pipes share the work roughly evenly.
 #pragma once
+#include <type_traits>
+
 #include "dem_ctx.cuh"
+#include "emu64.cuh"
 #include "math_exact.cuh"
 
 namespace dem {
+
+// Multiply policies.  MulFP64: the FP64 pipe.  MulInt: the branch-free
+// integer-pipe IEEE multiply; failed() reports an operand outside its fast
+// path (subnormal, infinite, NaN, out-of-range product), after which the
+// caller recomputes its block of arithmetic with MulFP64.
+struct MulFP64 {
+  __device__ __forceinline__ double mul(double a, double b) const { return __dmul_rn(a, b); }
+  __device__ __forceinline__ double twice(double a) const { return __dmul_rn(a, 2.0); }
+  __device__ __forceinline__ double half(double a) const { return __dmul_rn(a, 0.5); }
+  __device__ __forceinline__ double neghalf(double a) const { return __dmul_rn(a, -0.5); }
+  __device__ __forceinline__ bool failed() const { return false; }
+};
+struct MulInt {
+  bool bad = false;
+  __device__ __forceinline__ double mul(double a, double b) { return emu_dmul_nb(a, b, bad); }
+  __device__ __forceinline__ double twice(double a) { return emu_mul2_nb(a, bad); }
+  __device__ __forceinline__ double half(double a) { return emu_mulhalf_nb(a, bad); }
+  __device__ __forceinline__ double neghalf(double a) { return emu_mulnhalf_nb(a, bad); }
+  __device__ __forceinline__ bool failed() const { return bad; }
+};
+template <int Mode>
+using RotMul = typename std::conditional<(Mode & 1) != 0, MulInt, MulFP64>::type;
+template <int Mode>
+using LinMul = typename std::conditional<(Mode & 2) != 0, MulInt, MulFP64>::type;
+
+// the kernel instance compiled for a multiply placement
+template <class F>
+F by_mode(int mode, F m0, F m1, F m2, F m3) {
+  switch (mode & 3) {
+    case 1: return m1;
+    case 2: return m2;
+    case 3: return m3;
+    default: return m0;
+  }
+}
+
+// div_rn (math_exact.cuh) with its quotient estimate a*y through M
+template <class M>
+__device__ __forceinline__ double div_rn_m(M& mm, double a, double b, double y) {
+  if (a == 0.0) return mm.mul(a, y);
+  if (exp_in_safe_range(a) && exp_in_safe_range(b)) {
+    const double q = mm.mul(a, y);
+    const double r = fma(-q, b, a);
+    return fma(r, y, q);
+  }
+  return a / b;
+}
 
 struct Q4 {
   double w, x, y, z;
@@ -26,72 +85,142 @@ __device__ __forceinline__ V3 qrotate(Q4 q, V3 v) {
   return v + uv + uuv;
 }
 
+// v rotated by q (q v q*), in the form v + 2w (u x v) + 2 u x (u x v), the
+// operation order of qrotate, multiplies through M
+template <class M>
+__device__ __forceinline__ V3 qrotate_m(M& mm, Q4 q, V3 v) {
+  V3 uv = mk(mm.mul(q.y, v.z) - mm.mul(q.z, v.y), mm.mul(q.z, v.x) - mm.mul(q.x, v.z),
+             mm.mul(q.x, v.y) - mm.mul(q.y, v.x));
+  V3 uuv = mk(mm.mul(q.y, uv.z) - mm.mul(q.z, uv.y), mm.mul(q.z, uv.x) - mm.mul(q.x, uv.z),
+              mm.mul(q.x, uv.y) - mm.mul(q.y, uv.x));
+  const double w2 = mm.twice(q.w);
+  uv = mk(mm.mul(uv.x, w2), mm.mul(uv.y, w2), mm.mul(uv.z, w2));
+  uuv = mk(mm.twice(uuv.x), mm.twice(uuv.y), mm.twice(uuv.z));
+  return mk(v.x + uv.x + uuv.x, v.y + uv.y + uuv.y, v.z + uv.z + uuv.z);
+}
+
 // x += v dt + a dt^2/2; v += a dt/2; Q <- normalize(Q + dot(Q, w) dt); w += dt/2 arot
-__device__ __forceinline__ void prolog_one(const PArrays& P, uint64_t s, double delta_t, double half_delta_t,
-                                           double delta_t2_2) {
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    const double v = P.f[VX + d][s], a = P.f[FX + d][s];
-    P.f[RX + d][s] = P.f[RX + d][s] + (v * delta_t + a * delta_t2_2);
-    P.f[VX + d][s] = v + a * half_delta_t;
-  }
-  Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
-  const V3 om = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+struct ProlState {
+  V3 r, v, a, w, arot;
+  Q4 q;
+};
+template <class R, class L>
+__device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& in, double delta_t,
+                                                 double half_delta_t, double delta_t2_2) {
+  ProlState o = in;
+  o.r = mk(in.r.x + (lm.mul(in.v.x, delta_t) + lm.mul(in.a.x, delta_t2_2)),
+           in.r.y + (lm.mul(in.v.y, delta_t) + lm.mul(in.a.y, delta_t2_2)),
+           in.r.z + (lm.mul(in.v.z, delta_t) + lm.mul(in.a.z, delta_t2_2)));
+  o.v = mk(in.v.x + lm.mul(in.a.x, half_delta_t), in.v.y + lm.mul(in.a.y, half_delta_t),
+           in.v.z + lm.mul(in.a.z, half_delta_t));
+  Q4 Q = in.q;
+  const V3 om = in.w;
   Q4 d;
-  d.x = 0.5 * (om.y * Q.z - om.z * Q.y + om.x * Q.w);
-  d.y = 0.5 * (om.z * Q.x - om.x * Q.z + om.y * Q.w);
-  d.z = 0.5 * (om.x * Q.y - om.y * Q.x + om.z * Q.w);
-  d.w = -0.5 * (om.x * Q.x + om.y * Q.y + om.z * Q.z);
-  Q.w = Q.w + d.w * delta_t;
-  Q.x = Q.x + d.x * delta_t;
-  Q.y = Q.y + d.y * delta_t;
-  Q.z = Q.z + d.z * delta_t;
-  const double norm2 = Q.w * Q.w + (Q.x * Q.x + Q.y * Q.y + Q.z * Q.z);
+  d.x = rm.half(rm.mul(om.y, Q.z) - rm.mul(om.z, Q.y) + rm.mul(om.x, Q.w));
+  d.y = rm.half(rm.mul(om.z, Q.x) - rm.mul(om.x, Q.z) + rm.mul(om.y, Q.w));
+  d.z = rm.half(rm.mul(om.x, Q.y) - rm.mul(om.y, Q.x) + rm.mul(om.z, Q.w));
+  d.w = rm.neghalf(rm.mul(om.x, Q.x) + rm.mul(om.y, Q.y) + rm.mul(om.z, Q.z));
+  Q.w = Q.w + rm.mul(d.w, delta_t);
+  Q.x = Q.x + rm.mul(d.x, delta_t);
+  Q.y = Q.y + rm.mul(d.y, delta_t);
+  Q.z = Q.z + rm.mul(d.z, delta_t);
+  const double norm2 = rm.mul(Q.w, Q.w) + (rm.mul(Q.x, Q.x) + rm.mul(Q.y, Q.y) + rm.mul(Q.z, Q.z));
   if (norm2 <= 1e-9) {
     Q = {1.0, 0.0, 0.0, 0.0};
   } else {
     const double inv = 1.0 / sqrt(norm2);
-    Q = {Q.w * inv, Q.x * inv, Q.y * inv, Q.z * inv};
+    Q = {rm.mul(Q.w, inv), rm.mul(Q.x, inv), rm.mul(Q.y, inv), rm.mul(Q.z, inv)};
   }
-  P.f[QW][s] = Q.w;
-  P.f[QX][s] = Q.x;
-  P.f[QY][s] = Q.y;
-  P.f[QZ][s] = Q.z;
-  P.f[WX][s] = om.x + half_delta_t * P.f[AX][s];
-  P.f[WY][s] = om.y + half_delta_t * P.f[AY][s];
-  P.f[WZ][s] = om.z + half_delta_t * P.f[AZ][s];
+  o.q = Q;
+  o.w = mk(om.x + lm.mul(half_delta_t, in.arot.x), om.y + lm.mul(half_delta_t, in.arot.y),
+           om.z + lm.mul(half_delta_t, in.arot.z));
+  return o;
+}
+
+template <int Mode = 0>
+__device__ __forceinline__ void prolog_one(const PArrays& P, uint64_t s, double delta_t, double half_delta_t,
+                                           double delta_t2_2) {
+  ProlState in;
+  in.r = mk(P.f[RX][s], P.f[RY][s], P.f[RZ][s]);
+  in.v = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
+  in.a = mk(P.f[FX][s], P.f[FY][s], P.f[FZ][s]);
+  in.q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+  in.w = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+  in.arot = mk(P.f[AX][s], P.f[AY][s], P.f[AZ][s]);
+  RotMul<Mode> rm;
+  LinMul<Mode> lm;
+  ProlState o = prolog_math(rm, lm, in, delta_t, half_delta_t, delta_t2_2);
+  if (rm.failed() || lm.failed()) {
+    MulFP64 n;
+    o = prolog_math(n, n, in, delta_t, half_delta_t, delta_t2_2);
+  }
+  P.f[RX][s] = o.r.x;
+  P.f[RY][s] = o.r.y;
+  P.f[RZ][s] = o.r.z;
+  P.f[VX][s] = o.v.x;
+  P.f[VY][s] = o.v.y;
+  P.f[VZ][s] = o.v.z;
+  P.f[QW][s] = o.q.w;
+  P.f[QX][s] = o.q.x;
+  P.f[QY][s] = o.q.y;
+  P.f[QZ][s] = o.q.z;
+  P.f[WX][s] = o.w.x;
+  P.f[WY][s] = o.w.y;
+  P.f[WZ][s] = o.w.z;
 }
 
 // arot from the torque (Euler equations in the body frame), w += arot dt/2, v += a dt/2.
 // a is the acceleration (f after force_to_accel).  FastDiv: divisions by the
 // inertia through the precomputed reciprocals (div_rn, exact).
-template <bool FastDiv>
-__device__ __forceinline__ void epilog_one(const PArrays& P, uint64_t s, double half_delta_t, V3 a, V3 mom) {
-  const Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+struct EpiOut {
+  V3 arot, w, v;
+};
+template <bool FastDiv, class R, class L>
+__device__ __forceinline__ EpiOut epilog_math(R& rm, L& lm, Q4 Q, V3 vrot, V3 I, V3 II, V3 vel, V3 a, V3 mom,
+                                              double half_delta_t) {
   const Q4 Qinv = {Q.w, -Q.x, -Q.y, -Q.z};
-  const V3 vrot = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
-  const V3 I = mk(P.f[IX][s], P.f[IY][s], P.f[IZ][s]);
-  const V3 omega = qrotate(Qinv, vrot);
-  const V3 M = qrotate(Qinv, mom);
-  const double nx = M.x - (I.z - I.y) * omega.y * omega.z;
-  const double ny = M.y - (I.x - I.z) * omega.z * omega.x;
-  const double nz = M.z - (I.y - I.x) * omega.x * omega.y;
+  const V3 omega = qrotate_m(rm, Qinv, vrot);
+  const V3 M = qrotate_m(rm, Qinv, mom);
+  const double nx = M.x - rm.mul(rm.mul(I.z - I.y, omega.y), omega.z);
+  const double ny = M.y - rm.mul(rm.mul(I.x - I.z, omega.z), omega.x);
+  const double nz = M.z - rm.mul(rm.mul(I.y - I.x, omega.x), omega.y);
   V3 domega;
   if (FastDiv) {
-    domega = mk(div_rn(nx, I.x, P.f[IIX][s]), div_rn(ny, I.y, P.f[IIY][s]), div_rn(nz, I.z, P.f[IIZ][s]));
+    domega = mk(div_rn_m(lm, nx, I.x, II.x), div_rn_m(lm, ny, I.y, II.y), div_rn_m(lm, nz, I.z, II.z));
   } else {
     domega = mk(nx / I.x, ny / I.y, nz / I.z);
   }
-  const V3 arot = qrotate(Q, domega);
-  P.f[AX][s] = arot.x;
-  P.f[AY][s] = arot.y;
-  P.f[AZ][s] = arot.z;
-  P.f[WX][s] = vrot.x + arot.x * half_delta_t;
-  P.f[WY][s] = vrot.y + arot.y * half_delta_t;
-  P.f[WZ][s] = vrot.z + arot.z * half_delta_t;
-  P.f[VX][s] = P.f[VX][s] + a.x * half_delta_t;
-  P.f[VY][s] = P.f[VY][s] + a.y * half_delta_t;
-  P.f[VZ][s] = P.f[VZ][s] + a.z * half_delta_t;
+  EpiOut o;
+  o.arot = qrotate_m(rm, Q, domega);
+  o.w = mk(vrot.x + lm.mul(o.arot.x, half_delta_t), vrot.y + lm.mul(o.arot.y, half_delta_t),
+           vrot.z + lm.mul(o.arot.z, half_delta_t));
+  o.v = mk(vel.x + lm.mul(a.x, half_delta_t), vel.y + lm.mul(a.y, half_delta_t), vel.z + lm.mul(a.z, half_delta_t));
+  return o;
+}
+
+template <bool FastDiv, int Mode = 0>
+__device__ __forceinline__ void epilog_one(const PArrays& P, uint64_t s, double half_delta_t, V3 a, V3 mom) {
+  const Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+  const V3 vrot = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+  const V3 I = mk(P.f[IX][s], P.f[IY][s], P.f[IZ][s]);
+  const V3 II = FastDiv ? mk(P.f[IIX][s], P.f[IIY][s], P.f[IIZ][s]) : mk(0.0, 0.0, 0.0);
+  const V3 vel = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
+  RotMul<Mode> rm;
+  LinMul<Mode> lm;
+  EpiOut o = epilog_math<FastDiv>(rm, lm, Q, vrot, I, II, vel, a, mom, half_delta_t);
+  if (rm.failed() || lm.failed()) {
+    MulFP64 n;
+    o = epilog_math<FastDiv>(n, n, Q, vrot, I, II, vel, a, mom, half_delta_t);
+  }
+  P.f[AX][s] = o.arot.x;
+  P.f[AY][s] = o.arot.y;
+  P.f[AZ][s] = o.arot.z;
+  P.f[WX][s] = o.w.x;
+  P.f[WY][s] = o.w.y;
+  P.f[WZ][s] = o.w.z;
+  P.f[VX][s] = o.v.x;
+  P.f[VY][s] = o.v.y;
+  P.f[VZ][s] = o.v.z;
 }
 
 }  // namespace dem

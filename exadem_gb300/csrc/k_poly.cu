@@ -125,12 +125,13 @@ __global__ void k_poly_vertices(PolyArgs a, double thr2, unsigned long long* fla
 // FP32 per vertex (decide_displ); an undecided vertex is recomputed in FP64
 // exactly as the reference does (world vertex minus the stored backup vertex).
 // No vertex is written.
+template <int Mode>
 __global__ void k_poly_fused_prolog(PolyArgs a, double delta_t, double half_delta_t, double delta_t2_2,
                                     double thr2, float thr, unsigned long long* flag) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;
   if (s < a.n) {
-    prolog_one(a.P, s, delta_t, half_delta_t, delta_t2_2);
+    prolog_one<Mode>(a.P, s, delta_t, half_delta_t, delta_t2_2);
     const ShapeDev& sh = a.shapes[a.P.type[s]];
     const double h = a.P.f[HOM][s];
     const V3 p = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
@@ -1230,8 +1231,9 @@ int launch_poly_fused_prolog(dem_ctx* c) {
   const PolyArgs a = make_pargs(c);
   const double dt = c->prm.dt;
   const double md = c->prm.rcut_inc * 0.5;
-  k_poly_fused_prolog<<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, dt, dt * 0.5, dt * dt * 0.5, md * md, (float)md,
-                                                                 c->d_scalars);
+  const auto kern = by_mode(c->mul_mode, k_poly_fused_prolog<0>, k_poly_fused_prolog<1>, k_poly_fused_prolog<2>,
+                            k_poly_fused_prolog<3>);
+  kern<<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, dt, dt * 0.5, dt * dt * 0.5, md * md, (float)md, c->d_scalars);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

@@ -1,0 +1,144 @@
+// k_selftest_emu.cu -- GPU self-test of the integer-pipe binary64 multiply
+// (emu64.cuh) against the hardware multiply, and a probe of the multiply
+// rates of the FP64 pipe, the integer pipe, and both together.
+#include "../../include/dem_selftest.h"
+#include "dem_ctx.cuh"
+#include "emu64.cuh"
+
+namespace {
+__device__ __forceinline__ uint64_t mix(uint64_t x) {  // splitmix64 finaliser
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+// operand classes as in the host check: typical magnitudes, short
+// significands (exact products and ties), the whole normal range, boundary
+// exponents, zeros / subnormals, infinities / NaNs, all-ones significands
+__device__ double draw(uint64_t h1, uint64_t h2) {
+  const uint64_t sign = (h1 & 1) << 63;
+  const int cls = (int)((h1 >> 1) % 16);
+  uint64_t frac = h2 & 0xfffffffffffffull;
+  const uint64_t r = h1 >> 8;
+  uint64_t e;
+  if (cls < 7) {
+    e = 1023 - 60 + (r % 121);
+  } else if (cls < 10) {
+    const int keep = (int)(r % 12);
+    frac &= ~((1ull << (52 - keep)) - 1);
+    e = 1023 - 30 + ((r >> 8) % 61);
+  } else if (cls < 12) {
+    e = 1 + (r % 2046);
+  } else if (cls == 12) {
+    e = (r & 1) ? 1 + ((r >> 1) % 40) : 2046 - ((r >> 1) % 40);
+  } else if (cls == 13) {
+    e = 0;
+    if (r & 1) frac = 0;
+  } else if (cls == 14) {
+    e = 2047;
+    if (r & 1) frac = 0;
+  } else {
+    frac = (r & 1) ? 0xfffffffffffffull : 0;
+    e = 1023 - 8 + ((r >> 1) % 17);
+  }
+  return __longlong_as_double((long long)(sign | (e << 52) | frac));
+}
+
+__device__ __forceinline__ bool same_bits(double x, double y) {
+  return __double_as_longlong(x) == __double_as_longlong(y) || (x != x && y != y);
+}
+
+__global__ void k_emu_test(uint64_t n, uint64_t seed, unsigned long long* bad) {
+  unsigned long long nbad = 0;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t h = mix(seed ^ (4 * t));
+    const double a = draw(h, mix(h ^ 1)), b = draw(mix(h ^ 2), mix(h ^ 3));
+    nbad += same_bits(dem::emu_dmul(a, b), __dmul_rn(a, b)) ? 0 : 1;
+    nbad += same_bits(dem::emu_mul2(a), __dmul_rn(a, 2.0)) ? 0 : 1;
+    nbad += same_bits(dem::emu_mulhalf(a), __dmul_rn(a, 0.5)) ? 0 : 1;
+    nbad += same_bits(dem::emu_mulnhalf(a), __dmul_rn(a, -0.5)) ? 0 : 1;
+  }
+  atomicAdd(bad, nbad);
+}
+
+// NN chains multiplied on the FP64 pipe and NE chains on the integer pipe,
+// all in the same thread; factors alternate around 1 so values stay normal.
+// The factors are kernel arguments, so no part of the emulated product is
+// folded at compile time; the branch-free form is the one the integration
+// kernels use.
+template <int NN, int NE>
+__global__ void __launch_bounds__(256) k_rate(int iters, double seed, double c1, double c2, double* out) {
+  double xn[NN > 0 ? NN : 1], xe[NE > 0 ? NE : 1];
+  const double base = seed + 1e-3 * (double)(threadIdx.x & 31);
+#pragma unroll
+  for (int k = 0; k < NN; k++) xn[k] = base + k;
+#pragma unroll
+  for (int k = 0; k < NE; k++) xe[k] = base - k;
+  bool bad = false;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int k = 0; k < NN; k++) xn[k] = __dmul_rn(__dmul_rn(xn[k], c1), c2);
+#pragma unroll
+    for (int k = 0; k < NE; k++) xe[k] = dem::emu_dmul_nb(dem::emu_dmul_nb(xe[k], c1, bad), c2, bad);
+  }
+  double s = bad ? -1.0 : 0.0;
+#pragma unroll
+  for (int k = 0; k < NN; k++) s += xn[k];
+#pragma unroll
+  for (int k = 0; k < NE; k++) s += xe[k];
+  out[(uint64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <int NN, int NE>
+int time_rate(int blocks, int iters, double* out, double* gops) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const double c1 = 1.0 + 1.0 / 1048576.0, c2 = 1.0 - 1.0 / 2097152.0;
+  k_rate<NN, NE><<<blocks, 256>>>(iters / 8, 1.25, c1, c2, out);  // warm-up
+  cudaEventRecord(e0);
+  k_rate<NN, NE><<<blocks, 256>>>(iters, 1.25, c1, c2, out);
+  cudaEventRecord(e1);
+  cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cudaGetLastError() != cudaSuccess) return DEM_ERR_CUDA;
+  const double ops = 2.0 * (NN + NE) * (double)iters * (double)blocks * 256.0;
+  *gops = ops / (ms * 1e-3) * 1e-9;
+  return DEM_OK;
+}
+}  // namespace
+
+extern "C" int dem_selftest_emu_mul(uint64_t n, uint64_t seed, uint64_t* mismatches) {
+  if (!mismatches) return DEM_ERR_INVALID_ARG;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, sizeof(unsigned long long)) != cudaSuccess) return DEM_ERR_CUDA;
+  cudaMemset(d, 0, sizeof(unsigned long long));
+  k_emu_test<<<1216, 256>>>(n, seed, d);
+  unsigned long long h = 0;
+  const bool ok = cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaFree(d);
+  if (!ok || cudaGetLastError() != cudaSuccess) return DEM_ERR_CUDA;
+  *mismatches = h;
+  return DEM_OK;
+}
+
+extern "C" int dem_probe_mul_rates(int iters, double* gops) {
+  if (!gops || iters < 8) return DEM_ERR_INVALID_ARG;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = sms * 8;
+  double* out = nullptr;
+  if (cudaMalloc(&out, (size_t)blocks * 256 * sizeof(double)) != cudaSuccess) return DEM_ERR_CUDA;
+  int st = time_rate<4, 0>(blocks, iters, out, &gops[0]);
+  if (st == DEM_OK) st = time_rate<0, 4>(blocks, iters, out, &gops[1]);
+  if (st == DEM_OK) st = time_rate<4, 4>(blocks, iters, out, &gops[2]);
+  if (st == DEM_OK) st = time_rate<4, 2>(blocks, iters, out, &gops[3]);
+  if (st == DEM_OK) st = time_rate<2, 4>(blocks, iters, out, &gops[4]);
+  cudaFree(out);
+  return st;
+}

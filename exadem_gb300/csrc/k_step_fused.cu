@@ -246,12 +246,13 @@ __global__ void __launch_bounds__(FT) k_chooke(CArgs a) {
   }
 }
 
+template <int Mode>
 __global__ void k_fused_prolog(PArrays P, uint64_t n, double delta_t, double half_delta_t, double delta_t2_2,
                                double thr2, unsigned long long* flag, SysView sv) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;
   if (s < n) {
-    prolog_one(P, s, delta_t, half_delta_t, delta_t2_2);
+    prolog_one<Mode>(P, s, delta_t, half_delta_t, delta_t2_2);
     const double dx = P.f[RX][s] - P.f[BX][s], dy = P.f[RY][s] - P.f[BY][s], dz = P.f[RZ][s] - P.f[BZ][s];
     over = dx * dx + dy * dy + dz * dz >= thr2;
     if (over && sv.nsys > 1) atomicOr(&sv.trig[sv.of(s)], 1u);  // this system's own trigger
@@ -260,6 +261,7 @@ __global__ void k_fused_prolog(PArrays P, uint64_t n, double delta_t, double hal
 }
 
 // reset_force_moment + gravity_force + contact gather + force_to_accel + epilog
+template <int Mode>
 __global__ void __launch_bounds__(256) k_fused_epilog(PArrays P, Records R, uint64_t n,
                                                      const uint32_t* __restrict__ own_off,
                                                      const uint32_t* __restrict__ rev_off,
@@ -280,14 +282,16 @@ __global__ void __launch_bounds__(256) k_fused_epilog(PArrays P, Records R, uint
     mom = mom + mk(R.tj[0][k], R.tj[1][k], R.tj[2][k]);
   }
   const double im = P.f[IMASS][s];
-  const V3 acc = mk(div_rn(f.x, m, im), div_rn(f.y, m, im), div_rn(f.z, m, im));
+  LinMul<Mode> lm;
+  V3 acc = mk(div_rn_m(lm, f.x, m, im), div_rn_m(lm, f.y, m, im), div_rn_m(lm, f.z, m, im));
+  if (lm.failed()) acc = mk(div_rn(f.x, m, im), div_rn(f.y, m, im), div_rn(f.z, m, im));
   P.f[FX][s] = acc.x;
   P.f[FY][s] = acc.y;
   P.f[FZ][s] = acc.z;
   P.f[MX][s] = mom.x;
   P.f[MY][s] = mom.y;
   P.f[MZ][s] = mom.z;
-  epilog_one<true>(P, s, half_delta_t, acc, mom);
+  epilog_one<true, Mode>(P, s, half_delta_t, acc, mom);
 }
 
 CArgs make_cargs(dem_ctx* c) {
@@ -320,10 +324,11 @@ int launch_fused_prolog(dem_ctx* c) {
   const double max_displ = c->prm.rcut_inc * 0.5;
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars, 0, sizeof(unsigned long long), c->stream));
   ProfScope ps(c, K_PROLOG, c->n ? 1 : 0);
+  const auto kern = by_mode(c->mul_mode, k_fused_prolog<0>, k_fused_prolog<1>, k_fused_prolog<2>, k_fused_prolog<3>);
   if (c->n)
-    k_fused_prolog<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(c->P[c->pcur], c->n, delta_t,
-                                                                                   half_delta_t, delta_t2_2,
-                                                              max_displ * max_displ, c->d_scalars, c->sysview());
+    kern<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(c->P[c->pcur], c->n, delta_t, half_delta_t,
+                                                                         delta_t2_2, max_displ * max_displ,
+                                                                         c->d_scalars, c->sysview());
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }
@@ -345,12 +350,12 @@ int launch_contact_compact(dem_ctx* c) {
 
 int launch_fused_epilog(dem_ctx* c) {
   ProfScope ps(c, K_EPILOG, c->n ? 1 : 0);
+  const auto kern = by_mode(c->mul_mode, k_fused_epilog<0>, k_fused_epilog<1>, k_fused_epilog<2>, k_fused_epilog<3>);
   if (c->n)
-    k_fused_epilog<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(c->P[c->pcur], c->R, c->n,
-                                                                                   c->own_off[c->icur],
-                                                              c->rev_off, c->rev_idx, c->prm.gravity[0],
-                                                              c->prm.gravity[1], c->prm.gravity[2],
-                                                              c->prm.dt * 0.5);
+    kern<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(c->P[c->pcur], c->R, c->n,
+                                                                         c->own_off[c->icur], c->rev_off, c->rev_idx,
+                                                                         c->prm.gravity[0], c->prm.gravity[1],
+                                                                         c->prm.gravity[2], c->prm.dt * 0.5);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

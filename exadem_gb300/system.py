@@ -266,6 +266,15 @@ class System:
         self._check(self.b.autotune(self.h, int(steps_per_trial), int(skin_policy), C.byref(r)), "autotune")
         return {f: getattr(r, f) for f, _ in A.TuneResult._fields_}
 
+    def set_mul_mode(self, mode: int) -> None:
+        """dem_set_mul_mode: which integration multiplies run on the integer pipe (same bits)."""
+        self._check(self.b.set_mul_mode(self.h, int(mode)), "set_mul_mode")
+
+    def mul_mode(self) -> int:
+        v = C.c_int()
+        self._check(self.b.get_mul_mode(self.h, C.byref(v)), "get_mul_mode")
+        return int(v.value)
+
     def set_graph_capacity(self, capacity: int) -> None:
         self._check(self.b.set_graph_capacity(self.h, int(capacity)), "set_graph_capacity")
 

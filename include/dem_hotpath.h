@@ -323,8 +323,19 @@ typedef struct dem_tune_result {
   double ms_per_step_before;     /* model cost of the configuration before       */
   int32_t trials;
   float vmax;                    /* fastest particle speed used by the model     */
+  int32_t mul_mode;              /* multiply placement, see dem_set_mul_mode     */
 } dem_tune_result;
 int dem_autotune(dem_ctx* ctx, int steps_per_trial, int skin_policy, dem_tune_result* out);
+/* Multiply placement of the fused integration kernels (prolog, epilog).  The
+ * FP64 pipe of sm_103a retires ~2 lanes per clock per SM; an IEEE multiply
+ * built from integer partial products runs on the otherwise idle integer pipe
+ * and returns the same bits.  mode bit 0: rotation multiplies (quaternion
+ * rotations and derivative, normalisation, Euler terms) on the integer pipe;
+ * bit 1: the other multiplies (Verlet pushes, gravity, quotient estimates).
+ * 0 = FP64 pipe only.  Results are identical in every mode.  Default 1; the
+ * autotuner picks the fastest for the sphere step.                         */
+int dem_set_mul_mode(dem_ctx* ctx, int mode);
+int dem_get_mul_mode(dem_ctx* ctx, int* mode);
 /* Number of neighbour rebuilds done so far (trigger_move_particles count). */
 int dem_rebuild_count(dem_ctx* ctx, uint64_t* out);
 

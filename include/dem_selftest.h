@@ -21,6 +21,19 @@ int dem_selftest_division(uint64_t n, uint64_t seed, uint64_t* mismatches, uint6
  * counts[4 * kind + k] (24 entries), k = 0: decided cases whose result differs
  * from FP64 (must be 0), 1: undecided cases, 2: decided true, 3: FP64 true.  */
 int dem_selftest_poly_decisions(uint64_t n, uint64_t seed, uint64_t* counts);
+
+/* Draws n seeded operand pairs (typical magnitudes, short significands that
+ * give exact products and ties, the whole exponent range, boundaries, zeros,
+ * subnormals, infinities, NaNs) and counts the results of the integer-pipe
+ * binary64 multiply (emu_dmul, and the exact x*2 / x*0.5) that differ in any
+ * bit from the hardware multiply.                                          */
+int dem_selftest_emu_mul(uint64_t n, uint64_t seed, uint64_t* mismatches);
+
+/* Multiply throughput in G multiplies/s over all SMs, dependent chains, 8
+ * blocks of 256 threads per SM: gops[0] FP64 pipe alone, gops[1] integer pipe
+ * alone (emu_dmul), gops[2..4] both in the same threads, with native:emulated
+ * chain ratios 4:4, 4:2 and 2:4.                                           */
+int dem_probe_mul_rates(int iters, double* gops);
 #ifdef __cplusplus
 }
 #endif

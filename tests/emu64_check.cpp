@@ -1,0 +1,98 @@
+// Host check of exadem_gb300/csrc/emu64.cuh: emu_dmul, emu_mul2 and emu_mulhalf
+// against the host's IEEE binary64 multiply, bit for bit.
+// Usage: emu64_check <n_cases> <seed>; prints "cases <n> mismatches <m>".
+// Built by tests/test_emu64.py with g++ -O2 -ffp-contract=off.
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "emu64.cuh"
+
+static uint64_t sm_state;
+static uint64_t next64() {
+  uint64_t z = (sm_state += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+static uint64_t bits(double x) { return dem::emu_bits(x); }
+
+// operand classes: full random significand over a wide exponent band, short
+// significands (exact products and ties), boundary exponents, and specials
+static double draw() {
+  const uint64_t r = next64();
+  const uint64_t sign = (r & 1) << 63;
+  const int cls = (int)((r >> 1) % 16);
+  uint64_t frac = next64() & 0xfffffffffffffull;
+  uint64_t e;
+  if (cls < 7) {
+    e = 1023 - 60 + (next64() % 121);  // typical magnitudes 2^-60..2^60
+  } else if (cls < 10) {
+    const int keep = (int)(next64() % 12);  // short significand: ties and exact products
+    frac &= ~((1ull << (52 - keep)) - 1);
+    e = 1023 - 30 + (next64() % 61);
+  } else if (cls < 12) {
+    e = 1 + (next64() % 2046);  // whole normal range: overflow / underflow of the product
+  } else if (cls == 12) {
+    e = (next64() & 1) ? 1 + (next64() % 40) : 2046 - (next64() % 40);
+  } else if (cls == 13) {
+    e = 0;  // zero or subnormal
+    if (next64() & 1) frac = 0;
+  } else if (cls == 14) {
+    e = 2047;  // infinity or NaN
+    if (next64() & 1) frac = 0;
+  } else {
+    frac = (next64() & 1) ? 0xfffffffffffffull : 0;  // all-ones / power of two significands
+    e = 1023 - 8 + (next64() % 17);
+  }
+  double x;
+  const uint64_t u = sign | (e << 52) | frac;
+  memcpy(&x, &u, 8);
+  return x;
+}
+
+int main(int argc, char** argv) {
+  const long n = argc > 1 ? atol(argv[1]) : 1000000;
+  sm_state = argc > 2 ? strtoull(argv[2], 0, 10) : 1;
+  long bad = 0, flagged = 0;
+  for (long i = 0; i < n; i++) {
+    const double a = draw(), b = draw();
+    const double ref = a * b, got = dem::emu_dmul(a, b);
+    const bool nan_both = ref != ref && got != got;
+    if (bits(ref) != bits(got) && !nan_both) {
+      if (bad < 8)
+        printf("mul %016llx * %016llx: want %016llx got %016llx\n", (unsigned long long)bits(a),
+               (unsigned long long)bits(b), (unsigned long long)bits(ref), (unsigned long long)bits(got));
+      bad++;
+    }
+    bool fl = false;
+    const double gnb = dem::emu_dmul_nb(a, b, fl);
+    if (!fl && bits(ref) != bits(gnb)) {
+      if (bad < 8) printf("mul_nb %016llx * %016llx\n", (unsigned long long)bits(a), (unsigned long long)bits(b));
+      bad++;
+    }
+    flagged += fl ? 1 : 0;
+    const double sref[3] = {a * 2.0, a * 0.5, a * -0.5};
+    bool f2 = false, fh = false, fn = false;
+    const double snb[3] = {dem::emu_mul2_nb(a, f2), dem::emu_mulhalf_nb(a, fh), dem::emu_mulnhalf_nb(a, fn)};
+    const bool sfl[3] = {f2, fh, fn};
+    for (int q = 0; q < 3; q++)
+      if (!sfl[q] && bits(sref[q]) != bits(snb[q])) {
+        if (bad < 8) printf("scale_nb %d %016llx\n", q, (unsigned long long)bits(a));
+        bad++;
+      }
+    const double r2 = a * 2.0, g2 = dem::emu_mul2(a);
+    const double rh = a * 0.5, gh = dem::emu_mulhalf(a);
+    const double rn = a * -0.5, gn = dem::emu_mulnhalf(a);
+    if ((bits(r2) != bits(g2) && !(r2 != r2 && g2 != g2)) || (bits(rh) != bits(gh) && !(rh != rh && gh != gh)) ||
+        (bits(rn) != bits(gn) && !(rn != rn && gn != gn))) {
+      if (bad < 8) printf("scale %016llx\n", (unsigned long long)bits(a));
+      bad++;
+    }
+  }
+  printf("flagged %ld (branch-free form: recomputed by the caller)\n", flagged);
+  printf("cases %ld mismatches %ld\n", n, bad);
+  return bad ? 1 : 0;
+}

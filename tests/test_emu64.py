@@ -1,0 +1,39 @@
+"""The integer-pipe binary64 multiply (exadem_gb300/csrc/emu64.cuh) returns the
+IEEE product bit for bit: on the host against the host's multiply (CPU), and
+on the GPU against the hardware multiply, with its throughput next to the FP64
+pipe's."""
+import ctypes as C
+import shutil
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_emu_dmul_host_bit_exact(tmp_path):
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "emu64_check"
+    subprocess.run([gxx, "-O2", "-ffp-contract=off", "-I", str(ROOT / "exadem_gb300" / "csrc"),
+                    str(ROOT / "tests" / "emu64_check.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe), "4000000", "11"], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout
+    assert out.stdout.strip().endswith("mismatches 0")
+
+
+@pytest.mark.gpu
+def test_emu_dmul_gpu_bit_exact(native_lib):
+    bad = C.c_uint64(0)
+    assert native_lib.dem_selftest_emu_mul(200_000_000, 2024, C.byref(bad)) == 0
+    assert bad.value == 0
+
+
+@pytest.mark.gpu
+def test_mul_rates_probe(native_lib):
+    g = (C.c_double * 5)()
+    assert native_lib.dem_probe_mul_rates(4096, g) == 0
+    print("multiply rates, G/s: fp64 %.0f  integer %.0f  both 4:4 %.0f  4:2 %.0f  2:4 %.0f" % tuple(g))
+    assert all(x > 0 for x in g)
