@@ -41,7 +41,8 @@ CONTACT_BYTES_PER_INTERACTION = 104
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: the workload's whole run, e.g. 1000 for the 2M-sphere deposition)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--n", type=int, default=None, help="particle count (default: the workload's)")
@@ -162,6 +163,13 @@ def allsum(dist, x: float) -> float:
 
 
 def workload(args):
+    w = _workload(args)
+    if args.steps is None:
+        args.steps = int(w.steps)
+    return w
+
+
+def _workload(args):
     from exadem_gb300 import workloads as W
 
     opt = 0 if args.plain else 1
@@ -416,6 +424,14 @@ def run_native(args, rank, world, local, dist):
     total = allsum(dist, float(w.n * args.steps))
     value = total / (ms / 1e3)
 
+    # particles whose epilog rotation is exactly zero (no spin, no torque) at the end of the timed run
+    pp = s.particles(sort_by_id=False)
+    idle = np.ones(w.n, dtype=bool)
+    for k in ("vrotx", "vroty", "vrotz", "momx", "momy", "momz"):
+        idle &= pp[k].view(np.uint64) == 0
+    idle_fraction = float(idle.mean()) if w.n else 0.0
+    del pp
+
     # per-kernel times (profiled run, separate from the timed one)
     s.reset_kernel_stats()
     s.profile(True)
@@ -484,6 +500,7 @@ def run_native(args, rank, world, local, dist):
                            + (", whole step replayed as one CUDA graph" if getattr(w.params, "graph_step", 0) else "")
                            + (f", {w.info['systems']} systems in one context" if is_batch(w) else ""),
                    "mul_mode": None if args.plain else mul_mode,
+                   "rotation_idle_fraction_at_end": round(idle_fraction, 4),
                    "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
                    "parallelism": "replicas" if world > 1 else "single",
                    "inputs": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in w.info.items()

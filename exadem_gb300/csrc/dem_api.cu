@@ -81,6 +81,8 @@ int alloc_particles(dem_ctx* c, uint64_t n) {
     cudaFree(c->crel[q]);
     DEM_CUDA_TRY(c, cudaMalloc(&c->crel[q], cap * sizeof(float)));
   }
+  cudaFree(c->rot_list);
+  DEM_CUDA_TRY(c, cudaMalloc(&c->rot_list, cap * 4));
   c->pcap = cap;
   return DEM_OK;
 }
@@ -577,6 +579,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   cudaFree(c->perm);
   cudaFree(c->pcnt);
   for (int q = 0; q < 4; q++) cudaFree(c->crel[q]);
+  cudaFree(c->rot_list);
   cudaFree(c->scan_blk);
   cudaFree(c->d_scalars);
   cudaFree(c->d_red);

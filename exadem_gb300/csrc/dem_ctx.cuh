@@ -23,7 +23,7 @@ struct MlpState;  // k_mlp.cu
 // [3..4] compaction list counts, [8] learned-record overflows,
 // [16..23] learned bin counters and cursors (14 u32)
 constexpr int DEM_NSCALARS = 32;
-constexpr int SC_LEARNED_OVF = 8, SC_LEARNED_BINS = 16;
+constexpr int SC_ROT_CNT = 6, SC_LEARNED_OVF = 8, SC_LEARNED_BINS = 16;
 
 // features recorded per polyhedron unit by the count pass of the FP32-decided
 // enumeration; the fill pass copies them instead of deciding again
@@ -109,6 +109,7 @@ struct dem_ctx {
   // compacted contact passes (rcap each): work lists and detection results
   uint32_t* L1 = nullptr;
   uint32_t* L2 = nullptr;
+  uint32_t* rot_list = nullptr;  // pcap: particles whose epilog rotation runs in k_epilog_rotation
   double* Dscr[7] = {};
 
   // scan scratch

@@ -140,19 +140,25 @@ __device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& 
 template <int Mode = 0>
 __device__ __forceinline__ void prolog_one(const PArrays& P, uint64_t s, double delta_t, double half_delta_t,
                                            double delta_t2_2) {
-  ProlState in;
-  in.r = mk(P.f[RX][s], P.f[RY][s], P.f[RZ][s]);
-  in.v = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
-  in.a = mk(P.f[FX][s], P.f[FY][s], P.f[FZ][s]);
-  in.q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
-  in.w = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
-  in.arot = mk(P.f[AX][s], P.f[AY][s], P.f[AZ][s]);
+  auto load = [&]() {
+    ProlState in;
+    in.r = mk(P.f[RX][s], P.f[RY][s], P.f[RZ][s]);
+    in.v = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
+    in.a = mk(P.f[FX][s], P.f[FY][s], P.f[FZ][s]);
+    in.q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+    in.w = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+    in.arot = mk(P.f[AX][s], P.f[AY][s], P.f[AZ][s]);
+    return in;
+  };
   RotMul<Mode> rm;
   LinMul<Mode> lm;
-  ProlState o = prolog_math(rm, lm, in, delta_t, half_delta_t, delta_t2_2);
+  ProlState o = prolog_math(rm, lm, load(), delta_t, half_delta_t, delta_t2_2);
   if (rm.failed() || lm.failed()) {
+    // nothing is stored yet: reload the inputs (the barrier keeps the main
+    // path from holding them in registers for this rare case)
+    asm volatile("" ::: "memory");
     MulFP64 n;
-    o = prolog_math(n, n, in, delta_t, half_delta_t, delta_t2_2);
+    o = prolog_math(n, n, load(), delta_t, half_delta_t, delta_t2_2);
   }
   P.f[RX][s] = o.r.x;
   P.f[RY][s] = o.r.y;
@@ -198,20 +204,33 @@ __device__ __forceinline__ EpiOut epilog_math(R& rm, L& lm, Q4 Q, V3 vrot, V3 I,
   return o;
 }
 
-template <bool FastDiv, int Mode = 0>
+// A particle whose spin and torque are all +0.0 keeps arot = +0 and w = +0
+// bit for bit, provided the quaternion is finite and the inertia and its
+// reciprocal are positive and finite: every product of a quaternion or inertia
+// component with +0 is +-0; a sum whose first operand is +0 and whose other
+// operands are +-0 is +0 (round to nearest: -0 only for (-0) + (-0)); so
+// omega = qrotate(Q^-1, +0) = +0 and M = +0, the Euler numerators are
+// +0 - (+-0) = +0, div_rn(+0, I, 1/I) = +0 * (1/I) = +0, arot = qrotate(Q, +0)
+// = +0 and w = +0 + (+0 * dt/2) = +0.
+__device__ __forceinline__ bool finite_bits(double x) { return ((emu_bits(x) >> 52) & 0x7ffu) != 0x7ffu; }
+__device__ __forceinline__ bool positive_finite_bits(double x) { return (emu_bits(x) >> 52) < 0x7ffu; }
+__device__ __forceinline__ bool rotation_idle(Q4 Q, V3 vrot, V3 mom, V3 I, V3 II) {
+  const uint64_t z = emu_bits(vrot.x) | emu_bits(vrot.y) | emu_bits(vrot.z) | emu_bits(mom.x) | emu_bits(mom.y) |
+                     emu_bits(mom.z);
+  return z == 0 && finite_bits(Q.w) && finite_bits(Q.x) && finite_bits(Q.y) && finite_bits(Q.z) &&
+         positive_finite_bits(I.x) && positive_finite_bits(I.y) && positive_finite_bits(I.z) &&
+         positive_finite_bits(II.x) && positive_finite_bits(II.y) && positive_finite_bits(II.z);
+}
+
+template <bool FastDiv>
 __device__ __forceinline__ void epilog_one(const PArrays& P, uint64_t s, double half_delta_t, V3 a, V3 mom) {
+  MulFP64 rm, lm;
   const Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
   const V3 vrot = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
   const V3 I = mk(P.f[IX][s], P.f[IY][s], P.f[IZ][s]);
   const V3 II = FastDiv ? mk(P.f[IIX][s], P.f[IIY][s], P.f[IIZ][s]) : mk(0.0, 0.0, 0.0);
   const V3 vel = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
-  RotMul<Mode> rm;
-  LinMul<Mode> lm;
-  EpiOut o = epilog_math<FastDiv>(rm, lm, Q, vrot, I, II, vel, a, mom, half_delta_t);
-  if (rm.failed() || lm.failed()) {
-    MulFP64 n;
-    o = epilog_math<FastDiv>(n, n, Q, vrot, I, II, vel, a, mom, half_delta_t);
-  }
+  const EpiOut o = epilog_math<FastDiv>(rm, lm, Q, vrot, I, II, vel, a, mom, half_delta_t);
   P.f[AX][s] = o.arot.x;
   P.f[AY][s] = o.arot.y;
   P.f[AZ][s] = o.arot.z;
@@ -221,6 +240,45 @@ __device__ __forceinline__ void epilog_one(const PArrays& P, uint64_t s, double 
   P.f[VX][s] = o.v.x;
   P.f[VY][s] = o.v.y;
   P.f[VZ][s] = o.v.z;
+}
+
+// The rotational half of the fused epilog (arot and w from the torque stored
+// in mom; the velocity update is done by the caller), the operation order of
+// epilog_math.  An integer-pipe multiply that leaves its fast path makes the
+// whole half run again on the FP64 pipe from the stored inputs.
+template <int Mode>
+__device__ __forceinline__ void epilog_rotation(const PArrays& P, uint64_t s, double half_delta_t, V3 mom) {
+  auto run = [&](auto& rm, auto& lm, V3 tq, V3& arot, V3& w) {
+    const Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+    const V3 vrot = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+    const V3 I = mk(P.f[IX][s], P.f[IY][s], P.f[IZ][s]);
+    const V3 II = mk(P.f[IIX][s], P.f[IIY][s], P.f[IIZ][s]);
+    const Q4 Qinv = {Q.w, -Q.x, -Q.y, -Q.z};
+    const V3 omega = qrotate_m(rm, Qinv, vrot);
+    const V3 M = qrotate_m(rm, Qinv, tq);
+    const double nx = M.x - rm.mul(rm.mul(I.z - I.y, omega.y), omega.z);
+    const double ny = M.y - rm.mul(rm.mul(I.x - I.z, omega.z), omega.x);
+    const double nz = M.z - rm.mul(rm.mul(I.y - I.x, omega.x), omega.y);
+    const V3 domega = mk(div_rn_m(lm, nx, I.x, II.x), div_rn_m(lm, ny, I.y, II.y), div_rn_m(lm, nz, I.z, II.z));
+    arot = qrotate_m(rm, Q, domega);
+    w = mk(vrot.x + lm.mul(arot.x, half_delta_t), vrot.y + lm.mul(arot.y, half_delta_t),
+           vrot.z + lm.mul(arot.z, half_delta_t));
+  };
+  RotMul<Mode> rm;
+  LinMul<Mode> lm;
+  V3 arot, w;
+  run(rm, lm, mom, arot, w);
+  if (rm.failed() || lm.failed()) {
+    asm volatile("" ::: "memory");  // reload the inputs, nothing is stored yet
+    MulFP64 n;
+    run(n, n, mk(P.f[MX][s], P.f[MY][s], P.f[MZ][s]), arot, w);
+  }
+  P.f[AX][s] = arot.x;
+  P.f[AY][s] = arot.y;
+  P.f[AZ][s] = arot.z;
+  P.f[WX][s] = w.x;
+  P.f[WY][s] = w.y;
+  P.f[WZ][s] = w.z;
 }
 
 }  // namespace dem

@@ -126,7 +126,7 @@ __global__ void k_poly_vertices(PolyArgs a, double thr2, unsigned long long* fla
 // exactly as the reference does (world vertex minus the stored backup vertex).
 // No vertex is written.
 template <int Mode>
-__global__ void k_poly_fused_prolog(PolyArgs a, double delta_t, double half_delta_t, double delta_t2_2,
+__global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_poly_fused_prolog(PolyArgs a, double delta_t, double half_delta_t, double delta_t2_2,
                                     double thr2, float thr, unsigned long long* flag) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;

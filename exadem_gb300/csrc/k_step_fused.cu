@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(FT) k_chooke(CArgs a) {
 }
 
 template <int Mode>
-__global__ void k_fused_prolog(PArrays P, uint64_t n, double delta_t, double half_delta_t, double delta_t2_2,
+__global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_prolog(PArrays P, uint64_t n, double delta_t, double half_delta_t, double delta_t2_2,
                                double thr2, unsigned long long* flag, SysView sv) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;
@@ -260,38 +260,103 @@ __global__ void k_fused_prolog(PArrays P, uint64_t n, double delta_t, double hal
   if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
 }
 
-// reset_force_moment + gravity_force + contact gather + force_to_accel + epilog
+// reset_force_moment + gravity_force + contact gather + force_to_accel + epilog.
+// The velocity half of the epilog runs here for every particle.  The
+// rotational half is exactly zero for a particle without spin and torque
+// (rotation_idle); the others run it here when most of their warp needs it,
+// otherwise they are appended to rot_list for k_epilog_rotation, so sparse
+// rotating particles do not hold whole warps on the FP64 pipe.
+// Mode != 0: the integer-pipe multiplies raise register use; at most 80
+// registers keep 3 blocks of 256 per SM (measured faster than 2 blocks)
 template <int Mode>
-__global__ void __launch_bounds__(256) k_fused_epilog(PArrays P, Records R, uint64_t n,
-                                                     const uint32_t* __restrict__ own_off,
-                                                     const uint32_t* __restrict__ rev_off,
-                                                     const uint32_t* __restrict__ rev_idx, double gx, double gy,
-                                                     double gz, double half_delta_t) {
+__global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_epilog(PArrays P, Records R, uint64_t n,
+                                                                     const uint32_t* __restrict__ own_off,
+                                                                     const uint32_t* __restrict__ rev_off,
+                                                                     const uint32_t* __restrict__ rev_idx,
+                                                                     double gx, double gy, double gz,
+                                                                     double half_delta_t, uint32_t* rot_list,
+                                                                     unsigned long long* rot_cnt) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const double m = P.f[MASS][s];
-  V3 f = mk(0.0 + gx * m, 0.0 + gy * m, 0.0 + gz * m);
+  bool need = false;
   V3 mom = mk(0.0, 0.0, 0.0);
-  for (uint32_t k = own_off[s]; k < own_off[s + 1]; k++) {
-    f = f + mk(R.f[0][k], R.f[1][k], R.f[2][k]);
-    mom = mom + mk(R.ti[0][k], R.ti[1][k], R.ti[2][k]);
+  if (s < n) {
+    const double m = P.f[MASS][s];
+    V3 f = mk(0.0 + gx * m, 0.0 + gy * m, 0.0 + gz * m);
+    // f and mom start at +0 or a nonzero value and, in round to nearest, never
+    // become -0 (x + (-x) = +0; -0 needs two -0 operands), so a record whose six
+    // components are all +-0 (a listed pair that does not touch) leaves them
+    // unchanged bit for bit and its additions are skipped.
+    for (uint32_t k = own_off[s]; k < own_off[s + 1]; k++) {
+      const V3 rf = mk(R.f[0][k], R.f[1][k], R.f[2][k]), rt = mk(R.ti[0][k], R.ti[1][k], R.ti[2][k]);
+      if (((emu_bits(rf.x) | emu_bits(rf.y) | emu_bits(rf.z) | emu_bits(rt.x) | emu_bits(rt.y) | emu_bits(rt.z))
+           << 1) != 0) {
+        f = f + rf;
+        mom = mom + rt;
+      }
+    }
+    for (uint32_t q = rev_off[s]; q < rev_off[s + 1]; q++) {
+      const uint32_t k = rev_idx[q];
+      const V3 rf = mk(R.f[0][k], R.f[1][k], R.f[2][k]), rt = mk(R.tj[0][k], R.tj[1][k], R.tj[2][k]);
+      if (((emu_bits(rf.x) | emu_bits(rf.y) | emu_bits(rf.z) | emu_bits(rt.x) | emu_bits(rt.y) | emu_bits(rt.z))
+           << 1) != 0) {
+        f = f + (-rf);
+        mom = mom + rt;
+      }
+    }
+    const double im = P.f[IMASS][s];
+    LinMul<Mode> lm;
+    V3 acc = mk(div_rn_m(lm, f.x, m, im), div_rn_m(lm, f.y, m, im), div_rn_m(lm, f.z, m, im));
+    const V3 vel = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
+    V3 v = mk(vel.x + lm.mul(acc.x, half_delta_t), vel.y + lm.mul(acc.y, half_delta_t),
+              vel.z + lm.mul(acc.z, half_delta_t));
+    if (lm.failed()) {
+      acc = mk(div_rn(f.x, m, im), div_rn(f.y, m, im), div_rn(f.z, m, im));
+      v = mk(vel.x + acc.x * half_delta_t, vel.y + acc.y * half_delta_t, vel.z + acc.z * half_delta_t);
+    }
+    P.f[FX][s] = acc.x;
+    P.f[FY][s] = acc.y;
+    P.f[FZ][s] = acc.z;
+    P.f[MX][s] = mom.x;
+    P.f[MY][s] = mom.y;
+    P.f[MZ][s] = mom.z;
+    P.f[VX][s] = v.x;
+    P.f[VY][s] = v.y;
+    P.f[VZ][s] = v.z;
+    const V3 vrot = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+    need = true;
+    if (((emu_bits(vrot.x) | emu_bits(vrot.y) | emu_bits(vrot.z) | emu_bits(mom.x) | emu_bits(mom.y) |
+          emu_bits(mom.z))) == 0) {
+      const Q4 Q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+      const V3 I = mk(P.f[IX][s], P.f[IY][s], P.f[IZ][s]);
+      const V3 II = mk(P.f[IIX][s], P.f[IIY][s], P.f[IIZ][s]);
+      if (rotation_idle(Q, vrot, mom, I, II)) {
+        need = false;
+        P.f[AX][s] = 0.0;  // w stays +0
+        P.f[AY][s] = 0.0;
+        P.f[AZ][s] = 0.0;
+      }
+    }
   }
-  for (uint32_t q = rev_off[s]; q < rev_off[s + 1]; q++) {
-    const uint32_t k = rev_idx[q];
-    f = f + (-mk(R.f[0][k], R.f[1][k], R.f[2][k]));
-    mom = mom + mk(R.tj[0][k], R.tj[1][k], R.tj[2][k]);
+  const unsigned busy = __ballot_sync(0xffffffffu, need);
+  if (__popc(busy) > 24) {
+    if (need) epilog_rotation<Mode>(P, s, half_delta_t, mom);
+  } else {
+    const uint32_t pos = warp_append(need, rot_cnt);
+    if (need) rot_list[pos] = (uint32_t)s;
   }
-  const double im = P.f[IMASS][s];
-  LinMul<Mode> lm;
-  V3 acc = mk(div_rn_m(lm, f.x, m, im), div_rn_m(lm, f.y, m, im), div_rn_m(lm, f.z, m, im));
-  if (lm.failed()) acc = mk(div_rn(f.x, m, im), div_rn(f.y, m, im), div_rn(f.z, m, im));
-  P.f[FX][s] = acc.x;
-  P.f[FY][s] = acc.y;
-  P.f[FZ][s] = acc.z;
-  P.f[MX][s] = mom.x;
-  P.f[MY][s] = mom.y;
-  P.f[MZ][s] = mom.z;
-  epilog_one<true, Mode>(P, s, half_delta_t, acc, mom);
+}
+
+// the rotational half of the epilog for the particles listed by k_fused_epilog
+template <int Mode>
+__global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_epilog_rotation(PArrays P, const uint32_t* __restrict__ rot_list,
+                                                                        const unsigned long long* rot_cnt,
+                                                                        double half_delta_t) {
+  const uint64_t cnt = *rot_cnt;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < cnt; w += stride) {
+    const uint32_t s = rot_list[w];
+    epilog_rotation<Mode>(P, s, half_delta_t, mk(P.f[MX][s], P.f[MY][s], P.f[MZ][s]));
+  }
 }
 
 CArgs make_cargs(dem_ctx* c) {
@@ -349,13 +414,18 @@ int launch_contact_compact(dem_ctx* c) {
 }
 
 int launch_fused_epilog(dem_ctx* c) {
-  ProfScope ps(c, K_EPILOG, c->n ? 1 : 0);
+  ProfScope ps(c, K_EPILOG, c->n ? 2 : 0);
   const auto kern = by_mode(c->mul_mode, k_fused_epilog<0>, k_fused_epilog<1>, k_fused_epilog<2>, k_fused_epilog<3>);
-  if (c->n)
-    kern<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(c->P[c->pcur], c->R, c->n,
-                                                                         c->own_off[c->icur], c->rev_off, c->rev_idx,
-                                                                         c->prm.gravity[0], c->prm.gravity[1],
-                                                                         c->prm.gravity[2], c->prm.dt * 0.5);
+  const auto krot = by_mode(c->mul_mode, k_epilog_rotation<0>, k_epilog_rotation<1>, k_epilog_rotation<2>,
+                            k_epilog_rotation<3>);
+  unsigned long long* rot_cnt = c->d_scalars + SC_ROT_CNT;
+  DEM_CUDA_TRY(c, cudaMemsetAsync(rot_cnt, 0, sizeof(unsigned long long), c->stream));
+  if (c->n) {
+    kern<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(
+        c->P[c->pcur], c->R, c->n, c->own_off[c->icur], c->rev_off, c->rev_idx, c->prm.gravity[0],
+        c->prm.gravity[1], c->prm.gravity[2], c->prm.dt * 0.5, c->rot_list, rot_cnt);
+    krot<<<(unsigned)c->num_sms * 3, 256, 0, c->stream>>>(c->P[c->pcur], c->rot_list, rot_cnt, c->prm.dt * 0.5);
+  }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }
