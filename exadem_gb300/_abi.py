@@ -188,6 +188,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_selftest_division", [C.c_uint64, C.c_uint64, PU64, PU64])
     _sig(lib, "dem_selftest_poly_decisions", [C.c_uint64, C.c_uint64, PU64])
     _sig(lib, "dem_selftest_emu_mul", [C.c_uint64, C.c_uint64, PU64])
+    _sig(lib, "dem_selftest_rolling_clip", [C.c_uint64, C.c_uint64, PU64, PU64])
     _sig(lib, "dem_probe_mul_rates", [C.c_int, C.POINTER(C.c_double)])
 
 
@@ -199,7 +200,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
             "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
-            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_selftest_emu_mul", "dem_probe_mul_rates", "dem_set_shapes", "dem_compute_vertices",
+            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_selftest_emu_mul", "dem_selftest_rolling_clip", "dem_probe_mul_rates", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
             "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune", "dem_set_mul_mode", "dem_get_mul_mode", "dem_mlp_harvest",
             "dem_mlp_init", "dem_mlp_set_params", "dem_mlp_get_params", "dem_mlp_forward", "dem_mlp_loss_grad",

@@ -2,8 +2,120 @@
 // contact kernels (plain one-pass and compacted three-pass).
 #pragma once
 #include "dem_ctx.cuh"
+#include "mul_policy.cuh"
 
 namespace dem {
+
+// Rolling clip of contact_force_core with its mur = 0 (contact_force.hpp:225-234):
+//   r = (b.w)/(w.w); b' = b - r w; t = |0 * |b'| * |fn||;
+//   if (|m|^2 > 0 && |m|^2 > t^2) m = m * (t / |m|)
+// t is +0 when |b'| and |fn| are finite and NaN otherwise (0 * inf, NaN).
+// Both are finite, with no operation overflowing, when every |b_c| < 2^200,
+// every |fn_c| < 2^500, every |w_c| < 2^200 and some |w_c| >= 2^-200: then
+// w.w lies in [2^-400, 3 2^400], |r w| <= |b| (1 + 8u) (a projection), and
+// every square stays below 2^1024.  So in that range the clip is exactly
+// "if (|m|^2 > 0) m = m * (+0)" (the signed zeros of m; m * 0 of an infinite
+// component is NaN, as in the formula), without the two norms, the division
+// and the square roots.  Outside it (w = 0, whose 0/0 keeps the moment, huge
+// or non-finite values) the formula itself runs.
+__device__ __forceinline__ bool exp_below(double x, int e2) {  // |x| < 2^e2, x finite
+  return (int)((emu_bits(x) >> 52) & 0x7ffu) < 1023 + e2;
+}
+__device__ __forceinline__ bool exp_at_least(double x, int e2) {  // |x| >= 2^e2
+  return (int)((emu_bits(x) >> 52) & 0x7ffu) >= 1023 + e2;
+}
+__device__ __forceinline__ void rolling_clip_mur0(V3 branch, V3 vrot_i, V3 fn, V3& mom_i) {
+  const bool in_range = exp_below(branch.x, 200) && exp_below(branch.y, 200) && exp_below(branch.z, 200) &&
+                        exp_below(fn.x, 500) && exp_below(fn.y, 500) && exp_below(fn.z, 500) &&
+                        exp_below(vrot_i.x, 200) && exp_below(vrot_i.y, 200) && exp_below(vrot_i.z, 200) &&
+                        (exp_at_least(vrot_i.x, -200) || exp_at_least(vrot_i.y, -200) ||
+                         exp_at_least(vrot_i.z, -200));
+  const double mom_square = dot(mom_i, mom_i);
+  if (in_range) {
+    if (mom_square > 0.0) mom_i = mom_i * 0.0;
+    return;
+  }
+  const double r = (dot(branch, vrot_i)) / (dot(vrot_i, vrot_i));
+  branch = branch - r * vrot_i;
+  const double mur = 0;
+  const double threshold_mom = fabs(mur * vnorm(branch) * vnorm(fn));
+  if (mom_square > 0.0 && mom_square > threshold_mom * threshold_mom)
+    mom_i = mom_i * (threshold_mom / sqrt(mom_square));
+}
+
+template <class M>
+__device__ __forceinline__ V3 cross_m(M& mm, V3 a, V3 b) {
+  return mk(mm.mul(a.y, b.z) - mm.mul(a.z, b.y), mm.mul(a.z, b.x) - mm.mul(a.x, b.z),
+            mm.mul(a.x, b.y) - mm.mul(a.y, b.x));
+}
+template <class M>
+__device__ __forceinline__ double dot_m(M& mm, V3 a, V3 b) {
+  return mm.mul(a.x, b.x) + mm.mul(a.y, b.y) + mm.mul(a.z, b.z);
+}
+template <class M>
+__device__ __forceinline__ V3 scale_m(M& mm, double s, V3 a) {
+  return mk(mm.mul(s, a.x), mm.mul(s, a.y), mm.mul(s, a.z));
+}
+
+// contact_force_core below with its multiplies through mm, in the same
+// operation order, and the rolling clip through rolling_clip_mur0 (same
+// result); the clip's arithmetic keeps the FP64 pipe.
+template <class M>
+__device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, double dn, V3 n, double dt,
+                                                     const dem_contact_params& hkp, double meff, V3& ft, V3 cpos,
+                                                     V3 pos_i, V3 vel_i, V3& f_i, V3& mom_i, V3 vrot_i, V3 pos_j,
+                                                     V3 vel_j, V3 vrot_j) {
+  if (cohesive) {
+    if (dn >= 0) {
+      const double fn_value = mm.mul(hkp.fc / hkp.dncut, dn) - hkp.fc;
+      f_i = f_i + scale_m(mm, fn_value, n);
+      ft = mk(0, 0, 0);
+      return;
+    }
+  }
+  const double damp = mm.mul(mm.twice(hkp.damp_rate), sqrt(mm.mul(hkp.kn, meff)));
+  const V3 contribution_i = vel_i - cross_m(mm, cpos - pos_i, vrot_i);
+  const V3 contribution_j = vel_j - cross_m(mm, cpos - pos_j, vrot_j);
+  const V3 vel = contribution_j - contribution_i;
+  const double vn = dot_m(mm, vel, n);
+  V3 fn;
+  {
+    const double fne = mm.mul(-hkp.kn, dn);
+    const double fnv = mm.mul(damp, vn);
+    double nf = (fnv + fne > 0) ? fnv + fne : 0;
+    if (cohesive) {
+      const double fn_norm = nf - hkp.fc;
+      nf = fn_norm < (-hkp.fc) ? -hkp.fc : fn_norm;
+    }
+    fn = scale_m(mm, nf, n);
+  }
+  {
+    const V3 vt = vel - scale_m(mm, vn, n);
+    const V3 ftd = scale_m(mm, dt, vt);
+    ft = ft + scale_m(mm, hkp.kt, ftd);
+  }
+  double threshold_ft;
+  if (!cohesive) {
+    const double fne = mm.mul(hkp.kn, dn);
+    threshold_ft = fabs(mm.mul(hkp.mu, fne));
+  } else {
+    threshold_ft = fabs(mm.mul(hkp.mu, dot_m(mm, fn, n) + hkp.fc));
+  }
+  {
+    const double ft_square = dot_m(mm, ft, ft);
+    if (ft_square > 0.0 && ft_square > mm.mul(threshold_ft, threshold_ft)) {
+      const double s = threshold_ft / sqrt(ft_square);
+      ft = mk(mm.mul(ft.x, s), mm.mul(ft.y, s), mm.mul(ft.z, s));
+    }
+  }
+  f_i = fn + ft;
+  {
+    const V3 d = vrot_j - vrot_i;
+    mom_i = mom_i + mk(mm.mul(mm.mul(hkp.kr, d.x), dt), mm.mul(mm.mul(hkp.kr, d.y), dt),
+                       mm.mul(mm.mul(hkp.kr, d.z), dt));
+  }
+  rolling_clip_mur0(cpos - pos_i, vrot_i, fn, mom_i);
+}
 
 // contact_force_core (contact_force.hpp:146-235).  f_i must be {0,0,0} on entry.
 __device__ __forceinline__ void contact_force_core(bool cohesive, double dn, V3 n, double dt, const dem_contact_params& hkp,

@@ -988,7 +988,7 @@ int dem_set_graph_capacity(dem_ctx* c, uint64_t capacity) {
 }
 
 int dem_set_mul_mode(dem_ctx* c, int mode) {
-  if (!c || mode < 0 || mode > 3) return DEM_ERR_INVALID_ARG;
+  if (!c || mode < 0 || mode > 7) return DEM_ERR_INVALID_ARG;
   c->mul_mode = mode;
   c->gen++;  // a captured step holds the kernel instance of the old mode
   return DEM_OK;

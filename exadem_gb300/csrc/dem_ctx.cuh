@@ -9,11 +9,12 @@
 // Kernel classes for the built-in profiler (dem_profile / dem_kernel_stats).
 enum DemKClass : int {
   K_PROLOG, K_DISPL, K_BIN, K_REORDER, K_BROAD_COUNT, K_BROAD_FILL, K_REVERSE, K_SCAN,
-  K_CONTACT, K_GATHER, K_RESET, K_GRAVITY, K_F2A, K_EPILOG, K_STATE, K_NCLASS
+  K_CONTACT, K_GATHER, K_RESET, K_GRAVITY, K_F2A, K_EPILOG, K_STATE, K_CSCREEN, K_CDETECT, K_NCLASS
 };
 static const char* const kDemKClassNames[K_NCLASS] = {
     "prolog", "displ_over", "bin_cells", "reorder", "broad_count", "broad_fill", "reverse_lists", "scan",
-    "contact", "gather", "reset", "gravity", "force_to_accel", "epilog", "state"};
+    "contact", "gather", "reset", "gravity", "force_to_accel", "epilog", "state", "contact_screen",
+    "contact_detect"};
 
 namespace dem {
 struct MlpState;  // k_mlp.cu

@@ -255,8 +255,17 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
   // multiply placement of the integration kernels (same bits in every mode)
   int best_mode = mode0;
   for (int mode : {0, 1, 2, 3}) {
-    if (mode == mode0) continue;
+    if (mode == (mode0 & 3)) continue;
     double cost;
+    if ((rc = trial(best_skin, best_cell, best_block, best_bps, mode | (mode0 & 4), &cost))) return rc;
+    if (cost < best) {
+      best = cost;
+      best_mode = mode | (mode0 & 4);
+    }
+  }
+  {  // the contact law's multiplies
+    double cost;
+    const int mode = best_mode ^ 4;
     if ((rc = trial(best_skin, best_cell, best_block, best_bps, mode, &cost))) return rc;
     if (cost < best) {
       best = cost;

@@ -18,48 +18,12 @@
 // the FMAs of div_rn, the square root and the division stay on the FP64 pipe,
 // so with both bits set the two pipes share the work roughly evenly.
 #pragma once
-#include <type_traits>
-
 #include "dem_ctx.cuh"
 #include "emu64.cuh"
 #include "math_exact.cuh"
+#include "mul_policy.cuh"
 
 namespace dem {
-
-// Multiply policies.  MulFP64: the FP64 pipe.  MulInt: the branch-free
-// integer-pipe IEEE multiply; failed() reports an operand outside its fast
-// path (subnormal, infinite, NaN, out-of-range product), after which the
-// caller recomputes its block of arithmetic with MulFP64.
-struct MulFP64 {
-  __device__ __forceinline__ double mul(double a, double b) const { return __dmul_rn(a, b); }
-  __device__ __forceinline__ double twice(double a) const { return __dmul_rn(a, 2.0); }
-  __device__ __forceinline__ double half(double a) const { return __dmul_rn(a, 0.5); }
-  __device__ __forceinline__ double neghalf(double a) const { return __dmul_rn(a, -0.5); }
-  __device__ __forceinline__ bool failed() const { return false; }
-};
-struct MulInt {
-  bool bad = false;
-  __device__ __forceinline__ double mul(double a, double b) { return emu_dmul_nb(a, b, bad); }
-  __device__ __forceinline__ double twice(double a) { return emu_mul2_nb(a, bad); }
-  __device__ __forceinline__ double half(double a) { return emu_mulhalf_nb(a, bad); }
-  __device__ __forceinline__ double neghalf(double a) { return emu_mulnhalf_nb(a, bad); }
-  __device__ __forceinline__ bool failed() const { return bad; }
-};
-template <int Mode>
-using RotMul = typename std::conditional<(Mode & 1) != 0, MulInt, MulFP64>::type;
-template <int Mode>
-using LinMul = typename std::conditional<(Mode & 2) != 0, MulInt, MulFP64>::type;
-
-// the kernel instance compiled for a multiply placement
-template <class F>
-F by_mode(int mode, F m0, F m1, F m2, F m3) {
-  switch (mode & 3) {
-    case 1: return m1;
-    case 2: return m2;
-    case 3: return m3;
-    default: return m0;
-  }
-}
 
 // div_rn (math_exact.cuh) with its quotient estimate a*y through M
 template <class M>
@@ -104,7 +68,33 @@ struct ProlState {
   V3 r, v, a, w, arot;
   Q4 q;
 };
-template <class R, class L>
+// Quaternion step of a particle without spin (w = +0,+0,+0), finite Q and
+// 0 < dt < inf: every product w_k Q_l is a zero with the sign of Q_l, so the
+// derivative d is a signed zero whose sign follows from the signs of Q
+// (round to nearest: a sum of zeros is -0 only when every term is -0; a - b
+// adds -b); Q + d dt keeps every nonzero component and gives a zero component
+// the sign (sign(Q_c) and sign(d_c)).  spin_free_quaternion computes exactly
+// that with integer sign logic instead of the 24 FP64 operations.
+__device__ __forceinline__ bool spin_free_step(const Q4& Q, V3 om, double delta_t) {
+  const uint64_t ew = emu_bits(Q.w) >> 52 & 0x7ffu, ex = emu_bits(Q.x) >> 52 & 0x7ffu,
+                 ey = emu_bits(Q.y) >> 52 & 0x7ffu, ez = emu_bits(Q.z) >> 52 & 0x7ffu;
+  return (emu_bits(om.x) | emu_bits(om.y) | emu_bits(om.z)) == 0 && ew != 0x7ffu && ex != 0x7ffu &&
+         ey != 0x7ffu && ez != 0x7ffu && (emu_bits(delta_t) - 1u) < 0x7fefffffffffffffull;
+}
+__device__ __forceinline__ Q4 spin_free_quaternion(const Q4& Q) {
+  const uint64_t bw = emu_bits(Q.w), bx = emu_bits(Q.x), by = emu_bits(Q.y), bz = emu_bits(Q.z);
+  const uint64_t sw = bw >> 63, sx = bx >> 63, sy = by >> 63, sz = bz >> 63;
+  const uint64_t dx = sz & (sy ^ 1u) & sw;  // sign of d.x = half((w_y Q_z - w_z Q_y) + w_x Q_w)
+  const uint64_t dy = sx & (sz ^ 1u) & sw;
+  const uint64_t dz = sy & (sx ^ 1u) & sw;
+  const uint64_t dw = (sx & sy & sz) ^ 1u;  // -half(...) flips the sign
+  auto step = [](uint64_t b, uint64_t s, uint64_t sd) {
+    return (b << 1) == 0 ? emu_double((s & sd) << 63) : emu_double(b);
+  };
+  return Q4{step(bw, sw, dw), step(bx, sx, dx), step(by, sy, dy), step(bz, sz, dz)};
+}
+
+template <class R, class L, bool Shortcuts = false>
 __device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& in, double delta_t,
                                                  double half_delta_t, double delta_t2_2) {
   ProlState o = in;
@@ -115,19 +105,23 @@ __device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& 
            in.v.z + lm.mul(in.a.z, half_delta_t));
   Q4 Q = in.q;
   const V3 om = in.w;
-  Q4 d;
-  d.x = rm.half(rm.mul(om.y, Q.z) - rm.mul(om.z, Q.y) + rm.mul(om.x, Q.w));
-  d.y = rm.half(rm.mul(om.z, Q.x) - rm.mul(om.x, Q.z) + rm.mul(om.y, Q.w));
-  d.z = rm.half(rm.mul(om.x, Q.y) - rm.mul(om.y, Q.x) + rm.mul(om.z, Q.w));
-  d.w = rm.neghalf(rm.mul(om.x, Q.x) + rm.mul(om.y, Q.y) + rm.mul(om.z, Q.z));
-  Q.w = Q.w + rm.mul(d.w, delta_t);
-  Q.x = Q.x + rm.mul(d.x, delta_t);
-  Q.y = Q.y + rm.mul(d.y, delta_t);
-  Q.z = Q.z + rm.mul(d.z, delta_t);
+  if (Shortcuts && spin_free_step(Q, om, delta_t)) {
+    Q = spin_free_quaternion(Q);
+  } else {
+    Q4 d;
+    d.x = rm.half(rm.mul(om.y, Q.z) - rm.mul(om.z, Q.y) + rm.mul(om.x, Q.w));
+    d.y = rm.half(rm.mul(om.z, Q.x) - rm.mul(om.x, Q.z) + rm.mul(om.y, Q.w));
+    d.z = rm.half(rm.mul(om.x, Q.y) - rm.mul(om.y, Q.x) + rm.mul(om.z, Q.w));
+    d.w = rm.neghalf(rm.mul(om.x, Q.x) + rm.mul(om.y, Q.y) + rm.mul(om.z, Q.z));
+    Q.w = Q.w + rm.mul(d.w, delta_t);
+    Q.x = Q.x + rm.mul(d.x, delta_t);
+    Q.y = Q.y + rm.mul(d.y, delta_t);
+    Q.z = Q.z + rm.mul(d.z, delta_t);
+  }
   const double norm2 = rm.mul(Q.w, Q.w) + (rm.mul(Q.x, Q.x) + rm.mul(Q.y, Q.y) + rm.mul(Q.z, Q.z));
   if (norm2 <= 1e-9) {
     Q = {1.0, 0.0, 0.0, 0.0};
-  } else {
+  } else if (!(Shortcuts && norm2 == 1.0)) {  // norm2 == 1: 1/sqrt(1) = 1 and Q * 1 = Q exactly
     const double inv = 1.0 / sqrt(norm2);
     Q = {rm.mul(Q.w, inv), rm.mul(Q.x, inv), rm.mul(Q.y, inv), rm.mul(Q.z, inv)};
   }
@@ -137,7 +131,9 @@ __device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& 
   return o;
 }
 
-template <int Mode = 0>
+// Fused = true (the fused prolog kernels) takes the exact spin-free and unit
+// norm shortcuts of prolog_math; the operator kernel runs the plain formula.
+template <int Mode = 0, bool Fused = false>
 __device__ __forceinline__ void prolog_one(const PArrays& P, uint64_t s, double delta_t, double half_delta_t,
                                            double delta_t2_2) {
   auto load = [&]() {
@@ -152,13 +148,13 @@ __device__ __forceinline__ void prolog_one(const PArrays& P, uint64_t s, double 
   };
   RotMul<Mode> rm;
   LinMul<Mode> lm;
-  ProlState o = prolog_math(rm, lm, load(), delta_t, half_delta_t, delta_t2_2);
+  ProlState o = prolog_math<RotMul<Mode>, LinMul<Mode>, Fused>(rm, lm, load(), delta_t, half_delta_t, delta_t2_2);
   if (rm.failed() || lm.failed()) {
     // nothing is stored yet: reload the inputs (the barrier keeps the main
     // path from holding them in registers for this rare case)
     asm volatile("" ::: "memory");
     MulFP64 n;
-    o = prolog_math(n, n, load(), delta_t, half_delta_t, delta_t2_2);
+    o = prolog_math<MulFP64, MulFP64, Fused>(n, n, load(), delta_t, half_delta_t, delta_t2_2);
   }
   P.f[RX][s] = o.r.x;
   P.f[RY][s] = o.r.y;

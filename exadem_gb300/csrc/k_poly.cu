@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_poly_fused_prolog(PolyA
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;
   if (s < a.n) {
-    prolog_one<Mode>(a.P, s, delta_t, half_delta_t, delta_t2_2);
+    prolog_one<Mode, true>(a.P, s, delta_t, half_delta_t, delta_t2_2);
     const ShapeDev& sh = a.shapes[a.P.type[s]];
     const double h = a.P.f[HOM][s];
     const V3 p = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
@@ -1161,6 +1161,24 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
   }
 }
 
+// Fast (the fused step): the contact law with the exact rolling-clip shortcut
+// (contact_force_core_m, rolling_clip_mur0); the operator path keeps the
+// formula as written.
+template <bool Fast>
+__device__ __forceinline__ void hooke(bool cohesive, double dn, V3 n, double dt, const dem_contact_params& hkp,
+                                      double meff, V3& ft, V3 cpos, V3 pos_i, V3 vel_i, V3& f_i, V3& mom_i,
+                                      V3 vrot_i, V3 pos_j, V3 vel_j, V3 vrot_j) {
+  if (Fast) {
+    MulFP64 mm;
+    contact_force_core_m(mm, cohesive, dn, n, dt, hkp, meff, ft, cpos, pos_i, vel_i, f_i, mom_i, vrot_i, pos_j,
+                         vel_j, vrot_j);
+  } else {
+    contact_force_core(cohesive, dn, n, dt, hkp, meff, ft, cpos, pos_i, vel_i, f_i, mom_i, vrot_i, pos_j, vel_j,
+                       vrot_j);
+  }
+}
+
+template <bool Fast>
 __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
   const uint64_t n2 = a.cnt[1];
   if (blockIdx.x == 0 && threadIdx.x == 0) *a.n_active = n2;
@@ -1179,9 +1197,9 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
       const DriverDev& d = a.drv[a.I.partner[k]];
       const V3 r = ldv(a.P, RX, p), v = ldv(a.P, VX, p), w_ = ldv(a.P, WX, p);
       const double meff = a.P.f[MASS][p];
-      contact_force_core(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, r, v, f, mo, w_,
-                         mk(d.center[0], d.center[1], d.center[2]), mk(d.vel[0], d.vel[1], d.vel[2]),
-                         mk(d.vrot[0], d.vrot[1], d.vrot[2]));
+      hooke<Fast>(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, r, v, f, mo, w_,
+                  mk(d.center[0], d.center[1], d.center[2]), mk(d.vel[0], d.vel[1], d.vel[2]),
+                  mk(d.vrot[0], d.vrot[1], d.vrot[2]));
       pwrite(a, k, ft, mo, f, cross(cpos - r, f) + mo, mk(0, 0, 0));
       continue;
     }
@@ -1191,7 +1209,7 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
     const V3 w_i = ldv(a.P, WX, R.ip), w_j = ldv(a.P, WX, R.jp);
     const double m_i = a.P.f[MASS][R.ip], m_j = a.P.f[MASS][R.jp];
     const double meff = (m_i * m_j) / (m_i + m_j);
-    contact_force_core(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, r_i, v_i, f, mo, w_i, r_j, v_j, w_j);
+    hooke<Fast>(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, r_i, v_i, f, mo, w_i, r_j, v_j, w_j);
     const V3 t_i = cross(cpos - r_i, f) + mo;
     const V3 t_j = cross(cpos - r_j, -f) + (-mo);
     if ((meta >> 15) & 1u)
@@ -1486,7 +1504,10 @@ int launch_contact_poly(dem_ctx* c) {
   a.cnt = c->d_scalars + 3;
   a.n_active = c->d_scalars + 1;
   if (c->ni) k_pdetect<<<grid_for(c->ni, PT), PT, 0, c->stream>>>(a);
-  k_phooke<<<(unsigned)c->num_sms * 8u, PT, 0, c->stream>>>(a);
+  if (c->prm.fused_step)
+    k_phooke<true><<<(unsigned)c->num_sms * 8u, PT, 0, c->stream>>>(a);
+  else
+    k_phooke<false><<<(unsigned)c->num_sms * 8u, PT, 0, c->stream>>>(a);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

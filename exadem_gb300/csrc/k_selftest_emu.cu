@@ -1,7 +1,9 @@
-// k_selftest_emu.cu -- GPU self-test of the integer-pipe binary64 multiply
-// (emu64.cuh) against the hardware multiply, and a probe of the multiply
-// rates of the FP64 pipe, the integer pipe, and both together.
+// k_selftest_emu.cu -- GPU self-tests of the integer-pipe binary64 multiply
+// (emu64.cuh) against the hardware multiply and of the rolling-clip shortcut
+// (contact_core.cuh) against the formula, and a probe of the multiply rates
+// of the FP64 pipe, the integer pipe, and both together.
 #include "../../include/dem_selftest.h"
+#include "contact_core.cuh"
 #include "dem_ctx.cuh"
 #include "emu64.cuh"
 
@@ -60,6 +62,64 @@ __global__ void k_emu_test(uint64_t n, uint64_t seed, unsigned long long* bad) {
     nbad += same_bits(dem::emu_mulnhalf(a), __dmul_rn(a, -0.5)) ? 0 : 1;
   }
   atomicAdd(bad, nbad);
+}
+
+// operand for the rolling-clip test: magnitudes around the range bounds of
+// rolling_clip_mur0 (2^-200, 2^200, 2^500), typical values, zeros,
+// subnormals, infinities and NaNs
+__device__ double draw_clip(uint64_t h) {
+  const uint64_t sign = (h & 1) << 63;
+  const int cls = (int)((h >> 1) % 10);
+  const uint64_t frac = (h >> 12) & 0xfffffffffffffull;
+  const uint64_t r = h >> 5;
+  uint64_t e;
+  switch (cls) {
+    case 0: case 1: case 2: e = 1023 - 30 + (r % 60); break;   // typical
+    case 3: e = 1023 - 203 + (r % 7); break;                    // near 2^-200
+    case 4: e = 1023 + 197 + (r % 7); break;                    // near 2^200
+    case 5: e = 1023 + 497 + (r % 7); break;                    // near 2^500
+    case 6: return __longlong_as_double((long long)sign);        // signed zero
+    case 7: e = 0; break;                                       // subnormal
+    case 8: e = 1 + (r % 2046); break;                          // any normal
+    default: e = 2047; break;                                   // inf / NaN
+  }
+  return __longlong_as_double((long long)(sign | (e << 52) | frac));
+}
+
+__global__ void k_clip_test(uint64_t n, uint64_t seed, unsigned long long* bad, unsigned long long* fast) {
+  unsigned long long nbad = 0, nfast = 0;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+    uint64_t h = mix(seed ^ (16 * t));
+    double v[12];
+    for (int q = 0; q < 12; q++) {
+      v[q] = draw_clip(h);
+      h = mix(h ^ (uint64_t)(q + 1));
+    }
+    if ((t & 3) == 0) v[3] = v[4] = v[5] = 0.0;  // no spin: the 0/0 case
+    const dem::V3 branch = dem::mk(v[0], v[1], v[2]), vrot = dem::mk(v[3], v[4], v[5]);
+    const dem::V3 fn = dem::mk(v[6], v[7], v[8]);
+    dem::V3 m1 = dem::mk(v[9], v[10], v[11]), m2 = m1;
+    dem::rolling_clip_mur0(branch, vrot, fn, m1);
+    {  // the formula of contact_force_core
+      dem::V3 b = branch;
+      const double r = (dem::dot(b, vrot)) / (dem::dot(vrot, vrot));
+      b = b - r * vrot;
+      const double mur = 0;
+      const double threshold_mom = fabs(mur * dem::vnorm(b) * dem::vnorm(fn));
+      const double mom_square = dem::dot(m2, m2);
+      if (mom_square > 0.0 && mom_square > threshold_mom * threshold_mom)
+        m2 = m2 * (threshold_mom / sqrt(mom_square));
+    }
+    nbad += (same_bits(m1.x, m2.x) && same_bits(m1.y, m2.y) && same_bits(m1.z, m2.z)) ? 0 : 1;
+    nfast += (dem::exp_below(v[0], 200) && dem::exp_below(v[1], 200) && dem::exp_below(v[2], 200) &&
+              dem::exp_below(v[6], 500) && dem::exp_below(v[7], 500) && dem::exp_below(v[8], 500) &&
+              dem::exp_below(v[3], 200) && dem::exp_below(v[4], 200) && dem::exp_below(v[5], 200) &&
+              (dem::exp_at_least(v[3], -200) || dem::exp_at_least(v[4], -200) || dem::exp_at_least(v[5], -200)))
+                 ? 1
+                 : 0;
+  }
+  atomicAdd(bad, nbad);
+  atomicAdd(fast, nfast);
 }
 
 // NN chains multiplied on the FP64 pipe and NE chains on the integer pipe,
@@ -123,6 +183,21 @@ extern "C" int dem_selftest_emu_mul(uint64_t n, uint64_t seed, uint64_t* mismatc
   cudaFree(d);
   if (!ok || cudaGetLastError() != cudaSuccess) return DEM_ERR_CUDA;
   *mismatches = h;
+  return DEM_OK;
+}
+
+extern "C" int dem_selftest_rolling_clip(uint64_t n, uint64_t seed, uint64_t* mismatches, uint64_t* fast_path_taken) {
+  if (!mismatches || !fast_path_taken) return DEM_ERR_INVALID_ARG;
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return DEM_ERR_CUDA;
+  cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+  k_clip_test<<<1216, 256>>>(n, seed, d, d + 1);
+  unsigned long long h[2] = {0, 0};
+  const bool ok = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost) == cudaSuccess;
+  cudaFree(d);
+  if (!ok || cudaGetLastError() != cudaSuccess) return DEM_ERR_CUDA;
+  *mismatches = h[0];
+  *fast_path_taken = h[1];
   return DEM_OK;
 }
 

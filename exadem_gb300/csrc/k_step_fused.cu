@@ -208,39 +208,56 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
   }
 }
 
-__global__ void __launch_bounds__(FT) k_chooke(CArgs a) {
+// The Hooke law on the contacts found by k_cdetect.  Mode bit 2 (instance 1):
+// its multiplies on the integer pipe (contact_force_core_m); an operand outside
+// that fast path makes the pair run again on the FP64 pipe from its stored
+// inputs (nothing is written before write_result).
+template <int Mode>
+__global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
   const uint64_t n2 = a.cnt[1];
   if (blockIdx.x == 0 && threadIdx.x == 0) *a.n_active = n2;  // every L2 pair overlaps (dn < 0)
   const uint64_t stride = (uint64_t)gridDim.x * FT;
   for (uint64_t w = (uint64_t)blockIdx.x * FT + threadIdx.x; w < n2; w += stride) {
     const uint32_t k = a.L2[w];
-    const double dn = a.D[0][w];
-    const V3 n = mk(a.D[1][w], a.D[2][w], a.D[3][w]);
-    const V3 cpos = mk(a.D[4][w], a.D[5][w], a.D[6][w]);
-    const uint32_t meta = a.I.meta[k];
-    const uint32_t i = a.I.owner[k], j = a.I.partner[k];
-    const V3 ri = ldv(a.P, RX, i);
-    V3 ft = mk(a.I.ft[0][k], a.I.ft[1][k], a.I.ft[2][k]);
-    V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
-    V3 f = mk(0, 0, 0), ti, tj = mk(0, 0, 0);
-    const V3 vi = ldv(a.P, VX, i);
-    const V3 wi = ldv(a.P, WX, i);
-    if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
-      const V3 rj = partner_pos(a, meta, i, j);
-      const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
-      const double m_i = a.P.f[MASS][i], m_j = a.P.f[MASS][j];
-      const double meff = (m_i * m_j) / (m_i + m_j);
-      contact_force_core(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, ri, vi, f, mo, wi, rj, vj, wj);
-      ti = cross(cpos - ri, f) + mo;
-      tj = cross(cpos - rj, -f) + (-mo);
-    } else {
-      const DriverDev& d = a.drv[j];
-      const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
-      const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
-      const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
-      const double meff = a.P.f[MASS][i];
-      contact_force_core(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, ri, vi, f, mo, wi, dpos, dvel, dvrot);
-      ti = cross(cpos - ri, f) + mo;
+    auto run = [&](auto& mm, V3& ft, V3& mo, V3& f, V3& ti, V3& tj) {
+      const double dn = a.D[0][w];
+      const V3 n = mk(a.D[1][w], a.D[2][w], a.D[3][w]);
+      const V3 cpos = mk(a.D[4][w], a.D[5][w], a.D[6][w]);
+      const uint32_t meta = a.I.meta[k];
+      const uint32_t i = a.I.owner[k], j = a.I.partner[k];
+      const V3 ri = ldv(a.P, RX, i);
+      ft = mk(a.I.ft[0][k], a.I.ft[1][k], a.I.ft[2][k]);
+      mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+      f = mk(0, 0, 0);
+      tj = mk(0, 0, 0);
+      const V3 vi = ldv(a.P, VX, i);
+      const V3 wi = ldv(a.P, WX, i);
+      if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
+        const V3 rj = partner_pos(a, meta, i, j);
+        const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
+        const double m_i = a.P.f[MASS][i], m_j = a.P.f[MASS][j];
+        const double meff = mm.mul(m_i, m_j) / (m_i + m_j);
+        contact_force_core_m(mm, a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, ri, vi, f, mo, wi, rj, vj, wj);
+        ti = cross_m(mm, cpos - ri, f) + mo;
+        tj = cross_m(mm, cpos - rj, -f) + (-mo);
+      } else {
+        const DriverDev& d = a.drv[j];
+        const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
+        const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
+        const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
+        const double meff = a.P.f[MASS][i];
+        contact_force_core_m(mm, a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, ri, vi, f, mo, wi, dpos, dvel,
+                             dvrot);
+        ti = cross_m(mm, cpos - ri, f) + mo;
+      }
+    };
+    V3 ft, mo, f, ti, tj;
+    RotMul<Mode> mm;
+    run(mm, ft, mo, f, ti, tj);
+    if (mm.failed()) {
+      asm volatile("" ::: "memory");
+      MulFP64 nm;
+      run(nm, ft, mo, f, ti, tj);
     }
     write_result(a, k, ft, mo, f, ti, tj);
   }
@@ -252,7 +269,7 @@ __global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_prolog(PArrays P,
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool over = false;
   if (s < n) {
-    prolog_one<Mode>(P, s, delta_t, half_delta_t, delta_t2_2);
+    prolog_one<Mode, true>(P, s, delta_t, half_delta_t, delta_t2_2);
     const double dx = P.f[RX][s] - P.f[BX][s], dy = P.f[RY][s] - P.f[BY][s], dz = P.f[RZ][s] - P.f[BZ][s];
     over = dx * dx + dy * dy + dz * dz >= thr2;
     if (over && sv.nsys > 1) atomicOr(&sv.trig[sv.of(s)], 1u);  // this system's own trigger
@@ -400,15 +417,24 @@ int launch_fused_prolog(dem_ctx* c) {
 
 int launch_contact_compact(dem_ctx* c) {
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 3, 0, 2 * sizeof(unsigned long long), c->stream));
-  ProfScope ps(c, K_CONTACT, 3);
   const CArgs a = make_cargs(c);
   const unsigned persistent = (unsigned)c->num_sms * (unsigned)c->tune_contact_bps;
-  if (c->capturing)
-    k_cscreen<<<persistent, FT, 0, c->stream>>>(a);
-  else if (c->ni)
-    k_cscreen<<<grid_for(c->ni, FT), FT, 0, c->stream>>>(a);
-  k_cdetect<<<persistent, FT, 0, c->stream>>>(a);
-  k_chooke<<<persistent, FT, 0, c->stream>>>(a);
+  {
+    ProfScope ps(c, K_CSCREEN, c->capturing || c->ni ? 1 : 0);
+    if (c->capturing)
+      k_cscreen<<<persistent, FT, 0, c->stream>>>(a);
+    else if (c->ni)
+      k_cscreen<<<grid_for(c->ni, FT), FT, 0, c->stream>>>(a);
+  }
+  {
+    ProfScope ps(c, K_CDETECT, 1);
+    k_cdetect<<<persistent, FT, 0, c->stream>>>(a);
+  }
+  {
+    ProfScope ps(c, K_CONTACT, 1);  // the Hooke law on the contacts
+    const auto kh = (c->mul_mode & 4) ? k_chooke<1> : k_chooke<0>;  // mode bit 2: the contact law
+    kh<<<persistent, FT, 0, c->stream>>>(a);
+  }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

@@ -331,9 +331,10 @@ int dem_autotune(dem_ctx* ctx, int steps_per_trial, int skin_policy, dem_tune_re
  * built from integer partial products runs on the otherwise idle integer pipe
  * and returns the same bits.  mode bit 0: rotation multiplies (quaternion
  * rotations and derivative, normalisation, Euler terms) on the integer pipe;
- * bit 1: the other multiplies (Verlet pushes, gravity, quotient estimates).
- * 0 = FP64 pipe only.  Results are identical in every mode.  Default 1; the
- * autotuner picks the fastest for the sphere step.                         */
+ * bit 1: the other multiplies (Verlet pushes, quotient estimates); bit 2:
+ * the sphere contact law's multiplies.  0 = FP64 pipe only.  Results are
+ * identical in every mode (0..7).  Default 1; the autotuner picks the fastest
+ * for the sphere step.                                                     */
 int dem_set_mul_mode(dem_ctx* ctx, int mode);
 int dem_get_mul_mode(dem_ctx* ctx, int* mode);
 /* Number of neighbour rebuilds done so far (trigger_move_particles count). */

@@ -29,6 +29,12 @@ int dem_selftest_poly_decisions(uint64_t n, uint64_t seed, uint64_t* counts);
  * bit from the hardware multiply.                                          */
 int dem_selftest_emu_mul(uint64_t n, uint64_t seed, uint64_t* mismatches);
 
+/* Draws n seeded (branch, spin, normal force, moment) cases around the range
+ * bounds of the exact rolling-clip shortcut (mur = 0) and counts the moments
+ * that differ in any bit from the formula (r = b.w / w.w, ... , m * t/|m|);
+ * fast_path_taken counts the cases inside the shortcut's range.            */
+int dem_selftest_rolling_clip(uint64_t n, uint64_t seed, uint64_t* mismatches, uint64_t* fast_path_taken);
+
 /* Multiply throughput in G multiplies/s over all SMs, dependent chains, 8
  * blocks of 256 threads per SM: gops[0] FP64 pipe alone, gops[1] integer pipe
  * alone (emu_dmul), gops[2..4] both in the same threads, with native:emulated

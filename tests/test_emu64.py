@@ -37,3 +37,11 @@ def test_mul_rates_probe(native_lib):
     assert native_lib.dem_probe_mul_rates(4096, g) == 0
     print("multiply rates, G/s: fp64 %.0f  integer %.0f  both 4:4 %.0f  4:2 %.0f  2:4 %.0f" % tuple(g))
     assert all(x > 0 for x in g)
+
+
+@pytest.mark.gpu
+def test_rolling_clip_shortcut_bit_exact(native_lib):
+    bad, fast = C.c_uint64(0), C.c_uint64(0)
+    assert native_lib.dem_selftest_rolling_clip(50_000_000, 77, C.byref(bad), C.byref(fast)) == 0
+    assert bad.value == 0
+    assert fast.value > 1_000_000  # both the shortcut and the formula are exercised

@@ -25,7 +25,7 @@ def test_mul_modes_same_bits_drum(native_lib):
     rng = np.random.default_rng(31)
     for k in ("vrotx", "vroty", "vrotz"):
         w.particles[k] = rng.uniform(-5.0, 5.0, w.n)
-    runs = [_run(w, m, 300) for m in range(4)]
+    runs = [_run(w, m, 300) for m in (0, 1, 2, 3, 4, 7)]
     ref = runs[0].particles(sort_by_id=True)
     assert np.abs(ref["vrotx"]).max() > 0
     for s in runs[1:]:
@@ -45,11 +45,17 @@ def test_mul_modes_same_bits_spinning_polyhedra(native_lib):
         assert s.rebuild_count() == runs[0].rebuild_count()
 
 
-def test_mul_mode_integer_pipe_matches_oracle(native_lib):
-    """All multiplies of the integration on the integer pipe (mode 3) against the oracle."""
-    w = W.spheres_drum(n=3000, seed=41, fused_step=1, fp32_contact_screen=1, fp32_broad_phase=1)
+@pytest.mark.parametrize("case", ["drum", "cohesive_floor"])
+def test_mul_mode_integer_pipe_matches_oracle(native_lib, case):
+    """Every placement on the integer pipe (mode 7: integration and contact law)
+    against the oracle, for the plain Hooke law (a drum) and the cohesive one."""
+    flags = dict(fused_step=1, fp32_contact_screen=1, fp32_broad_phase=1)
+    if case == "drum":
+        w = W.spheres_drum(n=3000, seed=41, **flags)
+    else:
+        w = W.spheres_floor(n=4000, side=14.0, seed=41, **flags)
     g, o = pair(w)
-    g.set_mul_mode(3)
+    g.set_mul_mode(7)
     for s in (g, o):
         s.first_iteration()
         s.step(200)
@@ -63,4 +69,4 @@ def test_mul_mode_validation(native_lib):
     from exadem_gb300 import _abi as A
 
     with pytest.raises(A.DemError):
-        s.set_mul_mode(4)
+        s.set_mul_mode(8)
