@@ -105,8 +105,10 @@ __device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& 
            in.v.z + lm.mul(in.a.z, half_delta_t));
   Q4 Q = in.q;
   const V3 om = in.w;
+  bool still = false;  // spin-free with arot = +0: w = +0 + (dt/2)(+0) stays +0
   if (Shortcuts && spin_free_step(Q, om, delta_t)) {
     Q = spin_free_quaternion(Q);
+    still = (emu_bits(in.arot.x) | emu_bits(in.arot.y) | emu_bits(in.arot.z)) == 0;
   } else {
     Q4 d;
     d.x = rm.half(rm.mul(om.y, Q.z) - rm.mul(om.z, Q.y) + rm.mul(om.x, Q.w));
@@ -126,8 +128,9 @@ __device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& 
     Q = {rm.mul(Q.w, inv), rm.mul(Q.x, inv), rm.mul(Q.y, inv), rm.mul(Q.z, inv)};
   }
   o.q = Q;
-  o.w = mk(om.x + lm.mul(half_delta_t, in.arot.x), om.y + lm.mul(half_delta_t, in.arot.y),
-           om.z + lm.mul(half_delta_t, in.arot.z));
+  if (!still)  // (spin_free_step checked 0 < dt < inf, so (dt/2) * +0 = +0)
+    o.w = mk(om.x + lm.mul(half_delta_t, in.arot.x), om.y + lm.mul(half_delta_t, in.arot.y),
+             om.z + lm.mul(half_delta_t, in.arot.z));
   return o;
 }
 

@@ -145,12 +145,14 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         const double R = rad_i + rad_j;
         const V3 dist = ri - rj;
         const double dist_norm = vnorm(dist);
-        const double inv_dist_norm = 1.0 / dist_norm;
         dn = dist_norm - R;
-        n = dist * inv_dist_norm;
-        cpos = ri - n * (rad_i + 0.5 * dn);
         contact = dn < 0;
         dncut = a.cp.dncut;
+        if (contact || (a.cohesive && dn <= dncut)) {  // n and cpos are used only then
+          const double inv_dist_norm = 1.0 / dist_norm;
+          n = dist * inv_dist_norm;
+          cpos = ri - n * (rad_i + 0.5 * dn);
+        }
       } else {
         const DriverDev& d = a.drv[j];
         if (d.kind == 0) {
