@@ -32,7 +32,7 @@ __device__ __forceinline__ void rolling_clip_mur0(V3 branch, V3 vrot_i, V3 fn, V
                          exp_at_least(vrot_i.z, -200));
   const double mom_square = dot(mom_i, mom_i);
   if (in_range) {
-    if (mom_square > 0.0) mom_i = mom_i * 0.0;
+    if (emu_gt0(mom_square)) mom_i = mom_i * 0.0;
     return;
   }
   const double r = (dot(branch, vrot_i)) / (dot(vrot_i, vrot_i));
@@ -66,7 +66,7 @@ __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, doubl
                                                      V3 pos_i, V3 vel_i, V3& f_i, V3& mom_i, V3 vrot_i, V3 pos_j,
                                                      V3 vel_j, V3 vrot_j) {
   if (cohesive) {
-    if (dn >= 0) {
+    if (emu_ge0(dn)) {  // comparisons of this form on the integer pipe (emu64.cuh)
       const double fn_value = mm.mul(hkp.fc / hkp.dncut, dn) - hkp.fc;
       f_i = f_i + scale_m(mm, fn_value, n);
       ft = mk(0, 0, 0);
@@ -82,10 +82,10 @@ __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, doubl
   {
     const double fne = mm.mul(-hkp.kn, dn);
     const double fnv = mm.mul(damp, vn);
-    double nf = (fnv + fne > 0) ? fnv + fne : 0;
+    double nf = emu_gt0(fnv + fne) ? fnv + fne : 0;
     if (cohesive) {
       const double fn_norm = nf - hkp.fc;
-      nf = fn_norm < (-hkp.fc) ? -hkp.fc : fn_norm;
+      nf = emu_lt(fn_norm, -hkp.fc) ? -hkp.fc : fn_norm;
     }
     fn = scale_m(mm, nf, n);
   }
@@ -103,7 +103,7 @@ __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, doubl
   }
   {
     const double ft_square = dot_m(mm, ft, ft);
-    if (ft_square > 0.0 && ft_square > mm.mul(threshold_ft, threshold_ft)) {
+    if (emu_gt0(ft_square) && emu_gt_nonneg(ft_square, mm.mul(threshold_ft, threshold_ft))) {
       const double s = threshold_ft / sqrt(ft_square);
       ft = mk(mm.mul(ft.x, s), mm.mul(ft.y, s), mm.mul(ft.z, s));
     }

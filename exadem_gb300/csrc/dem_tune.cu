@@ -219,7 +219,10 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
     const float t_steps = tm.stop();
     const uint64_t extra = c->rebuilds - r0;
     const double t_step = std::max(0.0, ((double)t_steps - (double)extra * t_reb) / steps_per_trial);
-    const double interval = vmax > 0 ? std::max(1.0, 0.5 * skin / ((double)vmax * dt)) : 1e9;
+    // rebuild interval of this skin at the fastest particle's speed, at most 50
+    // steps: at rest (vmax = 0, the start of a deposition) rebuild cost still counts
+    const double interval =
+        vmax > 0 ? std::min(50.0, std::max(1.0, 0.5 * skin / ((double)vmax * dt))) : 50.0;
     *cost = t_step + t_reb / interval;
     trials++;
     return restore_state(c, base);

@@ -190,4 +190,36 @@ EMU_HD double emu_mulnhalf(double x) {
   return emu_native_mul(x, -0.5);
 }
 
+// IEEE comparisons decided from the bits on the integer pipe (an FP64
+// compare occupies the FP64 pipe like an add).  NaN compares false; -0 and +0
+// compare equal.
+EMU_HD bool emu_gt0(double x) {  // x > 0
+  const uint64_t b = emu_bits(x);
+  return (int64_t)b > 0 && b <= 0x7ff0000000000000ull;
+}
+EMU_HD bool emu_lt0(double x) {  // x < 0
+  const uint64_t b = emu_bits(x);
+  return b > 0x8000000000000000ull && b <= 0xfff0000000000000ull;
+}
+EMU_HD bool emu_ge0(double x) { return !emu_lt0(x) && (emu_bits(x) << 1) <= 0xffe0000000000000ull; }  // x >= 0
+EMU_HD bool emu_le0(double x) { return !emu_gt0(x) && (emu_bits(x) << 1) <= 0xffe0000000000000ull; }  // x <= 0
+// order key: monotone in the value, equal for -0 and +0 (caller excludes NaN)
+EMU_HD uint64_t emu_key(double x) {
+  uint64_t b = emu_bits(x);
+  if ((b << 1) == 0) b = 0;
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+EMU_HD bool emu_isnan(double x) { return (emu_bits(x) << 1) > 0xffe0000000000000ull; }
+EMU_HD bool emu_lt(double a, double b) { return !emu_isnan(a) && !emu_isnan(b) && emu_key(a) < emu_key(b); }
+EMU_HD bool emu_le(double a, double b) { return !emu_isnan(a) && !emu_isnan(b) && emu_key(a) <= emu_key(b); }
+// a > b and a >= b for a, b that are +0, positive or NaN (sums of squares)
+EMU_HD bool emu_gt_nonneg(double a, double b) {
+  const uint64_t ua = emu_bits(a), ub = emu_bits(b);
+  return ua > ub && ua <= 0x7ff0000000000000ull;
+}
+EMU_HD bool emu_ge_nonneg(double a, double b) {
+  const uint64_t ua = emu_bits(a), ub = emu_bits(b);
+  return ua >= ub && ua <= 0x7ff0000000000000ull && ub <= 0x7ff0000000000000ull;
+}
+
 }  // namespace dem

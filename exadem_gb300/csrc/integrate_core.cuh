@@ -28,7 +28,7 @@ namespace dem {
 // div_rn (math_exact.cuh) with its quotient estimate a*y through M
 template <class M>
 __device__ __forceinline__ double div_rn_m(M& mm, double a, double b, double y) {
-  if (a == 0.0) return mm.mul(a, y);
+  if ((emu_bits(a) << 1) == 0) return mm.mul(a, y);  // a == 0, decided on the integer pipe
   if (exp_in_safe_range(a) && exp_in_safe_range(b)) {
     const double q = mm.mul(a, y);
     const double r = fma(-q, b, a);
@@ -94,21 +94,17 @@ __device__ __forceinline__ Q4 spin_free_quaternion(const Q4& Q) {
   return Q4{step(bw, sw, dw), step(bx, sx, dx), step(by, sy, dy), step(bz, sz, dz)};
 }
 
-template <class R, class L, bool Shortcuts = false>
-__device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& in, double delta_t,
-                                                 double half_delta_t, double delta_t2_2) {
-  ProlState o = in;
-  o.r = mk(in.r.x + (lm.mul(in.v.x, delta_t) + lm.mul(in.a.x, delta_t2_2)),
-           in.r.y + (lm.mul(in.v.y, delta_t) + lm.mul(in.a.y, delta_t2_2)),
-           in.r.z + (lm.mul(in.v.z, delta_t) + lm.mul(in.a.z, delta_t2_2)));
-  o.v = mk(in.v.x + lm.mul(in.a.x, half_delta_t), in.v.y + lm.mul(in.a.y, half_delta_t),
-           in.v.z + lm.mul(in.a.z, half_delta_t));
-  Q4 Q = in.q;
-  const V3 om = in.w;
+// The rotational half of the prolog: Q <- normalize(Q + dot(Q, w) dt) and
+// w += dt/2 arot.  spin_free: the caller has checked spin_free_step, and the
+// signed-zero derivative replaces the 24 FP64 operations.
+template <class R, class L, bool Shortcuts>
+__device__ __forceinline__ void quat_math(R& rm, L& lm, Q4& Q, V3& w, V3 arot, bool spin_free, double delta_t,
+                                          double half_delta_t) {
+  const V3 om = w;
   bool still = false;  // spin-free with arot = +0: w = +0 + (dt/2)(+0) stays +0
-  if (Shortcuts && spin_free_step(Q, om, delta_t)) {
+  if (Shortcuts && spin_free) {
     Q = spin_free_quaternion(Q);
-    still = (emu_bits(in.arot.x) | emu_bits(in.arot.y) | emu_bits(in.arot.z)) == 0;
+    still = (emu_bits(arot.x) | emu_bits(arot.y) | emu_bits(arot.z)) == 0;
   } else {
     Q4 d;
     d.x = rm.half(rm.mul(om.y, Q.z) - rm.mul(om.z, Q.y) + rm.mul(om.x, Q.w));
@@ -121,17 +117,113 @@ __device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& 
     Q.z = Q.z + rm.mul(d.z, delta_t);
   }
   const double norm2 = rm.mul(Q.w, Q.w) + (rm.mul(Q.x, Q.x) + rm.mul(Q.y, Q.y) + rm.mul(Q.z, Q.z));
-  if (norm2 <= 1e-9) {
+  // Shortcuts compare on the integer pipe: norm2 is +0, positive or NaN, so
+  // its bits order like its value (NaN above every number)
+  const uint64_t nb = emu_bits(norm2);
+  if (Shortcuts ? nb <= 0x3e112e0be826d695ull /* bits of 1e-9 */ : norm2 <= 1e-9) {
     Q = {1.0, 0.0, 0.0, 0.0};
-  } else if (!(Shortcuts && norm2 == 1.0)) {  // norm2 == 1: 1/sqrt(1) = 1 and Q * 1 = Q exactly
+  } else if (!(Shortcuts && nb == 0x3ff0000000000000ull)) {  // norm2 == 1: 1/sqrt(1) = 1 and Q * 1 = Q exactly
     const double inv = 1.0 / sqrt(norm2);
     Q = {rm.mul(Q.w, inv), rm.mul(Q.x, inv), rm.mul(Q.y, inv), rm.mul(Q.z, inv)};
   }
-  o.q = Q;
   if (!still)  // (spin_free_step checked 0 < dt < inf, so (dt/2) * +0 = +0)
-    o.w = mk(om.x + lm.mul(half_delta_t, in.arot.x), om.y + lm.mul(half_delta_t, in.arot.y),
-             om.z + lm.mul(half_delta_t, in.arot.z));
+    w = mk(om.x + lm.mul(half_delta_t, arot.x), om.y + lm.mul(half_delta_t, arot.y),
+           om.z + lm.mul(half_delta_t, arot.z));
+}
+
+// The translational half: x += v dt + a dt^2/2; v += a dt/2
+template <class L>
+__device__ __forceinline__ void transl_math(L& lm, V3& r, V3& v, V3 a, double delta_t, double half_delta_t,
+                                            double delta_t2_2) {
+  r = mk(r.x + (lm.mul(v.x, delta_t) + lm.mul(a.x, delta_t2_2)), r.y + (lm.mul(v.y, delta_t) + lm.mul(a.y, delta_t2_2)),
+         r.z + (lm.mul(v.z, delta_t) + lm.mul(a.z, delta_t2_2)));
+  v = mk(v.x + lm.mul(a.x, half_delta_t), v.y + lm.mul(a.y, half_delta_t), v.z + lm.mul(a.z, half_delta_t));
+}
+
+template <class R, class L, bool Shortcuts = false>
+__device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& in, double delta_t,
+                                                 double half_delta_t, double delta_t2_2) {
+  ProlState o = in;
+  transl_math(lm, o.r, o.v, in.a, delta_t, half_delta_t, delta_t2_2);
+  quat_math<R, L, Shortcuts>(rm, lm, o.q, o.w, in.arot, Shortcuts && spin_free_step(in.q, in.w, delta_t), delta_t,
+                             half_delta_t);
   return o;
+}
+
+// Split form of the fused sphere prolog.  prolog_cheap: the translation and,
+// for a spin-free particle, its rotational half; returns true when the
+// particle spins (its rotational half is left to prolog_rotation).  The two
+// halves read disjoint inputs and write disjoint outputs, so running them in
+// separate launches gives the same bits as prolog_math.
+template <int Mode>
+__device__ __forceinline__ bool prolog_cheap(const PArrays& P, uint64_t s, double delta_t, double half_delta_t,
+                                             double delta_t2_2) {
+  const Q4 q0 = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+  const V3 w0 = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+  const bool spin_free = spin_free_step(q0, w0, delta_t);
+  auto run = [&](auto& rm, auto& lm, V3& r, V3& v, Q4& q, V3& w) {
+    r = mk(P.f[RX][s], P.f[RY][s], P.f[RZ][s]);
+    v = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
+    transl_math(lm, r, v, mk(P.f[FX][s], P.f[FY][s], P.f[FZ][s]), delta_t, half_delta_t, delta_t2_2);
+    q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+    w = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+    if (spin_free)
+      quat_math<std::remove_reference_t<decltype(rm)>, std::remove_reference_t<decltype(lm)>, true>(
+          rm, lm, q, w, mk(P.f[AX][s], P.f[AY][s], P.f[AZ][s]), true, delta_t, half_delta_t);
+  };
+  RotMul<Mode> rm;
+  LinMul<Mode> lm;
+  V3 r, v, w;
+  Q4 q;
+  run(rm, lm, r, v, q, w);
+  if (rm.failed() || lm.failed()) {
+    asm volatile("" ::: "memory");  // nothing is stored yet: reload
+    MulFP64 n;
+    run(n, n, r, v, q, w);
+  }
+  P.f[RX][s] = r.x;
+  P.f[RY][s] = r.y;
+  P.f[RZ][s] = r.z;
+  P.f[VX][s] = v.x;
+  P.f[VY][s] = v.y;
+  P.f[VZ][s] = v.z;
+  if (spin_free) {
+    P.f[QW][s] = q.w;
+    P.f[QX][s] = q.x;
+    P.f[QY][s] = q.y;
+    P.f[QZ][s] = q.z;
+    P.f[WX][s] = w.x;
+    P.f[WY][s] = w.y;
+    P.f[WZ][s] = w.z;
+  }
+  return !spin_free;
+}
+
+template <int Mode>
+__device__ __forceinline__ void prolog_rotation(const PArrays& P, uint64_t s, double delta_t, double half_delta_t) {
+  auto run = [&](auto& rm, auto& lm, Q4& q, V3& w) {
+    q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
+    w = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
+    quat_math<std::remove_reference_t<decltype(rm)>, std::remove_reference_t<decltype(lm)>, true>(
+        rm, lm, q, w, mk(P.f[AX][s], P.f[AY][s], P.f[AZ][s]), false, delta_t, half_delta_t);
+  };
+  RotMul<Mode> rm;
+  LinMul<Mode> lm;
+  Q4 q;
+  V3 w;
+  run(rm, lm, q, w);
+  if (rm.failed() || lm.failed()) {
+    asm volatile("" ::: "memory");
+    MulFP64 n;
+    run(n, n, q, w);
+  }
+  P.f[QW][s] = q.w;
+  P.f[QX][s] = q.x;
+  P.f[QY][s] = q.y;
+  P.f[QZ][s] = q.z;
+  P.f[WX][s] = w.x;
+  P.f[WY][s] = w.y;
+  P.f[WZ][s] = w.z;
 }
 
 // Fused = true (the fused prolog kernels) takes the exact spin-free and unit

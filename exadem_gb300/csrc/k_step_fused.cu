@@ -146,9 +146,9 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         const V3 dist = ri - rj;
         const double dist_norm = vnorm(dist);
         dn = dist_norm - R;
-        contact = dn < 0;
+        contact = emu_lt0(dn);  // comparisons of this kernel on the integer pipe (emu64.cuh)
         dncut = a.cp.dncut;
-        if (contact || (a.cohesive && dn <= dncut)) {  // n and cpos are used only then
+        if (contact || (a.cohesive && emu_le(dn, dncut))) {  // n and cpos are used only then
           const double inv_dist_norm = 1.0 / dist_norm;
           n = dist * inv_dist_norm;
           cpos = ri - n * (rad_i + 0.5 * dn);
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
           const V3 s2p = -(mk(d.center_proj[0], d.center_proj[1], d.center_proj[2]) - proj);
           const double dd = vnorm(s2p);
           dn = dd - rad_i;
-          contact = !(dn > 0);
+          contact = !emu_gt0(dn);
           if (contact) {
             n = s2p / dd;
             cpos = ri - n * (rad_i + 0.5 * dn);
@@ -171,7 +171,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
           const V3 dir = mk(d.center[0], d.center[1], d.center[2]) - proj;
           const double dd = vnorm(dir);
           dn = d.radius - (rad_i + dd);
-          contact = !(dn > 0);
+          contact = !emu_gt0(dn);
           if (contact) {
             n = dir / dd;
             cpos = ri - n * (rad_i + 0.5 * dn);
@@ -179,12 +179,12 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         }
         dncut = a.cpd.dncut;
       }
-      if (a.cohesive) contact = (contact || dn <= dncut);
+      if (a.cohesive) contact = (contact || emu_le(dn, dncut));
       const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
       if (!contact) {
         const V3 z = mk(0, 0, 0);
         write_result(a, k, z, z, z, z, z);
-      } else if (a.cohesive && dn >= 0) {
+      } else if (a.cohesive && emu_ge0(dn)) {
         // cohesive attraction before contact (contact_force.hpp:165-173): f = fn_value n, ft = 0
         const dem_contact_params& hkp = is_vv ? a.cp : a.cpd;
         const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
@@ -265,18 +265,45 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
   }
 }
 
+// prolog + displacement trigger.  Every particle gets its translation and, when
+// it does not spin, its (exact, integer sign logic) quaternion step here; the
+// spinning particles run the full quaternion update in place when most of their
+// warp spins, otherwise through prl_list in k_prolog_rotation, so sparse
+// spinning particles do not hold whole warps on the FP64 pipe.  The trigger
+// depends on positions only.
 template <int Mode>
-__global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_prolog(PArrays P, uint64_t n, double delta_t, double half_delta_t, double delta_t2_2,
-                               double thr2, unsigned long long* flag, SysView sv) {
+__global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_prolog(PArrays P, uint64_t n, double delta_t,
+                                                                     double half_delta_t, double delta_t2_2,
+                                                                     double thr2, unsigned long long* flag,
+                                                                     SysView sv, uint32_t* prl_list,
+                                                                     unsigned long long* prl_cnt) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  bool over = false;
+  bool over = false, need = false;
   if (s < n) {
-    prolog_one<Mode, true>(P, s, delta_t, half_delta_t, delta_t2_2);
+    need = prolog_cheap<Mode>(P, s, delta_t, half_delta_t, delta_t2_2);
     const double dx = P.f[RX][s] - P.f[BX][s], dy = P.f[RY][s] - P.f[BY][s], dz = P.f[RZ][s] - P.f[BZ][s];
-    over = dx * dx + dy * dy + dz * dz >= thr2;
+    over = emu_ge_nonneg(dx * dx + dy * dy + dz * dz, thr2);  // >= on the integer pipe
     if (over && sv.nsys > 1) atomicOr(&sv.trig[sv.of(s)], 1u);  // this system's own trigger
   }
   if (__any_sync(0xffffffffu, over) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+  const unsigned busy = __ballot_sync(0xffffffffu, need);
+  if (__popc(busy) > 24) {
+    if (need) prolog_rotation<Mode>(P, s, delta_t, half_delta_t);
+  } else {
+    const uint32_t pos = warp_append(need, prl_cnt);
+    if (need) prl_list[pos] = (uint32_t)s;
+  }
+}
+
+// the rotational half of the prolog for the particles listed by k_fused_prolog
+template <int Mode>
+__global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_prolog_rotation(PArrays P, const uint32_t* __restrict__ list,
+                                                                        const unsigned long long* cnt, double delta_t,
+                                                                        double half_delta_t) {
+  const uint64_t m = *cnt;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < m; w += stride)
+    prolog_rotation<Mode>(P, list[w], delta_t, half_delta_t);
 }
 
 // reset_force_moment + gravity_force + contact gather + force_to_accel + epilog.
@@ -407,12 +434,20 @@ int launch_fused_prolog(dem_ctx* c) {
   const double delta_t2_2 = delta_t * delta_t * 0.5;
   const double max_displ = c->prm.rcut_inc * 0.5;
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars, 0, sizeof(unsigned long long), c->stream));
-  ProfScope ps(c, K_PROLOG, c->n ? 1 : 0);
+  unsigned long long* prl_cnt = c->d_scalars + SC_ROT_CNT;  // the rotation list is free until the epilog
+  DEM_CUDA_TRY(c, cudaMemsetAsync(prl_cnt, 0, sizeof(unsigned long long), c->stream));
+  ProfScope ps(c, K_PROLOG, c->n ? 2 : 0);
   const auto kern = by_mode(c->mul_mode, k_fused_prolog<0>, k_fused_prolog<1>, k_fused_prolog<2>, k_fused_prolog<3>);
-  if (c->n)
+  const auto krot = by_mode(c->mul_mode, k_prolog_rotation<0>, k_prolog_rotation<1>, k_prolog_rotation<2>,
+                            k_prolog_rotation<3>);
+  if (c->n) {
     kern<<<grid_for(c->n, c->tune_block), c->tune_block, 0, c->stream>>>(c->P[c->pcur], c->n, delta_t, half_delta_t,
                                                                          delta_t2_2, max_displ * max_displ,
-                                                                         c->d_scalars, c->sysview());
+                                                                         c->d_scalars, c->sysview(), c->rot_list,
+                                                                         prl_cnt);
+    krot<<<(unsigned)c->num_sms * 3, 256, 0, c->stream>>>(c->P[c->pcur], c->rot_list, prl_cnt, delta_t,
+                                                            half_delta_t);
+  }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

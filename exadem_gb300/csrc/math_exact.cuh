@@ -24,7 +24,7 @@ __device__ __forceinline__ bool exp_in_safe_range(double x) {
 }
 
 __device__ __forceinline__ double div_rn(double a, double b, double y) {
-  if (a == 0.0) return a * y;
+  if ((__double_as_longlong(a) << 1) == 0) return a * y;  // a == 0, decided on the integer pipe
   if (exp_in_safe_range(a) && exp_in_safe_range(b)) {
     const double q = a * y;
     const double r = fma(-q, b, a);

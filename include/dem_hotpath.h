@@ -306,7 +306,7 @@ int dem_set_graph_capacity(dem_ctx* ctx, uint64_t capacity);
  * restored after each trial, a forced rebuild and steps_per_trial steps of
  * candidate cell sizes (1, 1.25, 1.5 x (2 r_max + skin)), skins (0.5 to 3 x the
  * current one) and launch shapes, and keeps the one with the lowest
- * t_step + t_rebuild / ((skin/2) / (v_max dt)).  Cell size and launch shapes
+ * t_step + t_rebuild / min(50, (skin/2) / (v_max dt)).  Cell size and launch shapes
  * never change the list or the arithmetic.  The skin is tuned
  *   skin_policy 0: never;
  *   skin_policy 1: only without cohesion and without periodic axes, where a

@@ -92,6 +92,19 @@ int main(int argc, char** argv) {
       bad++;
     }
   }
+  // integer-pipe comparisons against the host's FP64 comparisons
+  for (long i = 0; i < n / 4; i++) {
+    const double a = draw(), b = draw();
+    const double na = a * a, nb = b * b;  // +0, positive, inf or NaN
+    const bool ok = dem::emu_gt0(a) == (a > 0) && dem::emu_lt0(a) == (a < 0) && dem::emu_ge0(a) == (a >= 0) &&
+                    dem::emu_le0(a) == (a <= 0) && dem::emu_lt(a, b) == (a < b) && dem::emu_le(a, b) == (a <= b) &&
+                    dem::emu_gt_nonneg(na, nb) == (na > nb) && dem::emu_ge_nonneg(na, nb) == (na >= nb) &&
+                    dem::emu_lt(a, a) == (a < a) && dem::emu_le(a, -a) == (a <= -a);
+    if (!ok) {
+      if (bad < 8) printf("cmp %016llx %016llx\n", (unsigned long long)bits(a), (unsigned long long)bits(b));
+      bad++;
+    }
+  }
   printf("flagged %ld (branch-free form: recomputed by the caller)\n", flagged);
   printf("cases %ld mismatches %ld\n", n, bad);
   return bad ? 1 : 0;
