@@ -60,7 +60,10 @@ __device__ __forceinline__ V3 scale_m(M& mm, double s, V3 a) {
 // contact_force_core below with its multiplies through mm, in the same
 // operation order, and the rolling clip through rolling_clip_mur0 (same
 // result); the clip's arithmetic keeps the FP64 pipe.
-template <class M>
+// With Damp, `meff` carries the pair's damping coefficient damp_rate 2
+// sqrt(kn meff) itself, computed with the same operations when the list was
+// built (IArrays::damp), instead of the effective mass.
+template <class M, bool Damp = false>
 __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, double dn, V3 n, double dt,
                                                      const dem_contact_params& hkp, double meff, V3& ft, V3 cpos,
                                                      V3 pos_i, V3 vel_i, V3& f_i, V3& mom_i, V3 vrot_i, V3 pos_j,
@@ -73,7 +76,7 @@ __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, doubl
       return;
     }
   }
-  const double damp = mm.mul(mm.twice(hkp.damp_rate), sqrt(mm.mul(hkp.kn, meff)));
+  const double damp = Damp ? meff : mm.mul(mm.twice(hkp.damp_rate), sqrt(mm.mul(hkp.kn, meff)));
   const V3 contribution_i = vel_i - cross_m(mm, cpos - pos_i, vrot_i);
   const V3 contribution_j = vel_j - cross_m(mm, cpos - pos_j, vrot_j);
   const V3 vel = contribution_j - contribution_i;

@@ -97,6 +97,7 @@ void free_iarrays(IArrays& I) {
     cudaFree(I.ft[d]);
     cudaFree(I.mo[d]);
   }
+  cudaFree(I.damp);
   I = IArrays{};
 }
 
@@ -115,6 +116,7 @@ int alloc_iarrays(dem_ctx* c, int b, uint64_t need) {
     DEM_CUDA_TRY(c, cudaMalloc(&I.ft[d], cap * 8));
     DEM_CUDA_TRY(c, cudaMalloc(&I.mo[d], cap * 8));
   }
+  DEM_CUDA_TRY(c, cudaMalloc(&I.damp, cap * 8));
   c->icap[b] = cap;
   return DEM_OK;
 }
@@ -612,6 +614,9 @@ int dem_set_params(dem_ctx* c, const dem_params* p) {
   c->gen++;
   int rc = check_params(c, p);
   if (rc) return rc;
+  if (std::memcmp(&p->config, &c->prm.config, sizeof(p->config)) ||
+      std::memcmp(&p->config_driver, &c->prm.config_driver, sizeof(p->config_driver)))
+    c->damp_stale = true;  // the per-pair damping of the current list (refresh_pair_damp)
   const bool grid_changed = std::memcmp(p->bounds_lo, c->prm.bounds_lo, sizeof(p->bounds_lo)) ||
                             std::memcmp(p->bounds_hi, c->prm.bounds_hi, sizeof(p->bounds_hi)) ||
                             std::memcmp(p->periodic, c->prm.periodic, sizeof(p->periodic)) ||
@@ -923,6 +928,7 @@ int dem_step(dem_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return DEM_ERR_INVALID_ARG;
   int rc = need_list(c);
   if (rc) return rc;
+  if ((rc = refresh_pair_damp(c))) return rc;  // contact parameters changed since the list was built
   // graph replay unless per-kernel timing is on (events cannot be recorded inside a graph)
   if (c->prm.graph_step && c->prm.fused_step && !c->poly && nsteps > 0 && !c->prof_on) return step_graph(c, nsteps);
   for (int s = 0; s < nsteps; s++) {

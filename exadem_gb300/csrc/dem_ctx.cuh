@@ -66,7 +66,7 @@ struct dem_ctx {
   // launch shapes chosen by dem_autotune (no effect on results)
   int tune_block = 128;      // threads per block of the fused prolog / epilog (64..256)
   int tune_contact_bps = 8;  // persistent blocks per SM of the compacted contact law
-  int mul_mode = 1;          // multiply placement of the fused integration kernels (integrate_core.cuh)
+  int mul_mode = 2;          // multiply placement of the fused integration kernels (integrate_core.cuh)
 
   // graph step (dem_graph.cu)
   bool capturing = false;                  // kernels launched now go into a graph
@@ -111,6 +111,7 @@ struct dem_ctx {
   uint32_t* L1 = nullptr;
   uint32_t* L2 = nullptr;
   uint32_t* rot_list = nullptr;  // pcap: particles whose epilog rotation runs in k_epilog_rotation
+  bool damp_stale = false;       // contact parameters changed since the list's per-pair damping was set
   double* Dscr[7] = {};
 
   // scan scratch
@@ -212,6 +213,7 @@ int launch_bin_particles(dem_ctx* c);
 int launch_reorder_particles(dem_ctx* c);
 // k_neigh_sphere.cu
 int launch_count_sphere(dem_ctx* c);
+int refresh_pair_damp(dem_ctx* c);  // k_neigh_sphere.cu
 int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total);
 int launch_reverse_lists(dem_ctx* c);
 // k_contact_sphere.cu

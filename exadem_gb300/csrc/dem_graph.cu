@@ -69,6 +69,7 @@ __global__ void k_graph_copy_list(IArrays dst, IArrays src, const uint32_t* __re
       dst.ft[d][k] = src.ft[d][k];
       dst.mo[d][k] = src.mo[d][k];
     }
+    dst.damp[k] = src.damp[k];
   }
 }
 
@@ -89,6 +90,7 @@ int copy_list(dem_ctx* c, IArrays& to, const IArrays& from, uint64_t ni) {
     DEM_CUDA_TRY(c, cudaMemcpyAsync(to.ft[d], from.ft[d], ni * 8, cudaMemcpyDeviceToDevice, st));
     DEM_CUDA_TRY(c, cudaMemcpyAsync(to.mo[d], from.mo[d], ni * 8, cudaMemcpyDeviceToDevice, st));
   }
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(to.damp, from.damp, ni * 8, cudaMemcpyDeviceToDevice, st));
   return DEM_OK;
 }
 
@@ -241,7 +243,7 @@ int build_graph(dem_ctx* c) {
 int snapshot(dem_ctx* c, bool save) {
   const size_t pb = particle_block_bytes(c);
   const uint64_t ni = c->ni, n = c->n;
-  const size_t need = pb + (size_t)ni * 72 + (n + 1) * 4 + 256;
+  const size_t need = pb + (size_t)ni * 80 + (n + 1) * 4 + 256;
   if (save && need > c->snap_bytes) {
     cudaFree(c->snap);
     c->snap = nullptr;
@@ -270,6 +272,7 @@ int snapshot(dem_ctx* c, bool save) {
       DEM_CUDA_TRY(c, mv(I.ft[d], ni * 8));
       DEM_CUDA_TRY(c, mv(I.mo[d], ni * 8));
     }
+    DEM_CUDA_TRY(c, mv(I.damp, ni * 8));
   }
   return DEM_OK;
 }

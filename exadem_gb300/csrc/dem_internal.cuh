@@ -65,6 +65,7 @@ struct IArrays {
   uint32_t* sub;      // owner sub (low 16 bits) | partner sub (high 16 bits); polyhedra
   double* ft[3];      // history: attr::friction
   double* mo[3];      // history: attr::moment
+  double* damp;       // spheres: the pair's damping coefficient damp_rate 2 sqrt(kn meff), set at the build
 };
 
 struct Records {  // per-interaction force record of the last force pass

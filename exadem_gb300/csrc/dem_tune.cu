@@ -65,7 +65,7 @@ int save_state(dem_ctx* c, Saved& s) {
   s.tune_block = c->tune_block;
   s.tune_contact_bps = c->tune_contact_bps;
   s.mul_mode = c->mul_mode;
-  const size_t bytes = pblock_bytes(c) + (c->n + 1) * 4 + c->ni * 72 + 1024;
+  const size_t bytes = pblock_bytes(c) + (c->n + 1) * 4 + c->ni * 80 + 1024;
   DEM_CUDA_TRY(c, cudaMalloc(&s.dev, bytes));
   char* p = static_cast<char*>(s.dev);
   const IArrays& I = c->I[c->icur];
@@ -83,6 +83,7 @@ int save_state(dem_ctx* c, Saved& s) {
     put(I.sub, c->ni * 4);
     for (int d = 0; d < 3; d++) put(I.ft[d], c->ni * 8);
     for (int d = 0; d < 3; d++) put(I.mo[d], c->ni * 8);
+    put(I.damp, c->ni * 8);
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
@@ -121,6 +122,7 @@ int restore_state(dem_ctx* c, const Saved& s) {
     get(I.sub, c->ni * 4);
     for (int d = 0; d < 3; d++) get(I.ft[d], c->ni * 8);
     for (int d = 0; d < 3; d++) get(I.mo[d], c->ni * 8);
+    get(I.damp, c->ni * 8);
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
   if ((rc = launch_reverse_lists(c))) return rc;

@@ -190,6 +190,21 @@ EMU_HD double emu_mulnhalf(double x) {
   return emu_native_mul(x, -0.5);
 }
 
+// Sums with a zero addend, decided on the integer pipe: a + z for z = +-0
+// (sign bit zs) is a itself for a nonzero, non-NaN a, and for a zero a the
+// zero that is negative only when both are (round to nearest).  ok is false
+// for a NaN a (the hardware's NaN result is used then).
+EMU_HD double emu_add_zero(double a, uint64_t zs, bool& ok) {
+  const uint64_t ua = emu_bits(a);
+  ok = (ua << 1) <= 0xffe0000000000000ull;  // not NaN
+  return (ua << 1) != 0 ? a : emu_double((ua & (zs << 63)) & 0x8000000000000000ull);
+}
+EMU_HD bool emu_is_zero(double x) { return (emu_bits(x) << 1) == 0; }
+EMU_HD uint64_t emu_sign(double x) { return emu_bits(x) >> 63; }
+// a finite, non-negative factor (sign 0, exponent below 2047): its product with
+// a zero is the zero of the other factor's sign
+EMU_HD bool emu_nonneg_finite(double x) { return emu_bits(x) < 0x7ff0000000000000ull; }
+
 // IEEE comparisons decided from the bits on the integer pipe (an FP64
 // compare occupies the FP64 pipe like an add).  NaN compares false; -0 and +0
 // compare equal.

@@ -28,7 +28,8 @@ namespace dem {
 // div_rn (math_exact.cuh) with its quotient estimate a*y through M
 template <class M>
 __device__ __forceinline__ double div_rn_m(M& mm, double a, double b, double y) {
-  if ((emu_bits(a) << 1) == 0) return mm.mul(a, y);  // a == 0, decided on the integer pipe
+  // a == 0, decided on the integer pipe; a * y is a itself for y >= +0 finite
+  if ((emu_bits(a) << 1) == 0) return emu_nonneg_finite(y) ? a : mm.mul(a, y);
   if (exp_in_safe_range(a) && exp_in_safe_range(b)) {
     const double q = mm.mul(a, y);
     const double r = fma(-q, b, a);
@@ -140,11 +141,45 @@ __device__ __forceinline__ void transl_math(L& lm, V3& r, V3& v, V3 a, double de
   v = mk(v.x + lm.mul(a.x, half_delta_t), v.y + lm.mul(a.y, half_delta_t), v.z + lm.mul(a.z, half_delta_t));
 }
 
+// One component of transl_math for the fused kernels.  With v = +-0 and a = +-0
+// (and finite non-negative steps: zok) every product is the zero of the
+// factor's sign, v dt + a dt^2/2 and v + a dt/2 are the zero that is negative
+// only when both are, and r + that zero is r (emu_add_zero): decided on the
+// integer pipe.  A particle at rest along an axis (free fall under a gravity
+// along z) skips those FP64 operations.
+template <class L>
+__device__ __forceinline__ void transl_comp_z(L& lm, double& r, double& v, double a, double delta_t,
+                                              double half_delta_t, double delta_t2_2, bool zok) {
+  if (zok && emu_is_zero(v) && emu_is_zero(a)) {
+    const uint64_t sp = emu_sign(v) & emu_sign(a);
+    bool ok;
+    const double rz = emu_add_zero(r, sp, ok);
+    if (ok) {
+      r = rz;
+      v = emu_double(sp << 63);
+      return;
+    }
+  }
+  r = r + (lm.mul(v, delta_t) + lm.mul(a, delta_t2_2));
+  v = v + lm.mul(a, half_delta_t);
+}
+template <class L>
+__device__ __forceinline__ void transl_math_z(L& lm, V3& r, V3& v, V3 a, double delta_t, double half_delta_t,
+                                              double delta_t2_2) {
+  const bool zok = emu_nonneg_finite(delta_t) && emu_nonneg_finite(half_delta_t) && emu_nonneg_finite(delta_t2_2);
+  transl_comp_z(lm, r.x, v.x, a.x, delta_t, half_delta_t, delta_t2_2, zok);
+  transl_comp_z(lm, r.y, v.y, a.y, delta_t, half_delta_t, delta_t2_2, zok);
+  transl_comp_z(lm, r.z, v.z, a.z, delta_t, half_delta_t, delta_t2_2, zok);
+}
+
 template <class R, class L, bool Shortcuts = false>
 __device__ __forceinline__ ProlState prolog_math(R& rm, L& lm, const ProlState& in, double delta_t,
                                                  double half_delta_t, double delta_t2_2) {
   ProlState o = in;
-  transl_math(lm, o.r, o.v, in.a, delta_t, half_delta_t, delta_t2_2);
+  if (Shortcuts)
+    transl_math_z(lm, o.r, o.v, in.a, delta_t, half_delta_t, delta_t2_2);
+  else
+    transl_math(lm, o.r, o.v, in.a, delta_t, half_delta_t, delta_t2_2);
   quat_math<R, L, Shortcuts>(rm, lm, o.q, o.w, in.arot, Shortcuts && spin_free_step(in.q, in.w, delta_t), delta_t,
                              half_delta_t);
   return o;
@@ -164,7 +199,7 @@ __device__ __forceinline__ bool prolog_cheap(const PArrays& P, uint64_t s, doubl
   auto run = [&](auto& rm, auto& lm, V3& r, V3& v, Q4& q, V3& w) {
     r = mk(P.f[RX][s], P.f[RY][s], P.f[RZ][s]);
     v = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
-    transl_math(lm, r, v, mk(P.f[FX][s], P.f[FY][s], P.f[FZ][s]), delta_t, half_delta_t, delta_t2_2);
+    transl_math_z(lm, r, v, mk(P.f[FX][s], P.f[FY][s], P.f[FZ][s]), delta_t, half_delta_t, delta_t2_2);
     q = {P.f[QW][s], P.f[QX][s], P.f[QY][s], P.f[QZ][s]};
     w = mk(P.f[WX][s], P.f[WY][s], P.f[WZ][s]);
     if (spin_free)

@@ -39,7 +39,21 @@ struct BPArgs {
   const float* rf;
   float skin_f;
   uint64_t cap;  // interaction buffer capacity (graph step): a fill beyond it writes nothing
+  // per-pair damping damp_rate 2 sqrt(kn meff), in the operation order of the
+  // contact law: (damp_rate * 2) * sqrt(kn * meff), meff = (m_i m_j)/(m_i + m_j)
+  // for particle pairs, m_i for drivers
+  double dr2_pp, kn_pp, dr2_pd, kn_pd;
 };
+
+__device__ __forceinline__ double pair_damp(const BPArgs& a, uint32_t i, uint32_t j, uint32_t meta) {
+  const double mi = a.P.f[MASS][i];
+  if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
+    const double mj = a.P.f[MASS][j];
+    const double meff = (mi * mj) / (mi + mj);
+    return a.dr2_pp * sqrt(a.kn_pp * meff);
+  }
+  return a.dr2_pd * sqrt(a.kn_pd * mi);
+}
 
 // FP32 decision of the broad-phase filter d2 > 0 && d2 < (r_i + r_j + skin)^2.
 // Coordinates are relative to each particle's cell origin, so |x_rel| is
@@ -212,6 +226,7 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
         dst.ft[d][x] = old.ft[d][y];
         dst.mo[d][x] = old.mo[d][y];
       }
+      dst.damp[x] = old.damp[y];
     }
     return;
   }
@@ -250,6 +265,7 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
   for (uint32_t x = b; x < e; x++) {
     dst.owner[x] = (uint32_t)s;
     dst.sub[x] = 0u;
+    dst.damp[x] = pair_damp(a, (uint32_t)s, dst.partner[x], dst.meta[x]);
     double h[6] = {0, 0, 0, 0, 0, 0};
     const uint64_t pk = dst.pid[x];
     const uint32_t tk = meta_type(dst.meta[x]);
@@ -276,6 +292,12 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
     dst.mo[1][x] = h[4];
     dst.mo[2][x] = h[5];
   }
+}
+
+// per-pair damping of a kept list after the contact parameters changed
+__global__ void k_pair_damp(BPArgs a, IArrays I, uint64_t ni) {
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < ni; k += (uint64_t)gridDim.x * blockDim.x)
+    I.damp[k] = pair_damp(a, I.owner[k], I.partner[k], I.meta[k]);
 }
 
 __global__ void k_zero_u32(uint32_t* p, uint64_t n) {
@@ -342,9 +364,23 @@ BPArgs make_args(dem_ctx* c) {
   a.rf = c->crel[3];
   a.skin_f = (float)c->prm.rcut_inc;
   a.cap = c->capturing ? c->gcap : ~0ull;
+  a.dr2_pp = c->prm.config.damp_rate * 2.0;
+  a.kn_pp = c->prm.config.kn;
+  a.dr2_pd = c->prm.config_driver.damp_rate * 2.0;
+  a.kn_pd = c->prm.config_driver.kn;
   return a;
 }
 }  // namespace
+
+// recomputes the per-pair damping of the current sphere list (after dem_set_params)
+int refresh_pair_damp(dem_ctx* c) {
+  if (!c->damp_stale) return DEM_OK;
+  c->damp_stale = false;
+  if (c->poly || !c->have_list || !c->ni) return DEM_OK;
+  k_pair_damp<<<c->num_sms * 4, 256, 0, c->stream>>>(make_args(c), c->I[c->icur], c->ni);
+  DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
 
 int launch_count_sphere(dem_ctx* c) {
   ProfScope ps(c, K_BROAD_COUNT, c->n ? 1 : 0);

@@ -237,9 +237,10 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
       if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
         const V3 rj = partner_pos(a, meta, i, j);
         const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
-        const double m_i = a.P.f[MASS][i], m_j = a.P.f[MASS][j];
-        const double meff = mm.mul(m_i, m_j) / (m_i + m_j);
-        contact_force_core_m(mm, a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, ri, vi, f, mo, wi, rj, vj, wj);
+        // the pair's damping coefficient, set when the list was built (k_fill)
+        contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, a.cp,
+                                                                         a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
+                                                                         rj, vj, wj);
         ti = cross_m(mm, cpos - ri, f) + mo;
         tj = cross_m(mm, cpos - rj, -f) + (-mo);
       } else {
@@ -247,9 +248,9 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
         const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
         const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
         const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
-        const double meff = a.P.f[MASS][i];
-        contact_force_core_m(mm, a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, ri, vi, f, mo, wi, dpos, dvel,
-                             dvrot);
+        contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, a.cpd,
+                                                                         a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
+                                                                         dpos, dvel, dvrot);
         ti = cross_m(mm, cpos - ri, f) + mo;
       }
     };
@@ -327,7 +328,10 @@ __global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_epilog(PArrays P,
   V3 mom = mk(0.0, 0.0, 0.0);
   if (s < n) {
     const double m = P.f[MASS][s];
-    V3 f = mk(0.0 + gx * m, 0.0 + gy * m, 0.0 + gz * m);
+    // 0.0 + g_c m is +0 for g_c = +-0 and a finite m (+0 + +-0 = +0): no FP64 work
+    const bool mfin = ((emu_bits(m) >> 52) & 0x7ffu) != 0x7ffu;
+    V3 f = mk(emu_is_zero(gx) && mfin ? 0.0 : 0.0 + gx * m, emu_is_zero(gy) && mfin ? 0.0 : 0.0 + gy * m,
+              emu_is_zero(gz) && mfin ? 0.0 : 0.0 + gz * m);
     // f and mom start at +0 or a nonzero value and, in round to nearest, never
     // become -0 (x + (-x) = +0; -0 needs two -0 operands), so a record whose six
     // components are all +-0 (a listed pair that does not touch) leaves them
@@ -353,8 +357,17 @@ __global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_epilog(PArrays P,
     LinMul<Mode> lm;
     V3 acc = mk(div_rn_m(lm, f.x, m, im), div_rn_m(lm, f.y, m, im), div_rn_m(lm, f.z, m, im));
     const V3 vel = mk(P.f[VX][s], P.f[VY][s], P.f[VZ][s]);
-    V3 v = mk(vel.x + lm.mul(acc.x, half_delta_t), vel.y + lm.mul(acc.y, half_delta_t),
-              vel.z + lm.mul(acc.z, half_delta_t));
+    // v + a dt/2: a zero a gives the zero addend of emu_add_zero (integer pipe)
+    const bool hok = emu_nonneg_finite(half_delta_t);
+    auto vstep = [&](double vc, double ac) {
+      if (hok && emu_is_zero(ac)) {
+        bool ok;
+        const double r = emu_add_zero(vc, emu_sign(ac), ok);
+        if (ok) return r;
+      }
+      return vc + lm.mul(ac, half_delta_t);
+    };
+    V3 v = mk(vstep(vel.x, acc.x), vstep(vel.y, acc.y), vstep(vel.z, acc.z));
     if (lm.failed()) {
       acc = mk(div_rn(f.x, m, im), div_rn(f.y, m, im), div_rn(f.z, m, im));
       v = mk(vel.x + acc.x * half_delta_t, vel.y + acc.y * half_delta_t, vel.z + acc.z * half_delta_t);

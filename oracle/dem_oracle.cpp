@@ -1290,6 +1290,23 @@ int oracle_destroy(void* h) {
   delete (Oracle*)h;
   return DEM_OK;
 }
+// Parameters of a running system.  The contact law parameters (config /
+// config_driver slots), dt and gravity are read at every step by the
+// operators that use them (contact_force_sphere.cu.in, gravity_force.cu,
+// combined_compute_prolog.cu), so they may change between steps with the list
+// and its history kept.  A change of domain, skin or cell size needs a new
+// grid and is not supported here.
+int oracle_set_params(void* h, const dem_params* p) {
+  if (!h || !p) return DEM_ERR_INVALID_ARG;
+  Oracle& o = *(Oracle*)h;
+  if (std::memcmp(p->bounds_lo, o.prm.bounds_lo, sizeof(p->bounds_lo)) ||
+      std::memcmp(p->bounds_hi, o.prm.bounds_hi, sizeof(p->bounds_hi)) ||
+      std::memcmp(p->periodic, o.prm.periodic, sizeof(p->periodic)) || p->rcut_inc != o.prm.rcut_inc ||
+      p->cell_size != o.prm.cell_size)
+    return DEM_ERR_UNSUPPORTED;
+  o.prm = *p;
+  return DEM_OK;
+}
 int oracle_set_threads(int n) {
 #ifdef _OPENMP
   if (n > 0) omp_set_num_threads(n);

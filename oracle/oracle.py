@@ -26,6 +26,7 @@ def load(rebuild: bool = True):
         lib = C.CDLL(str(path))
         sig = lambda n, a, r=C.c_int: (setattr(getattr(lib, n), "argtypes", a), setattr(getattr(lib, n), "restype", r))
         sig("oracle_create", [C.POINTER(A.Params), C.POINTER(_CTX)])
+        sig("oracle_set_params", [_CTX, C.POINTER(A.Params)])
         sig("oracle_destroy", [_CTX])
         sig("oracle_set_threads", [C.c_int])
         sig("oracle_last_error", [_CTX], C.c_char_p)
@@ -74,7 +75,7 @@ class OracleBackend:
         return self.lib.oracle_get_particles(h, st)
 
     def set_params(self, h, p):
-        return 4  # DEM_ERR_UNSUPPORTED: the oracle takes its parameters at creation only
+        return self.lib.oracle_set_params(h, p)
 
     def __getattr__(self, name):
         return getattr(self.lib, self._MAP[name])

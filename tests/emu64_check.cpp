@@ -105,6 +105,19 @@ int main(int argc, char** argv) {
       bad++;
     }
   }
+  // zero addends
+  for (long i = 0; i < n / 4; i++) {
+    const double a = draw();
+    const double z = (next64() & 1) ? -0.0 : 0.0;
+    bool ok = false;
+    const double got = dem::emu_add_zero(a, dem::emu_sign(z), ok);
+    const double ref = a + z;
+    if (ok && bits(got) != bits(ref)) {
+      if (bad < 8) printf("addz %016llx %016llx\n", (unsigned long long)bits(a), (unsigned long long)bits(z));
+      bad++;
+    }
+    if (!ok && a == a) bad++;  // only NaN may leave the fast path
+  }
   printf("flagged %ld (branch-free form: recomputed by the caller)\n", flagged);
   printf("cases %ld mismatches %ld\n", n, bad);
   return bad ? 1 : 0;

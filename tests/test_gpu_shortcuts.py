@@ -6,6 +6,7 @@ the sign of zeros) with the oracle, which runs the plain formulas:
 - the idle rotation (no spin, no torque: arot = w = +0) next to rotating and
   touching particles;
 - skipped all-zero contact records in the force gather."""
+import copy
 import itertools
 
 import numpy as np
@@ -61,6 +62,34 @@ def test_spin_free_quaternions_bit_exact(native_lib, mode):
 
 
 @pytest.mark.parametrize("mode", [0, 1])
+def test_signed_zero_velocities_bit_exact(native_lib, mode):
+    """Zero-aware translation and velocity updates: velocity components drawn
+    from {+0, -0, 0.3, -0.3}, gravity (-0, +0, -9.81), no contacts."""
+    vals = np.array([0.0, -0.0, 0.3, -0.3])
+    combos = np.array(list(itertools.product(range(4), repeat=3)))
+    n = len(combos) * 4
+    w = W.spheres_box(n=n, box=60.0, seed=4, fused_step=1, fp32_contact_screen=1, fp32_broad_phase=1)
+    side = int(np.ceil(n ** (1 / 3)))
+    idx = np.arange(n)
+    w.particles["rx"] = 4.0 + 3.0 * (idx % side)
+    w.particles["ry"] = 4.0 + 3.0 * ((idx // side) % side)
+    w.particles["rz"] = 20.0 + 3.0 * (idx // (side * side))
+    c = np.tile(combos, (4, 1))
+    for k, f in enumerate(("vx", "vy", "vz")):
+        w.particles[f] = vals[c[:, k]].copy()
+    for f in ("vrotx", "vroty", "vrotz"):
+        w.particles[f] = np.zeros(n)
+    w.params.gravity[0] = -0.0
+    w.params.gravity[1] = 0.0
+    g, o = pair(w)
+    g.set_mul_mode(mode)
+    for s in (g, o):
+        s.first_iteration()
+        s.step(5)
+    _bits_equal(g.particles(sort_by_id=True), o.particles(sort_by_id=True))
+
+
+@pytest.mark.parametrize("mode", [0, 1])
 def test_idle_and_rotating_mix_bit_exact(native_lib, mode):
     """A settling box: some particles touch (torque), some spin freely, the rest
     are idle; zero records of listed but separated pairs are skipped."""
@@ -81,3 +110,23 @@ def test_idle_and_rotating_mix_bit_exact(native_lib, mode):
     for f in ("vrotx", "vroty", "vrotz", "momx", "momy", "momz"):
         idle &= pg[f].view(np.uint64) == 0
     assert 0 < idle.sum() < w.n
+
+
+@pytest.mark.parametrize("graph", [0, 1])
+def test_pair_damping_follows_parameter_change(native_lib, graph):
+    """The per-pair damping cached in the list is refreshed when the contact
+    parameters change without a rebuild (the oracle computes it per contact)."""
+    w = W.spheres_drum(n=3000, seed=51, fused_step=1, fp32_contact_screen=1, fp32_broad_phase=1, graph_step=graph)
+    g, o = pair(w)
+    for s in (g, o):
+        s.first_iteration()
+        s.step(80)
+    p2 = copy.deepcopy(w.params)
+    p2.config.kn = 2.0e4
+    p2.config.damp_rate = 0.5
+    p2.config_driver.kn = 1.5e4
+    for s in (g, o):
+        s.set_params(p2)
+        s.step(80)
+    _bits_equal(g.particles(sort_by_id=True), o.particles(sort_by_id=True))
+    assert_same_list(g.interactions(), o.interactions())
