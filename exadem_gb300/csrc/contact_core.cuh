@@ -16,8 +16,8 @@ namespace dem {
 // every square stays below 2^1024.  So in that range the clip is exactly
 // "if (|m|^2 > 0) m = m * (+0)" (the signed zeros of m; m * 0 of an infinite
 // component is NaN, as in the formula), without the two norms, the division
-// and the square roots.  Outside it (w = 0, whose 0/0 keeps the moment, huge
-// or non-finite values) the formula itself runs.
+// and the square roots.  A spin of exactly zero keeps the moment (0/0 below);
+// outside both cases (huge or non-finite values) the formula itself runs.
 __device__ __forceinline__ bool exp_below(double x, int e2) {  // |x| < 2^e2, x finite
   return (int)((emu_bits(x) >> 52) & 0x7ffu) < 1023 + e2;
 }
@@ -25,6 +25,9 @@ __device__ __forceinline__ bool exp_at_least(double x, int e2) {  // |x| >= 2^e2
   return (int)((emu_bits(x) >> 52) & 0x7ffu) >= 1023 + e2;
 }
 __device__ __forceinline__ void rolling_clip_mur0(V3 branch, V3 vrot_i, V3 fn, V3& mom_i) {
+  // w = +-0: r = (b.w)/(w.w) is (+-0 or NaN)/(+0) = NaN for any b, so t = NaN and
+  // the comparison with t^2 is false: the moment is kept as it is
+  if (((emu_bits(vrot_i.x) | emu_bits(vrot_i.y) | emu_bits(vrot_i.z)) << 1) == 0) return;
   const bool in_range = exp_below(branch.x, 200) && exp_below(branch.y, 200) && exp_below(branch.z, 200) &&
                         exp_below(fn.x, 500) && exp_below(fn.y, 500) && exp_below(fn.z, 500) &&
                         exp_below(vrot_i.x, 200) && exp_below(vrot_i.y, 200) && exp_below(vrot_i.z, 200) &&
