@@ -138,6 +138,7 @@ int alloc_records(dem_ctx* c, uint64_t need) {
     cudaFree(c->R.ti[d]);
     cudaFree(c->R.tj[d]);
   }
+  cudaFree(c->R.live);
   c->R = Records{};
   cudaFree(c->rev_idx);
   c->rev_idx = nullptr;
@@ -153,9 +154,13 @@ int alloc_records(dem_ctx* c, uint64_t need) {
   DEM_CUDA_TRY(c, cudaMalloc(&c->L1, cap * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->L2, cap * 4));
   for (int q = 0; q < 7; q++) DEM_CUDA_TRY(c, cudaMalloc(&c->Dscr[q], cap * 8));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->R.live, cap));
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->R.live, 1, cap, c->stream));
   c->rcap = cap;
   return DEM_OK;
 }
+
+
 
 // Cell grid: cell size >= nbh_dist = 2*r_max + rcut_inc (dem_rcut_max.cpp:60, config_globals.msp:35-37).
 // Cell grid of one system: cs = max(cell_size, nbh_dist) with nbh_dist =
@@ -403,7 +408,10 @@ int mark_all_triggered(dem_ctx* c) {
 
 int update_neighbors(dem_ctx* c) {
   c->gen++;  // buffers may move: a captured step graph is stale
-  if (c->poly) return update_neighbors_poly(c);
+  if (c->poly) {
+    const int rc = update_neighbors_poly(c);
+    return rc ? rc : mark_records_live(c);
+  }
   if (c->n == 0) {
     c->ni = 0;
     c->have_list = true;
@@ -427,6 +435,7 @@ int update_neighbors(dem_ctx* c) {
   c->have_list = true;
   c->hist_valid = true;
   if ((rc = launch_reverse_lists(c))) return rc;
+  if ((rc = mark_records_live(c))) return rc;  // new list indices: every record is stale
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->trig_dev, 0, c->nsys * sizeof(uint32_t), c->stream));
   c->rebuilds++;
   return DEM_OK;
@@ -463,6 +472,12 @@ int copy_field(dem_ctx* c, double* dst, const double* src, uint64_t n, cudaMemcp
 namespace dem {
 int ext_alloc_iarrays(dem_ctx* c, int b, uint64_t need) { return alloc_iarrays(c, b, need); }
 int ext_alloc_records(dem_ctx* c, uint64_t need) { return alloc_records(c, need); }
+// every record may be nonzero again (list rebuilt, state restored, or written by
+// a kernel that does not keep the flags)
+int mark_records_live(dem_ctx* c) {
+  if (c->R.live && c->rcap) DEM_CUDA_TRY(c, cudaMemsetAsync(c->R.live, 1, c->rcap, c->stream));
+  return DEM_OK;
+}
 void ext_free_iarrays(IArrays& I) { free_iarrays(I); }
 int ext_update_neighbors(dem_ctx* c) {
   int rc = mark_all_triggered(c);
@@ -567,6 +582,7 @@ int dem_ctx_destroy(dem_ctx* c) {
     cudaFree(c->R.ti[d]);
     cudaFree(c->R.tj[d]);
   }
+  cudaFree(c->R.live);
   cudaFree(c->rev_idx);
   free_compact(c);
   free_poly(c);

@@ -214,6 +214,7 @@ int launch_reorder_particles(dem_ctx* c);
 // k_neigh_sphere.cu
 int launch_count_sphere(dem_ctx* c);
 int refresh_pair_damp(dem_ctx* c);  // k_neigh_sphere.cu
+int mark_records_live(dem_ctx* c);  // dem_api.cu
 int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total);
 int launch_reverse_lists(dem_ctx* c);
 // k_contact_sphere.cu

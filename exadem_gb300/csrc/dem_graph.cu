@@ -130,6 +130,7 @@ int rebuild_body(dem_ctx* c) {
                                                                        n, c->d_gs);
   DEM_CUDA_TRY(c, cudaGetLastError());
   if ((rc = launch_reverse_lists(c))) return rc;
+  if ((rc = mark_records_live(c))) return rc;  // new list indices: every record is stale
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->trig_dev, 0, c->nsys * sizeof(uint32_t), c->stream));
   return DEM_OK;
 }
@@ -314,6 +315,7 @@ int step_graph(dem_ctx* c, int nsteps) {
     c->ni = ni0;
     if ((rc = snapshot(c, false))) return rc;
     if ((rc = launch_reverse_lists(c))) return rc;
+    if ((rc = mark_records_live(c))) return rc;  // the records were not saved
     DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
     c->gcap = 2 * c->gcap;
     destroy_graph(c);

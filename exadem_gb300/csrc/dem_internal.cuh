@@ -72,6 +72,11 @@ struct Records {  // per-interaction force record of the last force pass
   double* f[3];
   double* ti[3];
   double* tj[3];
+  // fused sphere step: 0 when the interaction's record and history are known to
+  // be zero (written as zeros by the screen or the detection and untouched since),
+  // so that the screen need not write them again and the gather need not read
+  // them; 1 otherwise.  Every rebuild sets all entries to 1.
+  uint8_t* live;
 };
 
 // drivers in device-friendly form (stationary; vrot enters the relative velocity)

@@ -126,6 +126,7 @@ int restore_state(dem_ctx* c, const Saved& s) {
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
   if ((rc = launch_reverse_lists(c))) return rc;
+  if ((rc = mark_records_live(c))) return rc;  // the records were not saved
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   c->gen++;
   return DEM_OK;

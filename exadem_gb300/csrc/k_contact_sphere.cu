@@ -198,7 +198,7 @@ int launch_contact_sphere(dem_ctx* c) {
   ProfScope ps(c, K_CONTACT, c->ni ? 1 : 0);
   if (c->ni) k_contact<<<grid_for(c->ni, 128), 128, 0, c->stream>>>(a);
   DEM_CUDA_TRY(c, cudaGetLastError());
-  return DEM_OK;
+  return mark_records_live(c);  // this kernel writes every record without keeping the flags
 }
 
 int launch_gather_forces(dem_ctx* c) {

@@ -110,8 +110,11 @@ __global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
       const float limf = (float)lim;
       if (lim > 1e-15 && lim < 1e15 && d2f > limf * limf * 1.0000039f) {
         want = false;
-        const V3 z = mk(0, 0, 0);
-        write_result(a, k, z, z, z, z, z);
+        if (a.R.live[k]) {  // not yet zero: reset history and record once
+          const V3 z = mk(0, 0, 0);
+          write_result(a, k, z, z, z, z, z);
+          a.R.live[k] = 0;
+        }
       }
     }
   }
@@ -182,8 +185,11 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
       if (a.cohesive) contact = (contact || emu_le(dn, dncut));
       const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
       if (!contact) {
-        const V3 z = mk(0, 0, 0);
-        write_result(a, k, z, z, z, z, z);
+        if (a.R.live[k]) {
+          const V3 z = mk(0, 0, 0);
+          write_result(a, k, z, z, z, z, z);
+          a.R.live[k] = 0;
+        }
       } else if (a.cohesive && emu_ge0(dn)) {
         // cohesive attraction before contact (contact_force.hpp:165-173): f = fn_value n, ft = 0
         const dem_contact_params& hkp = is_vv ? a.cp : a.cpd;
@@ -192,6 +198,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         const V3 ti = cross(cpos - ri, f) + mo;
         const V3 tj = is_vv ? cross(cpos - rj, -f) + (-mo) : mk(0, 0, 0);
         write_result(a, k, mk(0, 0, 0), mo, f, ti, tj);
+        a.R.live[k] = 1;
       } else {
         heavy = true;
       }
@@ -263,6 +270,7 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
       run(nm, ft, mo, f, ti, tj);
     }
     write_result(a, k, ft, mo, f, ti, tj);
+    a.R.live[k] = 1;
   }
 }
 
@@ -336,7 +344,9 @@ __global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_epilog(PArrays P,
     // become -0 (x + (-x) = +0; -0 needs two -0 operands), so a record whose six
     // components are all +-0 (a listed pair that does not touch) leaves them
     // unchanged bit for bit and its additions are skipped.
+    // (a record whose live flag is 0 is zero and is not read)
     for (uint32_t k = own_off[s]; k < own_off[s + 1]; k++) {
+      if (!R.live[k]) continue;
       const V3 rf = mk(R.f[0][k], R.f[1][k], R.f[2][k]), rt = mk(R.ti[0][k], R.ti[1][k], R.ti[2][k]);
       if (((emu_bits(rf.x) | emu_bits(rf.y) | emu_bits(rf.z) | emu_bits(rt.x) | emu_bits(rt.y) | emu_bits(rt.z))
            << 1) != 0) {
@@ -346,6 +356,7 @@ __global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_epilog(PArrays P,
     }
     for (uint32_t q = rev_off[s]; q < rev_off[s + 1]; q++) {
       const uint32_t k = rev_idx[q];
+      if (!R.live[k]) continue;
       const V3 rf = mk(R.f[0][k], R.f[1][k], R.f[2][k]), rt = mk(R.tj[0][k], R.tj[1][k], R.tj[2][k]);
       if (((emu_bits(rf.x) | emu_bits(rf.y) | emu_bits(rf.z) | emu_bits(rt.x) | emu_bits(rt.y) | emu_bits(rt.z))
            << 1) != 0) {
