@@ -175,21 +175,30 @@ __global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_poly_fused_prolog(PolyA
 }
 
 // vertices of the listed particles (those in the interaction list), FP64
+// One thread per (listed particle, vertex): world_vertex p + q (h v0) with the
+// multiplies of the rotation through the placement policy (mode bit 0) and the
+// product h v0 skipped for h = 1 (1 * x = x); an operand outside the integer
+// multiply's fast path makes the vertex run world_vertex itself.
+template <int Mode>
 __global__ void k_poly_vertices_listed(PolyArgs a, const uint32_t* __restrict__ list, uint64_t count) {
   const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count) return;
-  const uint32_t s = list[t];
+  if (t >= count * (uint64_t)a.MV) return;
+  const uint32_t s = list[t / (uint64_t)a.MV];
+  const int k = (int)(t % (uint64_t)a.MV);
   const ShapeDev& sh = a.shapes[a.P.type[s]];
+  if (k >= sh.nv) return;
   const V3 p = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
   const Q4 q = {a.P.f[QW][s], a.P.f[QX][s], a.P.f[QY][s], a.P.f[QZ][s]};
   const double h = a.P.f[HOM][s];
-  for (int k = 0; k < sh.nv; k++) {
-    const V3 v = world_vertex(sh, k, p, q, h);
-    const uint64_t idx = (uint64_t)s * a.MV + k;
-    a.vx[idx] = v.x;
-    a.vy[idx] = v.y;
-    a.vz[idx] = v.z;
-  }
+  RotMul<Mode> rm;
+  const V3 v0 = sh_v(sh, k);
+  const V3 hv = emu_bits(h) == 0x3ff0000000000000ull ? v0 : mk(rm.mul(h, v0.x), rm.mul(h, v0.y), rm.mul(h, v0.z));
+  V3 v = p + qrotate_m(rm, q, hv);
+  if (rm.failed()) v = world_vertex(sh, k, p, q, h);
+  const uint64_t idx = (uint64_t)s * a.MV + k;
+  a.vx[idx] = v.x;
+  a.vy[idx] = v.y;
+  a.vz[idx] = v.z;
 }
 
 // marks the particles whose vertices the interaction list uses: both sides of the
@@ -1276,7 +1285,9 @@ int launch_poly_vertices_listed(dem_ctx* c) {
   ProfScope ps(c, K_PROLOG, c->nvlist ? 1 : 0);
   if (!c->nvlist) return DEM_OK;
   const PolyArgs a = make_pargs(c);
-  k_poly_vertices_listed<<<grid_for(c->nvlist, PT), PT, 0, c->stream>>>(a, c->vlist, c->nvlist);
+  const auto kern = by_mode(c->mul_mode, k_poly_vertices_listed<0>, k_poly_vertices_listed<1>,
+                            k_poly_vertices_listed<2>, k_poly_vertices_listed<3>);
+  kern<<<grid_for(c->nvlist * (uint64_t)c->MV, PT), PT, 0, c->stream>>>(a, c->vlist, c->nvlist);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }

@@ -130,3 +130,24 @@ def test_pair_damping_follows_parameter_change(native_lib, graph):
         s.step(80)
     _bits_equal(g.particles(sort_by_id=True), o.particles(sort_by_id=True))
     assert_same_list(g.interactions(), o.interactions())
+
+
+def test_live_flags_across_plain_and_fused_steps(native_lib):
+    """Records written by the plain contact kernel (which does not keep the live
+    flags) are read again by the fused step's gather: switching the path between
+    steps keeps the oracle's bits."""
+    w = W.spheres_floor(n=4000, side=14.0, seed=61, fused_step=1, fp32_contact_screen=1, fp32_broad_phase=1)
+    g, o = pair(w)
+    for s in (g, o):
+        s.first_iteration()
+        s.step(60)
+    plain = copy.deepcopy(w.params)
+    plain.fused_step = 0
+    plain.fp32_contact_screen = 0
+    g.set_params(plain)
+    g.step(30)
+    g.set_params(w.params)
+    g.step(60)
+    o.step(90)
+    _bits_equal(g.particles(sort_by_id=True), o.particles(sort_by_id=True))
+    assert_same_list(g.interactions(), o.interactions())
