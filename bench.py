@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (cell size, launch shapes)")
     ap.add_argument("--mul-mode", type=int, default=None, choices=list(range(8)),
                     help="multiplies on the integer pipe: bit 0 integration rotations, bit 1 integration rest, "
-                         "bit 2 contact law (default: the autotuner's choice, else 1)")
+                         "bit 2 contact law (default: the autotuner's choice, else 2)")
     ap.add_argument("--learned", action="store_true",
                     help="polyhedra: harvest candidate pairs, train the MLP, time with learned sizing "
                          "and without it")

@@ -333,7 +333,7 @@ int dem_autotune(dem_ctx* ctx, int steps_per_trial, int skin_policy, dem_tune_re
  * rotations and derivative, normalisation, Euler terms) on the integer pipe;
  * bit 1: the other multiplies (Verlet pushes, quotient estimates); bit 2:
  * the sphere contact law's multiplies.  0 = FP64 pipe only.  Results are
- * identical in every mode (0..7).  Default 1; the autotuner picks the fastest
+ * identical in every mode (0..7).  Default 2; the autotuner picks the fastest
  * for the sphere step.                                                     */
 int dem_set_mul_mode(dem_ctx* ctx, int mode);
 int dem_get_mul_mode(dem_ctx* ctx, int* mode);
