@@ -26,6 +26,7 @@ ITYPE_VERTEX_CYLINDER = 4
 ITYPE_VERTEX_SURFACE = 5
 LAW_HOOKE_NONE = 0
 LAW_HOOKE_COHESIVE = 1
+LAW_HOOKE_DMT = 2
 
 D = C.c_double
 PD = C.POINTER(C.c_double)
@@ -36,7 +37,8 @@ PU8 = C.POINTER(C.c_uint8)
 
 
 class ContactParams(C.Structure):
-    _fields_ = [("kn", D), ("kt", D), ("kr", D), ("mu", D), ("damp_rate", D), ("fc", D), ("dncut", D)]
+    _fields_ = [("kn", D), ("kt", D), ("kr", D), ("mu", D), ("damp_rate", D), ("fc", D), ("dncut", D),
+                ("gamma", D)]
 
 
 class Params(C.Structure):

@@ -70,7 +70,7 @@ template <class M, bool Damp = false>
 __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, double dn, V3 n, double dt,
                                                      const dem_contact_params& hkp, double meff, V3& ft, V3 cpos,
                                                      V3 pos_i, V3 vel_i, V3& f_i, V3& mom_i, V3 vrot_i, V3 pos_j,
-                                                     V3 vel_j, V3 vrot_j) {
+                                                     V3 vel_j, V3 vrot_j, bool dmt = false, double reff = 0.0) {
   if (cohesive) {
     if (emu_ge0(dn)) {  // comparisons of this form on the integer pipe (emu64.cuh)
       const double fn_value = mm.mul(hkp.fc / hkp.dncut, dn) - hkp.fc;
@@ -115,6 +115,10 @@ __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, doubl
     }
   }
   f_i = fn + ft;
+  if (dmt && hkp.gamma > 0.0 && emu_lt0(dn)) {
+    const double F = mm.mul(mm.mul(2.0 * 3.14159265358979323846, reff), hkp.gamma);
+    f_i = f_i - scale_m(mm, F, n);
+  }
   {
     const V3 d = vrot_j - vrot_i;
     mom_i = mom_i + mk(mm.mul(mm.mul(hkp.kr, d.x), dt), mm.mul(mm.mul(hkp.kr, d.y), dt),
@@ -123,10 +127,19 @@ __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, doubl
   rolling_clip_mur0(cpos - pos_i, vrot_i, fn, mom_i);
 }
 
+// apply_dmt_force (contact_force.hpp:115-127): in contact (dn < 0) and for
+// gamma > 0, f_i -= (2 pi reff gamma) n, the operation order of the reference
+__device__ __forceinline__ double dmt_magnitude(double reff, double gamma) {
+  return 2.0 * 3.14159265358979323846 * reff * gamma;
+}
+
 // contact_force_core (contact_force.hpp:146-235).  f_i must be {0,0,0} on entry.
+// dmt: the Hooke_DMT law combination (contact_force.hpp:70-76) with reff the
+// effective radius of the pair.
 __device__ __forceinline__ void contact_force_core(bool cohesive, double dn, V3 n, double dt, const dem_contact_params& hkp,
                                           double meff, V3& ft, V3 cpos, V3 pos_i, V3 vel_i, V3& f_i, V3& mom_i,
-                                          V3 vrot_i, V3 pos_j, V3 vel_j, V3 vrot_j) {
+                                          V3 vrot_i, V3 pos_j, V3 vel_j, V3 vrot_j, bool dmt = false,
+                                          double reff = 0.0) {
   if (cohesive) {
     if (dn >= 0) {
       const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
@@ -171,6 +184,7 @@ __device__ __forceinline__ void contact_force_core(bool cohesive, double dn, V3 
     }
   }
   f_i = fn + ft;
+  if (dmt && hkp.gamma > 0.0 && dn < 0.0) f_i = f_i - dmt_magnitude(reff, hkp.gamma) * n;
   mom_i = mom_i + hkp.kr * (vrot_j - vrot_i) * dt;
   // rolling clip with mur = 0 (contact_force.hpp:225-234): the IEEE NaN of
   // 0/0 when vrot_i == 0 keeps the moment, otherwise the moment is scaled by 0.

@@ -25,9 +25,9 @@ int check_params(dem_ctx* c, const dem_params* p) {
   if (!(p->rcut_inc >= 0)) return c->fail(DEM_ERR_INVALID_ARG, "rcut_inc must be >= 0");
   if (!(p->dt > 0)) return c->fail(DEM_ERR_INVALID_ARG, "dt must be > 0");
   if (p->symetric != 1) return c->fail(DEM_ERR_UNSUPPORTED, "only symetric: true is supported");
-  if (p->law != DEM_LAW_HOOKE_NONE && p->law != DEM_LAW_HOOKE_COHESIVE)
+  if (p->law != DEM_LAW_HOOKE_NONE && p->law != DEM_LAW_HOOKE_COHESIVE && p->law != DEM_LAW_HOOKE_DMT)
     return c->fail(DEM_ERR_UNSUPPORTED, "unknown contact law");
-  if (p->law == DEM_LAW_HOOKE_NONE && (p->config.dncut > 0 || p->config_driver.dncut > 0))
+  if (p->law != DEM_LAW_HOOKE_COHESIVE && (p->config.dncut > 0 || p->config_driver.dncut > 0))
     return c->fail(DEM_ERR_INVALID_ARG,
                    "dncut is != 0 while the cohesive force is not used (contact_force_sphere.cu.in:280-292)");
   if (p->law == DEM_LAW_HOOKE_COHESIVE && (p->config.dncut == 0 || p->config_driver.dncut == 0))

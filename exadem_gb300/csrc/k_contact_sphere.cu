@@ -32,6 +32,7 @@ struct ContactArgs {
   dem_contact_params cpd;  // particle-driver
   double dt;
   int cohesive;
+  int dmt;  // Hooke_DMT law combination
   int screen;
   unsigned long long* n_active;
 };
@@ -87,7 +88,10 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
           const V3 wi = ldv(a.P, WX, i), wj = ldv(a.P, WX, j);
           const double m_i = a.P.f[MASS][i], m_j = a.P.f[MASS][j];
           const double meff = (m_i * m_j) / (m_i + m_j);
-          contact_force_core(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, ri, vi, f, mo, wi, rj, vj, wj);
+          // reff = compute_effective_radius (common_kernels.hpp:99-102), DMT only
+          const double reff = a.dmt ? (rad_i * rad_j) / (rad_i + rad_j) : 0.0;
+          contact_force_core(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, ri, vi, f, mo, wi, rj, vj, wj, a.dmt,
+                             reff);
           ti = cross(cpos - ri, f) + mo;
           tj = cross(cpos - rj, -f) + (-mo);
           act = dn < 0;
@@ -127,7 +131,8 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
         const V3 v = ldv(a.P, VX, i);
         const V3 wi = ldv(a.P, WX, i);
         const double meff = a.P.f[MASS][i];
-        contact_force_core(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, ri, v, f, mo, wi, dpos, dvel, dvrot);
+        contact_force_core(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, ri, v, f, mo, wi, dpos, dvel, dvrot, a.dmt,
+                           rad_i);  // reff = the particle's radius (contact_sphere.hpp:270)
         ti = cross(cpos - ri, f) + mo;
         act = dn < 0;
       }
@@ -192,6 +197,7 @@ int launch_contact_sphere(dem_ctx* c) {
   a.cpd = c->prm.config_driver;
   a.dt = c->prm.dt;
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
+  a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
   a.screen = c->prm.fp32_contact_screen;
   a.n_active = c->d_scalars + 1;
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 1, 0, sizeof(unsigned long long), c->stream));

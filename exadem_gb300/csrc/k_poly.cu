@@ -1015,6 +1015,7 @@ struct PCArgs {
   dem_contact_params cp, cpd;
   double dt;
   int cohesive;
+  int dmt;  // Hooke_DMT law combination
   uint32_t* L2;
   double* D[7];
   unsigned long long* cnt;  // [1] = L2 count
@@ -1176,14 +1177,14 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
 template <bool Fast>
 __device__ __forceinline__ void hooke(bool cohesive, double dn, V3 n, double dt, const dem_contact_params& hkp,
                                       double meff, V3& ft, V3 cpos, V3 pos_i, V3 vel_i, V3& f_i, V3& mom_i,
-                                      V3 vrot_i, V3 pos_j, V3 vel_j, V3 vrot_j) {
+                                      V3 vrot_i, V3 pos_j, V3 vel_j, V3 vrot_j, bool dmt, double reff) {
   if (Fast) {
     MulFP64 mm;
     contact_force_core_m(mm, cohesive, dn, n, dt, hkp, meff, ft, cpos, pos_i, vel_i, f_i, mom_i, vrot_i, pos_j,
-                         vel_j, vrot_j);
+                         vel_j, vrot_j, dmt, reff);
   } else {
     contact_force_core(cohesive, dn, n, dt, hkp, meff, ft, cpos, pos_i, vel_i, f_i, mom_i, vrot_i, pos_j, vel_j,
-                       vrot_j);
+                       vrot_j, dmt, reff);
   }
 }
 
@@ -1206,9 +1207,11 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
       const DriverDev& d = a.drv[a.I.partner[k]];
       const V3 r = ldv(a.P, RX, p), v = ldv(a.P, VX, p), w_ = ldv(a.P, WX, p);
       const double meff = a.P.f[MASS][p];
+      // DMT: reff = shp.minkowski(h) (polyhedron/contact.hpp:281)
+      const double reff = a.dmt ? a.P.f[HOM][p] * a.shapes[a.P.type[p]].r : 0.0;
       hooke<Fast>(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, r, v, f, mo, w_,
                   mk(d.center[0], d.center[1], d.center[2]), mk(d.vel[0], d.vel[1], d.vel[2]),
-                  mk(d.vrot[0], d.vrot[1], d.vrot[2]));
+                  mk(d.vrot[0], d.vrot[1], d.vrot[2]), a.dmt, reff);
       pwrite(a, k, ft, mo, f, cross(cpos - r, f) + mo, mk(0, 0, 0));
       continue;
     }
@@ -1218,7 +1221,14 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
     const V3 w_i = ldv(a.P, WX, R.ip), w_j = ldv(a.P, WX, R.jp);
     const double m_i = a.P.f[MASS][R.ip], m_j = a.P.f[MASS][R.jp];
     const double meff = (m_i * m_j) / (m_i + m_j);
-    hooke<Fast>(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, r_i, v_i, f, mo, w_i, r_j, v_j, w_j);
+    // DMT: reff = compute_effective_mass(rad_i, rad_j) of the Minkowski radii h r (polyhedron/contact.hpp:179-183)
+    double reff = 0.0;
+    if (a.dmt) {
+      const double rad_i = a.P.f[HOM][R.ip] * a.shapes[a.P.type[R.ip]].r;
+      const double rad_j = a.P.f[HOM][R.jp] * a.shapes[a.P.type[R.jp]].r;
+      reff = (rad_i * rad_j) / (rad_i + rad_j);
+    }
+    hooke<Fast>(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, r_i, v_i, f, mo, w_i, r_j, v_j, w_j, a.dmt, reff);
     const V3 t_i = cross(cpos - r_i, f) + mo;
     const V3 t_j = cross(cpos - r_j, -f) + (-mo);
     if ((meta >> 15) & 1u)
@@ -1510,6 +1520,7 @@ int launch_contact_poly(dem_ctx* c) {
   a.cpd = c->prm.config_driver;
   a.dt = c->prm.dt;
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
+  a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
   a.L2 = c->L2;
   for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];
   a.cnt = c->d_scalars + 3;

@@ -50,6 +50,7 @@ struct CArgs {
   dem_contact_params cp, cpd;
   double dt;
   int cohesive;
+  int dmt;  // Hooke_DMT law combination
   int screen;
   uint32_t* L1;
   uint32_t* L2;
@@ -244,10 +245,16 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
       if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
         const V3 rj = partner_pos(a, meta, i, j);
         const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
-        // the pair's damping coefficient, set when the list was built (k_fill)
+        // the pair's damping coefficient, set when the list was built (k_fill); DMT:
+        // reff = compute_effective_radius (common_kernels.hpp:99-102)
+        double reff = 0.0;
+        if (a.dmt) {
+          const double rad_i = a.P.f[RAD][i], rad_j = a.P.f[RAD][j];
+          reff = mm.mul(rad_i, rad_j) / (rad_i + rad_j);
+        }
         contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, a.cp,
                                                                          a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
-                                                                         rj, vj, wj);
+                                                                         rj, vj, wj, a.dmt, reff);
         ti = cross_m(mm, cpos - ri, f) + mo;
         tj = cross_m(mm, cpos - rj, -f) + (-mo);
       } else {
@@ -257,7 +264,7 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
         const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
         contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, a.cpd,
                                                                          a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
-                                                                         dpos, dvel, dvrot);
+                                                                         dpos, dvel, dvrot, a.dmt, a.P.f[RAD][i]);
         ti = cross_m(mm, cpos - ri, f) + mo;
       }
     };
@@ -442,6 +449,7 @@ CArgs make_cargs(dem_ctx* c) {
   a.cpd = c->prm.config_driver;
   a.dt = c->prm.dt;
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
+  a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
   a.screen = c->prm.fp32_contact_screen;
   a.L1 = c->L1;
   a.L2 = c->L2;

@@ -59,9 +59,9 @@ def make_params(bounds_lo, bounds_hi, periodic=(0, 0, 0), rcut_inc=0.05, dt=1e-3
     return p
 
 
-def contact_params(kn=1e4, kt=8e3, kr=0.0, mu=0.3, damp_rate=0.9, fc=0.0, dncut=0.0) -> A.ContactParams:
-    """ContactParams YAML keys (contact_parameters.hpp:138-190)."""
-    return A.ContactParams(kn, kt, kr, mu, damp_rate, fc, dncut)
+def contact_params(kn=1e4, kt=8e3, kr=0.0, mu=0.3, damp_rate=0.9, fc=0.0, dncut=0.0, gamma=0.0) -> A.ContactParams:
+    """ContactParams YAML keys (contact_parameters.hpp:138-190); gamma: DMT adhesion energy."""
+    return A.ContactParams(kn, kt, kr, mu, damp_rate, fc, dncut, gamma)
 
 
 def empty_particles(n: int) -> dict:

@@ -53,12 +53,16 @@ extern "C" {
 typedef struct dem_contact_params {
   double kn, kt, kr, mu, damp_rate;
   double fc, dncut;
+  double gamma; /* adhesion energy per unit surface of the DMT law (ContactParams::gamma_) */
 } dem_contact_params;
 
-/* Contact law variant, as in the operator names contact_singlemat_sphere_hooke_{none,cohesive}
- * (src/sphere/CMakeLists.txt:63-110, contact_force.hpp:26-48).           */
+/* Contact law variant, as in the operator names contact_singlemat_sphere_hooke_{none,cohesive,dmt}
+ * (src/sphere/CMakeLists.txt:63-110, contact_force.hpp:26-98).  DMT adds, in
+ * contact and for gamma > 0, the attraction -2 pi reff gamma n to the Hooke
+ * force (apply_dmt_force, contact_force.hpp:115-127).                     */
 #define DEM_LAW_HOOKE_NONE 0
 #define DEM_LAW_HOOKE_COHESIVE 1
+#define DEM_LAW_HOOKE_DMT 2
 
 /* ---- simulation / domain parameters ------------------------------------
  * domain: bounds + periodic flags (exaNBody Domain, e.g.

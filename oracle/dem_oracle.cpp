@@ -416,11 +416,12 @@ int update_neighbors(Oracle& o) {
 }
 
 // --------------------------------------------------------------- contact law
-// contact_force_core<Hooke, None|Cohesive> (src/forcefield/include/exaDEM/forcefield/contact_force.hpp:146-235)
-// with common_kernels.hpp:27-145.
+// contact_force_core<Hooke, None|Cohesive|DMT> (src/forcefield/include/exaDEM/forcefield/contact_force.hpp:146-235)
+// with common_kernels.hpp:27-145; dmt: apply_dmt_force (contact_force.hpp:115-127) with the pair's reff.
 void contact_force_core(bool cohesive, double dn, const V3& n, double dt, const dem_contact_params& hkp, double meff,
                         V3& ft, const V3& cp, const V3& pos_i, const V3& vel_i, V3& f_i, V3& mom_i,
-                        const V3& vrot_i, const V3& pos_j, const V3& vel_j, const V3& vrot_j) {
+                        const V3& vrot_i, const V3& pos_j, const V3& vel_j, const V3& vrot_j, bool dmt = false,
+                        double reff = 0.0) {
   if (cohesive) {
     if (dn >= 0) {
       const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
@@ -463,6 +464,10 @@ void contact_force_core(bool cohesive, double dn, const V3& n, double dt, const 
     if (ft_square > 0.0 && ft_square > threshold_ft * threshold_ft) ft *= (threshold_ft / std::sqrt(ft_square));
   }
   f_i = fn + ft;
+  if (dmt && hkp.gamma > 0.0 && dn < 0.0) {  // attraction -2 pi reff gamma n in contact
+    const double F_dmt = 2.0 * 3.14159265358979323846 * reff * hkp.gamma;
+    f_i -= F_dmt * n;
+  }
   mom_i += hkp.kr * (vrot_j - vrot_i) * dt;
   V3 branch = cp - pos_i;
   double r = (dot(branch, vrot_i)) / (dot(vrot_i, vrot_i));
@@ -481,6 +486,7 @@ void contact_one(Oracle& o, size_t k) {
   Rec& rc = o.rec[k];
   rc = Rec{};
   const bool cohesive = o.prm.law == DEM_LAW_HOOKE_COHESIVE;
+  const bool dmt = o.prm.law == DEM_LAW_HOOKE_DMT;
   const double dt = o.prm.dt;
   const size_t i = it.oi;
   const V3 ri = pos(o, i);
@@ -507,8 +513,9 @@ void contact_one(Oracle& o, size_t k) {
       const double m_i = o.mass[i], m_j = o.mass[j];
       V3 f = {0, 0, 0};
       const double meff = (m_i * m_j) / (m_i + m_j);  // compute_effective_mass
+      const double reff = dmt ? (rad_i * rad_j) / (rad_i + rad_j) : 0.0;  // compute_effective_radius
       contact_force_core(cohesive, dn, n, dt, cpar, meff, it.friction, cp, ri, vi, f, it.moment, vrot_i, rj, vj,
-                         vrot_j);
+                         vrot_j, dmt, reff);
       rc.f = f;
       rc.ti = cross(cp - ri, f) + it.moment;       // compute_moments
       rc.tj = cross(cp - rj, -f) + (-it.moment);
@@ -544,7 +551,7 @@ void contact_one(Oracle& o, size_t k) {
     const double meff = o.mass[i];
     V3 f = {0, 0, 0};
     contact_force_core(cohesive, dn, n, dt, cpar, meff, it.friction, cp, ri, v, f, it.moment, vrot_i, dpos, dvel,
-                       dvrot);
+                       dvrot, dmt, rad);  // reff = the particle's radius (contact_sphere.hpp:270)
     rc.f = f;
     rc.ti = cross(cp - ri, f) + it.moment;
     rc.active = dn < 0;
@@ -1170,6 +1177,7 @@ void contact_one_poly(Oracle& o, size_t k) {
   Rec& rc = o.rec[k];
   rc = Rec{};
   const bool cohesive = o.prm.law == DEM_LAW_HOOKE_COHESIVE;
+  const bool dmt = o.prm.law == DEM_LAW_HOOKE_DMT;
   const double dt = o.prm.dt;
   if (it.type >= DEM_ITYPE_VERTEX_CYLINDER) {
     const size_t p = it.oi;
@@ -1200,7 +1208,8 @@ void contact_one_poly(Oracle& o, size_t k) {
       const V3 vrot = {o.wx[p], o.wy[p], o.wz[p]};
       const double meff = o.mass[p];
       V3 f = {0, 0, 0};
-      contact_force_core(cohesive, dn, n, dt, cpar, meff, it.friction, cp, r, v, f, it.moment, vrot, dpos, dvel, dvrot);
+      contact_force_core(cohesive, dn, n, dt, cpar, meff, it.friction, cp, r, v, f, it.moment, vrot, dpos, dvel, dvrot,
+                         dmt, h * sh.r);  // reff = shp.minkowski(h) (polyhedron/contact.hpp:281)
       rc.f = f;
       rc.ti = cross(cp - r, f) + it.moment;
       rc.active = dn < 0;
@@ -1238,8 +1247,11 @@ void contact_one_poly(Oracle& o, size_t k) {
     const V3 w_i = {o.wx[ip], o.wy[ip], o.wz[ip]}, w_j = {o.wx[jp], o.wy[jp], o.wz[jp]};
     const double meff = (o.mass[ip] * o.mass[jp]) / (o.mass[ip] + o.mass[jp]);
     V3 f = {0, 0, 0};
+    // reff = compute_effective_mass(rad_i, rad_j) of the Minkowski radii (polyhedron/contact.hpp:179-183)
+    const double rad_i = o.hom[ip] * shi.r, rad_j = o.hom[jp] * shj.r;
+    const double reff = dmt ? (rad_i * rad_j) / (rad_i + rad_j) : 0.0;
     contact_force_core(cohesive, d.dn, d.n, dt, cpar, meff, it.friction, d.cp, r_i, v_i, f, it.moment, w_i, r_j, v_j,
-                       w_j);
+                       w_j, dmt, reff);
     const V3 t_i = cross(d.cp - r_i, f) + it.moment;
     const V3 t_j = cross(d.cp - r_j, -f) + (-it.moment);
     if (!it.swap) {
