@@ -35,6 +35,16 @@ int check_params(dem_ctx* c, const dem_params* p) {
   return DEM_OK;
 }
 
+// every particle group must index the multi-material table (the reference asserts it)
+int check_multimat_groups(dem_ctx* c) {
+  if (!c->mm_pp || !c->n) return DEM_OK;
+  std::vector<uint32_t> g(c->n);
+  DEM_CUDA_TRY(c, cudaMemcpy(g.data(), c->P[c->pcur].group, c->n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  for (uint32_t x : g)
+    if (x >= (uint32_t)c->mm_ng) return c->fail(DEM_ERR_INVALID_ARG, "a particle group is outside the multi-material table");
+  return DEM_OK;
+}
+
 void free_particles(dem_ctx* c) {
   for (int b = 0; b < 2; b++) {
     if (c->pblock[b]) cudaFree(c->pblock[b]);
@@ -569,6 +579,8 @@ int dem_ctx_create(const dem_params* params, dem_ctx** out) {
 int dem_ctx_destroy(dem_ctx* c) {
   if (!c) return DEM_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  cudaFree(c->mm_pp);
+  cudaFree(c->mm_pd);
   c->fold_events();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   c->ev_pool.clear();
@@ -709,7 +721,49 @@ int dem_set_particles(dem_ctx* c, const dem_particles* p, int on_device) {
   c->hist_valid = false;
   c->rebuilds = 0;
   if ((rc = alloc_poly(c))) return rc;
+  if ((rc = check_multimat_groups(c))) return rc;
   return setup_grid(c);
+}
+
+int dem_set_multimat(dem_ctx* c, int ngroups, const dem_contact_params* pairs, int ndrivers,
+                     const dem_contact_params* drivers) {
+  if (!c || ngroups < 0 || ndrivers < 0) return DEM_ERR_INVALID_ARG;
+  auto clear = [c]() {
+    cudaFree(c->mm_pp);
+    cudaFree(c->mm_pd);
+    c->mm_pp = c->mm_pd = nullptr;
+    c->mm_ng = c->mm_nd = 0;
+  };
+  c->gen++;  // the kernels of a captured step hold the old table
+  c->damp_stale = true;
+  if (ngroups == 0) {
+    clear();
+    return DEM_OK;
+  }
+  if (!pairs || (ndrivers > 0 && !drivers)) return DEM_ERR_INVALID_ARG;
+  if (ndrivers != c->ndrv) return c->fail(DEM_ERR_INVALID_ARG, "ndrivers must equal the number of registered drivers");
+  const size_t npp = (size_t)ngroups * ngroups, npd = (size_t)ngroups * ndrivers;
+  for (int a = 0; a < ngroups; a++)
+    for (int b = 0; b < ngroups; b++)
+      if (std::memcmp(&pairs[a * ngroups + b], &pairs[b * ngroups + a], sizeof(dem_contact_params)))
+        return c->fail(DEM_ERR_INVALID_ARG, "the pair table must be symmetric (register_multimat, multimat_parameters.hpp:181-186)");
+  for (size_t k = 0; k < npp + npd; k++) {
+    const dem_contact_params& q = k < npp ? pairs[k] : drivers[k - npp];
+    if (c->prm.law != DEM_LAW_HOOKE_COHESIVE && q.dncut > 0)
+      return c->fail(DEM_ERR_INVALID_ARG, "dncut is != 0 while the cohesive force is not used");
+    if (c->prm.law == DEM_LAW_HOOKE_COHESIVE && q.dncut == 0)
+      return c->fail(DEM_ERR_INVALID_ARG, "cohesive law needs dncut > 0");
+  }
+  clear();
+  DEM_CUDA_TRY(c, cudaMalloc(&c->mm_pp, npp * sizeof(dem_contact_params)));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->mm_pd, std::max<size_t>(npd, 1) * sizeof(dem_contact_params)));
+  DEM_CUDA_TRY(c, cudaMemcpy(c->mm_pp, pairs, npp * sizeof(dem_contact_params), cudaMemcpyHostToDevice));
+  if (npd) DEM_CUDA_TRY(c, cudaMemcpy(c->mm_pd, drivers, npd * sizeof(dem_contact_params), cudaMemcpyHostToDevice));
+  c->mm_ng = ngroups;
+  c->mm_nd = ndrivers;
+  const int rc = check_multimat_groups(c);
+  if (rc) clear();
+  return rc;
 }
 
 int dem_get_particles(dem_ctx* c, dem_particles* out, int on_device) {
@@ -944,6 +998,8 @@ int dem_step(dem_ctx* c, int nsteps) {
   if (!c || nsteps < 0) return DEM_ERR_INVALID_ARG;
   int rc = need_list(c);
   if (rc) return rc;
+  if (c->mm_pp && c->mm_nd != c->ndrv)
+    return c->fail(DEM_ERR_STATE, "drivers were registered after dem_set_multimat: set the table again");
   if ((rc = refresh_pair_damp(c))) return rc;  // contact parameters changed since the list was built
   // graph replay unless per-kernel timing is on (events cannot be recorded inside a graph)
   if (c->prm.graph_step && c->prm.fused_step && !c->poly && nsteps > 0 && !c->prof_on) return step_graph(c, nsteps);

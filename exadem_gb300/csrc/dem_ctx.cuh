@@ -112,6 +112,18 @@ struct dem_ctx {
   uint32_t* L2 = nullptr;
   uint32_t* rot_list = nullptr;  // pcap: particles whose epilog rotation runs in k_epilog_rotation
   bool damp_stale = false;       // contact parameters changed since the list's per-pair damping was set
+  // multi-material contact parameters (dem_set_multimat); mm_pp == nullptr: singlemat
+  int mm_ng = 0, mm_nd = 0;
+  dem_contact_params* mm_pp = nullptr;  // device, mm_ng * mm_ng
+  dem_contact_params* mm_pd = nullptr;  // device, mm_ng * mm_nd
+  dem::ParamTable ptable() const {
+    dem::ParamTable t;
+    t.pp = mm_pp;
+    t.pd = mm_pd;
+    t.ng = mm_ng;
+    t.nd = mm_nd;
+    return t;
+  }
   double* Dscr[7] = {};
 
   // scan scratch

@@ -79,6 +79,24 @@ struct Records {  // per-interaction force record of the last force pass
   uint8_t* live;
 };
 
+// Multi-material contact parameters (multimat_parameters.hpp:38-300,
+// contact_force_accessor.hpp:15-23): pp[g_i * ng + g_j] for a particle pair,
+// pd[g_i * nd + driver] for a particle and a driver, by the particles' group
+// field.  pp == nullptr: the single sets config / config_driver (singlemat).
+struct ParamTable {
+  const dem_contact_params* pp = nullptr;
+  const dem_contact_params* pd = nullptr;
+  int ng = 0, nd = 0;
+  __host__ __device__ inline const dem_contact_params& pair(const dem_contact_params& single, uint32_t gi,
+                                                            uint32_t gj) const {
+    return pp ? pp[gi * (uint32_t)ng + gj] : single;
+  }
+  __host__ __device__ inline const dem_contact_params& drv(const dem_contact_params& single, uint32_t gi,
+                                                           uint32_t d) const {
+    return pd ? pd[gi * (uint32_t)nd + d] : single;
+  }
+};
+
 // drivers in device-friendly form (stationary; vrot enters the relative velocity)
 struct DriverDev {
   int kind;  // 0 surface, 1 cylinder

@@ -32,7 +32,8 @@ struct ContactArgs {
   dem_contact_params cpd;  // particle-driver
   double dt;
   int cohesive;
-  int dmt;  // Hooke_DMT law combination
+  int dmt;        // Hooke_DMT law combination
+  ParamTable pt;  // multi-material parameters (pt.pp == nullptr: cp / cpd)
   int screen;
   unsigned long long* n_active;
 };
@@ -61,13 +62,14 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
         if (sz) rj.z = rj.z + (double)sz * g.L[2];
       }
       const double rad_j = a.P.f[RAD][j];
+      const dem_contact_params& cp = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]);  // contact_sphere.hpp:147-152
       bool skip = false;
       if (a.screen) {
         // FP32 proof of separation: |d|^2 computed in FP32 from FP64 differences
         // (relative error < 2^-21 for the sum of squares) against (R + dncut)^2 * (1 + 2^-18).
         const float ex = (float)(ri.x - rj.x), ey = (float)(ri.y - rj.y), ez = (float)(ri.z - rj.z);
         const float d2f = ex * ex + ey * ey + ez * ez;
-        const double lim = rad_i + rad_j + (a.cohesive ? fmax(a.cp.dncut, 0.0) : 0.0);
+        const double lim = rad_i + rad_j + (a.cohesive ? fmax(cp.dncut, 0.0) : 0.0);
         const float limf = (float)lim;
         // only where lim^2 is a normal FP32 number, so the relative bound holds
         skip = lim > 1e-15 && lim < 1e15 && d2f > limf * limf * 1.0000039f;
@@ -82,7 +84,7 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
         const V3 n = dist * inv_dist_norm;
         const V3 cpos = ri - n * (rad_i + 0.5 * dn);
         contact = dn < 0;
-        if (a.cohesive) contact = (contact || dn <= a.cp.dncut);
+        if (a.cohesive) contact = (contact || dn <= cp.dncut);
         if (contact) {
           const V3 vi = ldv(a.P, VX, i), vj = ldv(a.P, VX, j);
           const V3 wi = ldv(a.P, WX, i), wj = ldv(a.P, WX, j);
@@ -90,7 +92,7 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
           const double meff = (m_i * m_j) / (m_i + m_j);
           // reff = compute_effective_radius (common_kernels.hpp:99-102), DMT only
           const double reff = a.dmt ? (rad_i * rad_j) / (rad_i + rad_j) : 0.0;
-          contact_force_core(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, ri, vi, f, mo, wi, rj, vj, wj, a.dmt,
+          contact_force_core(a.cohesive, dn, n, a.dt, cp, meff, ft, cpos, ri, vi, f, mo, wi, rj, vj, wj, a.dmt,
                              reff);
           ti = cross(cpos - ri, f) + mo;
           tj = cross(cpos - rj, -f) + (-mo);
@@ -126,12 +128,13 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
       dpos = mk(d.center[0], d.center[1], d.center[2]);
       dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
       dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
-      if (a.cohesive) contact = (contact || dn <= a.cpd.dncut);
+      const dem_contact_params& cpd = a.pt.drv(a.cpd, a.P.group[i], j);  // contact_sphere.hpp:254-257
+      if (a.cohesive) contact = (contact || dn <= cpd.dncut);
       if (contact) {
         const V3 v = ldv(a.P, VX, i);
         const V3 wi = ldv(a.P, WX, i);
         const double meff = a.P.f[MASS][i];
-        contact_force_core(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, ri, v, f, mo, wi, dpos, dvel, dvrot, a.dmt,
+        contact_force_core(a.cohesive, dn, n, a.dt, cpd, meff, ft, cpos, ri, v, f, mo, wi, dpos, dvel, dvrot, a.dmt,
                            rad_i);  // reff = the particle's radius (contact_sphere.hpp:270)
         ti = cross(cpos - ri, f) + mo;
         act = dn < 0;
@@ -198,6 +201,7 @@ int launch_contact_sphere(dem_ctx* c) {
   a.dt = c->prm.dt;
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
   a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
+  a.pt = c->ptable();
   a.screen = c->prm.fp32_contact_screen;
   a.n_active = c->d_scalars + 1;
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 1, 0, sizeof(unsigned long long), c->stream));

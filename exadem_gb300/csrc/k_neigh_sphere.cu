@@ -41,18 +41,21 @@ struct BPArgs {
   uint64_t cap;  // interaction buffer capacity (graph step): a fill beyond it writes nothing
   // per-pair damping damp_rate 2 sqrt(kn meff), in the operation order of the
   // contact law: (damp_rate * 2) * sqrt(kn * meff), meff = (m_i m_j)/(m_i + m_j)
-  // for particle pairs, m_i for drivers
-  double dr2_pp, kn_pp, dr2_pd, kn_pd;
+  // for particle pairs, m_i for drivers; the pair's parameter set
+  dem_contact_params cp, cpd;
+  ParamTable pt;
 };
 
 __device__ __forceinline__ double pair_damp(const BPArgs& a, uint32_t i, uint32_t j, uint32_t meta) {
   const double mi = a.P.f[MASS][i];
   if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
+    const dem_contact_params& q = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]);
     const double mj = a.P.f[MASS][j];
     const double meff = (mi * mj) / (mi + mj);
-    return a.dr2_pp * sqrt(a.kn_pp * meff);
+    return q.damp_rate * 2.0 * sqrt(q.kn * meff);
   }
-  return a.dr2_pd * sqrt(a.kn_pd * mi);
+  const dem_contact_params& q = a.pt.drv(a.cpd, a.P.group[i], j);
+  return q.damp_rate * 2.0 * sqrt(q.kn * mi);
 }
 
 // FP32 decision of the broad-phase filter d2 > 0 && d2 < (r_i + r_j + skin)^2.
@@ -364,10 +367,9 @@ BPArgs make_args(dem_ctx* c) {
   a.rf = c->crel[3];
   a.skin_f = (float)c->prm.rcut_inc;
   a.cap = c->capturing ? c->gcap : ~0ull;
-  a.dr2_pp = c->prm.config.damp_rate * 2.0;
-  a.kn_pp = c->prm.config.kn;
-  a.dr2_pd = c->prm.config_driver.damp_rate * 2.0;
-  a.kn_pd = c->prm.config_driver.kn;
+  a.cp = c->prm.config;
+  a.cpd = c->prm.config_driver;
+  a.pt = c->ptable();
   return a;
 }
 }  // namespace

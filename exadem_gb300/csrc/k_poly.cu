@@ -1015,7 +1015,8 @@ struct PCArgs {
   dem_contact_params cp, cpd;
   double dt;
   int cohesive;
-  int dmt;  // Hooke_DMT law combination
+  int dmt;        // Hooke_DMT law combination
+  ParamTable pt;  // multi-material parameters (pt.pp == nullptr: cp / cpd)
   uint32_t* L2;
   double* D[7];
   unsigned long long* cnt;  // [1] = L2 count
@@ -1081,6 +1082,7 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
     V3 ri, rj = mk(0, 0, 0);
     bool is_pp = type <= DEM_ITYPE_EDGE_EDGE;
     double dncut;
+    const dem_contact_params* hp = &a.cp;
     uint32_t swap = (meta >> 15) & 1u;
     if (!is_pp) {
       const uint32_t p = a.I.owner[k];
@@ -1112,7 +1114,8 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
         }
       }
       ri = mk(a.P.f[RX][p], a.P.f[RY][p], a.P.f[RZ][p]);
-      dncut = a.cpd.dncut;
+      hp = &a.pt.drv(a.cpd, a.P.group[p], a.I.partner[k]);  // the pair's parameters (multimat)
+      dncut = hp->dncut;
     } else {
       const Roles R = roles(a, k);
       const ShapeDev& si = a.shapes[a.P.type[R.ip]];
@@ -1135,7 +1138,8 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
       }
       ri = mk(a.P.f[RX][R.ip], a.P.f[RY][R.ip], a.P.f[RZ][R.ip]);
       rj = mk(a.P.f[RX][R.jp], a.P.f[RY][R.jp], a.P.f[RZ][R.jp]);
-      dncut = a.cp.dncut;
+      hp = &a.pt.pair(a.cp, a.P.group[R.ip], a.P.group[R.jp]);
+      dncut = hp->dncut;
     }
     contact = d.c;
     if (a.cohesive) contact = (contact || d.dn <= dncut);
@@ -1143,7 +1147,7 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
       const V3 z = mk(0, 0, 0);
       pwrite(a, k, z, z, z, z, z);
     } else if (a.cohesive && d.dn >= 0) {
-      const dem_contact_params& hkp = is_pp ? a.cp : a.cpd;
+      const dem_contact_params& hkp = *hp;
       const double fn_value = (hkp.fc / hkp.dncut) * d.dn - hkp.fc;
       const V3 f = mk(0, 0, 0) + fn_value * d.n;
       const V3 ti = cross(d.cp - ri, f) + mo;
@@ -1209,7 +1213,8 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
       const double meff = a.P.f[MASS][p];
       // DMT: reff = shp.minkowski(h) (polyhedron/contact.hpp:281)
       const double reff = a.dmt ? a.P.f[HOM][p] * a.shapes[a.P.type[p]].r : 0.0;
-      hooke<Fast>(a.cohesive, dn, n, a.dt, a.cpd, meff, ft, cpos, r, v, f, mo, w_,
+      hooke<Fast>(a.cohesive, dn, n, a.dt, a.pt.drv(a.cpd, a.P.group[p], a.I.partner[k]), meff, ft, cpos, r, v, f,
+                  mo, w_,
                   mk(d.center[0], d.center[1], d.center[2]), mk(d.vel[0], d.vel[1], d.vel[2]),
                   mk(d.vrot[0], d.vrot[1], d.vrot[2]), a.dmt, reff);
       pwrite(a, k, ft, mo, f, cross(cpos - r, f) + mo, mk(0, 0, 0));
@@ -1228,7 +1233,8 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
       const double rad_j = a.P.f[HOM][R.jp] * a.shapes[a.P.type[R.jp]].r;
       reff = (rad_i * rad_j) / (rad_i + rad_j);
     }
-    hooke<Fast>(a.cohesive, dn, n, a.dt, a.cp, meff, ft, cpos, r_i, v_i, f, mo, w_i, r_j, v_j, w_j, a.dmt, reff);
+    hooke<Fast>(a.cohesive, dn, n, a.dt, a.pt.pair(a.cp, a.P.group[R.ip], a.P.group[R.jp]), meff, ft, cpos, r_i, v_i,
+                f, mo, w_i, r_j, v_j, w_j, a.dmt, reff);
     const V3 t_i = cross(cpos - r_i, f) + mo;
     const V3 t_j = cross(cpos - r_j, -f) + (-mo);
     if ((meta >> 15) & 1u)
@@ -1521,6 +1527,7 @@ int launch_contact_poly(dem_ctx* c) {
   a.dt = c->prm.dt;
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
   a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
+  a.pt = c->ptable();
   a.L2 = c->L2;
   for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];
   a.cnt = c->d_scalars + 3;

@@ -50,7 +50,8 @@ struct CArgs {
   dem_contact_params cp, cpd;
   double dt;
   int cohesive;
-  int dmt;  // Hooke_DMT law combination
+  int dmt;        // Hooke_DMT law combination
+  ParamTable pt;  // multi-material parameters (pt.pp == nullptr: cp / cpd)
   int screen;
   uint32_t* L1;
   uint32_t* L2;
@@ -107,7 +108,8 @@ __global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
       // same proof of separation as the one-pass kernel (k_contact_sphere.cu)
       const float ex = (float)(ri.x - rj.x), ey = (float)(ri.y - rj.y), ez = (float)(ri.z - rj.z);
       const float d2f = ex * ex + ey * ey + ez * ez;
-      const double lim = rad_i + rad_j + (a.cohesive ? fmax(a.cp.dncut, 0.0) : 0.0);
+      const double lim =
+          rad_i + rad_j + (a.cohesive ? fmax(a.pt.pair(a.cp, a.P.group[i], a.P.group[j]).dncut, 0.0) : 0.0);
       const float limf = (float)lim;
       if (lim > 1e-15 && lim < 1e15 && d2f > limf * limf * 1.0000039f) {
         want = false;
@@ -151,7 +153,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         const double dist_norm = vnorm(dist);
         dn = dist_norm - R;
         contact = emu_lt0(dn);  // comparisons of this kernel on the integer pipe (emu64.cuh)
-        dncut = a.cp.dncut;
+        dncut = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]).dncut;
         if (contact || (a.cohesive && emu_le(dn, dncut))) {  // n and cpos are used only then
           const double inv_dist_norm = 1.0 / dist_norm;
           n = dist * inv_dist_norm;
@@ -181,7 +183,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
             cpos = ri - n * (rad_i + 0.5 * dn);
           }
         }
-        dncut = a.cpd.dncut;
+        dncut = a.pt.drv(a.cpd, a.P.group[i], j).dncut;
       }
       if (a.cohesive) contact = (contact || emu_le(dn, dncut));
       const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
@@ -193,7 +195,8 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         }
       } else if (a.cohesive && emu_ge0(dn)) {
         // cohesive attraction before contact (contact_force.hpp:165-173): f = fn_value n, ft = 0
-        const dem_contact_params& hkp = is_vv ? a.cp : a.cpd;
+        const dem_contact_params& hkp =
+            is_vv ? a.pt.pair(a.cp, a.P.group[i], a.P.group[j]) : a.pt.drv(a.cpd, a.P.group[i], j);
         const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
         const V3 f = mk(0, 0, 0) + fn_value * n;
         const V3 ti = cross(cpos - ri, f) + mo;
@@ -252,7 +255,8 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
           const double rad_i = a.P.f[RAD][i], rad_j = a.P.f[RAD][j];
           reff = mm.mul(rad_i, rad_j) / (rad_i + rad_j);
         }
-        contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, a.cp,
+        const dem_contact_params& cp = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]);
+        contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, cp,
                                                                          a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
                                                                          rj, vj, wj, a.dmt, reff);
         ti = cross_m(mm, cpos - ri, f) + mo;
@@ -262,7 +266,8 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
         const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
         const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
         const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
-        contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, a.cpd,
+        const dem_contact_params& cpd = a.pt.drv(a.cpd, a.P.group[i], j);
+        contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, cpd,
                                                                          a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
                                                                          dpos, dvel, dvrot, a.dmt, a.P.f[RAD][i]);
         ti = cross_m(mm, cpos - ri, f) + mo;
@@ -450,6 +455,7 @@ CArgs make_cargs(dem_ctx* c) {
   a.dt = c->prm.dt;
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
   a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
+  a.pt = c->ptable();
   a.screen = c->prm.fp32_contact_screen;
   a.L1 = c->L1;
   a.L2 = c->L2;

@@ -266,6 +266,21 @@ class System:
         self._check(self.b.autotune(self.h, int(steps_per_trial), int(skin_policy), C.byref(r)), "autotune")
         return {f: getattr(r, f) for f, _ in A.TuneResult._fields_}
 
+    def set_multimat(self, pairs: list, drivers: list) -> None:
+        """dem_set_multimat: pairs is an ngroups x ngroups nested list of ContactParams
+        (symmetric), drivers an ngroups x ndrivers nested list; pairs = [] returns
+        to the single parameter sets."""
+        ng = len(pairs)
+        nd = len(drivers[0]) if ng and drivers else 0
+        pp = (A.ContactParams * max(ng * ng, 1))()
+        pd = (A.ContactParams * max(ng * nd, 1))()
+        for a in range(ng):
+            for b in range(ng):
+                pp[a * ng + b] = pairs[a][b]
+            for d in range(nd):
+                pd[a * nd + d] = drivers[a][d]
+        self._check(self.b.set_multimat(self.h, ng, pp, nd, pd), "set_multimat")
+
     def set_mul_mode(self, mode: int) -> None:
         """dem_set_mul_mode: which integration multiplies run on the integer pipe (same bits)."""
         self._check(self.b.set_mul_mode(self.h, int(mode)), "set_mul_mode")

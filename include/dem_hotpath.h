@@ -204,6 +204,17 @@ const char* dem_last_error(const dem_ctx* ctx);
  * parallel_execution_context() stream (classifier_for_all.hpp:244-255).  */
 int dem_ctx_stream(dem_ctx* ctx, void** stream);
 int dem_set_params(dem_ctx* ctx, const dem_params* params);
+/* Multi-material contact parameters (multimat_contact_params /
+ * drivers_contact_params operators, multimat_parameters.hpp:38-300; the
+ * contact_multimat_* operator variants).  The parameters of a particle pair
+ * are pairs[g_i * ngroups + g_j] and of a particle and driver d
+ * drivers[g_i * ndrivers + d], g the particle's group field; the law
+ * (dem_params.law) stays global.  pairs must be symmetric; ndrivers must equal
+ * the number of registered drivers; every particle group must be < ngroups
+ * (checked here and by dem_set_particles).  ngroups = 0 returns to the single
+ * sets config / config_driver.  Takes effect at the next step.            */
+int dem_set_multimat(dem_ctx* ctx, int ngroups, const dem_contact_params* pairs, int ndrivers,
+                     const dem_contact_params* drivers);
 
 /* ---- state binding ------------------------------------------------------ */
 /* Replaces the particle set (input_data + set_fields, src/field/set_fields.cu:238-330).

@@ -143,6 +143,16 @@ struct Rec {  // per-interaction force record
 
 struct Oracle {
   dem_params prm;
+  // multi-material contact parameters (multimat_parameters.hpp:38-300): mm_pp[g_i * ng + g_j],
+  // mm_pd[g_i * nd + driver]; empty: the single sets config / config_driver
+  int mm_ng = 0, mm_nd = 0;
+  std::vector<dem_contact_params> mm_pp, mm_pd;
+  const dem_contact_params& pair_params(size_t i, size_t j) const {
+    return mm_pp.empty() ? prm.config : mm_pp[(size_t)group[i] * mm_ng + group[j]];
+  }
+  const dem_contact_params& driver_params(size_t i, size_t d) const {
+    return mm_pp.empty() ? prm.config_driver : mm_pd[(size_t)group[i] * mm_nd + d];
+  }
   size_t n = 0;
   std::vector<double> rx, ry, rz, vx, vy, vz, fx, fy, fz, wx, wy, wz, ax, ay, az, mx, my, mz, qw, qx, qy, qz, ix,
       iy, iz, mass, rad, hom, bx, by, bz;
@@ -505,7 +515,7 @@ void contact_one(Oracle& o, size_t k) {
     const V3 n = dist * inv_dist_norm;
     const V3 cp = ri - n * (rad_i + 0.5 * dn);
     bool contact = dn < 0;
-    const dem_contact_params& cpar = o.prm.config;
+    const dem_contact_params& cpar = o.pair_params(i, j);  // contact_sphere.hpp:147-152
     if (cohesive) contact = (contact || dn <= cpar.dncut);
     if (contact) {
       const V3 vi = {o.vx[i], o.vy[i], o.vz[i]};
@@ -544,7 +554,7 @@ void contact_one(Oracle& o, size_t k) {
     dvel = dv.c.vel;
     dvrot = dv.c.vrot;
   }
-  const dem_contact_params& cpar = o.prm.config_driver;
+  const dem_contact_params& cpar = o.driver_params(i, it.pj);  // contact_sphere.hpp:254-257
   if (cohesive) contact = (contact || dn <= cpar.dncut);
   if (contact) {
     const V3 v = {o.vx[i], o.vy[i], o.vz[i]};
@@ -1201,7 +1211,7 @@ void contact_one_poly(Oracle& o, size_t k) {
       dvel = dv.c.vel;
       dvrot = dv.c.vrot;
     }
-    const dem_contact_params& cpar = o.prm.config_driver;
+    const dem_contact_params& cpar = o.driver_params(p, it.pj);
     if (cohesive) contact = (contact || dn <= cpar.dncut);
     if (contact) {
       const V3 v = {o.vx[p], o.vy[p], o.vz[p]};
@@ -1222,6 +1232,7 @@ void contact_one_poly(Oracle& o, size_t k) {
   // particle i of the contact law: pi_ (= owner unless swap)
   const size_t ip = it.swap ? it.pj : it.oi;
   const size_t jp = it.swap ? it.oi : it.pj;
+  const dem_contact_params& cpar = o.pair_params(ip, jp);
   const uint32_t sub_i = it.swap ? it.psub : it.osub;
   const uint32_t sub_j = it.swap ? it.osub : it.psub;
   const PShape& shi = o.shapes[o.type[ip]];
@@ -1239,7 +1250,6 @@ void contact_one_poly(Oracle& o, size_t k) {
                     rj_m);
   }
   bool contact = d.c;
-  const dem_contact_params& cpar = o.prm.config;
   if (cohesive) contact = (contact || d.dn <= cpar.dncut);
   if (contact) {
     const V3 r_i = pos(o, ip), r_j = pos(o, jp);
@@ -1308,6 +1318,16 @@ int oracle_destroy(void* h) {
 // combined_compute_prolog.cu), so they may change between steps with the list
 // and its history kept.  A change of domain, skin or cell size needs a new
 // grid and is not supported here.
+int oracle_set_multimat(void* h, int ng, const dem_contact_params* pairs, int nd, const dem_contact_params* drivers) {
+  if (!h || ng < 0 || nd < 0) return DEM_ERR_INVALID_ARG;
+  Oracle& o = *(Oracle*)h;
+  o.mm_ng = ng;
+  o.mm_nd = nd;
+  o.mm_pp.assign(pairs, pairs + (size_t)ng * ng);
+  o.mm_pd.assign(drivers, drivers + (size_t)ng * nd);
+  if (ng == 0) o.mm_pp.clear();
+  return DEM_OK;
+}
 int oracle_set_params(void* h, const dem_params* p) {
   if (!h || !p) return DEM_ERR_INVALID_ARG;
   Oracle& o = *(Oracle*)h;

@@ -27,6 +27,7 @@ def load(rebuild: bool = True):
         sig = lambda n, a, r=C.c_int: (setattr(getattr(lib, n), "argtypes", a), setattr(getattr(lib, n), "restype", r))
         sig("oracle_create", [C.POINTER(A.Params), C.POINTER(_CTX)])
         sig("oracle_set_params", [_CTX, C.POINTER(A.Params)])
+        sig("oracle_set_multimat", [_CTX, C.c_int, C.POINTER(A.ContactParams), C.c_int, C.POINTER(A.ContactParams)])
         sig("oracle_destroy", [_CTX])
         sig("oracle_set_threads", [C.c_int])
         sig("oracle_last_error", [_CTX], C.c_char_p)
@@ -63,7 +64,7 @@ class OracleBackend:
             "interaction_count": "oracle_interaction_count", "get_interactions": "oracle_get_interactions",
             "packing_profile": "oracle_packing_profile", "set_shapes": "oracle_set_shapes",
             "contact_polyhedron": "oracle_contact_sphere", "compute_vertices": "oracle_compute_vertices",
-            "vertex_displ_over": "oracle_displ_over"}
+            "vertex_displ_over": "oracle_displ_over", "set_multimat": "oracle_set_multimat"}
 
     def __init__(self):
         self.lib = load()
