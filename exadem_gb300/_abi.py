@@ -87,6 +87,10 @@ class TuneResult(C.Structure):
                 ("mul_mode", C.c_int32)]
 
 
+class ContactState(C.Structure):
+    _fields_ = [("capacity", C.c_uint64), ("count", C.c_uint64), ("dn", PD), ("cp", PD), ("fn", PD), ("ft", PD)]
+
+
 class InteractionList(C.Structure):
     _fields_ = [("capacity", C.c_uint64), ("count", C.c_uint64), ("owner_id", PU64), ("partner_id", PU64),
                 ("type", PU16), ("swap", PU8), ("owner_sub", PU32), ("partner_sub", PU32),
@@ -168,6 +172,9 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_autotune", [_CTX, C.c_int, C.c_int, C.POINTER(TuneResult)])
     _sig(lib, "dem_set_mul_mode", [_CTX, C.c_int])
     _sig(lib, "dem_set_multimat", [_CTX, C.c_int, C.POINTER(ContactParams), C.c_int, C.POINTER(ContactParams)])
+    _sig(lib, "dem_set_analysis", [_CTX, C.c_int])
+    _sig(lib, "dem_get_contact_state", [_CTX, C.POINTER(ContactState)])
+    _sig(lib, "dem_stress_tensor", [_CTX, PD, PD])
     _sig(lib, "dem_get_mul_mode", [_CTX, C.POINTER(C.c_int)])
     VP = C.c_void_p
     _sig(lib, "dem_mlp_harvest", [_CTX, VP, VP, C.c_uint64, PU64, PU64])
@@ -205,7 +212,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
             "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_selftest_emu_mul", "dem_selftest_rolling_clip", "dem_probe_mul_rates", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
-            "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune", "dem_set_mul_mode", "dem_get_mul_mode", "dem_set_multimat", "dem_mlp_harvest",
+            "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune", "dem_set_mul_mode", "dem_get_mul_mode", "dem_set_multimat", "dem_set_analysis", "dem_get_contact_state", "dem_stress_tensor", "dem_mlp_harvest",
             "dem_mlp_init", "dem_mlp_set_params", "dem_mlp_get_params", "dem_mlp_forward", "dem_mlp_loss_grad",
             "dem_mlp_train", "dem_learned_stats"]
 

@@ -141,6 +141,8 @@ void free_compact(dem_ctx* c) {
   }
 }
 
+int ensure_contact_state(dem_ctx* c);
+
 int alloc_records(dem_ctx* c, uint64_t need) {
   if (need <= c->rcap && c->rev_idx) return DEM_OK;
   for (int d = 0; d < 3; d++) {
@@ -167,6 +169,36 @@ int alloc_records(dem_ctx* c, uint64_t need) {
   DEM_CUDA_TRY(c, cudaMalloc(&c->R.live, cap));
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->R.live, 1, cap, c->stream));
   c->rcap = cap;
+  return ensure_contact_state(c);
+}
+
+void free_contact_state(dem_ctx* c) {
+  cudaFree(c->cs.dn);
+  for (int d = 0; d < 3; d++) {
+    cudaFree(c->cs.cp[d]);
+    cudaFree(c->cs.fn[d]);
+    cudaFree(c->cs.ft[d]);
+  }
+  c->cs = ContactStateArrays{};
+  c->cs_cap = 0;
+}
+
+// contact state arrays of the records' capacity while analysis is on
+int ensure_contact_state(dem_ctx* c) {
+  if (!c->analysis) {
+    free_contact_state(c);
+    return DEM_OK;
+  }
+  if (c->cs_cap >= c->rcap && c->cs.dn) return DEM_OK;
+  free_contact_state(c);
+  const uint64_t cap = std::max<uint64_t>(c->rcap, 1);
+  DEM_CUDA_TRY(c, cudaMalloc(&c->cs.dn, cap * 8));
+  for (int d = 0; d < 3; d++) {
+    DEM_CUDA_TRY(c, cudaMalloc(&c->cs.cp[d], cap * 8));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->cs.fn[d], cap * 8));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->cs.ft[d], cap * 8));
+  }
+  c->cs_cap = cap;
   return DEM_OK;
 }
 
@@ -482,6 +514,7 @@ int copy_field(dem_ctx* c, double* dst, const double* src, uint64_t n, cudaMemcp
 namespace dem {
 int ext_alloc_iarrays(dem_ctx* c, int b, uint64_t need) { return alloc_iarrays(c, b, need); }
 int ext_alloc_records(dem_ctx* c, uint64_t need) { return alloc_records(c, need); }
+int ext_ensure_contact_state(dem_ctx* c) { return ensure_contact_state(c); }
 // every record may be nonzero again (list rebuilt, state restored, or written by
 // a kernel that does not keep the flags)
 int mark_records_live(dem_ctx* c) {
@@ -581,6 +614,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   cudaFree(c->mm_pp);
   cudaFree(c->mm_pd);
+  free_contact_state(c);
   c->fold_events();
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   c->ev_pool.clear();

@@ -112,6 +112,10 @@ struct dem_ctx {
   uint32_t* L2 = nullptr;
   uint32_t* rot_list = nullptr;  // pcap: particles whose epilog rotation runs in k_epilog_rotation
   bool damp_stale = false;       // contact parameters changed since the list's per-pair damping was set
+  // analysis (dem_set_analysis): per-interaction contact state, rcap entries
+  bool analysis = false;
+  dem::ContactStateArrays cs{};
+  uint64_t cs_cap = 0;
   // multi-material contact parameters (dem_set_multimat); mm_pp == nullptr: singlemat
   int mm_ng = 0, mm_nd = 0;
   dem_contact_params* mm_pp = nullptr;  // device, mm_ng * mm_ng
@@ -227,6 +231,7 @@ int launch_reorder_particles(dem_ctx* c);
 int launch_count_sphere(dem_ctx* c);
 int refresh_pair_damp(dem_ctx* c);  // k_neigh_sphere.cu
 int mark_records_live(dem_ctx* c);  // dem_api.cu
+int ext_ensure_contact_state(dem_ctx* c);  // dem_api.cu: analysis arrays of the records' capacity
 int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total);
 int launch_reverse_lists(dem_ctx* c);
 // k_contact_sphere.cu

@@ -158,6 +158,31 @@ __host__ __device__ inline V3 cross(V3 a, V3 b) {
 }
 __host__ __device__ inline double vnorm(V3 a) { return sqrt(dot(a, a)); }
 
+// Per-interaction contact state of the last force pass (ContactState,
+// classifier/contact_state.hpp:22-50, written by AnalysisDataPacker,
+// classifier_for_all.hpp:55-97): overlap, contact point, normal force f - ft
+// and tangential force ft.  dn == nullptr: analysis off, nothing is written.
+struct ContactStateArrays {
+  double* dn = nullptr;
+  double* cp[3] = {nullptr, nullptr, nullptr};
+  double* fn[3] = {nullptr, nullptr, nullptr};
+  double* ft[3] = {nullptr, nullptr, nullptr};
+  __device__ inline void write(uint64_t k, double d, V3 c, V3 n, V3 t) const {
+    if (!dn) return;
+    dn[k] = d;
+    cp[0][k] = c.x;
+    cp[1][k] = c.y;
+    cp[2][k] = c.z;
+    fn[0][k] = n.x;
+    fn[1][k] = n.y;
+    fn[2][k] = n.z;
+    ft[0][k] = t.x;
+    ft[1][k] = t.y;
+    ft[2][k] = t.z;
+  }
+};
+
+
 // ----------------------------------------------------------------- errors
 struct Status {
   int code = DEM_OK;

@@ -34,6 +34,7 @@ struct ContactArgs {
   int cohesive;
   int dmt;        // Hooke_DMT law combination
   ParamTable pt;  // multi-material parameters (pt.pp == nullptr: cp / cpd)
+  ContactStateArrays cs;  // analysis (cs.dn == nullptr: off)
   int screen;
   unsigned long long* n_active;
 };
@@ -97,6 +98,9 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
           ti = cross(cpos - ri, f) + mo;
           tj = cross(cpos - rj, -f) + (-mo);
           act = dn < 0;
+          a.cs.write(k, dn, cpos, f - ft, ft);  // AnalysisDataPacker: fn = f - friction
+        } else {
+          a.cs.write(k, 0.0, cpos, mk(0, 0, 0), mk(0, 0, 0));  // item.reset(), dn = 0
         }
       }
     } else {
@@ -138,6 +142,9 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
                            rad_i);  // reff = the particle's radius (contact_sphere.hpp:270)
         ti = cross(cpos - ri, f) + mo;
         act = dn < 0;
+        a.cs.write(k, dn, cpos, f - ft, ft);
+      } else {
+        a.cs.write(k, 0.0, cpos, mk(0, 0, 0), mk(0, 0, 0));
       }
     }
     if (!contact) {
@@ -202,7 +209,8 @@ int launch_contact_sphere(dem_ctx* c) {
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
   a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
   a.pt = c->ptable();
-  a.screen = c->prm.fp32_contact_screen;
+  a.cs = c->cs;
+  a.screen = c->prm.fp32_contact_screen && !c->analysis;  // analysis: every pair's state
   a.n_active = c->d_scalars + 1;
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 1, 0, sizeof(unsigned long long), c->stream));
   ProfScope ps(c, K_CONTACT, c->ni ? 1 : 0);

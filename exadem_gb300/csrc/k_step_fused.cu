@@ -52,6 +52,7 @@ struct CArgs {
   int cohesive;
   int dmt;        // Hooke_DMT law combination
   ParamTable pt;  // multi-material parameters (pt.pp == nullptr: cp / cpd)
+  ContactStateArrays cs;  // analysis (cs.dn == nullptr: off)
   int screen;
   uint32_t* L1;
   uint32_t* L2;
@@ -154,7 +155,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         dn = dist_norm - R;
         contact = emu_lt0(dn);  // comparisons of this kernel on the integer pipe (emu64.cuh)
         dncut = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]).dncut;
-        if (contact || (a.cohesive && emu_le(dn, dncut))) {  // n and cpos are used only then
+        if (contact || (a.cohesive && emu_le(dn, dncut)) || a.cs.dn) {  // n and cpos are used only then
           const double inv_dist_norm = 1.0 / dist_norm;
           n = dist * inv_dist_norm;
           cpos = ri - n * (rad_i + 0.5 * dn);
@@ -188,7 +189,8 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
       if (a.cohesive) contact = (contact || emu_le(dn, dncut));
       const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
       if (!contact) {
-        if (a.R.live[k]) {
+        a.cs.write(k, 0.0, cpos, mk(0, 0, 0), mk(0, 0, 0));  // item.reset(), dn = 0
+        if (a.R.live[k] || a.cs.dn) {
           const V3 z = mk(0, 0, 0);
           write_result(a, k, z, z, z, z, z);
           a.R.live[k] = 0;
@@ -203,6 +205,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         const V3 tj = is_vv ? cross(cpos - rj, -f) + (-mo) : mk(0, 0, 0);
         write_result(a, k, mk(0, 0, 0), mo, f, ti, tj);
         a.R.live[k] = 1;
+        a.cs.write(k, dn, cpos, f - mk(0, 0, 0), mk(0, 0, 0));  // ft = 0 before contact
       } else {
         heavy = true;
       }
@@ -283,6 +286,7 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
     }
     write_result(a, k, ft, mo, f, ti, tj);
     a.R.live[k] = 1;
+    if (a.cs.dn) a.cs.write(k, a.D[0][w], mk(a.D[4][w], a.D[5][w], a.D[6][w]), f - ft, ft);
   }
 }
 
@@ -456,7 +460,8 @@ CArgs make_cargs(dem_ctx* c) {
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
   a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
   a.pt = c->ptable();
-  a.screen = c->prm.fp32_contact_screen;
+  a.cs = c->cs;
+  a.screen = c->prm.fp32_contact_screen && !c->analysis;  // analysis: every pair's state
   a.L1 = c->L1;
   a.L2 = c->L2;
   for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];

@@ -281,6 +281,25 @@ class System:
                 pd[a * nd + d] = drivers[a][d]
         self._check(self.b.set_multimat(self.h, ng, pp, nd, pd), "set_multimat")
 
+    def set_analysis(self, on: bool) -> None:
+        """dem_set_analysis: contact passes write the per-interaction contact state."""
+        self._check(self.b.set_analysis(self.h, int(bool(on))), "set_analysis")
+
+    def contact_state(self) -> dict:
+        """dem_get_contact_state, in the order of interactions()."""
+        cnt = self.interaction_count()
+        out = {"dn": np.zeros(cnt), "cp": np.zeros(3 * cnt), "fn": np.zeros(3 * cnt), "ft": np.zeros(3 * cnt)}
+        st = A.ContactState(cnt, 0, A.ptr(out["dn"]), A.ptr(out["cp"]), A.ptr(out["fn"]), A.ptr(out["ft"]))
+        self._check(self.b.get_contact_state(self.h, C.byref(st)), "get_contact_state")
+        return out
+
+    def stress_tensor(self) -> tuple:
+        """dem_stress_tensor: (per particle 9-component stress in the particles()
+        order of sort_by_id=False, total over the particles)."""
+        stress, total = np.zeros(9 * self.n), np.zeros(9)
+        self._check(self.b.stress_tensor(self.h, A.ptr(stress), A.ptr(total)), "stress_tensor")
+        return stress.reshape(self.n, 9), total
+
     def set_mul_mode(self, mode: int) -> None:
         """dem_set_mul_mode: which integration multiplies run on the integer pipe (same bits)."""
         self._check(self.b.set_mul_mode(self.h, int(mode)), "set_mul_mode")

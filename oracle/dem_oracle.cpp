@@ -139,6 +139,10 @@ inline bool key_eq(const Inter& a, const Inter& b) {  // interaction_pair.hpp:18
 struct Rec {  // per-interaction force record
   V3 f, ti, tj;
   int active;
+  // contact state (AnalysisDataPacker, classifier_for_all.hpp:55-97): dn (0 when
+  // the pair does not touch), contact point, fn = f - friction, ft = friction
+  double sdn = 0;
+  V3 scp{}, sfn{}, sft{};
 };
 
 struct Oracle {
@@ -530,9 +534,14 @@ void contact_one(Oracle& o, size_t k) {
       rc.ti = cross(cp - ri, f) + it.moment;       // compute_moments
       rc.tj = cross(cp - rj, -f) + (-it.moment);
       rc.active = dn < 0;
+      rc.sdn = dn;
+      rc.scp = cp;
+      rc.sfn = f - it.friction;
+      rc.sft = it.friction;
     } else {
       it.friction = {0, 0, 0};
       it.moment = {0, 0, 0};
+      rc.scp = cp;  // item.reset(), dn = 0, the detector's contact point
     }
     return;
   }
@@ -565,6 +574,10 @@ void contact_one(Oracle& o, size_t k) {
     rc.f = f;
     rc.ti = cross(cp - ri, f) + it.moment;
     rc.active = dn < 0;
+    rc.sdn = dn;
+    rc.scp = cp;
+    rc.sfn = f - it.friction;
+    rc.sft = it.friction;
   } else {
     it.friction = {0, 0, 0};
     it.moment = {0, 0, 0};
@@ -1574,6 +1587,62 @@ int oracle_get_interactions(void* h, dem_interaction_list* l) {
   }
   return DEM_OK;
 }
+// contact state of the last force pass, in InteractionPair order (spheres)
+int oracle_get_contact_state(void* h, dem_contact_state* out) {
+  Oracle& o = *(Oracle*)h;
+  if (o.poly) return DEM_ERR_UNSUPPORTED;
+  out->count = o.inter.size();
+  if (out->capacity < o.inter.size()) return DEM_ERR_INVALID_ARG;
+  for (size_t k = 0; k < o.rec.size() && k < o.inter.size(); k++) {
+    const Rec& r = o.rec[k];
+    if (out->dn) out->dn[k] = r.sdn;
+    const double c3[3] = {r.scp.x, r.scp.y, r.scp.z}, n3[3] = {r.sfn.x, r.sfn.y, r.sfn.z},
+                 t3[3] = {r.sft.x, r.sft.y, r.sft.z};
+    for (int d = 0; d < 3; d++) {
+      if (out->cp) out->cp[3 * k + d] = c3[d];
+      if (out->fn) out->fn[3 * k + d] = n3[d];
+      if (out->ft) out->ft[3 * k + d] = t3[d];
+    }
+  }
+  return DEM_OK;
+}
+// stress_tensor (src/interaction/stress_tensor.cu:40-75): per particle, its own
+// touching pairs then those where it is the partner, in InteractionPair order;
+// m += f c^T row major; total: the sum over the particles in id order
+int oracle_stress_tensor(void* h, double* stress, double* total) {
+  Oracle& o = *(Oracle*)h;
+  if (o.poly) return DEM_ERR_UNSUPPORTED;
+  std::vector<double> m(9 * o.n, 0.0);
+  auto add = [](double* a, const V3& u, const V3& v) {
+    const double uu[3] = {u.x, u.y, u.z}, vv[3] = {v.x, v.y, v.z};
+    for (int r = 0; r < 3; r++)
+      for (int c = 0; c < 3; c++) a[3 * r + c] = a[3 * r + c] + uu[r] * vv[c];
+  };
+  for (size_t i = 0; i < o.n; i++) {
+    double* a = &m[9 * i];
+    const V3 r = pos(o, i);
+    if (o.own_first[i] >= 0)
+      for (int32_t k = o.own_first[i]; k < o.own_first[i] + o.own_cnt[i]; k++) {
+        const Rec& q = o.rec[k];
+        if (q.sdn < 0.0) add(a, q.sfn + q.sft, q.scp - r);
+      }
+    for (size_t p = o.rev_off[i]; p < o.rev_off[i + 1]; p++) {
+      const Rec& q = o.rec[o.rev_idx[p]];
+      if (q.sdn < 0.0) add(a, -(q.sfn + q.sft), q.scp - r);
+    }
+  }
+  if (stress) std::copy(m.begin(), m.end(), stress);
+  if (total) {
+    std::vector<size_t> by_id(o.n);
+    for (size_t i = 0; i < o.n; i++) by_id[i] = i;
+    std::sort(by_id.begin(), by_id.end(), [&](size_t a, size_t b) { return o.id[a] < o.id[b]; });
+    for (int q = 0; q < 9; q++) total[q] = 0.0;
+    for (size_t i : by_id)
+      for (int q = 0; q < 9; q++) total[q] = total[q] + m[9 * i + q];
+  }
+  return DEM_OK;
+}
+int oracle_set_analysis(void*, int) { return DEM_OK; }  // the oracle always keeps the state
 int oracle_packing_profile(void* h, int nslabs, double zlo, double zhi, double* out) {
   Oracle& o = *(Oracle*)h;
   if (nslabs <= 0 || !(zhi > zlo)) return DEM_ERR_INVALID_ARG;

@@ -28,6 +28,9 @@ def load(rebuild: bool = True):
         sig("oracle_create", [C.POINTER(A.Params), C.POINTER(_CTX)])
         sig("oracle_set_params", [_CTX, C.POINTER(A.Params)])
         sig("oracle_set_multimat", [_CTX, C.c_int, C.POINTER(A.ContactParams), C.c_int, C.POINTER(A.ContactParams)])
+        sig("oracle_set_analysis", [_CTX, C.c_int])
+        sig("oracle_get_contact_state", [_CTX, C.POINTER(A.ContactState)])
+        sig("oracle_stress_tensor", [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_double)])
         sig("oracle_destroy", [_CTX])
         sig("oracle_set_threads", [C.c_int])
         sig("oracle_last_error", [_CTX], C.c_char_p)
@@ -64,7 +67,9 @@ class OracleBackend:
             "interaction_count": "oracle_interaction_count", "get_interactions": "oracle_get_interactions",
             "packing_profile": "oracle_packing_profile", "set_shapes": "oracle_set_shapes",
             "contact_polyhedron": "oracle_contact_sphere", "compute_vertices": "oracle_compute_vertices",
-            "vertex_displ_over": "oracle_displ_over", "set_multimat": "oracle_set_multimat"}
+            "vertex_displ_over": "oracle_displ_over", "set_multimat": "oracle_set_multimat",
+            "set_analysis": "oracle_set_analysis", "get_contact_state": "oracle_get_contact_state",
+            "stress_tensor": "oracle_stress_tensor"}
 
     def __init__(self):
         self.lib = load()
