@@ -25,10 +25,13 @@ __device__ __forceinline__ void add_tensor(double* m, V3 u, V3 v) {
 
 // ComputeStressTensorFunc (stress_tensor.cu:40-75) for every pair of a particle:
 // its own pairs, then those where it is the partner (the canonical order of
-// the force gather); a pair counts when dn < 0.
-__global__ void k_stress(PArrays P, ContactStateArrays cs, const uint32_t* __restrict__ own_off,
-                         const uint32_t* __restrict__ rev_off, const uint32_t* __restrict__ rev_idx, uint64_t n,
-                         double* __restrict__ out) {
+// the force gather); a pair counts when dn < 0.  The state is in the contact
+// law's frame: its particle i (I.i() = pi_) takes +(fn + ft), its particle j
+// -(fn + ft).  pi_ is the owner unless the polyhedron pair is swapped
+// (interaction_pair.hpp:70-112; swap = bit 15 of meta, nullptr for spheres).
+__global__ void k_stress(PArrays P, ContactStateArrays cs, const uint32_t* __restrict__ meta,
+                         const uint32_t* __restrict__ own_off, const uint32_t* __restrict__ rev_off,
+                         const uint32_t* __restrict__ rev_idx, uint64_t n, double* __restrict__ out) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   const V3 r = mk(P.f[RX][s], P.f[RY][s], P.f[RZ][s]);
@@ -37,20 +40,21 @@ __global__ void k_stress(PArrays P, ContactStateArrays cs, const uint32_t* __res
     if (!(cs.dn[k] < 0.0)) continue;
     const V3 fij = mk(cs.fn[0][k], cs.fn[1][k], cs.fn[2][k]) + mk(cs.ft[0][k], cs.ft[1][k], cs.ft[2][k]);
     const V3 cij = mk(cs.cp[0][k], cs.cp[1][k], cs.cp[2][k]) - r;
-    add_tensor(m, fij, cij);
+    const bool swap = meta && ((meta[k] >> 15) & 1u);
+    add_tensor(m, swap ? -fij : fij, cij);
   }
   for (uint32_t q = rev_off[s]; q < rev_off[s + 1]; q++) {
     const uint32_t k = rev_idx[q];
     if (!(cs.dn[k] < 0.0)) continue;
     const V3 fij = mk(cs.fn[0][k], cs.fn[1][k], cs.fn[2][k]) + mk(cs.ft[0][k], cs.ft[1][k], cs.ft[2][k]);
     const V3 cji = mk(cs.cp[0][k], cs.cp[1][k], cs.cp[2][k]) - r;
-    add_tensor(m, -fij, cji);
+    const bool swap = meta && ((meta[k] >> 15) & 1u);
+    add_tensor(m, swap ? fij : -fij, cji);
   }
   for (int c = 0; c < 9; c++) out[9 * s + c] = m[c];
 }
 
 int need_analysis(dem_ctx* c) {
-  if (c->poly) return c->fail(DEM_ERR_UNSUPPORTED, "the contact state is written for spheres only");
   if (!c->analysis || !c->cs.dn) return c->fail(DEM_ERR_STATE, "analysis is off: dem_set_analysis(ctx, 1) before the step");
   if (!c->have_list) return c->fail(DEM_ERR_STATE, "no interaction list");
   return DEM_OK;
@@ -121,7 +125,8 @@ extern "C" int dem_stress_tensor(dem_ctx* c, double* stress, double* total) {
   if (n) {
     double* d = nullptr;
     DEM_CUDA_TRY(c, cudaMalloc(&d, 9 * n * sizeof(double)));
-    k_stress<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->P[c->pcur], c->cs, c->own_off[c->icur],
+    const uint32_t* meta = c->poly ? c->I[c->icur].meta : nullptr;
+    k_stress<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->P[c->pcur], c->cs, meta, c->own_off[c->icur],
                                                                   c->rev_off, c->rev_idx, n, d);
     const cudaError_t e = cudaGetLastError();
     DEM_CUDA_TRY(c, cudaMemcpyAsync(h.data(), d, 9 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));

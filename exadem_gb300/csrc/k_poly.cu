@@ -1017,6 +1017,7 @@ struct PCArgs {
   int cohesive;
   int dmt;        // Hooke_DMT law combination
   ParamTable pt;  // multi-material parameters (pt.pp == nullptr: cp / cpd)
+  ContactStateArrays cs;  // analysis, in the contact law's frame (cs.dn == nullptr: off)
   uint32_t* L2;
   double* D[7];
   unsigned long long* cnt;  // [1] = L2 count
@@ -1146,11 +1147,13 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
     if (!contact) {
       const V3 z = mk(0, 0, 0);
       pwrite(a, k, z, z, z, z, z);
+      a.cs.write(k, 0.0, d.cp, z, z);  // item.reset(), dn = 0, the detector's contact point
     } else if (a.cohesive && d.dn >= 0) {
       const dem_contact_params& hkp = *hp;
       const double fn_value = (hkp.fc / hkp.dncut) * d.dn - hkp.fc;
       const V3 f = mk(0, 0, 0) + fn_value * d.n;
       const V3 ti = cross(d.cp - ri, f) + mo;
+      a.cs.write(k, d.dn, d.cp, f - mk(0, 0, 0), mk(0, 0, 0));  // fn = f - friction, friction reset
       if (!is_pp) {
         pwrite(a, k, mk(0, 0, 0), mo, f, ti, mk(0, 0, 0));
       } else {
@@ -1218,6 +1221,7 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
                   mk(d.center[0], d.center[1], d.center[2]), mk(d.vel[0], d.vel[1], d.vel[2]),
                   mk(d.vrot[0], d.vrot[1], d.vrot[2]), a.dmt, reff);
       pwrite(a, k, ft, mo, f, cross(cpos - r, f) + mo, mk(0, 0, 0));
+      a.cs.write(k, dn, cpos, f - ft, ft);
       continue;
     }
     const Roles R = roles(a, k);
@@ -1237,6 +1241,7 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
                 f, mo, w_i, r_j, v_j, w_j, a.dmt, reff);
     const V3 t_i = cross(cpos - r_i, f) + mo;
     const V3 t_j = cross(cpos - r_j, -f) + (-mo);
+    a.cs.write(k, dn, cpos, f - ft, ft);  // the law's particle i (polyhedron/contact.hpp:191-210)
     if ((meta >> 15) & 1u)
       pwrite(a, k, ft, mo, -f, t_j, t_i);
     else
@@ -1528,6 +1533,7 @@ int launch_contact_poly(dem_ctx* c) {
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
   a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
   a.pt = c->ptable();
+  a.cs = c->cs;
   a.L2 = c->L2;
   for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];
   a.cnt = c->d_scalars + 3;

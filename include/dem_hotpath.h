@@ -366,12 +366,13 @@ int dem_packing_profile(dem_ctx* ctx, int nslabs, double zlo, double zhi, double
 /* ---- analysis -------------------------------------------------------------
  * Contact state and stress tensor (classifier/contact_state.hpp:22-50,
  * AnalysisDataPacker classifier_for_all.hpp:55-97, stress_tensor.cu:30-160).
- * With dem_set_analysis(ctx, 1) every sphere contact pass writes, per
- * interaction, the overlap dn (0 for a pair that does not touch), the contact
- * point, the normal force f - ft and the tangential force ft; the FP32
- * separation screen and the skipped zero records are off while it is on, so
- * every pair's state is computed.  Spheres only (DEM_ERR_UNSUPPORTED for
- * polyhedra).                                                              */
+ * With dem_set_analysis(ctx, 1) every contact pass writes, per interaction,
+ * the overlap dn (0 for a pair that does not touch), the contact point, the
+ * normal force f - ft and the tangential force ft; the FP32 separation screen
+ * and the skipped zero records are off while it is on, so every pair's state
+ * is computed.  A polyhedron pair's state is in its contact law's frame: f is
+ * the force on pi_, which is the partner when the pair is swapped
+ * (interaction_pair.hpp:70-112, polyhedron/contact.hpp:191-210).          */
 typedef struct dem_contact_state {
   uint64_t capacity;  /* entries the caller's arrays hold                      */
   uint64_t count;     /* written: interactions, in dem_get_interactions order  */
@@ -384,8 +385,8 @@ int dem_set_analysis(dem_ctx* ctx, int on);
 int dem_get_contact_state(dem_ctx* ctx, dem_contact_state* out);
 /* stress_tensor: for every touching pair (dn < 0) of the last force pass,
  * fij = fn + ft and cij = cp - r_i add the outer product fij cij^T (row major,
- * m[3 r + c] = fij_r cij_c) to particle i, and -fij (cp - r_j)^T to the
- * partner j (not to a periodic image).  Each particle sums its own pairs, then
+ * m[3 r + c] = fij_r cij_c) to the law's particle i, and -fij (cp - r_j)^T to
+ * its particle j (not to a periodic image; drivers: particle i only).  Each particle sums its own pairs, then
  * the pairs where it is the partner, in InteractionPair order (the reference
  * adds with unordered atomics).  stress: 9 n doubles in the particles'
  * internal order (dem_get_particles); total: the 9-component sum over the

@@ -1236,9 +1236,14 @@ void contact_one_poly(Oracle& o, size_t k) {
       rc.f = f;
       rc.ti = cross(cp - r, f) + it.moment;
       rc.active = dn < 0;
+      rc.sdn = dn;  // polyhedron/contact.hpp:286-303
+      rc.scp = cp;
+      rc.sfn = f - it.friction;
+      rc.sft = it.friction;
     } else {
       it.friction = {0, 0, 0};
       it.moment = {0, 0, 0};
+      rc.scp = cp;  // dn = 0; the detector's contact point
     }
     return;
   }
@@ -1287,9 +1292,15 @@ void contact_one_poly(Oracle& o, size_t k) {
       rc.tj = t_i;
     }
     rc.active = d.dn < 0;
+    // the state in the contact law's frame (polyhedron/contact.hpp:191-210)
+    rc.sdn = d.dn;
+    rc.scp = d.cp;
+    rc.sfn = f - it.friction;
+    rc.sft = it.friction;
   } else {
     it.friction = {0, 0, 0};
     it.moment = {0, 0, 0};
+    rc.scp = d.cp;  // item.reset(), dn = 0
   }
 }
 
@@ -1587,10 +1598,10 @@ int oracle_get_interactions(void* h, dem_interaction_list* l) {
   }
   return DEM_OK;
 }
-// contact state of the last force pass, in InteractionPair order (spheres)
+// contact state of the last force pass, in InteractionPair order (polyhedron
+// pairs: in the contact law's frame, particle i = pi_)
 int oracle_get_contact_state(void* h, dem_contact_state* out) {
   Oracle& o = *(Oracle*)h;
-  if (o.poly) return DEM_ERR_UNSUPPORTED;
   out->count = o.inter.size();
   if (out->capacity < o.inter.size()) return DEM_ERR_INVALID_ARG;
   for (size_t k = 0; k < o.rec.size() && k < o.inter.size(); k++) {
@@ -1608,10 +1619,10 @@ int oracle_get_contact_state(void* h, dem_contact_state* out) {
 }
 // stress_tensor (src/interaction/stress_tensor.cu:40-75): per particle, its own
 // touching pairs then those where it is the partner, in InteractionPair order;
-// m += f c^T row major; total: the sum over the particles in id order
+// m += f c^T row major; total: the sum over the particles in id order.  I.i()
+// (pi_: the owner unless swap) takes +(fn + ft), I.j() -(fn + ft).
 int oracle_stress_tensor(void* h, double* stress, double* total) {
   Oracle& o = *(Oracle*)h;
-  if (o.poly) return DEM_ERR_UNSUPPORTED;
   std::vector<double> m(9 * o.n, 0.0);
   auto add = [](double* a, const V3& u, const V3& v) {
     const double uu[3] = {u.x, u.y, u.z}, vv[3] = {v.x, v.y, v.z};
@@ -1624,11 +1635,13 @@ int oracle_stress_tensor(void* h, double* stress, double* total) {
     if (o.own_first[i] >= 0)
       for (int32_t k = o.own_first[i]; k < o.own_first[i] + o.own_cnt[i]; k++) {
         const Rec& q = o.rec[k];
-        if (q.sdn < 0.0) add(a, q.sfn + q.sft, q.scp - r);
+        const V3 fij = q.sfn + q.sft;
+        if (q.sdn < 0.0) add(a, o.inter[k].swap ? -fij : fij, q.scp - r);
       }
     for (size_t p = o.rev_off[i]; p < o.rev_off[i + 1]; p++) {
       const Rec& q = o.rec[o.rev_idx[p]];
-      if (q.sdn < 0.0) add(a, -(q.sfn + q.sft), q.scp - r);
+      const V3 fij = q.sfn + q.sft;
+      if (q.sdn < 0.0) add(a, o.inter[o.rev_idx[p]].swap ? fij : -fij, q.scp - r);
     }
   }
   if (stress) std::copy(m.begin(), m.end(), stress);
