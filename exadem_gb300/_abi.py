@@ -69,6 +69,12 @@ class Cylinder(C.Structure):
     _fields_ = [("radius", D), ("axis", D * 3), ("center", D * 3), ("vel", D * 3), ("vrot", D * 3)]
 
 
+class Mesh(C.Structure):
+    _fields_ = [("nv", C.c_int32), ("ne", C.c_int32), ("nf", C.c_int32), ("vertices", C.POINTER(D)),
+                ("edges", C.POINTER(C.c_int32)), ("face_offsets", C.POINTER(C.c_int32)),
+                ("face_vertices", C.POINTER(C.c_int32)), ("minkowski", D), ("center", D * 3), ("quat", D * 4)]
+
+
 class State(C.Structure):
     _fields_ = [("kinetic_energy", D * 3), ("rotation_energy", D * 3), ("mass", D),
                 ("n_particles", C.c_uint64), ("n_interactions", C.c_uint64),
@@ -155,6 +161,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_get_particles", [_CTX, C.POINTER(Particles), C.c_int])
     _sig(lib, "dem_register_surface", [_CTX, C.POINTER(Surface)])
     _sig(lib, "dem_register_cylinder", [_CTX, C.POINTER(Cylinder)])
+    _sig(lib, "dem_register_mesh", [_CTX, C.POINTER(Mesh)])
     _sig(lib, "dem_particle_displ_over", [_CTX, C.POINTER(C.c_int)])
     for name in ["dem_update_particle_neighbors", "dem_reset_force_moment", "dem_gravity_force",
                  "dem_contact_sphere", "dem_force_to_accel", "dem_combined_compute_prolog",
@@ -205,6 +212,7 @@ def declare_library(lib) -> None:
 # Symbols declared in include/dem_hotpath.h, dem_workloads.h, dem_selftest.h and dem_learned.h.
 EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stream", "dem_set_params",
             "dem_set_particles", "dem_get_particles", "dem_register_surface", "dem_register_cylinder",
+            "dem_register_mesh",
             "dem_particle_displ_over", "dem_update_particle_neighbors", "dem_reset_force_moment",
             "dem_gravity_force", "dem_contact_sphere", "dem_force_to_accel", "dem_combined_compute_prolog",
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",

@@ -460,6 +460,7 @@ int update_neighbors(dem_ctx* c) {
     return DEM_OK;
   }
   int rc;
+  if (!c->capturing && (rc = ensure_mesh_bins(c))) return rc;
   if ((rc = launch_bin_particles(c))) return rc;
   if ((rc = launch_reorder_particles(c))) return rc;
   if ((rc = launch_count_sphere(c))) return rc;
@@ -650,6 +651,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   free_graph(c);
   mlp_free(c);
   cudaFree(c->drv_dev);
+  free_meshes(c);
   cudaFree(c->grids_dev);
   cudaFree(c->coff_dev);
   cudaFree(c->pfirst_dev);
@@ -834,6 +836,7 @@ static int add_driver(dem_ctx* c, const DriverDev& d) {
   return DEM_OK;
 }
 
+
 int dem_register_surface(dem_ctx* c, const dem_surface* s) {
   if (!c || !s) return DEM_ERR_INVALID_ARG;
   DriverDev d{};
@@ -986,6 +989,7 @@ int dem_set_shapes(dem_ctx* c, const dem_shape* shapes, int nshapes) {
     mv = std::max(mv, d.nv);
   }
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (!c->meshes.empty()) return c->fail(DEM_ERR_UNSUPPORTED, "mesh drivers are built for sphere systems");
   cudaFree(c->shapes_dev);
   c->shapes_dev = nullptr;
   DEM_CUDA_TRY(c, cudaMalloc(&c->shapes_dev, sizeof(ShapeDev) * nshapes));
@@ -1035,6 +1039,7 @@ int dem_step(dem_ctx* c, int nsteps) {
   if (c->mm_pp && c->mm_nd != c->ndrv)
     return c->fail(DEM_ERR_STATE, "drivers were registered after dem_set_multimat: set the table again");
   if ((rc = refresh_pair_damp(c))) return rc;  // contact parameters changed since the list was built
+  if ((rc = ensure_mesh_bins(c))) return rc;    // before a graph capture of the rebuild
   // graph replay unless per-kernel timing is on (events cannot be recorded inside a graph)
   if (c->prm.graph_step && c->prm.fused_step && !c->poly && nsteps > 0 && !c->prof_on) return step_graph(c, nsteps);
   for (int s = 0; s < nsteps; s++) {
@@ -1175,7 +1180,8 @@ int dem_get_interactions(dem_ctx* c, dem_interaction_list* l) {
       if (l->owner_id) l->owner_id[w] = id[owner[k]];
       if (l->partner_id) {
         const uint32_t t = meta_type(meta[k]);
-        const bool drv = t == DEM_ITYPE_VERTEX_CYLINDER || t == DEM_ITYPE_VERTEX_SURFACE;
+        const bool drv = t == DEM_ITYPE_VERTEX_CYLINDER || t == DEM_ITYPE_VERTEX_SURFACE ||
+                         (t >= DEM_ITYPE_VERTEX_MESH_VERTEX && t <= DEM_ITYPE_VERTEX_MESH_FACE);
         l->partner_id[w] = drv ? pid[k] - driver_base(owner[k]) : pid[k];
       }
       if (l->type) l->type[w] = (uint16_t)meta_type(meta[k]);
@@ -1234,3 +1240,8 @@ int dem_packing_profile(dem_ctx* c, int nslabs, double zlo, double zhi, double* 
 }
 
 }  // extern "C"
+
+// add_driver for dem_register_mesh (k_mesh.cu)
+namespace dem {
+int ext_add_driver(dem_ctx* c, const DriverDev& d) { return add_driver(c, d); }
+}  // namespace dem

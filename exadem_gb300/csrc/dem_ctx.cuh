@@ -30,6 +30,22 @@ constexpr int SC_ROT_CNT = 6, SC_LEARNED_OVF = 8, SC_LEARNED_BINS = 16;
 // enumeration; the fill pass copies them instead of deciding again
 constexpr int FEAT_SLOTS = 16;
 
+// one mesh driver (dem_register_mesh): device arrays, the host copy of the
+// world vertices and topology the bin grid is built from, and the sphere
+// radius bound and skin the current bins were built for
+struct MeshStore {
+  double* vtx = nullptr;  // 3 nv: x | y | z
+  int* e = nullptr;
+  int* fo = nullptr;
+  int* fv = nullptr;
+  uint32_t* boff = nullptr;
+  uint32_t* bitem = nullptr;
+  std::vector<double> hx, hy, hz;
+  std::vector<int> he, hfo, hfv;
+  double bin_rad = -1.0, bin_skin = -1.0;
+  dem::MeshDev dev{};
+};
+
 struct dem_ctx {
   dem_params prm{};
   cudaStream_t stream = nullptr;
@@ -48,6 +64,8 @@ struct dem_ctx {
   int ndrv = 0;
   dem::DriverDev drv_host[DEM_MAX_DRIVERS]{};
   dem::DriverDev* drv_dev = nullptr;
+  std::vector<MeshStore> meshes;        // mesh drivers (DriverDev::mesh indexes)
+  dem::MeshDev* mesh_dev = nullptr;     // device copy of meshes[k].dev
 
   // systems (batched context); one system spanning prm's domain otherwise
   std::vector<dem_system> systems;   // empty: single system from prm
@@ -234,6 +252,10 @@ int mark_records_live(dem_ctx* c);  // dem_api.cu
 int ext_ensure_contact_state(dem_ctx* c);  // dem_api.cu: analysis arrays of the records' capacity
 int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total);
 int launch_reverse_lists(dem_ctx* c);
+// k_mesh.cu: bins of the mesh drivers for the current radius bound and skin
+int ensure_mesh_bins(dem_ctx* c);
+void free_meshes(dem_ctx* c);
+int ext_add_driver(dem_ctx* c, const dem::DriverDev& d);  // dem_api.cu
 // k_contact_sphere.cu
 int launch_contact_sphere(dem_ctx* c);
 int launch_gather_forces(dem_ctx* c);

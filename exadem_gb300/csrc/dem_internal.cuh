@@ -99,9 +99,32 @@ struct ParamTable {
 
 // drivers in device-friendly form (stationary; vrot enters the relative velocity)
 struct DriverDev {
-  int kind;  // 0 surface, 1 cylinder
+  int kind;  // 0 surface, 1 cylinder, 2 mesh
+  int mesh;  // kind 2: index into the context's mesh table
   double offset, radius;
   double normal[3], center[3], center_proj[3], axis[3], vel[3], vrot[3];
+};
+
+// Mesh driver (RShapeDriver, rshape.hpp:104-420) on the device.  World vertices
+// center + quat * v in SoA; edges as vertex pairs; faces as CSR vertex lists.
+// A uniform bin grid covers the mesh: bin b lists (kind << 30 | index, kind 0
+// vertex, 1 edge, 2 face, in (kind, index) order) every feature whose Verlet
+// filter can pass for a sphere centred in b; a sphere outside the grid passes
+// none.  The bin of a point is floor((p - lo) * inv_bs) per axis.
+struct MeshDev {
+  int nv, ne, nf;
+  double r;  // Minkowski radius
+  const double* x;
+  const double* y;
+  const double* z;
+  const int* e;   // 2 ne
+  const int* fo;  // nf + 1
+  const int* fv;  // fo[nf]
+  double lo[3];
+  double inv_bs;
+  int dims[3];
+  const uint32_t* boff;   // bins + 1
+  const uint32_t* bitem;  // boff[bins]
 };
 struct GridDev {
   int dims[3];

@@ -17,6 +17,7 @@
 // squared distance, see DESIGN) takes the no-contact branch (history reset)
 // without any FP64 work; every other pair runs the full FP64 law.
 #include "contact_core.cuh"
+#include "mesh_core.cuh"
 
 namespace dem {
 namespace {
@@ -28,6 +29,7 @@ struct ContactArgs {
   uint64_t ni;
   SysView sv;  // periodic lengths of the owner's system
   const DriverDev* drv;
+  const MeshDev* mesh;
   dem_contact_params cp;   // particle-particle
   dem_contact_params cpd;  // particle-driver
   double dt;
@@ -107,7 +109,14 @@ __global__ void __launch_bounds__(128) k_contact(ContactArgs a) {
       const DriverDev& d = a.drv[j];
       double dn;
       V3 n = mk(0, 0, 0), cpos = mk(0, 0, 0), dpos, dvel, dvrot;
-      if (d.kind == 0) {
+      if (d.kind == 2) {
+        // ContactLawRShapeDriverFunc (contact_sphere.hpp:300-396): detect<7|8|9>
+        const DetD q = mesh_detect(a.mesh[d.mesh], type, a.I.sub[k] >> 16, ri, rad_i);
+        dn = q.dn;
+        contact = q.c;
+        n = q.n;
+        cpos = q.cp;
+      } else if (d.kind == 0) {
         const V3 nrm = mk(d.normal[0], d.normal[1], d.normal[2]);
         const V3 proj = dot(ri, nrm) * nrm;
         const V3 s2p = -(mk(d.center_proj[0], d.center_proj[1], d.center_proj[2]) - proj);
@@ -203,6 +212,7 @@ int launch_contact_sphere(dem_ctx* c) {
   a.ni = c->ni;
   a.sv = c->sysview();
   a.drv = c->drv_dev;
+  a.mesh = c->mesh_dev;
   a.cp = c->prm.config;
   a.cpd = c->prm.config_driver;
   a.dt = c->prm.dt;

@@ -18,6 +18,7 @@
 // its drivers; a system rebuilt without its own trigger kept its slots, and
 // its previous list is copied as is (so its list is the one it has alone).
 #include "dem_ctx.cuh"
+#include "mesh_core.cuh"
 
 namespace dem {
 namespace {
@@ -30,6 +31,7 @@ struct BPArgs {
   const uint32_t* cell_of;
   const DriverDev* drv;
   int ndrv;
+  const MeshDev* mesh;  // mesh drivers (DriverDev::mesh)
   double skin;
   double rcut2;
   // FP32 broad phase: cell-relative coordinates and radii, cell sizes, skin
@@ -107,9 +109,19 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
   const int2 dr = a.sv.drange[sys];
   for (int k = dr.x; k < dr.x + dr.y; k++) {
     const DriverDev& d = a.drv[k];
+    if (d.kind == 2) {
+      // detection_sphere_driver (nbh_sphere.hpp:25-86): every mesh vertex, edge
+      // and face of the sphere's bin that passes its filter; partner sub = feature
+      const MeshDev& m = a.mesh[d.mesh];
+      mesh_bin_items(m, ri, [&](uint32_t kind, uint32_t j) {
+        if (mesh_filter(m, kind, j, a.skin, ri, radi))
+          emit((uint32_t)k, (uint64_t)k, make_meta(DEM_ITYPE_VERTEX_MESH_VERTEX + kind, 0, 0, 0, false), j << 16);
+      });
+      continue;
+    }
     if (driver_filter(d, radi + a.skin, ri))
       emit((uint32_t)k, (uint64_t)k,
-           make_meta(d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER, 0, 0, 0, false));
+           make_meta(d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER, 0, 0, 0, false), 0u);
   }
   float xri = 0.f, yri = 0.f, zri = 0.f, rfi = 0.f, si = 0.f, cmax = 0.f;
   const float csx = (float)g.csz[0], csy = (float)g.csz[1], csz = (float)g.csz[2];
@@ -184,7 +196,7 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
             keep = (d2 > 0.0 && d2 < rmax * rmax && d2 < a.rcut2) ? 1 : 0;
           }
           if (!keep) continue;
-          emit(q, idj, make_meta(DEM_ITYPE_VERTEX_VERTEX, sx, sy, sz, ghost));
+          emit(q, idj, make_meta(DEM_ITYPE_VERTEX_VERTEX, sx, sy, sz, ghost), 0u);
         }
       }
     }
@@ -200,12 +212,14 @@ __global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt, const uint32_t* __
     return;
   }
   uint32_t m = 0;
-  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t) { m++; });
+  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t, uint32_t) { m++; });
   cnt[s] = m;
 }
 
-__device__ inline bool key_less(uint64_t pa, uint32_t ta, uint64_t pb, uint32_t tb) {
-  return pa < pb || (pa == pb && ta < tb);
+// InteractionPair order inside the owner: (partner id, type, partner sub); swap
+// and the owner sub are 0 for spheres
+__device__ inline bool key_less(uint64_t pa, uint32_t ta, uint32_t sa, uint64_t pb, uint32_t tb, uint32_t sb) {
+  return pa < pb || (pa == pb && (ta < tb || (ta == tb && sa < sb)));
 }
 
 template <bool F32>
@@ -234,29 +248,31 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
     return;
   }
   uint32_t w = b;
-  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta) {
+  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta, uint32_t sub) {
     if (w < e) {
       dst.partner[w] = q;
       dst.pid[w] = pid;
       dst.meta[w] = meta;
+      dst.sub[w] = sub;
     }
     w++;
   });
-  // InteractionPair order inside the owner: (partner id, type); swap and subs are 0 for spheres
   for (uint32_t x = b + 1; x < e; x++) {
     const uint64_t pk = dst.pid[x];
-    const uint32_t mk_ = dst.meta[x], qk = dst.partner[x];
+    const uint32_t mk_ = dst.meta[x], qk = dst.partner[x], sk = dst.sub[x];
     const uint32_t tk = meta_type(mk_);
     uint32_t y = x;
-    while (y > b && key_less(pk, tk, dst.pid[y - 1], meta_type(dst.meta[y - 1]))) {
+    while (y > b && key_less(pk, tk, sk, dst.pid[y - 1], meta_type(dst.meta[y - 1]), dst.sub[y - 1])) {
       dst.pid[y] = dst.pid[y - 1];
       dst.meta[y] = dst.meta[y - 1];
       dst.partner[y] = dst.partner[y - 1];
+      dst.sub[y] = dst.sub[y - 1];
       y--;
     }
     dst.pid[y] = pk;
     dst.meta[y] = mk_;
     dst.partner[y] = qk;
+    dst.sub[y] = sk;
   }
   // history carry-over: binary search in the previous list of the same particle
   uint32_t ob = 0, oe = 0;
@@ -267,20 +283,19 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
   }
   for (uint32_t x = b; x < e; x++) {
     dst.owner[x] = (uint32_t)s;
-    dst.sub[x] = 0u;
     dst.damp[x] = pair_damp(a, (uint32_t)s, dst.partner[x], dst.meta[x]);
     double h[6] = {0, 0, 0, 0, 0, 0};
     const uint64_t pk = dst.pid[x];
-    const uint32_t tk = meta_type(dst.meta[x]);
+    const uint32_t tk = meta_type(dst.meta[x]), sk = dst.sub[x];
     uint32_t lo = ob, hi = oe;
     while (lo < hi) {
       const uint32_t mid = (lo + hi) >> 1;
-      if (key_less(old.pid[mid], meta_type(old.meta[mid]), pk, tk))
+      if (key_less(old.pid[mid], meta_type(old.meta[mid]), old.sub[mid], pk, tk, sk))
         lo = mid + 1;
       else
         hi = mid;
     }
-    if (lo < oe && old.pid[lo] == pk && meta_type(old.meta[lo]) == tk) {
+    if (lo < oe && old.pid[lo] == pk && meta_type(old.meta[lo]) == tk && old.sub[lo] == sk) {
       h[0] = old.ft[0][lo];
       h[1] = old.ft[1][lo];
       h[2] = old.ft[2][lo];
@@ -358,6 +373,7 @@ BPArgs make_args(dem_ctx* c) {
   a.cell_of = c->cell_of;
   a.drv = c->drv_dev;
   a.ndrv = c->ndrv;
+  a.mesh = c->mesh_dev;
   a.skin = c->prm.rcut_inc;
   const double nd = 2 * c->rad_max + c->prm.rcut_inc;
   a.rcut2 = nd * nd;

@@ -20,6 +20,7 @@
 // kernels (contact_core.cuh, integrate_core.cuh).
 #include "contact_core.cuh"
 #include "integrate_core.cuh"
+#include "mesh_core.cuh"
 
 namespace dem {
 namespace {
@@ -47,6 +48,7 @@ struct CArgs {
   const unsigned long long* ni_dev;  // graph step: the count lives on the device
   SysView sv;  // periodic lengths of the owner's system
   const DriverDev* drv;
+  const MeshDev* mesh;
   dem_contact_params cp, cpd;
   double dt;
   int cohesive;
@@ -162,7 +164,13 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
         }
       } else {
         const DriverDev& d = a.drv[j];
-        if (d.kind == 0) {
+        if (d.kind == 2) {  // detect<7|8|9> (contact_sphere.hpp:300-396)
+          const DetD q = mesh_detect(a.mesh[d.mesh], meta_type(meta), a.I.sub[k] >> 16, ri, rad_i);
+          dn = q.dn;
+          contact = q.c;
+          n = q.n;
+          cpos = q.cp;
+        } else if (d.kind == 0) {
           const V3 nrm = mk(d.normal[0], d.normal[1], d.normal[2]);
           const V3 proj = dot(ri, nrm) * nrm;
           const V3 s2p = -(mk(d.center_proj[0], d.center_proj[1], d.center_proj[2]) - proj);
@@ -454,6 +462,7 @@ CArgs make_cargs(dem_ctx* c) {
   a.ni_dev = c->capturing ? c->d_ni : nullptr;
   a.sv = c->sysview();
   a.drv = c->drv_dev;
+  a.mesh = c->mesh_dev;
   a.cp = c->prm.config;
   a.cpd = c->prm.config_driver;
   a.dt = c->prm.dt;

@@ -1,0 +1,60 @@
+// mesh_core.cuh -- a sphere against the vertices, edges and faces of a mesh
+// driver (RShapeDriver): the Verlet filters of detection_sphere_driver
+// (sphere/nbh_sphere.hpp:25-86) and the detectors detect<7|8|9> for spheres
+// (shape_detection_api.hpp:357-386, shape_detection_core.hpp:57-220).  The
+// sphere is a vertex of radius rad; the mesh has homothety 1 and its
+// Minkowski radius.  World vertices are precomputed once (the mesh does not
+// move), which gives the values shape::get_vertex computes per call.
+#pragma once
+#include "../../include/dem_hotpath.h"
+#include "poly_core.cuh"
+
+namespace dem {
+
+__device__ __forceinline__ VView mesh_view(const MeshDev& m) { return VView{m.x, m.y, m.z}; }
+
+// kind 0 vertex, 1 edge, 2 face: filter_vertex_vertex_v2, filter_vertex_edge,
+// filter_vertex_face with rVerlet = the skin
+__device__ inline bool mesh_filter(const MeshDev& m, uint32_t kind, uint32_t j, double rV, V3 p, double rad) {
+  const VView v = mesh_view(m);
+  if (kind == 0) return filter_vv(rV, p, rad, v[j], m.r);
+  if (kind == 1) return filter_ve(rV, p, rad, v[m.e[2 * j]], v[m.e[2 * j + 1]], m.r);
+  double dist;
+  V3 n;
+  const int b = m.fo[j];
+  return vf_core_list(rad + m.r + rV, p, v, m.fv + b, m.fo[j + 1] - b, dist, n);
+}
+
+// detect<type> for a sphere and mesh feature j
+__device__ inline DetD mesh_detect(const MeshDev& m, uint32_t type, uint32_t j, V3 p, double rad) {
+  const VView v = mesh_view(m);
+  if (type == DEM_ITYPE_VERTEX_MESH_VERTEX) return detect_vv(p, rad, v[j], m.r);
+  if (type == DEM_ITYPE_VERTEX_MESH_EDGE) return detect_ve(p, rad, v[m.e[2 * j]], v[m.e[2 * j + 1]], m.r);
+  // detection_vertex_face for spheres (shape_detection_core.hpp:151-220)
+  const double R = rad + m.r;
+  double dist;
+  V3 n;
+  const int b = m.fo[j];
+  const bool inside = vf_core_list(R, p, v, m.fv + b, m.fo[j + 1] - b, dist, n);
+  if (dist > R) return det_none();
+  const double dn = dist - R;
+  return DetD{inside, dn, n, p - n * (rad + 0.5 * dn)};
+}
+
+// the features listed in the bin of p (none outside the bin grid)
+template <class F>
+__device__ inline void mesh_bin_items(const MeshDev& m, V3 p, F&& f) {
+  const double fx = (p.x - m.lo[0]) * m.inv_bs;
+  const double fy = (p.y - m.lo[1]) * m.inv_bs;
+  const double fz = (p.z - m.lo[2]) * m.inv_bs;
+  if (!(fx >= 0.0 && fx < (double)m.dims[0] && fy >= 0.0 && fy < (double)m.dims[1] && fz >= 0.0 &&
+        fz < (double)m.dims[2]))
+    return;
+  const uint64_t b = (uint64_t)(int)fx + (uint64_t)m.dims[0] * ((uint64_t)(int)fy + (uint64_t)m.dims[1] * (int)fz);
+  for (uint32_t q = m.boff[b]; q < m.boff[b + 1]; q++) {
+    const uint32_t it = m.bitem[q];
+    f(it >> 30, it & 0x3fffffffu);
+  }
+}
+
+}  // namespace dem

@@ -158,13 +158,13 @@ struct VView {
 };
 
 // point-in-face core shared by the face filter and detection; returns inside,
-// sets dist (unsigned plane distance) and n (oriented normal).
-__device__ inline bool vf_core(double lim, V3 vi, const VView& vaj, const ShapeDev& sj, int face, double& dist_out,
-                               V3& n_out) {
-  const int b = sj.fo[face], nf = sj.fo[face + 1] - sj.fo[face];
-  const V3 va = vaj[sj.fv[b]];
-  const V3 vb = vaj[sj.fv[b + 1]];
-  const V3 vc = vaj[sj.fv[b + nf - 1]];
+// sets dist (unsigned plane distance) and n (oriented normal).  The face is the
+// vertex list fv[0 .. nf) of vaj.
+__device__ inline bool vf_core_list(double lim, V3 vi, const VView& vaj, const int* fv, int nf, double& dist_out,
+                                    V3& n_out) {
+  const V3 va = vaj[fv[0]];
+  const V3 vb = vaj[fv[1]];
+  const V3 vc = vaj[fv[nf - 1]];
   const V3 v = vi - va;
   V3 v1 = vb - va;
   V3 v2 = vc - va;
@@ -187,8 +187,8 @@ __device__ inline bool vf_core(double lim, V3 vi, const VView& vaj, const ShapeD
   for (int iva = 0; iva < nf; ++iva) {
     int ivb = iva + 1;
     if (ivb == nf) ivb = 0;
-    const V3 _va = vaj[sj.fv[b + iva]];
-    const V3 _vb = vaj[sj.fv[b + ivb]];
+    const V3 _va = vaj[fv[iva]];
+    const V3 _vb = vaj[fv[ivb]];
     const double pa1 = dot(_va, v1);
     const double pb1 = dot(_vb, v1);
     const double pa2 = dot(_va, v2);
@@ -198,6 +198,11 @@ __device__ inline bool vf_core(double lim, V3 vi, const VView& vaj, const ShapeD
     }
   }
   return ODD == 1;
+}
+__device__ __forceinline__ bool vf_core(double lim, V3 vi, const VView& vaj, const ShapeDev& sj, int face,
+                                        double& dist_out, V3& n_out) {
+  const int b = sj.fo[face];
+  return vf_core_list(lim, vi, vaj, sj.fv + b, sj.fo[face + 1] - b, dist_out, n_out);
 }
 __device__ __forceinline__ bool filter_vf(double rV, V3 vi, double ri, const VView& vaj, const ShapeDev& sj, int face,
                                           double rj) {

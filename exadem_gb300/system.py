@@ -158,6 +158,22 @@ class System:
                        (C.c_double * 3)(*vrot))
         self._check(self.b.register_cylinder(self.h, C.byref(c)), "register_cylinder")
 
+    def register_mesh(self, vertices, edges, faces, minkowski, center=(0, 0, 0), quat=(1, 0, 0, 0)) -> None:
+        """register_stl_mesh / register_rshape with STATIONARY motion: vertices (nv, 3) in
+        the mesh frame, edges (ne, 2), faces (list of vertex lists), Minkowski radius,
+        position and orientation (w, x, y, z).  exadem_gb300.stl builds these arrays
+        from an STL file the way the reference converts it."""
+        v = np.ascontiguousarray(np.asarray(vertices, dtype=np.float64).reshape(-1))
+        e = np.ascontiguousarray(np.asarray(edges, dtype=np.int32).reshape(-1))
+        off = np.zeros(len(faces) + 1, dtype=np.int32)
+        off[1:] = np.cumsum([len(f) for f in faces])
+        fv = np.ascontiguousarray(np.concatenate([np.asarray(f, dtype=np.int32) for f in faces])
+                                  if len(faces) else np.zeros(0, np.int32))
+        m = A.Mesh(len(v) // 3, len(e) // 2, len(faces), A.ptr(v), A.ptr(e, C.POINTER(C.c_int32)),
+                   A.ptr(off, C.POINTER(C.c_int32)), A.ptr(fv, C.POINTER(C.c_int32)), float(minkowski),
+                   (C.c_double * 3)(*center), (C.c_double * 4)(*quat))
+        self._check(self.b.register_mesh(self.h, C.byref(m)), "register_mesh")
+
     def set_shapes(self, shapes: list) -> None:
         """shapes: dicts with vertices (nv,3), edges (ne,2), faces (list of vertex lists), radius,
         obb = dict(center, e1, e2, e3, extent) -- exaDEM's .shp content."""

@@ -28,6 +28,7 @@ class Workload:
     particles: dict
     surfaces: list = field(default_factory=list)   # kwargs of System.register_surface
     cylinders: list = field(default_factory=list)  # kwargs of System.register_cylinder
+    meshes: list = field(default_factory=list)     # kwargs of System.register_mesh
     steps: int = 1000
     info: dict = field(default_factory=dict)
     shapes: list = None  # polyhedron shapes (System.set_shapes), None for spheres
@@ -46,6 +47,8 @@ class Workload:
             s.register_surface(**kw)
         for kw in self.cylinders:
             s.register_cylinder(**kw)
+        for kw in self.meshes:
+            s.register_mesh(**kw)
         return s
 
 
@@ -146,6 +149,54 @@ def spheres_drum(n=20_000, rmin=0.45, rmax=0.55, fill=0.30, density=2.0, length=
                     **flags)
     cyl = dict(radius=R, axis=(1.0, 0.0, 1.0), center=(c, 0.0, c), vrot=(0.0, omega, 0.0))
     return Workload("spheres_drum", p, arr, cylinders=[cyl], steps=steps, info={"drum_radius": R, "length": length})
+
+
+def terrain_triangles(side, m, amp, waves, z0):
+    """(2 m^2, 3, 3) triangles of the height field z0 + amp sin(2 pi w x / side)
+    sin(2 pi w y / side) over [-side/2, side/2]^2 (a square grid, two triangles
+    per square)."""
+    xs = np.linspace(-side / 2, side / 2, m + 1)
+    h = lambda x, y: z0 + amp * math.sin(2 * math.pi * waves * x / side) * math.sin(2 * math.pi * waves * y / side)
+    tri = []
+    for i in range(m):
+        for j in range(m):
+            p = [(xs[a], xs[b], h(xs[a], xs[b])) for a, b in ((i, j), (i + 1, j), (i + 1, j + 1), (i, j + 1))]
+            tri.append([p[0], p[1], p[2]])
+            tri.append([p[0], p[2], p[3]])
+    return np.asarray(tri, dtype=np.float64)
+
+
+def spheres_mesh_terrain(n=3000, side=16.0, height=None, rmin=0.4, rmax=0.5, density=2.0, m=16, amp=0.8,
+                         waves=2, minkowski=0.05, vz=-3.0, seed=9, steps=400, dt=1e-3, skin=0.1,
+                         **flags) -> Workload:
+    """Spheres falling on a triangulated height field (a mesh driver,
+    register_stl_mesh with its STL conversion: every sphere against the mesh's
+    vertices, edges and faces) inside four walls.  The mesh is built about the
+    origin and placed by its center (side/2, side/2, amp + 0.2) and a quarter
+    turn about z.  Hooke kn=1e4, kt=8e3, kr=0, mu=0.4, damp 0.9 for pairs and walls; the
+    spheres start above the terrain moving down at vz."""
+    from exadem_gb300.stl import build_shape
+
+    ev = 4.0 / 3.0 * math.pi * (rmax ** 4 - rmin ** 4) / (4 * (rmax - rmin))
+    zc = amp + 0.2
+    z_lo = zc + amp + minkowski + rmax + 0.2
+    if height is None:
+        height = z_lo + n * ev / (0.25 * (side - 2 * rmax) ** 2) + 2 * rmax
+    arr, _ = rsa(n, rmin, rmax, density, (rmax, rmax, z_lo), (side - rmax, side - rmax, height - rmax), seed=seed,
+                 max_attempts=100000)
+    arr["vz"] = arr["vz"] + vz
+    cfg = dict(kn=1e4, kt=8e3, kr=0.0, mu=0.4, damp_rate=0.9)
+    p = make_params((0, 0, 0), (side, side, height), (0, 0, 0), rcut_inc=skin, dt=dt, gravity=(0, 0, -9.81),
+                    config=cfg, config_driver=cfg, **flags)
+    shp = build_shape(list(terrain_triangles(side, m, amp, waves, 0.0)))
+    c45 = math.cos(math.pi / 4)
+    mesh = dict(vertices=shp["vertices"], edges=shp["edges"], faces=shp["faces"], minkowski=minkowski,
+                center=(side / 2, side / 2, zc), quat=(c45, 0.0, 0.0, c45))
+    walls = [dict(offset=0.0, normal=(1.0, 0.0, 0.0)), dict(offset=-side, normal=(-1.0, 0.0, 0.0)),
+             dict(offset=0.0, normal=(0.0, 1.0, 0.0)), dict(offset=-side, normal=(0.0, -1.0, 0.0))]
+    return Workload("spheres_mesh_terrain", p, arr, surfaces=walls, meshes=[mesh], steps=steps,
+                    info={"mesh_vertices": len(shp["vertices"]), "mesh_edges": len(shp["edges"]),
+                          "mesh_faces": len(shp["faces"])})
 
 
 @dataclass

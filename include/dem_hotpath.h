@@ -45,6 +45,9 @@ extern "C" {
 #define DEM_ITYPE_EDGE_EDGE 3
 #define DEM_ITYPE_VERTEX_CYLINDER 4
 #define DEM_ITYPE_VERTEX_SURFACE 5
+#define DEM_ITYPE_VERTEX_MESH_VERTEX 7 /* VertexRshapeDriverVertex */
+#define DEM_ITYPE_VERTEX_MESH_EDGE 8   /* VertexRshapeDriverEdge   */
+#define DEM_ITYPE_VERTEX_MESH_FACE 9   /* VertexRshapeDriverFace   */
 
 /* ---- contact law parameters -------------------------------------------
  * Mirrors ContactParams {dncut, kn, kt, kr, fc, mu, damp_rate}
@@ -145,6 +148,24 @@ typedef struct dem_cylinder {
   double vrot[3];    /* drum angular velocity                               */
 } dem_cylinder;
 
+/* Mesh driver: register_stl_mesh / register_rshape (register_stl_mesh.cpp:40-147,
+ * rshape.hpp:104-420) with STATIONARY motion and zero velocities.  The shape
+ * is given as the reference's shape arrays after the STL conversion and
+ * rescale (stl_mesh_to_driver.hpp:26-121): vertices in the mesh frame, edges
+ * as vertex pairs, faces as vertex lists (at least 3 each).  World vertices are
+ * center + quat * vertex (shape::get_vertex with homothety 1).  Each of nv, ne,
+ * nf must be below 65535 (the partner sub of the list is 16 bits).         */
+typedef struct dem_mesh {
+  int32_t nv, ne, nf;
+  const double* vertices;       /* 3 * nv                                  */
+  const int32_t* edges;         /* 2 * ne                                  */
+  const int32_t* face_offsets;  /* nf + 1, face f = face_vertices[off[f] .. off[f+1]) */
+  const int32_t* face_vertices; /* face_offsets[nf]                        */
+  double minkowski;             /* Minkowski radius (shape::add_radius)    */
+  double center[3];
+  double quat[4];               /* w x y z                                 */
+} dem_mesh;
+
 /* ---- thermodynamic state (src/io/include/exaDEM/simulation_state.hpp:48-56) */
 typedef struct dem_state {
   double kinetic_energy[3];  /* sum 0.5*m*v*v per component            */
@@ -226,6 +247,10 @@ int dem_get_particles(dem_ctx* ctx, dem_particles* out, int on_device);
  * motion only; vrot enters the relative velocity (rotating drum).         */
 int dem_register_surface(dem_ctx* ctx, const dem_surface* s);
 int dem_register_cylinder(dem_ctx* ctx, const dem_cylinder* c);
+/* register_stl_mesh: sphere systems (interaction types 7-9: the sphere against a
+ * mesh vertex, edge or face, nbh_sphere.hpp:25-86, contact_sphere.hpp:300-396).
+ * The driver index is the registration order, shared with the other drivers. */
+int dem_register_mesh(dem_ctx* ctx, const dem_mesh* m);
 
 /* ---- batching: many independent systems in one context -------------------
  * No reference counterpart (one exaDEM run is one system).  Each system is a

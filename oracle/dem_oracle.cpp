@@ -106,9 +106,21 @@ struct Cylinder {
   V3 axis, center, vel, vrot;
 };
 struct Driver {
-  int kind;  // 0 surface, 1 cylinder
+  int kind;  // 0 surface, 1 cylinder, 2 mesh
   Surface s;
   Cylinder c;
+  int mesh = -1;  // kind 2: index into Oracle::meshes
+};
+
+// Mesh driver (RShapeDriver, rshape.hpp:104-420), stationary: world vertices
+// center + quat * (1.0 * v) (RShapeDriver::update_vertex), edges as vertex pairs,
+// faces as vertex lists, Minkowski radius r; position() = center, zero velocities.
+struct MeshO {
+  std::vector<V3> w;
+  std::vector<int> e;
+  std::vector<std::vector<int>> f;
+  double r = 0;
+  V3 center{};
 };
 
 // One interaction = InteractionPair + Interaction data (interaction_pair.hpp:56-71,
@@ -173,6 +185,7 @@ struct Oracle {
   // polyhedron mode
   bool poly = false;
   std::vector<struct PShape> shapes;
+  std::vector<MeshO> meshes;
   std::vector<std::vector<V3>> vtx;   // world vertices per particle
   std::vector<std::vector<V3>> bvtx;  // vertices at the last rebuild (backup_dem)
   uint64_t rebuilds = 0;
@@ -259,6 +272,10 @@ void wrap(Oracle& o) {
 // chunk_neighbors_contact + nbh_sphere (symetric) + classify, with history
 // carried over by InteractionPair equality (interaction_manager.hpp:89-112,
 // placeholder_interaction.hpp:398-408).
+// sphere-mesh candidates and detection (defined with the polyhedron geometry)
+void mesh_candidates(const Oracle& o, size_t k, size_t i, const V3& ri, double rad, double skin, std::vector<Inter>& lst);
+bool mesh_detect(const Oracle& o, const Inter& it, const V3& ri, double rad, double& dn, V3& n, V3& cp);
+
 int update_neighbors(Oracle& o) {
   wrap(o);
   const double skin = o.prm.rcut_inc;
@@ -318,6 +335,10 @@ int update_neighbors(Oracle& o) {
     // drivers first (nbh_sphere.cu:140-233)
     for (size_t k = 0; k < o.drivers.size(); k++) {
       const Driver& dv = o.drivers[k];
+      if (dv.kind == 2) {
+        mesh_candidates(o, k, i, ri, o.rad[i], skin, lst);
+        continue;
+      }
       const double rv = o.rad[i] + skin;
       bool keep = dv.kind == 0 ? surface_filter(dv.s, rv, ri) : cylinder_filter(dv.c, rv, ri);
       if (!keep) continue;
@@ -552,7 +573,12 @@ void contact_one(Oracle& o, size_t k) {
   V3 n{}, cp{};
   bool contact;
   V3 dpos, dvel, dvrot;
-  if (dv.kind == 0) {
+  if (dv.kind == 2) {  // ContactLawRShapeDriverFunc (contact_sphere.hpp:300-396)
+    contact = mesh_detect(o, it, ri, rad, dn, n, cp);
+    dpos = o.meshes[dv.mesh].center;
+    dvel = {0, 0, 0};
+    dvrot = {0, 0, 0};
+  } else if (dv.kind == 0) {
     contact = surface_detect(dv.s, rad, ri, dn, n, cp);
     dpos = dv.s.center;
     dvel = dv.s.vel;
@@ -581,6 +607,7 @@ void contact_one(Oracle& o, size_t k) {
   } else {
     it.friction = {0, 0, 0};
     it.moment = {0, 0, 0};
+    if (dv.kind == 2) rc.scp = cp;  // dn = 0, the detector's contact point
   }
 }
 
@@ -1002,6 +1029,48 @@ Det detect_ee(const V3& vfi, const V3& vsi, double ri, const V3& vfj, const V3& 
 }
 
 // world vertices: shape::get_vertex = p + q * (h * v0) (shape.hpp:245-262)
+// detection_sphere_driver (sphere/nbh_sphere.hpp:25-86): every vertex, edge and
+// face of the mesh whose Verlet filter passes for the sphere (rVerlet = the
+// skin), in (type, feature) order; the owner sub is 0, the partner sub the feature
+void mesh_candidates(const Oracle& o, size_t k, size_t i, const V3& ri, double rad, double skin,
+                     std::vector<Inter>& lst) {
+  const MeshO& m = o.meshes[o.drivers[k].mesh];
+  auto add = [&](int type, int j) {
+    Inter it{};
+    it.oid = o.id[i];
+    it.pid = k;
+    it.type = (uint16_t)type;
+    it.psub = (uint32_t)j;
+    it.oi = (int32_t)i;
+    it.pj = (int32_t)k;
+    lst.push_back(it);
+  };
+  for (int j = 0; j < (int)m.w.size(); j++)
+    if (filter_vv(skin, ri, rad, m.w[j], m.r)) add(DEM_ITYPE_VERTEX_MESH_VERTEX, j);
+  for (int j = 0; j < (int)m.e.size() / 2; j++)
+    if (filter_ve(skin, ri, rad, m.w[m.e[2 * j]], m.w[m.e[2 * j + 1]], m.r)) add(DEM_ITYPE_VERTEX_MESH_EDGE, j);
+  for (int j = 0; j < (int)m.f.size(); j++)
+    if (filter_vf(skin, ri, rad, m.w, m.f[j], m.r)) add(DEM_ITYPE_VERTEX_MESH_FACE, j);
+}
+
+// detect<7|8|9> for spheres (shape_detection_api.hpp:357-386,
+// shape_detection_core.hpp:57-220): the sphere as a vertex of radius rad
+bool mesh_detect(const Oracle& o, const Inter& it, const V3& ri, double rad, double& dn, V3& n, V3& cp) {
+  const MeshO& m = o.meshes[o.drivers[it.pj].mesh];
+  const int j = (int)it.psub;
+  Det d;
+  if (it.type == DEM_ITYPE_VERTEX_MESH_VERTEX)
+    d = detect_vv(ri, rad, m.w[j], m.r);
+  else if (it.type == DEM_ITYPE_VERTEX_MESH_EDGE)
+    d = detect_ve(ri, rad, m.w[m.e[2 * j]], m.w[m.e[2 * j + 1]], m.r);
+  else
+    d = detect_vf(ri, rad, m.w, m.f[j], m.r);
+  dn = d.dn;
+  n = d.n;
+  cp = d.cp;
+  return d.c;
+}
+
 void compute_vertices(Oracle& o) {
   o.vtx.resize(o.n);
 #pragma omp parallel for schedule(static)
@@ -1452,6 +1521,27 @@ int oracle_register_cylinder(void* h, const dem_cylinder* c) {
   d.c.center = d.c.axis * V3{c->center[0], c->center[1], c->center[2]};  // Cylinder::initialize
   d.c.vel = {c->vel[0], c->vel[1], c->vel[2]};
   d.c.vrot = {c->vrot[0], c->vrot[1], c->vrot[2]};
+  o.drivers.push_back(d);
+  return DEM_OK;
+}
+int oracle_register_mesh(void* h, const dem_mesh* s) {  // register_stl_mesh (register_stl_mesh.cpp:40-147)
+  Oracle& o = *(Oracle*)h;
+  if (o.poly) return DEM_ERR_UNSUPPORTED;
+  MeshO m;
+  m.r = s->minkowski;
+  m.center = {s->center[0], s->center[1], s->center[2]};
+  const Quat q = {s->quat[0], s->quat[1], s->quat[2], s->quat[3]};
+  for (int k = 0; k < s->nv; k++) {
+    const V3 v = {s->vertices[3 * k], s->vertices[3 * k + 1], s->vertices[3 * k + 2]};
+    m.w.push_back(m.center + rotate(q, 1.0 * v));  // shape::get_vertex(i, center, 1.0, quat)
+  }
+  m.e.assign(s->edges, s->edges + 2 * s->ne);
+  for (int f = 0; f < s->nf; f++)
+    m.f.emplace_back(s->face_vertices + s->face_offsets[f], s->face_vertices + s->face_offsets[f + 1]);
+  Driver d{};
+  d.kind = 2;
+  d.mesh = (int)o.meshes.size();
+  o.meshes.push_back(std::move(m));
   o.drivers.push_back(d);
   return DEM_OK;
 }

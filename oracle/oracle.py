@@ -38,6 +38,7 @@ def load(rebuild: bool = True):
         sig("oracle_get_particles", [_CTX, C.POINTER(A.Particles)])
         sig("oracle_register_surface", [_CTX, C.POINTER(A.Surface)])
         sig("oracle_register_cylinder", [_CTX, C.POINTER(A.Cylinder)])
+        sig("oracle_register_mesh", [_CTX, C.POINTER(A.Mesh)])
         sig("oracle_displ_over", [_CTX, C.POINTER(C.c_int)])
         for n in ["oracle_update_neighbors", "oracle_reset_force_moment", "oracle_gravity_force",
                   "oracle_contact_sphere", "oracle_force_to_accel", "oracle_prolog", "oracle_epilog",
@@ -58,6 +59,7 @@ def load(rebuild: bool = True):
 class OracleBackend:
     _MAP = {"ctx_create": "oracle_create", "ctx_destroy": "oracle_destroy", "last_error": "oracle_last_error",
             "register_surface": "oracle_register_surface", "register_cylinder": "oracle_register_cylinder",
+            "register_mesh": "oracle_register_mesh",
             "update_particle_neighbors": "oracle_update_neighbors", "particle_displ_over": "oracle_displ_over",
             "reset_force_moment": "oracle_reset_force_moment", "gravity_force": "oracle_gravity_force",
             "contact_sphere": "oracle_contact_sphere", "force_to_accel": "oracle_force_to_accel",
