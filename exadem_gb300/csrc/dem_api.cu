@@ -415,6 +415,7 @@ int update_neighbors_poly(dem_ctx* c) {
     return DEM_OK;
   }
   int rc;
+  if ((rc = ensure_mesh_bins(c))) return rc;
   if ((rc = alloc_poly(c))) return rc;
   if ((rc = launch_bin_particles(c))) return rc;
   if ((rc = launch_reorder_particles(c))) return rc;
@@ -989,7 +990,6 @@ int dem_set_shapes(dem_ctx* c, const dem_shape* shapes, int nshapes) {
     mv = std::max(mv, d.nv);
   }
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-  if (!c->meshes.empty()) return c->fail(DEM_ERR_UNSUPPORTED, "mesh drivers are built for sphere systems");
   cudaFree(c->shapes_dev);
   c->shapes_dev = nullptr;
   DEM_CUDA_TRY(c, cudaMalloc(&c->shapes_dev, sizeof(ShapeDev) * nshapes));

@@ -125,6 +125,10 @@ struct MeshDev {
   int dims[3];
   const uint32_t* boff;   // bins + 1
   const uint32_t* bitem;  // boff[bins]
+  // lowest bin (x | y << 21 | z << 42) of each feature's range, vertices then
+  // edges then faces: a query over a box of bins visits a feature once, in the
+  // first bin its range shares with the box
+  const uint64_t* flo;
 };
 struct GridDev {
   int dims[3];

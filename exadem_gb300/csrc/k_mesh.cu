@@ -1,5 +1,5 @@
 // k_mesh.cu -- mesh drivers (register_stl_mesh / register_rshape,
-// register_stl_mesh.cpp:40-147, rshape.hpp:104-420) for sphere systems.
+// register_stl_mesh.cpp:40-147, rshape.hpp:104-420).
 //
 // The reference lists, per grid cell, the mesh features whose enlarged OBB
 // meets the cell (grid_rshape_driver, grid_stl_mesh.cpp:30-265), and a sphere
@@ -7,9 +7,10 @@
 // (nbh_sphere.hpp:25-86).  With cells that cover the filter range that list
 // is the set of features passing the filter, which is what is built here: a
 // uniform bin grid of its own over the mesh lists, per bin, every feature whose
-// filter can pass for a sphere centred in the bin (the feature's box enlarged
-// by the filter range, with a margin for rounding), and the neighbour pass runs
-// the exact filter on the features of the sphere's bin.
+// filter can pass for a point of the bin (a sphere centre, a polyhedron vertex
+// or edge point: the feature's box enlarged by the filter range with the
+// largest particle radius, with a margin for rounding), and the neighbour pass
+// runs the exact filter on the features of the bins it visits.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -91,7 +92,7 @@ int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   if (box.empty() || !(std::isfinite(all.lo[0]) && std::isfinite(all.hi[0]) && std::isfinite(all.lo[1]) &&
                        std::isfinite(all.hi[1]) && std::isfinite(all.lo[2]) && std::isfinite(all.hi[2])))
     return c->fail(DEM_ERR_INVALID_ARG, "mesh: non-finite vertices");
-  // bin size: about the filter range, at most 2^22 bins
+  // bin size: about the filter range, at most 2^22 bins (each axis below 2^21)
   double ext = std::max(all.hi[0] - all.lo[0], std::max(all.hi[1] - all.lo[1], all.hi[2] - all.lo[2]));
   double bs = std::max(E, ext / 256.0);
   int dims[3];
@@ -114,6 +115,10 @@ int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   };
   const uint64_t nb = (uint64_t)dims[0] * dims[1] * dims[2];
   std::vector<uint32_t> cnt(nb + 1, 0);
+  std::vector<uint64_t> flo(box.size());
+  for (size_t k = 0; k < box.size(); k++)
+    flo[k] = (uint64_t)index(box[k].lo[0], 0) | ((uint64_t)index(box[k].lo[1], 1) << 21) |
+             ((uint64_t)index(box[k].lo[2], 2) << 42);
   auto for_bins = [&](const Box& b, auto&& f) {
     const int x0 = index(b.lo[0], 0), x1 = index(b.hi[0], 0);
     const int y0 = index(b.lo[1], 1), y1 = index(b.hi[1], 1);
@@ -140,16 +145,21 @@ int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   }
   cudaFree(m.boff);
   cudaFree(m.bitem);
+  cudaFree(m.flo);
   m.boff = nullptr;
   m.bitem = nullptr;
+  m.flo = nullptr;
   DEM_CUDA_TRY(c, cudaMalloc(&m.boff, (nb + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&m.bitem, std::max<uint64_t>(total, 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&m.flo, box.size() * 8));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(m.flo, flo.data(), box.size() * 8, cudaMemcpyHostToDevice, c->stream));
   DEM_CUDA_TRY(c, cudaMemcpyAsync(m.boff, cnt.data(), (nb + 1) * 4, cudaMemcpyHostToDevice, c->stream));
   if (total)
     DEM_CUDA_TRY(c, cudaMemcpyAsync(m.bitem, items.data(), total * 4, cudaMemcpyHostToDevice, c->stream));
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   D.boff = m.boff;
   D.bitem = m.bitem;
+  D.flo = m.flo;
   m.bin_rad = rad;
   m.bin_skin = skin;
   return DEM_OK;
@@ -170,6 +180,8 @@ int upload_mesh_table(dem_ctx* c) {
 }  // namespace
 
 int ensure_mesh_bins(dem_ctx* c) {
+  if (!c->meshes.empty() && c->poly && c->prm.learned_sizing)
+    return c->fail(DEM_ERR_UNSUPPORTED, "learned record sizing does not bound mesh units: learned_sizing = 0");
   bool changed = false;
   const double rad = c->rad_max, skin = c->prm.rcut_inc;
   for (MeshStore& m : c->meshes) {
@@ -192,6 +204,7 @@ void free_meshes(dem_ctx* c) {
     cudaFree(m.fv);
     cudaFree(m.boff);
     cudaFree(m.bitem);
+    cudaFree(m.flo);
   }
   c->meshes.clear();
   cudaFree(c->mesh_dev);
@@ -203,7 +216,6 @@ using namespace dem;
 
 extern "C" int dem_register_mesh(dem_ctx* c, const dem_mesh* s) {
   if (!c || !s) return DEM_ERR_INVALID_ARG;
-  if (c->poly) return c->fail(DEM_ERR_UNSUPPORTED, "mesh drivers are built for sphere systems");
   const int nv = s->nv, ne = s->ne, nf = s->nf;
   if (nv < 0 || ne < 0 || nf < 0 || nv + ne + nf == 0)
     return c->fail(DEM_ERR_INVALID_ARG, "mesh: no vertex, no edge and no face (RShape::initialize)");

@@ -23,6 +23,7 @@
 
 #include "contact_core.cuh"
 #include "integrate_core.cuh"
+#include "mesh_core.cuh"
 #include "poly_core.cuh"
 #include "poly_f32.cuh"
 
@@ -235,6 +236,7 @@ struct UnitArgs {
   const uint32_t* cell_of;
   const DriverDev* drv;
   int ndrv;
+  const MeshDev* mesh;
   const ShapeDev* shapes;
   double rV;
   double rcut2;
@@ -282,8 +284,19 @@ __device__ inline void for_each_unit(const UnitArgs& a, uint32_t s, Emit&& emit)
     const double h = a.P.f[HOM][s];
     const double reach = h * (sh.maxv + sh.r) + a.rV;
     const double rc = reach + 1e-9 * (1.0 + reach + fabs(ri.x) + fabs(ri.y) + fabs(ri.z));
-    for (int k = 0; k < a.ndrv; k++)
-      if (driver_reach(a.drv[k], rc, ri)) emit(1u, (uint32_t)k, (uint64_t)k);
+    for (int k = 0; k < a.ndrv; k++) {
+      const DriverDev& d = a.drv[k];
+      if (d.kind == 2) {  // a mesh unit when the reach sphere meets the mesh's bin grid
+        const MeshDev& m = a.mesh[d.mesh];
+        const double bs = 1.0 / m.inv_bs;
+        const bool meet = ri.x + rc >= m.lo[0] && ri.x - rc <= m.lo[0] + (m.dims[0] + 1) * bs &&
+                          ri.y + rc >= m.lo[1] && ri.y - rc <= m.lo[1] + (m.dims[1] + 1) * bs &&
+                          ri.z + rc >= m.lo[2] && ri.z - rc <= m.lo[2] + (m.dims[2] + 1) * bs;
+        if (meet) emit(1u, (uint32_t)k, (uint64_t)k);
+      } else if (driver_reach(d, rc, ri)) {
+        emit(1u, (uint32_t)k, (uint64_t)k);
+      }
+    }
   }
   float xri = 0.f, yri = 0.f, zri = 0.f, rfi = 0.f, si = 0.f, cmax = 0.f;
   if (a.f32) {
@@ -397,6 +410,7 @@ struct FeatArgs {
   PArrays P;
   const ShapeDev* shapes;
   const DriverDev* drv;
+  const MeshDev* mesh;
   int MV;
   const double* vx;
   const double* vy;
@@ -495,12 +509,164 @@ __device__ __forceinline__ uint32_t seg_type(int seg) {
 }
 __device__ __forceinline__ uint32_t seg_swap(int seg) { return (seg == 2 || seg == 4) ? 1u : 0u; }
 
+// Polyhedron A against a mesh driver (add_driver_interaction for RShapeDriver,
+// nbh_polyhedron_driver.hpp:61-192): types 7 (A vertex - mesh vertex), 8 (A
+// vertex - mesh edge), 9 (A vertex - mesh face), 10 (A edge - mesh edge), 11
+// (mesh vertex - A edge) and 12 (mesh vertex - A face), each through its Verlet
+// filter; 11 and 12 only for the mesh vertices whose box (vertex +- Minkowski
+// radius) meets A's OBB rotated and translated (homothety not applied) and
+// enlarged by rVerlet, the reference's gate.  The reference's type 9 gate (the
+// face's OBB against the vertex box) holds whenever the face filter passes and
+// is not evaluated.  Candidates are the mesh features listed in the bins under
+// A's box (mesh vertices: under the gate OBB's box too), each visited once;
+// the fill pass writes a unit's items in lane order and k_mesh_unit_sort puts
+// them in InteractionPair order.
+struct MeshQuery {
+  int lo[3], hi[3];
+  bool empty;
+};
+__device__ __forceinline__ MeshQuery mesh_query(const MeshDev& m, V3 lo, V3 hi) {
+  MeshQuery q;
+  q.empty = false;
+  const double l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+  for (int d = 0; d < 3; d++) {
+    const double fl = (l[d] - m.lo[d]) * m.inv_bs, fh = (h[d] - m.lo[d]) * m.inv_bs;
+    if (!(fh >= 0.0) || !(fl < (double)m.dims[d])) q.empty = true;
+    q.lo[d] = fl <= 0.0 ? 0 : (int)fl;
+    q.hi[d] = fh >= (double)m.dims[d] ? m.dims[d] - 1 : (fh <= 0.0 ? 0 : (int)fh);
+  }
+  return q;
+}
+
+// tests of one mesh feature against A's vertices, edges or faces; Write: items at w
+template <bool Write>
+__device__ uint32_t mesh_feature_tests(const FeatArgs& a, const MeshDev& m, uint32_t kind, uint32_t j,
+                                       const ShapeDev& SA, double ra, const VView& va, const OBBd& gate,
+                                       uint32_t A, uint32_t k, uint32_t w) {
+  const VView mv = mesh_view(m);
+  const double rV = a.rV, mr = m.r;
+  uint32_t n = 0;
+  auto out = [&](uint32_t type, int osub) {
+    if (Write) write_feature(a, w + n, A, k, (uint64_t)k, type, 0u, (uint32_t)osub, j);
+    n++;
+  };
+  if (kind == 0) {
+    const V3 p = mv[j];
+    for (int i = 0; i < SA.nv; i++)
+      if (filter_vv(rV, va[i], ra, p, mr)) out(DEM_ITYPE_VERTEX_MESH_VERTEX, i);
+    OBBd ov;
+    ov.c = p;
+    ov.e1 = mk(1, 0, 0);
+    ov.e2 = mk(0, 1, 0);
+    ov.e3 = mk(0, 0, 1);
+    ov.ext = mk(0, 0, 0);
+    obb_enlarge(ov, mr);
+    if (obb_intersect(ov, gate)) {  // obb_v_rshape_j.intersect(obb_i)
+      for (int e = 0; e < SA.ne; e++)
+        if (filter_ve(rV, p, mr, va[SA.e[2 * e]], va[SA.e[2 * e + 1]], ra)) out(DEM_ITYPE_MESH_VERTEX_EDGE, e);
+      for (int f = 0; f < SA.nf; f++)
+        if (filter_vf(rV, p, mr, va, SA, f, ra)) out(DEM_ITYPE_MESH_VERTEX_FACE, f);
+    }
+  } else if (kind == 1) {
+    const V3 m0 = mv[m.e[2 * j]], m1 = mv[m.e[2 * j + 1]];
+    for (int i = 0; i < SA.nv; i++)
+      if (filter_ve(rV, va[i], ra, m0, m1, mr)) out(DEM_ITYPE_VERTEX_MESH_EDGE, i);
+    for (int e = 0; e < SA.ne; e++)
+      if (filter_ee(rV, va[SA.e[2 * e]], va[SA.e[2 * e + 1]], ra, m0, m1, mr)) out(DEM_ITYPE_EDGE_MESH_EDGE, e);
+  } else {
+    const int b = m.fo[j], nf = m.fo[j + 1] - b;
+    for (int i = 0; i < SA.nv; i++) {
+      double dist;
+      V3 nn;
+      if (vf_core_list(ra + mr + rV, va[i], mv, m.fv + b, nf, dist, nn)) out(DEM_ITYPE_VERTEX_MESH_FACE, i);
+    }
+  }
+  return n;
+}
+
+template <bool Fill>
+__device__ void mesh_unit(const FeatArgs& a, uint64_t u, uint32_t A, const ShapeDev& SA, double ra, const VView& va,
+                          uint32_t base, int lane, uint32_t lt) {
+  const uint32_t k = a.u_partner[u];
+  const MeshDev& m = a.mesh[a.drv[k].mesh];
+  // A's vertex box
+  V3 lo = mk(HUGE_VAL, HUGE_VAL, HUGE_VAL), hi = mk(-HUGE_VAL, -HUGE_VAL, -HUGE_VAL);
+  for (int i = lane; i < SA.nv; i += 32) {
+    const V3 v = va[i];
+    lo = mk(fmin(lo.x, v.x), fmin(lo.y, v.y), fmin(lo.z, v.z));
+    hi = mk(fmax(hi.x, v.x), fmax(hi.y, v.y), fmax(hi.z, v.z));
+  }
+  for (int o = 16; o; o >>= 1) {
+    lo = mk(fmin(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o)), fmin(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o)),
+            fmin(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o)));
+    hi = mk(fmax(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o)), fmax(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o)),
+            fmax(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o)));
+  }
+  // the gate OBB: compute_obb with homothety 1, enlarged by rVerlet; its box with a margin for the SAT tolerance
+  const Q4 q{a.P.f[QW][A], a.P.f[QX][A], a.P.f[QY][A], a.P.f[QZ][A]};
+  OBBd gate = compute_obb(SA, mk(a.P.f[RX][A], a.P.f[RY][A], a.P.f[RZ][A]), q, 1.0);
+  obb_enlarge(gate, a.rV);
+  const V3 he = mk(fabs(gate.e1.x) * gate.ext.x + fabs(gate.e2.x) * gate.ext.y + fabs(gate.e3.x) * gate.ext.z,
+                   fabs(gate.e1.y) * gate.ext.x + fabs(gate.e2.y) * gate.ext.y + fabs(gate.e3.y) * gate.ext.z,
+                   fabs(gate.e1.z) * gate.ext.x + fabs(gate.e2.z) * gate.ext.y + fabs(gate.e3.z) * gate.ext.z);
+  const double gm = 1e-6 * (1.0 + fabs(gate.c.x) + fabs(gate.c.y) + fabs(gate.c.z) + he.x + he.y + he.z);
+  const V3 glo = gate.c - he - mk(gm, gm, gm), ghi = gate.c + he + mk(gm, gm, gm);
+  const MeshQuery r12 = mesh_query(m, lo, hi);
+  const MeshQuery r0 = mesh_query(m, mk(fmin(lo.x, glo.x), fmin(lo.y, glo.y), fmin(lo.z, glo.z)),
+                                  mk(fmax(hi.x, ghi.x), fmax(hi.y, ghi.y), fmax(hi.z, ghi.z)));
+  uint32_t total = 0;
+  if (!r0.empty) {
+    const uint32_t noff[3] = {0u, (uint32_t)m.nv, (uint32_t)(m.nv + m.ne)};
+    for (int z = r0.lo[2]; z <= r0.hi[2]; z++)
+      for (int y = r0.lo[1]; y <= r0.hi[1]; y++)
+        for (int x = r0.lo[0]; x <= r0.hi[0]; x++) {
+          const bool in12 = !r12.empty && x >= r12.lo[0] && x <= r12.hi[0] && y >= r12.lo[1] && y <= r12.hi[1] &&
+                            z >= r12.lo[2] && z <= r12.hi[2];
+          const uint64_t bb = (uint64_t)x + (uint64_t)m.dims[0] * ((uint64_t)y + (uint64_t)m.dims[1] * z);
+          const uint32_t q0 = m.boff[bb], q1 = m.boff[bb + 1];
+          for (uint32_t t0 = q0; t0 < q1; t0 += 32) {
+            const uint32_t t = t0 + lane;
+            uint32_t kind = 3, j = 0;
+            if (t < q1) {
+              const uint32_t it = m.bitem[t];
+              kind = it >> 30;
+              j = it & 0x3fffffffu;
+              const MeshQuery& R = kind == 0 ? r0 : r12;
+              const uint64_t f = m.flo[noff[kind] + j];
+              const int fx = (int)(f & 0x1fffffu), fy = (int)((f >> 21) & 0x1fffffu), fz = (int)(f >> 42);
+              if ((kind != 0 && !in12) || x != max(fx, R.lo[0]) || y != max(fy, R.lo[1]) || z != max(fz, R.lo[2]))
+                kind = 3;  // another bin of the box visits it, or the vertex box does not reach it
+            }
+            uint32_t n = kind < 3 ? mesh_feature_tests<false>(a, m, kind, j, SA, ra, va, gate, A, k, 0) : 0u;
+            if (Fill) {
+              uint32_t pre = n;  // inclusive warp scan of the per-lane counts
+              for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(0xffffffffu, pre, o);
+                if (lane >= o) pre += v;
+              }
+              if (n) mesh_feature_tests<true>(a, m, kind, j, SA, ra, va, gate, A, k, base + total + pre - n);
+              total += __shfl_sync(0xffffffffu, pre, 31);
+            } else {
+              for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+              total += n;
+            }
+          }
+        }
+  }
+  (void)lt;
+  if (!Fill && lane == 0) a.fcnt[u] = total;
+}
+
 // vertex - driver unit (add_driver_interaction): filter(rV + minkowski(h), vertex)
 template <bool Fill>
 __device__ __forceinline__ void driver_unit(const FeatArgs& a, uint64_t u, uint32_t A, const ShapeDev& SA, double ra,
                                             const VView& va, uint32_t base, int lane, uint32_t lt) {
   const uint32_t k = a.u_partner[u];
   const DriverDev& d = a.drv[k];
+  if (d.kind == 2) {
+    mesh_unit<Fill>(a, u, A, SA, ra, va, base, lane, lt);
+    return;
+  }
   const uint32_t type = d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER;
   const bool keep = lane < SA.nv && driver_reach(d, a.rV + ra, va[lane]);
   const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -992,6 +1158,39 @@ __global__ void k_harvest_write(uint64_t nu, const uint32_t* __restrict__ flag, 
   for (int k = 0; k < 4; k++) yo[p * 4 + k] = (uint8_t)((t >> (8 * k)) & 255u);
 }
 
+// InteractionPair order inside a mesh unit (the fill pass wrote it in lane order)
+__global__ void k_mesh_unit_sort(uint64_t nu, const uint32_t* __restrict__ u_kind, const uint32_t* __restrict__ u_partner,
+                                 const DriverDev* __restrict__ drv, const uint32_t* __restrict__ foff, IArrays I) {
+  const uint64_t u = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= nu || !u_kind[u] || drv[u_partner[u]].kind != 2) return;
+  const uint32_t b = foff[u], e = foff[u + 1];
+  auto key = [&](uint32_t x) {
+    const uint32_t m = I.meta[x], s = I.sub[x];
+    return skey(meta_type(m), (m >> 15) & 1u, s & 0xffffu, s >> 16);
+  };
+  for (uint32_t x = b + 1; x < e; x++) {
+    const uint64_t kx = key(x);
+    const uint32_t mx = I.meta[x], sx = I.sub[x];
+    double h[6] = {I.ft[0][x], I.ft[1][x], I.ft[2][x], I.mo[0][x], I.mo[1][x], I.mo[2][x]};
+    uint32_t y = x;
+    while (y > b && key(y - 1) > kx) {
+      I.meta[y] = I.meta[y - 1];
+      I.sub[y] = I.sub[y - 1];
+      for (int d = 0; d < 3; d++) {
+        I.ft[d][y] = I.ft[d][y - 1];
+        I.mo[d][y] = I.mo[d][y - 1];
+      }
+      y--;
+    }
+    I.meta[y] = mx;
+    I.sub[y] = sx;
+    for (int d = 0; d < 3; d++) {
+      I.ft[d][y] = h[d];
+      I.mo[d][y] = h[3 + d];
+    }
+  }
+}
+
 // own_off[s] = feature offset of the first unit of s
 __global__ void k_own_from_units(uint64_t n, const uint32_t* __restrict__ uoff, const uint32_t* __restrict__ foff,
                                  uint32_t* __restrict__ own) {
@@ -1018,9 +1217,10 @@ struct PCArgs {
   int dmt;        // Hooke_DMT law combination
   ParamTable pt;  // multi-material parameters (pt.pp == nullptr: cp / cpd)
   ContactStateArrays cs;  // analysis, in the contact law's frame (cs.dn == nullptr: off)
+  const MeshDev* mesh;
   uint32_t* L2;
   double* D[7];
-  unsigned long long* cnt;  // [1] = L2 count
+  unsigned long long* cnt;  // [1] = L2 count, [2] = L2 entries with dn >= 0 (cohesive mesh items)
   unsigned long long* n_active;
 };
 
@@ -1082,6 +1282,7 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
     bool contact;
     V3 ri, rj = mk(0, 0, 0);
     bool is_pp = type <= DEM_ITYPE_EDGE_EDGE;
+    bool is_mesh = false;  // mesh items go to the Hooke pass (types 11, 12 swap the law's roles)
     double dncut;
     const dem_contact_params* hp = &a.cp;
     uint32_t swap = (meta >> 15) & 1u;
@@ -1092,7 +1293,10 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
       const V3 vert = pview(a, p)[a.I.sub[k] & 0xffffu];
       const DriverDev& dv = a.drv[a.I.partner[k]];
       d = det_none();
-      if (dv.kind == 0) {
+      if (dv.kind == 2) {  // ContactLawRShapeDriverFunc (polyhedron/contact.hpp:305-432)
+        is_mesh = true;
+        d = poly_mesh_detect(a.mesh[dv.mesh], type, a.I.sub[k] & 0xffffu, a.I.sub[k] >> 16, pview(a, p), sh, rm);
+      } else if (dv.kind == 0) {
         const V3 nrm = mk(dv.normal[0], dv.normal[1], dv.normal[2]);
         const V3 proj = dot(vert, nrm) * nrm;
         const V3 s2p = -(mk(dv.center_proj[0], dv.center_proj[1], dv.center_proj[2]) - proj);
@@ -1148,7 +1352,7 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
       const V3 z = mk(0, 0, 0);
       pwrite(a, k, z, z, z, z, z);
       a.cs.write(k, 0.0, d.cp, z, z);  // item.reset(), dn = 0, the detector's contact point
-    } else if (a.cohesive && d.dn >= 0) {
+    } else if (a.cohesive && d.dn >= 0 && !is_mesh) {
       const dem_contact_params& hkp = *hp;
       const double fn_value = (hkp.fc / hkp.dncut) * d.dn - hkp.fc;
       const V3 f = mk(0, 0, 0) + fn_value * d.n;
@@ -1166,6 +1370,9 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
     }
   }
   const uint32_t pos = warp_append2(heavy, a.cnt + 1);
+  const bool idle = heavy && !(d.dn < 0);  // in the Hooke pass without overlap
+  const unsigned im = __ballot_sync(0xffffffffu, idle);
+  if (im && (threadIdx.x & 31) == __ffs(im) - 1) atomicAdd(a.cnt + 2, (unsigned long long)__popc(im));
   if (heavy) {
     a.L2[pos] = (uint32_t)k;
     a.D[0][pos] = d.dn;
@@ -1198,7 +1405,7 @@ __device__ __forceinline__ void hooke(bool cohesive, double dn, V3 n, double dt,
 template <bool Fast>
 __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
   const uint64_t n2 = a.cnt[1];
-  if (blockIdx.x == 0 && threadIdx.x == 0) *a.n_active = n2;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *a.n_active = n2 - a.cnt[2];
   const uint64_t stride = (uint64_t)gridDim.x * PT;
   for (uint64_t w = (uint64_t)blockIdx.x * PT + threadIdx.x; w < n2; w += stride) {
     const uint32_t k = a.L2[w];
@@ -1214,6 +1421,28 @@ __global__ void __launch_bounds__(PT) k_phooke(PCArgs a) {
       const DriverDev& d = a.drv[a.I.partner[k]];
       const V3 r = ldv(a.P, RX, p), v = ldv(a.P, VX, p), w_ = ldv(a.P, WX, p);
       const double meff = a.P.f[MASS][p];
+      if (d.kind == 2) {
+        // ContactLawRShapeDriverFunc (polyhedron/contact.hpp:305-432): reff =
+        // compute_effective_radius of the two Minkowski radii; types 7-10 apply the
+        // law with the particle as i, 11-12 with the mesh as i: the particle takes
+        // -f and -moment, and the friction is stored negated
+        const double ra = a.P.f[HOM][p] * a.shapes[a.P.type[p]].r, mr = a.mesh[d.mesh].r;
+        const double reff = a.dmt ? (ra * mr) / (ra + mr) : 0.0;
+        const dem_contact_params& hp = a.pt.drv(a.cpd, a.P.group[p], a.I.partner[k]);
+        const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
+        const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]), dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
+        if (meta_type(meta) <= DEM_ITYPE_EDGE_MESH_EDGE) {
+          hooke<Fast>(a.cohesive, dn, n, a.dt, hp, meff, ft, cpos, r, v, f, mo, w_, dpos, dvel, dvrot, a.dmt, reff);
+          pwrite(a, k, ft, mo, f, cross(cpos - r, f) + mo, mk(0, 0, 0));
+          a.cs.write(k, dn, cpos, f - ft, ft);
+        } else {
+          hooke<Fast>(a.cohesive, dn, n, a.dt, hp, meff, ft, cpos, dpos, dvel, f, mo, dvrot, r, v, w_, a.dmt, reff);
+          const V3 fp = -f;
+          pwrite(a, k, -ft, mo, fp, cross(cpos - r, fp) + (-mo), mk(0, 0, 0));
+          a.cs.write(k, dn, cpos, ft - f, -ft);
+        }
+        continue;
+      }
       // DMT: reff = shp.minkowski(h) (polyhedron/contact.hpp:281)
       const double reff = a.dmt ? a.P.f[HOM][p] * a.shapes[a.P.type[p]].r : 0.0;
       hooke<Fast>(a.cohesive, dn, n, a.dt, a.pt.drv(a.cpd, a.P.group[p], a.I.partner[k]), meff, ft, cpos, r, v, f,
@@ -1341,6 +1570,7 @@ int launch_poly_units(dem_ctx* c, uint64_t* nu_out, int (*grow_units)(dem_ctx*, 
   a.cell_of = c->cell_of;
   a.drv = c->drv_dev;
   a.ndrv = c->ndrv;
+  a.mesh = c->mesh_dev;
   a.shapes = (const ShapeDev*)c->shapes_dev;
   a.rV = c->prm.rcut_inc;
   const double nd = 2 * c->rad_max + c->prm.rcut_inc;
@@ -1377,6 +1607,7 @@ static FeatArgs make_fargs(dem_ctx* c, uint64_t nu) {
   a.P = c->P[c->pcur];
   a.shapes = (const ShapeDev*)c->shapes_dev;
   a.drv = c->drv_dev;
+  a.mesh = c->mesh_dev;
   a.MV = c->MV;
   a.vx = c->vtx[0];
   a.vy = c->vtx[1];
@@ -1442,6 +1673,9 @@ int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
     k_feat_dec<true><<<blocks, PT, 0, c->stream>>>(a);
   else if (nu)
     k_feat<true><<<blocks, PT, 0, c->stream>>>(a);
+  if (nu && !c->meshes.empty())
+    k_mesh_unit_sort<<<grid_for(nu, 128), 128, 0, c->stream>>>(nu, c->u_kind, c->u_partner, c->drv_dev, c->f_off,
+                                                              a.dst);
   k_own_from_units<<<grid_for(c->n + 1, 256), 256, 0, c->stream>>>(c->n, c->u_off, c->f_off, c->own_off[1 - c->icur]);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
@@ -1514,7 +1748,7 @@ int launch_harvest(dem_ctx* c, float* x, uint8_t* y, uint64_t capacity, uint64_t
 }
 
 int launch_contact_poly(dem_ctx* c) {
-  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 3, 0, 2 * sizeof(unsigned long long), c->stream));
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 3, 0, 3 * sizeof(unsigned long long), c->stream));
   ProfScope ps(c, K_CONTACT, 2);
   PCArgs a;
   a.P = c->P[c->pcur];
@@ -1534,6 +1768,7 @@ int launch_contact_poly(dem_ctx* c) {
   a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
   a.pt = c->ptable();
   a.cs = c->cs;
+  a.mesh = c->mesh_dev;
   a.L2 = c->L2;
   for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];
   a.cnt = c->d_scalars + 3;

@@ -41,6 +41,32 @@ __device__ inline DetD mesh_detect(const MeshDev& m, uint32_t type, uint32_t j, 
   return DetD{inside, dn, n, p - n * (rad + 0.5 * dn)};
 }
 
+// detect<7..12> for a polyhedron (shape_detection_api.hpp:357-405): its vertex,
+// edge or face osub (world vertices va, shape sh, Minkowski radius ra) against
+// the mesh's feature psub; 11 and 12 take the mesh vertex as the vertex side
+__device__ inline DetD poly_mesh_detect(const MeshDev& m, uint32_t type, uint32_t osub, uint32_t psub,
+                                        const VView& va, const ShapeDev& sh, double ra) {
+  const VView mv = mesh_view(m);
+  switch (type) {
+    case DEM_ITYPE_VERTEX_MESH_VERTEX: return detect_vv(va[osub], ra, mv[psub], m.r);
+    case DEM_ITYPE_VERTEX_MESH_EDGE: return detect_ve(va[osub], ra, mv[m.e[2 * psub]], mv[m.e[2 * psub + 1]], m.r);
+    case DEM_ITYPE_VERTEX_MESH_FACE: {
+      const double R = ra + m.r;
+      double dist;
+      V3 n;
+      const int b = m.fo[psub];
+      const bool inside = vf_core_list(R, va[osub], mv, m.fv + b, m.fo[psub + 1] - b, dist, n);
+      if (dist > R) return det_none();
+      const double dn = dist - R;
+      return DetD{inside, dn, n, va[osub] - n * (ra + 0.5 * dn)};
+    }
+    case DEM_ITYPE_EDGE_MESH_EDGE:
+      return detect_ee(va[sh.e[2 * osub]], va[sh.e[2 * osub + 1]], ra, mv[m.e[2 * psub]], mv[m.e[2 * psub + 1]], m.r);
+    case DEM_ITYPE_MESH_VERTEX_EDGE: return detect_ve(mv[psub], m.r, va[sh.e[2 * osub]], va[sh.e[2 * osub + 1]], ra);
+    default: return detect_vf(mv[psub], m.r, va, sh, (int)osub, ra);
+  }
+}
+
 // the features listed in the bin of p (none outside the bin grid)
 template <class F>
 __device__ inline void mesh_bin_items(const MeshDev& m, V3 p, F&& f) {

@@ -481,3 +481,56 @@ def polyhedra_lattice(nx=8, ny=8, nz=6, spacing=1.3, density=1.0, seed=7, radius
     w = Workload("polyhedra_lattice", p, arr, surfaces=surfaces, steps=100)
     w.shapes = shapes
     return w
+
+
+def polyhedra_mesh_terrain(nx=6, ny=6, nz=2, spacing=1.6, density=1.0, seed=11, radius=0.01, amp=0.3, waves=2,
+                           m=14, minkowski=0.02, vz=-3.0, dt=5e-4, skin=0.05, kn=1e4, steps=300,
+                           **flags) -> Workload:
+    """Polyhedra (cube / tetrahedron / octahedron mix, random orientations) on a
+    lattice above a triangulated height field (a mesh driver: interaction types
+    7-12 against its vertices, edges and faces) inside four walls, falling at
+    vz.  The mesh is built about the origin and placed by its center and a
+    quarter turn about z.  Hooke kn, kt = 0.8 kn, mu 0.5, damp 0.9."""
+    from exadem_gb300.stl import build_shape
+
+    shapes = [shape_cube(1.0, radius), shape_tetrahedron(1.2, radius), shape_octahedron(1.0, radius)]
+    rng = np.random.default_rng(seed)
+    n = nx * ny * nz
+    side = (nx + 1) * spacing
+    zc = amp + 0.2
+    z0 = zc + amp + minkowski + 1.0
+    g = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+    pos = np.stack([(g[:, 0] + 1.0) * spacing, (g[:, 1] + 1.0) * spacing, z0 + g[:, 2] * spacing], 1)
+    pos = pos + rng.uniform(-0.05, 0.05, (n, 3))
+    types = rng.integers(0, 3, n).astype(np.uint32)
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1)[:, None]
+    arr = empty_particles(n)
+    arr["rx"], arr["ry"], arr["rz"] = (np.ascontiguousarray(pos[:, k]) for k in range(3))
+    arr["qw"], arr["qx"], arr["qy"], arr["qz"] = (np.ascontiguousarray(q[:, k]) for k in range(4))
+    arr["vx"], arr["vy"] = (rng.uniform(-0.2, 0.2, n) for _ in range(2))
+    arr["vz"] = np.full(n, vz) + rng.uniform(-0.2, 0.2, n)
+    arr["vrotx"], arr["vroty"], arr["vrotz"] = (rng.uniform(-1.0, 1.0, n) for _ in range(3))
+    arr["type"] = types
+    arr["id"] = np.arange(n, dtype=np.uint64)
+    arr["radius"] = np.array([shapes[t]["max_rcut"] for t in types])
+    vol = np.array([shapes[t]["volume"] for t in types])
+    iom = np.array([shapes[t]["i_over_m"] for t in types])
+    arr["mass"] = density * vol
+    for ax in ("inertiax", "inertiay", "inertiaz"):
+        arr[ax] = arr["mass"] * iom
+    arr["homothety"] = np.ones(n)
+    hi = (side, side, z0 + nz * spacing + 1.0)
+    cfg = dict(kn=kn, kt=0.8 * kn, kr=0.0, mu=0.5, damp_rate=0.9)
+    p = make_params((0, 0, 0), hi, (0, 0, 0), rcut_inc=skin, dt=dt, gravity=(0, 0, -9.81), config=cfg,
+                    config_driver=cfg, **flags)
+    walls = [dict(offset=0.0, normal=(1.0, 0.0, 0.0)), dict(offset=side, normal=(1.0, 0.0, 0.0)),
+             dict(offset=0.0, normal=(0.0, 1.0, 0.0)), dict(offset=side, normal=(0.0, 1.0, 0.0))]
+    shp = build_shape(list(terrain_triangles(side, m, amp, waves, 0.0)))
+    c45 = math.cos(math.pi / 4)
+    mesh = dict(vertices=shp["vertices"], edges=shp["edges"], faces=shp["faces"], minkowski=minkowski,
+                center=(side / 2, side / 2, zc), quat=(c45, 0.0, 0.0, c45))
+    w = Workload("polyhedra_mesh_terrain", p, arr, surfaces=walls, meshes=[mesh], steps=steps)
+    w.shapes = shapes
+    return w
+

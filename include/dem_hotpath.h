@@ -48,6 +48,9 @@ extern "C" {
 #define DEM_ITYPE_VERTEX_MESH_VERTEX 7 /* VertexRshapeDriverVertex */
 #define DEM_ITYPE_VERTEX_MESH_EDGE 8   /* VertexRshapeDriverEdge   */
 #define DEM_ITYPE_VERTEX_MESH_FACE 9   /* VertexRshapeDriverFace   */
+#define DEM_ITYPE_EDGE_MESH_EDGE 10    /* EdgeRshapeDriverEdge     */
+#define DEM_ITYPE_MESH_VERTEX_EDGE 11  /* EdgeRshapeDriverVertex: particle edge, mesh vertex */
+#define DEM_ITYPE_MESH_VERTEX_FACE 12  /* FaceRshapeDriverVertex: particle face, mesh vertex */
 
 /* ---- contact law parameters -------------------------------------------
  * Mirrors ContactParams {dncut, kn, kt, kr, fc, mu, damp_rate}
@@ -247,9 +250,13 @@ int dem_get_particles(dem_ctx* ctx, dem_particles* out, int on_device);
  * motion only; vrot enters the relative velocity (rotating drum).         */
 int dem_register_surface(dem_ctx* ctx, const dem_surface* s);
 int dem_register_cylinder(dem_ctx* ctx, const dem_cylinder* c);
-/* register_stl_mesh: sphere systems (interaction types 7-9: the sphere against a
- * mesh vertex, edge or face, nbh_sphere.hpp:25-86, contact_sphere.hpp:300-396).
- * The driver index is the registration order, shared with the other drivers. */
+/* register_stl_mesh.  Spheres: interaction types 7-9, the sphere against a mesh
+ * vertex, edge or face (nbh_sphere.hpp:25-86, contact_sphere.hpp:300-396).
+ * Polyhedra: types 7-12 (nbh_polyhedron_driver.hpp:61-192,
+ * polyhedron/contact.hpp:305-432), owner sub = the particle's vertex, edge or
+ * face, partner sub = the mesh's.  The driver index is the registration order,
+ * shared with the other drivers.  Polyhedron systems with a mesh need
+ * learned_sizing = 0.                                                        */
 int dem_register_mesh(dem_ctx* ctx, const dem_mesh* m);
 
 /* ---- batching: many independent systems in one context -------------------

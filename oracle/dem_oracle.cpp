@@ -1071,6 +1071,59 @@ bool mesh_detect(const Oracle& o, const Inter& it, const V3& ri, double rad, dou
   return d.c;
 }
 
+// add_driver_interaction for an RShapeDriver (nbh_polyhedron_driver.hpp:61-192):
+// every particle-vertex / mesh-feature (7, 8, 9), particle-edge / mesh-edge (10)
+// and mesh-vertex / particle-edge or face (11, 12) pair whose Verlet filter
+// passes; 11 and 12 only for the mesh vertices whose box (vertex +- Minkowski
+// radius) meets the particle's OBB (rotated and translated, homothety not
+// applied) enlarged by rVerlet.  The type 9 gate of the reference (face OBB
+// against the vertex box) holds whenever the face filter passes.
+void poly_mesh_candidates(const Oracle& o, size_t k, size_t a, double rV, std::vector<Inter>& lst) {
+  const MeshO& m = o.meshes[o.drivers[k].mesh];
+  const PShape& sa = o.shapes[o.type[a]];
+  const double ra = sa.r * o.hom[a];
+  const std::vector<V3>& va = o.vtx[a];
+  auto add = [&](int type, int osub, int psub) {
+    Inter it{};
+    it.oid = o.id[a];
+    it.pid = k;
+    it.type = (uint16_t)type;
+    it.oi = (int32_t)a;
+    it.pj = (int32_t)k;
+    it.osub = (uint32_t)osub;
+    it.psub = (uint32_t)psub;
+    lst.push_back(it);
+  };
+  const int mnv = (int)m.w.size(), mne = (int)m.e.size() / 2, mnf = (int)m.f.size();
+  for (int i = 0; i < sa.nv(); i++) {
+    for (int j = 0; j < mnv; j++)
+      if (filter_vv(rV, va[i], ra, m.w[j], m.r)) add(DEM_ITYPE_VERTEX_MESH_VERTEX, i, j);
+    for (int j = 0; j < mne; j++)
+      if (filter_ve(rV, va[i], ra, m.w[m.e[2 * j]], m.w[m.e[2 * j + 1]], m.r)) add(DEM_ITYPE_VERTEX_MESH_EDGE, i, j);
+    for (int j = 0; j < mnf; j++)
+      if (filter_vf(rV, va[i], ra, m.w, m.f[j], m.r)) add(DEM_ITYPE_VERTEX_MESH_FACE, i, j);
+  }
+  for (int e = 0; e < sa.ne(); e++)
+    for (int j = 0; j < mne; j++)
+      if (filter_ee(rV, va[sa.e[2 * e]], va[sa.e[2 * e + 1]], ra, m.w[m.e[2 * j]], m.w[m.e[2 * j + 1]], m.r))
+        add(DEM_ITYPE_EDGE_MESH_EDGE, e, j);
+  OBBr gate = compute_obb(sa.obb, pos(o, a), {o.qw[a], o.qx[a], o.qy[a], o.qz[a]}, 1.0);
+  obb_enlarge(gate, rV);
+  for (int j = 0; j < mnv; j++) {
+    OBBr ov{};
+    ov.c = m.w[j];
+    ov.e1 = {1, 0, 0};
+    ov.e2 = {0, 1, 0};
+    ov.e3 = {0, 0, 1};
+    obb_enlarge(ov, m.r);
+    if (!obb_intersect(ov, gate)) continue;  // obb_v_rshape_j.intersect(obb_i)
+    for (int e = 0; e < sa.ne(); e++)
+      if (filter_ve(rV, m.w[j], m.r, va[sa.e[2 * e]], va[sa.e[2 * e + 1]], ra)) add(DEM_ITYPE_MESH_VERTEX_EDGE, e, j);
+    for (int f = 0; f < sa.nf(); f++)
+      if (filter_vf(rV, m.w[j], m.r, va, sa.f[f], ra)) add(DEM_ITYPE_MESH_VERTEX_FACE, f, j);
+  }
+}
+
 void compute_vertices(Oracle& o) {
   o.vtx.resize(o.n);
 #pragma omp parallel for schedule(static)
@@ -1125,6 +1178,10 @@ int update_neighbors_poly(Oracle& o) {
     // drivers: each vertex against each driver
     for (size_t k = 0; k < o.drivers.size(); k++) {
       const Driver& dv = o.drivers[k];
+      if (dv.kind == 2) {
+        poly_mesh_candidates(o, k, a, rV, lst);
+        continue;
+      }
       for (int v = 0; v < sa.nv(); v++) {
         const double rc = rV + ra;
         const bool keep = dv.kind == 0 ? surface_filter(dv.s, rc, o.vtx[a][v]) : cylinder_filter(dv.c, rc, o.vtx[a][v]);
@@ -1271,6 +1328,65 @@ void contact_one_poly(Oracle& o, size_t k) {
   const bool cohesive = o.prm.law == DEM_LAW_HOOKE_COHESIVE;
   const bool dmt = o.prm.law == DEM_LAW_HOOKE_DMT;
   const double dt = o.prm.dt;
+  if (it.type >= DEM_ITYPE_VERTEX_MESH_VERTEX) {
+    // ContactLawRShapeDriverFunc (polyhedron/contact.hpp:305-432): detect<type>,
+    // reff = compute_effective_radius of the Minkowski radii; types 7-10 apply the
+    // law with the particle as i, 11-12 with the mesh as i (the particle takes -f
+    // and -moment, the friction is stored negated)
+    const size_t p = it.oi;
+    const PShape& sh = o.shapes[o.type[p]];
+    const double ra = sh.r * o.hom[p];
+    const MeshO& m = o.meshes[o.drivers[it.pj].mesh];
+    const std::vector<V3>& va = o.vtx[p];
+    const int os = (int)it.osub, ps = (int)it.psub;
+    Det d;
+    switch (it.type) {
+      case DEM_ITYPE_VERTEX_MESH_VERTEX: d = detect_vv(va[os], ra, m.w[ps], m.r); break;
+      case DEM_ITYPE_VERTEX_MESH_EDGE: d = detect_ve(va[os], ra, m.w[m.e[2 * ps]], m.w[m.e[2 * ps + 1]], m.r); break;
+      case DEM_ITYPE_VERTEX_MESH_FACE: d = detect_vf(va[os], ra, m.w, m.f[ps], m.r); break;
+      case DEM_ITYPE_EDGE_MESH_EDGE:
+        d = detect_ee(va[sh.e[2 * os]], va[sh.e[2 * os + 1]], ra, m.w[m.e[2 * ps]], m.w[m.e[2 * ps + 1]], m.r);
+        break;
+      case DEM_ITYPE_MESH_VERTEX_EDGE: d = detect_ve(m.w[ps], m.r, va[sh.e[2 * os]], va[sh.e[2 * os + 1]], ra); break;
+      default: d = detect_vf(m.w[ps], m.r, va, sh.f[os], ra);
+    }
+    const dem_contact_params& cpar = o.driver_params(p, it.pj);
+    bool contact = d.c;
+    if (cohesive) contact = (contact || d.dn <= cpar.dncut);
+    if (contact) {
+      const V3 r = pos(o, p);
+      const V3 v = {o.vx[p], o.vy[p], o.vz[p]};
+      const V3 w = {o.wx[p], o.wy[p], o.wz[p]};
+      const double meff = o.mass[p];
+      const double reff = dmt ? (ra * m.r) / (ra + m.r) : 0.0;
+      const V3 zero = {0, 0, 0};
+      V3 f = {0, 0, 0};
+      if (it.type <= DEM_ITYPE_EDGE_MESH_EDGE) {
+        contact_force_core(cohesive, d.dn, d.n, dt, cpar, meff, it.friction, d.cp, r, v, f, it.moment, w, m.center,
+                           zero, zero, dmt, reff);
+        rc.f = f;
+        rc.ti = cross(d.cp - r, f) + it.moment;
+        rc.sfn = f - it.friction;
+        rc.sft = it.friction;
+      } else {
+        contact_force_core(cohesive, d.dn, d.n, dt, cpar, meff, it.friction, d.cp, m.center, zero, f, it.moment,
+                           zero, r, v, w, dmt, reff);
+        rc.f = -f;
+        rc.ti = cross(d.cp - r, -f) + (-it.moment);
+        rc.sfn = it.friction - f;
+        it.friction = -it.friction;
+        rc.sft = it.friction;
+      }
+      rc.active = d.dn < 0;
+      rc.sdn = d.dn;
+      rc.scp = d.cp;
+    } else {
+      it.friction = {0, 0, 0};
+      it.moment = {0, 0, 0};
+      rc.scp = d.cp;  // dn = 0, the detector's contact point
+    }
+    return;
+  }
   if (it.type >= DEM_ITYPE_VERTEX_CYLINDER) {
     const size_t p = it.oi;
     const PShape& sh = o.shapes[o.type[p]];
@@ -1526,7 +1642,6 @@ int oracle_register_cylinder(void* h, const dem_cylinder* c) {
 }
 int oracle_register_mesh(void* h, const dem_mesh* s) {  // register_stl_mesh (register_stl_mesh.cpp:40-147)
   Oracle& o = *(Oracle*)h;
-  if (o.poly) return DEM_ERR_UNSUPPORTED;
   MeshO m;
   m.r = s->minkowski;
   m.center = {s->center[0], s->center[1], s->center[2]};

@@ -1,9 +1,11 @@
-"""Mesh drivers (register_stl_mesh; interaction types 7-9, nbh_sphere.hpp:25-86,
-contact_sphere.hpp:300-396) on the GPU against the oracle, bit for bit: the
-interaction list (partner sub = the mesh feature), the particles and the
-contact state after spheres land on a triangulated terrain, on the plain and
-fused paths (graph replay included), with the cohesive and DMT laws and with
-multi-material tables; and the registration checks."""
+"""Mesh drivers (register_stl_mesh) on the GPU against the oracle, bit for bit:
+spheres (interaction types 7-9, nbh_sphere.hpp:25-86, contact_sphere.hpp:300-396)
+and polyhedra (types 7-12, nbh_polyhedron_driver.hpp:61-192,
+polyhedron/contact.hpp:305-432) landing on a triangulated terrain.  Compared:
+the interaction list (owner / partner sub = the particle's / mesh's feature),
+the particles and the contact state, on the plain and fused paths (graph
+replay included), with the cohesive and DMT laws and with multi-material
+tables; and the registration checks."""
 import numpy as np
 import pytest
 
@@ -96,6 +98,39 @@ def test_mesh_registration_checks(native_lib):
         s.register_mesh(**dict(m, faces=[[0, 1]]))  # a face needs 3 vertices
     with pytest.raises(A.DemError):
         s.register_mesh(**dict(m, minkowski=-1.0))
-    p = W.polyhedra_lattice(nx=2, ny=2, nz=2).build()
-    with pytest.raises(A.DemError):
-        p.register_mesh(**m)  # sphere systems only
+
+
+@pytest.mark.parametrize("path", ["plain", "fused"])
+def test_poly_mesh_terrain_matches_oracle(native_lib, path):
+    f = int(path == "fused")
+    w = W.polyhedra_mesh_terrain(amp=0.5, waves=3, fused_step=f, fp32_broad_phase=f, fp32_contact_screen=f)
+    g, o = _run(w, 600, analysis=(path == "plain"))
+    lg = g.interactions()
+    assert_same_list(lg, o.interactions())
+    t = lg["type"]
+    assert all(np.sum(t == k) > 0 for k in (8, 9, 10, 12)), {k: int(np.sum(t == k)) for k in range(13)}
+    if path == "plain":
+        cg, co = g.contact_state(), o.contact_state()
+        for k in ("dn", "cp", "fn", "ft"):
+            assert np.array_equal(_bits(cg[k]), _bits(co[k])), k
+        assert np.sum((cg["dn"] < 0) & (t >= 7)) > 0
+        sg, tg = g.stress_tensor()
+        so, to = o.stress_tensor()
+        assert np.array_equal(_bits(tg), _bits(to))
+    assert bit_equal_fraction(g.particles(sort_by_id=True), o.particles(sort_by_id=True)) == 1.0
+    assert g.simulation_state()["n_active_interactions"] == o.simulation_state()["n_active_interactions"]
+
+
+@pytest.mark.parametrize("law", [A.LAW_HOOKE_COHESIVE, A.LAW_HOOKE_DMT])
+def test_poly_mesh_laws_match_oracle(native_lib, law):
+    w = W.polyhedra_mesh_terrain(amp=0.5, waves=3, seed=31, fused_step=1, fp32_broad_phase=1, fp32_contact_screen=1)
+    w.params.law = law
+    for cp in (w.params.config, w.params.config_driver):
+        if law == A.LAW_HOOKE_COHESIVE:
+            cp.dncut, cp.fc = 0.01, 5.0
+        else:
+            cp.gamma = 2.0
+    g, o = _run(w, 600)
+    assert_same_list(g.interactions(), o.interactions())
+    assert bit_equal_fraction(g.particles(sort_by_id=True), o.particles(sort_by_id=True)) == 1.0
+    assert g.simulation_state()["n_active_interactions"] == o.simulation_state()["n_active_interactions"]
