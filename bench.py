@@ -46,9 +46,11 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--n", type=int, default=None, help="particle count (default: the workload's)")
-    ap.add_argument("--workload", default="spheres", choices=["spheres", "polyhedra", "polyhedra_dense", "drums"],
+    ap.add_argument("--workload", default="spheres",
+                    choices=["spheres", "polyhedra", "polyhedra_dense", "drums", "mixer"],
                     help="spheres: 2M spheres on a floor (headline); polyhedra: 200k polyhedra deposition; "
-                         "polyhedra_dense: polyhedra on a dense lattice; drums: 256 rotating drums batched")
+                         "polyhedra_dense: polyhedra on a dense lattice; drums: 256 rotating drums batched; "
+                         "mixer: 50k spheres falling into a mesh (STL) mixer")
     ap.add_argument("--systems", type=int, default=256, help="drums: number of drums")
     ap.add_argument("--plain", action="store_true", help="plain FP64 path (no FP32 screening)")
     ap.add_argument("--no-graph", action="store_true", help="fused step launched from the host, no CUDA graph")
@@ -174,7 +176,7 @@ def _workload(args):
 
     opt = 0 if args.plain else 1
     flags = dict(fp32_contact_screen=opt, fused_step=opt, fp32_broad_phase=opt)
-    if args.workload in ("spheres", "drums"):
+    if args.workload in ("spheres", "drums", "mixer"):
         flags["graph_step"] = opt and not args.no_graph
     if args.learned and args.workload in ("polyhedra", "polyhedra_dense"):
         flags["learned_sizing"] = args.learned_mode
@@ -185,6 +187,8 @@ def _workload(args):
         return W.polyhedra_lattice(nx=side, ny=side, nz=side, **flags)
     if args.workload == "drums":
         return W.drums_batch(nsys=args.systems, nmax=args.n or 200_000, **flags)
+    if args.workload == "mixer":
+        return W.spheres_mixer(n=args.n, **flags)
     return W.spheres_floor(n=args.n or 2_000_000, **flags)
 
 
@@ -212,6 +216,8 @@ def build_from_host(w, arrays):
         s.register_surface(**kw)
     for kw in w.cylinders:
         s.register_cylinder(**kw)
+    for kw in w.meshes:
+        s.register_mesh(**kw)
     s.set_particles(arrays)
     return s
 
@@ -225,6 +231,8 @@ WORKLOAD_DESC = {
                        "orientations, Hooke kn=1e4, dt=1e-4",
     "drums": "drums_batch: 256 rotating drums (spheres r~U[0.45,0.55], counts log-uniform in [2e3, 2e5], "
              "30% fill, 2 rad/s, periodic along the axis), Hooke kn=1e4 kt=8e3 mu=0.4, dt=5e-4",
+    "mixer": "spheres_mixer: 50,304 spheres r=2 (SC lattice 4.1 in a cylinder r=92) falling into a mesh mixer "
+             "(wall, bottom, 4 blades: 2064 triangles, Minkowski 0.1), Hooke kn=1e3 kt=1e3 mu=0.5, dt=1e-3",
 }
 
 
@@ -375,7 +383,7 @@ def run_native(args, rank, world, local, dist):
     ext = torch.cuda.ExternalStream(s.stream_handle())
     s.first_iteration()
     tune = None
-    if not args.plain and not args.no_tune and args.workload in ("spheres", "drums"):
+    if not args.plain and not args.no_tune and args.workload in ("spheres", "drums", "mixer"):
         # cell size and launch shapes; the skin only where it cannot change a bit
         tune = s.autotune(steps_per_trial=3, skin_policy=1)
     if args.mul_mode is not None:

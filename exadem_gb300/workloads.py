@@ -534,3 +534,73 @@ def polyhedra_mesh_terrain(nx=6, ny=6, nz=2, spacing=1.6, density=1.0, seed=11, 
     w.shapes = shapes
     return w
 
+
+def mixer_triangles(radius=100.0, z0=30.0, z1=170.0, nseg=96, nring=10, blades=4, blade_len=80.0,
+                    blade_w=4.0, blade_h=2.5, angle=0.0):
+    """(nt, 3, 3) triangles of a synthetic mixer: a cylinder wall (nseg x nring
+    quads), a bottom disk (nseg triangles) and `blades` box blades on the
+    bottom, the shapes of the reference's mixer deck (its STL files are not
+    part of this build)."""
+    tri = []
+    th = np.linspace(0.0, 2 * math.pi, nseg + 1)
+    zs = np.linspace(z0, z1, nring + 1)
+    ring = lambda t, z: (radius * math.cos(t), radius * math.sin(t), z)
+    for a in range(nseg):
+        for b in range(nring):
+            p = [ring(th[a], zs[b]), ring(th[a + 1], zs[b]), ring(th[a + 1], zs[b + 1]), ring(th[a], zs[b + 1])]
+            tri += [[p[0], p[1], p[2]], [p[0], p[2], p[3]]]
+        tri.append([(0.0, 0.0, z0), ring(th[a + 1], z0), ring(th[a], z0)])
+    for k in range(blades):
+        t = angle + 2 * math.pi * k / blades
+        c, s_ = math.cos(t), math.sin(t)
+        loc = [(x, y, z) for z in (z0 + 0.5, z0 + 0.5 + blade_h) for (x, y) in
+               ((2.0, -blade_w / 2), (blade_len, -blade_w / 2), (blade_len, blade_w / 2), (2.0, blade_w / 2))]
+        v = [(x * c - y * s_, x * s_ + y * c, z) for x, y, z in loc]
+        for f in ((0, 2, 1), (0, 3, 2), (4, 5, 6), (4, 6, 7), (0, 1, 5), (0, 5, 4), (1, 2, 6), (1, 6, 5),
+                  (2, 3, 7), (2, 7, 6), (3, 0, 4), (3, 4, 7)):
+            tri.append([v[f[0]], v[f[1]], v[f[2]]])
+    return np.asarray(tri, dtype=np.float64)
+
+
+def spheres_mixer(spacing=4.1, radius=2.0, density=0.0028, cyl_radius=92.0, z_lo=36.0, z_hi=166.3, minkowski=0.1,
+                  dt=1e-3, skin=1.2, seed=13, steps=1000, n=None, **flags) -> Workload:
+    """The mixer deck's shapes with spheres (example/spheres/mixer, 57k spheres):
+    a simple-cubic lattice of spacing 4.1 inside a cylinder of radius 92 between
+    z = 36 and 166.3 (about 51k spheres of radius 2, density 0.0028, velocity
+    (0, 0, -1) with a 0.001 spread), falling into a synthetic mixer mesh
+    (wall, bottom and four blades, Minkowski radius 0.1, mixer_triangles).
+    Hooke kn 1000, kt 1000, mu 0.5, damp 0.999 (pairs), kt 800 for the mesh;
+    dt 1e-3 (the deck's README), rcut_inc 1.2, 10 m cells.  n limits the count."""
+    from exadem_gb300.stl import build_shape
+
+    rng = np.random.default_rng(seed)
+    ax = np.arange(-cyl_radius, cyl_radius + 1e-9, spacing)
+    az = np.arange(z_lo, z_hi + 1e-9, spacing)
+    gx, gy, gz = np.meshgrid(ax, ax, az, indexing="ij")
+    keep = gx ** 2 + gy ** 2 < cyl_radius ** 2
+    pos = np.stack([gx[keep], gy[keep], gz[keep]], 1)
+    pos = pos[np.lexsort((pos[:, 0], pos[:, 1], pos[:, 2]))]
+    if n is not None:
+        pos = pos[:n]
+    m = len(pos)
+    arr = empty_particles(m)
+    arr["rx"], arr["ry"], arr["rz"] = (np.ascontiguousarray(pos[:, k]) for k in range(3))
+    arr["vx"], arr["vy"] = (rng.normal(0.0, 0.001, m) for _ in range(2))
+    arr["vz"] = -1.0 + rng.normal(0.0, 0.001, m)
+    arr["radius"] = np.full(m, radius)
+    arr["mass"] = np.full(m, density * 4.0 / 3.0 * math.pi * radius ** 3)
+    for a in ("inertiax", "inertiay", "inertiaz"):
+        arr[a] = 0.4 * arr["mass"] * radius * radius
+    arr["qw"] = np.ones(m)
+    arr["homothety"] = np.ones(m)
+    arr["id"] = np.arange(m, dtype=np.uint64)
+    cfg = dict(kn=1000.0, kt=1000.0, kr=0.0, mu=0.5, damp_rate=0.999)
+    cfgd = dict(kn=1000.0, kt=800.0, kr=0.0, mu=0.5, damp_rate=0.999)
+    p = make_params((-105.0, -105.0, 28.0), (105.0, 105.0, 172.0), (0, 0, 0), rcut_inc=skin, dt=dt,
+                    gravity=(0, 0, -9.81), config=cfg, config_driver=cfgd, cell_size=10.0, **flags)
+    shp = build_shape(list(mixer_triangles()))
+    mesh = dict(vertices=shp["vertices"], edges=shp["edges"], faces=shp["faces"], minkowski=minkowski)
+    return Workload("spheres_mixer", p, arr, meshes=[mesh], steps=steps,
+                    info={"mesh_vertices": len(shp["vertices"]), "mesh_edges": len(shp["edges"]),
+                          "mesh_faces": len(shp["faces"])})
+
