@@ -108,9 +108,9 @@ struct DriverDev {
 // Mesh driver (RShapeDriver, rshape.hpp:104-420) on the device.  World vertices
 // center + quat * v in SoA; edges as vertex pairs; faces as CSR vertex lists.
 // A uniform bin grid covers the mesh: bin b lists (kind << 30 | index, kind 0
-// vertex, 1 edge, 2 face, in (kind, index) order) every feature whose Verlet
-// filter can pass for a sphere centred in b; a sphere outside the grid passes
-// none.  The bin of a point is floor((p - lo) * inv_bs) per axis.
+// vertex, 1 edge, 2 face, sorted) every feature whose Verlet filter can pass
+// for a point of b; a point outside the grid passes none.  The bin of a point
+// is floor((p - lo) * inv_bs) per axis.
 struct MeshDev {
   int nv, ne, nf;
   double r;  // Minkowski radius
@@ -125,10 +125,6 @@ struct MeshDev {
   int dims[3];
   const uint32_t* boff;   // bins + 1
   const uint32_t* bitem;  // boff[bins]
-  // lowest bin (x | y << 21 | z << 42) of each feature's range, vertices then
-  // edges then faces: a query over a box of bins visits a feature once, in the
-  // first bin its range shares with the box
-  const uint64_t* flo;
 };
 struct GridDev {
   int dims[3];

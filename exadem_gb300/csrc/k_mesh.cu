@@ -37,6 +37,46 @@ struct Box {
   double lo[3], hi[3];
 };
 
+// ---- host geometry for the bin lists (distances from a bin centre)
+struct P3 {
+  double x, y, z;
+};
+inline P3 sub3(P3 a, P3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline double dot3(P3 a, P3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline P3 axpy(P3 a, double t, P3 d) { return {a.x + t * d.x, a.y + t * d.y, a.z + t * d.z}; }
+inline double dist3(P3 a, P3 b) { return std::sqrt(dot3(sub3(a, b), sub3(a, b))); }
+// distance from c to the segment a + t (b - a), t in [t0, t1]
+double seg_dist(P3 c, P3 a, P3 b, double t0, double t1) {
+  const P3 d = sub3(b, a);
+  const double dd = dot3(d, d);
+  double t = dd > 0.0 ? dot3(sub3(c, a), d) / dd : 0.0;
+  t = std::min(std::max(t, t0), t1);
+  return dist3(c, axpy(a, t, d));
+}
+// distance from c to the triangle abc (closest point on a triangle, Ericson's
+// Real-Time Collision Detection 5.1.5)
+double tri_dist(P3 p, P3 a, P3 b, P3 c) {
+  const P3 ab = sub3(b, a), ac = sub3(c, a), ap = sub3(p, a);
+  const double d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+  if (d1 <= 0.0 && d2 <= 0.0) return dist3(p, a);
+  const P3 bp = sub3(p, b);
+  const double d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+  if (d3 >= 0.0 && d4 <= d3) return dist3(p, b);
+  const double vc = d1 * d4 - d3 * d2;
+  if (vc <= 0.0 && d1 >= 0.0 && d3 <= 0.0) return dist3(p, axpy(a, d1 / (d1 - d3), ab));
+  const P3 cp = sub3(p, c);
+  const double d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+  if (d6 >= 0.0 && d5 <= d6) return dist3(p, c);
+  const double vb = d5 * d2 - d1 * d6;
+  if (vb <= 0.0 && d2 >= 0.0 && d6 <= 0.0) return dist3(p, axpy(a, d2 / (d2 - d6), ac));
+  const double va = d3 * d6 - d5 * d4;
+  if (va <= 0.0 && (d4 - d3) >= 0.0 && (d5 - d6) >= 0.0)
+    return dist3(p, axpy(b, (d4 - d3) / ((d4 - d3) + (d5 - d6)), sub3(c, b)));
+  const double den = 1.0 / (va + vb + vc);
+  const double v = vb * den, w = vc * den;
+  return dist3(p, axpy(axpy(a, v, ab), w, ac));
+}
+
 // bins of one mesh for spheres of radius <= rad and the skin
 int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   const int nv = m.dev.nv, ne = m.dev.ne, nf = m.dev.nf;
@@ -115,21 +155,41 @@ int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   };
   const uint64_t nb = (uint64_t)dims[0] * dims[1] * dims[2];
   std::vector<uint32_t> cnt(nb + 1, 0);
-  std::vector<uint64_t> flo(box.size());
-  for (size_t k = 0; k < box.size(); k++)
-    flo[k] = (uint64_t)index(box[k].lo[0], 0) | ((uint64_t)index(box[k].lo[1], 1) << 21) |
-             ((uint64_t)index(box[k].lo[2], 2) << 42);
-  auto for_bins = [&](const Box& b, auto&& f) {
+  // a bin lists a feature when its centre is within E + margin + half its
+  // diagonal of the feature's region (vertex; edge segment extended by the skin
+  // in its parameter; face polygon, fan-split: a superset for a non-convex one),
+  // which holds for every bin holding a point that passes the filter
+  const double reach = E + 2.0 * margin + 0.8660254037844387 * bs * (1.0 + 1e-12);
+  auto near = [&](size_t k, P3 ctr) {
+    if (k < (size_t)nv) return dist3(ctr, {m.hx[k], m.hy[k], m.hz[k]}) <= reach;
+    if (k < (size_t)nv + ne) {
+      const int a = m.he[2 * (k - nv)], b = m.he[2 * (k - nv) + 1];
+      return seg_dist(ctr, {m.hx[a], m.hy[a], m.hz[a]}, {m.hx[b], m.hy[b], m.hz[b]}, -skin, 1.0 + skin) <= reach;
+    }
+    const int f = (int)(k - nv - ne), b0 = m.hfo[f], nvf = m.hfo[f + 1] - b0;
+    const int i0 = m.hfv[b0];
+    const P3 a = {m.hx[i0], m.hy[i0], m.hz[i0]};
+    for (int q = 1; q + 1 < nvf; q++) {
+      const int i1 = m.hfv[b0 + q], i2 = m.hfv[b0 + q + 1];
+      if (tri_dist(ctr, a, {m.hx[i1], m.hy[i1], m.hz[i1]}, {m.hx[i2], m.hy[i2], m.hz[i2]}) <= reach) return true;
+    }
+    return false;
+  };
+  auto for_bins = [&](size_t k, auto&& f) {
+    const Box& b = box[k];
     const int x0 = index(b.lo[0], 0), x1 = index(b.hi[0], 0);
     const int y0 = index(b.lo[1], 1), y1 = index(b.hi[1], 1);
     const int z0 = index(b.lo[2], 2), z1 = index(b.hi[2], 2);
     for (int z = z0; z <= z1; z++)
       for (int y = y0; y <= y1; y++)
-        for (int x = x0; x <= x1; x++) f((uint64_t)x + (uint64_t)dims[0] * ((uint64_t)y + (uint64_t)dims[1] * z));
+        for (int x = x0; x <= x1; x++) {
+          const P3 ctr = {D.lo[0] + (x + 0.5) * bs, D.lo[1] + (y + 0.5) * bs, D.lo[2] + (z + 0.5) * bs};
+          if (near(k, ctr)) f((uint64_t)x + (uint64_t)dims[0] * ((uint64_t)y + (uint64_t)dims[1] * z));
+        }
   };
   uint64_t total = 0;
-  for (const Box& b : box)
-    for_bins(b, [&](uint64_t q) {
+  for (size_t k = 0; k < box.size(); k++)
+    for_bins(k, [&](uint64_t q) {
       cnt[q + 1]++;
       total++;
     });
@@ -141,25 +201,20 @@ int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   for (size_t k = 0; k < box.size(); k++) {
     const uint32_t kind = k < (size_t)nv ? 0u : (k < (size_t)nv + ne ? 1u : 2u);
     const uint32_t idx = (uint32_t)(kind == 0 ? k : (kind == 1 ? k - nv : k - nv - ne));
-    for_bins(box[k], [&](uint64_t q) { items[cur[q]++] = (kind << 30) | idx; });
+    for_bins(k, [&](uint64_t q) { items[cur[q]++] = (kind << 30) | idx; });
   }
   cudaFree(m.boff);
   cudaFree(m.bitem);
-  cudaFree(m.flo);
   m.boff = nullptr;
   m.bitem = nullptr;
-  m.flo = nullptr;
   DEM_CUDA_TRY(c, cudaMalloc(&m.boff, (nb + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&m.bitem, std::max<uint64_t>(total, 1) * 4));
-  DEM_CUDA_TRY(c, cudaMalloc(&m.flo, box.size() * 8));
-  DEM_CUDA_TRY(c, cudaMemcpyAsync(m.flo, flo.data(), box.size() * 8, cudaMemcpyHostToDevice, c->stream));
   DEM_CUDA_TRY(c, cudaMemcpyAsync(m.boff, cnt.data(), (nb + 1) * 4, cudaMemcpyHostToDevice, c->stream));
   if (total)
     DEM_CUDA_TRY(c, cudaMemcpyAsync(m.bitem, items.data(), total * 4, cudaMemcpyHostToDevice, c->stream));
   DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   D.boff = m.boff;
   D.bitem = m.bitem;
-  D.flo = m.flo;
   m.bin_rad = rad;
   m.bin_skin = skin;
   return DEM_OK;
@@ -185,7 +240,8 @@ int ensure_mesh_bins(dem_ctx* c) {
   bool changed = false;
   const double rad = c->rad_max, skin = c->prm.rcut_inc;
   for (MeshStore& m : c->meshes) {
-    if (m.boff && m.bin_rad == rad && m.bin_skin == skin) continue;
+    // bins built for a larger radius bound and skin list a superset: still exact
+    if (m.boff && m.bin_rad >= rad && m.bin_skin >= skin) continue;
     if (c->capturing) return c->fail(DEM_ERR_STATE, "mesh bins are stale inside a graph capture");
     const int rc = build_bins(c, m, rad, skin);
     if (rc) return rc;
@@ -204,7 +260,6 @@ void free_meshes(dem_ctx* c) {
     cudaFree(m.fv);
     cudaFree(m.boff);
     cudaFree(m.bitem);
-    cudaFree(m.flo);
   }
   c->meshes.clear();
   cudaFree(c->mesh_dev);

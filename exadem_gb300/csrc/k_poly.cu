@@ -518,9 +518,10 @@ __device__ __forceinline__ uint32_t seg_swap(int seg) { return (seg == 2 || seg 
 // enlarged by rVerlet, the reference's gate.  The reference's type 9 gate (the
 // face's OBB against the vertex box) holds whenever the face filter passes and
 // is not evaluated.  Candidates are the mesh features listed in the bins under
-// A's box (mesh vertices: under the gate OBB's box too), each visited once;
-// the fill pass writes a unit's items in lane order and k_mesh_unit_sort puts
-// them in InteractionPair order.
+// A's box (mesh vertices: under the gate OBB's box too), each taken in the
+// first of those bins (scan order z, y, x) that lists it; the fill pass writes
+// a unit's items in lane order and k_mesh_unit_sort puts them in
+// InteractionPair order.
 struct MeshQuery {
   int lo[3], hi[3];
   bool empty;
@@ -584,6 +585,28 @@ __device__ uint32_t mesh_feature_tests(const FeatArgs& a, const MeshDev& m, uint
   return n;
 }
 
+// whether a bin of R before (x, y, z) in scan order lists item it (bin lists are sorted)
+__device__ inline bool listed_before(const MeshDev& m, const MeshQuery& R, int x, int y, int z, uint32_t it) {
+  for (int zz = R.lo[2]; zz <= z; zz++)
+    for (int yy = R.lo[1]; yy <= R.hi[1]; yy++) {
+      if (zz == z && yy > y) return false;
+      for (int xx = R.lo[0]; xx <= R.hi[0]; xx++) {
+        if (zz == z && yy == y && xx >= x) return false;
+        const uint64_t bb = (uint64_t)xx + (uint64_t)m.dims[0] * ((uint64_t)yy + (uint64_t)m.dims[1] * zz);
+        uint32_t lo = m.boff[bb], hi = m.boff[bb + 1];
+        while (lo < hi) {
+          const uint32_t mid = (lo + hi) >> 1;
+          if (m.bitem[mid] < it)
+            lo = mid + 1;
+          else
+            hi = mid;
+        }
+        if (lo < m.boff[bb + 1] && m.bitem[lo] == it) return true;
+      }
+    }
+  return false;
+}
+
 template <bool Fill>
 __device__ void mesh_unit(const FeatArgs& a, uint64_t u, uint32_t A, const ShapeDev& SA, double ra, const VView& va,
                           uint32_t base, int lane, uint32_t lt) {
@@ -616,7 +639,6 @@ __device__ void mesh_unit(const FeatArgs& a, uint64_t u, uint32_t A, const Shape
                                   mk(fmax(hi.x, ghi.x), fmax(hi.y, ghi.y), fmax(hi.z, ghi.z)));
   uint32_t total = 0;
   if (!r0.empty) {
-    const uint32_t noff[3] = {0u, (uint32_t)m.nv, (uint32_t)(m.nv + m.ne)};
     for (int z = r0.lo[2]; z <= r0.hi[2]; z++)
       for (int y = r0.lo[1]; y <= r0.hi[1]; y++)
         for (int x = r0.lo[0]; x <= r0.hi[0]; x++) {
@@ -631,11 +653,8 @@ __device__ void mesh_unit(const FeatArgs& a, uint64_t u, uint32_t A, const Shape
               const uint32_t it = m.bitem[t];
               kind = it >> 30;
               j = it & 0x3fffffffu;
-              const MeshQuery& R = kind == 0 ? r0 : r12;
-              const uint64_t f = m.flo[noff[kind] + j];
-              const int fx = (int)(f & 0x1fffffu), fy = (int)((f >> 21) & 0x1fffffu), fz = (int)(f >> 42);
-              if ((kind != 0 && !in12) || x != max(fx, R.lo[0]) || y != max(fy, R.lo[1]) || z != max(fz, R.lo[2]))
-                kind = 3;  // another bin of the box visits it, or the vertex box does not reach it
+              if ((kind != 0 && !in12) || listed_before(m, kind == 0 ? r0 : r12, x, y, z, it))
+                kind = 3;  // an earlier bin of the box lists it, or the vertex box does not reach it
             }
             uint32_t n = kind < 3 ? mesh_feature_tests<false>(a, m, kind, j, SA, ra, va, gate, A, k, 0) : 0u;
             if (Fill) {
