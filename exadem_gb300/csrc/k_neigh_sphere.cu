@@ -114,7 +114,7 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
       // and face of the sphere's bin that passes its filter; partner sub = feature
       const MeshDev& m = a.mesh[d.mesh];
       mesh_bin_items(m, ri, [&](uint32_t kind, uint32_t j) {
-        if (mesh_filter(m, kind, j, a.skin, ri, radi))
+        if (F32 ? mesh_filter_f32(m, kind, j, a.skin, ri, radi) : mesh_filter(m, kind, j, a.skin, ri, radi))
           emit((uint32_t)k, (uint64_t)k, make_meta(DEM_ITYPE_VERTEX_MESH_VERTEX + kind, 0, 0, 0, false), j << 16);
       });
       continue;

@@ -274,12 +274,13 @@ __device__ __forceinline__ int decide_ve(F3 vi, F3 vf, F3 vs, float R, float rV,
 // The frame (v1, n, v2 = n x v1) is built from the face's first, second and last
 // vertices as in the FP64 code.  Decided when the plane distance and every
 // comparison of the crossing-parity test are beyond their bounds.
-__device__ inline int decide_vf(F3 vi, const FView& vf, const ShapeDev& sf, int face, float lim, float S) {
+// The face is given by its vertex count nf and V(k), its k-th vertex.
+template <class VertF>
+__device__ inline int decide_vf_list(F3 vi, int nf, VertF&& vtx, float lim, float S) {
   const float eta = F32_ETA * S;
-  const int b = sf.fo[face], nf = sf.fo[face + 1] - sf.fo[face];
-  const F3 va = vf[sf.fv[b]];
-  const F3 e1 = vf[sf.fv[b + 1]] - va;
-  const F3 e2 = vf[sf.fv[b + nf - 1]] - va;
+  const F3 va = vtx(0);
+  const F3 e1 = vtx(1) - va;
+  const F3 e2 = vtx(nf - 1) - va;
   const float L1 = flen(e1), L2 = flen(e2);
   if (!(L1 > 0.f)) return DEC_UNDECIDED;
   const F3 v1 = e1 * (1.f / L1);
@@ -303,7 +304,7 @@ __device__ inline int decide_vf(F3 vi, const FView& vf, const ShapeDev& sf, int 
   // D1 = (v_k - vi).v1 + dist n.v1 ; D2 likewise with v2 (n.v1, n.v2 are O(ef))
   const float eD = ef * (2.f * S + dist) + eta + 6.f * F32_U * 2.f * S;
   int odd = 0;
-  F3 pa = vf[sf.fv[b]] - vi;
+  F3 pa = vtx(0) - vi;
   float a1 = fdot(pa, v1), a2 = fdot(pa, v2);
   const int s_first = cmp_gt(a2, 0.f, eD);
   if (s_first == 0) return DEC_UNDECIDED;
@@ -312,12 +313,12 @@ __device__ inline int decide_vf(F3 vi, const FView& vf, const ShapeDev& sf, int 
     float b1, b2;
     int sb;
     if (k + 1 == nf) {
-      const F3 pb = vf[sf.fv[b]] - vi;
+      const F3 pb = vtx(0) - vi;
       b1 = fdot(pb, v1);
       b2 = fdot(pb, v2);
       sb = s_first;
     } else {
-      const F3 pb = vf[sf.fv[b + k + 1]] - vi;
+      const F3 pb = vtx(k + 1) - vi;
       b1 = fdot(pb, v1);
       b2 = fdot(pb, v2);
       sb = cmp_gt(b2, 0.f, eD);
@@ -339,6 +340,11 @@ __device__ inline int decide_vf(F3 vi, const FView& vf, const ShapeDev& sf, int 
     sa = sb;
   }
   return odd ? DEC_TRUE : DEC_FALSE;
+}
+
+__device__ __forceinline__ int decide_vf(F3 vi, const FView& vf, const ShapeDev& sf, int face, float lim, float S) {
+  const int b = sf.fo[face];
+  return decide_vf_list(vi, sf.fo[face + 1] - b, [&](int k) { return vf[sf.fv[b + k]]; }, lim, S);
 }
 
 // filter_ee: closest points of the two lines at s, t strictly inside (0, 1) and
