@@ -32,6 +32,7 @@ struct BPArgs {
   const DriverDev* drv;
   int ndrv;
   const MeshDev* mesh;  // mesh drivers (DriverDev::mesh)
+  int has_mesh;         // a mesh driver is registered: k_count / k_fill run mesh_phase
   double skin;
   double rcut2;
   // FP32 broad phase: cell-relative coordinates and radii, cell sizes, skin
@@ -109,16 +110,7 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
   const int2 dr = a.sv.drange[sys];
   for (int k = dr.x; k < dr.x + dr.y; k++) {
     const DriverDev& d = a.drv[k];
-    if (d.kind == 2) {
-      // detection_sphere_driver (nbh_sphere.hpp:25-86): every mesh vertex, edge
-      // and face of the sphere's bin that passes its filter; partner sub = feature
-      const MeshDev& m = a.mesh[d.mesh];
-      mesh_bin_items(m, ri, [&](uint32_t kind, uint32_t j) {
-        if (F32 ? mesh_filter_f32(m, kind, j, a.skin, ri, radi) : mesh_filter(m, kind, j, a.skin, ri, radi))
-          emit((uint32_t)k, (uint64_t)k, make_meta(DEM_ITYPE_VERTEX_MESH_VERTEX + kind, 0, 0, 0, false), j << 16);
-      });
-      continue;
-    }
+    if (d.kind == 2) continue;  // mesh drivers: mesh_phase
     if (driver_filter(d, radi + a.skin, ri))
       emit((uint32_t)k, (uint64_t)k,
            make_meta(d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER, 0, 0, 0, false), 0u);
@@ -203,15 +195,78 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
   }
 }
 
+// Mesh candidates (detection_sphere_driver, nbh_sphere.hpp:25-86): every mesh
+// vertex, edge and face of the sphere's bin that passes its filter, partner
+// sub = the feature.  A sphere's bin can list hundreds of features (where many
+// triangles meet), so the whole warp serves its spheres one at a time, a lane
+// per bin item; with Fill the passing items go, in bin order, to the start of
+// the sphere's segment [b, e) (the per-sphere sort orders the segment).
+// Returns the lane's own sphere's count.  Every lane of the warp calls it.
+template <bool F32, bool Fill>
+__device__ uint32_t mesh_phase(const BPArgs& a, uint64_t s, bool want, uint32_t b, uint32_t e, IArrays dst) {
+  const int lane = threadIdx.x & 31;
+  uint32_t mine = 0;
+  unsigned todo = __ballot_sync(0xffffffffu, want);
+  while (todo) {
+    const int L = __ffs(todo) - 1;
+    todo &= todo - 1u;
+    const uint32_t sL = (uint32_t)__shfl_sync(0xffffffffu, (unsigned long long)s, L);
+    const uint32_t bL = __shfl_sync(0xffffffffu, b, L), eL = __shfl_sync(0xffffffffu, e, L);
+    const V3 p = mk(a.P.f[RX][sL], a.P.f[RY][sL], a.P.f[RZ][sL]);
+    const double rad = a.P.f[RAD][sL];
+    const int2 dr = a.sv.drange[a.sv.of(sL)];
+    uint32_t n = 0;
+    for (int k = dr.x; k < dr.x + dr.y; k++) {
+      const DriverDev& d = a.drv[k];
+      if (d.kind != 2) continue;
+      const MeshDev& m = a.mesh[d.mesh];
+      const double fx = (p.x - m.lo[0]) * m.inv_bs, fy = (p.y - m.lo[1]) * m.inv_bs, fz = (p.z - m.lo[2]) * m.inv_bs;
+      if (!(fx >= 0.0 && fx < (double)m.dims[0] && fy >= 0.0 && fy < (double)m.dims[1] && fz >= 0.0 &&
+            fz < (double)m.dims[2]))
+        continue;
+      const uint64_t bb = (uint64_t)(int)fx + (uint64_t)m.dims[0] * ((uint64_t)(int)fy + (uint64_t)m.dims[1] * (int)fz);
+      const uint32_t q0 = m.boff[bb], q1 = m.boff[bb + 1];
+      for (uint32_t t0 = q0; t0 < q1; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        bool pass = false;
+        uint32_t kind = 0, j = 0;
+        if (t < q1) {
+          const uint32_t it = m.bitem[t];
+          kind = it >> 30;
+          j = it & 0x3fffffffu;
+          pass = F32 ? mesh_filter_f32(m, kind, j, a.skin, p, rad) : mesh_filter(m, kind, j, a.skin, p, rad);
+        }
+        const unsigned pm = __ballot_sync(0xffffffffu, pass);
+        if (Fill && pass) {
+          const uint32_t w = bL + n + __popc(pm & ((1u << lane) - 1u));
+          if (w < eL) {
+            dst.partner[w] = (uint32_t)k;
+            dst.pid[w] = (uint64_t)k;
+            dst.meta[w] = make_meta(DEM_ITYPE_VERTEX_MESH_VERTEX + kind, 0, 0, 0, false);
+            dst.sub[w] = j << 16;
+          }
+        }
+        n += __popc(pm);
+      }
+    }
+    if (lane == L) mine = n;
+  }
+  __syncwarp();  // the items other lanes wrote are read by the sphere's own lane
+  return mine;
+}
+
 template <bool F32>
 __global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ old_off) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= a.n) return;
-  if (!a.sv.triggered(a.sv.of(s))) {  // slot kept (k_perm_keep): the previous list is copied
+  const bool live = s < a.n;
+  const bool trig = live && a.sv.triggered(a.sv.of(s));
+  uint32_t m = 0;
+  if (a.has_mesh) m = mesh_phase<F32, false>(a, s, trig, 0u, 0u, IArrays{});
+  if (!live) return;
+  if (!trig) {  // slot kept (k_perm_keep): the previous list is copied
     cnt[s] = old_off[s + 1] - old_off[s];
     return;
   }
-  uint32_t m = 0;
   for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t, uint32_t) { m++; });
   cnt[s] = m;
 }
@@ -226,8 +281,12 @@ template <bool F32>
 __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, IArrays old,
                        const uint32_t* __restrict__ old_off, const uint32_t* __restrict__ perm, int have_old) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= a.n) return;
-  const uint32_t b = off[s], e = off[s + 1];
+  const bool live = s < a.n;
+  const uint32_t b = live ? off[s] : 0u, e = live ? off[s + 1] : 0u;
+  const bool trig = live && e <= a.cap && a.sv.triggered(a.sv.of(s));
+  uint32_t nm = 0;
+  if (a.has_mesh) nm = mesh_phase<F32, true>(a, s, trig, b, e, dst);
+  if (!live) return;
   if (e > a.cap) return;
   if (!a.sv.triggered(a.sv.of(s))) {  // slot kept, partners of the same system kept: copy
     const uint32_t ob = old_off[s];
@@ -247,7 +306,7 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
     }
     return;
   }
-  uint32_t w = b;
+  uint32_t w = b + nm;  // mesh items first (mesh_phase)
   for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta, uint32_t sub) {
     if (w < e) {
       dst.partner[w] = q;
@@ -374,6 +433,7 @@ BPArgs make_args(dem_ctx* c) {
   a.drv = c->drv_dev;
   a.ndrv = c->ndrv;
   a.mesh = c->mesh_dev;
+  a.has_mesh = c->meshes.empty() ? 0 : 1;
   a.skin = c->prm.rcut_inc;
   const double nd = 2 * c->rad_max + c->prm.rcut_inc;
   a.rcut2 = nd * nd;
