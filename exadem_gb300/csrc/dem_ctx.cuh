@@ -40,7 +40,6 @@ struct MeshStore {
   int* fv = nullptr;
   uint32_t* boff = nullptr;
   uint32_t* bitem = nullptr;
-  float* fvtx = nullptr;  // 3 nv: FP32 v - lo
   std::vector<double> hx, hy, hz;
   std::vector<int> he, hfo, hfv;
   double bin_rad = -1.0, bin_skin = -1.0;

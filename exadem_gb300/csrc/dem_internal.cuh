@@ -125,11 +125,6 @@ struct MeshDev {
   int dims[3];
   const uint32_t* boff;   // bins + 1
   const uint32_t* bitem;  // boff[bins]
-  // FP32 roundings of v - lo (each in [0, fS]) for the FP32-decided filters
-  const float* fx;
-  const float* fy;
-  const float* fz;
-  float fS;
 };
 struct GridDev {
   int dims[3];

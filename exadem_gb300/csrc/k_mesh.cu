@@ -205,22 +205,8 @@ int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   }
   cudaFree(m.boff);
   cudaFree(m.bitem);
-  cudaFree(m.fvtx);
   m.boff = nullptr;
   m.bitem = nullptr;
-  m.fvtx = nullptr;
-  std::vector<float> fv(3 * (size_t)std::max(nv, 1));
-  for (int k = 0; k < nv; k++) {
-    fv[k] = (float)(m.hx[k] - D.lo[0]);
-    fv[nv + k] = (float)(m.hy[k] - D.lo[1]);
-    fv[2 * (size_t)nv + k] = (float)(m.hz[k] - D.lo[2]);
-  }
-  DEM_CUDA_TRY(c, cudaMalloc(&m.fvtx, fv.size() * 4));
-  DEM_CUDA_TRY(c, cudaMemcpyAsync(m.fvtx, fv.data(), fv.size() * 4, cudaMemcpyHostToDevice, c->stream));
-  D.fx = m.fvtx;
-  D.fy = m.fvtx + nv;
-  D.fz = m.fvtx + 2 * (size_t)nv;
-  D.fS = (float)((double)std::max(dims[0], std::max(dims[1], dims[2])) * bs * 1.001);
   DEM_CUDA_TRY(c, cudaMalloc(&m.boff, (nb + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&m.bitem, std::max<uint64_t>(total, 1) * 4));
   DEM_CUDA_TRY(c, cudaMemcpyAsync(m.boff, cnt.data(), (nb + 1) * 4, cudaMemcpyHostToDevice, c->stream));
@@ -274,7 +260,6 @@ void free_meshes(dem_ctx* c) {
     cudaFree(m.fv);
     cudaFree(m.boff);
     cudaFree(m.bitem);
-    cudaFree(m.fvtx);
   }
   c->meshes.clear();
   cudaFree(c->mesh_dev);

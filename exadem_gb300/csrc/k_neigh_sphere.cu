@@ -226,8 +226,6 @@ __device__ uint32_t mesh_phase(const BPArgs& a, uint64_t s, bool want, uint32_t 
         continue;
       const uint64_t bb = (uint64_t)(int)fx + (uint64_t)m.dims[0] * ((uint64_t)(int)fy + (uint64_t)m.dims[1] * (int)fz);
       const uint32_t q0 = m.boff[bb], q1 = m.boff[bb + 1];
-      const F3 pf = f3((float)(p.x - m.lo[0]), (float)(p.y - m.lo[1]), (float)(p.z - m.lo[2]));
-      const float Rf = (float)(rad + m.r + a.skin);
       for (uint32_t t0 = q0; t0 < q1; t0 += 32) {
         const uint32_t t = t0 + lane;
         bool pass = false;
@@ -236,7 +234,7 @@ __device__ uint32_t mesh_phase(const BPArgs& a, uint64_t s, bool want, uint32_t 
           const uint32_t it = m.bitem[t];
           kind = it >> 30;
           j = it & 0x3fffffffu;
-          pass = F32 ? mesh_filter_f32(m, kind, j, a.skin, p, pf, Rf, rad) : mesh_filter(m, kind, j, a.skin, p, rad);
+          pass = F32 ? mesh_filter_f32(m, kind, j, a.skin, p, rad) : mesh_filter(m, kind, j, a.skin, p, rad);
         }
         const unsigned pm = __ballot_sync(0xffffffffu, pass);
         if (Fill && pass) {

@@ -26,24 +26,29 @@ __device__ inline bool mesh_filter(const MeshDev& m, uint32_t kind, uint32_t j, 
   return vf_core_list(rad + m.r + rV, p, v, m.fv + b, m.fo[j + 1] - b, dist, n);
 }
 
-// mesh_filter decided in FP32 first (poly_f32.cuh).  Inputs are the FP32
-// differences of the stored FP32 offsets v - lo (fx, fy, fz) and the sphere's
-// pf = p - lo rounded to FP32: every coordinate and offset lies in [0, fS],
-// each offset carries u fS and the difference adds u fS, within the 3 u S the
-// decisions assume with S = fS.  A decided test has the FP64 result; an
-// undecided one runs mesh_filter.  R = the filter range as FP32.
-__device__ inline bool mesh_filter_f32(const MeshDev& m, uint32_t kind, uint32_t j, double rV, V3 p, F3 pf, float R,
-                                       double rad) {
-  auto rel = [&](int k) { return f3(m.fx[k] - pf.x, m.fy[k] - pf.y, m.fz[k] - pf.z); };
-  const F3 o = f3(0.f, 0.f, 0.f);
+// mesh_filter decided in FP32 first (poly_f32.cuh): coordinates relative to the
+// sphere centre p, each an FP32 rounding of the FP64 difference (error u S with
+// S a bound of their lengths plus the filter range); a decided test has the
+// FP64 result, an undecided one runs mesh_filter
+__device__ inline bool mesh_filter_f32(const MeshDev& m, uint32_t kind, uint32_t j, double rV, V3 p, double rad) {
+  const VView v = mesh_view(m);
+  auto rel = [&](int k) {
+    const V3 w = v[k];
+    return f3((float)(w.x - p.x), (float)(w.y - p.y), (float)(w.z - p.z));
+  };
+  const float R = (float)(rad + m.r + rV);
   int dec;
   if (kind == 0) {
-    dec = decide_vv(o, rel((int)j), R, m.fS);
+    const F3 a = rel((int)j);
+    dec = decide_vv(f3(0.f, 0.f, 0.f), a, R, flen(a) * 1.000001f + R);
   } else if (kind == 1) {
-    dec = decide_ve(o, rel(m.e[2 * j]), rel(m.e[2 * j + 1]), R, (float)rV, m.fS);
+    const F3 a = rel(m.e[2 * j]), b = rel(m.e[2 * j + 1]);
+    dec = decide_ve(f3(0.f, 0.f, 0.f), a, b, R, (float)rV, fmaxf(flen(a), flen(b)) * 1.000001f + R);
   } else {
     const int b = m.fo[j], nf = m.fo[j + 1] - b;
-    dec = decide_vf_list(o, nf, [&](int k) { return rel(m.fv[b + k]); }, R, m.fS);
+    float S = 0.f;
+    for (int k = 0; k < nf; k++) S = fmaxf(S, flen(rel(m.fv[b + k])));
+    dec = decide_vf_list(f3(0.f, 0.f, 0.f), nf, [&](int k) { return rel(m.fv[b + k]); }, R, S * 1.000001f + R);
   }
   if (dec != DEC_UNDECIDED) return dec == DEC_TRUE;
   return mesh_filter(m, kind, j, rV, p, rad);
