@@ -66,6 +66,8 @@ struct dem_ctx {
   dem::DriverDev* drv_dev = nullptr;
   std::vector<MeshStore> meshes;        // mesh drivers (DriverDev::mesh indexes)
   dem::MeshDev* mesh_dev = nullptr;     // device copy of meshes[k].dev
+  uint32_t* mesh_cnt = nullptr;         // per sphere: mesh candidates of the last count pass
+  uint64_t mesh_cnt_cap = 0;
 
   // systems (batched context); one system spanning prm's domain otherwise
   std::vector<dem_system> systems;   // empty: single system from prm

@@ -235,6 +235,16 @@ int upload_mesh_table(dem_ctx* c) {
 }  // namespace
 
 int ensure_mesh_bins(dem_ctx* c) {
+  if (!c->meshes.empty() && !c->poly && c->mesh_cnt_cap < std::max<uint64_t>(c->pcap, 1)) {
+    if (c->capturing) return c->fail(DEM_ERR_STATE, "mesh count buffer too small inside a graph capture");
+    cudaFree(c->mesh_cnt);
+    c->mesh_cnt = nullptr;
+    c->mesh_cnt_cap = 0;
+    const uint64_t cap = std::max<uint64_t>(c->pcap, 1);
+    DEM_CUDA_TRY(c, cudaMalloc(&c->mesh_cnt, cap * 4));
+    c->mesh_cnt_cap = cap;
+    c->gen++;  // captured kernels hold the old buffer
+  }
   if (!c->meshes.empty() && c->poly && c->prm.learned_sizing)
     return c->fail(DEM_ERR_UNSUPPORTED, "learned record sizing does not bound mesh units: learned_sizing = 0");
   bool changed = false;
@@ -264,6 +274,9 @@ void free_meshes(dem_ctx* c) {
   c->meshes.clear();
   cudaFree(c->mesh_dev);
   c->mesh_dev = nullptr;
+  cudaFree(c->mesh_cnt);
+  c->mesh_cnt = nullptr;
+  c->mesh_cnt_cap = 0;
 }
 }  // namespace dem
 

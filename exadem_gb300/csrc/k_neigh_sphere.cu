@@ -32,7 +32,8 @@ struct BPArgs {
   const DriverDev* drv;
   int ndrv;
   const MeshDev* mesh;  // mesh drivers (DriverDev::mesh)
-  int has_mesh;         // a mesh driver is registered: k_count / k_fill run mesh_phase
+  int has_mesh;         // a mesh driver is registered: k_mesh_count / k_mesh_fill ran
+  const uint32_t* mcnt;  // per sphere: its mesh candidates (k_mesh_count)
   double skin;
   double rcut2;
   // FP32 broad phase: cell-relative coordinates and radii, cell sizes, skin
@@ -255,18 +256,34 @@ __device__ uint32_t mesh_phase(const BPArgs& a, uint64_t s, bool want, uint32_t 
   return mine;
 }
 
+// the mesh candidates of each triggered sphere (kept in their own kernels so the
+// particle-pair passes keep their register budget)
 template <bool F32>
-__global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ old_off) {
+__global__ void k_mesh_count(BPArgs a, uint32_t* __restrict__ mcnt) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = s < a.n;
   const bool trig = live && a.sv.triggered(a.sv.of(s));
-  uint32_t m = 0;
-  if (a.has_mesh) m = mesh_phase<F32, false>(a, s, trig, 0u, 0u, IArrays{});
-  if (!live) return;
-  if (!trig) {  // slot kept (k_perm_keep): the previous list is copied
+  const uint32_t m = mesh_phase<F32, false>(a, s, trig, 0u, 0u, IArrays{});
+  if (live) mcnt[s] = trig ? m : 0u;
+}
+template <bool F32>
+__global__ void k_mesh_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = s < a.n;
+  const uint32_t b = live ? off[s] : 0u, e = live ? off[s + 1] : 0u;
+  const bool trig = live && e <= a.cap && a.sv.triggered(a.sv.of(s));
+  mesh_phase<F32, true>(a, s, trig, b, e, dst);
+}
+
+template <bool F32>
+__global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ old_off) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  if (!a.sv.triggered(a.sv.of(s))) {  // slot kept (k_perm_keep): the previous list is copied
     cnt[s] = old_off[s + 1] - old_off[s];
     return;
   }
+  uint32_t m = a.has_mesh ? a.mcnt[s] : 0u;
   for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t, uint32_t) { m++; });
   cnt[s] = m;
 }
@@ -281,12 +298,8 @@ template <bool F32>
 __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, IArrays old,
                        const uint32_t* __restrict__ old_off, const uint32_t* __restrict__ perm, int have_old) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = s < a.n;
-  const uint32_t b = live ? off[s] : 0u, e = live ? off[s + 1] : 0u;
-  const bool trig = live && e <= a.cap && a.sv.triggered(a.sv.of(s));
-  uint32_t nm = 0;
-  if (a.has_mesh) nm = mesh_phase<F32, true>(a, s, trig, b, e, dst);
-  if (!live) return;
+  if (s >= a.n) return;
+  const uint32_t b = off[s], e = off[s + 1];
   if (e > a.cap) return;
   if (!a.sv.triggered(a.sv.of(s))) {  // slot kept, partners of the same system kept: copy
     const uint32_t ob = old_off[s];
@@ -306,7 +319,7 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
     }
     return;
   }
-  uint32_t w = b + nm;  // mesh items first (mesh_phase)
+  uint32_t w = b + (a.has_mesh ? a.mcnt[s] : 0u);  // mesh items first (k_mesh_fill)
   for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta, uint32_t sub) {
     if (w < e) {
       dst.partner[w] = q;
@@ -434,6 +447,7 @@ BPArgs make_args(dem_ctx* c) {
   a.ndrv = c->ndrv;
   a.mesh = c->mesh_dev;
   a.has_mesh = c->meshes.empty() ? 0 : 1;
+  a.mcnt = c->mesh_cnt;
   a.skin = c->prm.rcut_inc;
   const double nd = 2 * c->rad_max + c->prm.rcut_inc;
   a.rcut2 = nd * nd;
@@ -461,7 +475,15 @@ int refresh_pair_damp(dem_ctx* c) {
 }
 
 int launch_count_sphere(dem_ctx* c) {
-  ProfScope ps(c, K_BROAD_COUNT, c->n ? 1 : 0);
+  const bool mesh = !c->meshes.empty();
+  ProfScope ps(c, K_BROAD_COUNT, c->n ? (mesh ? 2 : 1) : 0);
+  if (c->n && mesh) {
+    if (!c->mesh_cnt) return c->fail(DEM_ERR_STATE, "mesh count buffer missing");
+    if (c->prm.fp32_broad_phase)
+      k_mesh_count<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->mesh_cnt);
+    else
+      k_mesh_count<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->mesh_cnt);
+  }
   if (c->n) {
     if (c->prm.fp32_broad_phase)
       k_count<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt, c->own_off[c->icur]);
@@ -475,7 +497,14 @@ int launch_count_sphere(dem_ctx* c) {
 int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total) {
   (void)total;
   const int nw = 1 - c->icur;
-  ProfScope ps(c, K_BROAD_FILL, c->n ? 1 : 0);
+  const bool mesh = !c->meshes.empty();
+  ProfScope ps(c, K_BROAD_FILL, c->n ? (mesh ? 2 : 1) : 0);
+  if (c->n && mesh) {
+    if (c->prm.fp32_broad_phase)
+      k_mesh_fill<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw]);
+    else
+      k_mesh_fill<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw]);
+  }
   if (c->n) {
     if (c->prm.fp32_broad_phase)
       k_fill<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw], c->I[c->icur],
