@@ -40,6 +40,7 @@ struct MeshStore {
   int* fv = nullptr;
   uint32_t* boff = nullptr;
   uint32_t* bitem = nullptr;
+  float4* fsph = nullptr;
   std::vector<double> hx, hy, hz;
   std::vector<int> he, hfo, hfv;
   double bin_rad = -1.0, bin_skin = -1.0;

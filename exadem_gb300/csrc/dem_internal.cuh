@@ -125,6 +125,10 @@ struct MeshDev {
   int dims[3];
   const uint32_t* boff;   // bins + 1
   const uint32_t* bitem;  // boff[bins]
+  // per feature (vertices, edges, faces): a bounding sphere (x, y, z, r) in FP32
+  // of its vertex, its segment extended by the bins' skin in the line
+  // parameter, or its polygon
+  const float4* fsph;
 };
 struct GridDev {
   int dims[3];

@@ -205,8 +205,33 @@ int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   }
   cudaFree(m.boff);
   cudaFree(m.bitem);
+  cudaFree(m.fsph);
   m.boff = nullptr;
   m.bitem = nullptr;
+  m.fsph = nullptr;
+  // bounding spheres of the features (centre rounded to FP32, radius rounded up)
+  std::vector<float4> sph(box.size());
+  auto put = [&](size_t k, double x, double y, double z, double r) {
+    sph[k] = make_float4((float)x, (float)y, (float)z, (float)(r * (1.0 + 1e-6)) + 1e-6f);
+  };
+  for (int k = 0; k < nv; k++) put(k, m.hx[k], m.hy[k], m.hz[k], 0.0);
+  for (int k = 0; k < ne; k++) {
+    const int a = m.he[2 * k], b = m.he[2 * k + 1];
+    const P3 pa = {m.hx[a], m.hy[a], m.hz[a]}, d = sub3({m.hx[b], m.hy[b], m.hz[b]}, pa);
+    const P3 mid = axpy(pa, 0.5, d);
+    put((size_t)nv + k, mid.x, mid.y, mid.z, (0.5 + skin) * std::sqrt(dot3(d, d)));
+  }
+  for (int f = 0; f < nf; f++) {
+    P3 cgm = {0, 0, 0};
+    const int b0 = m.hfo[f], nvf = m.hfo[f + 1] - b0;
+    for (int q = 0; q < nvf; q++) cgm = axpy(cgm, 1.0 / nvf, {m.hx[m.hfv[b0 + q]], m.hy[m.hfv[b0 + q]], m.hz[m.hfv[b0 + q]]});
+    double r = 0.0;
+    for (int q = 0; q < nvf; q++) r = std::max(r, dist3(cgm, {m.hx[m.hfv[b0 + q]], m.hy[m.hfv[b0 + q]], m.hz[m.hfv[b0 + q]]}));
+    put((size_t)nv + ne + f, cgm.x, cgm.y, cgm.z, r);
+  }
+  DEM_CUDA_TRY(c, cudaMalloc(&m.fsph, sph.size() * sizeof(float4)));
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(m.fsph, sph.data(), sph.size() * sizeof(float4), cudaMemcpyHostToDevice, c->stream));
+  D.fsph = m.fsph;
   DEM_CUDA_TRY(c, cudaMalloc(&m.boff, (nb + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&m.bitem, std::max<uint64_t>(total, 1) * 4));
   DEM_CUDA_TRY(c, cudaMemcpyAsync(m.boff, cnt.data(), (nb + 1) * 4, cudaMemcpyHostToDevice, c->stream));
@@ -270,6 +295,7 @@ void free_meshes(dem_ctx* c) {
     cudaFree(m.fv);
     cudaFree(m.boff);
     cudaFree(m.bitem);
+    cudaFree(m.fsph);
   }
   c->meshes.clear();
   cudaFree(c->mesh_dev);

@@ -539,11 +539,23 @@ __device__ __forceinline__ MeshQuery mesh_query(const MeshDev& m, V3 lo, V3 hi) 
   return q;
 }
 
-// tests of one mesh feature against A's vertices, edges or faces; Write: items at w
-template <bool Write>
+// FP32 context of a mesh unit's decided tests (k_feat_dec): A's vertices
+// relative to its centre cA (the FP32 arrays of the list build), mesh vertices
+// relative to cA rounded to FP32, S a bound of every such |coordinate| for the
+// feature at hand, Rf / rVf the filter range and rVerlet in FP32
+struct MeshDecCtx {
+  FView fa;
+  V3 cA;
+  float S, Rf, rVf;
+};
+
+// tests of one mesh feature against A's vertices, edges or faces; Write: items at
+// w.  Dec: each filter decided in FP32 first (poly_f32.cuh), the FP64 filter
+// where undecided, so the result is the FP64 one
+template <bool Write, bool Dec>
 __device__ uint32_t mesh_feature_tests(const FeatArgs& a, const MeshDev& m, uint32_t kind, uint32_t j,
                                        const ShapeDev& SA, double ra, const VView& va, const OBBd& gate,
-                                       uint32_t A, uint32_t k, uint32_t w) {
+                                       uint32_t A, uint32_t k, uint32_t w, const MeshDecCtx& dc) {
   const VView mv = mesh_view(m);
   const double rV = a.rV, mr = m.r;
   uint32_t n = 0;
@@ -551,10 +563,19 @@ __device__ uint32_t mesh_feature_tests(const FeatArgs& a, const MeshDev& m, uint
     if (Write) write_feature(a, w + n, A, k, (uint64_t)k, type, 0u, (uint32_t)osub, j);
     n++;
   };
+  auto mrel = [&](int q) {
+    const V3 v = mv[q];
+    return f3((float)(v.x - dc.cA.x), (float)(v.y - dc.cA.y), (float)(v.z - dc.cA.z));
+  };
+  // decided result, else the FP64 test
+  auto pass = [&](int dec, auto&& exact) { return Dec && dec != DEC_UNDECIDED ? dec == DEC_TRUE : (bool)exact(); };
   if (kind == 0) {
     const V3 p = mv[j];
+    const F3 pf = Dec ? mrel((int)j) : f3(0.f, 0.f, 0.f);
     for (int i = 0; i < SA.nv; i++)
-      if (filter_vv(rV, va[i], ra, p, mr)) out(DEM_ITYPE_VERTEX_MESH_VERTEX, i);
+      if (pass(Dec ? decide_vv(dc.fa[i], pf, dc.Rf, dc.S) : DEC_UNDECIDED,
+               [&] { return filter_vv(rV, va[i], ra, p, mr); }))
+        out(DEM_ITYPE_VERTEX_MESH_VERTEX, i);
     OBBd ov;
     ov.c = p;
     ov.e1 = mk(1, 0, 0);
@@ -564,22 +585,36 @@ __device__ uint32_t mesh_feature_tests(const FeatArgs& a, const MeshDev& m, uint
     obb_enlarge(ov, mr);
     if (obb_intersect(ov, gate)) {  // obb_v_rshape_j.intersect(obb_i)
       for (int e = 0; e < SA.ne; e++)
-        if (filter_ve(rV, p, mr, va[SA.e[2 * e]], va[SA.e[2 * e + 1]], ra)) out(DEM_ITYPE_MESH_VERTEX_EDGE, e);
+        if (pass(Dec ? decide_ve(pf, dc.fa[SA.e[2 * e]], dc.fa[SA.e[2 * e + 1]], dc.Rf, dc.rVf, dc.S) : DEC_UNDECIDED,
+                 [&] { return filter_ve(rV, p, mr, va[SA.e[2 * e]], va[SA.e[2 * e + 1]], ra); }))
+          out(DEM_ITYPE_MESH_VERTEX_EDGE, e);
       for (int f = 0; f < SA.nf; f++)
-        if (filter_vf(rV, p, mr, va, SA, f, ra)) out(DEM_ITYPE_MESH_VERTEX_FACE, f);
+        if (pass(Dec ? decide_vf(pf, dc.fa, SA, f, dc.Rf, dc.S) : DEC_UNDECIDED,
+                 [&] { return filter_vf(rV, p, mr, va, SA, f, ra); }))
+          out(DEM_ITYPE_MESH_VERTEX_FACE, f);
     }
   } else if (kind == 1) {
     const V3 m0 = mv[m.e[2 * j]], m1 = mv[m.e[2 * j + 1]];
+    const F3 f0 = Dec ? mrel(m.e[2 * j]) : f3(0.f, 0.f, 0.f), f1 = Dec ? mrel(m.e[2 * j + 1]) : f3(0.f, 0.f, 0.f);
     for (int i = 0; i < SA.nv; i++)
-      if (filter_ve(rV, va[i], ra, m0, m1, mr)) out(DEM_ITYPE_VERTEX_MESH_EDGE, i);
+      if (pass(Dec ? decide_ve(dc.fa[i], f0, f1, dc.Rf, dc.rVf, dc.S) : DEC_UNDECIDED,
+               [&] { return filter_ve(rV, va[i], ra, m0, m1, mr); }))
+        out(DEM_ITYPE_VERTEX_MESH_EDGE, i);
     for (int e = 0; e < SA.ne; e++)
-      if (filter_ee(rV, va[SA.e[2 * e]], va[SA.e[2 * e + 1]], ra, m0, m1, mr)) out(DEM_ITYPE_EDGE_MESH_EDGE, e);
+      if (pass(Dec ? decide_ee(dc.fa[SA.e[2 * e]], dc.fa[SA.e[2 * e + 1]], f0, f1, dc.Rf, dc.S) : DEC_UNDECIDED,
+               [&] { return filter_ee(rV, va[SA.e[2 * e]], va[SA.e[2 * e + 1]], ra, m0, m1, mr); }))
+        out(DEM_ITYPE_EDGE_MESH_EDGE, e);
   } else {
     const int b = m.fo[j], nf = m.fo[j + 1] - b;
     for (int i = 0; i < SA.nv; i++) {
-      double dist;
-      V3 nn;
-      if (vf_core_list(ra + mr + rV, va[i], mv, m.fv + b, nf, dist, nn)) out(DEM_ITYPE_VERTEX_MESH_FACE, i);
+      const int dec = Dec ? decide_vf_list(dc.fa[i], nf, [&](int q) { return mrel(m.fv[b + q]); }, dc.Rf, dc.S)
+                          : DEC_UNDECIDED;
+      if (pass(dec, [&] {
+            double dist;
+            V3 nn;
+            return vf_core_list(ra + mr + rV, va[i], mv, m.fv + b, nf, dist, nn);
+          }))
+        out(DEM_ITYPE_VERTEX_MESH_FACE, i);
     }
   }
   return n;
@@ -607,7 +642,7 @@ __device__ inline bool listed_before(const MeshDev& m, const MeshQuery& R, int x
   return false;
 }
 
-template <bool Fill>
+template <bool Fill, bool Dec>
 __device__ void mesh_unit(const FeatArgs& a, uint64_t u, uint32_t A, const ShapeDev& SA, double ra, const VView& va,
                           uint32_t base, int lane, uint32_t lt) {
   const uint32_t k = a.u_partner[u];
@@ -637,6 +672,23 @@ __device__ void mesh_unit(const FeatArgs& a, uint64_t u, uint32_t A, const Shape
   const MeshQuery r12 = mesh_query(m, lo, hi);
   const MeshQuery r0 = mesh_query(m, mk(fmin(lo.x, glo.x), fmin(lo.y, glo.y), fmin(lo.z, glo.z)),
                                   mk(fmax(hi.x, ghi.x), fmax(hi.y, ghi.y), fmax(hi.z, ghi.z)));
+  // reach of A: a feature whose bounding sphere is farther than this from A's
+  // centre passes none of the six filters (A's vertices lie within h maxv of the
+  // centre, its edges extended by rVerlet in their parameter within
+  // h maxv (1 + 2 rVerlet), and every filter range is ra + mr + rVerlet)
+  const float rp = (float)(a.P.f[HOM][A] * SA.maxv * (1.0 + 2.0 * a.rV) + ra + m.r + a.rV);
+  const F3 cA = f3((float)a.P.f[RX][A], (float)a.P.f[RY][A], (float)a.P.f[RZ][A]);
+  const float rpm = rp + 1e-4f * (1.f + fabsf(cA.x) + fabsf(cA.y) + fabsf(cA.z) + rp);
+  const uint32_t noff[3] = {0u, (uint32_t)m.nv, (uint32_t)(m.nv + m.ne)};
+  MeshDecCtx dc;
+  if (Dec) {
+    const uint64_t oA = (uint64_t)A * a.MV;
+    dc.fa = FView{a.fvx + oA, a.fvy + oA, a.fvz + oA, f3(0.f, 0.f, 0.f)};
+    dc.cA = mk(a.P.f[RX][A], a.P.f[RY][A], a.P.f[RZ][A]);
+    dc.Rf = (float)(ra + m.r + a.rV);
+    dc.rVf = (float)a.rV;
+  }
+  const float hm = (float)(a.P.f[HOM][A] * SA.maxv);
   uint32_t total = 0;
   if (!r0.empty) {
     for (int z = r0.lo[2]; z <= r0.hi[2]; z++)
@@ -649,21 +701,31 @@ __device__ void mesh_unit(const FeatArgs& a, uint64_t u, uint32_t A, const Shape
           for (uint32_t t0 = q0; t0 < q1; t0 += 32) {
             const uint32_t t = t0 + lane;
             uint32_t kind = 3, j = 0;
+            float Sitem = 0.f;
             if (t < q1) {
               const uint32_t it = m.bitem[t];
               kind = it >> 30;
               j = it & 0x3fffffffu;
-              if ((kind != 0 && !in12) || listed_before(m, kind == 0 ? r0 : r12, x, y, z, it))
+              const float4 sp = m.fsph[noff[kind] + j];
+              const float dx = sp.x - cA.x, dy = sp.y - cA.y, dz = sp.z - cA.z, lim = sp.w + rpm;
+              const float d2 = dx * dx + dy * dy + dz * dz;
+              // bound of |coordinate| relative to A's centre: the feature's vertices, A's vertices
+              Sitem = (sqrtf(d2) + sp.w + hm) * 1.001f + dc.Rf + 1e-3f + 1e-6f * (fabsf(cA.x) + fabsf(cA.y) + fabsf(cA.z));
+              if (d2 > lim * lim)
+                kind = 3;  // out of A's reach
+              else if ((kind != 0 && !in12) || listed_before(m, kind == 0 ? r0 : r12, x, y, z, it))
                 kind = 3;  // an earlier bin of the box lists it, or the vertex box does not reach it
             }
-            uint32_t n = kind < 3 ? mesh_feature_tests<false>(a, m, kind, j, SA, ra, va, gate, A, k, 0) : 0u;
+            MeshDecCtx dci = dc;
+            dci.S = Sitem;
+            uint32_t n = kind < 3 ? mesh_feature_tests<false, Dec>(a, m, kind, j, SA, ra, va, gate, A, k, 0, dci) : 0u;
             if (Fill) {
               uint32_t pre = n;  // inclusive warp scan of the per-lane counts
               for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t v = __shfl_up_sync(0xffffffffu, pre, o);
                 if (lane >= o) pre += v;
               }
-              if (n) mesh_feature_tests<true>(a, m, kind, j, SA, ra, va, gate, A, k, base + total + pre - n);
+              if (n) mesh_feature_tests<true, Dec>(a, m, kind, j, SA, ra, va, gate, A, k, base + total + pre - n, dci);
               total += __shfl_sync(0xffffffffu, pre, 31);
             } else {
               for (int o = 16; o; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
@@ -682,10 +744,7 @@ __device__ __forceinline__ void driver_unit(const FeatArgs& a, uint64_t u, uint3
                                             const VView& va, uint32_t base, int lane, uint32_t lt) {
   const uint32_t k = a.u_partner[u];
   const DriverDev& d = a.drv[k];
-  if (d.kind == 2) {
-    mesh_unit<Fill>(a, u, A, SA, ra, va, base, lane, lt);
-    return;
-  }
+  if (d.kind == 2) return;  // mesh units: k_mesh_units
   const uint32_t type = d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER;
   const bool keep = lane < SA.nv && driver_reach(d, a.rV + ra, va[lane]);
   const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -693,6 +752,24 @@ __device__ __forceinline__ void driver_unit(const FeatArgs& a, uint64_t u, uint3
     if (keep) write_feature(a, base + __popc(m & lt), A, k, a.u_pid[u], type, 0, lane, 0xffffu);
   } else if (lane == 0) {
     a.fcnt[u] = __popc(m);
+  }
+}
+
+// One warp per mesh unit (the other units are skipped): kept out of k_feat /
+// k_feat_dec so that the particle-pair enumeration keeps its register budget.
+// Fill = false: counts into fcnt; Fill = true: writes at foff.  Dec: the
+// FP32-decided tests (the FP32 broad phase).
+template <bool Fill, bool Dec>
+__global__ void __launch_bounds__(PT) k_mesh_units(FeatArgs a) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
+  for (uint64_t u = warp; u < a.nu; u += nwarps) {
+    if (!a.u_kind[u] || !a.pass[u] || a.drv[a.u_partner[u]].kind != 2) continue;
+    const uint32_t A = a.u_owner[u];
+    const ShapeDev& SA = a.shapes[a.P.type[A]];
+    const double ra = SA.r * a.P.f[HOM][A];
+    mesh_unit<Fill, Dec>(a, u, A, SA, ra, vview(a, A), Fill ? a.foff[u] : 0u, lane, 0u);
   }
 }
 
@@ -1661,11 +1738,16 @@ int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total) {
   FeatArgs a = make_fargs(c, nu);
   const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
   {
-    ProfScope ps(c, K_BROAD_COUNT, nu ? 1 : 0);
+    const bool mesh = !c->meshes.empty();
+    ProfScope ps(c, K_BROAD_COUNT, nu ? (mesh ? 2 : 1) : 0);
     if (nu && c->prm.fp32_broad_phase)
       k_feat_dec<false><<<blocks, PT, 0, c->stream>>>(a);
     else if (nu)
       k_feat<false><<<blocks, PT, 0, c->stream>>>(a);
+    if (nu && mesh && c->prm.fp32_broad_phase)
+      k_mesh_units<false, true><<<blocks, PT, 0, c->stream>>>(a);
+    else if (nu && mesh)
+      k_mesh_units<false, false><<<blocks, PT, 0, c->stream>>>(a);
   }
   int rc = scan_exclusive_u32(c, c->f_cnt, c->f_off, nu);
   if (rc) return rc;
@@ -1687,12 +1769,17 @@ int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total) {
 int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
   FeatArgs a = make_fargs(c, nu);
   const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
-  ProfScope ps(c, K_BROAD_FILL, 2);
+  const bool mesh = !c->meshes.empty();
+  ProfScope ps(c, K_BROAD_FILL, mesh ? 4 : 2);
   if (nu && c->prm.fp32_broad_phase)
     k_feat_dec<true><<<blocks, PT, 0, c->stream>>>(a);
   else if (nu)
     k_feat<true><<<blocks, PT, 0, c->stream>>>(a);
-  if (nu && !c->meshes.empty())
+  if (nu && mesh && c->prm.fp32_broad_phase)
+    k_mesh_units<true, true><<<blocks, PT, 0, c->stream>>>(a);
+  else if (nu && mesh)
+    k_mesh_units<true, false><<<blocks, PT, 0, c->stream>>>(a);
+  if (nu && mesh)
     k_mesh_unit_sort<<<grid_for(nu, 128), 128, 0, c->stream>>>(nu, c->u_kind, c->u_partner, c->drv_dev, c->f_off,
                                                               a.dst);
   k_own_from_units<<<grid_for(c->n + 1, 256), 256, 0, c->stream>>>(c->n, c->u_off, c->f_off, c->own_off[1 - c->icur]);
