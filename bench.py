@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--n", type=int, default=None, help="particle count (default: the workload's)")
     ap.add_argument("--workload", default="spheres",
-                    choices=["spheres", "polyhedra", "polyhedra_dense", "drums", "mixer"],
+                    choices=["spheres", "polyhedra", "polyhedra_dense", "drums", "mixer", "polyhedra_mesh"],
                     help="spheres: 2M spheres on a floor (headline); polyhedra: 200k polyhedra deposition; "
                          "polyhedra_dense: polyhedra on a dense lattice; drums: 256 rotating drums batched; "
                          "mixer: 50k spheres falling into a mesh (STL) mixer")
@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--epochs", type=int, default=20, help="learned: training epochs")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rebuild-ms", type=int, default=0,
+                    help="after the run, time this many explicit list rebuilds (CUDA events on the library's "
+                         "stream); with mesh drivers also on the same particles without the meshes")
     return ap.parse_args()
 
 
@@ -189,6 +192,9 @@ def _workload(args):
         return W.drums_batch(nsys=args.systems, nmax=args.n or 200_000, **flags)
     if args.workload == "mixer":
         return W.spheres_mixer(n=args.n, **flags)
+    if args.workload == "polyhedra_mesh":
+        side = round(((args.n or 4800) / 3) ** 0.5)
+        return W.polyhedra_mesh_terrain(nx=side, ny=side, nz=3, amp=0.5, waves=6, m=60, **flags)
     return W.spheres_floor(n=args.n or 2_000_000, **flags)
 
 
@@ -231,6 +237,8 @@ WORKLOAD_DESC = {
                        "orientations, Hooke kn=1e4, dt=1e-4",
     "drums": "drums_batch: 256 rotating drums (spheres r~U[0.45,0.55], counts log-uniform in [2e3, 2e5], "
              "30% fill, 2 rad/s, periodic along the axis), Hooke kn=1e4 kt=8e3 mu=0.4, dt=5e-4",
+    "polyhedra_mesh": "polyhedra_mesh_terrain: 4800 cubes/tetrahedra/octahedra (40 x 40 x 3 lattice) falling on "
+                      "a 7200-triangle terrain mesh (Minkowski 0.02) inside four walls, Hooke kn=1e4, dt=5e-4",
     "mixer": "spheres_mixer: 50,304 spheres r=2 (SC lattice 4.1 in a cylinder r=92) falling into a mesh mixer "
              "(wall, bottom, 4 blades: 2064 triangles, Minkowski 0.1), Hooke kn=1e3 kt=1e3 mu=0.5, dt=1e-3",
 }
@@ -361,6 +369,36 @@ def train_learned(args):
                     "label_means": [round(v, 4) for v in y.float().mean(0).tolist()]}
 
 
+def rebuild_timing(args, w, s):
+    """Time of one explicit list rebuild in the state the run ended in; with mesh
+    drivers, also on the same particles in a system without the meshes."""
+    import numpy as np
+    import torch
+
+    def timed(sys_):
+        ext = torch.cuda.ExternalStream(sys_.stream_handle())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(args.rebuild_ms):
+            sys_.update_particle_neighbors()
+        e1.record(ext)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / args.rebuild_ms
+
+    out = {"rebuilds_timed": args.rebuild_ms, "rebuild_ms": timed(s)}
+    if getattr(w, "meshes", None):
+        p = s.particles(sort_by_id=True)
+        w2 = workload(args)
+        w2.meshes = []
+        w2.particles = {k: np.ascontiguousarray(v) for k, v in p.items() if k in w2.particles}
+        s2 = w2.build()
+        s2.first_iteration()
+        out["rebuild_ms_without_meshes"] = timed(s2)
+        s2.close()
+    return out
+
+
 def run_native(args, rank, world, local, dist):
     import numpy as np
     import torch
@@ -461,6 +499,7 @@ def run_native(args, rank, world, local, dist):
               for k, v in prof.items() if v["total_ms"] > 0}
     state = s.simulation_state()
     mul_mode = s.mul_mode()
+    rebuild = rebuild_timing(args, w, s) if args.rebuild_ms > 0 else None
     s.close()
 
     # end to end through the C ABI from pinned host buffers
@@ -529,6 +568,7 @@ def run_native(args, rank, world, local, dist):
         "rebuilds_in_timed_region": rebuilds, "gpu_launches": launches,
         "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu,
         "state_after": {"n_interactions": state["n_interactions"], "n_active": state["n_active_interactions"]},
+        "rebuild_timing": rebuild,
     }
     if rank == 0:
         print(json.dumps(line))
