@@ -148,7 +148,7 @@ int build_bins(dem_ctx* c, MeshStore& m, double rad, double skin) {
   for (int d = 0; d < 3; d++) D.lo[d] = all.lo[d];
   D.inv_bs = 1.0 / bs;
   for (int d = 0; d < 3; d++) D.dims[d] = dims[d];
-  // the bin range of a box: the index formula of mesh_bin_items, monotone in the coordinate
+  // the bin range of a box: the index formula of mesh_bin_of (mesh_core.cuh), monotone in the coordinate
   auto index = [&](double x, int d) {
     const double f = (x - D.lo[d]) * D.inv_bs;
     return std::min(std::max((int)std::floor(f), 0), dims[d] - 1);

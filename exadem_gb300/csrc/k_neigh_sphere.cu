@@ -221,11 +221,8 @@ __device__ uint32_t mesh_phase(const BPArgs& a, uint64_t s, bool want, uint32_t 
       const DriverDev& d = a.drv[k];
       if (d.kind != 2) continue;
       const MeshDev& m = a.mesh[d.mesh];
-      const double fx = (p.x - m.lo[0]) * m.inv_bs, fy = (p.y - m.lo[1]) * m.inv_bs, fz = (p.z - m.lo[2]) * m.inv_bs;
-      if (!(fx >= 0.0 && fx < (double)m.dims[0] && fy >= 0.0 && fy < (double)m.dims[1] && fz >= 0.0 &&
-            fz < (double)m.dims[2]))
-        continue;
-      const uint64_t bb = (uint64_t)(int)fx + (uint64_t)m.dims[0] * ((uint64_t)(int)fy + (uint64_t)m.dims[1] * (int)fz);
+      uint64_t bb;
+      if (!mesh_bin_of(m, p, bb)) continue;
       const uint32_t q0 = m.boff[bb], q1 = m.boff[bb + 1];
       for (uint32_t t0 = q0; t0 < q1; t0 += 32) {
         const uint32_t t = t0 + lane;

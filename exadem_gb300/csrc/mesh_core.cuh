@@ -96,20 +96,16 @@ __device__ inline DetD poly_mesh_detect(const MeshDev& m, uint32_t type, uint32_
   }
 }
 
-// the features listed in the bin of p (none outside the bin grid)
-template <class F>
-__device__ inline void mesh_bin_items(const MeshDev& m, V3 p, F&& f) {
+// the bin of p: false outside the bin grid (no feature can pass there)
+__device__ inline bool mesh_bin_of(const MeshDev& m, V3 p, uint64_t& b) {
   const double fx = (p.x - m.lo[0]) * m.inv_bs;
   const double fy = (p.y - m.lo[1]) * m.inv_bs;
   const double fz = (p.z - m.lo[2]) * m.inv_bs;
   if (!(fx >= 0.0 && fx < (double)m.dims[0] && fy >= 0.0 && fy < (double)m.dims[1] && fz >= 0.0 &&
         fz < (double)m.dims[2]))
-    return;
-  const uint64_t b = (uint64_t)(int)fx + (uint64_t)m.dims[0] * ((uint64_t)(int)fy + (uint64_t)m.dims[1] * (int)fz);
-  for (uint32_t q = m.boff[b]; q < m.boff[b + 1]; q++) {
-    const uint32_t it = m.bitem[q];
-    f(it >> 30, it & 0x3fffffffu);
-  }
+    return false;
+  b = (uint64_t)(int)fx + (uint64_t)m.dims[0] * ((uint64_t)(int)fy + (uint64_t)m.dims[1] * (int)fz);
+  return true;
 }
 
 }  // namespace dem
