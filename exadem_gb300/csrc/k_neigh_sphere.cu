@@ -253,23 +253,26 @@ __device__ uint32_t mesh_phase(const BPArgs& a, uint64_t s, bool want, uint32_t 
   return mine;
 }
 
-// the mesh candidates of each triggered sphere (kept in their own kernels so the
-// particle-pair passes keep their register budget)
+// the mesh candidates of each triggered sphere, one warp per sphere (lane 0
+// asks mesh_phase for its sphere): a sphere whose bin lists hundreds of
+// features gets a warp of its own.  Kept out of k_count / k_fill so the
+// particle-pair passes keep their register budget.
 template <bool F32>
 __global__ void k_mesh_count(BPArgs a, uint32_t* __restrict__ mcnt) {
-  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = s < a.n;
-  const bool trig = live && a.sv.triggered(a.sv.of(s));
-  const uint32_t m = mesh_phase<F32, false>(a, s, trig, 0u, 0u, IArrays{});
-  if (live) mcnt[s] = trig ? m : 0u;
+  const uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= a.n) return;  // the whole warp
+  const bool lead = (threadIdx.x & 31) == 0;
+  const bool trig = a.sv.triggered(a.sv.of(s));
+  const uint32_t m = mesh_phase<F32, false>(a, s, lead && trig, 0u, 0u, IArrays{});
+  if (lead) mcnt[s] = trig ? m : 0u;
 }
 template <bool F32>
 __global__ void k_mesh_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst) {
-  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = s < a.n;
-  const uint32_t b = live ? off[s] : 0u, e = live ? off[s + 1] : 0u;
-  const bool trig = live && e <= a.cap && a.sv.triggered(a.sv.of(s));
-  mesh_phase<F32, true>(a, s, trig, b, e, dst);
+  const uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (s >= a.n) return;  // the whole warp
+  const uint32_t b = off[s], e = off[s + 1];
+  const bool trig = e <= a.cap && a.sv.triggered(a.sv.of(s));
+  mesh_phase<F32, true>(a, s, (threadIdx.x & 31) == 0 && trig, b, e, dst);
 }
 
 template <bool F32>
@@ -477,9 +480,9 @@ int launch_count_sphere(dem_ctx* c) {
   if (c->n && mesh) {
     if (!c->mesh_cnt) return c->fail(DEM_ERR_STATE, "mesh count buffer missing");
     if (c->prm.fp32_broad_phase)
-      k_mesh_count<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->mesh_cnt);
+      k_mesh_count<true><<<grid_for(c->n * 32, 128), 128, 0, c->stream>>>(make_args(c), c->mesh_cnt);
     else
-      k_mesh_count<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->mesh_cnt);
+      k_mesh_count<false><<<grid_for(c->n * 32, 128), 128, 0, c->stream>>>(make_args(c), c->mesh_cnt);
   }
   if (c->n) {
     if (c->prm.fp32_broad_phase)
@@ -498,9 +501,9 @@ int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total) {
   ProfScope ps(c, K_BROAD_FILL, c->n ? (mesh ? 2 : 1) : 0);
   if (c->n && mesh) {
     if (c->prm.fp32_broad_phase)
-      k_mesh_fill<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw]);
+      k_mesh_fill<true><<<grid_for(c->n * 32, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw]);
     else
-      k_mesh_fill<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw]);
+      k_mesh_fill<false><<<grid_for(c->n * 32, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw]);
   }
   if (c->n) {
     if (c->prm.fp32_broad_phase)
