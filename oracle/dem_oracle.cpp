@@ -7,8 +7,11 @@
  *
  * It restates, in plain sequential C++ (OpenMP only over independent items,
  * so results do not depend on the thread count), the arithmetic of the
- * reference CPU path for spheres.  Each function cites the reference lines it
- * follows (paths relative to the exaDEM source tree).  Two external libraries
+ * reference CPU path: spheres and polyhedra, surfaces, cylinders and
+ * stationary mesh drivers (the mesh candidates brute force over every feature),
+ * the Hooke / cohesive / DMT laws, multi-material tables, the contact state
+ * and the stress tensor.  Each function cites the reference lines it follows
+ * (paths relative to the exaDEM source tree).  Two external libraries
  * of the reference are not vendored and are restated from their mathematics:
  *   - onika (Collab4exaNBody/onika, unpinned HEAD): Vec3d operators
  *     (component-wise), dot/cross/norm, Quaternion*Vec3d rotation,
@@ -22,7 +25,8 @@
  *     and particle_displ_over (|r - r_backup|^2 >= max_displ^2).
  * Parity status: the reference itself cannot be compiled here (exaNBody, onika,
  * MPI and yaml-cpp are absent) and ships no golden values for this path, so
- * this restatement is pinned only by analytic known-answer tests.
+ * this restatement is pinned only by analytic known-answer tests (parity
+ * unpinned against the reference itself).
  *
  * Canonical summation order (the reference sums with unordered atomics,
  * contact_sphere.hpp:183-196): for each particle, f = g*m, then the
