@@ -1,7 +1,8 @@
 """The learned part (include/dem_learned.h): per-pair feature-contact counts
 predicted by a 16-64-64-4 MLP trained on the GPU by the library's own BF16 /
 FP32 kernels, used to size the polyhedron feature records and to order the
-candidate pairs into warp bins.  The exact enumeration stays the judge.
+candidate pairs into warp bins.  The exact enumeration still decides every
+interaction.
 
 Device buffers are torch CUDA tensors (plain device memory); the arithmetic is
 the library's."""

@@ -2,7 +2,7 @@
  * dem_learned.h -- the learned part: per-pair feature-contact counts predicted
  * by a small MLP, used to size the polyhedron feature buffers and to order the
  * candidate pairs into warp bins.  No reference counterpart.  The exact
- * enumeration stays the judge: a pair whose features do not fit the predicted
+ * enumeration still decides every interaction: a pair whose features do not fit the predicted
  * record is enumerated again exactly, so the interaction list is unchanged.
  *
  * Network: 16 -> 64 (ReLU) -> 64 (ReLU) -> 4, BF16 weights and inputs, FP32
