@@ -22,6 +22,12 @@ def test_headers_declare_functions():
     assert "dem_ctx_create" in names and "dem_step" in names and len(names) >= 20
 
 
+def test_python_binding_declares_every_symbol():
+    from exadem_gb300 import _abi as A
+
+    assert set(A.EXPORTED) == set(declared_functions())
+
+
 def test_library_exports_every_declared_symbol(native_lib):
     lib = ctypes.CDLL(str(ROOT / "exadem_gb300" / "libexadem_gb300.so"))
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
