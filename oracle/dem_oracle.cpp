@@ -1099,21 +1099,46 @@ void poly_mesh_candidates(const Oracle& o, size_t k, size_t a, double rV, std::v
     lst.push_back(it);
   };
   const int mnv = (int)m.w.size(), mne = (int)m.e.size() / 2, mnf = (int)m.f.size();
+  // features out of the particle's reach pass none of the six filters: its
+  // vertices lie within h max|v0| of its centre, its edges extended by rVerlet
+  // in their parameter within h max|v0| (1 + 2 rVerlet), every filter range is
+  // ra + mr + rVerlet, and a feature lies within its bounding sphere (an edge's
+  // extended by rVerlet in its parameter); skipping them saves time only
+  const V3 c = pos(o, a);
+  double vmax = 0.0;
+  for (const V3& v : sa.v) vmax = std::max(vmax, norm(v));
+  const double reach = o.hom[a] * vmax * (1.0 + 2.0 * rV) + ra + m.r + rV;
+  const double slack = 1e-9 * (1.0 + std::fabs(c.x) + std::fabs(c.y) + std::fabs(c.z) + reach);
+  std::vector<char> nv_(mnv), ne_(mne), nf_(mnf);
+  for (int j = 0; j < mnv; j++) nv_[j] = norm(m.w[j] - c) <= reach + slack;
+  for (int j = 0; j < mne; j++) {
+    const V3 p0 = m.w[m.e[2 * j]], d = m.w[m.e[2 * j + 1]] - p0;
+    ne_[j] = norm(p0 + 0.5 * d - c) <= reach + (0.5 + rV) * norm(d) + slack;
+  }
+  for (int j = 0; j < mnf; j++) {
+    V3 g = {0, 0, 0};
+    for (int q : m.f[j]) g = g + m.w[q] * (1.0 / (double)m.f[j].size());
+    double rf = 0.0;
+    for (int q : m.f[j]) rf = std::max(rf, norm(m.w[q] - g));
+    nf_[j] = norm(g - c) <= reach + rf + slack;
+  }
   for (int i = 0; i < sa.nv(); i++) {
     for (int j = 0; j < mnv; j++)
-      if (filter_vv(rV, va[i], ra, m.w[j], m.r)) add(DEM_ITYPE_VERTEX_MESH_VERTEX, i, j);
+      if (nv_[j] && filter_vv(rV, va[i], ra, m.w[j], m.r)) add(DEM_ITYPE_VERTEX_MESH_VERTEX, i, j);
     for (int j = 0; j < mne; j++)
-      if (filter_ve(rV, va[i], ra, m.w[m.e[2 * j]], m.w[m.e[2 * j + 1]], m.r)) add(DEM_ITYPE_VERTEX_MESH_EDGE, i, j);
+      if (ne_[j] && filter_ve(rV, va[i], ra, m.w[m.e[2 * j]], m.w[m.e[2 * j + 1]], m.r))
+        add(DEM_ITYPE_VERTEX_MESH_EDGE, i, j);
     for (int j = 0; j < mnf; j++)
-      if (filter_vf(rV, va[i], ra, m.w, m.f[j], m.r)) add(DEM_ITYPE_VERTEX_MESH_FACE, i, j);
+      if (nf_[j] && filter_vf(rV, va[i], ra, m.w, m.f[j], m.r)) add(DEM_ITYPE_VERTEX_MESH_FACE, i, j);
   }
   for (int e = 0; e < sa.ne(); e++)
     for (int j = 0; j < mne; j++)
-      if (filter_ee(rV, va[sa.e[2 * e]], va[sa.e[2 * e + 1]], ra, m.w[m.e[2 * j]], m.w[m.e[2 * j + 1]], m.r))
+      if (ne_[j] && filter_ee(rV, va[sa.e[2 * e]], va[sa.e[2 * e + 1]], ra, m.w[m.e[2 * j]], m.w[m.e[2 * j + 1]], m.r))
         add(DEM_ITYPE_EDGE_MESH_EDGE, e, j);
   OBBr gate = compute_obb(sa.obb, pos(o, a), {o.qw[a], o.qx[a], o.qy[a], o.qz[a]}, 1.0);
   obb_enlarge(gate, rV);
   for (int j = 0; j < mnv; j++) {
+    if (!nv_[j]) continue;
     OBBr ov{};
     ov.c = m.w[j];
     ov.e1 = {1, 0, 0};
