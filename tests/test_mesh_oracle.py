@@ -134,3 +134,29 @@ def test_mesh_candidates_cover_the_touching_features():
     assert mesh_items.sum() > 0
     assert ((cs["dn"] < 0) & mesh_items).sum() > 0
     assert np.all(it["partner_id"][mesh_items] == 4)  # the driver after the four walls
+
+
+def test_stl_file_to_simulation(tmp_path):
+    """register_stl_mesh from a file: the STL read, converted and rescaled
+    (float32 vertices, scale 2) gives the same run as the same arrays given
+    directly."""
+    tri = W.terrain_triangles(8.0, 8, 0.4, 1, 0.0)
+    path = str(tmp_path / "terrain.stl")
+    stl.write_stl_binary(path, tri)
+    shp = stl.load_stl_mesh(path, True, scale=2.0)
+    direct = stl.rescale(stl.build_shape(list(tri.astype(np.float32).astype(np.float64))), 2.0)
+    assert np.array_equal(shp["vertices"], direct["vertices"])
+    runs = []
+    for sh in (shp, direct):
+        w = W.spheres_mesh_terrain(n=400, side=16.0, seed=61)
+        w.meshes = [dict(w.meshes[0], vertices=sh["vertices"], edges=sh["edges"], faces=sh["faces"])]
+        s = w.build(oracle_system)
+        s.first_iteration()
+        s.step(300)
+        runs.append((s.interactions(), s.particles(sort_by_id=True)))
+    (la, pa), (lb, pb) = runs
+    assert np.sum((la["type"] >= 7) & (la["type"] <= 9)) > 0
+    for k in la:
+        assert np.array_equal(la[k], lb[k]), k
+    for k in ("rx", "ry", "rz", "vx", "vy", "vz"):
+        assert np.array_equal(pa[k], pb[k]), k
