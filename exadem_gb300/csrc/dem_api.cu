@@ -852,6 +852,15 @@ int dem_register_surface(dem_ctx* c, const dem_surface* s) {
   const bool vrot0 = s->vrot[0] == 0.0 && s->vrot[1] == 0.0 && s->vrot[2] == 0.0;
   const bool c0 = s->center[0] == 0.0 && s->center[1] == 0.0 && s->center[2] == 0.0;
   for (int k = 0; k < 3; k++) d.center[k] = (vrot0 && c0) ? d.offset * d.normal[k] : s->center[k];
+  // Surface::initialize replaces a centre off the plane on the normal's side (surface.hpp:166-173)
+  double off = 0.0, back = 0.0;
+  off = (d.center[0] - d.center_proj[0]) * d.normal[0] + (d.center[1] - d.center_proj[1]) * d.normal[1] +
+        (d.center[2] - d.center_proj[2]) * d.normal[2];
+  if (off >= 1e-14) {
+    back = (d.center_proj[0] - d.center[0]) * d.normal[0] + (d.center_proj[1] - d.center[1]) * d.normal[1] +
+           (d.center_proj[2] - d.center[2]) * d.normal[2];
+    for (int k = 0; k < 3; k++) d.center[k] = back * d.normal[k] + d.center_proj[k];
+  }
   return add_driver(c, d);
 }
 

@@ -328,7 +328,8 @@ def build_obb(vertices, radius):
     mu = [0.0, 0.0, 0.0]
     for v in vs:
         mu = [mu[0] + v[0], mu[1] + v[1], mu[2] + v[2]]
-    mu = [mu[0] / n, mu[1] / n, mu[2] / n]
+    inv_n = 1.0 / float(n)  # vec3::operator/= multiplies by the reciprocal (type/vec3.hpp:179-185)
+    mu = [mu[0] * inv_n, mu[1] * inv_n, mu[2] * inv_n]
     cxx = cxy = cxz = cyy = cyz = czz = 0.0
     for p in vs:
         cxx += p[0] * p[0] - mu[0] * mu[0]

@@ -3,8 +3,9 @@
 Produces ``oracle/libdem_oracle.so`` from ``oracle/dem_oracle.cpp`` with g++,
 OpenMP and no FP contraction (``-ffp-contract=off``; GCC contracts to FMA by
 default on aarch64), so its arithmetic is plain IEEE double in source order.
-The reference exaDEM itself cannot be compiled here (it needs exaNBody, onika,
-MPI and yaml-cpp, none of which is available), so there is no ``oracle/_ref``.
+exaDEM's own hot-path headers are compiled separately, against stand-ins for
+its missing dependencies, by ``oracle/ref_build.py`` (``oracle/_ref``); the tests
+compare the two libraries function by function.
 """
 from __future__ import annotations
 

@@ -23,10 +23,23 @@
  *     src/grid/chunk_neighbors_contact.cpp:45-57), periodic ghost images,
  *     PushVec3{First,Second}OrderFunctor (x += v*dt + a*dt^2/2, v += a*dt/2)
  *     and particle_displ_over (|r - r_backup|^2 >= max_displ^2).
- * Parity status: the reference itself cannot be compiled here (exaNBody, onika,
- * MPI and yaml-cpp are absent) and ships no golden values for this path, so
- * this restatement is pinned only by analytic known-answer tests (parity
- * unpinned against the reference itself).
+ * Parity status: exaDEM as a whole cannot be built here (exaNBody, onika, MPI
+ * and yaml-cpp are absent), but its hot-path arithmetic lives in headers that
+ * compile on the host against small stand-ins for those libraries
+ * (oracle/ref_harness.cpp, oracle/ref_shim/, built by oracle/ref_build.py).
+ * The oracle_unit_* entry points at the end of this file run the functions
+ * below on rows of inputs; tests/test_oracle_vs_ref.py compares them with
+ * exaDEM's own functions bit for bit (contact_force_core for the three laws,
+ * compute_moments, the damping and effective mass, the vertex-vertex, -edge,
+ * -face and edge-edge filters and detections, OBB intersect / compute_obb /
+ * enlarge, shape::get_vertex, the rotation functors of the prolog and epilog,
+ * InteractionPair ordering, the Surface and Cylinder drivers), and
+ * tests/test_oracle_golden.py repeats it on stored exaDEM outputs.  Still
+ * restated without a compiled counterpart: the neighbour search and periodic
+ * images (exaNBody), the translation pushes (exaNBody functors), the loops of
+ * nbh_sphere / nbh_polyhedron that decide which features are tested (grid and
+ * cell machinery), and the Vec3d / Quaternion operators themselves (onika,
+ * restated identically in the stand-ins).
  *
  * Canonical summation order (the reference sums with unordered atomics,
  * contact_sphere.hpp:183-196): for each particle, f = g*m, then the
@@ -252,6 +265,34 @@ bool cylinder_detect(const Cylinder& c, double rcut, const V3& pi, double& dn, V
   return true;
 }
 
+// register_surface: the YAML decoder's default centre (surface.hpp:68-84), then
+// Surface::initialize (surface.hpp:145-175) for a stationary surface.
+Surface surface_from(const dem_surface* s) {
+  Surface w{};
+  w.offset = s->offset;
+  w.normal = {s->normal[0], s->normal[1], s->normal[2]};
+  w.vel = {s->vel[0], s->vel[1], s->vel[2]};
+  w.vrot = {s->vrot[0], s->vrot[1], s->vrot[2]};
+  w.center_proj = w.offset * w.normal;
+  if (is_null(w.vrot) && is_null({s->center[0], s->center[1], s->center[2]}))
+    w.center = w.offset * w.normal;
+  else
+    w.center = {s->center[0], s->center[1], s->center[2]};
+  // a centre off the plane on the normal's side is replaced (surface.hpp:166-173)
+  if (dot(w.center - w.center_proj, w.normal) >= 1e-14) w.center = dot(w.center_proj - w.center, w.normal) * w.normal + w.center_proj;
+  return w;
+}
+// register_cylinder: Cylinder::initialize (cylinder.hpp:94-105) stores axis * center.
+Cylinder cylinder_from(const dem_cylinder* c) {
+  Cylinder w{};
+  w.radius = c->radius;
+  w.axis = {c->axis[0], c->axis[1], c->axis[2]};
+  w.center = w.axis * V3{c->center[0], c->center[1], c->center[2]};
+  w.vel = {c->vel[0], c->vel[1], c->vel[2]};
+  w.vrot = {c->vrot[0], c->vrot[1], c->vrot[2]};
+  return w;
+}
+
 // ---------------------------------------------------------- neighbour build
 // Periodic wrap done by move_particles before each rebuild.
 void wrap(Oracle& o) {
@@ -454,6 +495,22 @@ int update_neighbors(Oracle& o) {
   return DEM_OK;
 }
 
+// ---- detection cores: {contact, dn, n, cp}; no contact returns dn = 0 like contact()
+struct Det {
+  bool c = false;
+  double dn = 0;
+  V3 n = {0, 0, 0}, cp = {0, 0, 0};
+};
+Det detect_vv(const V3& pi, double ri, const V3& pj, double rj) {  // :57-81
+  const double R = ri + rj;
+  const V3 dist = pi - pj;
+  const double dist_norm = norm(dist);
+  const double inv_dist_norm = 1.0 / dist_norm;
+  const double dn = dist_norm - R;
+  const V3 n = dist * inv_dist_norm;
+  const V3 cp = pi - n * (ri + 0.5 * dn);
+  return {dn < 0, dn, n, cp};
+}
 // --------------------------------------------------------------- contact law
 // contact_force_core<Hooke, None|Cohesive|DMT> (src/forcefield/include/exaDEM/forcefield/contact_force.hpp:146-235)
 // with common_kernels.hpp:27-145; dmt: apply_dmt_force (contact_force.hpp:115-127) with the pair's reff.
@@ -536,14 +593,10 @@ void contact_one(Oracle& o, size_t k) {
     const double rad_i = o.rad[i], rad_j = o.rad[j];
     const V3 vrot_j = {o.wx[j], o.wy[j], o.wz[j]};
     // detection_vertex_vertex_core (src/shape/include/exaDEM/shape_detection_core.hpp:57-81)
-    const double R = rad_i + rad_j;
-    const V3 dist = ri - rj;
-    const double dist_norm = norm(dist);
-    const double inv_dist_norm = 1.0 / dist_norm;
-    double dn = dist_norm - R;
-    const V3 n = dist * inv_dist_norm;
-    const V3 cp = ri - n * (rad_i + 0.5 * dn);
-    bool contact = dn < 0;
+    const Det det = detect_vv(ri, rad_i, rj, rad_j);
+    const double dn = det.dn;
+    const V3 n = det.n, cp = det.cp;
+    bool contact = det.c;
     const dem_contact_params& cpar = o.pair_params(i, j);  // contact_sphere.hpp:147-152
     if (cohesive) contact = (contact || dn <= cpar.dncut);
     if (contact) {
@@ -680,6 +733,24 @@ void force_to_accel(Oracle& o) {  // force_to_accel.hpp:26-33
     o.fz[i] /= o.mass[i];
   }
 }
+// PushToQuaternionFunctor (push_to_quaternion.hpp:26-38): Q += dot(Q, w) dt, normalize, w += dt/2 a.
+inline void push_quaternion(Quat& Q, V3& w, const V3& a, double delta_t, double half_delta_t) {
+  const Quat d = qdot(Q, w);
+  Q = {Q.w + d.w * delta_t, Q.x + d.x * delta_t, Q.y + d.y * delta_t, Q.z + d.z * delta_t};
+  Q = qnormalize(Q);
+  w.x += half_delta_t * a.x;
+  w.y += half_delta_t * a.y;
+  w.z += half_delta_t * a.z;
+}
+// PushToAngularAccelerationFunctor (angular_acceleration.hpp:27-43): Euler's equations in the body frame.
+inline V3 angular_acceleration(const Quat& Q, const V3& mom, const V3& vrot, const V3& I) {
+  const Quat Qinv = {Q.w, -Q.x, -Q.y, -Q.z};
+  const V3 omega = rotate(Qinv, vrot);
+  const V3 M = rotate(Qinv, mom);
+  const V3 domega = {(M.x - (I.z - I.y) * omega.y * omega.z) / I.x, (M.y - (I.x - I.z) * omega.z * omega.x) / I.y,
+                     (M.z - (I.y - I.x) * omega.x * omega.y) / I.z};
+  return rotate(Q, domega);
+}
 // combined_compute_prolog (combined_compute_prolog.cu:94-116): PushVec3SecondOrder,
 // PushVec3FirstOrder, PushToQuaternion (push_to_quaternion.hpp:26-38).
 void prolog(Oracle& o) {
@@ -695,17 +766,15 @@ void prolog(Oracle& o) {
     o.vy[i] += o.fy[i] * half_delta_t;
     o.vz[i] += o.fz[i] * half_delta_t;
     Quat Q = {o.qw[i], o.qx[i], o.qy[i], o.qz[i]};
-    const V3 w = {o.wx[i], o.wy[i], o.wz[i]};
-    const Quat d = qdot(Q, w);
-    Q = {Q.w + d.w * delta_t, Q.x + d.x * delta_t, Q.y + d.y * delta_t, Q.z + d.z * delta_t};
-    Q = qnormalize(Q);
+    V3 w = {o.wx[i], o.wy[i], o.wz[i]};
+    push_quaternion(Q, w, {o.ax[i], o.ay[i], o.az[i]}, delta_t, half_delta_t);
     o.qw[i] = Q.w;
     o.qx[i] = Q.x;
     o.qy[i] = Q.y;
     o.qz[i] = Q.z;
-    o.wx[i] += half_delta_t * o.ax[i];
-    o.wy[i] += half_delta_t * o.ay[i];
-    o.wz[i] += half_delta_t * o.az[i];
+    o.wx[i] = w.x;
+    o.wy[i] = w.y;
+    o.wz[i] = w.z;
   }
 }
 // combined_compute_epilog (combined_compute_epilog.cu:94-113) with
@@ -715,15 +784,8 @@ void epilog(Oracle& o) {
 #pragma omp parallel for schedule(static)
   for (long i = 0; i < (long)o.n; i++) {
     const Quat Q = {o.qw[i], o.qx[i], o.qy[i], o.qz[i]};
-    const Quat Qinv = {Q.w, -Q.x, -Q.y, -Q.z};
-    const V3 vrot = {o.wx[i], o.wy[i], o.wz[i]};
-    const V3 mom = {o.mx[i], o.my[i], o.mz[i]};
-    const V3 I = {o.ix[i], o.iy[i], o.iz[i]};
-    const V3 omega = rotate(Qinv, vrot);
-    const V3 M = rotate(Qinv, mom);
-    const V3 domega = {(M.x - (I.z - I.y) * omega.y * omega.z) / I.x, (M.y - (I.x - I.z) * omega.z * omega.x) / I.y,
-                       (M.z - (I.y - I.x) * omega.x * omega.y) / I.z};
-    const V3 arot = rotate(Q, domega);
+    const V3 arot = angular_acceleration(Q, {o.mx[i], o.my[i], o.mz[i]}, {o.wx[i], o.wy[i], o.wz[i]},
+                                         {o.ix[i], o.iy[i], o.iz[i]});
     o.ax[i] = arot.x;
     o.ay[i] = arot.y;
     o.az[i] = arot.z;
@@ -967,22 +1029,6 @@ bool filter_ee(double rV, const V3& vfi, const V3& vsi, double ri, const V3& vfj
   return false;
 }
 
-// ---- detection cores: {contact, dn, n, cp}; no contact returns dn = 0 like contact()
-struct Det {
-  bool c = false;
-  double dn = 0;
-  V3 n = {0, 0, 0}, cp = {0, 0, 0};
-};
-Det detect_vv(const V3& pi, double ri, const V3& pj, double rj) {  // :57-81
-  const double R = ri + rj;
-  const V3 dist = pi - pj;
-  const double dist_norm = norm(dist);
-  const double inv_dist_norm = 1.0 / dist_norm;
-  const double dn = dist_norm - R;
-  const V3 n = dist * inv_dist_norm;
-  const V3 cp = pi - n * (ri + 0.5 * dn);
-  return {dn < 0, dn, n, cp};
-}
 Det detect_ve(const V3& vi, double ri, const V3& vf, const V3& vs, double rj) {  // :122-148
   const V3 distfs = vs - vf;
   const V3 distfi = vi - vf;
@@ -1645,15 +1691,7 @@ int oracle_register_surface(void* h, const dem_surface* s) {
   Oracle& o = *(Oracle*)h;
   Driver d{};
   d.kind = 0;
-  d.s.offset = s->offset;
-  d.s.normal = {s->normal[0], s->normal[1], s->normal[2]};
-  d.s.vel = {s->vel[0], s->vel[1], s->vel[2]};
-  d.s.vrot = {s->vrot[0], s->vrot[1], s->vrot[2]};
-  d.s.center_proj = d.s.offset * d.s.normal;  // Surface::initialize (surface.hpp:138)
-  if (is_null(d.s.vrot) && is_null({s->center[0], s->center[1], s->center[2]}))
-    d.s.center = d.s.offset * d.s.normal;  // YAML default (surface.hpp:74)
-  else
-    d.s.center = {s->center[0], s->center[1], s->center[2]};
+  d.s = surface_from(s);
   o.drivers.push_back(d);
   return DEM_OK;
 }
@@ -1661,11 +1699,7 @@ int oracle_register_cylinder(void* h, const dem_cylinder* c) {
   Oracle& o = *(Oracle*)h;
   Driver d{};
   d.kind = 1;
-  d.c.radius = c->radius;
-  d.c.axis = {c->axis[0], c->axis[1], c->axis[2]};
-  d.c.center = d.c.axis * V3{c->center[0], c->center[1], c->center[2]};  // Cylinder::initialize
-  d.c.vel = {c->vel[0], c->vel[1], c->vel[2]};
-  d.c.vrot = {c->vrot[0], c->vrot[1], c->vrot[2]};
+  d.c = cylinder_from(c);
   o.drivers.push_back(d);
   return DEM_OK;
 }
@@ -1904,6 +1938,232 @@ int oracle_packing_profile(void* h, int nslabs, double zlo, double zhi, double* 
     for (int s = a; s <= b; s++) vol[s] += sphere_slab_volume(zc, r, zlo + s * dz, zlo + (s + 1) * dz);
   }
   for (int s = 0; s < nslabs; s++) out[s] = vol[s] / (area * dz);
+  return DEM_OK;
+}
+// ------------------------------------------------------------ unit entry points
+// Per-function entry points over n cases, with the row layouts of
+// oracle/ref_harness.cpp (exaDEM's own functions compiled on the host), so the
+// restatement above can be compared with exaDEM bit for bit.  Each calls the
+// oracle function the step uses.
+static inline V3 rv(const double* p) { return {p[0], p[1], p[2]}; }
+static inline void wv(double* o, const V3& v) {
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+}
+static inline void wdet(double* o, const Det& d) {
+  o[0] = d.c ? 1.0 : 0.0;
+  o[1] = d.dn;
+  wv(o + 2, d.n);
+  wv(o + 5, d.cp);
+}
+static inline OBBr robb(const double* p) { return OBBr{rv(p), rv(p + 3), rv(p + 6), rv(p + 9), rv(p + 12)}; }
+static inline void wobb(double* o, const OBBr& b) {
+  wv(o, b.c);
+  wv(o + 3, b.e1);
+  wv(o + 6, b.e2);
+  wv(o + 9, b.e3);
+  wv(o + 12, b.ext);
+}
+int oracle_unit_contact_force_core(int law, long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 45 * c;
+    double* o = out + 12 * c;
+    dem_contact_params hkp{};
+    hkp.kn = p[5];
+    hkp.kt = p[6];
+    hkp.kr = p[7];
+    hkp.mu = p[8];
+    hkp.damp_rate = p[9];
+    hkp.fc = p[10];
+    hkp.dncut = p[11];
+    hkp.gamma = p[12];
+    V3 ft = rv(p + 15), f_i = rv(p + 27), mom_i = rv(p + 30);
+    const V3 cp = rv(p + 18), pos_i = rv(p + 21);
+    contact_force_core(law == 1, p[0], rv(p + 1), p[4], hkp, p[13], ft, cp, pos_i, rv(p + 24), f_i, mom_i, rv(p + 33),
+                       rv(p + 36), rv(p + 39), rv(p + 42), law == 2, p[14]);
+    wv(o, f_i);
+    wv(o + 3, ft);
+    wv(o + 6, mom_i);
+    wv(o + 9, cross(cp - pos_i, f_i) + mom_i);  // compute_moments, as in the force records
+  }
+  return DEM_OK;
+}
+int oracle_unit_damping(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 5 * c;
+    const double meff = (p[2] * p[3]) / (p[2] + p[3]);
+    out[2 * c] = meff;
+    out[2 * c + 1] = p[0] * 2.0 * std::sqrt(p[1] * meff);
+  }
+  return DEM_OK;
+}
+int oracle_unit_detect_vv(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 8 * c;
+    wdet(out + 8 * c, detect_vv(rv(p), p[3], rv(p + 4), p[7]));
+  }
+  return DEM_OK;
+}
+int oracle_unit_detect_ve(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 11 * c;
+    wdet(out + 8 * c, detect_ve(rv(p), p[3], rv(p + 4), rv(p + 7), p[10]));
+  }
+  return DEM_OK;
+}
+int oracle_unit_detect_ee(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 14 * c;
+    wdet(out + 8 * c, detect_ee(rv(p), rv(p + 3), p[6], rv(p + 7), rv(p + 10), p[13]));
+  }
+  return DEM_OK;
+}
+int oracle_unit_filter(int kind, long n, const double* in, double* out) {
+  const int k = kind == 0 ? 9 : kind == 1 ? 12 : 15;
+  for (long c = 0; c < n; c++) {
+    const double* p = in + k * c;
+    bool r;
+    if (kind == 0)
+      r = filter_vv(p[0], rv(p + 1), p[4], rv(p + 5), p[8]);
+    else if (kind == 1)
+      r = filter_ve(p[0], rv(p + 1), p[4], rv(p + 5), rv(p + 8), p[11]);
+    else
+      r = filter_ee(p[0], rv(p + 1), rv(p + 4), p[7], rv(p + 8), rv(p + 11), p[14]);
+    out[c] = r ? 1.0 : 0.0;
+  }
+  return DEM_OK;
+}
+int oracle_unit_world_vertex(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 11 * c;
+    const Quat q = {p[3], p[4], p[5], p[6]};
+    wv(out + 3 * c, rv(p) + rotate(q, p[7] * rv(p + 8)));  // compute_vertices
+  }
+  return DEM_OK;
+}
+// face: the vertex indices of the face; radius: the shape's Minkowski radius (scaled by hj as the list build does)
+int oracle_unit_vertex_face(const int32_t* face, int nfv, int nv, double radius, long n, const double* in,
+                            double* out) {
+  const std::vector<int> f(face, face + nfv);
+  std::vector<V3> va(nv);
+  for (long c = 0; c < n; c++) {
+    const double* p = in + (6 + 3 * nv) * c;
+    for (int k = 0; k < nv; k++) va[k] = rv(p + 6 + 3 * k);
+    const double rj = radius * p[5];
+    double* o = out + 9 * c;
+    o[0] = filter_vf(p[0], rv(p + 1), p[4], va, f, rj) ? 1.0 : 0.0;
+    wdet(o + 1, detect_vf(rv(p + 1), p[4], va, f, rj));
+  }
+  return DEM_OK;
+}
+int oracle_unit_obb_intersect(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) out[c] = obb_intersect(robb(in + 30 * c), robb(in + 30 * c + 15)) ? 1.0 : 0.0;
+  return DEM_OK;
+}
+int oracle_unit_compute_obb(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 24 * c;
+    OBBr b = compute_obb(robb(p), rv(p + 15), Quat{p[18], p[19], p[20], p[21]}, p[22]);
+    obb_enlarge(b, p[23]);
+    wobb(out + 15 * c, b);
+  }
+  return DEM_OK;
+}
+int oracle_unit_push_quaternion(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 11 * c;
+    const double delta_t = p[10];
+    Quat Q = {p[0], p[1], p[2], p[3]};
+    V3 w = rv(p + 4);
+    push_quaternion(Q, w, rv(p + 7), delta_t, delta_t * 0.5);
+    double* o = out + 7 * c;
+    o[0] = Q.w;
+    o[1] = Q.x;
+    o[2] = Q.y;
+    o[3] = Q.z;
+    wv(o + 4, w);
+  }
+  return DEM_OK;
+}
+int oracle_unit_angular(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 15 * c;
+    const double half_delta_t = p[13] * 0.5;
+    const V3 arot = angular_acceleration(Quat{p[0], p[1], p[2], p[3]}, rv(p + 4), rv(p + 7), rv(p + 10));
+    V3 w = rv(p + 7);
+    w.x += arot.x * half_delta_t;
+    w.y += arot.y * half_delta_t;
+    w.z += arot.z * half_delta_t;
+    wv(out + 6 * c, arot);
+    wv(out + 6 * c + 3, w);
+  }
+  return DEM_OK;
+}
+int oracle_unit_pair_order(long n, const uint64_t* keys, int32_t* out) {
+  for (long c = 0; c < n; c++) {
+    const uint64_t* k = keys + 12 * c;
+    Inter a{}, b{};
+    for (Inter* x : {&a, &b}) {
+      const uint64_t* q = x == &a ? k : k + 6;
+      x->oid = q[0];
+      x->pid = q[1];
+      x->type = (uint16_t)q[2];
+      x->swap = (uint8_t)q[3];
+      x->osub = (uint32_t)q[4];
+      x->psub = (uint32_t)q[5];
+    }
+    out[2 * c] = key_less(a, b);
+    out[2 * c + 1] = key_eq(a, b);
+  }
+  return DEM_OK;
+}
+int oracle_unit_surface(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 11 * c;
+    dem_surface ds{};
+    ds.offset = p[0];
+    for (int d = 0; d < 3; d++) {
+      ds.normal[d] = p[1 + d];
+      ds.center[d] = p[4 + d];
+    }
+    const Surface w = surface_from(&ds);
+    double* o = out + 13 * c;
+    o[0] = surface_filter(w, p[7], rv(p + 8)) ? 1.0 : 0.0;
+    double dn = 0;
+    V3 nn{}, cp{};
+    const bool hit = surface_detect(w, p[7], rv(p + 8), dn, nn, cp);
+    o[1] = hit ? 1.0 : 0.0;
+    o[2] = dn;
+    wv(o + 3, nn);
+    wv(o + 6, cp);
+    wv(o + 9, w.center);
+    o[12] = 0.0;
+  }
+  return DEM_OK;
+}
+int oracle_unit_cylinder(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 11 * c;
+    dem_cylinder dc{};
+    dc.radius = p[0];
+    for (int d = 0; d < 3; d++) {
+      dc.axis[d] = p[1 + d];
+      dc.center[d] = p[4 + d];
+    }
+    const Cylinder w = cylinder_from(&dc);
+    double* o = out + 13 * c;
+    o[0] = cylinder_filter(w, p[7], rv(p + 8)) ? 1.0 : 0.0;
+    double dn = 0;
+    V3 nn{}, cp{};
+    const bool hit = cylinder_detect(w, p[7], rv(p + 8), dn, nn, cp);
+    o[1] = hit ? 1.0 : 0.0;
+    o[2] = dn;
+    wv(o + 3, nn);
+    wv(o + 6, cp);
+    wv(o + 9, w.center);
+    o[12] = 0.0;
+  }
   return DEM_OK;
 }
 const char* oracle_last_error(void* h) { return ((Oracle*)h)->err.c_str(); }
