@@ -13,6 +13,8 @@ import numpy as np
 
 PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "libexadem_gb300.so"
+# the seeded input generator (include/dem_workloads.h), host code in a library of its own
+WORKLOADS_LIB_PATH = PKG / "libdem_workloads.so"
 
 DEM_OK = 0
 ERRORS = {1: "DEM_ERR_INVALID_ARG", 2: "DEM_ERR_CUDA", 3: "DEM_ERR_OOM", 4: "DEM_ERR_UNSUPPORTED",
@@ -197,7 +199,6 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_interaction_count", [_CTX, PU64])
     _sig(lib, "dem_get_interactions", [_CTX, C.POINTER(InteractionList)])
     _sig(lib, "dem_packing_profile", [_CTX, C.c_int, D, D, PD])
-    _sig(lib, "dem_generate_rsa_spheres", [C.POINTER(RsaSpec), C.POINTER(Particles), PD])
     _sig(lib, "dem_profile", [_CTX, C.c_int])
     _sig(lib, "dem_kernel_stats", [_CTX, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)])
     _sig(lib, "dem_reset_kernel_stats", [_CTX])
@@ -206,10 +207,9 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_selftest_poly_decisions", [C.c_uint64, C.c_uint64, PU64])
     _sig(lib, "dem_selftest_emu_mul", [C.c_uint64, C.c_uint64, PU64])
     _sig(lib, "dem_selftest_rolling_clip", [C.c_uint64, C.c_uint64, PU64, PU64])
-    _sig(lib, "dem_probe_mul_rates", [C.c_int, C.POINTER(C.c_double)])
 
 
-# Symbols declared in include/dem_hotpath.h, dem_workloads.h, dem_selftest.h and dem_learned.h.
+# Symbols declared in include/dem_hotpath.h, dem_selftest.h and dem_learned.h (the product library).
 EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stream", "dem_set_params",
             "dem_set_particles", "dem_get_particles", "dem_register_surface", "dem_register_cylinder",
             "dem_register_mesh",
@@ -217,8 +217,8 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_gravity_force", "dem_contact_sphere", "dem_force_to_accel", "dem_combined_compute_prolog",
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
             "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
-            "dem_generate_rsa_spheres", "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
-            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_selftest_emu_mul", "dem_selftest_rolling_clip", "dem_probe_mul_rates", "dem_set_shapes", "dem_compute_vertices",
+            "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
+            "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_selftest_emu_mul", "dem_selftest_rolling_clip", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
             "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune", "dem_set_mul_mode", "dem_get_mul_mode", "dem_set_multimat", "dem_set_analysis", "dem_get_contact_state", "dem_stress_tensor", "dem_mlp_harvest",
             "dem_mlp_init", "dem_mlp_set_params", "dem_mlp_get_params", "dem_mlp_forward", "dem_mlp_loss_grad",
@@ -238,6 +238,23 @@ def load(path: Path | None = None):
         declare_library(lib)
         _LIB = lib
     return _LIB
+
+
+WORKLOADS_EXPORTED = ["dem_generate_rsa_spheres"]
+_WLIB = None
+
+
+def load_workloads(path: Path | None = None):
+    """Loads (once) the input generator library (host code, no CUDA)."""
+    global _WLIB
+    if _WLIB is None:
+        p = Path(path) if path else WORKLOADS_LIB_PATH
+        if not p.exists():
+            raise RuntimeError(f"generator library missing: {p} (run exadem_gb300.build.build())")
+        lib = C.CDLL(str(p))
+        _sig(lib, "dem_generate_rsa_spheres", [C.POINTER(RsaSpec), C.POINTER(Particles), PD])
+        _WLIB = lib
+    return _WLIB
 
 
 class DemError(RuntimeError):

@@ -2,7 +2,8 @@
 
 Every ``csrc/*.cu`` translation unit is compiled by nvcc in parallel, the host
 ``csrc/*.cpp`` units by g++, and all are linked into one shared library next
-to this file.  FP64 contraction is disabled (``--fmad=false``) so the contact
+to this file.  The seeded input generator (``gen/``) is a separate host
+library, ``libdem_workloads.so``.  FP64 contraction is disabled (``--fmad=false``) so the contact
 law keeps the reference's operation order bit for bit.
 """
 from __future__ import annotations
@@ -18,6 +19,8 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libexadem_gb300.so"
+GEN = PKG / "gen"
+WORKLOADS_LIB = PKG / "libdem_workloads.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
@@ -72,7 +75,17 @@ def build(verbose: bool = False, force: bool = False, extra_nvcc: list[str] | No
                 fut.result()
     if force or jobs or _stale(LIB, objs):
         _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs)])
+    build_workloads(force)
     return LIB
+
+
+def build_workloads(force: bool = False) -> Path:
+    """The seeded input generator (gen/*.cpp, include/dem_workloads.h) as a host library of its own."""
+    srcs = sorted(GEN.glob("*.cpp"))
+    deps = srcs + list((PKG.parent / "include").glob("*.h"))
+    if force or _stale(WORKLOADS_LIB, deps):
+        _run(["g++", *CXX_FLAGS, "-shared", "-o", str(WORKLOADS_LIB), *map(str, srcs)])
+    return WORKLOADS_LIB
 
 
 if __name__ == "__main__":

@@ -1,7 +1,6 @@
 // k_selftest_emu.cu -- GPU self-tests of the integer-pipe binary64 multiply
 // (emu64.cuh) against the hardware multiply and of the rolling-clip shortcut
-// (contact_core.cuh) against the formula, and a probe of the multiply rates
-// of the FP64 pipe, the integer pipe, and both together.
+// (contact_core.cuh) against the formula.
 #include "../../include/dem_selftest.h"
 #include "contact_core.cuh"
 #include "dem_ctx.cuh"
@@ -122,54 +121,6 @@ __global__ void k_clip_test(uint64_t n, uint64_t seed, unsigned long long* bad, 
   atomicAdd(fast, nfast);
 }
 
-// NN chains multiplied on the FP64 pipe and NE chains on the integer pipe,
-// all in the same thread; factors alternate around 1 so values stay normal.
-// The factors are kernel arguments, so no part of the emulated product is
-// folded at compile time; the branch-free form is the one the integration
-// kernels use.
-template <int NN, int NE>
-__global__ void __launch_bounds__(256) k_rate(int iters, double seed, double c1, double c2, double* out) {
-  double xn[NN > 0 ? NN : 1], xe[NE > 0 ? NE : 1];
-  const double base = seed + 1e-3 * (double)(threadIdx.x & 31);
-#pragma unroll
-  for (int k = 0; k < NN; k++) xn[k] = base + k;
-#pragma unroll
-  for (int k = 0; k < NE; k++) xe[k] = base - k;
-  bool bad = false;
-  for (int i = 0; i < iters; i++) {
-#pragma unroll
-    for (int k = 0; k < NN; k++) xn[k] = __dmul_rn(__dmul_rn(xn[k], c1), c2);
-#pragma unroll
-    for (int k = 0; k < NE; k++) xe[k] = dem::emu_dmul_nb(dem::emu_dmul_nb(xe[k], c1, bad), c2, bad);
-  }
-  double s = bad ? -1.0 : 0.0;
-#pragma unroll
-  for (int k = 0; k < NN; k++) s += xn[k];
-#pragma unroll
-  for (int k = 0; k < NE; k++) s += xe[k];
-  out[(uint64_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
-}
-
-template <int NN, int NE>
-int time_rate(int blocks, int iters, double* out, double* gops) {
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  const double c1 = 1.0 + 1.0 / 1048576.0, c2 = 1.0 - 1.0 / 2097152.0;
-  k_rate<NN, NE><<<blocks, 256>>>(iters / 8, 1.25, c1, c2, out);  // warm-up
-  cudaEventRecord(e0);
-  k_rate<NN, NE><<<blocks, 256>>>(iters, 1.25, c1, c2, out);
-  cudaEventRecord(e1);
-  cudaEventSynchronize(e1);
-  float ms = 0.f;
-  cudaEventElapsedTime(&ms, e0, e1);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  if (cudaGetLastError() != cudaSuccess) return DEM_ERR_CUDA;
-  const double ops = 2.0 * (NN + NE) * (double)iters * (double)blocks * 256.0;
-  *gops = ops / (ms * 1e-3) * 1e-9;
-  return DEM_OK;
-}
 }  // namespace
 
 extern "C" int dem_selftest_emu_mul(uint64_t n, uint64_t seed, uint64_t* mismatches) {
@@ -199,21 +150,4 @@ extern "C" int dem_selftest_rolling_clip(uint64_t n, uint64_t seed, uint64_t* mi
   *mismatches = h[0];
   *fast_path_taken = h[1];
   return DEM_OK;
-}
-
-extern "C" int dem_probe_mul_rates(int iters, double* gops) {
-  if (!gops || iters < 8) return DEM_ERR_INVALID_ARG;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int blocks = sms * 8;
-  double* out = nullptr;
-  if (cudaMalloc(&out, (size_t)blocks * 256 * sizeof(double)) != cudaSuccess) return DEM_ERR_CUDA;
-  int st = time_rate<4, 0>(blocks, iters, out, &gops[0]);
-  if (st == DEM_OK) st = time_rate<0, 4>(blocks, iters, out, &gops[1]);
-  if (st == DEM_OK) st = time_rate<4, 4>(blocks, iters, out, &gops[2]);
-  if (st == DEM_OK) st = time_rate<4, 2>(blocks, iters, out, &gops[3]);
-  if (st == DEM_OK) st = time_rate<2, 4>(blocks, iters, out, &gops[4]);
-  cudaFree(out);
-  return st;
 }

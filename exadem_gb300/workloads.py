@@ -1,7 +1,8 @@
 """Seeded synthetic workloads of the benchmark configurations.
 
 No public dataset is involved: every input is generated from a fixed seed by
-random sequential addition (``dem_generate_rsa_spheres``, include/dem_workloads.h).
+random sequential addition (``dem_generate_rsa_spheres``, include/dem_workloads.h,
+built as its own host library ``libdem_workloads.so``, apart from the product library).
 
 * ``spheres_box``     -- config 1: monodisperse spheres in a walled box.
 * ``spheres_floor``   -- config 2: polydisperse spheres, periodic in x/y,
@@ -54,7 +55,7 @@ class Workload:
 
 def rsa(n, rmin, rmax, density, lo, hi, periodic=(0, 0, 0), grow_axis=-1, seed=1, vmin=0.0, vmax=0.0,
         region=0, cyl_center=(0.0, 0.0), cyl_radius=0.0, max_attempts=64, id_offset=0, radii=None):
-    lib = A.load()
+    lib = A.load_workloads()
     spec = A.RsaSpec()
     spec.n = n
     spec.rmin, spec.rmax, spec.density = rmin, rmax, density

@@ -35,11 +35,6 @@ int dem_selftest_emu_mul(uint64_t n, uint64_t seed, uint64_t* mismatches);
  * fast_path_taken counts the cases inside the shortcut's range.            */
 int dem_selftest_rolling_clip(uint64_t n, uint64_t seed, uint64_t* mismatches, uint64_t* fast_path_taken);
 
-/* Multiply throughput in G multiplies/s over all SMs, dependent chains, 8
- * blocks of 256 threads per SM: gops[0] FP64 pipe alone, gops[1] integer pipe
- * alone (emu_dmul), gops[2..4] both in the same threads, with native:emulated
- * chain ratios 4:4, 4:2 and 2:4.                                           */
-int dem_probe_mul_rates(int iters, double* gops);
 #ifdef __cplusplus
 }
 #endif

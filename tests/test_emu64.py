@@ -31,10 +31,29 @@ def test_emu_dmul_gpu_bit_exact(native_lib):
     assert bad.value == 0
 
 
+def _probe_lib():
+    """tests/probe_mul_rates.cu, a measurement probe kept out of the library, built on demand."""
+    import subprocess
+    from pathlib import Path
+
+    from exadem_gb300 import build as B
+
+    here = Path(__file__).resolve().parent
+    out = here / "_build" / "libdem_probe.so"
+    src = here / "probe_mul_rates.cu"
+    if not out.exists() or out.stat().st_mtime < src.stat().st_mtime:
+        out.parent.mkdir(exist_ok=True)
+        subprocess.run([B._nvcc(), *B.ARCH, "-O3", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-shared",
+                        "-o", str(out), str(src)], check=True)
+    lib = C.CDLL(str(out))
+    lib.dem_probe_mul_rates.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    return lib
+
+
 @pytest.mark.gpu
 def test_mul_rates_probe(native_lib):
     g = (C.c_double * 5)()
-    assert native_lib.dem_probe_mul_rates(4096, g) == 0
+    assert _probe_lib().dem_probe_mul_rates(4096, g) == 0
     print("multiply rates, G/s: fp64 %.0f  integer %.0f  both 4:4 %.0f  4:2 %.0f  2:4 %.0f" % tuple(g))
     assert all(x > 0 for x in g)
 
