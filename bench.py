@@ -7,15 +7,26 @@ one Verlet iteration of the reference deck: prolog, displacement trigger and
 (when triggered) neighbour rebuild, reset, gravity, contact law, gather,
 force_to_accel, epilog.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl native|reference] [--n N]
+Pre-roll: before any timing, each workload runs a fixed number of untimed
+steps (``--preroll``, independent of ``--warmup``).  For the spheres it is 3000
+steps (1.5 s of deposition): the RSA column (solid fraction 0.30, the random
+sequential addition jams near 0.38) has collapsed into a bed at a solid
+fraction of about 0.6 over its height, the contact count has reached its
+plateau and the bed still moves enough to trigger a neighbour rebuild every
+ten steps or so.  The timed window starts there.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--preroll P] [--impl native|reference] [--n N]
 
 Prints one JSON line.  `value` is device-resident throughput (inputs already in
 HBM, CUDA events on the library's stream); `e2e` is the same metric through
-the public C ABI from pinned host buffers, with the host->device upload, the
-first force pass and the device->host readback inside the timed region.
+the public C ABI from pinned host buffers holding the pre-rolled state, with
+the host->device upload, the first force pass and the device->host readback
+inside the timed region.  `vs_plain` times the plain FP64 operator kernels on
+the same pre-rolled state and checks that both paths end in the same bits.
 `--impl reference` times the CPU restatement of the reference algorithm
-(OpenMP, all host cores) on the same workload.  With N > 1 (torchrun) every
-rank runs an independent replica: the path does not shard.
+(OpenMP, all host cores) on a periodic patch of the same workload, pre-rolled
+the same way.  With N > 1 (torchrun) every rank runs an independent replica:
+the path does not shard.
 """
 from __future__ import annotations
 
@@ -36,6 +47,17 @@ UNIT = "particle-steps/s"
 # Algorithmic bytes of the contact kernel per interaction: history friction +
 # moment read and written (2 x 48 B) + two u32 particle indices.
 CONTACT_BYTES_PER_INTERACTION = 104
+# Algorithmic bytes of the particle integration per particle-step (prolog and
+# epilog together): read r, v, omega, alpha, q, a (19 doubles) and m, R, I (5),
+# write r, v, omega, alpha, q, a (19).
+PARTICLE_BYTES_PER_STEP = 344
+# Untimed steps before the warm-up, per workload (--preroll overrides).
+PREROLL = {"spheres": 3000, "polyhedra": 0, "polyhedra_dense": 0, "drums": 0, "mixer": 300, "polyhedra_mesh": 0}
+# DRAM bytes (read + write) per step of the integration kernels (k_fused_prolog,
+# k_prolog_rotation, k_fused_epilog, k_epilog_rotation) and of the contact phase
+# (k_cscreen, k_cdetect, k_chooke), from the ncu captures summarised under
+# profiles/ (per particle and per listed pair, so they scale to the bench state).
+TRAFFIC = {"source": None, "integration_bytes_per_particle": None, "contact_bytes_per_listed_pair": None}
 
 
 def parse():
@@ -44,6 +66,13 @@ def parse():
     ap.add_argument("--steps", type=int, default=None,
                     help="timed steps (default: the workload's whole run, e.g. 1000 for the 2M-sphere deposition)")
     ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--preroll", type=int, default=None,
+                    help="untimed steps run before the warm-up (default: the workload's pre-roll, 3000 for the "
+                         "spheres; 0 disables)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 path leg (vs_plain)")
+    ap.add_argument("--patch", type=int, default=125_000,
+                    help="spheres: particle count of the periodic patch the CPU legs time (same workload, "
+                         "footprint scaled to keep the density)")
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--n", type=int, default=None, help="particle count (default: the workload's)")
     ap.add_argument("--workload", default="spheres",
@@ -244,8 +273,16 @@ WORKLOAD_DESC = {
 }
 
 
-def cpu_baseline(w, budget_s: float = 20.0):
-    """The oracle (C++ restatement of the reference CPU path, OpenMP, all cores) on a bounded sample."""
+def cpu_sample(args, w, max_steps: int, budget_s: float):
+    """The oracle (C++ restatement of the reference CPU path, OpenMP, all host
+    cores) on a bounded sample of the workload.  Spheres: a periodic patch of
+    the same workload (args.patch spheres, footprint scaled to keep the density,
+    same generator and physics), pre-rolled like the GPU legs, then timed for up
+    to max_steps steps or budget_s seconds.  Other workloads: the workload itself
+    (one drum at a time for the batched drums), without pre-roll."""
+    import math as _m
+
+    from exadem_gb300 import workloads as W
     from oracle.oracle import oracle_system, set_threads
 
     cores = set_threads(os.cpu_count() or 1)
@@ -264,25 +301,44 @@ def cpu_baseline(w, budget_s: float = 20.0):
             o.close()
             if t_all > budget_s:
                 break
-        return {"value": done / t_all, "unit": UNIT, "cores": cores, "kind": "port",
+        return {"value": done / t_all, "unit": UNIT, "cores": cores, "kind": "port", "steps": 10,
+                "seconds": t_all,
                 "sample": f"10 Verlet steps of each of the first {nd} drums ({int(done / 10)} spheres), "
                           f"{t_all:.1f} s"}
-    o = w.build(oracle_system)
+    pre = preroll_steps(args)
+    if args.workload == "spheres":
+        n = min(args.patch, w.n)
+        side = 400.0 * _m.sqrt(n / 2_000_000)
+        ws = W.spheres_floor(n=n, side=side)
+        what = f"periodic {side:.1f} x {side:.1f} patch of the same workload ({n} spheres)"
+    else:
+        ws, n, pre = w, w.n, 0
+        what = f"the full {w.n}-particle workload"
+    o = ws.build(oracle_system)
     t0 = time.perf_counter()
     o.first_iteration()
-    t_first = time.perf_counter() - t0
+    if pre:
+        o.step(pre)
+    o.step(max(1, min(args.warmup, 3)))
+    t_pre = time.perf_counter() - t0
+    r0 = o.rebuild_count()
     steps = 0
     t0 = time.perf_counter()
     while True:
         o.step(1)
         steps += 1
         el = time.perf_counter() - t0
-        if el > budget_s or steps >= 50:
+        if el > budget_s or steps >= max_steps:
             break
+    rebuilds = o.rebuild_count() - r0
     o.close()
-    return {"value": w.n * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{steps} Verlet steps of the full {w.n}-sphere workload after first_iteration "
-                      f"({t_first:.1f} s), {el:.1f} s"}
+    return {"value": n * steps / el, "unit": UNIT, "cores": cores, "kind": "port", "steps": steps, "seconds": el,
+            "sample": f"{steps} Verlet steps ({rebuilds} rebuilds) of a {what}, after first_iteration, "
+                      f"{pre} pre-roll steps and the warm-up ({t_pre:.1f} s, untimed); {el:.1f} s timed"}
+
+
+def cpu_baseline(args, w):
+    return cpu_sample(args, w, max_steps=50, budget_s=20.0)
 
 
 def run_drums_separate(args, w, rank, world, local, dist):
@@ -399,6 +455,60 @@ def rebuild_timing(args, w, s):
     return out
 
 
+def preroll_steps(args) -> int:
+    return PREROLL.get(args.workload, 0) if args.preroll is None else max(0, args.preroll)
+
+
+def plain_variant(w):
+    """The same workload (same particles, drivers and physics) on the plain FP64
+    operator kernels: no fused step, no FP32 screening, no graph, no learned sizing."""
+    import copy
+
+    from exadem_gb300 import _abi as A
+
+    q = A.Params.from_buffer_copy(w.params)
+    q.fp32_broad_phase = q.fp32_contact_screen = q.fused_step = q.graph_step = q.learned_sizing = 0
+    w2 = copy.copy(w)
+    w2.params = q
+    return w2
+
+
+def event_timed(s, steps: int, local: int, dist):
+    """K steps timed with CUDA events on the library's stream, barrier and synchronise on both sides."""
+    import torch
+
+    ext = torch.cuda.ExternalStream(s.stream_handle())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    r0 = s.rebuild_count()
+    with Clocks(local) as clk:
+        barrier(dist)
+        torch.cuda.synchronize()
+        ev0.record(ext)
+        s.step(steps)
+        ev1.record(ext)
+        ev1.synchronize()
+        torch.cuda.synchronize()
+        barrier(dist)
+    return ev0.elapsed_time(ev1), s.rebuild_count() - r0, clk.summary()
+
+
+def bed_fraction(s, w) -> dict:
+    """Solid fraction of the spheres' bed: the packing profile (analytic sphere-slab
+    volumes, 50 slabs from the floor to the highest centre) and its mean over the
+    slabs between two diameters above the floor and two diameters below the top."""
+    import numpy as np
+
+    p = s.particles(sort_by_id=False)
+    zmax = float(np.max(p["rz"]))
+    rmax = float(np.max(p["radius"]))
+    prof = s.packing_profile(50, 0.0, zmax)
+    dz = zmax / 50
+    lo, hi = int(np.ceil(2 * rmax / dz)), int(np.floor((zmax - 2 * rmax) / dz))
+    core = prof[lo:hi] if hi > lo else prof
+    return {"phi_bed": round(float(np.mean(core)), 4), "phi_profile_max": round(float(np.max(prof)), 4),
+            "bed_top": round(zmax, 3)}
+
+
 def run_native(args, rank, world, local, dist):
     import numpy as np
     import torch
@@ -410,6 +520,7 @@ def run_native(args, rank, world, local, dist):
     w = workload(args)
     if is_batch(w) and args.plain:
         return run_drums_separate(args, w, rank, world, local, dist)
+    pre = preroll_steps(args)
     learned = None
     if args.learned and args.workload in ("polyhedra", "polyhedra_dense"):
         params, learned = train_learned(args)
@@ -418,8 +529,16 @@ def run_native(args, rank, world, local, dist):
         from exadem_gb300.learned import Learned
 
         Learned(s).set_params(params)
-    ext = torch.cuda.ExternalStream(s.stream_handle())
     s.first_iteration()
+    t0 = time.perf_counter()
+    if pre:
+        s.step(pre)
+        torch.cuda.synchronize()
+    preroll_s = time.perf_counter() - t0
+    state_pre = s.simulation_state()
+    # the pre-rolled particle state, read back for the end-to-end leg
+    host_pre = None if (args.no_e2e or is_batch(w)) else s.particles(sort_by_id=True)
+    bed = bed_fraction(s, w) if args.workload == "spheres" and pre else None
     tune = None
     if not args.plain and not args.no_tune and args.workload in ("spheres", "drums", "mixer"):
         # cell size and launch shapes; the skin only where it cannot change a bit.
@@ -432,19 +551,7 @@ def run_native(args, rank, world, local, dist):
     s.step(args.warmup)
     torch.cuda.synchronize()
     s.reset_kernel_stats()
-    r0 = s.rebuild_count()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(local) as clk:
-        barrier(dist)
-        torch.cuda.synchronize()
-        ev0.record(ext)
-        s.step(args.steps)
-        ev1.record(ext)
-        ev1.synchronize()
-        torch.cuda.synchronize()
-        barrier(dist)
-    ms = ev0.elapsed_time(ev1)
-    rebuilds = s.rebuild_count() - r0
+    ms, rebuilds, clocks = event_timed(s, args.steps, local, dist)
     if learned is not None:
         from exadem_gb300.learned import Learned
 
@@ -453,15 +560,9 @@ def run_native(args, rank, world, local, dist):
         w0 = workload(argparse.Namespace(**{**vars(args), "learned": False}))
         s0 = w0.build()
         s0.first_iteration()
-        s0.step(args.warmup)
-        ext0 = torch.cuda.ExternalStream(s0.stream_handle())
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(ext0)
-        s0.step(args.steps)
-        e1.record(ext0)
-        e1.synchronize()
-        learned["ms_per_step_without"] = e0.elapsed_time(e1) / args.steps
+        s0.step(pre + args.warmup)
+        ms0, _, _ = event_timed(s0, args.steps, local, None)
+        learned["ms_per_step_without"] = ms0 / args.steps
         learned["ms_per_step_with"] = ms / args.steps
         learned["rebuilds_without"] = s0.rebuild_count()
         learned["same_state"] = bool(s0.simulation_state()["kinetic_energy"].tolist()
@@ -472,6 +573,27 @@ def run_native(args, rank, world, local, dist):
     ms = allmax(dist, ms)
     total = allsum(dist, float(w.n * args.steps))
     value = total / (ms / 1e3)
+    state_end = s.simulation_state()
+
+    # the plain FP64 operator path from the same initial state, same pre-roll and
+    # warm-up: its speed, and whether it ends in the same bits
+    vs_plain = None
+    if not args.plain and not args.no_plain and not is_batch(w):
+        sp = plain_variant(w).build()
+        sp.first_iteration()
+        sp.step(pre + args.warmup)
+        torch.cuda.synchronize()
+        msp, rebp, _ = event_timed(sp, args.steps, local, dist)
+        a, b = s.particles(sort_by_id=True), sp.particles(sort_by_id=True)
+        same = all(np.array_equal(np.ascontiguousarray(a[k]).view(np.uint8), np.ascontiguousarray(b[k]).view(np.uint8))
+                   for k in a)
+        msp = allmax(dist, msp)
+        vs_plain = {"value": total / (msp / 1e3), "unit": UNIT, "ms_per_step": msp / args.steps,
+                    "ratio": msp / ms, "rebuilds_in_timed_region": rebp, "same_bits": bool(same),
+                    "path": "plain FP64 operator kernels (one kernel per reference operator, exact two-pass "
+                            "lists, no FP32 screening, no graph), same pre-roll and warm-up"}
+        del a, b
+        sp.close()
 
     # particles whose epilog rotation is exactly zero (no spin, no torque) at the end of the timed run
     pp = s.particles(sort_by_id=False)
@@ -485,30 +607,51 @@ def run_native(args, rank, world, local, dist):
     s.reset_kernel_stats()
     s.profile(True)
     kprof_steps = max(20, args.steps // 4)
+    ni0 = s.interaction_count()
     s.step(kprof_steps)
     prof = s.kernel_stats()
     s.profile(False)
-    ni = s.interaction_count()
+    ni = (ni0 + s.interaction_count()) // 2
     peak, peak_kind = peaks()
+
+    def per_step(keys):
+        return sum(prof[k]["total_ms"] for k in keys if k in prof) / kprof_steps / 1e3
+
     # the contact phase: screen + detect + Hooke law (fused step) or one kernel (plain)
     t_contact = sum(prof[k]["total_ms"] / max(prof[k]["timed"], 1)
                     for k in ("contact_screen", "contact_detect", "contact") if k in prof) / 1e3
-    achieved = CONTACT_BYTES_PER_INTERACTION * ni / t_contact / 1e9
+    achieved_c = CONTACT_BYTES_PER_INTERACTION * ni / t_contact / 1e9 if t_contact > 0 else 0.0
+    t_integ = per_step(("prolog", "epilog"))
+    achieved_i = PARTICLE_BYTES_PER_STEP * w.n / t_integ / 1e9 if t_integ > 0 else 0.0
     step_ms_prof = sum(v["total_ms"] for v in prof.values()) / kprof_steps
-    shares = {k: round(v["total_ms"] / max(sum(x["total_ms"] for x in prof.values()), 1e-9), 4)
-              for k, v in prof.items() if v["total_ms"] > 0}
-    state = s.simulation_state()
+    tot_ms = max(sum(x["total_ms"] for x in prof.values()), 1e-9)
+    shares = {k: round(v["total_ms"] / tot_ms, 4) for k, v in prof.items() if v["total_ms"] > 0}
+    t_i = TRAFFIC["integration_bytes_per_particle"]
+    t_c = TRAFFIC["contact_bytes_per_listed_pair"]
+    roofline = {"bound": "hbm", "kernel": "integration (k_fused_prolog + k_fused_epilog + rotation kernels)",
+                "achieved": achieved_i, "peak": peak, "unit": "GB/s", "frac": achieved_i / peak,
+                "peak_kind": peak_kind, "traffic": (t_i * w.n if t_i else None),
+                "algorithmic_bytes_per_launch": PARTICLE_BYTES_PER_STEP * w.n,
+                "avg_launch_ms": t_integ * 1e3, "share_of_step": round(shares.get("prolog", 0) + shares.get("epilog", 0), 4),
+                "traffic_source": TRAFFIC["source"],
+                "note": "344 B per particle-step (prolog and epilog together, per step); FP64-pipe bound in "
+                        "practice (profiles/)"}
+    roofline_contact = {"bound": "hbm", "kernel": "contact phase (k_cscreen + k_cdetect + k_chooke)",
+                        "achieved": achieved_c, "peak": peak, "unit": "GB/s", "frac": achieved_c / peak,
+                        "traffic": (t_c * ni if t_c else None),
+                        "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni, "interactions": ni,
+                        "avg_launch_ms": t_contact * 1e3}
     mul_mode = s.mul_mode()
     rebuild = rebuild_timing(args, w, s) if args.rebuild_ms > 0 else None
     s.close()
 
-    # end to end through the C ABI from pinned host buffers
+    # end to end through the C ABI from pinned host buffers (the pre-rolled state)
     e2e = None
     if not args.no_e2e:
         from exadem_gb300 import System
 
         pinned = {}
-        host = w.particles() if is_batch(w) else w.particles
+        host = w.particles() if is_batch(w) else host_pre
         for k, v in host.items():
             t = torch.empty(v.shape, dtype=torch.from_numpy(v).dtype, pin_memory=True)
             t.numpy()[:] = v
@@ -532,77 +675,77 @@ def run_native(args, rank, world, local, dist):
         el = allmax(dist, el)
         e2e = {"value": total / el, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                "d2h_bytes_per_step": d2h / args.steps,
-               "note": "context setup, initial state uploaded, first_iteration, K steps, final state read back; "
-                       "all timed"}
+               "note": "context setup, the pre-rolled particle state uploaded from pinned host memory, "
+                       "first_iteration, K steps, final state read back; all timed"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(w)
+        cpu = cpu_baseline(args, w)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded random sequential addition)",
-        "config": {"workload": WORKLOAD_DESC[args.workload] if args.n is None and args.systems == 256
-                   else f"{args.workload} n={w.n}",
-                   "n_particles": w.n,
-                   "path": "plain FP64 operator kernels" if args.plain else
-                           "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division"
-                           + (", whole step replayed as one CUDA graph" if getattr(w.params, "graph_step", 0) else "")
-                           + (f", {w.info['systems']} systems in one context" if is_batch(w) else ""),
-                   "mul_mode": None if args.plain else mul_mode,
-                   "rotation_idle_fraction_at_end": round(idle_fraction, 4),
-                   "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
-                   "parallelism": "replicas" if world > 1 else "single",
-                   "inputs": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in w.info.items()
-                              if k != "counts"}},
-        "roofline": {"bound": "hbm", "kernel": "contact", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                     "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni,
-                     "interactions": ni, "avg_launch_ms": t_contact * 1e3,
-                     "note": "FP64-pipe bound in practice (per-kernel rooflines under profiles/)"},
+        "config": config_block(args, w, pre, preroll_s, bed, mul_mode, idle_fraction),
+        "vs_plain": vs_plain,
+        "roofline": roofline, "roofline_contact": roofline_contact,
         "autotune": ({k: (round(v, 6) if isinstance(v, float) else v) for k, v in tune.items()}
                      if tune else None),
         "learned": learned,
         "kernel_shares": shares, "profiled_ms_per_step": step_ms_prof,
         "rebuilds_in_timed_region": rebuilds, "gpu_launches": launches,
-        "clocks": clk.summary(), "e2e": e2e, "cpu_baseline": cpu,
-        "state_after": {"n_interactions": state["n_interactions"], "n_active": state["n_active_interactions"]},
+        "clocks": clocks, "e2e": e2e, "cpu_baseline": cpu,
+        "state_after_preroll": {"n_interactions": state_pre["n_interactions"],
+                                "n_active": state_pre["n_active_interactions"]},
+        "state_after": {"n_interactions": state_end["n_interactions"], "n_active": state_end["n_active_interactions"]},
         "rebuild_timing": rebuild,
     }
     if rank == 0:
         print(json.dumps(line))
 
 
+def config_block(args, w, pre, preroll_s, bed, mul_mode, idle_fraction):
+    cfg = {"workload": WORKLOAD_DESC[args.workload] if args.n is None and args.systems == 256
+           else f"{args.workload} n={w.n}",
+           "n_particles": w.n,
+           "path": "plain FP64 operator kernels" if args.plain else
+                   "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division"
+                   + (", whole step replayed as one CUDA graph" if getattr(w.params, "graph_step", 0) else "")
+                   + (f", {w.info['systems']} systems in one context" if is_batch(w) else ""),
+           "preroll_steps": pre, "preroll_s": round(preroll_s, 2),
+           "timed_window": f"steps {pre + args.warmup + 1}..{pre + args.warmup + args.steps} after first_iteration",
+           "mul_mode": None if args.plain else mul_mode,
+           "rotation_idle_fraction_at_end": round(idle_fraction, 4),
+           "l2": "inputs larger than L2 (particle state 0.5 GB, interactions > 0.5 GB)",
+           "parallelism": "replicas" if args.gpus > 1 else "single",
+           "inputs": {k: (round(v, 4) if isinstance(v, float) else v) for k, v in w.info.items() if k != "counts"}}
+    if bed:
+        cfg["bed"] = {**bed, "phi_target": 0.55,
+                      "note": "solid fraction of the bed the pre-roll deposited (the RSA initial state jams "
+                              "below 0.38)"}
+    return cfg
+
+
 def run_reference(args, rank, world, local, dist):
+    """The reference arm: the oracle (C++ restatement of exaDEM's CPU path,
+    pinned function by function against exaDEM's own headers; exaDEM itself
+    cannot be built without exaNBody/onika/MPI) on all host cores, timed on a
+    bounded sample of the native arm's workload (cpu_sample)."""
     if rank != 0:
         return
-    from oracle.oracle import oracle_system, set_threads
-
-    cores = set_threads(os.cpu_count() or 1)
     w = workload(args)
-    if is_batch(w):
-        cb = cpu_baseline(w, budget_s=60.0)
-        steps, v = 10, cb["value"]
-        el = w.n * steps / v
-        sample = cb["sample"] + " (C++ restatement of the reference CPU path, one drum at a time)"
-    else:
-        o = w.build(oracle_system)
-        o.first_iteration()
-        o.step(max(1, min(args.warmup, 3)))
-        steps = max(1, min(args.steps, 20))
-        t0 = time.perf_counter()
-        o.step(steps)
-        el = time.perf_counter() - t0
-        v = w.n * steps / el
-        sample = (f"{steps} steps of the full workload (C++ restatement of the reference "
-                  f"CPU path; exaDEM itself cannot be built without exaNBody/onika/MPI)")
+    cb = cpu_sample(args, w, max_steps=max(1, args.steps), budget_s=60.0)
+    v = cb["value"]
+    steps = cb["steps"]
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": steps, "warmup": args.warmup,
-            "ms_per_step": el * 1e3 / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded random sequential addition)", "impl": "reference",
-            "config": {"workload": WORKLOAD_DESC[args.workload] if args.n is None else f"{args.workload} n={w.n}",
-                       "n_particles": w.n},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "ms_per_step": cb["seconds"] * 1e3 / steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random sequential addition)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD_DESC[args.workload] if args.n is None and args.systems == 256
+                       else f"{args.workload} n={w.n}",
+                       "n_particles": w.n, "preroll_steps": preroll_steps(args)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": cb["kind"],
+                             "sample": cb["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
