@@ -22,7 +22,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .workloads import build_obb
+from .workloads import build_obb, max_rcut
 
 
 class _Stream:
@@ -122,7 +122,7 @@ def _read_one(st: _Stream) -> dict:
             raise ValueError(f".shp: shape {name!r}: face {f} refers to a missing vertex")
     return {"name": name, "vertices": v, "edges": np.asarray(edges, dtype=np.int32).reshape(-1, 2),
             "faces": faces, "radius": radius, "obb": build_obb(v, radius), "volume": volume,
-            "i_over_m": tuple(iom), "max_rcut": float(max(np.linalg.norm(x) for x in v) + radius)}
+            "i_over_m": tuple(iom), "max_rcut": max_rcut(v, radius)}
 
 
 def parse_shps(text: str) -> list[dict]:

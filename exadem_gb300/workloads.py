@@ -53,6 +53,64 @@ class Workload:
         return s
 
 
+def save_workload(w: Workload, path) -> None:
+    """A workload in one .npz file: particle arrays, parameters, drivers, shapes, meshes."""
+    import json
+
+    meta = {"name": w.name, "steps": w.steps, "surfaces": w.surfaces, "cylinders": w.cylinders,
+            "info": {k: v for k, v in w.info.items() if isinstance(v, (int, float, str, list, dict, bool))},
+            "params": {f: (list(getattr(w.params, f)) if hasattr(getattr(w.params, f), "__len__") else
+                           getattr(w.params, f)) for f, _ in A.Params._fields_ if f not in ("config", "config_driver")},
+            "config": {f: getattr(w.params.config, f) for f, _ in A.ContactParams._fields_},
+            "config_driver": {f: getattr(w.params.config_driver, f) for f, _ in A.ContactParams._fields_},
+            "shapes": [], "meshes": []}
+    arrays = {f"p/{k}": np.asarray(v) for k, v in w.particles.items()}
+    for k, s in enumerate(w.shapes or []):
+        meta["shapes"].append({"name": s["name"], "radius": s["radius"], "volume": s["volume"],
+                               "i_over_m": list(np.atleast_1d(s["i_over_m"]).astype(float)), "faces": s["faces"]})
+        arrays[f"s{k}/vertices"] = np.asarray(s["vertices"], dtype=np.float64)
+        arrays[f"s{k}/edges"] = np.asarray(s["edges"], dtype=np.int32)
+    for k, m in enumerate(w.meshes):
+        meta["meshes"].append({"faces": [list(map(int, f)) for f in m["faces"]], "minkowski": m["minkowski"],
+                               "center": list(m.get("center", (0, 0, 0))), "quat": list(m.get("quat", (1, 0, 0, 0)))})
+        arrays[f"m{k}/vertices"] = np.asarray(m["vertices"], dtype=np.float64)
+        arrays[f"m{k}/edges"] = np.asarray(m["edges"], dtype=np.int32)
+    arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(path, **arrays)
+
+
+def load_workload(path) -> Workload:
+    """The workload save_workload wrote."""
+    import json
+
+    z = np.load(path)
+    meta = json.loads(z["meta"].tobytes().decode())
+    p = A.Params()
+    for f, v in meta["params"].items():
+        cur = getattr(p, f)
+        if hasattr(cur, "__len__"):
+            cur[:] = v
+        else:
+            setattr(p, f, v)
+    p.config = contact_params(**meta["config"])
+    p.config_driver = contact_params(**meta["config_driver"])
+    parts = {k[2:]: np.ascontiguousarray(z[k]) for k in z.files if k.startswith("p/")}
+    shapes = []
+    for k, s in enumerate(meta["shapes"]):
+        iom = s["i_over_m"]
+        shapes.append(_shape(s["name"], z[f"s{k}/vertices"], z[f"s{k}/edges"], s["faces"], s["radius"], s["volume"],
+                             tuple(iom) if len(iom) == 3 else iom[0]))
+    meshes = [dict(vertices=z[f"m{k}/vertices"], edges=z[f"m{k}/edges"], faces=m["faces"], minkowski=m["minkowski"],
+                   center=tuple(m["center"]), quat=tuple(m["quat"])) for k, m in enumerate(meta["meshes"])]
+    w = Workload(meta["name"], p, parts, surfaces=[{k: (tuple(v) if isinstance(v, list) else v) for k, v in d.items()}
+                                                   for d in meta["surfaces"]],
+                 cylinders=[{k: (tuple(v) if isinstance(v, list) else v) for k, v in d.items()}
+                            for d in meta["cylinders"]],
+                 meshes=meshes, steps=meta["steps"], info=meta["info"])
+    w.shapes = shapes or None
+    return w
+
+
 def rsa(n, rmin, rmax, density, lo, hi, periodic=(0, 0, 0), grow_axis=-1, seed=1, vmin=0.0, vmax=0.0,
         region=0, cyl_center=(0.0, 0.0), cyl_radius=0.0, max_attempts=64, id_offset=0, radii=None):
     lib = A.load_workloads()
@@ -368,7 +426,15 @@ def _shape(name, vertices, edges, faces, radius, volume, i_over_m):
     v = np.asarray(vertices, dtype=np.float64)
     return {"name": name, "vertices": v, "edges": np.asarray(edges, dtype=np.int32), "faces": faces,
             "radius": radius, "obb": build_obb(v, radius), "volume": volume, "i_over_m": i_over_m,
-            "max_rcut": float(max(np.linalg.norm(x) for x in v) + radius)}
+            "max_rcut": max_rcut(v, radius)}
+
+
+def max_rcut(vertices, radius) -> float:
+    """shape::compute_max_rcut (shape.hpp:479-489): max over vertices of |v| + radius."""
+    rc = 0.0
+    for x, y, z in np.asarray(vertices, dtype=np.float64).tolist():
+        rc = max(rc, math.sqrt(x * x + y * y + z * z) + radius)
+    return rc
 
 
 def shape_cube(a=1.0, radius=0.01):

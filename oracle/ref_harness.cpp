@@ -217,6 +217,17 @@ int ref_shape_arrays(int s, double* vertices, int32_t* edges, int32_t* faces, do
   return 0;
 }
 
+/* Derived shape quantities set_fields uses (set_fields.cu:296-300): compute_max_rcut
+ * (shape.hpp:479-489), get_volume(h) (:145-148) and get_Im(h) (:163-164).
+ * out (5): max_rcut, volume(h), I/m(h)[3] */
+int ref_shape_derived(int s, double h, double* out) {
+  const exaDEM::shape& sh = g_shapes[s];
+  out[0] = sh.compute_max_rcut();
+  out[1] = sh.get_volume(h);
+  put(out + 2, sh.get_Im(h));
+  return 0;
+}
+
 /* shape::get_vertex (shape.hpp:245-262): p + Q * (h * v0).
  * in (11): p[3], Q[4], h, v0[3] (the shape's vertex is replaced by v0).  out (3) */
 int ref_unit_world_vertex(long n, const double* in, double* out) {

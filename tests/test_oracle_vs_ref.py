@@ -108,6 +108,14 @@ def test_shp_reader_and_shape_obb(libs):
                 assert same_bits(np.atleast_2d(r[k]), np.atleast_2d(m[k])).all(), (f, k)
             for k in ("center", "e1", "e2", "e3", "extent"):
                 assert same_bits(np.atleast_2d(r["obb"][k]), np.atleast_2d(m["obb"][k])).all(), (f, "obb", k)
+            # the quantities set_fields takes from the shape (radius, mass and inertia of a polyhedron)
+            ref.ref_shape_derived.argtypes = [C.c_int, C.c_double, C.POINTER(C.c_double)]
+            for h in (1.0, 0.8, 1.3):
+                d = np.zeros(5)
+                ref.ref_shape_derived(r["index"], h, d.ctypes.data_as(C.POINTER(C.c_double)))
+                iom = m["i_over_m"]
+                mine = np.array([m["max_rcut"], h * h * h * m["volume"], h * h * iom[0], h * h * iom[1], h * h * iom[2]])
+                assert same_bits(d[None], mine[None]).all(), (f, h)
     assert nshapes >= 40
 
 
