@@ -209,10 +209,21 @@ extern "C" int dem_register_mesh(dem_ctx* c, const dem_mesh* s) {
   d.kind = 2;
   d.mesh = (int)c->meshes.size();
   for (int k = 0; k < 3; k++) d.center[k] = s->center[k];  // driver.position(); velocities 0 (STATIONARY)
+  const int ndrv0 = c->ndrv;
   c->meshes.push_back(m);
   MeshStore& mm = c->meshes.back();
   mm.dev.boff = nullptr;  // built by the next neighbour pass (ensure_mesh_bins)
   int rc = upload_mesh_table(c);
-  if (rc) return rc;
-  return ext_add_driver(c, d);
+  if (rc == DEM_OK) rc = ext_add_driver(c, d);
+  if (rc && c->ndrv == ndrv0) {
+    // the driver was not added: take the mesh back out so that no mesh is left without its driver
+    MeshStore gone = c->meshes.back();
+    c->meshes.pop_back();
+    cudaFree(gone.vtx);
+    cudaFree(gone.e);
+    cudaFree(gone.fo);
+    cudaFree(gone.fv);
+    upload_mesh_table(c);
+  }
+  return rc;
 }

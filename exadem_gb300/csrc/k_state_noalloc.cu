@@ -10,16 +10,20 @@
 // device array below, sized for DEM_STATE_NOALLOC_MAX_PARTICLES particles.
 // Every GPU that loads the library holds this array until the process exits.
 //
-// Set-up: the first call on a device, with that device current, looks up the
-// array's device address with cudaGetSymbolAddress (checked) and caches it.
-// Make that first call before any stream capture on the device.
+// Set-up: every call, with the device current, looks up the array's device
+// address with cudaGetSymbolAddress (checked).  Looking it up each time keeps
+// the address right on every device and after a cudaDeviceReset, which reloads
+// the module.  The first call on a device also loads the module's device code,
+// so make it before any stream capture on that device.
+//
+// A CUDA error still pending from earlier work of the caller is not taken as
+// this call's: the call then returns DEM_ERR_CUDA without launching anything
+// and leaves the error for the caller to read.
 //
 // Calls share the array and it keeps the last call's contents.  Every partial
 // read by a call is first written by the same call, so nothing has to start at
 // zero; but two calls whose kernels overlap on the GPU (different streams, no
 // ordering between them) race on the array and give wrong results.
-#include <mutex>
-
 #include "dem_ctx.cuh"
 
 namespace {
@@ -31,10 +35,6 @@ static_assert(DEM_STATE_NOALLOC_MAX_PARTICLES % NA_TILE == 0, "tile must divide 
 
 // 7 partial sums (kinetic xyz, rotation xyz, mass) per block: 448 KiB.
 static __device__ __align__(256) double g_state_noalloc_partials[7 * NA_MAX_BLOCKS];
-
-constexpr int NA_MAX_DEVICES = 64;
-std::mutex g_mutex;
-double* g_scratch[NA_MAX_DEVICES] = {};
 
 __global__ void k_na_partial(const double* __restrict__ vx, const double* __restrict__ vy,
                              const double* __restrict__ vz, const double* __restrict__ wx,
@@ -78,18 +78,13 @@ __global__ void k_na_final(const double* __restrict__ part, uint64_t nb, double*
   }
 }
 
-// Device address of the scratch array on the current device (set up once per device).
+// Device address of the scratch array on the current device.
 int scratch_for_current_device(double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DEM_ERR_NO_DEVICE;
-  if (dev < 0 || dev >= NA_MAX_DEVICES) return DEM_ERR_UNSUPPORTED;
-  std::lock_guard<std::mutex> lock(g_mutex);
-  if (!g_scratch[dev]) {
-    double* ptr = nullptr;
-    if (cudaGetSymbolAddress((void**)&ptr, g_state_noalloc_partials) != cudaSuccess || !ptr) return DEM_ERR_CUDA;
-    g_scratch[dev] = ptr;
-  }
-  *out = g_scratch[dev];
+  double* ptr = nullptr;
+  if (cudaGetSymbolAddress((void**)&ptr, g_state_noalloc_partials) != cudaSuccess || !ptr) return DEM_ERR_CUDA;
+  *out = ptr;
   return DEM_OK;
 }
 }  // namespace
@@ -99,6 +94,7 @@ extern "C" int dem_simulation_state_noalloc(const dem_particles* dev, double* de
   if (dev->n > DEM_STATE_NOALLOC_MAX_PARTICLES) return DEM_ERR_INVALID_ARG;  // beyond the scratch array
   if (!dev->vx || !dev->vy || !dev->vz || !dev->vrotx || !dev->vroty || !dev->vrotz || !dev->mass)
     return DEM_ERR_INVALID_ARG;
+  if (cudaPeekAtLastError() != cudaSuccess) return DEM_ERR_CUDA;  // an earlier error of the caller, left pending
   double* part = nullptr;
   int rc = scratch_for_current_device(&part);
   if (rc) return rc;

@@ -130,9 +130,37 @@ inline int build(const Input& m, double rad, double skin, Output& out) {
     span = std::max(span, std::max(b.hi[0] - b.lo[0], std::max(b.hi[1] - b.lo[1], b.hi[2] - b.lo[2])));
     box.push_back(b);
   }
+  // The face filter (filter_vertex_face) projects on the plane through the face's
+  // first, second and last vertices.  A point it keeps lies within E of that
+  // plane above the projected polygon, hence within E + flat[k] of the fan of
+  // the face's own triangles, flat[k] being the largest distance of a face
+  // vertex from that plane (0 for a planar face).
+  std::vector<double> flat(nf, 0.0);
   for (int k = 0; k < nf; k++) {
     Box b = empty();
     for (int q = m.fo[k]; q < m.fo[k + 1]; q++) grow(b, V(m.fv[q]));
+    const int b0 = m.fo[k], nvf = m.fo[k + 1] - b0;
+    if (nvf > 3) {
+      const P3 o = V(m.fv[b0]);
+      const P3 u = sub3(V(m.fv[b0 + 1]), o), w = sub3(V(m.fv[b0 + nvf - 1]), o);
+      P3 nn = {u.y * w.z - u.z * w.y, u.z * w.x - u.x * w.z, u.x * w.y - u.y * w.x};
+      const double len = std::sqrt(nn.x * nn.x + nn.y * nn.y + nn.z * nn.z);
+      double dmax = 0.0;
+      if (len > 0.0) {
+        nn = {nn.x / len, nn.y / len, nn.z / len};
+        for (int q = 2; q + 1 < nvf; q++) {
+          const P3 r = sub3(V(m.fv[b0 + q]), o);
+          dmax = std::max(dmax, std::fabs(r.x * nn.x + r.y * nn.y + r.z * nn.z));
+        }
+      } else {  // degenerate first corner: bound by the face's extent
+        for (int d = 0; d < 3; d++) dmax = std::max(dmax, b.hi[d] - b.lo[d]);
+      }
+      flat[k] = dmax * (1.0 + 1e-12);
+    }
+    for (int d = 0; d < 3; d++) {
+      b.lo[d] -= flat[k];
+      b.hi[d] += flat[k];
+    }
     box.push_back(b);
   }
   const double margin = 1e-7 * (E + amax + span) + 1e-12;
@@ -177,7 +205,7 @@ inline int build(const Input& m, double rad, double skin, Output& out) {
     }
     const int f = (int)(k - nv - ne), b0 = m.fo[f], nvf = m.fo[f + 1] - b0;
     for (int q = 1; q + 1 < nvf; q++)
-      if (tri_dist(ctr, V(m.fv[b0]), V(m.fv[b0 + q]), V(m.fv[b0 + q + 1])) <= reach) return true;
+      if (tri_dist(ctr, V(m.fv[b0]), V(m.fv[b0 + q]), V(m.fv[b0 + q + 1])) <= reach + flat[f]) return true;
     return false;
   };
   auto for_bins = [&](size_t k, auto&& f) {

@@ -453,8 +453,11 @@ int dem_reset_kernel_stats(dem_ctx* ctx);
  *   dev_out: device array of 7 doubles, written in the order
  *            kinetic_energy x,y,z, rotation_energy x,y,z, mass;
  *   stream:  cudaStream_t (NULL = legacy default stream); asynchronous.
- * The first call on a device looks up the scratch address (make it before any
- * stream capture).  Calls share the scratch: calls that overlap on the GPU race. */
+ * Every call looks up the scratch address on the current device; the first
+ * call on a device also loads the device code (make it before any stream
+ * capture).  A CUDA error pending from the caller's earlier work makes the
+ * call return DEM_ERR_CUDA without launching.  Calls share the scratch: calls
+ * that overlap on the GPU race. */
 #define DEM_STATE_NOALLOC_MAX_PARTICLES 16777216ull
 int dem_simulation_state_noalloc(const dem_particles* dev, double* dev_out, void* stream);
 

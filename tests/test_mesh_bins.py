@@ -94,3 +94,35 @@ def test_bins_hold_every_candidate(mb, case):
             assert want in set(buf[:n]), (int(it["type"][k]), int(it["partner_sub"][k]))
     finally:
         mb.mb_free(h)
+
+
+def test_nonplanar_face_in_bins(mb, oracle_lib):
+    """A non-planar quad: every point the reference's face filter keeps (it projects on
+    the plane of the first, second and last vertex) is in a bin listing the face."""
+    from oracle import units as U
+
+    h_warp = 0.6
+    mesh = {"vertices": [[0, 0, 0], [2, 0, 0], [2, 2, h_warp], [0, 2, 0]], "edges": [[0, 1], [1, 2], [2, 3], [3, 0]],
+            "faces": [[0, 1, 2, 3]], "minkowski": 0.02}
+    rad, skin = 0.3, 0.1
+    hb = _bins(mb, mesh, rad, skin)
+    rng = np.random.default_rng(5)
+    pts = rng.uniform([-0.5, -0.5, -0.6], [2.5, 2.5, 1.2], (40000, 3))
+    rows = np.zeros((len(pts), 6 + 12))
+    rows[:, 0] = skin
+    rows[:, 1:4] = pts
+    rows[:, 4] = rad
+    rows[:, 5] = 1.0
+    rows[:, 6:] = np.asarray(mesh["vertices"], dtype=np.float64).reshape(-1)
+    shape = {"vertices": np.asarray(mesh["vertices"], dtype=np.float64), "faces": mesh["faces"],
+             "radius": mesh["minkowski"]}
+    keep = U.run_vertex_face_oracle(oracle_lib, shape, 0, rows)[:, 0] > 0
+    assert keep.sum() > 1000
+    buf = (C.c_uint32 * 4096)()
+    face_item = (2 << 30) | 0
+    try:
+        for x, y, z in pts[keep]:
+            n = mb.mb_items(hb, x, y, z, buf, 4096)
+            assert face_item in set(buf[:n]), (x, y, z)
+    finally:
+        mb.mb_free(hb)
