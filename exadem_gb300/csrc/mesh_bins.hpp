@@ -256,7 +256,7 @@ inline int build(const Input& m, double rad, double skin, Output& out) {
     for (int q = 0; q < nvf; q++) cgm = axpy(cgm, 1.0 / nvf, V(m.fv[b0 + q]));
     double r = 0.0;
     for (int q = 0; q < nvf; q++) r = std::max(r, dist3(cgm, V(m.fv[b0 + q])));
-    put((size_t)nv + ne + f, cgm, r);
+    put((size_t)nv + ne + f, cgm, r + flat[f]);  // the filter's projected polygon lies within flat[f] of the face
   }
   return OK;
 }

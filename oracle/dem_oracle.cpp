@@ -1128,6 +1128,28 @@ bool mesh_detect(const Oracle& o, const Inter& it, const V3& ri, double rad, dou
 // radius) meets the particle's OBB (rotated and translated, homothety not
 // applied) enlarged by rVerlet.  The type 9 gate of the reference (face OBB
 // against the vertex box) holds whenever the face filter passes.
+// Largest distance of a face's vertices from the plane through its first,
+// second and last vertex, the plane filter_vertex_face projects on (0 for a
+// planar face; the face's extent when that corner is degenerate).
+double face_flatness(const std::vector<V3>& w, const std::vector<int>& f) {
+  const int nvf = (int)f.size();
+  if (nvf <= 3) return 0.0;
+  const V3 o = w[f[0]];
+  V3 nn = cross(w[f[1]] - o, w[f[nvf - 1]] - o);
+  const double len = norm(nn);
+  double dmax = 0.0;
+  if (len > 0.0) {
+    nn = nn / len;
+    for (int q = 2; q + 1 < nvf; q++) dmax = std::max(dmax, std::fabs(dot(w[f[q]] - o, nn)));
+  } else {
+    for (int q = 1; q < nvf; q++) dmax = std::max(dmax, norm(w[f[q]] - o));
+  }
+  return dmax * (1.0 + 1e-12);
+}
+
+// Test switch: 1 = the polyhedron-mesh candidates test every mesh feature (no reach prefilter).
+int g_mesh_brute_force = 0;
+
 void poly_mesh_candidates(const Oracle& o, size_t k, size_t a, double rV, std::vector<Inter>& lst) {
   const MeshO& m = o.meshes[o.drivers[k].mesh];
   const PShape& sa = o.shapes[o.type[a]];
@@ -1149,7 +1171,8 @@ void poly_mesh_candidates(const Oracle& o, size_t k, size_t a, double rV, std::v
   // vertices lie within h max|v0| of its centre, its edges extended by rVerlet
   // in their parameter within h max|v0| (1 + 2 rVerlet), every filter range is
   // ra + mr + rVerlet, and a feature lies within its bounding sphere (an edge's
-  // extended by rVerlet in its parameter); skipping them saves time only
+  // extended by rVerlet in its parameter, a face's grown by its flatness, as the
+  // face filter projects on a plane); skipping them saves time only
   const V3 c = pos(o, a);
   double vmax = 0.0;
   for (const V3& v : sa.v) vmax = std::max(vmax, norm(v));
@@ -1166,7 +1189,12 @@ void poly_mesh_candidates(const Oracle& o, size_t k, size_t a, double rV, std::v
     for (int q : m.f[j]) g = g + m.w[q] * (1.0 / (double)m.f[j].size());
     double rf = 0.0;
     for (int q : m.f[j]) rf = std::max(rf, norm(m.w[q] - g));
-    nf_[j] = norm(g - c) <= reach + rf + slack;
+    nf_[j] = norm(g - c) <= reach + rf + face_flatness(m.w, m.f[j]) + slack;
+  }
+  if (g_mesh_brute_force) {
+    std::fill(nv_.begin(), nv_.end(), 1);
+    std::fill(ne_.begin(), ne_.end(), 1);
+    std::fill(nf_.begin(), nf_.end(), 1);
   }
   for (int i = 0; i < sa.nv(); i++) {
     for (int j = 0; j < mnv; j++)
@@ -1621,6 +1649,10 @@ int oracle_set_params(void* h, const dem_params* p) {
       p->cell_size != o.prm.cell_size)
     return DEM_ERR_UNSUPPORTED;
   o.prm = *p;
+  return DEM_OK;
+}
+int oracle_set_mesh_brute_force(int on) {
+  g_mesh_brute_force = on ? 1 : 0;
   return DEM_OK;
 }
 int oracle_set_threads(int n) {

@@ -33,6 +33,7 @@ def load(rebuild: bool = True):
         sig("oracle_stress_tensor", [_CTX, C.POINTER(C.c_double), C.POINTER(C.c_double)])
         sig("oracle_destroy", [_CTX])
         sig("oracle_set_threads", [C.c_int])
+        sig("oracle_set_mesh_brute_force", [C.c_int])
         sig("oracle_last_error", [_CTX], C.c_char_p)
         sig("oracle_set_particles", [_CTX, C.POINTER(A.Particles)])
         sig("oracle_get_particles", [_CTX, C.POINTER(A.Particles)])

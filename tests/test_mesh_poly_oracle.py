@@ -111,3 +111,43 @@ def test_spike_tip_against_the_cube(case):
     assert np.dot(f, away) > 0  # pushed away from the tip
     if len(types) == 1:
         assert math.isclose(np.linalg.norm(f), 1e4 * d, rel_tol=1e-9)
+
+
+@pytest.mark.parametrize("homothety,skin", [(1.0, 0.05), (1.9, 0.05), (0.6, 0.6)])
+def test_prefilter_keeps_every_candidate(oracle_lib, homothety, skin):
+    """The oracle's reach prefilter of polyhedron-mesh candidates removes only
+    features no filter keeps: the lists equal those of testing every feature, for
+    random poses, large homothety and a large skin, on a terrain plus warped quads."""
+    from oracle.oracle import oracle_system
+    from tests.helpers import assert_same_list
+
+    w = W.polyhedra_mesh_terrain(nx=4, ny=4, nz=2, amp=0.5, waves=3, m=8, skin=skin, seed=23)
+    w.particles["homothety"] = np.full(w.n, homothety)
+    w.particles["radius"] = w.particles["radius"] * homothety
+    # a ring of warped quads near the lattice (non-planar faces)
+    quads, verts = [], []
+    for k in range(6):
+        x0 = 1.0 + 1.3 * k
+        base = len(verts)
+        verts += [[x0, 1.0, 2.0], [x0 + 1.2, 1.0, 2.0], [x0 + 1.2, 2.2, 2.0 + 0.5 * (k % 3)], [x0, 2.2, 2.0]]
+        quads.append([base, base + 1, base + 2, base + 3])
+    edges = [[q[i], q[(i + 1) % 4]] for q in quads for i in range(4)]
+    w.meshes.append(dict(vertices=np.asarray(verts, dtype=np.float64), edges=np.asarray(edges, dtype=np.int32),
+                         faces=quads, minkowski=0.02))
+    lists = []
+    for brute in (1, 0):
+        oracle_lib.oracle_set_mesh_brute_force(brute)
+        try:
+            s = w.build(oracle_system)
+            s.first_iteration()
+            out = [s.interactions()]
+            s.step(150)
+            s.update_particle_neighbors()
+            out.append(s.interactions())
+            s.close()
+        finally:
+            oracle_lib.oracle_set_mesh_brute_force(0)
+        lists.append(out)
+    assert sum(int((a["type"] >= 7).sum()) for a in lists[0]) > 0
+    for a, b in zip(*lists):
+        assert_same_list(a, b)
