@@ -198,6 +198,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_simulation_state_systems", [_CTX, C.POINTER(State), C.c_int])
     _sig(lib, "dem_interaction_count", [_CTX, PU64])
     _sig(lib, "dem_get_interactions", [_CTX, C.POINTER(InteractionList)])
+    _sig(lib, "dem_set_interactions", [_CTX, C.POINTER(InteractionList)])
     _sig(lib, "dem_packing_profile", [_CTX, C.c_int, D, D, PD])
     _sig(lib, "dem_profile", [_CTX, C.c_int])
     _sig(lib, "dem_kernel_stats", [_CTX, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)])
@@ -216,7 +217,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_particle_displ_over", "dem_update_particle_neighbors", "dem_reset_force_moment",
             "dem_gravity_force", "dem_contact_sphere", "dem_force_to_accel", "dem_combined_compute_prolog",
             "dem_combined_compute_epilog", "dem_simulation_state", "dem_first_iteration", "dem_step",
-            "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_packing_profile",
+            "dem_rebuild_count", "dem_interaction_count", "dem_get_interactions", "dem_set_interactions", "dem_packing_profile",
             "dem_profile", "dem_kernel_stats", "dem_reset_kernel_stats",
             "dem_simulation_state_noalloc", "dem_selftest_division", "dem_selftest_poly_decisions", "dem_selftest_emu_mul", "dem_selftest_rolling_clip", "dem_set_shapes", "dem_compute_vertices",
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",

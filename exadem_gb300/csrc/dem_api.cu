@@ -8,6 +8,7 @@
 #include <cstring>
 #include <new>
 #include <numeric>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/dem_learned.h"
@@ -1136,6 +1137,118 @@ int dem_interaction_count(dem_ctx* c, uint64_t* out) {
   if (!c || !out) return DEM_ERR_INVALID_ARG;
   *out = c->ni;
   return DEM_OK;
+}
+
+// read_dump_particle_interaction: the history of a saved list, installed as the
+// previous list of the particles currently set, for the next build to carry over
+int dem_set_interactions(dem_ctx* c, const dem_interaction_list* l) {
+  if (!c || !l) return DEM_ERR_INVALID_ARG;
+  const uint64_t m = l->count, n = c->n;
+  if (m && (!l->owner_id || !l->partner_id || !l->type || !l->swap || !l->owner_sub || !l->partner_sub ||
+            !l->friction || !l->moment))
+    return c->fail(DEM_ERR_INVALID_ARG, "set_interactions: every array of the list is needed");
+  if (m >= (1ull << 31)) return c->fail(DEM_ERR_INVALID_ARG, "set_interactions: too many interactions");
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  std::vector<uint64_t> id(n);
+  if (n) DEM_CUDA_TRY(c, cudaMemcpy(id.data(), c->P[c->pcur].id, n * 8, cudaMemcpyDeviceToHost));
+  std::unordered_map<uint64_t, uint32_t> slot;
+  slot.reserve(n * 2 + 1);
+  for (uint64_t s2 = 0; s2 < n; s2++)
+    if (!slot.emplace(id[s2], (uint32_t)s2).second) return c->fail(DEM_ERR_INVALID_ARG, "set_interactions: duplicate particle id");
+  auto driver_base = [&](uint32_t sl) -> uint64_t {  // inverse of dem_get_interactions' per-system driver index
+    if (c->systems.empty()) return 0;
+    size_t lo = 0, hi = c->systems.size() - 1;
+    while (lo < hi) {
+      const size_t mid = (lo + hi + 1) / 2;
+      if (c->systems[mid].first <= sl)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    return (uint64_t)c->systems[lo].driver_first;
+  };
+  struct Row {
+    uint32_t owner, partner, meta, sub;
+    uint64_t pid;
+    double h[6];
+  };
+  std::vector<Row> rows(m);
+  for (uint64_t k = 0; k < m; k++) {
+    const auto it = slot.find(l->owner_id[k]);
+    if (it == slot.end()) return c->fail(DEM_ERR_INVALID_ARG, "set_interactions: owner id is not a particle");
+    Row& r = rows[k];
+    r.owner = it->second;
+    const uint32_t t = l->type[k];
+    const bool drv = t == DEM_ITYPE_VERTEX_CYLINDER || t == DEM_ITYPE_VERTEX_SURFACE ||
+                     (t >= DEM_ITYPE_VERTEX_MESH_VERTEX && t <= DEM_ITYPE_MESH_VERTEX_FACE);
+    if (drv) {
+      r.pid = l->partner_id[k] + driver_base(r.owner);
+      if (r.pid >= (uint64_t)c->ndrv) return c->fail(DEM_ERR_INVALID_ARG, "set_interactions: unknown driver");
+      r.partner = (uint32_t)r.pid;
+    } else {
+      const auto jt = slot.find(l->partner_id[k]);
+      if (jt == slot.end()) return c->fail(DEM_ERR_INVALID_ARG, "set_interactions: partner id is not a particle");
+      r.pid = l->partner_id[k];
+      r.partner = jt->second;
+    }
+    r.meta = (t & 0xffu) | ((uint32_t)(l->swap[k] & 1u) << 15);
+    const uint32_t ps = l->partner_sub[k] == 0xffffffffu ? 0xffffu : (l->partner_sub[k] & 0xffffu);
+    r.sub = (l->owner_sub[k] & 0xffffu) | (ps << 16);
+    for (int d = 0; d < 3; d++) {
+      r.h[d] = l->friction[3 * k + d];
+      r.h[3 + d] = l->moment[3 * k + d];
+    }
+  }
+  // the order the builds' binary searches assume inside an owner: spheres (partner id, type, sub),
+  // polyhedra (partner id, type, swap, owner sub, partner sub)
+  auto skey = [](const Row& r) {
+    return ((uint64_t)(r.meta & 0xffu) << 48) | ((uint64_t)((r.meta >> 15) & 1u) << 40) |
+           ((uint64_t)(r.sub & 0xffffu) << 20) | (uint64_t)(r.sub >> 16);
+  };
+  const bool poly = c->poly;
+  std::stable_sort(rows.begin(), rows.end(), [&](const Row& a, const Row& b) {
+    if (a.owner != b.owner) return a.owner < b.owner;
+    if (a.pid != b.pid) return a.pid < b.pid;
+    if (poly) return skey(a) < skey(b);
+    if ((a.meta & 0xffu) != (b.meta & 0xffu)) return (a.meta & 0xffu) < (b.meta & 0xffu);
+    return a.sub < b.sub;
+  });
+  const int b = c->icur;
+  int rc = alloc_iarrays(c, b, m);
+  if (rc) return rc;
+  std::vector<uint32_t> owner(m), partner(m), meta(m), sub(m), off(n + 1, 0);
+  std::vector<uint64_t> pid(m);
+  std::vector<double> h[6];
+  for (int q = 0; q < 6; q++) h[q].resize(m);
+  for (uint64_t k = 0; k < m; k++) {
+    owner[k] = rows[k].owner;
+    partner[k] = rows[k].partner;
+    meta[k] = rows[k].meta;
+    sub[k] = rows[k].sub;
+    pid[k] = rows[k].pid;
+    for (int q = 0; q < 6; q++) h[q][k] = rows[k].h[q];
+    off[rows[k].owner + 1]++;
+  }
+  for (uint64_t s2 = 0; s2 < n; s2++) off[s2 + 1] += off[s2];
+  const IArrays& I = c->I[b];
+  if (m) {
+    DEM_CUDA_TRY(c, cudaMemcpy(I.owner, owner.data(), m * 4, cudaMemcpyHostToDevice));
+    DEM_CUDA_TRY(c, cudaMemcpy(I.partner, partner.data(), m * 4, cudaMemcpyHostToDevice));
+    DEM_CUDA_TRY(c, cudaMemcpy(I.meta, meta.data(), m * 4, cudaMemcpyHostToDevice));
+    DEM_CUDA_TRY(c, cudaMemcpy(I.sub, sub.data(), m * 4, cudaMemcpyHostToDevice));
+    DEM_CUDA_TRY(c, cudaMemcpy(I.pid, pid.data(), m * 8, cudaMemcpyHostToDevice));
+    for (int d = 0; d < 3; d++) {
+      DEM_CUDA_TRY(c, cudaMemcpy(I.ft[d], h[d].data(), m * 8, cudaMemcpyHostToDevice));
+      DEM_CUDA_TRY(c, cudaMemcpy(I.mo[d], h[3 + d].data(), m * 8, cudaMemcpyHostToDevice));
+    }
+    DEM_CUDA_TRY(c, cudaMemset(I.damp, 0, m * 8));
+  }
+  DEM_CUDA_TRY(c, cudaMemcpy(c->own_off[b], off.data(), (n + 1) * 4, cudaMemcpyHostToDevice));
+  c->ni = m;
+  c->gen++;
+  c->have_list = false;  // the next build makes the list; this one only holds the history
+  c->hist_valid = true;
+  return mark_all_triggered(c);
 }
 
 int dem_get_interactions(dem_ctx* c, dem_interaction_list* l) {

@@ -360,6 +360,23 @@ class System:
         out["moment"] = out["moment"].reshape(-1, 3)
         return out
 
+    def set_interactions(self, lst: dict) -> None:
+        """read_dump_particle_interaction's restore: the history of a saved list
+        (a dict as interactions() returns) for the next neighbour build."""
+        m = len(lst["owner_id"])
+        a = {"owner_id": np.ascontiguousarray(lst["owner_id"], dtype=np.uint64),
+             "partner_id": np.ascontiguousarray(lst["partner_id"], dtype=np.uint64),
+             "type": np.ascontiguousarray(lst["type"], dtype=np.uint16),
+             "swap": np.ascontiguousarray(lst["swap"], dtype=np.uint8),
+             "owner_sub": np.ascontiguousarray(lst["owner_sub"], dtype=np.uint32),
+             "partner_sub": np.ascontiguousarray(lst["partner_sub"], dtype=np.uint32),
+             "friction": np.ascontiguousarray(np.asarray(lst["friction"], dtype=np.float64).reshape(-1)),
+             "moment": np.ascontiguousarray(np.asarray(lst["moment"], dtype=np.float64).reshape(-1))}
+        st = A.InteractionList(m, m, A.ptr(a["owner_id"], A.PU64), A.ptr(a["partner_id"], A.PU64),
+                               A.ptr(a["type"], A.PU16), A.ptr(a["swap"], A.PU8), A.ptr(a["owner_sub"], A.PU32),
+                               A.ptr(a["partner_sub"], A.PU32), A.ptr(a["friction"]), A.ptr(a["moment"]))
+        self._check(self.b.set_interactions(self.h, C.byref(st)), "set_interactions")
+
     # ---------------------------------------------------------- profiling
     def profile(self, enable: bool = True) -> None:
         self._check(self.b.profile(self.h, int(enable)), "profile")

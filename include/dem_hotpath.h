@@ -390,6 +390,18 @@ int dem_rebuild_count(dem_ctx* ctx, uint64_t* out);
 /* ---- analysis / parity readback ------------------------------------------ */
 int dem_interaction_count(dem_ctx* ctx, uint64_t* out);
 int dem_get_interactions(dem_ctx* ctx, dem_interaction_list* out);
+/* read_dump_particle_interaction (src/io/sim_dump_reader_interaction.cpp:56-63):
+ * restart from a checkpoint.  Installs the friction/moment history of a saved
+ * list (rows as dem_get_interactions writes them, count = rows) for the
+ * particles currently set, matched by id; the next neighbour build carries it
+ * over by InteractionPair key, as a rebuild of a running context does.  To
+ * resume a run: dem_set_particles with the saved state (f holding the
+ * accelerations of the saved step), dem_set_interactions with the saved list,
+ * dem_update_particle_neighbors, then dem_step: the run continues with the
+ * same bits as if it had not stopped (no dem_first_iteration, whose forces
+ * would replace the saved accelerations).  Call it after dem_set_particles
+ * and after registering the drivers.                                       */
+int dem_set_interactions(dem_ctx* ctx, const dem_interaction_list* list);
 /* Packing-fraction profile: solid volume fraction of the spheres in nslabs
  * equal horizontal slabs between zlo and zhi (no reference counterpart;
  * analytic sphere/slab volumes).  out has nslabs entries.                 */

@@ -1873,6 +1873,41 @@ int oracle_interaction_count(void* h, uint64_t* out) {
   *out = ((Oracle*)h)->inter.size();
   return DEM_OK;
 }
+// read_dump_particle_interaction (src/io/sim_dump_reader_interaction.cpp:56-63): the saved
+// list becomes the list the next rebuild carries history from, by key.
+int oracle_set_interactions(void* h, const dem_interaction_list* l) {
+  Oracle& o = *(Oracle*)h;
+  std::vector<int32_t> idx_of;
+  std::vector<std::pair<uint64_t, int32_t>> ids(o.n);
+  for (size_t i = 0; i < o.n; i++) ids[i] = {o.id[i], (int32_t)i};
+  std::sort(ids.begin(), ids.end());
+  auto find = [&](uint64_t id) -> int32_t {
+    auto it = std::lower_bound(ids.begin(), ids.end(), std::make_pair(id, (int32_t)-1));
+    return (it != ids.end() && it->first == id) ? it->second : -1;
+  };
+  std::vector<Inter> lst(l->count);
+  for (uint64_t k = 0; k < l->count; k++) {
+    Inter& it = lst[k];
+    it = Inter{};
+    it.oid = l->owner_id[k];
+    it.pid = l->partner_id[k];
+    it.type = l->type[k];
+    it.swap = l->swap[k];
+    it.osub = l->owner_sub[k];
+    it.psub = l->partner_sub[k];
+    it.oi = find(it.oid);
+    if (it.oi < 0) {
+      o.err = "set_interactions: owner id is not a particle";
+      return DEM_ERR_INVALID_ARG;
+    }
+    it.friction = {l->friction[3 * k], l->friction[3 * k + 1], l->friction[3 * k + 2]};
+    it.moment = {l->moment[3 * k], l->moment[3 * k + 1], l->moment[3 * k + 2]};
+  }
+  std::stable_sort(lst.begin(), lst.end(), key_less);
+  o.inter.swap(lst);
+  o.rec.assign(o.inter.size(), Rec{});
+  return DEM_OK;
+}
 int oracle_get_interactions(void* h, dem_interaction_list* l) {
   Oracle& o = *(Oracle*)h;
   l->count = o.inter.size();

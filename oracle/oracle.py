@@ -50,6 +50,7 @@ def load(rebuild: bool = True):
         sig("oracle_state", [_CTX, C.POINTER(A.State)])
         sig("oracle_interaction_count", [_CTX, A.PU64])
         sig("oracle_get_interactions", [_CTX, C.POINTER(A.InteractionList)])
+        sig("oracle_set_interactions", [_CTX, C.POINTER(A.InteractionList)])
         sig("oracle_packing_profile", [_CTX, C.c_int, C.c_double, C.c_double, A.PD])
         sig("oracle_set_shapes", [_CTX, C.POINTER(A.Shape), C.c_int])
         sig("oracle_compute_vertices", [_CTX])
@@ -68,6 +69,7 @@ class OracleBackend:
             "first_iteration": "oracle_first_iteration", "step": "oracle_step",
             "rebuild_count": "oracle_rebuild_count", "simulation_state": "oracle_state",
             "interaction_count": "oracle_interaction_count", "get_interactions": "oracle_get_interactions",
+            "set_interactions": "oracle_set_interactions",
             "packing_profile": "oracle_packing_profile", "set_shapes": "oracle_set_shapes",
             "contact_polyhedron": "oracle_contact_sphere", "compute_vertices": "oracle_compute_vertices",
             "vertex_displ_over": "oracle_displ_over", "set_multimat": "oracle_set_multimat",
