@@ -92,7 +92,7 @@ class SystemDesc(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("rcut_inc", D), ("cell_size", D), ("block", C.c_int32), ("contact_blocks_per_sm", C.c_int32),
                 ("ms_per_step", D), ("ms_per_step_before", D), ("trials", C.c_int32), ("vmax", C.c_float),
-                ("mul_mode", C.c_int32)]
+                ("mul_mode", C.c_int32), ("fused_contact", C.c_int32)]
 
 
 class ContactState(C.Structure):

@@ -87,6 +87,7 @@ struct dem_ctx {
   // launch shapes chosen by dem_autotune (no effect on results)
   int tune_block = 128;      // threads per block of the fused prolog / epilog (64..256)
   int tune_contact_bps = 8;  // persistent blocks per SM of the compacted contact law
+  bool fuse_contact = true;  // compacted contact: detection and law in one kernel (k_cfused), else two
   int mul_mode = 2;          // multiply placement of the fused integration kernels (integrate_core.cuh)
 
   // graph step (dem_graph.cu)

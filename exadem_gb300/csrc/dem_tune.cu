@@ -52,6 +52,7 @@ struct Saved {
   bool have_list, hist_valid;
   dem_params prm;
   int tune_block, tune_contact_bps, mul_mode;
+  bool fuse_contact;
 };
 
 int save_state(dem_ctx* c, Saved& s) {
@@ -65,6 +66,7 @@ int save_state(dem_ctx* c, Saved& s) {
   s.tune_block = c->tune_block;
   s.tune_contact_bps = c->tune_contact_bps;
   s.mul_mode = c->mul_mode;
+  s.fuse_contact = c->fuse_contact;
   const size_t bytes = pblock_bytes(c) + (c->n + 1) * 4 + c->ni * 80 + 1024;
   DEM_CUDA_TRY(c, cudaMalloc(&s.dev, bytes));
   char* p = static_cast<char*>(s.dev);
@@ -99,6 +101,7 @@ int restore_state(dem_ctx* c, const Saved& s) {
   c->tune_block = s.tune_block;
   c->tune_contact_bps = s.tune_contact_bps;
   c->mul_mode = s.mul_mode;
+  c->fuse_contact = s.fuse_contact;
   if (std::memcmp(&c->prm, &s.prm, sizeof(dem_params))) {
     c->prm = s.prm;
     int rc = ext_setup_grid(c);
@@ -278,6 +281,16 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
       best_mode = mode;
     }
   }
+  bool best_fuse = c->fuse_contact;
+  {  // detection and law of the compacted contact in one kernel or in two (same bits)
+    double cost;
+    c->fuse_contact = !best_fuse;  // the trial restores the saved value after it
+    if ((rc = trial(best_skin, best_cell, best_block, best_bps, best_mode, &cost))) return rc;
+    if (cost < best) {
+      best = cost;
+      best_fuse = !best_fuse;
+    }
+  }
   cudaFree(base.dev);
 
   // apply: launch shapes and cell size keep the current list (they take effect at the
@@ -285,6 +298,7 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
   c->tune_block = best_block;
   c->tune_contact_bps = best_bps;
   c->mul_mode = best_mode;
+  c->fuse_contact = best_fuse;
   const bool skin_changed = best_skin != skin0;
   c->prm.cell_size = best_cell;
   c->prm.rcut_inc = best_skin;
@@ -302,5 +316,6 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
   out->trials = trials;
   out->vmax = vmax;
   out->mul_mode = best_mode;
+  out->fused_contact = best_fuse ? 1 : 0;
   return DEM_OK;
 }

@@ -129,6 +129,91 @@ __global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
   }
 }
 
+// FP64 detection of interaction k; a pair that does not touch, and the cohesive
+// attraction before contact, are finished here.  Returns true for an
+// overlapping pair, whose law is left to the caller with (dn, n, cpos).
+__device__ __forceinline__ bool detect_pair(const CArgs& a, uint32_t k, double& dn, V3& n, V3& cpos) {
+  bool heavy = false;
+  const uint32_t meta = a.I.meta[k];
+  const uint32_t i = a.I.owner[k], j = a.I.partner[k];
+  const V3 ri = ldv(a.P, RX, i);
+  const double rad_i = a.P.f[RAD][i];
+  bool contact;
+  bool is_vv = meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX;
+  V3 rj = mk(0, 0, 0);
+  double dncut;
+  if (is_vv) {
+    rj = partner_pos(a, meta, i, j);
+    const double rad_j = a.P.f[RAD][j];
+    const double R = rad_i + rad_j;
+    const V3 dist = ri - rj;
+    const double dist_norm = vnorm(dist);
+    dn = dist_norm - R;
+    contact = emu_lt0(dn);  // comparisons of this kernel on the integer pipe (emu64.cuh)
+    dncut = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]).dncut;
+    if (contact || (a.cohesive && emu_le(dn, dncut)) || a.cs.dn) {  // n and cpos are used only then
+      const double inv_dist_norm = 1.0 / dist_norm;
+      n = dist * inv_dist_norm;
+      cpos = ri - n * (rad_i + 0.5 * dn);
+    }
+  } else {
+    const DriverDev& d = a.drv[j];
+    if (d.kind == 2) {  // detect<7|8|9> (contact_sphere.hpp:300-396)
+      const DetD q = mesh_detect(a.mesh[d.mesh], meta_type(meta), a.I.sub[k] >> 16, ri, rad_i);
+      dn = q.dn;
+      contact = q.c;
+      n = q.n;
+      cpos = q.cp;
+    } else if (d.kind == 0) {
+      const V3 nrm = mk(d.normal[0], d.normal[1], d.normal[2]);
+      const V3 proj = dot(ri, nrm) * nrm;
+      const V3 s2p = -(mk(d.center_proj[0], d.center_proj[1], d.center_proj[2]) - proj);
+      const double dd = vnorm(s2p);
+      dn = dd - rad_i;
+      contact = !emu_gt0(dn);
+      if (contact) {
+        n = s2p / dd;
+        cpos = ri - n * (rad_i + 0.5 * dn);
+      }
+    } else {
+      const V3 proj = ri * mk(d.axis[0], d.axis[1], d.axis[2]);
+      const V3 dir = mk(d.center[0], d.center[1], d.center[2]) - proj;
+      const double dd = vnorm(dir);
+      dn = d.radius - (rad_i + dd);
+      contact = !emu_gt0(dn);
+      if (contact) {
+        n = dir / dd;
+        cpos = ri - n * (rad_i + 0.5 * dn);
+      }
+    }
+    dncut = a.pt.drv(a.cpd, a.P.group[i], j).dncut;
+  }
+  if (a.cohesive) contact = (contact || emu_le(dn, dncut));
+  const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+  if (!contact) {
+    a.cs.write(k, 0.0, cpos, mk(0, 0, 0), mk(0, 0, 0));  // item.reset(), dn = 0
+    if (a.R.live[k] || a.cs.dn) {
+      const V3 z = mk(0, 0, 0);
+      write_result(a, k, z, z, z, z, z);
+      a.R.live[k] = 0;
+    }
+  } else if (a.cohesive && emu_ge0(dn)) {
+    // cohesive attraction before contact (contact_force.hpp:165-173): f = fn_value n, ft = 0
+    const dem_contact_params& hkp =
+        is_vv ? a.pt.pair(a.cp, a.P.group[i], a.P.group[j]) : a.pt.drv(a.cpd, a.P.group[i], j);
+    const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
+    const V3 f = mk(0, 0, 0) + fn_value * n;
+    const V3 ti = cross(cpos - ri, f) + mo;
+    const V3 tj = is_vv ? cross(cpos - rj, -f) + (-mo) : mk(0, 0, 0);
+    write_result(a, k, mk(0, 0, 0), mo, f, ti, tj);
+    a.R.live[k] = 1;
+    a.cs.write(k, dn, cpos, f - mk(0, 0, 0), mk(0, 0, 0));  // ft = 0 before contact
+  } else {
+    heavy = true;
+  }
+  return heavy;
+}
+
 __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
   const uint64_t n1 = a.cnt[0];
   const uint64_t stride = (uint64_t)gridDim.x * FT;
@@ -140,83 +225,7 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
     V3 n = mk(0, 0, 0), cpos = mk(0, 0, 0);
     if (w < n1) {
       k = a.L1[w];
-      const uint32_t meta = a.I.meta[k];
-      const uint32_t i = a.I.owner[k], j = a.I.partner[k];
-      const V3 ri = ldv(a.P, RX, i);
-      const double rad_i = a.P.f[RAD][i];
-      bool contact;
-      bool is_vv = meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX;
-      V3 rj = mk(0, 0, 0);
-      double dncut;
-      if (is_vv) {
-        rj = partner_pos(a, meta, i, j);
-        const double rad_j = a.P.f[RAD][j];
-        const double R = rad_i + rad_j;
-        const V3 dist = ri - rj;
-        const double dist_norm = vnorm(dist);
-        dn = dist_norm - R;
-        contact = emu_lt0(dn);  // comparisons of this kernel on the integer pipe (emu64.cuh)
-        dncut = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]).dncut;
-        if (contact || (a.cohesive && emu_le(dn, dncut)) || a.cs.dn) {  // n and cpos are used only then
-          const double inv_dist_norm = 1.0 / dist_norm;
-          n = dist * inv_dist_norm;
-          cpos = ri - n * (rad_i + 0.5 * dn);
-        }
-      } else {
-        const DriverDev& d = a.drv[j];
-        if (d.kind == 2) {  // detect<7|8|9> (contact_sphere.hpp:300-396)
-          const DetD q = mesh_detect(a.mesh[d.mesh], meta_type(meta), a.I.sub[k] >> 16, ri, rad_i);
-          dn = q.dn;
-          contact = q.c;
-          n = q.n;
-          cpos = q.cp;
-        } else if (d.kind == 0) {
-          const V3 nrm = mk(d.normal[0], d.normal[1], d.normal[2]);
-          const V3 proj = dot(ri, nrm) * nrm;
-          const V3 s2p = -(mk(d.center_proj[0], d.center_proj[1], d.center_proj[2]) - proj);
-          const double dd = vnorm(s2p);
-          dn = dd - rad_i;
-          contact = !emu_gt0(dn);
-          if (contact) {
-            n = s2p / dd;
-            cpos = ri - n * (rad_i + 0.5 * dn);
-          }
-        } else {
-          const V3 proj = ri * mk(d.axis[0], d.axis[1], d.axis[2]);
-          const V3 dir = mk(d.center[0], d.center[1], d.center[2]) - proj;
-          const double dd = vnorm(dir);
-          dn = d.radius - (rad_i + dd);
-          contact = !emu_gt0(dn);
-          if (contact) {
-            n = dir / dd;
-            cpos = ri - n * (rad_i + 0.5 * dn);
-          }
-        }
-        dncut = a.pt.drv(a.cpd, a.P.group[i], j).dncut;
-      }
-      if (a.cohesive) contact = (contact || emu_le(dn, dncut));
-      const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
-      if (!contact) {
-        a.cs.write(k, 0.0, cpos, mk(0, 0, 0), mk(0, 0, 0));  // item.reset(), dn = 0
-        if (a.R.live[k] || a.cs.dn) {
-          const V3 z = mk(0, 0, 0);
-          write_result(a, k, z, z, z, z, z);
-          a.R.live[k] = 0;
-        }
-      } else if (a.cohesive && emu_ge0(dn)) {
-        // cohesive attraction before contact (contact_force.hpp:165-173): f = fn_value n, ft = 0
-        const dem_contact_params& hkp =
-            is_vv ? a.pt.pair(a.cp, a.P.group[i], a.P.group[j]) : a.pt.drv(a.cpd, a.P.group[i], j);
-        const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
-        const V3 f = mk(0, 0, 0) + fn_value * n;
-        const V3 ti = cross(cpos - ri, f) + mo;
-        const V3 tj = is_vv ? cross(cpos - rj, -f) + (-mo) : mk(0, 0, 0);
-        write_result(a, k, mk(0, 0, 0), mo, f, ti, tj);
-        a.R.live[k] = 1;
-        a.cs.write(k, dn, cpos, f - mk(0, 0, 0), mk(0, 0, 0));  // ft = 0 before contact
-      } else {
-        heavy = true;
-      }
+      heavy = detect_pair(a, k, dn, n, cpos);
     }
     const uint32_t pos = warp_append(heavy, a.cnt + 1);
     if (heavy) {
@@ -237,65 +246,139 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
 // that fast path makes the pair run again on the FP64 pipe from its stored
 // inputs (nothing is written before write_result).
 template <int Mode>
+__device__ __forceinline__ void hooke_pair(const CArgs& a, uint32_t k, double dn, V3 n, V3 cpos) {
+  auto run = [&](auto& mm, V3& ft, V3& mo, V3& f, V3& ti, V3& tj) {
+    const uint32_t meta = a.I.meta[k];
+    const uint32_t i = a.I.owner[k], j = a.I.partner[k];
+    const V3 ri = ldv(a.P, RX, i);
+    ft = mk(a.I.ft[0][k], a.I.ft[1][k], a.I.ft[2][k]);
+    mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+    f = mk(0, 0, 0);
+    tj = mk(0, 0, 0);
+    const V3 vi = ldv(a.P, VX, i);
+    const V3 wi = ldv(a.P, WX, i);
+    if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
+      const V3 rj = partner_pos(a, meta, i, j);
+      const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
+      // the pair's damping coefficient, set when the list was built (k_fill); DMT:
+      // reff = compute_effective_radius (common_kernels.hpp:99-102)
+      double reff = 0.0;
+      if (a.dmt) {
+        const double rad_i = a.P.f[RAD][i], rad_j = a.P.f[RAD][j];
+        reff = mm.mul(rad_i, rad_j) / (rad_i + rad_j);
+      }
+      const dem_contact_params& cp = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]);
+      contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, cp,
+                                                                       a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
+                                                                       rj, vj, wj, a.dmt, reff);
+      ti = cross_m(mm, cpos - ri, f) + mo;
+      tj = cross_m(mm, cpos - rj, -f) + (-mo);
+    } else {
+      const DriverDev& d = a.drv[j];
+      const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
+      const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
+      const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
+      const dem_contact_params& cpd = a.pt.drv(a.cpd, a.P.group[i], j);
+      contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, cpd,
+                                                                       a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
+                                                                       dpos, dvel, dvrot, a.dmt, a.P.f[RAD][i]);
+      ti = cross_m(mm, cpos - ri, f) + mo;
+    }
+  };
+  V3 ft, mo, f, ti, tj;
+  RotMul<Mode> mm;
+  run(mm, ft, mo, f, ti, tj);
+  if (mm.failed()) {
+    asm volatile("" ::: "memory");
+    MulFP64 nm;
+    run(nm, ft, mo, f, ti, tj);
+  }
+  write_result(a, k, ft, mo, f, ti, tj);
+  a.R.live[k] = 1;
+  if (a.cs.dn) a.cs.write(k, dn, cpos, f - ft, ft);
+}
+
+// The Hooke law on the contacts found by k_cdetect.  Mode bit 2 (instance 1):
+// its multiplies on the integer pipe (contact_force_core_m); an operand outside
+// that fast path makes the pair run again on the FP64 pipe from its stored
+// inputs (nothing is written before write_result).
+template <int Mode>
 __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
   const uint64_t n2 = a.cnt[1];
   if (blockIdx.x == 0 && threadIdx.x == 0) *a.n_active = n2;  // every L2 pair overlaps (dn < 0)
   const uint64_t stride = (uint64_t)gridDim.x * FT;
-  for (uint64_t w = (uint64_t)blockIdx.x * FT + threadIdx.x; w < n2; w += stride) {
-    const uint32_t k = a.L2[w];
-    auto run = [&](auto& mm, V3& ft, V3& mo, V3& f, V3& ti, V3& tj) {
-      const double dn = a.D[0][w];
-      const V3 n = mk(a.D[1][w], a.D[2][w], a.D[3][w]);
-      const V3 cpos = mk(a.D[4][w], a.D[5][w], a.D[6][w]);
-      const uint32_t meta = a.I.meta[k];
-      const uint32_t i = a.I.owner[k], j = a.I.partner[k];
-      const V3 ri = ldv(a.P, RX, i);
-      ft = mk(a.I.ft[0][k], a.I.ft[1][k], a.I.ft[2][k]);
-      mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
-      f = mk(0, 0, 0);
-      tj = mk(0, 0, 0);
-      const V3 vi = ldv(a.P, VX, i);
-      const V3 wi = ldv(a.P, WX, i);
-      if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
-        const V3 rj = partner_pos(a, meta, i, j);
-        const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
-        // the pair's damping coefficient, set when the list was built (k_fill); DMT:
-        // reff = compute_effective_radius (common_kernels.hpp:99-102)
-        double reff = 0.0;
-        if (a.dmt) {
-          const double rad_i = a.P.f[RAD][i], rad_j = a.P.f[RAD][j];
-          reff = mm.mul(rad_i, rad_j) / (rad_i + rad_j);
-        }
-        const dem_contact_params& cp = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]);
-        contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, cp,
-                                                                         a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
-                                                                         rj, vj, wj, a.dmt, reff);
-        ti = cross_m(mm, cpos - ri, f) + mo;
-        tj = cross_m(mm, cpos - rj, -f) + (-mo);
-      } else {
-        const DriverDev& d = a.drv[j];
-        const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
-        const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
-        const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
-        const dem_contact_params& cpd = a.pt.drv(a.cpd, a.P.group[i], j);
-        contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, cpd,
-                                                                         a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
-                                                                         dpos, dvel, dvrot, a.dmt, a.P.f[RAD][i]);
-        ti = cross_m(mm, cpos - ri, f) + mo;
-      }
-    };
-    V3 ft, mo, f, ti, tj;
-    RotMul<Mode> mm;
-    run(mm, ft, mo, f, ti, tj);
-    if (mm.failed()) {
-      asm volatile("" ::: "memory");
-      MulFP64 nm;
-      run(nm, ft, mo, f, ti, tj);
-    }
-    write_result(a, k, ft, mo, f, ti, tj);
-    a.R.live[k] = 1;
-    if (a.cs.dn) a.cs.write(k, a.D[0][w], mk(a.D[4][w], a.D[5][w], a.D[6][w]), f - ft, ft);
+  for (uint64_t w = (uint64_t)blockIdx.x * FT + threadIdx.x; w < n2; w += stride)
+    hooke_pair<Mode>(a, a.L2[w], a.D[0][w], mk(a.D[1][w], a.D[2][w], a.D[3][w]), mk(a.D[4][w], a.D[5][w], a.D[6][w]));
+}
+
+// Detection and the Hooke law in one kernel.  The overlapping pairs a block's
+// detection finds wait in shared memory until a full tile of them is ready;
+// then every thread of the block runs the law on one of them, so the FP64
+// warps of the law stay dense as in k_chooke, while the detection results
+// never go through global memory.  Each pair is computed exactly as by
+// k_cdetect + k_chooke and writes only its own records: the same bits.
+// The overlapping pairs are counted into *n_active (zeroed by the launcher).
+template <int Mode>
+__global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_cfused(CArgs a) {
+  __shared__ uint32_t q_k[2 * FT];
+  __shared__ double q_d[7][2 * FT];
+  __shared__ uint32_t q_n, q_tot;
+  if (threadIdx.x == 0) {
+    q_n = 0;
+    q_tot = 0;
   }
+  __syncthreads();
+  const uint64_t n1 = a.cnt[0];
+  const uint64_t stride = (uint64_t)gridDim.x * FT;
+  const int lane = threadIdx.x & 31;
+  for (uint64_t base = (uint64_t)blockIdx.x * FT; base < n1; base += stride) {  // the same trips for the block
+    const uint64_t w = base + threadIdx.x;
+    bool heavy = false;
+    uint32_t k = 0;
+    double dn = 0;
+    V3 n = mk(0, 0, 0), cpos = mk(0, 0, 0);
+    if (w < n1) {
+      k = a.L1[w];
+      heavy = detect_pair(a, k, dn, n, cpos);
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, heavy);
+    uint32_t wb = 0;
+    if (lane == 0 && mask) {
+      wb = atomicAdd(&q_n, (uint32_t)__popc(mask));
+      atomicAdd(&q_tot, (uint32_t)__popc(mask));
+    }
+    wb = __shfl_sync(0xffffffffu, wb, 0);
+    if (heavy) {
+      const uint32_t pos = wb + (uint32_t)__popc(mask & ((1u << lane) - 1u));  // < 2 FT: at most FT - 1 wait
+      q_k[pos] = k;
+      q_d[0][pos] = dn;
+      q_d[1][pos] = n.x;
+      q_d[2][pos] = n.y;
+      q_d[3][pos] = n.z;
+      q_d[4][pos] = cpos.x;
+      q_d[5][pos] = cpos.y;
+      q_d[6][pos] = cpos.z;
+    }
+    __syncthreads();
+    const uint32_t have = q_n;
+    if (have >= FT) {  // a full tile: one pair per thread
+      const uint32_t t = threadIdx.x;
+      hooke_pair<Mode>(a, q_k[t], q_d[0][t], mk(q_d[1][t], q_d[2][t], q_d[3][t]), mk(q_d[4][t], q_d[5][t], q_d[6][t]));
+      __syncthreads();
+      const uint32_t rest = have - FT;  // < FT: the waiting pairs move to the front
+      if (t < rest) {
+        q_k[t] = q_k[FT + t];
+#pragma unroll
+        for (int c = 0; c < 7; c++) q_d[c][t] = q_d[c][FT + t];
+      }
+      if (t == 0) q_n = rest;
+      __syncthreads();
+    }
+  }
+  const uint32_t t = threadIdx.x;
+  if (t < q_n)
+    hooke_pair<Mode>(a, q_k[t], q_d[0][t], mk(q_d[1][t], q_d[2][t], q_d[3][t]), mk(q_d[4][t], q_d[5][t], q_d[6][t]));
+  if (t == 0 && q_tot) atomicAdd(a.n_active, (unsigned long long)q_tot);
 }
 
 // prolog + displacement trigger.  Every particle gets its translation and, when
@@ -515,11 +598,16 @@ int launch_contact_compact(dem_ctx* c) {
     else if (c->ni)
       k_cscreen<<<grid_for(c->ni, FT), FT, 0, c->stream>>>(a);
   }
-  {
-    ProfScope ps(c, K_CDETECT, 1);
-    k_cdetect<<<persistent, FT, 0, c->stream>>>(a);
-  }
-  {
+  if (c->fuse_contact) {  // detection and law in one kernel (k_cfused)
+    DEM_CUDA_TRY(c, cudaMemsetAsync(a.n_active, 0, sizeof(unsigned long long), c->stream));
+    ProfScope ps(c, K_CONTACT, 1);
+    const auto kf = (c->mul_mode & 4) ? k_cfused<1> : k_cfused<0>;  // mode bit 2: the contact law
+    kf<<<persistent, FT, 0, c->stream>>>(a);
+  } else {
+    {
+      ProfScope ps(c, K_CDETECT, 1);
+      k_cdetect<<<persistent, FT, 0, c->stream>>>(a);
+    }
     ProfScope ps(c, K_CONTACT, 1);  // the Hooke law on the contacts
     const auto kh = (c->mul_mode & 4) ? k_chooke<1> : k_chooke<0>;  // mode bit 2: the contact law
     kh<<<persistent, FT, 0, c->stream>>>(a);

@@ -371,6 +371,8 @@ typedef struct dem_tune_result {
   int32_t trials;
   float vmax;                    /* fastest particle speed used by the model     */
   int32_t mul_mode;              /* multiply placement, see dem_set_mul_mode     */
+  int32_t fused_contact;         /* 1: detection and law of the compacted contact
+                                    in one kernel, 0: in two (same bits)         */
 } dem_tune_result;
 int dem_autotune(dem_ctx* ctx, int steps_per_trial, int skin_policy, dem_tune_result* out);
 /* Multiply placement of the fused integration kernels (prolog, epilog).  The
