@@ -53,11 +53,14 @@ CONTACT_BYTES_PER_INTERACTION = 104
 PARTICLE_BYTES_PER_STEP = 344
 # Untimed steps before the warm-up, per workload (--preroll overrides).
 PREROLL = {"spheres": 3000, "polyhedra": 0, "polyhedra_dense": 0, "drums": 0, "mixer": 300, "polyhedra_mesh": 0}
-# DRAM bytes (read + write) per step of the integration kernels (k_fused_prolog,
-# k_prolog_rotation, k_fused_epilog, k_epilog_rotation) and of the contact phase
-# (k_cscreen, k_cdetect, k_chooke), from the ncu captures summarised under
-# profiles/ (per particle and per listed pair, so they scale to the bench state).
-TRAFFIC = {"source": None, "integration_bytes_per_particle": None, "contact_bytes_per_listed_pair": None}
+# DRAM bytes (read + write) per launch of k_cfused per listed pair and of
+# k_fused_epilog per particle, from the ncu capture of the pre-rolled 250k-sphere
+# bed (the same workload at 1/8 of its size); they scale with the listed pairs and
+# the particles.  Both kernels run their FP64 pipe at the fraction recorded here
+# (sm__pipe_fp64_cycles_active of peak sustained).
+TRAFFIC = {"source": "profiles/k_cfused_epilog_spheres_bed_250k.md",
+           "contact_bytes_per_listed_pair": 188.0, "epilog_bytes_per_particle": 445.0,
+           "contact_fp64_pipe_active": 0.825, "epilog_fp64_pipe_active": 0.820}
 
 
 def parse():
@@ -620,30 +623,50 @@ def run_native(args, rank, world, local, dist):
     def per_step(keys):
         return sum(prof[k]["total_ms"] for k in keys if k in prof) / kprof_steps / 1e3
 
-    # the contact phase: screen + detect + Hooke law (fused step) or one kernel (plain)
-    t_contact = sum(prof[k]["total_ms"] / max(prof[k]["timed"], 1)
-                    for k in ("contact_screen", "contact_detect", "contact") if k in prof) / 1e3
-    achieved_c = CONTACT_BYTES_PER_INTERACTION * ni / t_contact / 1e9 if t_contact > 0 else 0.0
-    t_integ = per_step(("prolog", "epilog"))
-    achieved_i = PARTICLE_BYTES_PER_STEP * w.n / t_integ / 1e9 if t_integ > 0 else 0.0
+    def per_launch(key):
+        v = prof.get(key)
+        return v["total_ms"] / max(v["timed"], 1) / 1e3 if v else 0.0
+
     step_ms_prof = sum(v["total_ms"] for v in prof.values()) / kprof_steps
     tot_ms = max(sum(x["total_ms"] for x in prof.values()), 1e-9)
     shares = {k: round(v["total_ms"] / tot_ms, 4) for k, v in prof.items() if v["total_ms"] > 0}
-    t_i = TRAFFIC["integration_bytes_per_particle"]
-    t_c = TRAFFIC["contact_bytes_per_listed_pair"]
-    roofline = {"bound": "hbm", "kernel": "integration (k_fused_prolog + k_fused_epilog + rotation kernels)",
-                "achieved": achieved_i, "peak": peak, "unit": "GB/s", "frac": achieved_i / peak,
-                "peak_kind": peak_kind, "traffic": (t_i * w.n if t_i else None),
-                "algorithmic_bytes_per_launch": PARTICLE_BYTES_PER_STEP * w.n,
-                "avg_launch_ms": t_integ * 1e3, "share_of_step": round(shares.get("prolog", 0) + shares.get("epilog", 0), 4),
-                "traffic_source": TRAFFIC["source"],
-                "note": "344 B per particle-step (prolog and epilog together, per step); FP64-pipe bound in "
-                        "practice (profiles/)"}
-    roofline_contact = {"bound": "hbm", "kernel": "contact phase (k_cscreen + k_cdetect + k_chooke)",
-                        "achieved": achieved_c, "peak": peak, "unit": "GB/s", "frac": achieved_c / peak,
-                        "traffic": (t_c * ni if t_c else None),
-                        "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni, "interactions": ni,
-                        "avg_launch_ms": t_contact * 1e3}
+    # the dominant kernel: the contact law over the listed pairs ("contact" is k_cfused when
+    # detection and law are fused, k_chooke when they are separate, the whole plain kernel otherwise)
+    fused_contact = "contact_detect" not in prof and "contact_screen" in prof
+    t_law = per_launch("contact")
+    achieved_c = CONTACT_BYTES_PER_INTERACTION * ni / t_law / 1e9 if t_law > 0 else 0.0
+    t_c = TRAFFIC["contact_bytes_per_listed_pair"] if fused_contact else None
+    roofline = {"bound": "hbm",
+                "kernel": ("k_cfused (contact detection + contact law over the listed pairs)" if fused_contact
+                           else "contact law kernel over the listed pairs"),
+                "achieved": achieved_c, "peak": peak, "unit": "GB/s", "frac": achieved_c / peak,
+                "peak_kind": peak_kind, "traffic": (t_c * ni if t_c else None),
+                "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni, "listed_pairs": ni,
+                "algorithmic_bytes_per_unit": CONTACT_BYTES_PER_INTERACTION, "avg_launch_ms": t_law * 1e3,
+                "share_of_step": shares.get("contact", 0.0),
+                "traffic_source": TRAFFIC["source"] if fused_contact else None,
+                "traffic_scaling": ("188 B per listed pair measured at 250k spheres (826k listed pairs), "
+                                    "times the listed pairs here") if fused_contact else None,
+                "fp64_pipe_active": TRAFFIC["contact_fp64_pipe_active"] if fused_contact else None,
+                "note": "FP64-pipe bound, not HBM bound: the FP64 pipe runs at the fp64_pipe_active fraction of "
+                        "its peak (2 FP64 instructions per cycle per SM)"}
+    t_integ = per_step(("prolog", "epilog"))
+    achieved_i = PARTICLE_BYTES_PER_STEP * w.n / t_integ / 1e9 if t_integ > 0 else 0.0
+    t_e = TRAFFIC["epilog_bytes_per_particle"]
+    roofline_integration = {
+        "bound": "hbm", "kernel": "integration (k_fused_prolog + k_fused_epilog + rotation kernels)",
+        "achieved": achieved_i, "peak": peak, "unit": "GB/s", "frac": achieved_i / peak, "peak_kind": peak_kind,
+        "epilog_traffic": (t_e * w.n if fused_contact else None),
+        "algorithmic_bytes_per_launch": PARTICLE_BYTES_PER_STEP * w.n,
+        "avg_launch_ms": t_integ * 1e3, "share_of_step": round(shares.get("prolog", 0) + shares.get("epilog", 0), 4),
+        "epilog_fp64_pipe_active": TRAFFIC["epilog_fp64_pipe_active"] if fused_contact else None,
+        "note": "344 B per particle-step (prolog and epilog together, per step)"}
+    t_contact = sum(per_launch(k) for k in ("contact_screen", "contact_detect", "contact"))
+    achieved_p = CONTACT_BYTES_PER_INTERACTION * ni / t_contact / 1e9 if t_contact > 0 else 0.0
+    roofline_contact_phase = {"bound": "hbm", "kernel": "contact phase (k_cscreen + contact kernels)",
+                              "achieved": achieved_p, "peak": peak, "unit": "GB/s", "frac": achieved_p / peak,
+                              "algorithmic_bytes_per_launch": CONTACT_BYTES_PER_INTERACTION * ni,
+                              "avg_launch_ms": t_contact * 1e3}
     mul_mode = s.mul_mode()
     rebuild = rebuild_timing(args, w, s) if args.rebuild_ms > 0 else None
     s.close()
@@ -691,7 +714,8 @@ def run_native(args, rank, world, local, dist):
         "dtype": "f64", "data": "synthetic (seeded random sequential addition)",
         "config": config_block(args, w, pre, preroll_s, bed, mul_mode, idle_fraction),
         "vs_plain": vs_plain,
-        "roofline": roofline, "roofline_contact": roofline_contact,
+        "roofline": roofline, "roofline_integration": roofline_integration,
+        "roofline_contact_phase": roofline_contact_phase,
         "autotune": ({k: (round(v, 6) if isinstance(v, float) else v) for k, v in tune.items()}
                      if tune else None),
         "learned": learned,
