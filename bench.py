@@ -632,7 +632,8 @@ def run_native(args, rank, world, local, dist):
     shares = {k: round(v["total_ms"] / tot_ms, 4) for k, v in prof.items() if v["total_ms"] > 0}
     # the dominant kernel: the contact law over the listed pairs ("contact" is k_cfused when
     # detection and law are fused, k_chooke when they are separate, the whole plain kernel otherwise)
-    fused_contact = "contact_detect" not in prof and "contact_screen" in prof
+    ran = lambda k: prof.get(k, {}).get("total_ms", 0.0) > 0.0
+    fused_contact = ran("contact_screen") and not ran("contact_detect")
     t_law = per_launch("contact")
     achieved_c = CONTACT_BYTES_PER_INTERACTION * ni / t_law / 1e9 if t_law > 0 else 0.0
     t_c = TRAFFIC["contact_bytes_per_listed_pair"] if fused_contact else None

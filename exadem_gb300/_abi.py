@@ -105,6 +105,37 @@ class InteractionList(C.Structure):
                 ("friction", PD), ("moment", PD)]
 
 
+class InnerBondParams(C.Structure):
+    _fields_ = [("kn", D), ("kt", D), ("damp_rate", D), ("mode", C.c_int32), ("pad", C.c_int32), ("crit1", D),
+                ("crit2", D)]
+
+
+class BondList(C.Structure):
+    _fields_ = [("capacity", C.c_uint64), ("count", C.c_uint64), ("id_i", PU64), ("id_j", PU64), ("sub_i", PU32),
+                ("sub_j", PU32), ("dn0", PD), ("weight", PD), ("mode", C.POINTER(C.c_int32)), ("crit1", PD),
+                ("crit2", PD), ("en", PD), ("et", PD), ("tds", PD), ("friction", PD), ("unbroken", PU8)]
+
+
+RUPTURE_ENERGY_MIXED, RUPTURE_ENERGY_SEPARATE, RUPTURE_STRESS_ENERGY_SEPARATE = 0, 1, 2
+
+# dem_bond_list columns: name -> (dtype, values per row)
+BOND_COLUMNS = {"id_i": (np.uint64, 1), "id_j": (np.uint64, 1), "sub_i": (np.uint32, 1), "sub_j": (np.uint32, 1),
+                "dn0": (np.float64, 1), "weight": (np.float64, 1), "mode": (np.int32, 1), "crit1": (np.float64, 1),
+                "crit2": (np.float64, 1), "en": (np.float64, 1), "et": (np.float64, 1), "tds": (np.float64, 3),
+                "friction": (np.float64, 3), "unbroken": (np.uint8, 1)}
+
+
+def bond_struct(cols: dict, capacity: int, count: int = 0) -> BondList:
+    """A dem_bond_list over the arrays of `cols` (BOND_COLUMNS names)."""
+    types = {np.uint64: PU64, np.uint32: PU32, np.float64: PD, np.int32: C.POINTER(C.c_int32), np.uint8: PU8}
+    st = BondList()
+    st.capacity = capacity
+    st.count = count
+    for k, (dt, _w) in BOND_COLUMNS.items():
+        setattr(st, k, ptr(cols[k], types[dt]))
+    return st
+
+
 class KernelStat(C.Structure):
     _fields_ = [("name", C.c_char * 24), ("launches", C.c_uint64), ("timed", C.c_uint64), ("total_ms", D)]
 
@@ -200,6 +231,14 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_get_interactions", [_CTX, C.POINTER(InteractionList)])
     _sig(lib, "dem_set_interactions", [_CTX, C.POINTER(InteractionList)])
     _sig(lib, "dem_packing_profile", [_CTX, C.c_int, D, D, PD])
+    _sig(lib, "dem_set_inner_bond_params", [_CTX, C.c_int, C.POINTER(InnerBondParams)])
+    _sig(lib, "dem_stick_polyhedra", [_CTX, PU64, PD, C.c_uint64, D, PU64])
+    _sig(lib, "dem_bond_count", [_CTX, PU64])
+    _sig(lib, "dem_get_bonds", [_CTX, C.POINTER(BondList)])
+    _sig(lib, "dem_set_bonds", [_CTX, C.POINTER(BondList)])
+    _sig(lib, "dem_broken_interface_count", [_CTX, PU64])
+    _sig(lib, "dem_inner_bond_polyhedron", [_CTX])
+    _sig(lib, "dem_apply_interface_fracture_criterion", [_CTX, PU64])
     _sig(lib, "dem_profile", [_CTX, C.c_int])
     _sig(lib, "dem_kernel_stats", [_CTX, C.POINTER(KernelStat), C.c_int, C.POINTER(C.c_int)])
     _sig(lib, "dem_reset_kernel_stats", [_CTX])
@@ -223,7 +262,9 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_contact_polyhedron", "dem_vertex_displ_over", "dem_set_systems", "dem_system_count",
             "dem_simulation_state_systems", "dem_set_graph_capacity", "dem_autotune", "dem_set_mul_mode", "dem_get_mul_mode", "dem_set_multimat", "dem_set_analysis", "dem_get_contact_state", "dem_stress_tensor", "dem_mlp_harvest",
             "dem_mlp_init", "dem_mlp_set_params", "dem_mlp_get_params", "dem_mlp_forward", "dem_mlp_loss_grad",
-            "dem_mlp_train", "dem_learned_stats"]
+            "dem_mlp_train", "dem_learned_stats", "dem_set_inner_bond_params", "dem_stick_polyhedra",
+            "dem_bond_count", "dem_get_bonds", "dem_set_bonds", "dem_broken_interface_count",
+            "dem_inner_bond_polyhedron", "dem_apply_interface_fracture_criterion"]
 
 _LIB = None
 

@@ -418,8 +418,10 @@ int update_neighbors_poly(dem_ctx* c) {
   int rc;
   if ((rc = ensure_mesh_bins(c))) return rc;
   if ((rc = alloc_poly(c))) return rc;
+  if ((rc = bonds_before_reorder(c))) return rc;  // broken bonds -> history, interfaces
   if ((rc = launch_bin_particles(c))) return rc;
   if ((rc = launch_reorder_particles(c))) return rc;
+  if ((rc = bonds_after_reorder(c))) return rc;   // bonds follow the particles
   if ((rc = launch_poly_vertices(c, 2))) return rc;
   uint64_t nu = 0;
   if ((rc = launch_poly_units(c, &nu, grow_units))) return rc;
@@ -486,11 +488,13 @@ int update_neighbors(dem_ctx* c) {
   return DEM_OK;
 }
 
+// gravity, contact laws, gather; then the inner bonds (config_fragmentation.msp compute_force)
 int compute_force(dem_ctx* c) {
   int rc;
   if ((rc = launch_gravity(c))) return rc;
   if ((rc = c->poly ? launch_contact_poly(c) : launch_contact_sphere(c))) return rc;
-  return launch_gather_forces(c);
+  if ((rc = launch_gather_forces(c))) return rc;
+  return c->poly ? launch_bond_force(c) : DEM_OK;
 }
 
 int need_list(dem_ctx* c) {
@@ -636,6 +640,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   free_compact(c);
   free_poly(c);
   free_units(c);
+  free_bonds(c);
   cudaFree(c->shapes_dev);
   cudaFree(c->rev_off);
   cudaFree(c->rev_cnt);
@@ -758,6 +763,7 @@ int dem_set_particles(dem_ctx* c, const dem_particles* p, int on_device) {
   c->have_list = false;
   c->hist_valid = false;
   c->rebuilds = 0;
+  clear_bonds(c);  // bonds refer to the particles they were made for
   if ((rc = alloc_poly(c))) return rc;
   if ((rc = check_multimat_groups(c))) return rc;
   return setup_grid(c);
@@ -1004,6 +1010,8 @@ int dem_set_shapes(dem_ctx* c, const dem_shape* shapes, int nshapes) {
   c->shapes_dev = nullptr;
   DEM_CUDA_TRY(c, cudaMalloc(&c->shapes_dev, sizeof(ShapeDev) * nshapes));
   DEM_CUDA_TRY(c, cudaMemcpy(c->shapes_dev, h.data(), sizeof(ShapeDev) * nshapes, cudaMemcpyHostToDevice));
+  c->shapes_host.assign(reinterpret_cast<const char*>(h.data()),
+                        reinterpret_cast<const char*>(h.data()) + sizeof(ShapeDev) * nshapes);
   c->nshapes = nshapes;
   if (mv != c->MV) free_poly(c);
   c->MV = mv;
@@ -1054,9 +1062,12 @@ int dem_step(dem_ctx* c, int nsteps) {
   if (c->prm.graph_step && c->prm.fused_step && !c->poly && nsteps > 0 && !c->prof_on) return step_graph(c, nsteps);
   for (int s = 0; s < nsteps; s++) {
     if (c->poly && c->prm.fused_step) {
-      // prolog + vertex_displ_over decided in FP32; rebuild (all vertices) or the
-      // vertices of the particles in the list; contact; gather + f2a + epilog
+      // prolog + vertex_displ_over decided in FP32; interface criterion (raises the
+      // same flag); rebuild (all vertices) or the vertices of the particles in the
+      // list and the bonds; contact; gather + f2a + epilog (with bonds: gather,
+      // bond pass, f2a, epilog)
       if ((rc = launch_poly_fused_prolog(c))) return rc;
+      if ((rc = launch_bond_criterion(c))) return rc;
       if ((rc = read_flag(c, 0))) return rc;
       if (c->h_scalars[0]) {
         if ((rc = update_neighbors(c))) return rc;
@@ -1064,22 +1075,34 @@ int dem_step(dem_ctx* c, int nsteps) {
         return rc;
       }
       if ((rc = launch_contact_poly(c))) return rc;
-      if ((rc = launch_fused_epilog(c))) return rc;
+      if (c->nb) {
+        if ((rc = launch_reset_force_moment(c))) return rc;
+        if ((rc = launch_gravity(c))) return rc;
+        if ((rc = launch_gather_forces(c))) return rc;
+        if ((rc = launch_bond_force(c))) return rc;
+        if ((rc = launch_force_to_accel(c))) return rc;
+        if ((rc = launch_epilog(c))) return rc;
+      } else if ((rc = launch_fused_epilog(c))) {
+        return rc;
+      }
       continue;
     }
     if (c->poly) {
-      // prolog, vertices + vertex_displ_over, rebuild if needed, forces, force_to_accel, epilog
+      // prolog, vertices + vertex_displ_over, interface criterion, rebuild if
+      // needed, forces, force_to_accel, epilog
       if ((rc = launch_prolog(c))) return rc;
       if ((rc = launch_poly_vertices(c, 1))) return rc;
+      if ((rc = launch_bond_criterion(c))) return rc;
       if ((rc = read_flag(c, 0))) return rc;
       if (c->h_scalars[0] && (rc = update_neighbors(c))) return rc;
       if ((rc = launch_contact_poly(c))) return rc;
-      if (c->prm.fused_step) {
+      if (c->prm.fused_step && !c->nb) {
         if ((rc = launch_fused_epilog(c))) return rc;
       } else {
         if ((rc = launch_reset_force_moment(c))) return rc;
         if ((rc = launch_gravity(c))) return rc;
         if ((rc = launch_gather_forces(c))) return rc;
+        if ((rc = launch_bond_force(c))) return rc;
         if ((rc = launch_force_to_accel(c))) return rc;
         if ((rc = launch_epilog(c))) return rc;
       }

@@ -9,22 +9,22 @@
 // Kernel classes for the built-in profiler (dem_profile / dem_kernel_stats).
 enum DemKClass : int {
   K_PROLOG, K_DISPL, K_BIN, K_REORDER, K_BROAD_COUNT, K_BROAD_FILL, K_REVERSE, K_SCAN,
-  K_CONTACT, K_GATHER, K_RESET, K_GRAVITY, K_F2A, K_EPILOG, K_STATE, K_CSCREEN, K_CDETECT, K_NCLASS
+  K_CONTACT, K_GATHER, K_RESET, K_GRAVITY, K_F2A, K_EPILOG, K_STATE, K_CSCREEN, K_CDETECT, K_BOND, K_NCLASS
 };
 static const char* const kDemKClassNames[K_NCLASS] = {
     "prolog", "displ_over", "bin_cells", "reorder", "broad_count", "broad_fill", "reverse_lists", "scan",
     "contact", "gather", "reset", "gravity", "force_to_accel", "epilog", "state", "contact_screen",
-    "contact_detect"};
+    "contact_detect", "bonds"};
 
 namespace dem {
 struct MlpState;  // k_mlp.cu
 }
 
 // device scalars (d_scalars, u64): [0] rebuild trigger, [1] active contacts,
-// [3..4] compaction list counts, [8] learned-record overflows,
+// [3..4] compaction list counts, [8] learned-record overflows, [12] interfaces broken,
 // [16..23] learned bin counters and cursors (14 u32)
 constexpr int DEM_NSCALARS = 32;
-constexpr int SC_ROT_CNT = 6, SC_LEARNED_OVF = 8, SC_LEARNED_BINS = 16;
+constexpr int SC_ROT_CNT = 6, SC_LEARNED_OVF = 8, SC_BROKEN = 12, SC_LEARNED_BINS = 16;
 
 // features recorded per polyhedron unit by the count pass of the FP32-decided
 // enumeration; the fill pass copies them instead of deciding again
@@ -98,8 +98,8 @@ struct dem_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   bool capturing_body = false;             // capturing the conditional rebuild
-  uint64_t graph_launches_per_step[16] = {};     // kernel launches of one replay, per class
-  uint64_t graph_launches_per_rebuild[16] = {};  // and of the conditional rebuild
+  uint64_t graph_launches_per_step[K_NCLASS] = {};     // kernel launches of one replay, per class
+  uint64_t graph_launches_per_rebuild[K_NCLASS] = {};  // and of the conditional rebuild
   uint64_t gen = 0;        // bumped by every host-side change a captured graph depends on
   uint64_t graph_gen = ~0ull;
   void* snap = nullptr;                    // state snapshot for the overflow rollback
@@ -203,6 +203,30 @@ struct dem_ctx {
   uint32_t* f_off = nullptr;          // feature offsets (ucap+1)
   uint64_t ucap = 0;
 
+  // inner bonds (k_bond.cu), double-buffered for the compaction at a rebuild
+  uint64_t nb = 0, bcap = 0, nif = 0;
+  dem::BondArrays B[2]{};
+  void* bblock[2] = {nullptr, nullptr};
+  int bcur = 0;
+  uint32_t* b_scan = nullptr;        // bcap + 1: flags, then offsets
+  uint32_t* b_iface = nullptr;       // bcap + 1: interface offsets
+  uint64_t* bh_oid = nullptr;        // bcap: bonds broken since the last rebuild, as vertex-vertex history
+  uint64_t* bh_pid = nullptr;
+  uint32_t* bh_sub = nullptr;
+  double* bh_ft[3] = {};
+  uint64_t nbh = 0;
+  uint32_t* b_own_first = nullptr;   // bpcap each: owned bonds of a slot
+  uint32_t* b_own_cnt = nullptr;
+  uint32_t* b_rev_off = nullptr;     // bpcap + 1: bonds where the slot is j
+  uint32_t* b_rev_cur = nullptr;     // bpcap + 1
+  uint32_t* b_rev_idx = nullptr;     // bcap
+  uint32_t* b_inv = nullptr;         // bpcap: old slot -> new slot at a reorder
+  uint64_t bpcap = 0;
+  int ib_ng = -1;                    // -1: no inner bond parameters; 0: one set
+  dem_inner_bond_params* ibp_dev = nullptr;
+  std::vector<dem_inner_bond_params> ibp_host;
+  std::vector<char> shapes_host;     // host copy of the dem::ShapeDev array (stick_polyhedra)
+
   // built-in profiler: launches always counted; CUDA-event times when enabled
   bool prof_on = false;
   uint64_t launches[K_NCLASS] = {};
@@ -296,6 +320,14 @@ void ext_free_iarrays(IArrays& I);
 int launch_poly_fused_prolog(dem_ctx* c);     // prolog + FP32-decided vertex_displ_over flag
 int launch_vertex_list(dem_ctx* c);           // particles whose vertices the list uses (host sync)
 int launch_poly_vertices_listed(dem_ctx* c);  // FP64 vertices of those particles
+// k_bond.cu
+int bonds_before_reorder(dem_ctx* c);  // rebuild: broken bonds -> history; interfaces
+int bonds_after_reorder(dem_ctx* c);   // rebuild: new slots, per-slot bond lists
+int launch_bond_criterion(dem_ctx* c); // ORs the rebuild flag when an interface breaks
+int launch_bond_force(dem_ctx* c);     // bond pass + bond gather (after the contact gather)
+int launch_bond_needs(dem_ctx* c, uint32_t* need);
+void free_bonds(dem_ctx* c);
+void clear_bonds(dem_ctx* c);
 // k_step_fused.cu
 int launch_fused_prolog(dem_ctx* c);
 int launch_contact_compact(dem_ctx* c);

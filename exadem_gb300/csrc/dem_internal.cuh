@@ -79,6 +79,34 @@ struct Records {  // per-interaction force record of the last force pass
   uint8_t* live;
 };
 
+// Inner bonds (fragmentation), in bond order (id_i, id_j, sub_i): keys, the
+// bonded vertices, parameters fixed at the stick, the bond state
+// (InnerBondInteraction, inner_bond_interaction.hpp:28-62) and the record of
+// the last bond pass (force, torques, dn and fn = f - friction for the
+// fracture criterion).
+struct BondArrays {
+  uint64_t* id_i;
+  uint64_t* id_j;
+  uint32_t* i;        // particle slots (remapped at every reorder)
+  uint32_t* j;
+  uint32_t* sub;      // sub_i (low 16 bits) | sub_j (high 16 bits)
+  int32_t* mode;      // rupture mode (DEM_RUPTURE_*)
+  uint8_t* unbroken;
+  double* dn0;
+  double* weight;
+  double* c1;
+  double* c2;
+  double* en;
+  double* et;
+  double* ft[3];      // attr::friction
+  double* tds[3];
+  double* f[3];       // record: force on i
+  double* ti[3];
+  double* tj[3];
+  double* dn;
+  double* fn[3];
+};
+
 // Multi-material contact parameters (multimat_parameters.hpp:38-300,
 // contact_force_accessor.hpp:15-23): pp[g_i * ng + g_j] for a particle pair,
 // pd[g_i * nd + driver] for a particle and a driver, by the particles' group

@@ -247,7 +247,22 @@ struct UnitArgs {
   float csz[3];
   float skin_f;
   int f32;
+  // bonds owned by each slot (nullptr: no bonds): nothing is listed between
+  // bonded particles, nor with a driver whose index is a bonded partner's id
+  const uint32_t* b_first;
+  const uint32_t* b_cnt;
+  const uint64_t* b_idj;
 };
+
+__device__ __forceinline__ bool bonded_to(const UnitArgs& a, uint32_t s, uint64_t id) {
+  if (!a.b_cnt) return false;
+  const uint32_t cn = a.b_cnt[s];
+  if (!cn) return false;
+  const uint32_t b0 = a.b_first[s];
+  for (uint32_t k = b0; k < b0 + cn; k++)
+    if (a.b_idj[k] == id) return true;
+  return false;
+}
 
 __device__ __forceinline__ bool driver_reach(const DriverDev& d, double rcut, V3 p) {
   if (d.kind == 0) {
@@ -286,6 +301,7 @@ __device__ inline void for_each_unit(const UnitArgs& a, uint32_t s, Emit&& emit)
     const double rc = reach + 1e-9 * (1.0 + reach + fabs(ri.x) + fabs(ri.y) + fabs(ri.z));
     for (int k = 0; k < a.ndrv; k++) {
       const DriverDev& d = a.drv[k];
+      if (bonded_to(a, s, (uint64_t)k)) continue;
       if (d.kind == 2) {  // a mesh unit when the reach sphere meets the mesh's bin grid
         const MeshDev& m = a.mesh[d.mesh];
         const double bs = 1.0 / m.inv_bs;
@@ -327,6 +343,7 @@ __device__ inline void for_each_unit(const UnitArgs& a, uint32_t s, Emit&& emit)
         for (uint32_t q = a.cell_start[cc]; q < a.cell_start[cc + 1]; q++) {
           const uint64_t idj = a.P.id[q];
           if (idi >= idj) continue;
+          if (bonded_to(a, s, idj)) continue;
           int keep = -1;
           if (a.f32) {
             const float xj = a.xr[q], yj = a.yr[q], zj = a.zr[q];
@@ -438,6 +455,14 @@ struct FeatArgs {
   const uint32_t* slot_off;  // learned sizing: record of unit u = [slot_off[u], slot_off[u+1]); else FEAT_SLOTS each
   const uint32_t* order;     // warp bins: the count pass visits units in this order (else 0, 1, ...)
   uint32_t* utypes;          // count pass: VV, VE, VF, EE counts of each unit (u8 x 4, saturated)
+  // bonds broken since the last build, as vertex-vertex history in key order
+  // (owner id, partner id, owner sub | partner sub << 16); searched when the
+  // old list has no entry for a vertex-vertex pair
+  const uint64_t* bh_oid;
+  const uint64_t* bh_pid;
+  const uint32_t* bh_sub;
+  const double* bh_ft[3];
+  uint64_t nbh;
 };
 
 __device__ __forceinline__ VView vview(const FeatArgs& a, uint32_t s) {
@@ -464,6 +489,7 @@ __device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uin
   a.dst.meta[w] = type | (swap << 15);
   a.dst.sub[w] = (osub & 0xffffu) | ((psub & 0xffffu) << 16);
   double h[6] = {0, 0, 0, 0, 0, 0};
+  bool found = false;
   if (a.have_old) {
     const uint32_t os = a.perm[owner];
     uint32_t lo = a.old_off[os], hi = a.old_off[os + 1];
@@ -481,6 +507,7 @@ __device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uin
     if (lo < oe && a.old.pid[lo] == pid) {
       const uint32_t om = a.old.meta[lo], osb = a.old.sub[lo];
       if (skey(meta_type(om), (om >> 15) & 1u, osb & 0xffffu, osb >> 16) == sk) {
+        found = true;
         h[0] = a.old.ft[0][lo];
         h[1] = a.old.ft[1][lo];
         h[2] = a.old.ft[2][lo];
@@ -488,6 +515,31 @@ __device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uin
         h[4] = a.old.mo[1][lo];
         h[5] = a.old.mo[2][lo];
       }
+    }
+  }
+  if (!found && a.nbh && type == DEM_ITYPE_VERTEX_VERTEX && swap == 0u) {
+    // a broken bond of this vertex pair (broke_interaction: friction, moment 0)
+    const uint64_t oid = a.P.id[owner];
+    const uint32_t os = osub & 0xffffu, ps = psub & 0xffffu;
+    uint64_t lo = 0, hi = a.nbh;
+    auto less = [&](uint64_t m) {  // entry m < key
+      if (a.bh_oid[m] != oid) return a.bh_oid[m] < oid;
+      if (a.bh_pid[m] != pid) return a.bh_pid[m] < pid;
+      const uint32_t ms = a.bh_sub[m];
+      if ((ms & 0xffffu) != os) return (ms & 0xffffu) < os;
+      return (ms >> 16) < ps;
+    };
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (less(mid))
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    if (lo < a.nbh && a.bh_oid[lo] == oid && a.bh_pid[lo] == pid && a.bh_sub[lo] == (os | (ps << 16))) {
+      h[0] = a.bh_ft[0][lo];
+      h[1] = a.bh_ft[1][lo];
+      h[2] = a.bh_ft[2][lo];
     }
   }
   a.dst.ft[0][w] = h[0];
@@ -1617,7 +1669,9 @@ int launch_vertex_list(dem_ctx* c) {
   DEM_CUDA_TRY(c, cudaMemsetAsync(c->vneed, 0, (c->n + 1) * 4, c->stream));
   if (c->ni)
     k_vertex_needs<<<grid_for(c->ni, 256), 256, 0, c->stream>>>(c->I[c->icur], c->ni, c->vneed);
-  int rc = scan_exclusive_u32(c, c->vneed, c->vneed_off, c->n);
+  int rc = launch_bond_needs(c, c->vneed);  // the bonded vertices are read every step
+  if (rc) return rc;
+  rc = scan_exclusive_u32(c, c->vneed, c->vneed_off, c->n);
   if (rc) return rc;
   k_vertex_compact<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->vneed, c->vneed_off, c->n, c->vlist);
   uint32_t cnt = 0;
@@ -1678,6 +1732,9 @@ int launch_poly_units(dem_ctx* c, uint64_t* nu_out, int (*grow_units)(dem_ctx*, 
   for (int d = 0; d < 3; d++) a.csz[d] = (float)c->grid.csz[d];
   a.skin_f = (float)c->prm.rcut_inc;
   a.f32 = c->prm.fp32_broad_phase;
+  a.b_first = c->nb ? c->b_own_first : nullptr;
+  a.b_cnt = c->nb ? c->b_own_cnt : nullptr;
+  a.b_idj = c->nb ? c->B[c->bcur].id_j : nullptr;
   {
     ProfScope ps(c, K_BROAD_COUNT, 1);
     k_unit_count<<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, c->pcnt);
@@ -1731,6 +1788,11 @@ static FeatArgs make_fargs(dem_ctx* c, uint64_t nu) {
   a.slot_off = c->learned_slots ? c->u_slotoff : nullptr;
   a.order = (c->learned_slots && c->prm.learned_sizing >= 2) ? c->u_order : nullptr;
   a.utypes = c->u_types;
+  a.bh_oid = c->bh_oid;
+  a.bh_pid = c->bh_pid;
+  a.bh_sub = c->bh_sub;
+  for (int d = 0; d < 3; d++) a.bh_ft[d] = c->bh_ft[d];
+  a.nbh = c->nbh;
   return a;
 }
 

@@ -377,6 +377,74 @@ class System:
                                A.ptr(a["partner_sub"], A.PU32), A.ptr(a["friction"]), A.ptr(a["moment"]))
         self._check(self.b.set_interactions(self.h, C.byref(st)), "set_interactions")
 
+    # ------------------------------------------------------- inner bonds
+    def set_inner_bond_params(self, params) -> None:
+        """inner_bond_params: one dict (kn, kt, damp_rate and g, or gn + gt, or g +
+        sigma) for every pair, or an ngroups x ngroups nested list of them."""
+        def one(d):
+            if isinstance(d, A.InnerBondParams):
+                return d
+            if "sigma" in d:
+                mode, c1, c2 = A.RUPTURE_STRESS_ENERGY_SEPARATE, d["g"], d["sigma"]
+            elif "g" in d:
+                mode, c1, c2 = A.RUPTURE_ENERGY_MIXED, d["g"], 0.0
+            else:
+                mode, c1, c2 = A.RUPTURE_ENERGY_SEPARATE, d["gn"], d["gt"]
+            return A.InnerBondParams(float(d["kn"]), float(d["kt"]), float(d["damp_rate"]), mode, 0, float(c1),
+                                     float(c2))
+        if isinstance(params, (dict, A.InnerBondParams)):
+            arr = (A.InnerBondParams * 1)(one(params))
+            ng = 0
+        else:
+            ng = len(params)
+            arr = (A.InnerBondParams * (ng * ng))(*[one(params[i][j]) for i in range(ng) for j in range(ng)])
+        self._check(self.b.set_inner_bond_params(self.h, ng, arr), "set_inner_bond_params")
+
+    def stick_polyhedra(self, ids, cluster, sticking_threshold: float) -> int:
+        """stick_polyhedra: bonds between the touching faces of particles of the same cluster."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint64)
+        cl = np.ascontiguousarray(cluster, dtype=np.float64)
+        nb = C.c_uint64()
+        self._check(self.b.stick_polyhedra(self.h, A.ptr(ids, A.PU64), A.ptr(cl), len(ids),
+                                           float(sticking_threshold), C.byref(nb)), "stick_polyhedra")
+        return int(nb.value)
+
+    def bond_count(self) -> int:
+        v = C.c_uint64()
+        self._check(self.b.bond_count(self.h, C.byref(v)), "bond_count")
+        return int(v.value)
+
+    def bonds(self) -> dict:
+        m = self.bond_count()
+        out = {k: np.zeros(m * w, dtype=dt) for k, (dt, w) in A.BOND_COLUMNS.items()}
+        st = A.bond_struct(out, m)
+        self._check(self.b.get_bonds(self.h, C.byref(st)), "get_bonds")
+        out["tds"] = out["tds"].reshape(-1, 3)
+        out["friction"] = out["friction"].reshape(-1, 3)
+        return out
+
+    def set_bonds(self, bonds: dict) -> None:
+        """read_dump_particle_fragmentation's restore (a dict as bonds() returns)."""
+        m = len(bonds["id_i"])
+        cols = {k: np.ascontiguousarray(np.asarray(bonds[k], dtype=dt).reshape(-1))
+                for k, (dt, _w) in A.BOND_COLUMNS.items()}
+        st = A.bond_struct(cols, m, m)
+        self._check(self.b.set_bonds(self.h, C.byref(st)), "set_bonds")
+
+    def inner_bond_polyhedron(self) -> None:
+        self._check(self.b.inner_bond_polyhedron(self.h), "inner_bond_polyhedron")
+
+    def apply_interface_fracture_criterion(self) -> int:
+        v = C.c_uint64()
+        self._check(self.b.apply_interface_fracture_criterion(self.h, C.byref(v)),
+                    "apply_interface_fracture_criterion")
+        return int(v.value)
+
+    def broken_interface_count(self) -> int:
+        v = C.c_uint64()
+        self._check(self.b.broken_interface_count(self.h, C.byref(v)), "broken_interface_count")
+        return int(v.value)
+
     # ---------------------------------------------------------- profiling
     def profile(self, enable: bool = True) -> None:
         self._check(self.b.profile(self.h, int(enable)), "profile")

@@ -33,6 +33,9 @@ class Workload:
     steps: int = 1000
     info: dict = field(default_factory=dict)
     shapes: list = None  # polyhedron shapes (System.set_shapes), None for spheres
+    # fragmentation: {"params": inner bond parameters (System.set_inner_bond_params),
+    # "cluster": cluster of each particle, "threshold": sticking threshold}
+    bonds: dict = None
 
     @property
     def n(self) -> int:
@@ -50,6 +53,11 @@ class Workload:
             s.register_cylinder(**kw)
         for kw in self.meshes:
             s.register_mesh(**kw)
+        if self.bonds:
+            s.set_inner_bond_params(self.bonds["params"])
+            ids = self.particles.get("id")
+            ids = np.arange(self.n, dtype=np.uint64) if ids is None else ids
+            s.stick_polyhedra(ids, self.bonds["cluster"], self.bonds["threshold"])
         return s
 
 
@@ -548,6 +556,73 @@ def polyhedra_lattice(nx=8, ny=8, nz=6, spacing=1.3, density=1.0, seed=7, radius
                 dict(offset=hi[1], normal=(0.0, 1.0, 0.0))]
     w = Workload("polyhedra_lattice", p, arr, surfaces=surfaces, steps=100)
     w.shapes = shapes
+    return w
+
+
+def fragment_blocks(nblocks=2, nx=3, ny=3, nz=3, edge=1.0, radius=0.01, density=1.0, seed=5, vz=-3.0, tilt=0.3,
+                    gap=0.05, dt=1e-4, skin=0.05, kn=1e5, bond=None, threshold=1e-4, steps=400,
+                    **flags) -> Workload:
+    """Fragmentation: nblocks blocks of nx x ny x nz cubes (edge `edge`, Minkowski
+    radius `radius`), the cubes of a block face to face (centres 2 radius +
+    edge apart, so bonded vertices touch: dn 0), each block one cluster and
+    turned as a whole by a random rotation of angle up to `tilt`, its lowest
+    corner gap to 2 gap above a floor, falling at vz under gravity.  The pairs of touching faces of a block are
+    bonded by stick_polyhedra (sticking threshold `threshold`) with the inner
+    bond parameters `bond` (default kn 1e4, kt 8e3, damp_rate 0.87 as in
+    exaDEM's two-fragments example, mixed mode g 0.05: at vz -3 part of the
+    interfaces break at the impact); contacts: Hooke kn, kt = 0.8 kn, mu 0.3,
+    damp_rate 0.87.  The bond damping is not scaled by the bond weight
+    (inner_bond_force.hpp:41), so kn must stay small enough for the explicit
+    step: damp_rate 2 sqrt(kn m/2) dt x bonds per particle well below 2 m."""
+    shp = shape_cube(edge, radius)
+    rng = np.random.default_rng(seed)
+    pitch = edge + 2 * radius
+    pos, cl, q = [], [], []
+    ext = np.array([nx, ny, nz], dtype=np.float64) * pitch
+    span = float(np.linalg.norm(ext))
+    per_row = max(1, int(math.ceil(math.sqrt(nblocks))))
+    for b in range(nblocks):
+        ax = rng.standard_normal(3)
+        ax /= np.linalg.norm(ax)
+        ang = rng.uniform(-tilt, tilt)
+        qb = np.array([math.cos(ang / 2), *(math.sin(ang / 2) * ax)])
+        w, x, y, z = qb
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        g = np.stack(np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij"), -1).reshape(-1, 3)
+        local = (g - (np.array([nx, ny, nz]) - 1) / 2.0) * pitch
+        corners = np.array([[sx, sy, sz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)]) * (0.5 * ext)
+        low = float(min((R @ c)[2] for c in corners))  # lowest point of the turned block above its centre
+        centre = np.array([(b % per_row + 0.5) * (span + 1.0), (b // per_row + 0.5) * (span + 1.0),
+                           -low + gap + rng.uniform(0, gap)])
+        for p in local:
+            pos.append(centre + R @ p)
+            cl.append(float(b))
+            q.append(qb)
+    pos, q = np.asarray(pos), np.asarray(q)
+    n = len(pos)
+    arr = empty_particles(n)
+    arr["rx"], arr["ry"], arr["rz"] = (np.ascontiguousarray(pos[:, k]) for k in range(3))
+    arr["qw"], arr["qx"], arr["qy"], arr["qz"] = (np.ascontiguousarray(q[:, k]) for k in range(4))
+    arr["vz"] = np.full(n, float(vz))
+    arr["vx"], arr["vy"] = np.zeros(n), np.zeros(n)
+    arr["type"] = np.zeros(n, dtype=np.uint32)
+    arr["id"] = np.arange(n, dtype=np.uint64)
+    arr["radius"] = np.full(n, shp["max_rcut"])
+    arr["mass"] = np.full(n, density * shp["volume"])
+    for ax_ in ("inertiax", "inertiay", "inertiaz"):
+        arr[ax_] = arr["mass"] * shp["i_over_m"]
+    arr["homothety"] = np.ones(n)
+    side = per_row * (span + 1.0)
+    hi = (side, side, float(pos[:, 2].max()) + span)
+    cfg = dict(kn=kn, kt=0.8 * kn, kr=0.0, mu=0.3, damp_rate=0.87)
+    p = make_params((0, 0, 0), hi, (0, 0, 0), rcut_inc=skin, dt=dt, gravity=(0, 0, -9.81), config=cfg,
+                    config_driver=cfg, **flags)
+    w = Workload("fragment_blocks", p, arr, surfaces=[dict(offset=0.0, normal=(0.0, 0.0, 1.0))], steps=steps)
+    w.shapes = [shp]
+    w.bonds = {"params": bond or dict(kn=1e4, kt=8e3, damp_rate=0.87, g=0.05), "cluster": np.asarray(cl),
+               "threshold": threshold}
     return w
 
 

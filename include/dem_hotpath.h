@@ -454,6 +454,104 @@ int dem_profile(dem_ctx* ctx, int enable);
 int dem_kernel_stats(dem_ctx* ctx, dem_kernel_stat* out, int capacity, int* count);
 int dem_reset_kernel_stats(dem_ctx* ctx);
 
+/* ---- fragmentation: inner bonds between polyhedra --------------------------
+ * A bond ties vertex sub_i of particle id_i to vertex sub_j of particle id_j
+ * (id_i < id_j), InnerBondInteraction (interaction/inner_bond_interaction.hpp:
+ * 28-62, interaction type 13).  The bonds of one particle pair form an
+ * interface (interface/interface.hpp:27-31) that breaks as a whole.  Bonds are
+ * kept in (id_i, id_j, sub_i) order.  Every step:
+ *   - after the prolog, apply_interface_fracture_criterion (interface/
+ *     apply_interface_fracture_criterion.hpp:35-76) on the energies and forces
+ *     of the previous force pass, per interface: En = sum en, Et = sum et, S =
+ *     (sum of |fn| over the bonds with dn > 0) / size; it breaks when
+ *       DEM_RUPTURE_ENERGY_MIXED:          En + Et > crit1,
+ *       DEM_RUPTURE_ENERGY_SEPARATE:       En > crit1 or Et > crit2,
+ *       DEM_RUPTURE_STRESS_ENERGY_SEPARATE: En > crit1 and S > crit2;
+ *     broken_interface_friction_updater (broken_interface_friction_updater.cpp:
+ *     52-86) then clips each bond's friction to mu |fn| (mu of the contact
+ *     parameters of the two groups), or zeroes it where dn > 0;
+ *   - a broken interface forces a neighbour rebuild, where its bonds become
+ *     vertex-vertex history (broke_interaction, inner_bond_interaction.hpp:
+ *     202-210: friction kept, moment 0, carried by key like any history) and
+ *     leave the bond list;
+ *   - a rebuild lists no contact between two bonded particles (the ignore list
+ *     of interaction_manager.hpp:114-160; as there, a particle that owns a bond
+ *     to the particle of id k also lists no interaction with driver k);
+ *   - the force pass runs inner_bond_law (polyhedron/inner_bond.hpp:112-186,
+ *     forcefield/inner_bond_force.hpp:24-70) on every bond after the contacts;
+ *     each particle adds gravity, its contacts (owned, then as partner) and
+ *     then its bonds (owned, then as partner), each in list order.
+ * The criterion is stored per bond (2 area g, ... as dem_stick_polyhedra
+ * computes it); an interface uses the one of its first bond.               */
+#define DEM_RUPTURE_ENERGY_MIXED 0
+#define DEM_RUPTURE_ENERGY_SEPARATE 1
+#define DEM_RUPTURE_STRESS_ENERGY_SEPARATE 2
+/* InnerBondParams (forcefield/inner_bond_parameters.hpp:27-35). */
+typedef struct dem_inner_bond_params {
+  double kn, kt, damp_rate;
+  int32_t mode; /* DEM_RUPTURE_*                                            */
+  int32_t pad;
+  double crit1; /* g (mixed, stress-energy) or gn (separate)                */
+  double crit2; /* unused (mixed), gt (separate) or sigma (stress-energy)   */
+} dem_inner_bond_params;
+/* inner_bond_params (src/forcefield/multimat_inner_bond.cpp:104-200): the
+ * table pairs[g_i * ngroups + g_j] by the particles' group field, or with
+ * ngroups = 0 the one set pairs[0] for every pair.                        */
+int dem_set_inner_bond_params(dem_ctx* ctx, int ngroups, const dem_inner_bond_params* pairs);
+/* stick_polyhedra (src/polyhedron/stick_polyhedra.cpp:60-360): bonds between
+ * the faces that touch.  cluster[k] is the cluster of particle ids[k] (the
+ * cluster field; every particle must be listed).  For each pair of particles of
+ * the same cluster with id_i < id_j and centres closer than the neighbour
+ * distance, the first face i of particle id_i (file order) and face j of id_j
+ * with the same vertex count (>= 3), areas within 1 %, and parallel unit
+ * normals (|n_i x n_j| <= 1e-10) bond each vertex of face i to the first
+ * vertex of face j closer than sticking_threshold (vertex-vertex dn); a face
+ * match with fewer than 3 such vertices is dropped and the search goes on.
+ * Weight 1/(bonds of the pair); criterion 2 area g (area of face i scaled by
+ * h_i^2; stress-energy: area sigma) from the pair's inner bond parameters;
+ * the bond vertices of particle id_i must be coplanar (1e-10).  Replaces
+ * the bond list; the contacts of bonded pairs leave the list at the next
+ * rebuild (call it before dem_first_iteration).  nbonds: bonds made.      */
+int dem_stick_polyhedra(dem_ctx* ctx, const uint64_t* ids, const double* cluster, uint64_t n,
+                        double sticking_threshold, uint64_t* nbonds);
+/* One row per bond, in bond order (en, et: energies of the last force pass;
+ * tds: cumulated tangential displacement; friction = kt weight tds). */
+typedef struct dem_bond_list {
+  uint64_t capacity; /* rows the caller's arrays hold                         */
+  uint64_t count;    /* rows written (get) or given (set)                     */
+  uint64_t* id_i;
+  uint64_t* id_j;
+  uint32_t* sub_i;
+  uint32_t* sub_j;
+  double* dn0;
+  double* weight;
+  int32_t* mode;
+  double* crit1;
+  double* crit2;
+  double* en;
+  double* et;
+  double* tds;      /* 3 per row */
+  double* friction; /* 3 per row */
+  uint8_t* unbroken;
+} dem_bond_list;
+int dem_bond_count(dem_ctx* ctx, uint64_t* out);
+int dem_get_bonds(dem_ctx* ctx, dem_bond_list* out);
+/* read_dump_particle_fragmentation: installs a saved bond list (rows as
+ * dem_get_bonds writes them) for the particles currently set, by id.     */
+int dem_set_bonds(dem_ctx* ctx, const dem_bond_list* list);
+/* Interfaces broken since the context was made (the sum of the
+ * apply_interface_fracture_criterion results). */
+int dem_broken_interface_count(dem_ctx* ctx, uint64_t* out);
+/* The two operators on their own, for callers that schedule the operators
+ * themselves (dem_step runs both):
+ * inner_bond_polyhedron (src/polyhedron/inner_bond_force.cu:98-134): the bond
+ * pass on the current vertices, its forces added after the contact gather;
+ * apply_interface_fracture_criterion + broken_interface_friction_updater
+ * (apply_interface_fracture_criterion.cu:44-86): broken = interfaces broken
+ * now; their bonds leave the list at the next dem_update_particle_neighbors. */
+int dem_inner_bond_polyhedron(dem_ctx* ctx);
+int dem_apply_interface_fracture_criterion(dem_ctx* ctx, uint64_t* broken);
+
 /* ---- state reduction without any device allocation ---------------------
  * No counterpart in the reference.  For callers that may not call cudaMalloc
  * (their device memory is owned by another allocator, or they must not pay

@@ -174,6 +174,32 @@ struct Rec {  // per-interaction force record
   V3 scp{}, sfn{}, sft{};
 };
 
+// InnerBondInteraction (interaction/inner_bond_interaction.hpp:28-62): particle
+// indices i (owner, id_i < id_j) and j, bonded vertices, dn0, weight, the
+// rupture criterion (rupture_criterion.hpp:35-40) and the bond's state.
+struct Bond {
+  uint64_t id_i, id_j;
+  int32_t i, j;
+  uint32_t sub_i, sub_j;
+  double dn0 = 0, weight = 1;
+  int32_t mode = 0;
+  double c1 = 0, c2 = 0;
+  V3 friction{}, tds{};
+  double en = 0, et = 0;
+  uint8_t unbroken = 1;
+};
+inline bool bond_less(const Bond& a, const Bond& b) {  // InteractionPair order within type 13
+  if (a.id_i != b.id_i) return a.id_i < b.id_i;
+  if (a.id_j != b.id_j) return a.id_j < b.id_j;
+  if (a.sub_i != b.sub_i) return a.sub_i < b.sub_i;
+  return a.sub_j < b.sub_j;
+}
+struct BondRec {  // force record and contact state of the last bond pass
+  V3 f{}, ti{}, tj{};
+  double dn = 0;
+  V3 fn{};
+};
+
 struct Oracle {
   dem_params prm;
   // multi-material contact parameters (multimat_parameters.hpp:38-300): mm_pp[g_i * ng + g_j],
@@ -207,6 +233,21 @@ struct Oracle {
   std::vector<std::vector<V3>> bvtx;  // vertices at the last rebuild (backup_dem)
   uint64_t rebuilds = 0;
   uint64_t n_active = 0;
+  // inner bonds (fragmentation), in bond order
+  std::vector<Bond> bonds;
+  std::vector<BondRec> brec;
+  std::vector<size_t> iface;        // interface offsets into bonds (nif + 1)
+  std::vector<int32_t> bown_first;  // per particle: first owned bond or -1
+  std::vector<int32_t> bown_cnt;
+  std::vector<size_t> brev_off;     // per particle: bonds where it is j
+  std::vector<int32_t> brev_idx;
+  int ib_ng = -1;                   // -1: no inner bond parameters; 0: one set
+  std::vector<dem_inner_bond_params> ibp;
+  const dem_inner_bond_params& bond_params(size_t i, size_t j) const {
+    return ib_ng == 0 ? ibp[0] : ibp[(size_t)group[i] * ib_ng + group[j]];
+  }
+  std::vector<Inter> broken_hist;   // bonds broken since the last rebuild, as vertex-vertex history
+  uint64_t broken_total = 0;
   std::string err;
 };
 
@@ -809,9 +850,13 @@ int displ_over(const Oracle& o) {
   return over;
 }
 
+void bond_force(Oracle& o);
+// compute_force with fragmentation (config_fragmentation.msp compute_force):
+// gravity, the contact laws, then inner_bond_polyhedron
 void compute_force(Oracle& o) {
   gravity_force(o);
   contact_all(o);
+  if (o.poly && !o.bonds.empty()) bond_force(o);
 }
 
 // Profile: solid fraction of spheres in horizontal slabs (analytic cap volumes).
@@ -836,6 +881,7 @@ struct PShape {
   std::vector<int> e;                  // 2*ne
   std::vector<std::vector<int>> f;     // faces
   double r = 0;                        // Minkowski radius
+  std::vector<double> fa;              // face areas (shape::compute_face_areas, shape.hpp:674-697)
   OBBr obb;
   int nv() const { return (int)v.size(); }
   int ne() const { return (int)e.size() / 2; }
@@ -1241,14 +1287,20 @@ void compute_vertices(Oracle& o) {
   }
 }
 
+bool bonded_to(const Oracle& o, size_t a, uint64_t id);
+void drop_broken_bonds(Oracle& o);
+
 // nbh_polyhedron (src/polyhedron/nbh_polyhedron.cpp:75-384) + add_driver_interaction
-// (nbh_polyhedron_driver.hpp:216-238), history by key, canonical order.
+// (nbh_polyhedron_driver.hpp:216-238), history by key, canonical order.  With
+// bonds: the broken ones become history first; no interaction is listed for a
+// bonded pair (nor for a driver whose index is the id of a bonded partner).
 int update_neighbors_poly(Oracle& o) {
   for (int d = 0; d < 3; d++)
     if (o.prm.periodic[d]) {
       o.err = "periodic boundaries are not supported for polyhedra";
       return DEM_ERR_UNSUPPORTED;
     }
+  if (!o.bonds.empty() || !o.bown_first.empty()) drop_broken_bonds(o);
   compute_vertices(o);
   const double rV = o.prm.rcut_inc;
   const double nd = nbh_dist(o);
@@ -1281,6 +1333,7 @@ int update_neighbors_poly(Oracle& o) {
     // drivers: each vertex against each driver
     for (size_t k = 0; k < o.drivers.size(); k++) {
       const Driver& dv = o.drivers[k];
+      if (bonded_to(o, a, (uint64_t)k)) continue;
       if (dv.kind == 2) {
         poly_mesh_candidates(o, k, a, rV, lst);
         continue;
@@ -1314,6 +1367,7 @@ int update_neighbors_poly(Oracle& o) {
             const double rmax = o.rad[a] + o.rad[b] + rV;
             if (!(d2 > 0.0 && d2 < rmax * rmax && d2 < rcut2)) continue;
             if (o.id[a] >= o.id[b]) continue;
+            if (bonded_to(o, a, o.id[b])) continue;
             const PShape& sb = o.shapes[o.type[b]];
             const double hb = o.hom[b];
             const double rb = sb.r * hb;
@@ -1392,8 +1446,15 @@ int update_neighbors_poly(Oracle& o) {
     if (lb != o.inter.end() && key_eq(*lb, it)) {
       it.friction = lb->friction;
       it.moment = lb->moment;
+    } else if (!o.broken_hist.empty()) {
+      auto bb = std::lower_bound(o.broken_hist.begin(), o.broken_hist.end(), it, key_less);
+      if (bb != o.broken_hist.end() && key_eq(*bb, it)) {
+        it.friction = bb->friction;
+        it.moment = bb->moment;
+      }
     }
   }
+  o.broken_hist.clear();
   o.inter.swap(fresh);
   o.own_first.assign(o.n, -1);
   o.own_cnt.assign(o.n, 0);
@@ -1608,6 +1669,298 @@ int vertex_displ_over(const Oracle& o) {
   return over;
 }
 
+
+// ------------------------------------------------------------ inner bonds
+// shape::compute_face_areas (src/shape/include/exaDEM/shape.hpp:674-697): the
+// fan of triangles from the face's first vertex
+double face_area(const PShape& sh, const std::vector<int>& f) {
+  double surface = 0;
+  if (f.size() < 3) return 0;
+  const V3& v0 = sh.v[f[0]];
+  for (int j = 1; j < (int)f.size() - 1; j++) {
+    const int k = j + 1;
+    const V3 v1 = sh.v[f[j]] - v0;
+    const V3 v2 = sh.v[f[k]] - v0;
+    surface += 0.5 * norm(cross(v1, v2));
+  }
+  return surface;
+}
+inline V3 stick_normalize(const V3& in) {  // normalize (stick_polyhedra.cpp:40-43)
+  const double inv_norm = 1.0 / norm(in);
+  return in * inv_norm;
+}
+
+// check_stiked_face (interaction_manager.hpp:225-277): the bonded vertices of
+// particle i lie in the plane of the first three
+bool check_stuck_face(const std::vector<Bond>& local, const std::vector<V3>& va) {
+  if (local.empty()) return true;
+  if (local.size() <= 2) return false;
+  std::vector<V3> v;
+  for (const Bond& b : local) v.push_back(va[b.sub_i]);
+  const V3 normal = cross(v[1] - v[0], v[2] - v[0]);
+  for (size_t j = 3; j < v.size(); j++)
+    if (std::fabs(dot(v[j] - v[0], normal)) > 1.e-10) return false;
+  return true;
+}
+
+// The bonds of the pair (a, b), id_a < id_b (stick_polyhedra.cpp:235-350).
+void stick_pair(const Oracle& o, size_t a, size_t b, double dn_crit, std::vector<Bond>& out) {
+  const PShape& si = o.shapes[o.type[a]];
+  const PShape& sj = o.shapes[o.type[b]];
+  const double hi = o.hom[a], hj = o.hom[b];
+  const double ri = si.r * hi, rj = sj.r * hj;
+  const std::vector<V3>& va = o.vtx[a];
+  const std::vector<V3>& vb = o.vtx[b];
+  const dem_inner_bond_params& ibp = o.bond_params(a, b);
+  const int nfi = si.nf(), nfj = sj.nf();
+  std::vector<V3> nj(nfj);
+  for (int j = 0; j < nfj; j++) {
+    const std::vector<int>& f = sj.f[j];
+    if (f.size() < 3) continue;
+    nj[j] = stick_normalize(cross(vb[f[1]] - vb[f[0]], vb[f[2]] - vb[f[0]]));
+  }
+  std::vector<Bond> local;
+  bool found = false;
+  for (int i = 0; i < nfi && !found; i++) {
+    const std::vector<int>& fi = si.f[i];
+    if (fi.size() < 3) continue;
+    const V3 ni = stick_normalize(cross(va[fi[1]] - va[fi[0]], va[fi[2]] - va[fi[0]]));
+    const double area_i = si.fa[i];
+    for (int j = 0; j < nfj && !found; j++) {
+      const std::vector<int>& fj = sj.f[j];
+      if (fj.size() < 3) continue;
+      if (fi.size() != fj.size()) continue;
+      const double surface_ratio = area_i / sj.fa[j];
+      if (surface_ratio > 1.01 || surface_ratio < 0.99) continue;
+      if (norm(cross(ni, nj[j])) > 1.e-10) continue;
+      const double area = si.fa[i] * hi * hi;  // get_face_area(i, h_i): id_i < id_j
+      Bond proto{};
+      proto.id_i = o.id[a];
+      proto.id_j = o.id[b];
+      proto.i = (int32_t)a;
+      proto.j = (int32_t)b;
+      proto.mode = ibp.mode;
+      switch (ibp.mode) {
+        case DEM_RUPTURE_ENERGY_MIXED: proto.c1 = 2 * area * ibp.crit1; break;
+        case DEM_RUPTURE_ENERGY_SEPARATE:
+          proto.c1 = 2 * area * ibp.crit1;
+          proto.c2 = 2 * area * ibp.crit2;
+          break;
+        default:
+          proto.c1 = 2 * area * ibp.crit1;
+          proto.c2 = area * ibp.crit2;
+          break;
+      }
+      found = true;
+      for (size_t ivf = 0; ivf < fi.size(); ivf++) {
+        for (size_t jvf = 0; jvf < fj.size(); jvf++) {
+          const Det d = detect_vv(va[fi[ivf]], ri, vb[fj[jvf]], rj);
+          if (d.dn <= dn_crit) {
+            Bond bnd = proto;
+            bnd.sub_i = (uint32_t)fi[ivf];
+            bnd.sub_j = (uint32_t)fj[jvf];
+            bnd.dn0 = d.dn;
+            local.push_back(bnd);
+            break;
+          }
+        }
+      }
+      if (local.size() <= 2) {
+        local.clear();
+        found = false;
+      }
+    }
+  }
+  for (Bond& bnd : local) bnd.weight = 1. / static_cast<double>(local.size());
+  if (check_stuck_face(local, va)) out.insert(out.end(), local.begin(), local.end());
+}
+
+// interfaces (update_interfaces.cpp:48-79) and the per-particle bond lists
+void bond_lists(Oracle& o) {
+  const size_t nb = o.bonds.size();
+  o.iface.clear();
+  for (size_t k = 0; k < nb; k++)
+    if (k == 0 || o.bonds[k].id_i != o.bonds[k - 1].id_i || o.bonds[k].id_j != o.bonds[k - 1].id_j)
+      o.iface.push_back(k);
+  // the reference's scan never compares the last bond with the one before it:
+  // a last interface of one bond joins the interface before it
+  if (o.iface.size() >= 2 && o.iface.back() == nb - 1) o.iface.pop_back();
+  o.iface.push_back(nb);
+  o.bown_first.assign(o.n, -1);
+  o.bown_cnt.assign(o.n, 0);
+  o.brev_off.assign(o.n + 1, 0);
+  for (size_t k = 0; k < nb; k++) {
+    const Bond& b = o.bonds[k];
+    if (o.bown_first[b.i] < 0) o.bown_first[b.i] = (int32_t)k;
+    o.bown_cnt[b.i]++;
+    o.brev_off[b.j + 1]++;
+  }
+  for (size_t i = 0; i < o.n; i++) o.brev_off[i + 1] += o.brev_off[i];
+  o.brev_idx.assign(nb, 0);
+  std::vector<size_t> cur(o.brev_off.begin(), o.brev_off.end() - 1);
+  for (size_t k = 0; k < nb; k++) o.brev_idx[cur[o.bonds[k].j]++] = (int32_t)k;
+}
+
+// particle a owns an unbroken bond to the particle of id `id` (the ignore list,
+// interaction_manager.hpp:114-160; a driver's partner id is its index)
+bool bonded_to(const Oracle& o, size_t a, uint64_t id) {
+  if (o.bown_first.size() != o.n || o.bown_first[a] < 0) return false;
+  for (int32_t k = o.bown_first[a]; k < o.bown_first[a] + o.bown_cnt[a]; k++)
+    if (o.bonds[k].id_j == id && o.bonds[k].unbroken) return true;
+  return false;
+}
+
+// the broken bonds leave the list as vertex-vertex history (broke_interaction,
+// inner_bond_interaction.hpp:202-210), for the rebuild that follows
+void drop_broken_bonds(Oracle& o) {
+  std::vector<Bond> keep;
+  std::vector<BondRec> keep_rec;
+  for (size_t k = 0; k < o.bonds.size(); k++) {
+    const Bond& b = o.bonds[k];
+    if (b.unbroken) {
+      keep.push_back(b);
+      keep_rec.push_back(k < o.brec.size() ? o.brec[k] : BondRec{});
+      continue;
+    }
+    Inter it{};
+    it.oid = b.id_i;
+    it.pid = b.id_j;
+    it.type = DEM_ITYPE_VERTEX_VERTEX;
+    it.swap = 0;
+    it.osub = b.sub_i;
+    it.psub = b.sub_j;
+    it.oi = b.i;
+    it.pj = b.j;
+    it.friction = b.friction;
+    it.moment = {0, 0, 0};
+    o.broken_hist.push_back(it);
+  }
+  o.bonds.swap(keep);
+  o.brec.swap(keep_rec);
+  std::stable_sort(o.broken_hist.begin(), o.broken_hist.end(), key_less);
+  bond_lists(o);
+}
+
+// force_law_core (forcefield/inner_bond_force.hpp:24-70)
+void bond_law_core(double dn, const V3& n, double dn0, double weight, double dt, const dem_inner_bond_params& p,
+                   double meff, double& En, V3& tds, double& Et, V3& ft, const V3& cp, const V3& pos_i,
+                   const V3& vel_i, V3& f_i, const V3& vrot_i, const V3& pos_j, const V3& vel_j,
+                   const V3& vrot_j) {
+  const double damp = p.damp_rate * 2.0 * std::sqrt(p.kn * meff);  // compute_damp
+  const V3 contribution_i = vel_i - cross(cp - pos_i, vrot_i);     // compute_relative_velocity
+  const V3 contribution_j = vel_j - cross(cp - pos_j, vrot_j);
+  const V3 vel = contribution_j - contribution_i;
+  const double vn = dot(vel, n);
+  const double delta = dn - dn0;
+  const double kn_w = p.kn * weight;
+  const double kt_w = p.kt * weight;
+  const double fne = -kn_w * delta;
+  const double fnv = damp * vn;
+  const double fn = fne + fnv;
+  const V3 vfn = fn * n;
+  const V3 vt = vel - vn * n;  // compute_tangential_force(dt, vn, n, vel)
+  const V3 ds = dt * vt;
+  tds += ds;
+  ft = kt_w * tds;
+  f_i = vfn + ft;
+  En = static_cast<double>(fne <= 0) * (0.5 * kn_w * delta * delta);
+  Et = 0.5 * kt_w * dot(tds, tds);
+}
+
+// inner_bond_law (polyhedron/inner_bond.hpp:112-186): vertex-vertex detection of
+// the bonded vertices, force_law_core, compute_moments with a zero moment
+void bond_one(Oracle& o, size_t k) {
+  Bond& B = o.bonds[k];
+  BondRec& r = o.brec[k];
+  const size_t i = (size_t)B.i, j = (size_t)B.j;
+  const double ri = o.shapes[o.type[i]].r * o.hom[i];
+  const double rj = o.shapes[o.type[j]].r * o.hom[j];
+  const Det d = detect_vv(o.vtx[i][B.sub_i], ri, o.vtx[j][B.sub_j], rj);
+  const V3 pos_i = pos(o, i), pos_j = pos(o, j);
+  const double mi = o.mass[i], mj = o.mass[j];
+  const double meff = (mi * mj) / (mi + mj);
+  V3 f{};
+  bond_law_core(d.dn, d.n, B.dn0, B.weight, o.prm.dt, o.bond_params(i, j), meff, B.en, B.tds, B.et, B.friction, d.cp,
+                pos_i, {o.vx[i], o.vy[i], o.vz[i]}, f, {o.wx[i], o.wy[i], o.wz[i]}, pos_j,
+                {o.vx[j], o.vy[j], o.vz[j]}, {o.wx[j], o.wy[j], o.wz[j]});
+  r.f = f;
+  r.ti = cross(d.cp - pos_i, f) + V3{0, 0, 0};
+  r.tj = cross(d.cp - pos_j, -f) + V3{0, 0, 0};
+  r.dn = d.dn;
+  r.fn = f - B.friction;
+}
+
+// bond pass, then per particle its owned bonds and the bonds where it is j, in bond order
+void bond_force(Oracle& o) {
+  if (o.brec.size() != o.bonds.size()) o.brec.assign(o.bonds.size(), BondRec{});
+#pragma omp parallel for schedule(static)
+  for (long k = 0; k < (long)o.bonds.size(); k++) bond_one(o, (size_t)k);
+#pragma omp parallel for schedule(static)
+  for (long ii = 0; ii < (long)o.n; ii++) {
+    const size_t i = (size_t)ii;
+    V3 f = {o.fx[i], o.fy[i], o.fz[i]};
+    V3 m = {o.mx[i], o.my[i], o.mz[i]};
+    if (o.bown_first[i] >= 0)
+      for (int32_t k = o.bown_first[i]; k < o.bown_first[i] + o.bown_cnt[i]; k++) {
+        f += o.brec[k].f;
+        m += o.brec[k].ti;
+      }
+    for (size_t q = o.brev_off[i]; q < o.brev_off[i + 1]; q++) {
+      const BondRec& r = o.brec[o.brev_idx[q]];
+      f += -r.f;
+      m += r.tj;
+    }
+    o.fx[i] = f.x;
+    o.fy[i] = f.y;
+    o.fz[i] = f.z;
+    o.mx[i] = m.x;
+    o.my[i] = m.y;
+    o.mz[i] = m.z;
+  }
+}
+
+// apply_interface_fracture_criterion (apply_interface_fracture_criterion.hpp:35-76)
+// and broken_interface_friction_updater (broken_interface_friction_updater.cpp:
+// 52-86), on the state of the last bond pass.  Returns the interfaces broken.
+uint64_t fracture(Oracle& o) {
+  const long nif = (long)o.iface.size() - 1;
+  if (nif <= 0 || o.brec.size() != o.bonds.size()) return 0;
+  uint64_t broken = 0;
+#pragma omp parallel for schedule(static) reduction(+ : broken)
+  for (long q = 0; q < nif; q++) {
+    const size_t off = o.iface[q], size = o.iface[q + 1] - off;
+    double En = 0.0, Et = 0.0, S = 0.0;
+    for (size_t j = off; j < off + size; j++) {
+      En += o.bonds[j].en;
+      Et += o.bonds[j].et;
+      if (o.brec[j].dn > 0.0) S += norm(o.brec[j].fn);
+    }
+    S /= size;
+    const Bond& c = o.bonds[off];
+    bool brk = false;
+    if (c.mode == DEM_RUPTURE_ENERGY_MIXED) {
+      if (En + Et > c.c1) brk = true;
+    } else if (c.mode == DEM_RUPTURE_ENERGY_SEPARATE) {
+      if (En > c.c1 || Et > c.c2) brk = true;
+    } else if (c.mode == DEM_RUPTURE_STRESS_ENERGY_SEPARATE) {
+      if ((En > c.c1) && (S > c.c2)) brk = true;
+    }
+    if (!brk) continue;
+    broken++;
+    for (size_t j = off; j < off + size; j++) {
+      Bond& b = o.bonds[j];
+      b.unbroken = 0;
+      const V3 ftv = b.friction;
+      const double ft = norm(ftv);
+      const double mu = o.pair_params((size_t)b.i, (size_t)b.j).mu;
+      const double ft_threshold = mu * norm(o.brec[j].fn);
+      if (ft > ft_threshold && ft > 0) b.friction = ftv * ft_threshold / ft;
+      if (o.brec[j].dn > 0) b.friction = {0, 0, 0};
+    }
+  }
+  o.broken_total += broken;
+  return broken;
+}
 }  // namespace
 
 // ============================================================== C interface
@@ -1696,6 +2049,11 @@ int oracle_set_particles(void* h, const dem_particles* p) {
   o.own_cnt.assign(n, 0);
   o.rev_off.assign(n + 1, 0);
   o.rev_idx.clear();
+  o.bonds.clear();
+  o.brec.clear();
+  o.broken_hist.clear();
+  o.bown_first.clear();
+  o.iface.assign(1, 0);
   return DEM_OK;
 }
 int oracle_get_particles(void* h, dem_particles* p) {
@@ -1793,6 +2151,7 @@ int oracle_set_shapes(void* h, const dem_shape* shp, int nshapes) {
     ps.obb.e2 = {d.obb_e2[0], d.obb_e2[1], d.obb_e2[2]};
     ps.obb.e3 = {d.obb_e3[0], d.obb_e3[1], d.obb_e3[2]};
     ps.obb.ext = {d.obb_extent[0], d.obb_extent[1], d.obb_extent[2]};
+    for (const auto& f : ps.f) ps.fa.push_back(face_area(ps, f));
     o.shapes.push_back(ps);
   }
   o.poly = true;
@@ -1836,7 +2195,11 @@ int oracle_step(void* h, int nsteps) {
   Oracle& o = *(Oracle*)h;
   for (int s = 0; s < nsteps; s++) {
     prolog(o);
-    if (trigger(o)) {
+    // evaluate_particle_displ with fragmentation (config_fragmentation.msp:28-38):
+    // vertex displacement, then the interface criterion; either one rebuilds
+    int over = trigger(o);
+    if (o.poly && !o.bonds.empty() && fracture(o) > 0) over = 1;
+    if (over) {
       int rc = rebuild(o);
       if (rc) return rc;
     }
@@ -1845,6 +2208,156 @@ int oracle_step(void* h, int nsteps) {
     force_to_accel(o);
     epilog(o);
   }
+  return DEM_OK;
+}
+// ---- inner bonds
+int oracle_set_inner_bond_params(void* h, int ng, const dem_inner_bond_params* pairs) {
+  Oracle& o = *(Oracle*)h;
+  if (ng < 0 || !pairs) return DEM_ERR_INVALID_ARG;
+  const size_t cnt = ng == 0 ? 1 : (size_t)ng * ng;
+  for (size_t k = 0; k < cnt; k++)
+    if (pairs[k].mode < DEM_RUPTURE_ENERGY_MIXED || pairs[k].mode > DEM_RUPTURE_STRESS_ENERGY_SEPARATE)
+      return DEM_ERR_INVALID_ARG;
+  o.ibp.assign(pairs, pairs + cnt);
+  o.ib_ng = ng;
+  return DEM_OK;
+}
+static int index_of_ids(Oracle& o, std::vector<std::pair<uint64_t, int32_t>>& ids) {
+  ids.resize(o.n);
+  for (size_t i = 0; i < o.n; i++) ids[i] = {o.id[i], (int32_t)i};
+  std::sort(ids.begin(), ids.end());
+  return DEM_OK;
+}
+static int32_t find_id(const std::vector<std::pair<uint64_t, int32_t>>& ids, uint64_t id) {
+  auto it = std::lower_bound(ids.begin(), ids.end(), std::make_pair(id, (int32_t)-1));
+  return (it != ids.end() && it->first == id) ? it->second : -1;
+}
+// stick_polyhedra: replaces the interaction storage with the bonds (the contacts'
+// history is dropped, stick_polyhedra.cpp:116-120 and update_extra_storage<false>)
+int oracle_stick_polyhedra(void* h, const uint64_t* ids_in, const double* cluster_in, uint64_t n, double thr,
+                           uint64_t* nbonds) {
+  Oracle& o = *(Oracle*)h;
+  if (!o.poly || o.ib_ng < 0) return DEM_ERR_STATE;
+  if (n != o.n || (n && (!ids_in || !cluster_in))) return DEM_ERR_INVALID_ARG;
+  std::vector<std::pair<uint64_t, int32_t>> ids;
+  index_of_ids(o, ids);
+  std::vector<double> cl(o.n);
+  std::vector<uint8_t> seen(o.n, 0);
+  for (uint64_t k = 0; k < n; k++) {
+    const int32_t i = find_id(ids, ids_in[k]);
+    if (i < 0 || seen[i]) return DEM_ERR_INVALID_ARG;
+    seen[i] = 1;
+    cl[i] = cluster_in[k];
+  }
+  compute_vertices(o);
+  const double nd = nbh_dist(o);
+  const double rcut2 = nd * nd;
+  std::vector<std::vector<Bond>> per(o.n);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (long aa = 0; aa < (long)o.n; aa++) {
+    const size_t a = (size_t)aa;
+    for (size_t b = 0; b < o.n; b++) {
+      if (b == a || cl[b] != cl[a] || o.id[a] >= o.id[b]) continue;
+      const double dx = o.rx[b] - o.rx[a], dy = o.ry[b] - o.ry[a], dz = o.rz[b] - o.rz[a];
+      if (!(dx * dx + dy * dy + dz * dz < rcut2)) continue;
+      stick_pair(o, a, b, thr, per[a]);
+    }
+  }
+  o.bonds.clear();
+  for (auto& v : per) o.bonds.insert(o.bonds.end(), v.begin(), v.end());
+  std::stable_sort(o.bonds.begin(), o.bonds.end(), bond_less);
+  o.brec.assign(o.bonds.size(), BondRec{});
+  o.broken_hist.clear();
+  o.inter.clear();
+  o.rec.clear();
+  o.own_first.assign(o.n, -1);
+  o.own_cnt.assign(o.n, 0);
+  o.rev_off.assign(o.n + 1, 0);
+  o.rev_idx.clear();
+  bond_lists(o);
+  if (nbonds) *nbonds = o.bonds.size();
+  return DEM_OK;
+}
+int oracle_bond_count(void* h, uint64_t* out) {
+  *out = ((Oracle*)h)->bonds.size();
+  return DEM_OK;
+}
+int oracle_get_bonds(void* h, dem_bond_list* l) {
+  Oracle& o = *(Oracle*)h;
+  l->count = o.bonds.size();
+  if (l->capacity < o.bonds.size()) return DEM_ERR_INVALID_ARG;
+  for (size_t k = 0; k < o.bonds.size(); k++) {
+    const Bond& b = o.bonds[k];
+    if (l->id_i) l->id_i[k] = b.id_i;
+    if (l->id_j) l->id_j[k] = b.id_j;
+    if (l->sub_i) l->sub_i[k] = b.sub_i;
+    if (l->sub_j) l->sub_j[k] = b.sub_j;
+    if (l->dn0) l->dn0[k] = b.dn0;
+    if (l->weight) l->weight[k] = b.weight;
+    if (l->mode) l->mode[k] = b.mode;
+    if (l->crit1) l->crit1[k] = b.c1;
+    if (l->crit2) l->crit2[k] = b.c2;
+    if (l->en) l->en[k] = b.en;
+    if (l->et) l->et[k] = b.et;
+    const double t3[3] = {b.tds.x, b.tds.y, b.tds.z}, f3[3] = {b.friction.x, b.friction.y, b.friction.z};
+    for (int d = 0; d < 3; d++) {
+      if (l->tds) l->tds[3 * k + d] = t3[d];
+      if (l->friction) l->friction[3 * k + d] = f3[d];
+    }
+    if (l->unbroken) l->unbroken[k] = b.unbroken;
+  }
+  return DEM_OK;
+}
+// read_dump_particle_fragmentation: the saved bonds, by particle id (the state
+// of the last bond pass, dn and fn, starts at zero)
+int oracle_set_bonds(void* h, const dem_bond_list* l) {
+  Oracle& o = *(Oracle*)h;
+  if (!o.poly) return DEM_ERR_STATE;
+  std::vector<std::pair<uint64_t, int32_t>> ids;
+  index_of_ids(o, ids);
+  std::vector<Bond> lst(l->count);
+  for (uint64_t k = 0; k < l->count; k++) {
+    Bond& b = lst[k];
+    b.id_i = l->id_i[k];
+    b.id_j = l->id_j[k];
+    b.i = find_id(ids, b.id_i);
+    b.j = find_id(ids, b.id_j);
+    if (b.i < 0 || b.j < 0 || b.id_i >= b.id_j) return DEM_ERR_INVALID_ARG;
+    b.sub_i = l->sub_i[k];
+    b.sub_j = l->sub_j[k];
+    if (b.sub_i >= (uint32_t)o.shapes[o.type[b.i]].nv() || b.sub_j >= (uint32_t)o.shapes[o.type[b.j]].nv())
+      return DEM_ERR_INVALID_ARG;
+    b.dn0 = l->dn0[k];
+    b.weight = l->weight[k];
+    b.mode = l->mode[k];
+    b.c1 = l->crit1[k];
+    b.c2 = l->crit2[k];
+    b.en = l->en[k];
+    b.et = l->et[k];
+    b.tds = {l->tds[3 * k], l->tds[3 * k + 1], l->tds[3 * k + 2]};
+    b.friction = {l->friction[3 * k], l->friction[3 * k + 1], l->friction[3 * k + 2]};
+    b.unbroken = l->unbroken[k] ? 1 : 0;
+  }
+  std::stable_sort(lst.begin(), lst.end(), bond_less);
+  o.bonds.swap(lst);
+  o.brec.assign(o.bonds.size(), BondRec{});
+  o.broken_hist.clear();
+  bond_lists(o);
+  return DEM_OK;
+}
+int oracle_inner_bond_polyhedron(void* h) {
+  Oracle& o = *(Oracle*)h;
+  if (o.poly && !o.bonds.empty()) bond_force(o);
+  return DEM_OK;
+}
+int oracle_apply_interface_fracture_criterion(void* h, uint64_t* broken) {
+  Oracle& o = *(Oracle*)h;
+  const uint64_t b = o.poly ? fracture(o) : 0;
+  if (broken) *broken = b;
+  return DEM_OK;
+}
+int oracle_broken_interface_count(void* h, uint64_t* out) {
+  *out = ((Oracle*)h)->broken_total;
   return DEM_OK;
 }
 int oracle_rebuild_count(void* h, uint64_t* out) {
@@ -2031,6 +2544,46 @@ static inline void wobb(double* o, const OBBr& b) {
   wv(o + 6, b.e2);
   wv(o + 9, b.e3);
   wv(o + 12, b.ext);
+}
+// in (35): dn, n[3], dn0, weight, dt, kn, kt, damp_rate, meff, tds[3], cp[3], pos_i[3],
+// vel_i[3], vrot_i[3], pos_j[3], vel_j[3], vrot_j[3]
+// out (20): En, Et, tds[3], ft[3], f_i[3], torque_i[3], torque_j[3], fn[3] (= f_i - ft)
+int oracle_unit_bond_law(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 35 * c;
+    double* o = out + 20 * c;
+    dem_inner_bond_params prm{};
+    prm.kn = p[7];
+    prm.kt = p[8];
+    prm.damp_rate = p[9];
+    double En = 0, Et = 0;
+    V3 tds = rv(p + 11), ft{}, f{};
+    const V3 cp = rv(p + 14), pos_i = rv(p + 17), pos_j = rv(p + 26);
+    bond_law_core(p[0], rv(p + 1), p[4], p[5], p[6], prm, p[10], En, tds, Et, ft, cp, pos_i, rv(p + 20), f,
+                  rv(p + 23), pos_j, rv(p + 29), rv(p + 32));
+    o[0] = En;
+    o[1] = Et;
+    wv(o + 2, tds);
+    wv(o + 5, ft);
+    wv(o + 8, f);
+    wv(o + 11, cross(cp - pos_i, f) + V3{0, 0, 0});
+    wv(o + 14, cross(cp - pos_j, -f) + V3{0, 0, 0});
+    wv(o + 17, f - ft);
+  }
+  return DEM_OK;
+}
+// face areas of a shape scaled by h^2 (get_face_area(i, h), shape.hpp:359-362)
+int oracle_unit_face_areas(const double* vertices, int nv, const int32_t* face_sizes, const int32_t* face_vertices,
+                           int nf, double h, double* out) {
+  PShape sh;
+  for (int k = 0; k < nv; k++) sh.v.push_back(rv(vertices + 3 * k));
+  int off = 0;
+  for (int f = 0; f < nf; f++) {
+    std::vector<int> fv(face_vertices + off, face_vertices + off + face_sizes[f]);
+    off += face_sizes[f];
+    out[f] = face_area(sh, fv) * h * h;
+  }
+  return DEM_OK;
 }
 int oracle_unit_contact_force_core(int law, long n, const double* in, double* out) {
   for (long c = 0; c < n; c++) {

@@ -54,6 +54,14 @@ def load(rebuild: bool = True):
         sig("oracle_packing_profile", [_CTX, C.c_int, C.c_double, C.c_double, A.PD])
         sig("oracle_set_shapes", [_CTX, C.POINTER(A.Shape), C.c_int])
         sig("oracle_compute_vertices", [_CTX])
+        sig("oracle_set_inner_bond_params", [_CTX, C.c_int, C.POINTER(A.InnerBondParams)])
+        sig("oracle_stick_polyhedra", [_CTX, A.PU64, A.PD, C.c_uint64, C.c_double, A.PU64])
+        sig("oracle_bond_count", [_CTX, A.PU64])
+        sig("oracle_get_bonds", [_CTX, C.POINTER(A.BondList)])
+        sig("oracle_set_bonds", [_CTX, C.POINTER(A.BondList)])
+        sig("oracle_broken_interface_count", [_CTX, A.PU64])
+        sig("oracle_inner_bond_polyhedron", [_CTX])
+        sig("oracle_apply_interface_fracture_criterion", [_CTX, A.PU64])
         _LIB = lib
     return _LIB
 
@@ -74,7 +82,12 @@ class OracleBackend:
             "contact_polyhedron": "oracle_contact_sphere", "compute_vertices": "oracle_compute_vertices",
             "vertex_displ_over": "oracle_displ_over", "set_multimat": "oracle_set_multimat",
             "set_analysis": "oracle_set_analysis", "get_contact_state": "oracle_get_contact_state",
-            "stress_tensor": "oracle_stress_tensor"}
+            "stress_tensor": "oracle_stress_tensor", "set_inner_bond_params": "oracle_set_inner_bond_params",
+            "stick_polyhedra": "oracle_stick_polyhedra", "bond_count": "oracle_bond_count",
+            "get_bonds": "oracle_get_bonds", "set_bonds": "oracle_set_bonds",
+            "broken_interface_count": "oracle_broken_interface_count",
+            "inner_bond_polyhedron": "oracle_inner_bond_polyhedron",
+            "apply_interface_fracture_criterion": "oracle_apply_interface_fracture_criterion"}
 
     def __init__(self):
         self.lib = load()

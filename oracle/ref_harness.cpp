@@ -20,6 +20,7 @@
 #include <vector>
 
 #include <exaDEM/forcefield/contact_force.hpp>   // contact_force_core, common_kernels
+#include <exaDEM/forcefield/inner_bond_force.hpp>  // force_law_core of the inner bonds
 #include <exaDEM/shape.hpp>                      // shape, get_vertex, minkowski
 #include <exaDEM/shape_detection.hpp>            // filters and detection cores
 #include <exaDEM/shape_reader.hpp>               // read_shp
@@ -109,6 +110,36 @@ int ref_unit_contact_force_core(int law, long n, const double* in, double* out) 
     put(o + 3, ft);
     put(o + 6, mom_i);
     put(o + 9, exaDEM::compute_moments(cp, pos_i, f_i, mom_i));
+  }
+  return 0;
+}
+
+/* force_law_core (inner_bond_force.hpp:24-70) followed by compute_moments with a zero
+ * moment on both particles and fn = f_i - ft (inner_bond.hpp:166-183).
+ * in (35): dn, n[3], dn0, weight, dt, kn, kt, damp_rate, meff, tds[3], cp[3], pos_i[3],
+ *          vel_i[3], vrot_i[3], pos_j[3], vel_j[3], vrot_j[3]
+ * out (20): En, Et, tds[3], ft[3], f_i[3], torque_i[3], torque_j[3], fn[3] */
+int ref_unit_bond_law(long n, const double* in, double* out) {
+  for (long c = 0; c < n; c++) {
+    const double* p = in + 35 * c;
+    double* o = out + 20 * c;
+    exaDEM::InnerBondParams ibp;
+    ibp.kn_ = p[7];
+    ibp.kt_ = p[8];
+    ibp.damp_rate_ = p[9];
+    double En = 0, Et = 0;
+    Vec3d tds = V(p + 11), ft, f_i;
+    const Vec3d cp = V(p + 14), pos_i = V(p + 17), pos_j = V(p + 26);
+    exaDEM::force_law_core(p[0], V(p + 1), p[4], p[5], p[6], ibp, p[10], En, tds, Et, ft, cp, pos_i, V(p + 20),
+                           f_i, V(p + 23), pos_j, V(p + 29), V(p + 32));
+    o[0] = En;
+    o[1] = Et;
+    put(o + 2, tds);
+    put(o + 5, ft);
+    put(o + 8, f_i);
+    put(o + 11, exaDEM::compute_moments(cp, pos_i, f_i, Vec3d{}));
+    put(o + 14, exaDEM::compute_moments(cp, pos_j, -f_i, Vec3d{}));
+    put(o + 17, f_i - ft);
   }
   return 0;
 }
@@ -225,6 +256,14 @@ int ref_shape_derived(int s, double h, double* out) {
   out[0] = sh.compute_max_rcut();
   out[1] = sh.get_volume(h);
   put(out + 2, sh.get_Im(h));
+  return 0;
+}
+
+/* get_face_area(i, h) (shape.hpp:359-362) of every face, from compute_face_areas
+ * (shape.hpp:674-697) run by read_shp.  out (nf) */
+int ref_shape_face_areas(int s, double h, double* out) {
+  const exaDEM::shape& sh = g_shapes[s];
+  for (int f = 0; f < sh.get_number_of_faces(); f++) out[f] = sh.get_face_area(f, h);
   return 0;
 }
 

@@ -33,6 +33,7 @@ LAYOUT = {
     "angular": (15, 6, None),
     "surface": (11, 13, None),
     "cylinder": (11, 13, None),
+    "bond_law": (35, 20, None),
 }
 FILTER_KIND = {"filter_vv": 0, "filter_ve": 1, "filter_ee": 2}
 
@@ -142,6 +143,36 @@ def _contact_force_core(rng, n):
     r[:, 36:39] = pos_i + rng.standard_normal((n, 3))              # pos_j
     r[:, 39:42] = rng.standard_normal((n, 3))
     r[:, 42:45] = _maybe_zero(rng, rng.standard_normal((n, 3)), 0.3)
+    return r
+
+
+def _bond_law(rng, n):
+    """force_law_core inputs: dn around dn0 on both sides (tension and compression,
+    delta exactly 0), weights 1/k, zero and nonzero cumulated displacements and spins."""
+    r = np.zeros((n, 35))
+    dn0 = np.where(rng.random(n) < 0.3, 0.0, rng.standard_normal(n) * 1e-6)
+    u = rng.random(n)
+    dn = dn0 + rng.standard_normal(n) * 10.0 ** rng.uniform(-9, -2, n)
+    dn = np.where(u < 0.1, dn0, dn)                                 # delta exactly zero
+    r[:, 0] = dn
+    r[:, 1:4] = _unit(rng, n)
+    r[:, 4] = dn0
+    r[:, 5] = 1.0 / rng.integers(1, 9, n)                          # weight 1/(bonds of the interface)
+    r[:, 6] = 10.0 ** rng.uniform(-5, -3, n)                       # dt
+    kn = 10.0 ** rng.uniform(3, 7, n)
+    r[:, 7] = kn
+    r[:, 8] = kn * rng.uniform(0.5, 1.0, n)                        # kt
+    r[:, 9] = np.where(rng.random(n) < 0.05, 0.0, rng.uniform(0, 1, n))  # damp_rate
+    r[:, 10] = 10.0 ** rng.uniform(-3, 1, n)                       # meff
+    r[:, 11:14] = _maybe_zero(rng, rng.standard_normal((n, 3)) * 10.0 ** rng.uniform(-9, -3, (n, 1)), 0.3)  # tds
+    pos_i = rng.uniform(-5, 5, (n, 3))
+    r[:, 17:20] = pos_i
+    r[:, 14:17] = pos_i + rng.standard_normal((n, 3)) * 0.5        # contact point
+    r[:, 20:23] = _maybe_zero(rng, rng.standard_normal((n, 3)), 0.2)
+    r[:, 23:26] = _maybe_zero(rng, rng.standard_normal((n, 3)), 0.4)
+    r[:, 26:29] = pos_i + rng.standard_normal((n, 3))              # pos_j
+    r[:, 29:32] = _maybe_zero(rng, rng.standard_normal((n, 3)), 0.2)
+    r[:, 32:35] = _maybe_zero(rng, rng.standard_normal((n, 3)), 0.4)
     return r
 
 
@@ -364,6 +395,7 @@ def pair_keys(n: int, seed: int) -> np.ndarray:
 
 
 _GEN = {
+    "bond_law": _bond_law,
     "contact_force_core": _contact_force_core, "damping": _damping, "detect_vv": _detect_vv,
     "detect_ve": _detect_ve, "detect_ee": _detect_ee, "filter_vv": _filter_vv, "filter_ve": _filter_ve,
     "filter_ee": _filter_ee, "world_vertex": _world_vertex, "obb_intersect": _obb_intersect,
@@ -425,6 +457,36 @@ def run_vertex_face_oracle(lib, shape: dict, face: int, rows: np.ndarray) -> np.
     fn.argtypes = [C.POINTER(C.c_int32), C.c_int, C.c_int, C.c_double, C.c_long, PD, PD]
     assert fn(f.ctypes.data_as(C.POINTER(C.c_int32)), len(f), nv, float(shape["radius"]), rows.shape[0],
               _ptr(rows), _ptr(out)) == 0
+    return out
+
+
+FACE_AREA_H = (1.0, 0.8, 1.3)
+
+
+def face_areas_ref(lib, shape_index: int, nf: int) -> np.ndarray:
+    """get_face_area(f, h) of every face for the homotheties FACE_AREA_H (rows)."""
+    lib.ref_shape_face_areas.argtypes = [C.c_int, C.c_double, PD]
+    out = np.zeros((len(FACE_AREA_H), nf))
+    for k, h in enumerate(FACE_AREA_H):
+        row = np.zeros(nf)
+        assert lib.ref_shape_face_areas(shape_index, h, _ptr(row)) == 0
+        out[k] = row
+    return out
+
+
+def face_areas_oracle(lib, shape: dict) -> np.ndarray:
+    v = np.ascontiguousarray(shape["vertices"], dtype=np.float64).reshape(-1)
+    sizes = np.asarray([len(f) for f in shape["faces"]], dtype=np.int32)
+    fv = np.asarray([x for f in shape["faces"] for x in f], dtype=np.int32)
+    P32 = C.POINTER(C.c_int32)
+    fn = lib.oracle_unit_face_areas
+    fn.argtypes = [PD, C.c_int, P32, P32, C.c_int, C.c_double, PD]
+    out = np.zeros((len(FACE_AREA_H), len(sizes)))
+    for k, h in enumerate(FACE_AREA_H):
+        row = np.zeros(len(sizes))
+        assert fn(_ptr(v), len(v) // 3, sizes.ctypes.data_as(P32), fv.ctypes.data_as(P32), len(sizes), h,
+                  _ptr(row)) == 0
+        out[k] = row
     return out
 
 

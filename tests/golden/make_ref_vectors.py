@@ -6,7 +6,7 @@ own headers into oracle/_ref/libexadem_ref.so).  Each record holds seeded input
 rows (oracle/units.py) and the rows exaDEM's functions return on them; the
 vertex-face records also hold the shape, written by this project's .shp writer
 from its own cube, tetrahedron and octahedron builders, together with exaDEM's
-read_shp result for it.  tests/test_oracle_golden.py checks the oracle against
+read_shp result for it (vertices, OBB, face areas).  tests/test_oracle_golden.py checks the oracle against
 these outputs bit for bit wherever the sources are absent.
 
     python tests/golden/make_ref_vectors.py
@@ -58,6 +58,7 @@ def main() -> None:
             rec[f"{tag}/vertices"] = r["vertices"]
             rec[f"{tag}/obb"] = np.concatenate([np.asarray(r["obb"][k_], dtype=np.float64)
                                                 for k_ in ("center", "e1", "e2", "e3", "extent")])
+            rec[f"{tag}/face_areas"] = U.face_areas_ref(ref, r["index"], len(s["faces"]))
             for face in range(len(s["faces"])):
                 x = U.vertex_face_cases(s, face, ROWS // 4, 9200 + face)
                 rec[f"{tag}/vf{face}/in"] = x

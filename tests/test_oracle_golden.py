@@ -56,6 +56,7 @@ def test_shapes_and_vertex_face_match_exadem(data, orc, name):
     assert np.array_equal(bits(s["vertices"]), bits(data[f"{tag}/vertices"]))
     obb = np.concatenate([np.asarray(s["obb"][k], dtype=np.float64) for k in ("center", "e1", "e2", "e3", "extent")])
     assert np.array_equal(bits(obb), bits(data[f"{tag}/obb"]))
+    assert np.array_equal(bits(U.face_areas_oracle(orc, s)), bits(data[f"{tag}/face_areas"]))
     for face in range(len(s["faces"])):
         x = data[f"{tag}/vf{face}/in"]
         got = U.run_vertex_face_oracle(orc, s, face, x)

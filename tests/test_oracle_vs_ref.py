@@ -92,7 +92,7 @@ def test_shp_reader_and_shape_obb(libs):
     workloads.build_obb gives the shape OBB of build_obb_from_shape, bit for bit."""
     from exadem_gb300 import shp
 
-    ref, _ = libs
+    ref, orc_lib = libs
     files = _exadem_shape_files()
     assert len(files) >= 10
     nshapes = 0
@@ -116,6 +116,10 @@ def test_shp_reader_and_shape_obb(libs):
                 iom = m["i_over_m"]
                 mine = np.array([m["max_rcut"], h * h * h * m["volume"], h * h * iom[0], h * h * iom[1], h * h * iom[2]])
                 assert same_bits(d[None], mine[None]).all(), (f, h)
+            # the face areas (compute_face_areas; the criterion area of stick_polyhedra)
+            if all(len(fc) >= 3 for fc in m["faces"]):
+                assert same_bits(U.face_areas_ref(ref, r["index"], len(m["faces"])),
+                                 U.face_areas_oracle(orc_lib, m)).all(), f
     assert nshapes >= 40
 
 
