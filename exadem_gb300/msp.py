@@ -357,6 +357,10 @@ def deck_workload(deck: dict, base_dir=".", seed: int = 1, **flags):
         if op == "gravity_force":
             if "gravity" in prm:
                 gravity = tuple(_vec(prm["gravity"]))
+        elif op == "inner_bond_polyhedron" or op in ("rebind", "body", "condition"):
+            pass  # bonds: run by every step of a system with bonds; the others: block structure
+        elif not op.startswith("contact_"):
+            notes.append(f"compute_force: operator {op} ignored")
         elif op.startswith("contact_"):
             contact_op = op
             cfg = prm.get("config", {}) or {}
@@ -380,8 +384,21 @@ def deck_workload(deck: dict, base_dir=".", seed: int = 1, **flags):
     shapes: list = []
     polyhedra = contact_op.startswith("contact_polyhedron") or "polyhedron" in contact_op
     lattices, fields = [], []
+    ibp = None
     for op, prm in _expand(deck, "input_data"):
-        if op == "particle_type":
+        if op == "add_cube":  # AddShapeCubeOperator (src/shape/add_cube.cpp:31-58)
+            from .workloads import exadem_cube
+
+            name = str(prm.get("name", "cube"))
+            shapes.append(exadem_cube(name, float(prm.get("length", 1.0)), float(prm.get("minkowski", 0.01))))
+            if name not in types:
+                types.append(name)
+            for k in prm:
+                if k not in ("name", "length", "minkowski"):
+                    notes.append(f"add_cube: key {k} is not a slot of add_cube; ignored")
+        elif op == "inner_bond_params":
+            ibp = _inner_bond_params(prm)
+        elif op == "particle_type":
             for t in prm.get("type", []):
                 if t not in types:
                     types.append(t)
@@ -544,4 +561,40 @@ def deck_workload(deck: dict, base_dir=".", seed: int = 1, **flags):
     w = Workload("deck", p, arr, surfaces=surfaces, cylinders=cylinders, meshes=meshes, steps=steps,
                  info={"contact_operator": contact_op, "types": types, "notes": notes})
     w.shapes = shapes if polyhedra else None
+    # fragmentation (config_fragmentation.msp prepro_fragmentation): stick_polyhedra
+    # when apply_particle_sticking is set; the cluster field is 0 for the particles
+    # a lattice places (one cluster)
+    if polyhedra and glob.get("apply_particle_sticking") is True:
+        if ibp is None:
+            raise ValueError("apply_particle_sticking needs inner_bond_params in input_data")
+        w.bonds = {"params": ibp, "cluster": np.zeros(n), "threshold": float(glob.get("sticking_threshold", 2e-5))}
     return w
+
+
+def _inner_bond_params(prm: dict):
+    """inner_bond_params (src/forcefield/multimat_inner_bond.cpp:104-200): a
+    default_config dict, or per group pair lists (group1, group2, kn, kt,
+    damp_rate and g, gn + gt or g + sigma), as System.set_inner_bond_params takes."""
+    def one(c):
+        out = {k: float(c[k]) for k in ("kn", "kt", "damp_rate") if k in c}
+        for k in ("g", "gn", "gt", "sigma"):
+            if k in c:
+                out[k] = float(c[k])
+        if not {"kn", "kt", "damp_rate"} <= set(out) or not ("g" in out or {"gn", "gt"} <= set(out)):
+            raise ValueError(f"inner_bond_params: incomplete parameters {c}")
+        return out
+
+    default = prm.get("default_config")
+    if prm.get("group1") is None:
+        if default is None:
+            raise ValueError("inner_bond_params: define group1/group2 lists or a default_config")
+        return one(default)
+    g1, g2 = [int(x) for x in prm["group1"]], [int(x) for x in prm["group2"]]
+    ng = max(g1 + g2) + 1
+    table = [[one(default) if default is not None else None for _ in range(ng)] for _ in range(ng)]
+    for p_, (a, b) in enumerate(zip(g1, g2)):
+        c = {k: prm[k][p_] for k in ("kn", "kt", "damp_rate", "g", "gn", "gt", "sigma") if prm.get(k) is not None}
+        table[a][b] = table[b][a] = one(c)
+    if any(x is None for row in table for x in row):
+        raise ValueError("inner_bond_params: a group pair has no parameters and there is no default_config")
+    return table

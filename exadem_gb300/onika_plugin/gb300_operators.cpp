@@ -20,6 +20,8 @@
 
 #include <exaDEM/cylinder.hpp>
 #include <exaDEM/forcefield/contact_parameters.hpp>
+#include <exaDEM/forcefield/inner_bond_parameters.hpp>
+#include <exaDEM/forcefield/multimat_parameters.hpp>
 #include <exaDEM/surface.hpp>
 
 #include "gb300_bridge.hpp"
@@ -65,6 +67,27 @@ inline Bridge& configured(GridT& grid, F&& edit) {
   b.configure(p);
   b.pull(grid);
   return b;
+}
+// inner_bond_params (multimat_inner_bond.cpp:104-200) as the library's table:
+// one group (a default_config) becomes the one set for every pair
+inline void set_inner_bond_params(Bridge& b, const MultiMatParamsT<InnerBondParams>& m) {
+  const int ng = m.number_of_groups_;
+  std::vector<dem_inner_bond_params> t;
+  for (int i = 0; i < ng * ng; i++) {
+    const InnerBondParams& q = m.multimat_cp_[i];
+    dem_inner_bond_params p{};
+    p.kn = q.kn_;
+    p.kt = q.kt_;
+    p.damp_rate = q.damp_rate_;
+    p.mode = q.mode_ == RuptureMode::EnergySeparateMode         ? DEM_RUPTURE_ENERGY_SEPARATE
+             : q.mode_ == RuptureMode::StressEnergySeparateMode ? DEM_RUPTURE_STRESS_ENERGY_SEPARATE
+                                                                : DEM_RUPTURE_ENERGY_MIXED;
+    p.crit1 = q.crit1_;
+    p.crit2 = q.crit2_;
+    t.push_back(p);
+  }
+  if (t.empty()) gb300::check(DEM_ERR_INVALID_ARG, nullptr, "inner_bond_params: no parameters");
+  gb300::check(dem_set_inner_bond_params(b.ctx, ng <= 1 ? 0 : ng, t.data()), b.ctx, "inner_bond_params");
 }
 }  // namespace gb300_detail
 
@@ -223,6 +246,69 @@ class GB300DisplOver : public OperatorNode {
 template <class G> using GB300SphereDispl = GB300DisplOver<G, false>;
 template <class G> using GB300VertexDispl = GB300DisplOver<G, true>;
 
+// stick_polyhedra (src/polyhedron/stick_polyhedra.cpp:365-369): bonds between the
+// touching faces of the particles of one cluster (the grid's cluster field).
+template <typename GridT>
+class GB300StickPolyhedra : public OperatorNode {
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT, REQUIRED);
+  ADD_SLOT(double, sticking_threshold, INPUT, REQUIRED);
+  ADD_SLOT(MultiMatParamsT<InnerBondParams>, multimat_ibp, INPUT, REQUIRED);
+
+ public:
+  inline void execute() final {
+    Bridge& b = gb300_detail::configured(*grid, [](dem_params&) {});
+    gb300_detail::set_inner_bond_params(b, *multimat_ibp);
+    std::vector<uint64_t> ids;
+    std::vector<double> cluster;
+    auto cells = grid->cells();
+    for (size_t c = 0; c < grid->number_of_cells(); c++) {
+      if (grid->is_ghost_cell(c)) continue;
+      for (size_t p = 0; p < cells[c].size(); p++) {
+        ids.push_back(cells[c][field::id][p]);
+        cluster.push_back(cells[c][field::cluster][p]);
+      }
+    }
+    uint64_t nb = 0;
+    gb300::check(dem_stick_polyhedra(b.ctx, ids.data(), cluster.data(), ids.size(), *sticking_threshold, &nb), b.ctx,
+                 "stick_polyhedra");
+  }
+};
+
+// inner_bond_polyhedron (src/polyhedron/inner_bond_force.cu:138-141)
+template <typename GridT>
+class GB300InnerBond : public OperatorNode {
+  ADD_SLOT(GridT, grid, INPUT_OUTPUT, REQUIRED);
+  ADD_SLOT(MultiMatParamsT<InnerBondParams>, multimat_ibp, INPUT, REQUIRED);
+  ADD_SLOT(double, dt, INPUT, REQUIRED);
+
+ public:
+  inline void execute() final {
+    Bridge& b = gb300_detail::configured(*grid, [&](dem_params& p) { p.dt = *dt; });
+    gb300_detail::set_inner_bond_params(b, *multimat_ibp);
+    gb300::check(dem_inner_bond_polyhedron(b.ctx), b.ctx, "inner_bond_polyhedron");
+    b.push(*grid, {gb300::FX, gb300::MX});
+  }
+};
+
+// apply_interface_fracture_criterion (src/interaction/apply_interface_fracture_criterion.cu:92-95);
+// the library applies broken_interface_friction_updater in the same pass.
+template <typename GridT>
+class GB300FractureCriterion : public OperatorNode {
+  ADD_SLOT(GridT, grid, INPUT, REQUIRED);
+  ADD_SLOT(bool, result, OUTPUT);
+  ADD_SLOT(bool, display, INPUT, false);
+
+ public:
+  inline void execute() final {
+    Bridge& b = gb300_detail::configured(*grid, [](dem_params&) {});
+    uint64_t broken = 0;
+    gb300::check(dem_apply_interface_fracture_criterion(b.ctx, &broken), b.ctx, "apply_interface_fracture_criterion");
+    if (*display && broken > 0)
+      lout << broken << (broken == 1 ? " interface has been broken." : " interfaces have been broken.") << std::endl;
+    *result = broken > 0;
+  }
+};
+
 // register_surface / register_cylinder (src/driver/drivers.hpp:291-320), stationary drivers.
 template <typename GridT>
 class GB300RegisterSurface : public OperatorNode {
@@ -285,6 +371,13 @@ ONIKA_AUTORUN_INIT(gb300_operators) {
   f->register_factory("combined_compute_epilog", make_grid_variant_operator<GB300Epilog>);
   f->register_factory("particle_displ_over", make_grid_variant_operator<GB300SphereDispl>);
   f->register_factory("vertex_displ_over", make_grid_variant_operator<GB300VertexDispl>);
+  f->register_factory("stick_polyhedra", make_grid_variant_operator<GB300StickPolyhedra>);
+  f->register_factory("inner_bond_polyhedron", make_grid_variant_operator<GB300InnerBond>);
+  f->register_factory("apply_interface_fracture_criterion", make_grid_variant_operator<GB300FractureCriterion>);
+  // done by the criterion pass, the neighbour build and the bond list of the library
+  f->register_factory("broken_interface_friction_updater", make_grid_variant_operator<GB300NoOp>);
+  f->register_factory("update_interfaces", make_grid_variant_operator<GB300NoOp>);
+  f->register_factory("update_persistent_interactions", make_grid_variant_operator<GB300NoOp>);
   f->register_factory("register_surface", make_grid_variant_operator<GB300RegisterSurface>);
   f->register_factory("register_cylinder", make_grid_variant_operator<GB300RegisterCylinder>);
 }

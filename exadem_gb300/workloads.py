@@ -83,6 +83,9 @@ def save_workload(w: Workload, path) -> None:
                                "center": list(m.get("center", (0, 0, 0))), "quat": list(m.get("quat", (1, 0, 0, 0)))})
         arrays[f"m{k}/vertices"] = np.asarray(m["vertices"], dtype=np.float64)
         arrays[f"m{k}/edges"] = np.asarray(m["edges"], dtype=np.int32)
+    if w.bonds:
+        meta["bonds"] = {"params": w.bonds["params"], "threshold": float(w.bonds["threshold"])}
+        arrays["b/cluster"] = np.asarray(w.bonds["cluster"], dtype=np.float64)
     arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
     np.savez_compressed(path, **arrays)
 
@@ -116,6 +119,9 @@ def load_workload(path) -> Workload:
                             for d in meta["cylinders"]],
                  meshes=meshes, steps=meta["steps"], info=meta["info"])
     w.shapes = shapes or None
+    if "bonds" in meta:
+        w.bonds = {"params": meta["bonds"]["params"], "threshold": meta["bonds"]["threshold"],
+                   "cluster": np.ascontiguousarray(z["b/cluster"])}
     return w
 
 
@@ -467,6 +473,30 @@ def shape_octahedron(a=1.0, radius=0.01):
     e = [[0, 2], [2, 1], [1, 3], [3, 0], [0, 4], [2, 4], [1, 4], [3, 4], [0, 5], [2, 5], [1, 5], [3, 5]]
     f = [[0, 2, 4], [2, 1, 4], [1, 3, 4], [3, 0, 4], [0, 5, 2], [2, 5, 1], [1, 5, 3], [3, 5, 0]]
     return _shape("Octahedron", v, e, f, radius, math.sqrt(2.0) / 3.0 * a ** 3, a * a / 10.0)
+
+
+def exadem_cube(name="cube", length=1.0, minkowski=0.01):
+    """The cube of exaDEM's add_cube operator, restating basic_shape::create_cube
+    (src/shape/include/exaDEM/shape/basic_shape/cube.hpp:14-88): unit-cube
+    vertices scaled by the length, its edge and face order, the volume and the
+    inertia over mass of the Minkowski-rounded cube."""
+    c, r, pi = float(length), float(minkowski), math.pi
+    volume = c * c * c + 6.0 * c * c * r + 3.0 * pi * r * r * c + (4.0 / 3.0) * pi * r * r * r
+    inertia = (1.0 / 6.0) * math.pow(c, 5)
+    d = 0.5 * (c + r)
+    i_face = (1.0 / 12.0) * c * c * r * (c * c + r * r)
+    v_face = c * c * r
+    inertia += 6.0 * (i_face + v_face * d * d)
+    v_edges = 3.0 * pi * r * r * c
+    inertia += v_edges * ((c * c) / 12.0 + (r * r) / 2.0)
+    inertia += (8.0 / 15.0) * pi * math.pow(r, 5)
+    iom = inertia / (1.0 * 1.0 * 1.0 * volume) * 1.0  # I / get_volume() * (1, 1, 1)
+    unit = [[-0.5, -0.5, -0.5], [0.5, -0.5, -0.5], [0.5, 0.5, -0.5], [-0.5, 0.5, -0.5],
+            [-0.5, -0.5, 0.5], [0.5, -0.5, 0.5], [0.5, 0.5, 0.5], [-0.5, 0.5, 0.5]]
+    v = [[x * c for x in p] for p in unit]
+    e = [[0, 1], [1, 2], [2, 3], [3, 0], [4, 5], [5, 6], [6, 7], [7, 4], [0, 4], [1, 5], [2, 6], [3, 7]]
+    f = [[3, 2, 1, 0], [4, 5, 6, 7], [0, 1, 5, 4], [2, 3, 7, 6], [4, 7, 3, 0], [1, 2, 6, 5]]
+    return _shape(name, v, e, f, r, volume, (iom, iom, iom))
 
 
 def polyhedra_floor(n=200_000, side=None, density=0.02, seed=3, steps=2000, dt=1e-4, skin=0.05,

@@ -24,6 +24,7 @@
 #include <exaDEM/shape.hpp>                      // shape, get_vertex, minkowski
 #include <exaDEM/shape_detection.hpp>            // filters and detection cores
 #include <exaDEM/shape_reader.hpp>               // read_shp
+#include <exaDEM/shape/basic_shape/cube.hpp>     // create_cube (add_cube)
 #include <exaDEM/basic_types.hpp>                // compute_obb
 #include <exaDEM/angular_acceleration.hpp>       // PushToAngularAccelerationFunctor
 #include <exaDEM/push_to_quaternion.hpp>         // PushToQuaternionFunctor
@@ -223,6 +224,14 @@ int ref_read_shps(const char* path, int* first, int* count) {
   return 0;
 }
 /* counts (4): nv, ne, nf, size of the face array (faces_[0] = nf, then per face its count and vertices) */
+/* basic_shape::create_cube (add_cube): appends the cube to the shapes read so
+ * far; *index is its index for ref_shape_info / ref_shape_arrays. */
+int ref_create_cube(double length, double minkowski, int* index) {
+  g_shapes.push_back(exaDEM::basic_shape::create_cube("cube", length, minkowski));
+  *index = (int)g_shapes.size() - 1;
+  return 0;
+}
+
 int ref_shape_info(int s, int64_t* counts) {
   const exaDEM::shape& sh = g_shapes[s];
   counts[0] = sh.get_number_of_vertices();

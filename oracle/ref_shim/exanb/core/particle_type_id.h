@@ -4,3 +4,7 @@
 namespace exanb {
 using ParticleTypeMap = std::map<std::string, int>;
 }
+// exaDEM's headers name it unqualified (exaNBody's own headers make it visible there)
+namespace exaDEM {
+using exanb::ParticleTypeMap;
+}

@@ -31,6 +31,7 @@ inline constexpr Tag<Vec3d, 16> vrot{};
 inline constexpr Tag<Vec3d, 17> arot{};
 inline constexpr Tag<Vec3d, 18> mom{};
 inline constexpr Tag<Vec3d, 19> inertia{};
+inline constexpr Tag<double, 20> cluster{};
 }  // namespace field
 struct MockCell {
   std::size_t size() const { return 0; }

@@ -95,3 +95,29 @@ def test_fixture_steps_on_oracle(key):
     p = o.particles()
     assert all(np.isfinite(p[k]).all() for k in ("rx", "ry", "rz", "vx", "vy", "vz"))
     o.close()
+
+
+@needs_src
+@pytest.mark.parametrize("test,g", [("traction", 1e-2), ("shear", 5e-3)])
+def test_fragmentation_verification_deck(tmp_path, test, g):
+    """exaDEM's bonded-cube verification decks (traction and shear of two cubes
+    made by add_cube, stuck by stick_polyhedra): the deck gives the cube of
+    create_cube and, through inner_bond_params and apply_particle_sticking, four
+    bonds with the criterion 2 A g of the 0.98 x 0.98 face.  The decks' imposed
+    motion (pas_libere_pas_delivre, set_velocity in compute_force) is reported
+    as ignored."""
+    from oracle.oracle import oracle_system
+
+    src = EXADEM / "example/polyhedra/fragmentation/verification_test" / test / f"{test}.msp"
+    text = src.read_text().replace("GC", repr(g))  # the value its run script substitutes
+    p = tmp_path / f"{test}.msp"
+    p.write_text(text)
+    w = msp.deck_workload(msp.load_deck(p, [EXADEM / "data/config"]), base_dir=src.parent)
+    assert w.n == 2 and w.shapes[0]["name"] == "cube" and w.bonds is not None
+    assert any("pas_libere_pas_delivre" in x for x in w.info["notes"])
+    s = w.build(oracle_system)
+    b = s.bonds()
+    assert s.bond_count() == 4 and np.all(b["weight"] == 0.25)
+    face = 0.98 * 0.98
+    assert np.allclose(b["crit1"], 2 * face * g, rtol=1e-14, atol=0)
+    # (the decks' domain is periodic in y, which the polyhedron path does not run)

@@ -46,3 +46,11 @@ def test_gpu_checkpoint_resumes_on_oracle(native_lib, tmp_path):
     assert np.array_equal(lg["friction"].view(np.uint64), lo["friction"].view(np.uint64))
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("fused", [0, 1])
+def test_restart_fragmentation(native_lib, tmp_path, fused):
+    """Bonds saved before the impact and restored (read_dump_particle_fragmentation)
+    break the same interfaces with the same bits as the run that never stopped."""
+    flags = dict(fused_step=fused, fp32_broad_phase=fused, fp32_contact_screen=fused)
+    run_restart(W.fragment_blocks(nblocks=2, **flags), None, 40, 300, tmp_path)

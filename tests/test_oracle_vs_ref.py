@@ -123,6 +123,25 @@ def test_shp_reader_and_shape_obb(libs):
     assert nshapes >= 40
 
 
+@pytest.mark.parametrize("length,mink", [(1.0, 0.01), (0.98, 0.01), (0.25, 1e-4), (2.5, 0.2)])
+def test_add_cube_shape(libs, length, mink):
+    """workloads.exadem_cube against exaDEM's create_cube (add_cube): vertices,
+    edges, faces, volume, inertia over mass and shape OBB, bit for bit."""
+    from exadem_gb300 import workloads as W
+
+    ref, orc_lib = libs
+    idx = C.c_int()
+    ref.ref_create_cube.argtypes = [C.c_double, C.c_double, C.POINTER(C.c_int)]
+    assert ref.ref_create_cube(length, mink, C.byref(idx)) == 0
+    r, m = U._ref_shape(ref, idx.value), W.exadem_cube("cube", length, mink)
+    assert r["faces"] == m["faces"] and np.array_equal(r["edges"], np.asarray(m["edges"]))
+    for k in ("vertices", "radius", "volume", "i_over_m"):
+        assert same_bits(np.atleast_2d(r[k]), np.atleast_2d(np.asarray(m[k], dtype=np.float64))).all(), k
+    for k in ("center", "e1", "e2", "e3", "extent"):
+        assert same_bits(np.atleast_2d(r["obb"][k]), np.atleast_2d(np.asarray(m["obb"][k]))).all(), ("obb", k)
+    assert same_bits(U.face_areas_ref(ref, idx.value, 6), U.face_areas_oracle(orc_lib, m)).all()
+
+
 def _shape_files(tmp_path):
     from exadem_gb300 import shp, workloads as W
 

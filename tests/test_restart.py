@@ -60,6 +60,29 @@ def test_restart_polyhedra_oracle(tmp_path):
     run_restart(W.polyhedra_lattice(nx=5, ny=5, nz=4, vmax=0.5), oracle_system, 150, 100, tmp_path)
 
 
+def test_restart_fragmentation_oracle(tmp_path):
+    """With bonds: the checkpoint (write_dump_particle_fragmentation) carries the
+    bond list; stopped before the impact, the restarted run breaks the same
+    interfaces with the same bits."""
+    from oracle.oracle import oracle_system
+
+    w = W.fragment_blocks(nblocks=2)
+    run_restart(w, oracle_system, 40, 300, tmp_path)
+    a = w.build(oracle_system)
+    a.first_iteration()
+    a.step(40)
+    path = tmp_path / "frag.npz"
+    dump.write_dump_particle_fragmentation(a, path, timestep=40)
+    c = w.build(oracle_system)
+    dump.read_dump_particle_fragmentation(c, path)
+    a.step(300)
+    c.step(300)
+    assert a.broken_interface_count() > 0 and c.broken_interface_count() == a.broken_interface_count()
+    ba, bc = a.bonds(), c.bonds()
+    for k in ba:
+        assert np.array_equal(np.asarray(ba[k]).view(np.uint8), np.asarray(bc[k]).view(np.uint8)), k
+
+
 def test_restart_rejects_unknown_ids(tmp_path):
     from oracle.oracle import oracle_system
 
