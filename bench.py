@@ -52,7 +52,8 @@ CONTACT_BYTES_PER_INTERACTION = 104
 # write r, v, omega, alpha, q, a (19).
 PARTICLE_BYTES_PER_STEP = 344
 # Untimed steps before the warm-up, per workload (--preroll overrides).
-PREROLL = {"spheres": 3000, "polyhedra": 0, "polyhedra_dense": 0, "drums": 0, "mixer": 300, "polyhedra_mesh": 0}
+PREROLL = {"spheres": 3000, "polyhedra": 0, "polyhedra_dense": 0, "drums": 0, "mixer": 300, "polyhedra_mesh": 0,
+           "fragments": 0}
 # DRAM bytes (read + write) per launch of k_cfused per listed pair and of
 # k_fused_epilog per particle, from the ncu capture of the pre-rolled 250k-sphere
 # bed (the same workload at 1/8 of its size); they scale with the listed pairs and
@@ -79,7 +80,8 @@ def parse():
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--n", type=int, default=None, help="particle count (default: the workload's)")
     ap.add_argument("--workload", default="spheres",
-                    choices=["spheres", "polyhedra", "polyhedra_dense", "drums", "mixer", "polyhedra_mesh"],
+                    choices=["spheres", "polyhedra", "polyhedra_dense", "drums", "mixer", "polyhedra_mesh",
+                             "fragments"],
                     help="spheres: 2M spheres on a floor (headline); polyhedra: 200k polyhedra deposition; "
                          "polyhedra_dense: polyhedra on a dense lattice; drums: 256 rotating drums batched; "
                          "mixer: 50k spheres falling into a mesh (STL) mixer")
@@ -224,6 +226,9 @@ def _workload(args):
         return W.drums_batch(nsys=args.systems, nmax=args.n or 200_000, **flags)
     if args.workload == "mixer":
         return W.spheres_mixer(n=args.n, **flags)
+    if args.workload == "fragments":
+        return W.fragment_blocks(nblocks=max(1, round((args.n or 128_000) / 125)), nx=5, ny=5, nz=5, seed=5,
+                                 steps=400, **flags)
     if args.workload == "polyhedra_mesh":
         side = round(((args.n or 4800) / 3) ** 0.5)
         return W.polyhedra_mesh_terrain(nx=side, ny=side, nz=3, amp=0.5, waves=6, m=60, **flags)
@@ -258,6 +263,9 @@ def build_from_host(w, arrays):
     for kw in w.meshes:
         s.register_mesh(**kw)
     s.set_particles(arrays)
+    if w.bonds:
+        s.set_inner_bond_params(w.bonds["params"])
+        s.stick_polyhedra(arrays["id"], w.bonds["cluster"], w.bonds["threshold"])
     return s
 
 
@@ -272,6 +280,9 @@ WORKLOAD_DESC = {
              "30% fill, 2 rad/s, periodic along the axis), Hooke kn=1e4 kt=8e3 mu=0.4, dt=5e-4",
     "polyhedra_mesh": "polyhedra_mesh_terrain: 4800 cubes/tetrahedra/octahedra (40 x 40 x 3 lattice) falling on "
                       "a 7200-triangle terrain mesh (Minkowski 0.02) inside four walls, Hooke kn=1e4, dt=5e-4",
+    "fragments": "fragment_blocks: 1024 blocks of 5 x 5 x 5 unit cubes (Minkowski 0.01), face-bonded per block by "
+                 "stick_polyhedra (1.2M bonds, 307k interfaces; kn=1e4 kt=8e3 damp 0.87, mixed mode g=0.05), "
+                 "turned and falling at 3 m/s onto a floor; Hooke kn=1e5 kt=8e4 mu=0.3, dt=1e-4",
     "mixer": "spheres_mixer: 50,304 spheres r=2 (SC lattice 4.1 in a cylinder r=92) falling into a mesh mixer "
              "(wall, bottom, 4 blades: 2064 triangles, Minkowski 0.1), Hooke kn=1e3 kt=1e3 mu=0.5, dt=1e-3",
 }

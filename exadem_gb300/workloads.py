@@ -602,7 +602,7 @@ def fragment_blocks(nblocks=2, nx=3, ny=3, nz=3, edge=1.0, radius=0.01, density=
     exaDEM's two-fragments example, mixed mode g 0.05: at vz -3 part of the
     interfaces break at the impact); contacts: Hooke kn, kt = 0.8 kn, mu 0.3,
     damp_rate 0.87.  The bond damping is not scaled by the bond weight
-    (inner_bond_force.hpp:41), so kn must stay small enough for the explicit
+    (inner_bond_force.hpp:45), so kn must stay small enough for the explicit
     step: damp_rate 2 sqrt(kn m/2) dt x bonds per particle well below 2 m."""
     shp = shape_cube(edge, radius)
     rng = np.random.default_rng(seed)
