@@ -59,9 +59,9 @@ PREROLL = {"spheres": 3000, "polyhedra": 0, "polyhedra_dense": 0, "drums": 0, "m
 # bed (the same workload at 1/8 of its size); they scale with the listed pairs and
 # the particles.  Both kernels run their FP64 pipe at the fraction recorded here
 # (sm__pipe_fp64_cycles_active of peak sustained).
-TRAFFIC = {"source": "profiles/k_cfused_epilog_spheres_bed_250k.md",
-           "contact_bytes_per_listed_pair": 188.0, "epilog_bytes_per_particle": 445.0,
-           "contact_fp64_pipe_active": 0.825, "epilog_fp64_pipe_active": 0.820}
+TRAFFIC = {"source": "profiles/k_cfused_fp64_lanes_spheres_bed_250k.md",
+           "contact_bytes_per_listed_pair": 212.0, "epilog_bytes_per_particle": 445.0,
+           "contact_fp64_pipe_active": 0.807, "epilog_fp64_pipe_active": 0.820}
 
 
 def parse():
@@ -657,7 +657,7 @@ def run_native(args, rank, world, local, dist):
                 "algorithmic_bytes_per_unit": CONTACT_BYTES_PER_INTERACTION, "avg_launch_ms": t_law * 1e3,
                 "share_of_step": shares.get("contact", 0.0),
                 "traffic_source": TRAFFIC["source"] if fused_contact else None,
-                "traffic_scaling": ("188 B per listed pair measured at 250k spheres (826k listed pairs), "
+                "traffic_scaling": ("212 B per listed pair measured at 250k spheres (826k listed pairs), "
                                     "times the listed pairs here") if fused_contact else None,
                 "fp64_pipe_active": TRAFFIC["contact_fp64_pipe_active"] if fused_contact else None,
                 "note": "FP64-pipe bound, not HBM bound: the FP64 pipe runs at the fp64_pipe_active fraction of "

@@ -59,9 +59,17 @@ struct CArgs {
   uint32_t* L1;
   uint32_t* L2;
   double* D[7];  // dn, n(3), cp(3) of the L2 entries
-  unsigned long long* cnt;  // [0] L1 count, [1] L2 count
+  unsigned long long* cnt;  // [0] L1 count (particle pairs), [1] L2 count, [2] driver pairs of L1
+  uint64_t l1cap;           // L1 entries: particle pairs from the front, driver pairs from the back
   unsigned long long* n_active;
 };
+
+// L1 as one list: the particle pairs (front, n1 of them), then the driver pairs
+// (stored from the back).  Grouping the two kinds keeps each warp on one
+// detection and one law, so neither runs with the other's lanes idle.
+__device__ __forceinline__ uint32_t l1_at(const CArgs& a, uint64_t w, uint64_t n1) {
+  return w < n1 ? a.L1[w] : a.L1[a.l1cap - 1 - (w - n1)];
+}
 
 __device__ __forceinline__ void write_result(const CArgs& a, uint64_t k, V3 ft, V3 mo, V3 f, V3 ti, V3 tj) {
   a.I.ft[0][k] = ft.x;
@@ -99,10 +107,11 @@ __global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
   const uint64_t stride = (uint64_t)gridDim.x * FT;
   for (uint64_t base = (uint64_t)blockIdx.x * FT; base < ni; base += stride) {
   const uint64_t k = base + threadIdx.x;
-  bool want = false;
+  bool want = false, drv = false;
   if (k < ni) {
     const uint32_t meta = a.I.meta[k];
     want = true;
+    drv = meta_type(meta) != DEM_ITYPE_VERTEX_VERTEX;
     if (a.screen && meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
       const uint32_t i = a.I.owner[k], j = a.I.partner[k];
       const V3 ri = ldv(a.P, RX, i);
@@ -124,16 +133,21 @@ __global__ void __launch_bounds__(FT) k_cscreen(CArgs a) {
       }
     }
   }
-  const uint32_t pos = warp_append(want, a.cnt);
-  if (want) a.L1[pos] = (uint32_t)k;
+  drv = drv && want;
+  const uint32_t pos = warp_append(want && !drv, a.cnt);
+  const uint32_t pd = warp_append(drv, a.cnt + 2);
+  if (want && !drv) a.L1[pos] = (uint32_t)k;
+  if (drv) a.L1[a.l1cap - 1 - pd] = (uint32_t)k;
   }
 }
 
-// FP64 detection of interaction k; a pair that does not touch, and the cohesive
-// attraction before contact, are finished here.  Returns true for an
-// overlapping pair, whose law is left to the caller with (dn, n, cpos).
-__device__ __forceinline__ bool detect_pair(const CArgs& a, uint32_t k, double& dn, V3& n, V3& cpos) {
-  bool heavy = false;
+// FP64 detection of interaction k; a pair that does not touch is finished here.
+// Returns PAIR_DONE for it, PAIR_HOOKE for an overlapping pair and PAIR_ATTRACT
+// for the cohesive attraction before contact; their law is left to the caller
+// (hooke_pair, attract_pair) with (dn, n, cpos).
+constexpr int PAIR_DONE = 0, PAIR_HOOKE = 1, PAIR_ATTRACT = 2;
+__device__ __forceinline__ int detect_pair(const CArgs& a, uint32_t k, double& dn, V3& n, V3& cpos) {
+  int kind = PAIR_DONE;
   const uint32_t meta = a.I.meta[k];
   const uint32_t i = a.I.owner[k], j = a.I.partner[k];
   const V3 ri = ldv(a.P, RX, i);
@@ -189,7 +203,6 @@ __device__ __forceinline__ bool detect_pair(const CArgs& a, uint32_t k, double& 
     dncut = a.pt.drv(a.cpd, a.P.group[i], j).dncut;
   }
   if (a.cohesive) contact = (contact || emu_le(dn, dncut));
-  const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
   if (!contact) {
     a.cs.write(k, 0.0, cpos, mk(0, 0, 0), mk(0, 0, 0));  // item.reset(), dn = 0
     if (a.R.live[k] || a.cs.dn) {
@@ -198,34 +211,46 @@ __device__ __forceinline__ bool detect_pair(const CArgs& a, uint32_t k, double& 
       a.R.live[k] = 0;
     }
   } else if (a.cohesive && emu_ge0(dn)) {
-    // cohesive attraction before contact (contact_force.hpp:165-173): f = fn_value n, ft = 0
-    const dem_contact_params& hkp =
-        is_vv ? a.pt.pair(a.cp, a.P.group[i], a.P.group[j]) : a.pt.drv(a.cpd, a.P.group[i], j);
-    const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
-    const V3 f = mk(0, 0, 0) + fn_value * n;
-    const V3 ti = cross(cpos - ri, f) + mo;
-    const V3 tj = is_vv ? cross(cpos - rj, -f) + (-mo) : mk(0, 0, 0);
-    write_result(a, k, mk(0, 0, 0), mo, f, ti, tj);
-    a.R.live[k] = 1;
-    a.cs.write(k, dn, cpos, f - mk(0, 0, 0), mk(0, 0, 0));  // ft = 0 before contact
+    kind = PAIR_ATTRACT;
   } else {
-    heavy = true;
+    kind = PAIR_HOOKE;
   }
-  return heavy;
+  return kind;
+}
+
+// cohesive attraction before contact (contact_force.hpp:165-173): f = fn_value n, ft = 0
+__device__ __forceinline__ void attract_pair(const CArgs& a, uint32_t k, double dn, V3 n, V3 cpos) {
+  const uint32_t meta = a.I.meta[k];
+  const uint32_t i = a.I.owner[k], j = a.I.partner[k];
+  const bool is_vv = meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX;
+  const V3 ri = ldv(a.P, RX, i);
+  const V3 mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+  const dem_contact_params& hkp =
+      is_vv ? a.pt.pair(a.cp, a.P.group[i], a.P.group[j]) : a.pt.drv(a.cpd, a.P.group[i], j);
+  const double fn_value = (hkp.fc / hkp.dncut) * dn - hkp.fc;
+  const V3 f = mk(0, 0, 0) + fn_value * n;
+  const V3 ti = cross(cpos - ri, f) + mo;
+  V3 tj = mk(0, 0, 0);
+  if (is_vv) tj = cross(cpos - partner_pos(a, meta, i, j), -f) + (-mo);
+  write_result(a, k, mk(0, 0, 0), mo, f, ti, tj);
+  a.R.live[k] = 1;
+  a.cs.write(k, dn, cpos, f - mk(0, 0, 0), mk(0, 0, 0));  // ft = 0 before contact
 }
 
 __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
-  const uint64_t n1 = a.cnt[0];
+  const uint64_t n1 = a.cnt[0], nl = n1 + a.cnt[2];
   const uint64_t stride = (uint64_t)gridDim.x * FT;
-  for (uint64_t base = (uint64_t)blockIdx.x * FT; base < n1; base += stride) {
+  for (uint64_t base = (uint64_t)blockIdx.x * FT; base < nl; base += stride) {
     const uint64_t w = base + threadIdx.x;
     bool heavy = false;
     uint32_t k = 0;
     double dn = 0;
     V3 n = mk(0, 0, 0), cpos = mk(0, 0, 0);
-    if (w < n1) {
-      k = a.L1[w];
-      heavy = detect_pair(a, k, dn, n, cpos);
+    if (w < nl) {
+      k = l1_at(a, w, n1);
+      const int kind = detect_pair(a, k, dn, n, cpos);
+      if (kind == PAIR_ATTRACT) attract_pair(a, k, dn, n, cpos);
+      heavy = kind == PAIR_HOOKE;
     }
     const uint32_t pos = warp_append(heavy, a.cnt + 1);
     if (heavy) {
@@ -311,73 +336,90 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
     hooke_pair<Mode>(a, a.L2[w], a.D[0][w], mk(a.D[1][w], a.D[2][w], a.D[3][w]), mk(a.D[4][w], a.D[5][w], a.D[6][w]));
 }
 
-// Detection and the Hooke law in one kernel.  The overlapping pairs a block's
-// detection finds wait in shared memory until a full tile of them is ready;
-// then every thread of the block runs the law on one of them, so the FP64
-// warps of the law stay dense as in k_chooke, while the detection results
-// never go through global memory.  Each pair is computed exactly as by
-// k_cdetect + k_chooke and writes only its own records: the same bits.
-// The overlapping pairs are counted into *n_active (zeroed by the launcher).
+// Detection and the contact laws in one kernel.  The pairs a block's detection
+// finds overlapping (Hooke law) or within the cohesion distance (attraction)
+// wait in shared memory, one queue per law, until a full tile of one kind is
+// ready; then every thread of the block runs that law on one of them, so the
+// FP64 warps stay dense and on one law, while the detection results never go
+// through global memory.  The particle pairs of L1 come before its driver
+// pairs, so the warps of both stages see one kind of pair at a time.  Each
+// pair is computed exactly as by k_cdetect + k_chooke and writes only its own
+// records: the same bits.  The overlapping pairs are counted into *n_active
+// (zeroed by the launcher).
 template <int Mode>
 __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_cfused(CArgs a) {
-  __shared__ uint32_t q_k[2 * FT];
-  __shared__ double q_d[7][2 * FT];
-  __shared__ uint32_t q_n, q_tot;
+  __shared__ uint32_t q_k[2][2 * FT];
+  __shared__ double q_d[2][7][2 * FT];
+  __shared__ uint32_t q_n[2], q_tot;
   if (threadIdx.x == 0) {
-    q_n = 0;
+    q_n[0] = q_n[1] = 0;
     q_tot = 0;
   }
   __syncthreads();
-  const uint64_t n1 = a.cnt[0];
+  const uint64_t n1 = a.cnt[0], nl = n1 + a.cnt[2];
   const uint64_t stride = (uint64_t)gridDim.x * FT;
   const int lane = threadIdx.x & 31;
-  for (uint64_t base = (uint64_t)blockIdx.x * FT; base < n1; base += stride) {  // the same trips for the block
+  const uint32_t t = threadIdx.x;
+  auto run_tile = [&](int q, uint32_t idx) {
+    const V3 n = mk(q_d[q][1][idx], q_d[q][2][idx], q_d[q][3][idx]);
+    const V3 cpos = mk(q_d[q][4][idx], q_d[q][5][idx], q_d[q][6][idx]);
+    if (q == 0)
+      hooke_pair<Mode>(a, q_k[0][idx], q_d[0][0][idx], n, cpos);
+    else
+      attract_pair(a, q_k[1][idx], q_d[1][0][idx], n, cpos);
+  };
+  for (uint64_t base = (uint64_t)blockIdx.x * FT; base < nl; base += stride) {  // the same trips for the block
     const uint64_t w = base + threadIdx.x;
-    bool heavy = false;
+    int kind = PAIR_DONE;
     uint32_t k = 0;
     double dn = 0;
     V3 n = mk(0, 0, 0), cpos = mk(0, 0, 0);
-    if (w < n1) {
-      k = a.L1[w];
-      heavy = detect_pair(a, k, dn, n, cpos);
+    if (w < nl) {
+      k = l1_at(a, w, n1);
+      kind = detect_pair(a, k, dn, n, cpos);
     }
-    const unsigned mask = __ballot_sync(0xffffffffu, heavy);
-    uint32_t wb = 0;
-    if (lane == 0 && mask) {
-      wb = atomicAdd(&q_n, (uint32_t)__popc(mask));
-      atomicAdd(&q_tot, (uint32_t)__popc(mask));
-    }
-    wb = __shfl_sync(0xffffffffu, wb, 0);
-    if (heavy) {
-      const uint32_t pos = wb + (uint32_t)__popc(mask & ((1u << lane) - 1u));  // < 2 FT: at most FT - 1 wait
-      q_k[pos] = k;
-      q_d[0][pos] = dn;
-      q_d[1][pos] = n.x;
-      q_d[2][pos] = n.y;
-      q_d[3][pos] = n.z;
-      q_d[4][pos] = cpos.x;
-      q_d[5][pos] = cpos.y;
-      q_d[6][pos] = cpos.z;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+      const bool mine = kind == (q == 0 ? PAIR_HOOKE : PAIR_ATTRACT);
+      const unsigned mask = __ballot_sync(0xffffffffu, mine);
+      uint32_t wb = 0;
+      if (lane == 0 && mask) {
+        wb = atomicAdd(&q_n[q], (uint32_t)__popc(mask));
+        if (q == 0) atomicAdd(&q_tot, (uint32_t)__popc(mask));
+      }
+      wb = __shfl_sync(0xffffffffu, wb, 0);
+      if (mine) {
+        const uint32_t pos = wb + (uint32_t)__popc(mask & ((1u << lane) - 1u));  // < 2 FT: at most FT - 1 wait
+        q_k[q][pos] = k;
+        q_d[q][0][pos] = dn;
+        q_d[q][1][pos] = n.x;
+        q_d[q][2][pos] = n.y;
+        q_d[q][3][pos] = n.z;
+        q_d[q][4][pos] = cpos.x;
+        q_d[q][5][pos] = cpos.y;
+        q_d[q][6][pos] = cpos.z;
+      }
     }
     __syncthreads();
-    const uint32_t have = q_n;
-    if (have >= FT) {  // a full tile: one pair per thread
-      const uint32_t t = threadIdx.x;
-      hooke_pair<Mode>(a, q_k[t], q_d[0][t], mk(q_d[1][t], q_d[2][t], q_d[3][t]), mk(q_d[4][t], q_d[5][t], q_d[6][t]));
-      __syncthreads();
-      const uint32_t rest = have - FT;  // < FT: the waiting pairs move to the front
-      if (t < rest) {
-        q_k[t] = q_k[FT + t];
 #pragma unroll
-        for (int c = 0; c < 7; c++) q_d[c][t] = q_d[c][FT + t];
+    for (int q = 0; q < 2; q++) {
+      const uint32_t have = q_n[q];
+      if (have >= FT) {  // a full tile: one pair per thread
+        run_tile(q, t);
+        __syncthreads();
+        const uint32_t rest = have - FT;  // < FT: the waiting pairs move to the front
+        if (t < rest) {
+          q_k[q][t] = q_k[q][FT + t];
+#pragma unroll
+          for (int c = 0; c < 7; c++) q_d[q][c][t] = q_d[q][c][FT + t];
+        }
+        if (t == 0) q_n[q] = rest;
+        __syncthreads();
       }
-      if (t == 0) q_n = rest;
-      __syncthreads();
     }
   }
-  const uint32_t t = threadIdx.x;
-  if (t < q_n)
-    hooke_pair<Mode>(a, q_k[t], q_d[0][t], mk(q_d[1][t], q_d[2][t], q_d[3][t]), mk(q_d[4][t], q_d[5][t], q_d[6][t]));
+  if (t < q_n[0]) run_tile(0, t);
+  if (t < q_n[1]) run_tile(1, t);
   if (t == 0 && q_tot) atomicAdd(a.n_active, (unsigned long long)q_tot);
 }
 
@@ -558,6 +600,7 @@ CArgs make_cargs(dem_ctx* c) {
   a.L2 = c->L2;
   for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];
   a.cnt = c->d_scalars + 3;
+  a.l1cap = c->rcap;
   a.n_active = c->d_scalars + 1;
   return a;
 }
@@ -588,7 +631,7 @@ int launch_fused_prolog(dem_ctx* c) {
 }
 
 int launch_contact_compact(dem_ctx* c) {
-  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 3, 0, 2 * sizeof(unsigned long long), c->stream));
+  DEM_CUDA_TRY(c, cudaMemsetAsync(c->d_scalars + 3, 0, 3 * sizeof(unsigned long long), c->stream));
   const CArgs a = make_cargs(c);
   const unsigned persistent = (unsigned)c->num_sms * (unsigned)c->tune_contact_bps;
   {
