@@ -92,6 +92,9 @@ def parse():
     ap.add_argument("--mul-mode", type=int, default=None, choices=list(range(8)),
                     help="multiplies on the integer pipe: bit 0 integration rotations, bit 1 integration rest, "
                          "bit 2 contact law (default: the autotuner's choice, else 2)")
+    ap.add_argument("--int-share", type=int, default=None, choices=list(range(9)),
+                    help="eighths of the fused contact tiles whose law runs on the integer pipe (no effect on "
+                         "results; default: the autotuner's choice)")
     ap.add_argument("--learned", action="store_true",
                     help="polyhedra: harvest candidate pairs, train the MLP, time with learned sizing "
                          "and without it")
@@ -565,6 +568,8 @@ def run_native(args, rank, world, local, dist):
         tune = s.autotune(steps_per_trial=3, skin_policy=0 if args.workload == "mixer" else 1)
     if args.mul_mode is not None:
         s.set_mul_mode(args.mul_mode)
+    if args.int_share is not None:
+        s.set_contact_int_share(args.int_share)
     s.step(args.warmup)
     torch.cuda.synchronize()
     s.reset_kernel_stats()

@@ -92,7 +92,7 @@ class SystemDesc(C.Structure):
 class TuneResult(C.Structure):
     _fields_ = [("rcut_inc", D), ("cell_size", D), ("block", C.c_int32), ("contact_blocks_per_sm", C.c_int32),
                 ("ms_per_step", D), ("ms_per_step_before", D), ("trials", C.c_int32), ("vmax", C.c_float),
-                ("mul_mode", C.c_int32), ("fused_contact", C.c_int32)]
+                ("mul_mode", C.c_int32), ("fused_contact", C.c_int32), ("contact_int_share", C.c_int32)]
 
 
 class ContactState(C.Structure):
@@ -211,6 +211,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_set_graph_capacity", [_CTX, C.c_uint64])
     _sig(lib, "dem_autotune", [_CTX, C.c_int, C.c_int, C.POINTER(TuneResult)])
     _sig(lib, "dem_set_mul_mode", [_CTX, C.c_int])
+    _sig(lib, "dem_set_contact_int_share", [_CTX, C.c_int])
     _sig(lib, "dem_set_multimat", [_CTX, C.c_int, C.POINTER(ContactParams), C.c_int, C.POINTER(ContactParams)])
     _sig(lib, "dem_set_analysis", [_CTX, C.c_int])
     _sig(lib, "dem_get_contact_state", [_CTX, C.POINTER(ContactState)])
@@ -264,7 +265,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_mlp_init", "dem_mlp_set_params", "dem_mlp_get_params", "dem_mlp_forward", "dem_mlp_loss_grad",
             "dem_mlp_train", "dem_learned_stats", "dem_set_inner_bond_params", "dem_stick_polyhedra",
             "dem_bond_count", "dem_get_bonds", "dem_set_bonds", "dem_broken_interface_count",
-            "dem_inner_bond_polyhedron", "dem_apply_interface_fracture_criterion"]
+            "dem_inner_bond_polyhedron", "dem_apply_interface_fracture_criterion", "dem_set_contact_int_share"]
 
 _LIB = None
 

@@ -24,7 +24,14 @@ __device__ __forceinline__ bool exp_below(double x, int e2) {  // |x| < 2^e2, x 
 __device__ __forceinline__ bool exp_at_least(double x, int e2) {  // |x| >= 2^e2
   return (int)((emu_bits(x) >> 52) & 0x7ffu) >= 1023 + e2;
 }
+template <class M>
+__device__ __forceinline__ void rolling_clip_mur0_m(M& mm, V3 branch, V3 vrot_i, V3 fn, V3& mom_i);
 __device__ __forceinline__ void rolling_clip_mur0(V3 branch, V3 vrot_i, V3 fn, V3& mom_i) {
+  MulFP64 mm;
+  rolling_clip_mur0_m(mm, branch, vrot_i, fn, mom_i);
+}
+template <class M>
+__device__ __forceinline__ void rolling_clip_mur0_m(M& mm, V3 branch, V3 vrot_i, V3 fn, V3& mom_i) {
   // w = +-0: r = (b.w)/(w.w) is (+-0 or NaN)/(+0) = NaN for any b, so t = NaN and
   // the comparison with t^2 is false: the moment is kept as it is
   if (((emu_bits(vrot_i.x) | emu_bits(vrot_i.y) | emu_bits(vrot_i.z)) << 1) == 0) return;
@@ -33,9 +40,9 @@ __device__ __forceinline__ void rolling_clip_mur0(V3 branch, V3 vrot_i, V3 fn, V
                         exp_below(vrot_i.x, 200) && exp_below(vrot_i.y, 200) && exp_below(vrot_i.z, 200) &&
                         (exp_at_least(vrot_i.x, -200) || exp_at_least(vrot_i.y, -200) ||
                          exp_at_least(vrot_i.z, -200));
-  const double mom_square = dot(mom_i, mom_i);
+  const double mom_square = dot_m(mm, mom_i, mom_i);
   if (in_range) {
-    if (emu_gt0(mom_square)) mom_i = mom_i * 0.0;
+    if (emu_gt0(mom_square)) mom_i = mk(mm.mul(mom_i.x, 0.0), mm.mul(mom_i.y, 0.0), mm.mul(mom_i.z, 0.0));
     return;
   }
   const double r = (dot(branch, vrot_i)) / (dot(vrot_i, vrot_i));
@@ -48,12 +55,20 @@ __device__ __forceinline__ void rolling_clip_mur0(V3 branch, V3 vrot_i, V3 fn, V
 
 template <class M>
 __device__ __forceinline__ V3 cross_m(M& mm, V3 a, V3 b) {
-  return mk(mm.mul(a.y, b.z) - mm.mul(a.z, b.y), mm.mul(a.z, b.x) - mm.mul(a.x, b.z),
-            mm.mul(a.x, b.y) - mm.mul(a.y, b.x));
+  return mk(mm.sub(mm.mul(a.y, b.z), mm.mul(a.z, b.y)), mm.sub(mm.mul(a.z, b.x), mm.mul(a.x, b.z)),
+            mm.sub(mm.mul(a.x, b.y), mm.mul(a.y, b.x)));
 }
 template <class M>
 __device__ __forceinline__ double dot_m(M& mm, V3 a, V3 b) {
-  return mm.mul(a.x, b.x) + mm.mul(a.y, b.y) + mm.mul(a.z, b.z);
+  return mm.add(mm.add(mm.mul(a.x, b.x), mm.mul(a.y, b.y)), mm.mul(a.z, b.z));
+}
+template <class M>
+__device__ __forceinline__ V3 add_m(M& mm, V3 a, V3 b) {
+  return mk(mm.add(a.x, b.x), mm.add(a.y, b.y), mm.add(a.z, b.z));
+}
+template <class M>
+__device__ __forceinline__ V3 sub_m(M& mm, V3 a, V3 b) {
+  return mk(mm.sub(a.x, b.x), mm.sub(a.y, b.y), mm.sub(a.z, b.z));
 }
 template <class M>
 __device__ __forceinline__ V3 scale_m(M& mm, double s, V3 a) {
@@ -73,39 +88,40 @@ __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, doubl
                                                      V3 vel_j, V3 vrot_j, bool dmt = false, double reff = 0.0) {
   if (cohesive) {
     if (emu_ge0(dn)) {  // comparisons of this form on the integer pipe (emu64.cuh)
-      const double fn_value = mm.mul(hkp.fc / hkp.dncut, dn) - hkp.fc;
-      f_i = f_i + scale_m(mm, fn_value, n);
+      const double fn_value = mm.sub(mm.mul(hkp.fc / hkp.dncut, dn), hkp.fc);
+      f_i = add_m(mm, f_i, scale_m(mm, fn_value, n));
       ft = mk(0, 0, 0);
       return;
     }
   }
   const double damp = Damp ? meff : mm.mul(mm.twice(hkp.damp_rate), sqrt(mm.mul(hkp.kn, meff)));
-  const V3 contribution_i = vel_i - cross_m(mm, cpos - pos_i, vrot_i);
-  const V3 contribution_j = vel_j - cross_m(mm, cpos - pos_j, vrot_j);
-  const V3 vel = contribution_j - contribution_i;
+  const V3 contribution_i = sub_m(mm, vel_i, cross_m(mm, sub_m(mm, cpos, pos_i), vrot_i));
+  const V3 contribution_j = sub_m(mm, vel_j, cross_m(mm, sub_m(mm, cpos, pos_j), vrot_j));
+  const V3 vel = sub_m(mm, contribution_j, contribution_i);
   const double vn = dot_m(mm, vel, n);
   V3 fn;
   {
     const double fne = mm.mul(-hkp.kn, dn);
     const double fnv = mm.mul(damp, vn);
-    double nf = emu_gt0(fnv + fne) ? fnv + fne : 0;
+    const double s = mm.add(fnv, fne);
+    double nf = emu_gt0(s) ? s : 0;
     if (cohesive) {
-      const double fn_norm = nf - hkp.fc;
+      const double fn_norm = mm.sub(nf, hkp.fc);
       nf = emu_lt(fn_norm, -hkp.fc) ? -hkp.fc : fn_norm;
     }
     fn = scale_m(mm, nf, n);
   }
   {
-    const V3 vt = vel - scale_m(mm, vn, n);
+    const V3 vt = sub_m(mm, vel, scale_m(mm, vn, n));
     const V3 ftd = scale_m(mm, dt, vt);
-    ft = ft + scale_m(mm, hkp.kt, ftd);
+    ft = add_m(mm, ft, scale_m(mm, hkp.kt, ftd));
   }
   double threshold_ft;
   if (!cohesive) {
     const double fne = mm.mul(hkp.kn, dn);
     threshold_ft = fabs(mm.mul(hkp.mu, fne));
   } else {
-    threshold_ft = fabs(mm.mul(hkp.mu, dot_m(mm, fn, n) + hkp.fc));
+    threshold_ft = fabs(mm.mul(hkp.mu, mm.add(dot_m(mm, fn, n), hkp.fc)));
   }
   {
     const double ft_square = dot_m(mm, ft, ft);
@@ -114,17 +130,17 @@ __device__ __forceinline__ void contact_force_core_m(M& mm, bool cohesive, doubl
       ft = mk(mm.mul(ft.x, s), mm.mul(ft.y, s), mm.mul(ft.z, s));
     }
   }
-  f_i = fn + ft;
+  f_i = add_m(mm, fn, ft);
   if (dmt && hkp.gamma > 0.0 && emu_lt0(dn)) {
     const double F = mm.mul(mm.mul(2.0 * 3.14159265358979323846, reff), hkp.gamma);
-    f_i = f_i - scale_m(mm, F, n);
+    f_i = sub_m(mm, f_i, scale_m(mm, F, n));
   }
   {
-    const V3 d = vrot_j - vrot_i;
-    mom_i = mom_i + mk(mm.mul(mm.mul(hkp.kr, d.x), dt), mm.mul(mm.mul(hkp.kr, d.y), dt),
-                       mm.mul(mm.mul(hkp.kr, d.z), dt));
+    const V3 d = sub_m(mm, vrot_j, vrot_i);
+    mom_i = add_m(mm, mom_i, mk(mm.mul(mm.mul(hkp.kr, d.x), dt), mm.mul(mm.mul(hkp.kr, d.y), dt),
+                                mm.mul(mm.mul(hkp.kr, d.z), dt)));
   }
-  rolling_clip_mur0(cpos - pos_i, vrot_i, fn, mom_i);
+  rolling_clip_mur0_m(mm, sub_m(mm, cpos, pos_i), vrot_i, fn, mom_i);
 }
 
 // apply_dmt_force (contact_force.hpp:115-127): in contact (dn < 0) and for

@@ -1144,6 +1144,13 @@ int dem_set_mul_mode(dem_ctx* c, int mode) {
   return DEM_OK;
 }
 
+int dem_set_contact_int_share(dem_ctx* c, int eighths) {
+  if (!c || eighths < 0 || eighths > 8) return DEM_ERR_INVALID_ARG;
+  c->tune_int_share = eighths;
+  c->gen++;  // a captured step holds the kernel arguments of the old share
+  return DEM_OK;
+}
+
 int dem_get_mul_mode(dem_ctx* c, int* mode) {
   if (!c || !mode) return DEM_ERR_INVALID_ARG;
   *mode = c->mul_mode;

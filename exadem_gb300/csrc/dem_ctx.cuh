@@ -89,6 +89,7 @@ struct dem_ctx {
   int tune_contact_bps = 8;  // persistent blocks per SM of the compacted contact law
   bool fuse_contact = true;  // compacted contact: detection and law in one kernel (k_cfused), else two
   int mul_mode = 2;          // multiply placement of the fused integration kernels (integrate_core.cuh)
+  int tune_int_share = 0;    // k_cfused: Hooke tiles out of 8 whose arithmetic runs on the integer pipe
 
   // graph step (dem_graph.cu)
   bool capturing = false;                  // kernels launched now go into a graph

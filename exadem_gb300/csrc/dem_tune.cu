@@ -51,7 +51,7 @@ struct Saved {
   uint64_t ni, rebuilds;
   bool have_list, hist_valid;
   dem_params prm;
-  int tune_block, tune_contact_bps, mul_mode;
+  int tune_block, tune_contact_bps, mul_mode, int_share;
   bool fuse_contact;
 };
 
@@ -66,6 +66,7 @@ int save_state(dem_ctx* c, Saved& s) {
   s.tune_block = c->tune_block;
   s.tune_contact_bps = c->tune_contact_bps;
   s.mul_mode = c->mul_mode;
+  s.int_share = c->tune_int_share;
   s.fuse_contact = c->fuse_contact;
   const size_t bytes = pblock_bytes(c) + (c->n + 1) * 4 + c->ni * 80 + 1024;
   DEM_CUDA_TRY(c, cudaMalloc(&s.dev, bytes));
@@ -101,6 +102,7 @@ int restore_state(dem_ctx* c, const Saved& s) {
   c->tune_block = s.tune_block;
   c->tune_contact_bps = s.tune_contact_bps;
   c->mul_mode = s.mul_mode;
+  c->tune_int_share = s.int_share;
   c->fuse_contact = s.fuse_contact;
   if (std::memcmp(&c->prm, &s.prm, sizeof(dem_params))) {
     c->prm = s.prm;
@@ -291,6 +293,10 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
       best_fuse = !best_fuse;
     }
   }
+  // (the integer-pipe share of the contact tiles, dem_set_contact_int_share, is not
+  // tried: on GB300 its emulated additions made the contact kernel slower at every
+  // share measured, 2/8 to 8/8)
+  const int best_share = c->tune_int_share;
   cudaFree(base.dev);
 
   // apply: launch shapes and cell size keep the current list (they take effect at the
@@ -299,6 +305,7 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
   c->tune_contact_bps = best_bps;
   c->mul_mode = best_mode;
   c->fuse_contact = best_fuse;
+  c->tune_int_share = best_share;
   const bool skin_changed = best_skin != skin0;
   c->prm.cell_size = best_cell;
   c->prm.rcut_inc = best_skin;
@@ -317,5 +324,6 @@ extern "C" int dem_autotune(dem_ctx* c, int steps_per_trial, int skin_policy, de
   out->vmax = vmax;
   out->mul_mode = best_mode;
   out->fused_contact = best_fuse ? 1 : 0;
+  out->contact_int_share = best_share;
   return DEM_OK;
 }

@@ -190,6 +190,61 @@ EMU_HD double emu_mulnhalf(double x) {
   return emu_native_mul(x, -0.5);
 }
 
+// IEEE 754 binary64 addition, round to nearest even, on the integer pipe, in
+// the branch-free form of emu_dmul_nb.  Textbook method (as in Hauser's
+// SoftFloat): order the operands by magnitude, place both significands with
+// their hidden bit at bit 62 (10 bits below the result's last bit), shift the
+// smaller one right by the exponent difference with every bit shifted out
+// ORed into bit 0 ("jamming"), add or subtract, normalise the top bit back to
+// bit 62 (a carry shifts right, jamming again; a cancellation shifts left,
+// exactly, since it only happens when nothing was shifted out or by one
+// place), then round on bit 9 with the bits below as sticky and pack.  The
+// jammed bit 0 makes the computed sum odd whenever bits were lost, so it can
+// never sit on a rounding boundary (multiples of 2^8): it rounds like the
+// exact sum.  Operands that are zero or normal stay on the fast path; an exact
+// cancellation gives +0 and the sum of two zeros the zero that is negative
+// only when both are.  A subnormal, infinite or NaN operand, or a result
+// below the normal range or overflowing before rounding, sets `bad` (the
+// caller recomputes with the FP64 pipe); rounding that carries into the
+// exponent 2047 packs to infinity, the correctly rounded overflow.
+EMU_HD int emu_clz64(uint64_t x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+EMU_HD double emu_dadd_nb(double a, double b, bool& bad) {
+  const uint64_t ua = emu_bits(a), ub = emu_bits(b);
+  const uint64_t mag = 0x7fffffffffffffffull, frac = 0xfffffffffffffull;
+  const bool sw = (ua & mag) < (ub & mag);
+  const uint64_t ux = sw ? ub : ua, uy = sw ? ua : ub;  // |x| >= |y|
+  const uint32_t ex = (uint32_t)(ux >> 52) & 0x7ffu, ey = (uint32_t)(uy >> 52) & 0x7ffu;
+  const bool zx = (ux << 1) == 0, zy = (uy << 1) == 0;
+  const bool ok_in = (ex - 1u < 2046u || zx) && (ey - 1u < 2046u || zy);
+  const uint64_t mx = zx ? 0ull : (((ux & frac) | (1ull << 52)) << 10);
+  const uint64_t my0 = zy ? 0ull : (((uy & frac) | (1ull << 52)) << 10);
+  const uint32_t d = zy ? 63u : (ex - ey < 63u ? ex - ey : 63u);
+  const uint64_t lost = d ? (my0 << (64u - d)) : 0ull;
+  const uint64_t my = (my0 >> d) | (lost != 0 ? 1ull : 0ull);
+  const bool sub = ((ux ^ uy) >> 63) != 0;
+  uint64_t r = sub ? mx - my : mx + my;
+  const uint32_t c = (uint32_t)(r >> 63);
+  r = c ? ((r >> 1) | (r & 1ull)) : r;
+  const int lz = r ? emu_clz64(r) - 1 : 0;
+  r <<= lz;
+  const int e = (int)ex + (int)c - lz;
+  const uint64_t m = r >> 10;
+  const uint64_t inc = ((r >> 9) & 1ull) & (((r & 0x1ffull) != 0 ? 1ull : 0ull) | (m & 1ull));
+  const uint64_t sx = ux & 0x8000000000000000ull;
+  const uint64_t zsign = sub ? 0ull : sx;  // x + (-x) = +0; -0 + -0 = -0
+  bad |= !(ok_in && (r == 0 || (uint32_t)(e - 1) < 2046u));
+  return emu_double(r == 0 ? zsign : (sx | ((((uint64_t)(e - 1)) << 52) + m + inc)));
+}
+EMU_HD double emu_dsub_nb(double a, double b, bool& bad) {
+  return emu_dadd_nb(a, emu_double(emu_bits(b) ^ 0x8000000000000000ull), bad);
+}
+
 // Sums with a zero addend, decided on the integer pipe: a + z for z = +-0
 // (sign bit zs) is a itself for a nonzero, non-NaN a, and for a zero a the
 // zero that is negative only when both are (round to nearest).  ok is false

@@ -1,5 +1,5 @@
 // k_selftest_emu.cu -- GPU self-tests of the integer-pipe binary64 multiply
-// (emu64.cuh) against the hardware multiply and of the rolling-clip shortcut
+// and addition (emu64.cuh) against the hardware multiply and addition and of the rolling-clip shortcut
 // (contact_core.cuh) against the formula.
 #include "../../include/dem_selftest.h"
 #include "contact_core.cuh"
@@ -59,6 +59,20 @@ __global__ void k_emu_test(uint64_t n, uint64_t seed, unsigned long long* bad) {
     nbad += same_bits(dem::emu_mul2(a), __dmul_rn(a, 2.0)) ? 0 : 1;
     nbad += same_bits(dem::emu_mulhalf(a), __dmul_rn(a, 0.5)) ? 0 : 1;
     nbad += same_bits(dem::emu_mulnhalf(a), __dmul_rn(a, -0.5)) ? 0 : 1;
+    // sums: the drawn pair, a against its negation and its neighbours, and a
+    // gap of 0..70 binades between the operands
+    const uint64_t ua = (uint64_t)__double_as_longlong(a), h4 = mix(h ^ 5);
+    const uint64_t ea = (ua >> 52) & 0x7ff, gap = h4 % 71;
+    const double pairs[4] = {b, -a, __longlong_as_double((long long)((ua ^ 0x8000000000000000ull) + (h4 % 9) - 4)),
+                             __longlong_as_double((long long)(((h4 >> 8) & 1) << 63 |
+                                                              ((ea > gap ? ea - gap : 1) << 52) |
+                                                              (mix(h4) & 0xfffffffffffffull)))};
+    for (int q = 0; q < 4; q++) {
+      bool fa = false, fs = false;
+      const double ga = dem::emu_dadd_nb(a, pairs[q], fa), gs = dem::emu_dsub_nb(a, pairs[q], fs);
+      nbad += (fa || same_bits(ga, __dadd_rn(a, pairs[q]))) ? 0 : 1;
+      nbad += (fs || same_bits(gs, __dsub_rn(a, pairs[q]))) ? 0 : 1;
+    }
   }
   atomicAdd(bad, nbad);
 }

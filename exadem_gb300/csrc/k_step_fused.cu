@@ -61,6 +61,7 @@ struct CArgs {
   double* D[7];  // dn, n(3), cp(3) of the L2 entries
   unsigned long long* cnt;  // [0] L1 count (particle pairs), [1] L2 count, [2] driver pairs of L1
   uint64_t l1cap;           // L1 entries: particle pairs from the front, driver pairs from the back
+  int int_share;            // k_cfused: Hooke tiles out of 8 run with AllInt (the integer pipe)
   unsigned long long* n_active;
 };
 
@@ -266,61 +267,74 @@ __global__ void __launch_bounds__(FT) k_cdetect(CArgs a) {
   }
 }
 
-// The Hooke law on the contacts found by k_cdetect.  Mode bit 2 (instance 1):
-// its multiplies on the integer pipe (contact_force_core_m); an operand outside
-// that fast path makes the pair run again on the FP64 pipe from its stored
-// inputs (nothing is written before write_result).
-template <int Mode>
-__device__ __forceinline__ void hooke_pair(const CArgs& a, uint32_t k, double dn, V3 n, V3 cpos) {
-  auto run = [&](auto& mm, V3& ft, V3& mo, V3& f, V3& ti, V3& tj) {
-    const uint32_t meta = a.I.meta[k];
-    const uint32_t i = a.I.owner[k], j = a.I.partner[k];
-    const V3 ri = ldv(a.P, RX, i);
-    ft = mk(a.I.ft[0][k], a.I.ft[1][k], a.I.ft[2][k]);
-    mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
-    f = mk(0, 0, 0);
-    tj = mk(0, 0, 0);
-    const V3 vi = ldv(a.P, VX, i);
-    const V3 wi = ldv(a.P, WX, i);
-    if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
-      const V3 rj = partner_pos(a, meta, i, j);
-      const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
-      // the pair's damping coefficient, set when the list was built (k_fill); DMT:
-      // reff = compute_effective_radius (common_kernels.hpp:99-102)
-      double reff = 0.0;
-      if (a.dmt) {
-        const double rad_i = a.P.f[RAD][i], rad_j = a.P.f[RAD][j];
-        reff = mm.mul(rad_i, rad_j) / (rad_i + rad_j);
-      }
-      const dem_contact_params& cp = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]);
-      contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, cp,
-                                                                       a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
-                                                                       rj, vj, wj, a.dmt, reff);
-      ti = cross_m(mm, cpos - ri, f) + mo;
-      tj = cross_m(mm, cpos - rj, -f) + (-mo);
-    } else {
-      const DriverDev& d = a.drv[j];
-      const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
-      const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
-      const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
-      const dem_contact_params& cpd = a.pt.drv(a.cpd, a.P.group[i], j);
-      contact_force_core_m<std::remove_reference_t<decltype(mm)>, true>(mm, a.cohesive, dn, n, a.dt, cpd,
-                                                                       a.I.damp[k], ft, cpos, ri, vi, f, mo, wi,
-                                                                       dpos, dvel, dvrot, a.dmt, a.P.f[RAD][i]);
-      ti = cross_m(mm, cpos - ri, f) + mo;
+// The Hooke law of one overlapping pair with the arithmetic policy Pol
+// (mul_policy.cuh): MulFP64, MulInt (its multiplies on the integer pipe) or
+// AllInt (multiplies and additions there).  An operand outside an integer
+// path makes the pair run again on the FP64 pipe from its stored inputs
+// (nothing is written before write_result): the same bits in every case.
+template <class M>
+__device__ __forceinline__ void hooke_run(M& mm, const CArgs& a, uint32_t k, double dn, V3 n, V3 cpos, V3& ft,
+                                          V3& mo, V3& f, V3& ti, V3& tj) {
+  const uint32_t meta = a.I.meta[k];
+  const uint32_t i = a.I.owner[k], j = a.I.partner[k];
+  const V3 ri = ldv(a.P, RX, i);
+  ft = mk(a.I.ft[0][k], a.I.ft[1][k], a.I.ft[2][k]);
+  mo = mk(a.I.mo[0][k], a.I.mo[1][k], a.I.mo[2][k]);
+  f = mk(0, 0, 0);
+  tj = mk(0, 0, 0);
+  const V3 vi = ldv(a.P, VX, i);
+  const V3 wi = ldv(a.P, WX, i);
+  if (meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX) {
+    const V3 rj = partner_pos(a, meta, i, j);
+    const V3 vj = ldv(a.P, VX, j), wj = ldv(a.P, WX, j);
+    // the pair's damping coefficient, set when the list was built (k_fill); DMT:
+    // reff = compute_effective_radius (common_kernels.hpp:99-102)
+    double reff = 0.0;
+    if (a.dmt) {
+      const double rad_i = a.P.f[RAD][i], rad_j = a.P.f[RAD][j];
+      reff = mm.mul(rad_i, rad_j) / mm.add(rad_i, rad_j);
     }
-  };
+    const dem_contact_params& cp = a.pt.pair(a.cp, a.P.group[i], a.P.group[j]);
+    contact_force_core_m<M, true>(mm, a.cohesive, dn, n, a.dt, cp, a.I.damp[k], ft, cpos, ri, vi, f, mo, wi, rj,
+                                  vj, wj, a.dmt, reff);
+    ti = add_m(mm, cross_m(mm, sub_m(mm, cpos, ri), f), mo);
+    tj = add_m(mm, cross_m(mm, sub_m(mm, cpos, rj), -f), -mo);
+  } else {
+    const DriverDev& d = a.drv[j];
+    const V3 dpos = mk(d.center[0], d.center[1], d.center[2]);
+    const V3 dvel = mk(d.vel[0], d.vel[1], d.vel[2]);
+    const V3 dvrot = mk(d.vrot[0], d.vrot[1], d.vrot[2]);
+    const dem_contact_params& cpd = a.pt.drv(a.cpd, a.P.group[i], j);
+    contact_force_core_m<M, true>(mm, a.cohesive, dn, n, a.dt, cpd, a.I.damp[k], ft, cpos, ri, vi, f, mo, wi, dpos,
+                                  dvel, dvrot, a.dmt, a.P.f[RAD][i]);
+    ti = add_m(mm, cross_m(mm, sub_m(mm, cpos, ri), f), mo);
+  }
+}
+
+// The Hooke law of one overlapping pair with the arithmetic policy Pol
+// (mul_policy.cuh): MulFP64, MulInt (its multiplies on the integer pipe) or
+// AllInt (multiplies and additions there).  An operand outside an integer
+// path makes the pair run again on the FP64 pipe from its stored inputs
+// (nothing is written before write_result): the same bits in every case.
+template <class Pol>
+__device__ __forceinline__ void hooke_pair_p(const CArgs& a, uint32_t k, double dn, V3 n, V3 cpos) {
   V3 ft, mo, f, ti, tj;
-  RotMul<Mode> mm;
-  run(mm, ft, mo, f, ti, tj);
+  Pol mm;
+  hooke_run(mm, a, k, dn, n, cpos, ft, mo, f, ti, tj);
   if (mm.failed()) {
     asm volatile("" ::: "memory");
     MulFP64 nm;
-    run(nm, ft, mo, f, ti, tj);
+    hooke_run(nm, a, k, dn, n, cpos, ft, mo, f, ti, tj);
   }
   write_result(a, k, ft, mo, f, ti, tj);
   a.R.live[k] = 1;
   if (a.cs.dn) a.cs.write(k, dn, cpos, f - ft, ft);
+}
+
+// Mode bit 2 (instance 1): the law's multiplies on the integer pipe
+template <int Mode>
+__device__ __forceinline__ void hooke_pair(const CArgs& a, uint32_t k, double dn, V3 n, V3 cpos) {
+  hooke_pair_p<RotMul<Mode>>(a, k, dn, n, cpos);
 }
 
 // The Hooke law on the contacts found by k_cdetect.  Mode bit 2 (instance 1):
@@ -336,6 +350,24 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
     hooke_pair<Mode>(a, a.L2[w], a.D[0][w], mk(a.D[1][w], a.D[2][w], a.D[3][w]), mk(a.D[4][w], a.D[5][w], a.D[6][w]));
 }
 
+// The law of queued pair idx of queue q (0: Hooke, 1: attraction); a share of
+// the Hooke tiles runs on the integer pipe, so both pipes work at once.
+template <int Mode, bool IntTiles>
+__device__ __forceinline__ void run_queued(const CArgs& a, int q, uint32_t idx, const uint32_t* qk,
+                                           const double (*qd)[2 * FT], uint32_t& tiles) {
+  const V3 n = mk(qd[1][idx], qd[2][idx], qd[3][idx]);
+  const V3 cpos = mk(qd[4][idx], qd[5][idx], qd[6][idx]);
+  if (q == 0) {
+    if (IntTiles && (int)(tiles & 7u) < a.int_share)
+      hooke_pair_p<AllInt>(a, qk[idx], qd[0][idx], n, cpos);
+    else
+      hooke_pair<Mode>(a, qk[idx], qd[0][idx], n, cpos);
+    tiles++;
+  } else {
+    attract_pair(a, qk[idx], qd[0][idx], n, cpos);
+  }
+}
+
 // Detection and the contact laws in one kernel.  The pairs a block's detection
 // finds overlapping (Hooke law) or within the cohesion distance (attraction)
 // wait in shared memory, one queue per law, until a full tile of one kind is
@@ -346,8 +378,10 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_chooke(CArgs a) {
 // pair is computed exactly as by k_cdetect + k_chooke and writes only its own
 // records: the same bits.  The overlapping pairs are counted into *n_active
 // (zeroed by the launcher).
-template <int Mode>
-__global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_cfused(CArgs a) {
+// IntTiles: the instance with the integer-pipe tiles (int_share > 0); it needs
+// more registers, so the FP64-only instance stays the lean one.
+template <int Mode, bool IntTiles>
+__global__ void __launch_bounds__(FT, (Mode ? 4 : (IntTiles ? 3 : 1))) k_cfused(CArgs a) {
   __shared__ uint32_t q_k[2][2 * FT];
   __shared__ double q_d[2][7][2 * FT];
   __shared__ uint32_t q_n[2], q_tot;
@@ -360,14 +394,7 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_cfused(CArgs a) {
   const uint64_t stride = (uint64_t)gridDim.x * FT;
   const int lane = threadIdx.x & 31;
   const uint32_t t = threadIdx.x;
-  auto run_tile = [&](int q, uint32_t idx) {
-    const V3 n = mk(q_d[q][1][idx], q_d[q][2][idx], q_d[q][3][idx]);
-    const V3 cpos = mk(q_d[q][4][idx], q_d[q][5][idx], q_d[q][6][idx]);
-    if (q == 0)
-      hooke_pair<Mode>(a, q_k[0][idx], q_d[0][0][idx], n, cpos);
-    else
-      attract_pair(a, q_k[1][idx], q_d[1][0][idx], n, cpos);
-  };
+  uint32_t tiles = 0;  // Hooke tiles run by this block (the same count in every thread)
   for (uint64_t base = (uint64_t)blockIdx.x * FT; base < nl; base += stride) {  // the same trips for the block
     const uint64_t w = base + threadIdx.x;
     int kind = PAIR_DONE;
@@ -405,7 +432,7 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_cfused(CArgs a) {
     for (int q = 0; q < 2; q++) {
       const uint32_t have = q_n[q];
       if (have >= FT) {  // a full tile: one pair per thread
-        run_tile(q, t);
+        run_queued<Mode, IntTiles>(a, q, t, q_k[q], q_d[q], tiles);
         __syncthreads();
         const uint32_t rest = have - FT;  // < FT: the waiting pairs move to the front
         if (t < rest) {
@@ -418,8 +445,8 @@ __global__ void __launch_bounds__(FT, (Mode ? 4 : 1)) k_cfused(CArgs a) {
       }
     }
   }
-  if (t < q_n[0]) run_tile(0, t);
-  if (t < q_n[1]) run_tile(1, t);
+  if (t < q_n[0]) run_queued<Mode, IntTiles>(a, 0, t, q_k[0], q_d[0], tiles);
+  if (t < q_n[1]) run_queued<Mode, IntTiles>(a, 1, t, q_k[1], q_d[1], tiles);
   if (t == 0 && q_tot) atomicAdd(a.n_active, (unsigned long long)q_tot);
 }
 
@@ -494,22 +521,25 @@ __global__ void __launch_bounds__(256, (Mode ? 3 : 1)) k_fused_epilog(PArrays P,
     // components are all +-0 (a listed pair that does not touch) leaves them
     // unchanged bit for bit and its additions are skipped.
     // (a record whose live flag is 0 is zero and is not read)
-    for (uint32_t k = own_off[s]; k < own_off[s + 1]; k++) {
+    // The owned records, then the partner records, in one loop: a particle's
+    // owned and partner counts vary a lot (by id order), their sum (its
+    // neighbour count) much less, so one loop keeps the warp's FP64 adds on
+    // most lanes.  The order of the additions is that of two loops.
+    const uint32_t o0 = own_off[s], no = own_off[s + 1] - o0;
+    const uint32_t r0 = rev_off[s], nt = no + (rev_off[s + 1] - r0);
+    for (uint32_t m = 0; m < nt; m++) {
+      const bool own = m < no;
+      const uint32_t k = own ? o0 + m : rev_idx[r0 + (m - no)];
       if (!R.live[k]) continue;
-      const V3 rf = mk(R.f[0][k], R.f[1][k], R.f[2][k]), rt = mk(R.ti[0][k], R.ti[1][k], R.ti[2][k]);
+      const double* t0 = own ? R.ti[0] : R.tj[0];
+      const double* t1 = own ? R.ti[1] : R.tj[1];
+      const double* t2 = own ? R.ti[2] : R.tj[2];
+      const V3 rf = mk(R.f[0][k], R.f[1][k], R.f[2][k]), rt = mk(t0[k], t1[k], t2[k]);
       if (((emu_bits(rf.x) | emu_bits(rf.y) | emu_bits(rf.z) | emu_bits(rt.x) | emu_bits(rt.y) | emu_bits(rt.z))
            << 1) != 0) {
-        f = f + rf;
-        mom = mom + rt;
-      }
-    }
-    for (uint32_t q = rev_off[s]; q < rev_off[s + 1]; q++) {
-      const uint32_t k = rev_idx[q];
-      if (!R.live[k]) continue;
-      const V3 rf = mk(R.f[0][k], R.f[1][k], R.f[2][k]), rt = mk(R.tj[0][k], R.tj[1][k], R.tj[2][k]);
-      if (((emu_bits(rf.x) | emu_bits(rf.y) | emu_bits(rf.z) | emu_bits(rt.x) | emu_bits(rt.y) | emu_bits(rt.z))
-           << 1) != 0) {
-        f = f + (-rf);
+        const uint64_t flip = own ? 0ull : 0x8000000000000000ull;  // -rf for a partner record (exact)
+        f = f + mk(emu_double(emu_bits(rf.x) ^ flip), emu_double(emu_bits(rf.y) ^ flip),
+                   emu_double(emu_bits(rf.z) ^ flip));
         mom = mom + rt;
       }
     }
@@ -601,6 +631,7 @@ CArgs make_cargs(dem_ctx* c) {
   for (int q = 0; q < 7; q++) a.D[q] = c->Dscr[q];
   a.cnt = c->d_scalars + 3;
   a.l1cap = c->rcap;
+  a.int_share = c->tune_int_share;
   a.n_active = c->d_scalars + 1;
   return a;
 }
@@ -644,7 +675,10 @@ int launch_contact_compact(dem_ctx* c) {
   if (c->fuse_contact) {  // detection and law in one kernel (k_cfused)
     DEM_CUDA_TRY(c, cudaMemsetAsync(a.n_active, 0, sizeof(unsigned long long), c->stream));
     ProfScope ps(c, K_CONTACT, 1);
-    const auto kf = (c->mul_mode & 4) ? k_cfused<1> : k_cfused<0>;  // mode bit 2: the contact law
+    // mode bit 2: the contact law's multiplies on the integer pipe; int_share: a
+    // share of its tiles with multiplies and additions there
+    const auto kf = (c->mul_mode & 4) ? k_cfused<1, false>
+                                      : (c->tune_int_share > 0 ? k_cfused<0, true> : k_cfused<0, false>);
     kf<<<persistent, FT, 0, c->stream>>>(a);
   } else {
     {

@@ -320,6 +320,9 @@ class System:
         """dem_set_mul_mode: which integration multiplies run on the integer pipe (same bits)."""
         self._check(self.b.set_mul_mode(self.h, int(mode)), "set_mul_mode")
 
+    def set_contact_int_share(self, eighths: int) -> None:
+        self._check(self.b.set_contact_int_share(self.h, int(eighths)), "set_contact_int_share")
+
     def mul_mode(self) -> int:
         v = C.c_int()
         self._check(self.b.get_mul_mode(self.h, C.byref(v)), "get_mul_mode")

@@ -373,6 +373,7 @@ typedef struct dem_tune_result {
   int32_t mul_mode;              /* multiply placement, see dem_set_mul_mode     */
   int32_t fused_contact;         /* 1: detection and law of the compacted contact
                                     in one kernel, 0: in two (same bits)         */
+  int32_t contact_int_share;     /* see dem_set_contact_int_share                */
 } dem_tune_result;
 int dem_autotune(dem_ctx* ctx, int steps_per_trial, int skin_policy, dem_tune_result* out);
 /* Multiply placement of the fused integration kernels (prolog, epilog).  The
@@ -386,6 +387,15 @@ int dem_autotune(dem_ctx* ctx, int steps_per_trial, int skin_policy, dem_tune_re
  * for the sphere step.                                                     */
 int dem_set_mul_mode(dem_ctx* ctx, int mode);
 int dem_get_mul_mode(dem_ctx* ctx, int* mode);
+/* Share (0..8, in eighths) of the fused contact kernel's tiles of overlapping
+ * pairs whose contact-law multiplies and additions run on the integer pipe
+ * (IEEE binary64 round-to-nearest built from integer operations; square roots
+ * and divisions stay on the FP64 pipe), so that both pipes work at once.
+ * Results are identical for every share.  Default 0.  Measured on GB300 (2 M
+ * sphere bed): every share from 2/8 up slows the kernel (2/8: 1.9x), because
+ * an emulated addition costs several times an FP64 one; the autotuner leaves
+ * it at 0.  No reference counterpart (a placement of the same arithmetic). */
+int dem_set_contact_int_share(dem_ctx* ctx, int eighths);
 /* Number of neighbour rebuilds done so far (trigger_move_particles count). */
 int dem_rebuild_count(dem_ctx* ctx, uint64_t* out);
 

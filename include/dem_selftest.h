@@ -26,7 +26,10 @@ int dem_selftest_poly_decisions(uint64_t n, uint64_t seed, uint64_t* counts);
  * give exact products and ties, the whole exponent range, boundaries, zeros,
  * subnormals, infinities, NaNs) and counts the results of the integer-pipe
  * binary64 multiply (emu_dmul, and the exact x*2 / x*0.5) that differ in any
- * bit from the hardware multiply.                                          */
+ * bit from the hardware multiply; for each pair and three derived ones (the
+ * negation of a, its neighbours, a gap of 0..70 binades) also the sums and
+ * differences of the integer-pipe addition (emu_dadd_nb, emu_dsub_nb) that
+ * differ from the hardware's, where the addition keeps its fast path.     */
 int dem_selftest_emu_mul(uint64_t n, uint64_t seed, uint64_t* mismatches);
 
 /* Draws n seeded (branch, spin, normal force, moment) cases around the range

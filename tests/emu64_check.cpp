@@ -1,5 +1,6 @@
-// Host check of exadem_gb300/csrc/emu64.cuh: emu_dmul, emu_mul2 and emu_mulhalf
-// against the host's IEEE binary64 multiply, bit for bit.
+// Host check of exadem_gb300/csrc/emu64.cuh: emu_dmul, emu_mul2, emu_mulhalf and
+// emu_dadd_nb / emu_dsub_nb against the host's IEEE binary64 multiply and
+// addition, bit for bit.
 // Usage: emu64_check <n_cases> <seed>; prints "cases <n> mismatches <m>".
 // Built by tests/test_emu64.py with g++ -O2 -ffp-contract=off.
 #include <stdint.h>
@@ -117,6 +118,43 @@ int main(int argc, char** argv) {
       bad++;
     }
     if (!ok && a == a) bad++;  // only NaN may leave the fast path
+  }
+  // sums: independent operands, and pairs built for the cases addition branches
+  // on (cancellation, exponent gaps 0..70, short significands for ties,
+  // neighbours of -a, zeros)
+  for (long i = 0; i < n; i++) {
+    double a = draw(), b;
+    const int cls = (int)(next64() % 6);
+    if (cls == 0) {
+      b = draw();
+    } else if (cls == 1) {
+      b = -a;
+    } else if (cls == 2) {
+      const uint64_t gap = next64() % 71, ua = bits(a);
+      const uint64_t e = (ua >> 52) & 0x7ff;
+      const uint64_t eb = e > gap ? e - gap : 1;
+      uint64_t u = ((next64() & 1) << 63) | (eb << 52) | (next64() & 0xfffffffffffffull);
+      memcpy(&b, &u, 8);
+    } else if (cls == 3) {
+      uint64_t u = bits(-a) + (next64() % 9) - 4;
+      memcpy(&b, &u, 8);
+    } else if (cls == 4) {
+      const int keep = (int)(next64() % 10);
+      uint64_t u = bits(draw()) & ~((1ull << (52 - keep)) - 1);
+      memcpy(&b, &u, 8);
+      uint64_t v = bits(a) & ~((1ull << 40) - 1);
+      memcpy(&a, &v, 8);
+    } else {
+      b = (next64() & 1) ? 0.0 : -0.0;
+    }
+    bool fa = false, fs = false;
+    const double ga = dem::emu_dadd_nb(a, b, fa), gs = dem::emu_dsub_nb(a, b, fs);
+    const double ra = a + b, rs = a - b;
+    if ((!fa && bits(ga) != bits(ra)) || (!fs && bits(gs) != bits(rs))) {
+      if (bad < 8) printf("add %016llx + %016llx\n", (unsigned long long)bits(a), (unsigned long long)bits(b));
+      bad++;
+    }
+    flagged += fa ? 1 : 0;
   }
   printf("flagged %ld (branch-free form: recomputed by the caller)\n", flagged);
   printf("cases %ld mismatches %ld\n", n, bad);

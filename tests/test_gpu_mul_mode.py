@@ -70,3 +70,36 @@ def test_mul_mode_validation(native_lib):
 
     with pytest.raises(A.DemError):
         s.set_mul_mode(8)
+
+
+@pytest.mark.parametrize("share", [3, 8])
+@pytest.mark.parametrize("case", ["drum", "cohesive_floor", "dmt_floor"])
+def test_contact_int_share_matches_oracle(native_lib, case, share):
+    """A share of the fused contact kernel's Hooke tiles (or all of them) with
+    the law's multiplies and additions on the integer pipe: the same bits as
+    the oracle, for the plain Hooke law (a drum), the cohesive law on a periodic
+    floor and the DMT law."""
+    from exadem_gb300 import _abi as A
+
+    flags = dict(fused_step=1, fp32_contact_screen=1, fp32_broad_phase=1)
+    if case == "drum":
+        w = W.spheres_drum(n=3000, seed=43, **flags)
+    elif case == "cohesive_floor":
+        w = W.spheres_floor(n=4000, side=14.0, seed=43, **flags)
+    else:
+        w = W.spheres_floor(n=4000, side=14.0, seed=43, **flags)
+        w.params.law = A.LAW_HOOKE_DMT
+        for cfg in (w.params.config, w.params.config_driver):
+            cfg.gamma, cfg.fc, cfg.dncut = 0.5, 0.0, 0.0
+    g, o = pair(w)
+    g.set_contact_int_share(share)
+    for s in (g, o):
+        s.first_iteration()
+        s.step(200)
+    assert g.simulation_state()["n_active_interactions"] > 0
+    assert_same_list(g.interactions(), o.interactions())
+    lg, lo = g.interactions(), o.interactions()
+    assert np.array_equal(lg["friction"].view(np.uint64), lo["friction"].view(np.uint64))
+    assert bit_equal_fraction(g.particles(sort_by_id=True), o.particles(sort_by_id=True)) == 1.0
+    with pytest.raises(A.DemError):
+        g.set_contact_int_share(9)
