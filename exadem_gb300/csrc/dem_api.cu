@@ -477,6 +477,7 @@ int update_neighbors(dem_ctx* c) {
   if ((rc = alloc_iarrays(c, nw, total))) return rc;
   if ((rc = alloc_records(c, total))) return rc;
   if ((rc = launch_fill_sphere(c, new_off, total))) return rc;
+  c->damp_stale = false;  // the new list's damping is that of the current parameters
   c->icur = nw;
   c->ni = total;
   c->have_list = true;
@@ -1276,6 +1277,7 @@ int dem_set_interactions(dem_ctx* c, const dem_interaction_list* l) {
   DEM_CUDA_TRY(c, cudaMemcpy(c->own_off[b], off.data(), (n + 1) * 4, cudaMemcpyHostToDevice));
   c->ni = m;
   c->gen++;
+  c->damp_stale = true;  // the installed list carries no damping
   c->have_list = false;  // the next build makes the list; this one only holds the history
   c->hist_valid = true;
   return mark_all_triggered(c);

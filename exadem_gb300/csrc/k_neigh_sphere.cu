@@ -294,9 +294,13 @@ __device__ inline bool key_less(uint64_t pa, uint32_t ta, uint32_t sa, uint64_t 
   return pa < pb || (pa == pb && (ta < tb || (ta == tb && sa < sb)));
 }
 
+// reuse_damp: the previous list's damping was computed with the current contact
+// parameters (no dem_set_params / dem_set_multimat since, not a list installed by
+// dem_set_interactions), so a pair found in it keeps its damping bits.
 template <bool F32>
 __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, IArrays old,
-                       const uint32_t* __restrict__ old_off, const uint32_t* __restrict__ perm, int have_old) {
+                       const uint32_t* __restrict__ old_off, const uint32_t* __restrict__ perm, int have_old,
+                       int reuse_damp) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
   const uint32_t b = off[s], e = off[s + 1];
@@ -355,7 +359,6 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
   }
   for (uint32_t x = b; x < e; x++) {
     dst.owner[x] = (uint32_t)s;
-    dst.damp[x] = pair_damp(a, (uint32_t)s, dst.partner[x], dst.meta[x]);
     double h[6] = {0, 0, 0, 0, 0, 0};
     const uint64_t pk = dst.pid[x];
     const uint32_t tk = meta_type(dst.meta[x]), sk = dst.sub[x];
@@ -374,6 +377,12 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
       h[3] = old.mo[0][lo];
       h[4] = old.mo[1][lo];
       h[5] = old.mo[2][lo];
+      // the same pair in the previous list: the same masses and (reuse_damp) the
+      // same parameters, so the same damping bits, without the FP64 square root
+      // and division
+      dst.damp[x] = reuse_damp ? old.damp[lo] : pair_damp(a, (uint32_t)s, dst.partner[x], dst.meta[x]);
+    } else {
+      dst.damp[x] = pair_damp(a, (uint32_t)s, dst.partner[x], dst.meta[x]);
     }
     dst.ft[0][x] = h[0];
     dst.ft[1][x] = h[1];
@@ -467,8 +476,9 @@ BPArgs make_args(dem_ctx* c) {
 // recomputes the per-pair damping of the current sphere list (after dem_set_params)
 int refresh_pair_damp(dem_ctx* c) {
   if (!c->damp_stale) return DEM_OK;
+  if (!c->have_list) return DEM_OK;  // still stale: the next build computes every pair's damping
   c->damp_stale = false;
-  if (c->poly || !c->have_list || !c->ni) return DEM_OK;
+  if (c->poly || !c->ni) return DEM_OK;
   k_pair_damp<<<c->num_sms * 4, 256, 0, c->stream>>>(make_args(c), c->I[c->icur], c->ni);
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
@@ -506,12 +516,13 @@ int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total) {
       k_mesh_fill<false><<<grid_for(c->n * 32, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw]);
   }
   if (c->n) {
+    const int have_old = c->hist_valid ? 1 : 0, reuse = (c->hist_valid && !c->damp_stale) ? 1 : 0;
     if (c->prm.fp32_broad_phase)
       k_fill<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw], c->I[c->icur],
-                                                               c->own_off[c->icur], c->perm, c->hist_valid ? 1 : 0);
+                                                               c->own_off[c->icur], c->perm, have_old, reuse);
     else
       k_fill<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw], c->I[c->icur],
-                                                                c->own_off[c->icur], c->perm, c->hist_valid ? 1 : 0);
+                                                                c->own_off[c->icur], c->perm, have_old, reuse);
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
