@@ -298,16 +298,35 @@ __device__ inline int decide_vf_list(F3 vi, int nf, VertF&& vtx, float lim, floa
   const float edist = en * V + eta + 4.f * F32_U * V;
   const int cd = cmp_gt(dist, lim, edist + F32_U * lim);
   if (cd > 0) return DEC_FALSE;
-  if (cd == 0) return DEC_UNDECIDED;
   const F3 v2 = fcross(n, v1);
   // in-plane coordinates of the face vertices relative to the projection P of vi:
   // D1 = (v_k - vi).v1 + dist n.v1 ; D2 likewise with v2 (n.v1, n.v2 are O(ef))
   const float eD = ef * (2.f * S + dist) + eta + 6.f * F32_U * 2.f * S;
+  // P outside the face's extent along v1 or v2 (every D1, or every D2, beyond 0 on
+  // one side): along v2 no edge straddles the line through P; along v1 every
+  // straddling edge crosses it on the same side of P, and a closed polygon has an
+  // even number of straddling edges.  The parity is then even, so the FP64 test
+  // is false whatever its ties in the other direction or its plane distance.
+  // Taken where a comparison is undecided: coplanar neighbours put P on the line
+  // of a face edge.
+  auto outside = [&]() -> bool {
+    int lo1 = 0, hi1 = 0, lo2 = 0, hi2 = 0;
+    for (int k = 0; k < nf; k++) {
+      const F3 p = vtx(k) - vi;
+      const int c1 = cmp_gt(fdot(p, v1), 0.f, eD), c2 = cmp_gt(fdot(p, v2), 0.f, eD);
+      lo1 += c1 < 0;
+      hi1 += c1 > 0;
+      lo2 += c2 < 0;
+      hi2 += c2 > 0;
+    }
+    return lo1 == nf || hi1 == nf || lo2 == nf || hi2 == nf;
+  };
+  if (cd == 0) return outside() ? DEC_FALSE : DEC_UNDECIDED;
   int odd = 0;
   F3 pa = vtx(0) - vi;
   float a1 = fdot(pa, v1), a2 = fdot(pa, v2);
   const int s_first = cmp_gt(a2, 0.f, eD);
-  if (s_first == 0) return DEC_UNDECIDED;
+  if (s_first == 0) return outside() ? DEC_FALSE : DEC_UNDECIDED;
   int sa = s_first;
   for (int k = 0; k < nf; k++) {
     float b1, b2;
@@ -322,7 +341,7 @@ __device__ inline int decide_vf_list(F3 vi, int nf, VertF&& vtx, float lim, floa
       b1 = fdot(pb, v1);
       b2 = fdot(pb, v2);
       sb = cmp_gt(b2, 0.f, eD);
-      if (sb == 0) return DEC_UNDECIDED;
+      if (sb == 0) return outside() ? DEC_FALSE : DEC_UNDECIDED;
     }
     if (sa != sb) {  // the edge straddles the line through P along v1
       // crossing abscissa relative to P: X = a1 + t (b1 - a1), t = -a2 / (b2 - a2) in [0, 1]
@@ -332,7 +351,7 @@ __device__ inline int decide_vf_list(F3 vi, int nf, VertF&& vtx, float lim, floa
       const float et = 3.f * eD / fabsf(den) + 2.f * F32_U;
       const float eX = eD + et * fabsf(b1 - a1) + 2.f * eD + 3.f * F32_U * (fabsf(a1) + fabsf(b1 - a1));
       const int cx = cmp_gt(0.f, X, eX);  // X < 0
-      if (cx == 0) return DEC_UNDECIDED;
+      if (cx == 0) return outside() ? DEC_FALSE : DEC_UNDECIDED;
       if (cx > 0) odd ^= 1;
     }
     a1 = b1;
