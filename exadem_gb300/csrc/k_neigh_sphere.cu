@@ -424,24 +424,42 @@ __global__ void k_rev_fill(IArrays I, uint64_t ni, const unsigned long long* ni_
     }
   }
 }
-// order of the partner-side contributions: InteractionPair order = (owner id, index)
-__global__ void k_rev_sort(uint64_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ owner,
-                           const uint64_t* __restrict__ id, uint32_t* __restrict__ idx) {
-  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  const uint32_t b = off[s], e = off[s + 1];
-  for (uint32_t x = b + 1; x < e; x++) {
-    const uint32_t k = idx[x];
-    const uint64_t ok = id[owner[k]];
-    uint32_t y = x;
-    while (y > b) {
-      const uint32_t kp = idx[y - 1];
-      const uint64_t op = id[owner[kp]];
-      if (op < ok || (op == ok && kp < k)) break;
-      idx[y] = kp;
-      y--;
+// order of the partner-side contributions: InteractionPair order = (owner id, index).
+// One warp per particle: the entries of its reverse list, filled in any order
+// into `unsorted`, go to idx at their rank, the number of entries of the list
+// with a smaller (owner id, index) key (keys are distinct: the index is).
+// Lanes hold 32 entries at a time and count against every chunk of 32 of the
+// list broadcast by shuffles.
+__global__ void __launch_bounds__(256) k_rev_rank(uint64_t n, const uint32_t* __restrict__ off,
+                                                  const uint32_t* __restrict__ owner,
+                                                  const uint64_t* __restrict__ id,
+                                                  const uint32_t* __restrict__ unsorted, uint32_t* __restrict__ idx) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < n; s += nw) {
+    const uint32_t b = off[s], m = off[s + 1] - b;
+    for (uint32_t i0 = 0; i0 < m; i0 += 32) {
+      const bool have = i0 + lane < m;
+      const uint32_t k = have ? unsorted[b + i0 + lane] : 0u;
+      const uint64_t o = have ? id[owner[k]] : 0ull;
+      uint32_t rank = 0;
+      for (uint32_t j0 = 0; j0 < m; j0 += 32) {
+        uint32_t kj = k;
+        uint64_t oj = o;
+        if (j0 != i0) {
+          const bool hj = j0 + lane < m;
+          kj = hj ? unsorted[b + j0 + lane] : 0u;
+          oj = hj ? id[owner[kj]] : 0ull;
+        }
+        const uint32_t nj = m - j0 < 32u ? m - j0 : 32u;
+        for (uint32_t q = 0; q < nj; q++) {
+          const uint32_t kq = __shfl_sync(0xffffffffu, kj, (int)q);
+          const uint64_t oq = __shfl_sync(0xffffffffu, oj, (int)q);
+          rank += (oq < o || (oq == o && kq < k)) ? 1u : 0u;
+        }
+      }
+      if (have) idx[b + rank] = k;
     }
-    idx[y] = k;
   }
 }
 
@@ -544,9 +562,15 @@ int launch_reverse_lists(dem_ctx* c) {
   int rc = scan_exclusive_u32(c, c->rev_cnt, c->rev_off, n);
   if (rc) return rc;
   ProfScope ps(c, K_REVERSE, 1 + (go ? 1 : 0) + (n ? 1 : 0));
+  // the contact work list L1 (capacity rcap, like rev_idx) holds the unsorted
+  // lists: the step's contact phase, after the rebuild, refills it
+  uint32_t* unsorted = c->L1;
   k_zero_u32<<<grid_for(n + 1, 256), 256, 0, st>>>(c->rev_cnt, n + 1);
-  if (go) k_rev_fill<<<gi, 256, 0, st>>>(I, ni, nd, c->rev_off, c->rev_cnt, c->rev_idx);
-  if (n) k_rev_sort<<<grid_for(n, 256), 256, 0, st>>>(n, c->rev_off, I.owner, c->P[c->pcur].id, c->rev_idx);
+  if (go) k_rev_fill<<<gi, 256, 0, st>>>(I, ni, nd, c->rev_off, c->rev_cnt, unsorted);
+  if (n) {
+    const unsigned gr = (unsigned)std::min<uint64_t>((n * 32 + 255) / 256, (uint64_t)c->num_sms * 16);
+    k_rev_rank<<<gr, 256, 0, st>>>(n, c->rev_off, I.owner, c->P[c->pcur].id, unsorted, c->rev_idx);
+  }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
 }
