@@ -95,6 +95,9 @@ def parse():
     ap.add_argument("--int-share", type=int, default=None, choices=list(range(9)),
                     help="eighths of the fused contact tiles whose law runs on the integer pipe (no effect on "
                          "results; default: the autotuner's choice)")
+    ap.add_argument("--cell-broad-phase", action="store_true",
+                    help="spheres: the warp-per-cell staged broad phase instead of thread per owner "
+                         "(same lists)")
     ap.add_argument("--learned", action="store_true",
                     help="polyhedra: harvest candidate pairs, train the MLP, time with learned sizing "
                          "and without it")
@@ -570,6 +573,8 @@ def run_native(args, rank, world, local, dist):
         s.set_mul_mode(args.mul_mode)
     if args.int_share is not None:
         s.set_contact_int_share(args.int_share)
+    if args.cell_broad_phase:
+        s.set_sphere_cell_broad_phase(1)
     s.step(args.warmup)
     torch.cuda.synchronize()
     s.reset_kernel_stats()
@@ -755,7 +760,8 @@ def config_block(args, w, pre, preroll_s, bed, mul_mode, idle_fraction):
            "path": "plain FP64 operator kernels" if args.plain else
                    "fused step, FP32 broad phase and contact screen, compacted FP64 contact law, exact fast division"
                    + (", whole step replayed as one CUDA graph" if getattr(w.params, "graph_step", 0) else "")
-                   + (f", {w.info['systems']} systems in one context" if is_batch(w) else ""),
+                   + (f", {w.info['systems']} systems in one context" if is_batch(w) else "")
+                   + (", warp-per-cell staged sphere broad phase" if args.cell_broad_phase else ""),
            "preroll_steps": pre, "preroll_s": round(preroll_s, 2),
            "timed_window": f"steps {pre + args.warmup + 1}..{pre + args.warmup + args.steps} after first_iteration",
            "mul_mode": None if args.plain else mul_mode,

@@ -212,6 +212,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_autotune", [_CTX, C.c_int, C.c_int, C.POINTER(TuneResult)])
     _sig(lib, "dem_set_mul_mode", [_CTX, C.c_int])
     _sig(lib, "dem_set_contact_int_share", [_CTX, C.c_int])
+    _sig(lib, "dem_set_sphere_cell_broad_phase", [_CTX, C.c_int])
     _sig(lib, "dem_set_multimat", [_CTX, C.c_int, C.POINTER(ContactParams), C.c_int, C.POINTER(ContactParams)])
     _sig(lib, "dem_set_analysis", [_CTX, C.c_int])
     _sig(lib, "dem_get_contact_state", [_CTX, C.POINTER(ContactState)])
@@ -265,7 +266,8 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_mlp_init", "dem_mlp_set_params", "dem_mlp_get_params", "dem_mlp_forward", "dem_mlp_loss_grad",
             "dem_mlp_train", "dem_learned_stats", "dem_set_inner_bond_params", "dem_stick_polyhedra",
             "dem_bond_count", "dem_get_bonds", "dem_set_bonds", "dem_broken_interface_count",
-            "dem_inner_bond_polyhedron", "dem_apply_interface_fracture_criterion", "dem_set_contact_int_share"]
+            "dem_inner_bond_polyhedron", "dem_apply_interface_fracture_criterion", "dem_set_contact_int_share",
+            "dem_set_sphere_cell_broad_phase"]
 
 _LIB = None
 

@@ -1152,6 +1152,13 @@ int dem_set_contact_int_share(dem_ctx* c, int eighths) {
   return DEM_OK;
 }
 
+int dem_set_sphere_cell_broad_phase(dem_ctx* c, int on) {
+  if (!c || on < 0 || on > 1) return DEM_ERR_INVALID_ARG;
+  c->cell_broad_phase = on;
+  c->gen++;  // a captured step holds the broad-phase kernels of the old choice
+  return DEM_OK;
+}
+
 int dem_get_mul_mode(dem_ctx* c, int* mode) {
   if (!c || !mode) return DEM_ERR_INVALID_ARG;
   *mode = c->mul_mode;

@@ -90,6 +90,7 @@ struct dem_ctx {
   bool fuse_contact = true;  // compacted contact: detection and law in one kernel (k_cfused), else two
   int mul_mode = 2;          // multiply placement of the fused integration kernels (integrate_core.cuh)
   int tune_int_share = 0;    // k_cfused: Hooke tiles out of 8 whose arithmetic runs on the integer pipe
+  int cell_broad_phase = 0;  // spheres, FP32 broad phase: warp per cell with staged neighbourhoods
 
   // graph step (dem_graph.cu)
   bool capturing = false;                  // kernels launched now go into a graph

@@ -12,9 +12,12 @@
 //   - each owner's list sorted by InteractionPair order, history (friction,
 //     moment) carried over from the previous list by key equality
 //     (interaction_manager.hpp:89-112, placeholder_interaction.hpp:398-408).
-// One thread per owner particle; particles are in cell order so the stencil
-// reads of neighbouring threads hit the same cells (L1/L2 reuse).  In a
-// batched context the particle's system gives the grid, its cell block and
+// Plain FP64 path (k_count / k_fill): one thread per owner particle; particles
+// are in cell order so the stencil reads of neighbouring threads hit the same
+// cells (L1/L2 reuse).  FP32 broad phase (k_cell_count / k_cell_fill): one warp
+// per cell, its 27-cell neighbourhood staged in shared memory, candidates
+// compacted with ballots, each owner's list ordered by a warp rank sort; the
+// drivers per particle (k_pre_count / k_pre_fill).  In a batched context the particle's system gives the grid, its cell block and
 // its drivers; a system rebuilt without its own trigger kept its slots, and
 // its previous list is copied as is (so its list is the one it has alone).
 #include "dem_ctx.cuh"
@@ -95,19 +98,11 @@ __device__ inline bool driver_filter(const DriverDev& d, double rcut, V3 p) {
   return dn <= 0;
 }
 
-template <bool F32, class Emit>
-__device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& emit) {
-  const double* __restrict__ rx = a.P.f[RX];
-  const double* __restrict__ ry = a.P.f[RY];
-  const double* __restrict__ rz = a.P.f[RZ];
-  const double* __restrict__ rad = a.P.f[RAD];
-  const uint64_t* __restrict__ id = a.P.id;
-  const V3 ri = mk(rx[s], ry[s], rz[s]);
-  const double radi = rad[s];
-  const uint64_t idi = id[s];
-  const int sys = a.sv.of(s);
-  const GridDev& g = a.sv.g[sys];
-  const uint32_t coff = a.sv.coff[sys];
+// the stationary drivers (surfaces, cylinders) of particle s's system that pass the filter
+template <class Emit>
+__device__ inline void for_each_driver(const BPArgs& a, uint32_t s, int sys, Emit&& emit) {
+  const V3 ri = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
+  const double radi = a.P.f[RAD][s];
   const int2 dr = a.sv.drange[sys];
   for (int k = dr.x; k < dr.x + dr.y; k++) {
     const DriverDev& d = a.drv[k];
@@ -116,6 +111,21 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
       emit((uint32_t)k, (uint64_t)k,
            make_meta(d.kind == 0 ? DEM_ITYPE_VERTEX_SURFACE : DEM_ITYPE_VERTEX_CYLINDER, 0, 0, 0, false), 0u);
   }
+}
+
+// the particle candidates of owner s over the 27-cell stencil, in stencil order
+template <bool F32, class Emit>
+__device__ inline void for_each_particle(const BPArgs& a, uint32_t s, int sys, Emit&& emit) {
+  const double* __restrict__ rx = a.P.f[RX];
+  const double* __restrict__ ry = a.P.f[RY];
+  const double* __restrict__ rz = a.P.f[RZ];
+  const double* __restrict__ rad = a.P.f[RAD];
+  const uint64_t* __restrict__ id = a.P.id;
+  const V3 ri = mk(rx[s], ry[s], rz[s]);
+  const double radi = rad[s];
+  const uint64_t idi = id[s];
+  const GridDev& g = a.sv.g[sys];
+  const uint32_t coff = a.sv.coff[sys];
   float xri = 0.f, yri = 0.f, zri = 0.f, rfi = 0.f, si = 0.f, cmax = 0.f;
   const float csx = (float)g.csz[0], csy = (float)g.csz[1], csz = (float)g.csz[2];
   if (F32) {
@@ -194,6 +204,14 @@ __device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& em
       }
     }
   }
+}
+
+// drivers, then particles (the emission order of the thread-per-owner kernels)
+template <bool F32, class Emit>
+__device__ inline void for_each_candidate(const BPArgs& a, uint32_t s, Emit&& emit) {
+  const int sys = a.sv.of(s);
+  for_each_driver(a, s, sys, emit);
+  for_each_particle<F32>(a, s, sys, emit);
 }
 
 // Mesh candidates (detection_sphere_driver, nbh_sphere.hpp:25-86): every mesh
@@ -294,6 +312,71 @@ __device__ inline bool key_less(uint64_t pa, uint32_t ta, uint32_t sa, uint64_t 
   return pa < pb || (pa == pb && (ta < tb || (ta == tb && sa < sb)));
 }
 
+// orders owner s's segment [b, e) by InteractionPair order and carries the
+// history over from the previous list
+__device__ inline void finish_owner(const BPArgs& a, uint32_t s, uint32_t b, uint32_t e, IArrays dst, IArrays old,
+                                    const uint32_t* __restrict__ old_off, const uint32_t* __restrict__ perm,
+                                    int have_old, int reuse_damp) {
+  for (uint32_t x = b + 1; x < e; x++) {
+    const uint64_t pk = dst.pid[x];
+    const uint32_t mk_ = dst.meta[x], qk = dst.partner[x], sk = dst.sub[x];
+    const uint32_t tk = meta_type(mk_);
+    uint32_t y = x;
+    while (y > b && key_less(pk, tk, sk, dst.pid[y - 1], meta_type(dst.meta[y - 1]), dst.sub[y - 1])) {
+      dst.pid[y] = dst.pid[y - 1];
+      dst.meta[y] = dst.meta[y - 1];
+      dst.partner[y] = dst.partner[y - 1];
+      dst.sub[y] = dst.sub[y - 1];
+      y--;
+    }
+    dst.pid[y] = pk;
+    dst.meta[y] = mk_;
+    dst.partner[y] = qk;
+    dst.sub[y] = sk;
+  }
+  // history carry-over: binary search in the previous list of the same particle
+  uint32_t ob = 0, oe = 0;
+  if (have_old) {
+    const uint32_t os = perm[s];
+    ob = old_off[os];
+    oe = old_off[os + 1];
+  }
+  for (uint32_t x = b; x < e; x++) {
+    dst.owner[x] = s;
+    double h[6] = {0, 0, 0, 0, 0, 0};
+    const uint64_t pk = dst.pid[x];
+    const uint32_t tk = meta_type(dst.meta[x]), sk = dst.sub[x];
+    uint32_t lo = ob, hi = oe;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (key_less(old.pid[mid], meta_type(old.meta[mid]), old.sub[mid], pk, tk, sk))
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    if (lo < oe && old.pid[lo] == pk && meta_type(old.meta[lo]) == tk && old.sub[lo] == sk) {
+      h[0] = old.ft[0][lo];
+      h[1] = old.ft[1][lo];
+      h[2] = old.ft[2][lo];
+      h[3] = old.mo[0][lo];
+      h[4] = old.mo[1][lo];
+      h[5] = old.mo[2][lo];
+      // the same pair in the previous list: the same masses and (reuse_damp) the
+      // same parameters, so the same damping bits, without the FP64 square root
+      // and division
+      dst.damp[x] = reuse_damp ? old.damp[lo] : pair_damp(a, s, dst.partner[x], dst.meta[x]);
+    } else {
+      dst.damp[x] = pair_damp(a, s, dst.partner[x], dst.meta[x]);
+    }
+    dst.ft[0][x] = h[0];
+    dst.ft[1][x] = h[1];
+    dst.ft[2][x] = h[2];
+    dst.mo[0][x] = h[3];
+    dst.mo[1][x] = h[4];
+    dst.mo[2][x] = h[5];
+  }
+}
+
 // reuse_damp: the previous list's damping was computed with the current contact
 // parameters (no dem_set_params / dem_set_multimat since, not a list installed by
 // dem_set_interactions), so a pair found in it keeps its damping bits.
@@ -333,64 +416,287 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
     }
     w++;
   });
-  for (uint32_t x = b + 1; x < e; x++) {
-    const uint64_t pk = dst.pid[x];
-    const uint32_t mk_ = dst.meta[x], qk = dst.partner[x], sk = dst.sub[x];
-    const uint32_t tk = meta_type(mk_);
-    uint32_t y = x;
-    while (y > b && key_less(pk, tk, sk, dst.pid[y - 1], meta_type(dst.meta[y - 1]), dst.sub[y - 1])) {
-      dst.pid[y] = dst.pid[y - 1];
-      dst.meta[y] = dst.meta[y - 1];
-      dst.partner[y] = dst.partner[y - 1];
-      dst.sub[y] = dst.sub[y - 1];
-      y--;
+  finish_owner(a, (uint32_t)s, b, e, dst, old, old_off, perm, have_old, reuse_damp);
+}
+
+// ---- warp-per-cell broad phase (FP32 decisions)
+// One warp per cell.  The particles of the cell's 27 stencil cells are staged
+// in shared memory (FP32 cell-relative coordinates and radius, id, index and
+// stencil slot, in stencil order), and the warp tests each owner of the cell
+// against them 32 candidates at a time, compacting the kept ones with ballots.
+// A neighbourhood of more than CELL_STAGE particles is walked per owner, lanes
+// over owners (for_each_particle).  The decisions are those of for_each_particle
+// (same FP32 expressions, same FP64 fallback), so the lists are the same.
+// Drivers are tested per particle (k_pre_count / k_pre_fill), where every lane
+// has an owner; in an owner's segment the mesh items come first, the particle
+// candidates next and the drivers last, and k_fill_finish then orders each
+// segment with the sort of k_fill.  The keys of a segment are distinct (a
+// periodic dimension has at least three cells, each at least the reach, so a
+// partner is in reach through one image at most), so the order of the
+// segment's parts does not matter.
+constexpr int CELL_WARPS = 4;
+constexpr int CELL_STAGE = 128;  // staged neighbourhood particles per warp
+constexpr uint8_t SLOT_OFF = 0x80u;  // stencil slot outside a non-periodic grid
+
+struct CellStage {
+  uint32_t q0[27];   // first particle of stencil slot l
+  uint32_t pre[28];  // staged candidates before slot l; pre[27] = all
+  uint8_t sh[27];    // (sx + 1) | (sy + 1) << 2 | (sz + 1) << 4 of slot l, or SLOT_OFF
+  float x[CELL_STAGE], y[CELL_STAGE], z[CELL_STAGE], r[CELL_STAGE];
+  uint64_t id[CELL_STAGE];
+  uint32_t q[CELL_STAGE];
+  uint8_t l[CELL_STAGE];
+};
+
+// stencil slots of cell c (local index in its system's grid) and the staging of
+// their particles; returns the neighbourhood's particle count (staged when at most CELL_STAGE)
+__device__ inline uint32_t stage_cell(const BPArgs& a, const GridDev& g, uint32_t coff, uint32_t c, CellStage& st,
+                                      int lane) {
+  uint32_t n = 0;
+  if (lane < 27) {
+    const int dz = lane / 9 - 1, dy = (lane / 3) % 3 - 1, dx = lane % 3 - 1;
+    const int d0 = g.dims[0], d1 = g.dims[1], d2n = g.dims[2];
+    const int cx = (int)(c % (uint32_t)d0);
+    const int cy = (int)((c / (uint32_t)d0) % (uint32_t)d1);
+    const int cz = (int)(c / ((uint32_t)d0 * (uint32_t)d1));
+    int x = cx + dx, y = cy + dy, z = cz + dz, sx = 0, sy = 0, sz = 0;
+    bool ok = true;
+    if (x < 0) { ok &= g.periodic[0] != 0; x += d0; sx = -1; } else if (x >= d0) { ok &= g.periodic[0] != 0; x -= d0; sx = 1; }
+    if (y < 0) { ok &= g.periodic[1] != 0; y += d1; sy = -1; } else if (y >= d1) { ok &= g.periodic[1] != 0; y -= d1; sy = 1; }
+    if (z < 0) { ok &= g.periodic[2] != 0; z += d2n; sz = -1; } else if (z >= d2n) { ok &= g.periodic[2] != 0; z -= d2n; sz = 1; }
+    uint32_t q0 = 0;
+    if (ok) {
+      const uint32_t cc = coff + (uint32_t)x + (uint32_t)d0 * ((uint32_t)y + (uint32_t)d1 * (uint32_t)z);
+      q0 = a.cell_start[cc];
+      n = a.cell_start[cc + 1] - q0;
     }
-    dst.pid[y] = pk;
-    dst.meta[y] = mk_;
-    dst.partner[y] = qk;
-    dst.sub[y] = sk;
+    st.q0[lane] = q0;
+    st.sh[lane] = ok ? (uint8_t)((sx + 1) | ((sy + 1) << 2) | ((sz + 1) << 4)) : SLOT_OFF;
   }
-  // history carry-over: binary search in the previous list of the same particle
-  uint32_t ob = 0, oe = 0;
-  if (have_old) {
-    const uint32_t os = perm[s];
-    ob = old_off[os];
-    oe = old_off[os + 1];
+  uint32_t v = n;  // inclusive scan over the slots
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
   }
-  for (uint32_t x = b; x < e; x++) {
-    dst.owner[x] = (uint32_t)s;
-    double h[6] = {0, 0, 0, 0, 0, 0};
-    const uint64_t pk = dst.pid[x];
-    const uint32_t tk = meta_type(dst.meta[x]), sk = dst.sub[x];
-    uint32_t lo = ob, hi = oe;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (key_less(old.pid[mid], meta_type(old.meta[mid]), old.sub[mid], pk, tk, sk))
-        lo = mid + 1;
-      else
-        hi = mid;
+  if (lane < 27) st.pre[lane] = v - n;
+  const uint32_t T = __shfl_sync(0xffffffffu, v, 31);
+  if (lane == 0) st.pre[27] = T;
+  __syncwarp();
+  if (T <= (uint32_t)CELL_STAGE) {
+    for (uint32_t i = (uint32_t)lane; i < T; i += 32) {
+      int lo = 0, hi = 27;  // last slot l with pre[l] <= i (a slot holding i is not empty)
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (st.pre[mid] <= i)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      const uint32_t q = st.q0[lo] + (i - st.pre[lo]);
+      st.x[i] = a.xr[q];
+      st.y[i] = a.yr[q];
+      st.z[i] = a.zr[q];
+      st.r[i] = a.rf[q];
+      st.id[i] = a.P.id[q];
+      st.q[i] = q;
+      st.l[i] = (uint8_t)lo;
     }
-    if (lo < oe && old.pid[lo] == pk && meta_type(old.meta[lo]) == tk && old.sub[lo] == sk) {
-      h[0] = old.ft[0][lo];
-      h[1] = old.ft[1][lo];
-      h[2] = old.ft[2][lo];
-      h[3] = old.mo[0][lo];
-      h[4] = old.mo[1][lo];
-      h[5] = old.mo[2][lo];
-      // the same pair in the previous list: the same masses and (reuse_damp) the
-      // same parameters, so the same damping bits, without the FP64 square root
-      // and division
-      dst.damp[x] = reuse_damp ? old.damp[lo] : pair_damp(a, (uint32_t)s, dst.partner[x], dst.meta[x]);
-    } else {
-      dst.damp[x] = pair_damp(a, (uint32_t)s, dst.partner[x], dst.meta[x]);
-    }
-    dst.ft[0][x] = h[0];
-    dst.ft[1][x] = h[1];
-    dst.ft[2][x] = h[2];
-    dst.mo[0][x] = h[3];
-    dst.mo[1][x] = h[4];
-    dst.mo[2][x] = h[5];
   }
+  __syncwarp();
+  return T;
+}
+
+// staged candidate i against owner s: for_each_particle's decision
+__device__ __forceinline__ bool cell_keep(const BPArgs& a, const GridDev& g, const CellStage& st, uint32_t i,
+                                          uint64_t idi, float xri, float yri, float zri, float rfi, float si,
+                                          float cmax, V3 ri, double radi, uint32_t& meta) {
+  const int l = st.l[i];
+  const int sh = st.sh[l];
+  const int sx = (sh & 3) - 1, sy = ((sh >> 2) & 3) - 1, sz = ((sh >> 4) & 3) - 1;
+  const bool ghost = (sx | sy | sz) != 0;
+  if (!ghost && idi >= st.id[i]) return false;  // owner rule first
+  const float oxf = (float)(l % 3 - 1) * (float)g.csz[0], oyf = (float)((l / 3) % 3 - 1) * (float)g.csz[1],
+              ozf = (float)(l / 9 - 1) * (float)g.csz[2];
+  const float xj = st.x[i], yj = st.y[i], zj = st.z[i];
+  const float sj = fmaxf(fabsf(xj), fmaxf(fabsf(yj), fabsf(zj)));
+  int keep = f32_decide((xj - xri) + oxf, (yj - yri) + oyf, (zj - zri) + ozf, si, sj, cmax, rfi + st.r[i] + a.skin_f);
+  if (keep < 0) {
+    const uint32_t q = st.q[i];
+    V3 rj = mk(a.P.f[RX][q], a.P.f[RY][q], a.P.f[RZ][q]);
+    if (sx) rj.x = rj.x + (double)sx * g.L[0];
+    if (sy) rj.y = rj.y + (double)sy * g.L[1];
+    if (sz) rj.z = rj.z + (double)sz * g.L[2];
+    const double ddx = rj.x - ri.x, ddy = rj.y - ri.y, ddz = rj.z - ri.z;
+    const double d2 = ddx * ddx + ddy * ddy + ddz * ddz;
+    const double rmax = radi + a.P.f[RAD][q] + a.skin;
+    keep = (d2 > 0.0 && d2 < rmax * rmax && d2 < a.rcut2) ? 1 : 0;
+  }
+  meta = make_meta(DEM_ITYPE_VERTEX_VERTEX, sx, sy, sz, ghost);
+  return keep != 0;
+}
+
+// the particle candidates of every owner of cell C: counted (Fill = false: added
+// to cnt) or written at b + mesh items (Fill = true)
+template <bool Fill>
+__device__ inline void cell_particles(const BPArgs& a, uint32_t C, uint32_t o0, uint32_t o1, int sys, CellStage& st,
+                                      int lane, uint32_t* cnt, const uint32_t* off, IArrays dst) {
+  const GridDev& g = a.sv.g[sys];
+  const uint32_t coff = a.sv.coff[sys];
+  const uint32_t T = stage_cell(a, g, coff, C - coff, st, lane);
+  const uint32_t lt = (1u << lane) - 1u;
+  if (T > (uint32_t)CELL_STAGE) {  // dense neighbourhood: lanes over owners
+    for (uint32_t s = o0 + (uint32_t)lane; s < o1; s += 32) {
+      if (Fill) {
+        const uint32_t b = off[s], e = off[s + 1];
+        if (e > a.cap) continue;
+        uint32_t w = b + (a.has_mesh ? a.mcnt[s] : 0u);
+        for_each_particle<true>(a, s, sys, [&](uint32_t q, uint64_t pid, uint32_t meta, uint32_t sub) {
+          if (w < e) {
+            dst.partner[w] = q;
+            dst.pid[w] = pid;
+            dst.meta[w] = meta;
+            dst.sub[w] = sub;
+          }
+          w++;
+        });
+      } else {
+        uint32_t m = 0;
+        for_each_particle<true>(a, s, sys, [&](uint32_t, uint64_t, uint32_t, uint32_t) { m++; });
+        cnt[s] += m;
+      }
+    }
+    __syncwarp();
+    return;
+  }
+  const float cmax = fmaxf((float)g.csz[0], fmaxf((float)g.csz[1], (float)g.csz[2]));
+  for (uint32_t s = o0; s < o1; s++) {
+    uint32_t w = 0, e = 0;
+    if (Fill) {
+      e = off[s + 1];
+      if (e > a.cap) continue;
+      w = off[s] + (a.has_mesh ? a.mcnt[s] : 0u);
+    }
+    const float xri = a.xr[s], yri = a.yr[s], zri = a.zr[s], rfi = a.rf[s];
+    const float si = fmaxf(fabsf(xri), fmaxf(fabsf(yri), fabsf(zri)));
+    const uint64_t idi = a.P.id[s];
+    const V3 ri = mk(a.P.f[RX][s], a.P.f[RY][s], a.P.f[RZ][s]);
+    const double radi = a.P.f[RAD][s];
+    uint32_t m = 0;
+    for (uint32_t c0 = 0; c0 < T; c0 += 32) {
+      const uint32_t i = c0 + (uint32_t)lane;
+      uint32_t meta = 0;
+      const bool keep = i < T && cell_keep(a, g, st, i, idi, xri, yri, zri, rfi, si, cmax, ri, radi, meta);
+      const unsigned bm = __ballot_sync(0xffffffffu, keep);
+      if (Fill && keep) {
+        const uint32_t x = w + m + __popc(bm & lt);
+        if (x < e) {
+          dst.partner[x] = st.q[i];
+          dst.pid[x] = st.id[i];
+          dst.meta[x] = meta;
+          dst.sub[x] = 0u;
+        }
+      }
+      m += __popc(bm);
+    }
+    if (!Fill && lane == 0) cnt[s] += m;
+  }
+}
+
+// drivers of each particle (after the mesh items, counted in k_mesh_count), or
+// the previous count of a particle whose system kept its list
+__global__ void k_pre_count(BPArgs a, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ old_off) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  const int sys = a.sv.of(s);
+  if (!a.sv.triggered(sys)) {
+    cnt[s] = old_off[s + 1] - old_off[s];
+    return;
+  }
+  uint32_t m = a.has_mesh ? a.mcnt[s] : 0u;
+  for_each_driver(a, (uint32_t)s, sys, [&](uint32_t, uint64_t, uint32_t, uint32_t) { m++; });
+  cnt[s] = m;
+}
+
+// drivers at the end of each particle's segment; a particle whose system kept
+// its list copies it
+__global__ void k_pre_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, IArrays old,
+                           const uint32_t* __restrict__ old_off) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  const uint32_t b = off[s], e = off[s + 1];
+  if (e > a.cap) return;
+  const int sys = a.sv.of(s);
+  if (!a.sv.triggered(sys)) {
+    const uint32_t ob = old_off[s];
+    for (uint32_t x = b; x < e; x++) {
+      const uint32_t y = ob + (x - b);
+      dst.owner[x] = (uint32_t)s;
+      dst.partner[x] = old.partner[y];
+      dst.pid[x] = old.pid[y];
+      dst.meta[x] = old.meta[y];
+      dst.sub[x] = old.sub[y];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        dst.ft[d][x] = old.ft[d][y];
+        dst.mo[d][x] = old.mo[d][y];
+      }
+      dst.damp[x] = old.damp[y];
+    }
+    return;
+  }
+  uint32_t nd = 0;
+  for_each_driver(a, (uint32_t)s, sys, [&](uint32_t, uint64_t, uint32_t, uint32_t) { nd++; });
+  uint32_t w = e - nd;
+  for_each_driver(a, (uint32_t)s, sys, [&](uint32_t k, uint64_t pid, uint32_t meta, uint32_t sub) {
+    dst.partner[w] = k;
+    dst.pid[w] = pid;
+    dst.meta[w] = meta;
+    dst.sub[w] = sub;
+    w++;
+  });
+}
+
+__global__ void __launch_bounds__(CELL_WARPS * 32) k_cell_count(BPArgs a, uint32_t* __restrict__ cnt,
+                                                                uint64_t ncell) {
+  __shared__ CellStage stage[CELL_WARPS];
+  const int lane = threadIdx.x & 31;
+  CellStage& st = stage[threadIdx.x >> 5];
+  const uint64_t nw = (uint64_t)gridDim.x * CELL_WARPS;
+  for (uint64_t C = (uint64_t)blockIdx.x * CELL_WARPS + (threadIdx.x >> 5); C < ncell; C += nw) {
+    const uint32_t o0 = a.cell_start[C], o1 = a.cell_start[C + 1];
+    if (o0 == o1) continue;
+    const int sys = a.sv.of(o0);
+    if (!a.sv.triggered(sys)) continue;
+    cell_particles<false>(a, (uint32_t)C, o0, o1, sys, st, lane, cnt, nullptr, IArrays{});
+  }
+}
+
+__global__ void __launch_bounds__(CELL_WARPS * 32) k_cell_fill(BPArgs a, const uint32_t* __restrict__ off,
+                                                               IArrays dst, uint64_t ncell) {
+  __shared__ CellStage stage[CELL_WARPS];
+  const int lane = threadIdx.x & 31;
+  CellStage& st = stage[threadIdx.x >> 5];
+  const uint64_t nw = (uint64_t)gridDim.x * CELL_WARPS;
+  for (uint64_t C = (uint64_t)blockIdx.x * CELL_WARPS + (threadIdx.x >> 5); C < ncell; C += nw) {
+    const uint32_t o0 = a.cell_start[C], o1 = a.cell_start[C + 1];
+    if (o0 == o1) continue;
+    const int sys = a.sv.of(o0);
+    if (!a.sv.triggered(sys)) continue;
+    cell_particles<true>(a, (uint32_t)C, o0, o1, sys, st, lane, nullptr, off, dst);
+  }
+}
+
+// after k_mesh_fill, k_pre_fill and k_cell_fill: each owner's segment ordered and
+// its history carried over, one thread per owner
+__global__ void k_fill_finish(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, IArrays old,
+                              const uint32_t* __restrict__ old_off, const uint32_t* __restrict__ perm, int have_old,
+                              int reuse_damp) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= a.n) return;
+  const uint32_t b = off[s], e = off[s + 1];
+  if (e > a.cap || !a.sv.triggered(a.sv.of(s))) return;
+  finish_owner(a, (uint32_t)s, b, e, dst, old, old_off, perm, have_old, reuse_damp);
 }
 
 // per-pair damping of a kept list after the contact parameters changed
@@ -502,6 +808,12 @@ int refresh_pair_damp(dem_ctx* c) {
   return DEM_OK;
 }
 
+// the warp-per-cell kernels: a grid-stride loop over the cells
+static unsigned cell_grid(const dem_ctx* c) {
+  const uint64_t want = (c->ncell + CELL_WARPS - 1) / CELL_WARPS;
+  return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)c->num_sms * 16));
+}
+
 int launch_count_sphere(dem_ctx* c) {
   const bool mesh = !c->meshes.empty();
   ProfScope ps(c, K_BROAD_COUNT, c->n ? (mesh ? 2 : 1) : 0);
@@ -513,10 +825,15 @@ int launch_count_sphere(dem_ctx* c) {
       k_mesh_count<false><<<grid_for(c->n * 32, 128), 128, 0, c->stream>>>(make_args(c), c->mesh_cnt);
   }
   if (c->n) {
-    if (c->prm.fp32_broad_phase)
+    if (c->prm.fp32_broad_phase && c->cell_broad_phase) {
+      const BPArgs a = make_args(c);
+      k_pre_count<<<grid_for(c->n, 128), 128, 0, c->stream>>>(a, c->pcnt, c->own_off[c->icur]);
+      k_cell_count<<<cell_grid(c), CELL_WARPS * 32, 0, c->stream>>>(a, c->pcnt, c->ncell);
+    } else if (c->prm.fp32_broad_phase) {
       k_count<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt, c->own_off[c->icur]);
-    else
+    } else {
       k_count<false><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), c->pcnt, c->own_off[c->icur]);
+    }
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
@@ -535,7 +852,14 @@ int launch_fill_sphere(dem_ctx* c, uint32_t* new_off, uint64_t total) {
   }
   if (c->n) {
     const int have_old = c->hist_valid ? 1 : 0, reuse = (c->hist_valid && !c->damp_stale) ? 1 : 0;
-    if (c->prm.fp32_broad_phase)
+    if (c->prm.fp32_broad_phase && c->cell_broad_phase) {
+      const BPArgs a = make_args(c);
+      k_pre_fill<<<grid_for(c->n, 128), 128, 0, c->stream>>>(a, new_off, c->I[nw], c->I[c->icur],
+                                                             c->own_off[c->icur]);
+      k_cell_fill<<<cell_grid(c), CELL_WARPS * 32, 0, c->stream>>>(a, new_off, c->I[nw], c->ncell);
+      k_fill_finish<<<grid_for(c->n, 128), 128, 0, c->stream>>>(a, new_off, c->I[nw], c->I[c->icur],
+                                                                c->own_off[c->icur], c->perm, have_old, reuse);
+    } else if (c->prm.fp32_broad_phase)
       k_fill<true><<<grid_for(c->n, 128), 128, 0, c->stream>>>(make_args(c), new_off, c->I[nw], c->I[c->icur],
                                                                c->own_off[c->icur], c->perm, have_old, reuse);
     else

@@ -323,6 +323,10 @@ class System:
     def set_contact_int_share(self, eighths: int) -> None:
         self._check(self.b.set_contact_int_share(self.h, int(eighths)), "set_contact_int_share")
 
+    def set_sphere_cell_broad_phase(self, on: int) -> None:
+        """dem_set_sphere_cell_broad_phase: warp-per-cell staged sphere broad phase (same lists)."""
+        self._check(self.b.set_sphere_cell_broad_phase(self.h, int(on)), "set_sphere_cell_broad_phase")
+
     def mul_mode(self) -> int:
         v = C.c_int()
         self._check(self.b.get_mul_mode(self.h, C.byref(v)), "get_mul_mode")

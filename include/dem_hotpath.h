@@ -396,6 +396,16 @@ int dem_get_mul_mode(dem_ctx* ctx, int* mode);
  * an emulated addition costs several times an FP64 one; the autotuner leaves
  * it at 0.  No reference counterpart (a placement of the same arithmetic). */
 int dem_set_contact_int_share(dem_ctx* ctx, int eighths);
+/* Sphere broad phase with fp32_broad_phase (replaces the particle-pair part of
+ * nbh_sphere, src/sphere/nbh_sphere.cu:64-309, as the default kernels do):
+ * 0 = one thread per owner particle (default); 1 = one warp per cell, the
+ * 27-cell neighbourhood's FP32 coordinates, radii and ids staged in shared
+ * memory, candidates compacted with warp ballots, drivers tested per particle.
+ * The lists are identical in both modes.  Measured on GB300 (2 M sphere bed,
+ * about 35 particles per neighbourhood): mode 1 runs the count and fill passes
+ * slower, since a warp per cell leaves lanes idle where a thread per owner keeps
+ * all 32 busy and L1 already serves the stencil reuse. */
+int dem_set_sphere_cell_broad_phase(dem_ctx* ctx, int on);
 /* Number of neighbour rebuilds done so far (trigger_move_particles count). */
 int dem_rebuild_count(dem_ctx* ctx, uint64_t* out);
 
