@@ -373,6 +373,12 @@ void free_units(dem_ctx* c) {
   c->slot_cap = 0;
   cudaFree(c->f_cnt);
   cudaFree(c->f_off);
+  cudaFree(c->u_rec);
+  cudaFree(c->t_cnt);
+  cudaFree(c->t_off);
+  cudaFree(c->t_keep);
+  c->u_rec = c->t_cnt = c->t_off = c->t_keep = nullptr;
+  c->t_keepcap = 0;
   c->u_owner = c->u_partner = c->u_kind = c->f_cnt = c->f_off = nullptr;
   c->u_pid = nullptr;
   c->u_pass = nullptr;
@@ -398,6 +404,9 @@ int grow_units(dem_ctx* c, uint64_t need) {
   DEM_CUDA_TRY(c, cudaMalloc(&c->u_rates, cap * DEM_MLP_OUT * sizeof(float)));
   DEM_CUDA_TRY(c, cudaMalloc(&c->f_cnt, (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->f_off, (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->u_rec, cap * 64));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->t_cnt, (6 * cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->t_off, (6 * cap + 1) * 4));
   c->ucap = cap;
   return DEM_OK;
 }

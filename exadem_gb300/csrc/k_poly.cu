@@ -1149,6 +1149,274 @@ __global__ void __launch_bounds__(PT, 4) k_feat_dec(FeatArgs a) {
   }
 }
 
+// ---- flattened FP32-decided enumeration (count pass without learned sizing)
+// The tests of k_feat_dec, spread over the whole GPU instead of a warp per unit:
+//   k_feat_prep   one warp per unit: the vertex gates and the near-feature
+//                 filters of k_feat_dec, kept as bit masks (UnitRec), and the
+//                 test count of each of the six segments;
+//   scan          over the (segment, unit) test counts, segment-major: the test
+//                 index space is (segment, unit, row, column);
+//   k_feat_test   32 consecutive tests per warp: every lane of a warp runs the
+//                 same decision (one segment) on its own test, so the FP32
+//                 arithmetic is dense and the kernel small; one kept-bit per test;
+//   k_feat_collect one warp per unit: the kept bits of its six segments, in
+//                 segment order, give its count (and its types), or in the fill
+//                 pass its features in the order k_feat writes them.
+// The decisions and the FP64 fallback are those of dec_segment, so the list is
+// the same bit for bit.
+struct UnitRec {
+  uint32_t gA, gB, vB, fA, fB;  // gated A vertices, gated B vertices, B vertices near A, A / B faces near the other
+  uint32_t eA[2], eB[2];        // A / B edges near the other (64 bits)
+  float dRx, dRy, dRz, S, R;
+  uint32_t pad[2];
+};
+static_assert(sizeof(UnitRec) == 64, "UnitRec is one 64-byte line");
+
+__device__ __forceinline__ uint64_t u64of(uint32_t lo, uint32_t hi) { return (uint64_t)lo | ((uint64_t)hi << 32); }
+__device__ __forceinline__ int nth_bit64(uint64_t m, int r) {
+  const uint32_t lo = (uint32_t)m;
+  const int pl = __popc(lo);
+  return r < pl ? nth_bit(lo, r) : 32 + nth_bit((uint32_t)(m >> 32), r - pl);
+}
+// rows and columns of segment seg (see dec_segment)
+__device__ __forceinline__ void seg_masks(const UnitRec& q, int seg, uint64_t& rows, uint64_t& cols) {
+  const uint64_t eA = u64of(q.eA[0], q.eA[1]), eB = u64of(q.eB[0], q.eB[1]);
+  rows = (seg == 2 || seg == 5) ? eA : (seg == 4 ? (uint64_t)q.fA : (uint64_t)q.gA);
+  cols = seg == 0 ? (uint64_t)q.vB : (seg == 1 || seg == 5 ? eB : (seg == 3 ? (uint64_t)q.fB : (uint64_t)q.gB));
+}
+
+__global__ void __launch_bounds__(PT) k_feat_prep(FeatArgs a, UnitRec* __restrict__ rec, uint32_t* __restrict__ tcnt) {
+  const int lane = threadIdx.x & 31;
+  const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
+  for (uint64_t u = warp; u < a.nu; u += nwarps) {
+    if (!a.pass[u] || a.u_kind[u]) {
+      if (lane < 6) tcnt[(uint64_t)lane * a.nu + u] = 0u;
+      continue;
+    }
+    const uint32_t A = a.u_owner[u], B = a.u_partner[u];
+    const ShapeDev& SA = a.shapes[a.P.type[A]];
+    const ShapeDev& SB = a.shapes[a.P.type[B]];
+    const double ra = SA.r * a.P.f[HOM][A], rb = SB.r * a.P.f[HOM][B];
+    const F3 dR = f3((float)(a.P.f[RX][B] - a.P.f[RX][A]), (float)(a.P.f[RY][B] - a.P.f[RY][A]),
+                     (float)(a.P.f[RZ][B] - a.P.f[RZ][A]));
+    const F3 zero = f3(0.f, 0.f, 0.f);
+    const uint64_t oA = (uint64_t)A * a.MV, oB = (uint64_t)B * a.MV;
+    const FView fa{a.fvx + oA, a.fvy + oA, a.fvz + oA, zero};
+    const FView fb{a.fvx + oB, a.fvy + oB, a.fvz + oB, dR};
+    float sv = fmaxf(lane < SA.nv ? flen(fa[lane]) : 0.f, lane < SB.nv ? flen(fb[lane]) : 0.f);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) sv = fmaxf(sv, __shfl_xor_sync(0xffffffffu, sv, o));
+    const float S = sv * 1.001f + (float)(ra + rb + a.rV);
+    const float R = (float)(ra + rb + a.rV);
+    const float lim = R + S * 6.1035156e-05f;  // R + 2^-14 S
+    const float* bA = a.fbox + (uint64_t)A * FBOX_STRIDE;
+    const float* bB = a.fbox + (uint64_t)B * FBOX_STRIDE;
+    UnitRec q{};
+    for (int k0 = 0; k0 < SA.nv + SB.nv; k0 += 32) {
+      const int k = k0 + lane;
+      const bool sideA = k < SA.nv, valid = k < SA.nv + SB.nv;
+      const int vi = sideA ? k : k - SA.nv;
+      int d = DEC_FALSE;
+      bool near = false;
+      if (valid) {
+        const F3 p = sideA ? fa[vi] : fb[vi];
+        d = decide_gate(load_obbf(sideA ? bB : bA, sideA ? dR : zero), p, (float)(sideA ? ra : rb), S);
+        if (!sideA) near = slab_near_point(load_slabs(bA, zero), p, lim);
+      }
+      bool g = d == DEC_TRUE;
+      if (__any_sync(0xffffffffu, d == DEC_UNDECIDED) && d == DEC_UNDECIDED) {
+        OBBd o = load_obb(a.obb + (uint64_t)(sideA ? B : A) * 15);
+        obb_enlarge(o, 0.5 * a.rV);
+        obb_enlarge(o, 0.5 * a.rV);
+        g = vertex_gate(o, sideA ? vview(a, A)[vi] : vview(a, B)[vi], sideA ? ra : rb);
+      }
+      q.gA |= __reduce_or_sync(0xffffffffu, (g && sideA) ? 1u << vi : 0u);
+      q.gB |= __reduce_or_sync(0xffffffffu, (g && valid && !sideA) ? 1u << vi : 0u);
+      q.vB |= __reduce_or_sync(0xffffffffu, near ? 1u << vi : 0u);
+    }
+    for (int k0 = 0; k0 < SA.ne + SB.ne; k0 += 32) {
+      const int k = k0 + lane;
+      const bool sideA = k < SA.ne, valid = k < SA.ne + SB.ne;
+      const int e = sideA ? k : k - SA.ne;
+      bool near = false;
+      if (valid) {
+        const FView& fv = sideA ? fa : fb;
+        const int* ev = sideA ? SA.e : SB.e;
+        near = slab_near_segment(load_slabs(sideA ? bB : bA, sideA ? dR : zero), fv[ev[2 * e]], fv[ev[2 * e + 1]],
+                                 (float)a.rV, lim);
+      }
+      const uint32_t lo = (near && e < 32) ? 1u << e : 0u, hi = (near && e >= 32) ? 1u << (e - 32) : 0u;
+      q.eA[0] |= __reduce_or_sync(0xffffffffu, sideA ? lo : 0u);
+      q.eA[1] |= __reduce_or_sync(0xffffffffu, sideA ? hi : 0u);
+      q.eB[0] |= __reduce_or_sync(0xffffffffu, sideA ? 0u : lo);
+      q.eB[1] |= __reduce_or_sync(0xffffffffu, sideA ? 0u : hi);
+    }
+    for (int k0 = 0; k0 < SA.nf + SB.nf; k0 += 32) {
+      const int k = k0 + lane;
+      const bool sideA = k < SA.nf, valid = k < SA.nf + SB.nf;
+      const int f = sideA ? k : k - SA.nf;
+      bool near = false;
+      if (valid)
+        near = slab_near_face(load_slabs(sideA ? bB : bA, sideA ? dR : zero), sideA ? fa : fb, sideA ? SA : SB, f,
+                              lim);
+      q.fA |= __reduce_or_sync(0xffffffffu, (near && sideA) ? 1u << f : 0u);
+      q.fB |= __reduce_or_sync(0xffffffffu, (near && !sideA) ? 1u << f : 0u);
+    }
+    if (lane == 0) {
+      q.dRx = dR.x;
+      q.dRy = dR.y;
+      q.dRz = dR.z;
+      q.S = S;
+      q.R = R;
+      rec[u] = q;
+    }
+    if (lane < 6) {
+      uint64_t rows, cols;
+      seg_masks(q, lane, rows, cols);
+      tcnt[(uint64_t)lane * a.nu + u] = (uint32_t)(__popcll(rows) * __popcll(cols));
+    }
+  }
+}
+
+// last group g in [lo, hi] with off[g] <= t (a group holding t is not empty)
+__device__ __forceinline__ uint32_t group_of(const uint32_t* __restrict__ off, uint32_t lo, uint32_t hi, uint32_t t) {
+  while (lo < hi) {
+    const uint32_t mid = lo + ((hi - lo + 1) >> 1);
+    if (off[mid] <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(PT) k_feat_test(FeatArgs a, const UnitRec* __restrict__ rec,
+                                                  const uint32_t* __restrict__ toff, uint32_t ntests,
+                                                  uint32_t* __restrict__ keep) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t ng = (uint32_t)(6 * a.nu);
+  const uint32_t nu = (uint32_t)a.nu;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
+  for (uint64_t w = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5; w * 32 < ntests; w += nwarps) {
+    const uint32_t T0 = (uint32_t)(w * 32), Tl = min(T0 + 31u, ntests - 1u);
+    uint32_t gb = 0;
+    if (lane == 0) gb = group_of(toff, 0u, ng - 1u, T0);
+    if (lane == 31) gb = group_of(toff, 0u, ng - 1u, Tl);
+    const uint32_t g0 = __shfl_sync(0xffffffffu, gb, 0), g1 = __shfl_sync(0xffffffffu, gb, 31);
+    const uint32_t T = T0 + (uint32_t)lane;
+    bool kp = false;
+    if (T < ntests) {
+      const uint32_t g = group_of(toff, g0, g1, T);
+      const int seg = (int)(g / nu);
+      const uint32_t u = g - (uint32_t)seg * nu;
+      const uint32_t loc = T - toff[g];
+      const UnitRec q = rec[u];
+      uint64_t rows, cols;
+      seg_masks(q, seg, rows, cols);
+      const uint32_t nc = (uint32_t)__popcll(cols);
+      const uint32_t r = loc / nc;
+      const int i = nth_bit64(rows, (int)r), j = nth_bit64(cols, (int)(loc - r * nc));
+      const uint32_t A = a.u_owner[u], B = a.u_partner[u];
+      const ShapeDev& SA = a.shapes[a.P.type[A]];
+      const ShapeDev& SB = a.shapes[a.P.type[B]];
+      const uint64_t oA = (uint64_t)A * a.MV, oB = (uint64_t)B * a.MV;
+      const FView fa{a.fvx + oA, a.fvy + oA, a.fvz + oA, f3(0.f, 0.f, 0.f)};
+      const FView fb{a.fvx + oB, a.fvy + oB, a.fvz + oB, f3(q.dRx, q.dRy, q.dRz)};
+      int d;
+      if (seg == 0) {
+        d = decide_vv(fa[i], fb[j], q.R, q.S);
+      } else if (seg == 1) {
+        d = decide_ve(fa[i], fb[SB.e[2 * j]], fb[SB.e[2 * j + 1]], q.R, (float)a.rV, q.S);
+      } else if (seg == 2) {
+        d = decide_ve(fb[j], fa[SA.e[2 * i]], fa[SA.e[2 * i + 1]], q.R, (float)a.rV, q.S);
+      } else if (seg == 3) {
+        d = decide_vf_nf(fa[i], fb, SB, j, q.R, q.S);
+      } else if (seg == 4) {
+        d = decide_vf_nf(fb[j], fa, SA, i, q.R, q.S);
+      } else {
+        d = decide_ee(fa[SA.e[2 * i]], fa[SA.e[2 * i + 1]], fb[SB.e[2 * j]], fb[SB.e[2 * j + 1]], q.R, q.S);
+      }
+      kp = d == DEC_TRUE;
+      if (d == DEC_UNDECIDED)
+        kp = exact_filter(seg, i, j, a.rV, vview(a, A), SA.r * a.P.f[HOM][A], SA, vview(a, B),
+                          SB.r * a.P.f[HOM][B], SB);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, kp);
+    if (lane == 0) keep[w] = m;
+  }
+}
+
+template <bool Fill>
+__global__ void __launch_bounds__(PT) k_feat_collect(FeatArgs a, const UnitRec* __restrict__ rec,
+                                                     const uint32_t* __restrict__ toff,
+                                                     const uint32_t* __restrict__ keep) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
+  for (uint64_t u = warp; u < a.nu; u += nwarps) {
+    const uint32_t base = Fill ? a.foff[u] : 0u;
+    if (!a.pass[u]) {
+      if (!Fill && lane == 0) {
+        a.fcnt[u] = 0;
+        a.utypes[u] = 0u;
+      }
+      continue;
+    }
+    const uint32_t A = a.u_owner[u];
+    if (a.u_kind[u]) {
+      const ShapeDev& SA = a.shapes[a.P.type[A]];
+      driver_unit<Fill>(a, u, A, SA, SA.r * a.P.f[HOM][A], vview(a, A), base, lane, lt);
+      if (!Fill && lane == 0) a.utypes[u] = 0u;
+      continue;
+    }
+    const UnitRec q = rec[u];
+    uint32_t count = 0, ty[4] = {0u, 0u, 0u, 0u};
+    for (int seg = 0; seg < 6; seg++) {
+      const uint64_t g = (uint64_t)seg * a.nu + u;
+      const uint32_t b = toff[g], e = toff[g + 1];
+      uint32_t n = 0;
+      if (Fill) {
+        uint64_t rows, cols;
+        seg_masks(q, seg, rows, cols);
+        const uint32_t nc = (uint32_t)__popcll(cols);
+        for (uint32_t t0 = b; t0 < e; t0 += 32) {
+          const uint32_t t = t0 + (uint32_t)lane;
+          const bool kp = t < e && ((keep[t >> 5] >> (t & 31u)) & 1u);
+          const unsigned m = __ballot_sync(0xffffffffu, kp);
+          if (kp) {
+            const uint32_t loc = t - b, r = loc / nc;
+            write_feature(a, base + count + n + __popc(m & lt), A, a.u_partner[u], a.u_pid[u], seg_type(seg),
+                          seg_swap(seg), nth_bit64(rows, (int)r), nth_bit64(cols, (int)(loc - r * nc)));
+          }
+          n += __popc(m);
+        }
+      } else {
+        uint32_t c = 0;
+        for (uint32_t w0 = (b >> 5); w0 <= ((e - 1u) >> 5) && b < e; w0 += 32) {
+          const uint32_t wd = w0 + (uint32_t)lane;
+          if (wd <= ((e - 1u) >> 5)) {
+            uint32_t bits = keep[wd];
+            const uint32_t lo = wd << 5;  // first test of the word
+            if (b > lo) bits &= ~0u << (b - lo);
+            if (e - lo < 32u) bits &= (1u << (e - lo)) - 1u;
+            c += __popc(bits);
+          }
+        }
+        n = __reduce_add_sync(0xffffffffu, c);
+      }
+      count += n;
+      ty[(seg + 1) >> 1] += n;
+    }
+    if (!Fill && lane == 0) {
+      a.fcnt[u] = count;
+      auto sat = [](uint32_t v) { return v > 255u ? 255u : v; };
+      a.utypes[u] = sat(ty[0]) | (sat(ty[1]) << 8) | (sat(ty[2]) << 16) | (sat(ty[3]) << 24);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- learned part
 // MLP inputs of unit u (dem_learned.h): B's centre in A's body frame / (r_A + r_B),
 // q_A^-1 q_B (w >= 0), one-hot of the unordered shape pair (types mod 3), and
@@ -1799,8 +2067,36 @@ static FeatArgs make_fargs(dem_ctx* c, uint64_t nu) {
 int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total) {
   FeatArgs a = make_fargs(c, nu);
   const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
-  {
-    const bool mesh = !c->meshes.empty();
+  const bool mesh = !c->meshes.empty();
+  c->t_flat = nu && c->prm.fp32_broad_phase && !c->learned_slots;
+  if (c->t_flat) {  // flattened enumeration: prep, scan of the test counts, tests, per-unit counts
+    UnitRec* rec = reinterpret_cast<UnitRec*>(c->u_rec);
+    {
+      ProfScope ps(c, K_BROAD_COUNT, 1);
+      k_feat_prep<<<blocks, PT, 0, c->stream>>>(a, rec, c->t_cnt);
+    }
+    int rc = scan_exclusive_u32(c, c->t_cnt, c->t_off, 6 * nu);
+    if (rc) return rc;
+    uint32_t nt = 0;
+    DEM_CUDA_TRY(c, cudaMemcpyAsync(&nt, c->t_off + 6 * nu, 4, cudaMemcpyDeviceToHost, c->stream));
+    DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+    const uint64_t words = ((uint64_t)nt + 31) / 32;
+    if (words > c->t_keepcap) {
+      cudaFree(c->t_keep);
+      c->t_keep = nullptr;
+      c->t_keepcap = 0;
+      const uint64_t cap = words + words / 4 + 1024;
+      DEM_CUDA_TRY(c, cudaMalloc(&c->t_keep, cap * 4));
+      c->t_keepcap = cap;
+    }
+    ProfScope ps(c, K_BROAD_COUNT, (nt ? 2 : 1) + (mesh ? 1 : 0));
+    if (nt) {
+      const unsigned tb = (unsigned)std::min<uint64_t>((words * 32 + PT - 1) / PT, (uint64_t)c->num_sms * 32);
+      k_feat_test<<<tb, PT, 0, c->stream>>>(a, rec, c->t_off, nt, c->t_keep);
+    }
+    k_feat_collect<false><<<blocks, PT, 0, c->stream>>>(a, rec, c->t_off, c->t_keep);
+    if (mesh) k_mesh_units<false, true><<<blocks, PT, 0, c->stream>>>(a);
+  } else {
     ProfScope ps(c, K_BROAD_COUNT, nu ? (mesh ? 2 : 1) : 0);
     if (nu && c->prm.fp32_broad_phase)
       k_feat_dec<false><<<blocks, PT, 0, c->stream>>>(a);
@@ -1833,7 +2129,10 @@ int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
   const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
   const bool mesh = !c->meshes.empty();
   ProfScope ps(c, K_BROAD_FILL, mesh ? 4 : 2);
-  if (nu && c->prm.fp32_broad_phase)
+  if (nu && c->t_flat)
+    k_feat_collect<true><<<blocks, PT, 0, c->stream>>>(a, reinterpret_cast<const UnitRec*>(c->u_rec), c->t_off,
+                                                      c->t_keep);
+  else if (nu && c->prm.fp32_broad_phase)
     k_feat_dec<true><<<blocks, PT, 0, c->stream>>>(a);
   else if (nu)
     k_feat<true><<<blocks, PT, 0, c->stream>>>(a);
