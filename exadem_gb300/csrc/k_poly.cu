@@ -1185,7 +1185,7 @@ __device__ __forceinline__ void seg_masks(const UnitRec& q, int seg, uint64_t& r
   cols = seg == 0 ? (uint64_t)q.vB : (seg == 1 || seg == 5 ? eB : (seg == 3 ? (uint64_t)q.fB : (uint64_t)q.gB));
 }
 
-__global__ void __launch_bounds__(PT) k_feat_prep(FeatArgs a, UnitRec* __restrict__ rec, uint32_t* __restrict__ tcnt) {
+__global__ void __launch_bounds__(PT, 4) k_feat_prep(FeatArgs a, UnitRec* __restrict__ rec, uint32_t* __restrict__ tcnt) {
   const int lane = threadIdx.x & 31;
   const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
@@ -1291,7 +1291,7 @@ __device__ __forceinline__ uint32_t group_of(const uint32_t* __restrict__ off, u
   return lo;
 }
 
-__global__ void __launch_bounds__(PT) k_feat_test(FeatArgs a, const UnitRec* __restrict__ rec,
+__global__ void __launch_bounds__(PT, 8) k_feat_test(FeatArgs a, const UnitRec* __restrict__ rec,
                                                   const uint32_t* __restrict__ toff, uint32_t ntests,
                                                   uint32_t* __restrict__ keep) {
   const int lane = threadIdx.x & 31;
