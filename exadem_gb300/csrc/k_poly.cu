@@ -343,7 +343,6 @@ __device__ inline void for_each_unit(const UnitArgs& a, uint32_t s, Emit&& emit)
         for (uint32_t q = a.cell_start[cc]; q < a.cell_start[cc + 1]; q++) {
           const uint64_t idj = a.P.id[q];
           if (idi >= idj) continue;
-          if (bonded_to(a, s, idj)) continue;
           int keep = -1;
           if (a.f32) {
             const float xj = a.xr[q], yj = a.yr[q], zj = a.zr[q];
@@ -357,7 +356,9 @@ __device__ inline void for_each_unit(const UnitArgs& a, uint32_t s, Emit&& emit)
             const double rmax = radi + a.P.f[RAD][q] + a.rV;
             keep = (d2 > 0.0 && d2 < rmax * rmax && d2 < a.rcut2) ? 1 : 0;
           }
-          if (keep) emit(0u, q, idj);
+          // the bond list (the ignore list of inner_bond_interaction.hpp) only for
+          // the pairs in reach: the same units, fewer list walks
+          if (keep && !bonded_to(a, s, idj)) emit(0u, q, idj);
         }
       }
     }
@@ -481,8 +482,12 @@ __device__ __forceinline__ uint64_t skey(uint32_t type, uint32_t swap, uint32_t 
          (uint64_t)(psub & 0xfffffu);
 }
 
-__device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uint32_t partner, uint64_t pid,
-                              uint32_t type, uint32_t swap, uint32_t osub, uint32_t psub) {
+// The history of a new feature is searched in [hlo, hhi) of the previous list:
+// the owner's previous entries, or (the fill of one unit) the part of them with
+// the unit's partner id, which holds every entry the owner's range would match.
+__device__ void write_feature_in(const FeatArgs& a, uint32_t w, uint32_t owner, uint32_t partner, uint64_t pid,
+                                 uint32_t type, uint32_t swap, uint32_t osub, uint32_t psub, uint32_t hlo,
+                                 uint32_t hhi) {
   a.dst.owner[w] = owner;
   a.dst.partner[w] = partner;
   a.dst.pid[w] = pid;
@@ -491,8 +496,7 @@ __device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uin
   double h[6] = {0, 0, 0, 0, 0, 0};
   bool found = false;
   if (a.have_old) {
-    const uint32_t os = a.perm[owner];
-    uint32_t lo = a.old_off[os], hi = a.old_off[os + 1];
+    uint32_t lo = hlo, hi = hhi;
     const uint32_t oe = hi;
     const uint64_t sk = skey(type, swap, osub & 0xffffu, psub & 0xffffu);
     while (lo < hi) {
@@ -548,6 +552,17 @@ __device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uin
   a.dst.mo[0][w] = h[3];
   a.dst.mo[1][w] = h[4];
   a.dst.mo[2][w] = h[5];
+}
+
+__device__ void write_feature(const FeatArgs& a, uint32_t w, uint32_t owner, uint32_t partner, uint64_t pid,
+                              uint32_t type, uint32_t swap, uint32_t osub, uint32_t psub) {
+  uint32_t lo = 0, hi = 0;
+  if (a.have_old) {
+    const uint32_t os = a.perm[owner];
+    lo = a.old_off[os];
+    hi = a.old_off[os + 1];
+  }
+  write_feature_in(a, w, owner, partner, pid, type, swap, osub, psub, lo, hi);
 }
 
 // ---------------------------------------------------------------- split precision
@@ -1372,6 +1387,32 @@ __global__ void __launch_bounds__(PT) k_feat_collect(FeatArgs a, const UnitRec* 
       continue;
     }
     const UnitRec q = rec[u];
+    const uint32_t B = a.u_partner[u];
+    const uint64_t pid = a.u_pid[u];
+    uint32_t hlo = 0, hhi = 0;  // previous entries of the pair (owner A, partner id pid)
+    if (Fill && a.have_old) {
+      const uint32_t os = a.perm[A];
+      hlo = a.old_off[os];
+      hhi = a.old_off[os + 1];
+      uint32_t lo = hlo, hi = hhi;
+      while (lo < hi) {  // first entry with partner id >= pid
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a.old.pid[mid] < pid)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      hlo = lo;
+      hi = hhi;
+      while (lo < hi) {  // first entry with partner id > pid
+        const uint32_t mid = (lo + hi) >> 1;
+        if (a.old.pid[mid] <= pid)
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      hhi = lo;
+    }
     uint32_t count = 0, ty[4] = {0u, 0u, 0u, 0u};
     for (int seg = 0; seg < 6; seg++) {
       const uint64_t g = (uint64_t)seg * a.nu + u;
@@ -1387,8 +1428,8 @@ __global__ void __launch_bounds__(PT) k_feat_collect(FeatArgs a, const UnitRec* 
           const unsigned m = __ballot_sync(0xffffffffu, kp);
           if (kp) {
             const uint32_t loc = t - b, r = loc / nc;
-            write_feature(a, base + count + n + __popc(m & lt), A, a.u_partner[u], a.u_pid[u], seg_type(seg),
-                          seg_swap(seg), nth_bit64(rows, (int)r), nth_bit64(cols, (int)(loc - r * nc)));
+            write_feature_in(a, base + count + n + __popc(m & lt), A, B, pid, seg_type(seg), seg_swap(seg),
+                             nth_bit64(rows, (int)r), nth_bit64(cols, (int)(loc - r * nc)), hlo, hhi);
           }
           n += __popc(m);
         }
