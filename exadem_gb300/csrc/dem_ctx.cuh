@@ -314,6 +314,7 @@ int launch_contact_poly(dem_ctx* c);
 int launch_state_systems(dem_ctx* c, dem_state* out);  // one state per system
 void mlp_free(dem_ctx* c);
 int mlp_rates(dem_ctx* c, const float* dev_x, uint64_t n, float* dev_rates);
+int mlp_check(dem_ctx* c);
 bool mlp_ready(const dem_ctx* c);
 int launch_unit_features(dem_ctx* c, uint64_t nu);       // u_x of every unit
 int launch_learned_sizing(dem_ctx* c, uint64_t nu);      // rates -> records, bins (host sync)

@@ -2,11 +2,13 @@
 // candidate polyhedron pair, its number of vertex-vertex, vertex-edge,
 // vertex-face and edge-edge feature contacts.  No reference counterpart.
 //
-// Arithmetic: BF16 inputs and weights, FP32 accumulation.  The activation
-// products run on the tensor cores as warp-level mma.m16n8k16 (BF16 in, FP32
-// accumulate): a warp owns 16 samples; the FP32 result fragments of one layer
-// are, element for element, the A fragments of the next layer's product, so
-// the whole forward and backward chain of a 16-sample tile stays in registers.
+// Arithmetic: BF16 inputs and weights, FP32 accumulation.  Inference (the
+// rates a rebuild sizes its records with, dem_mlp_forward) runs on the
+// tcgen05 tensor cores with TMEM accumulators, 128 samples per CTA tile
+// (k_mlp_infer_tc).  Training keeps warp-level mma.m16n8k16 products: a warp
+// owns 16 gathered samples, the FP32 result fragments of one layer are, element
+// for element, the A fragments of the next layer's product, and the forward and
+// backward chain of a tile stays in registers.
 // Weight gradients are split-K reductions over the batch (FP32 FMA, fixed
 // order, deterministic), then Adam (FP32 master weights, BF16 copies).
 // Loss: Poisson with log link, rate = exp(z), loss = mean(exp(z) - y z).
@@ -129,28 +131,209 @@ __device__ __forceinline__ void forward_tile(const MlpWeights& w, const float* _
   z[3] = d[3] + w.b3[2 * t + 1];
 }
 
-// rates exp(z) of n samples; one warp per 16-sample tile
-__global__ void __launch_bounds__(128) k_mlp_infer(const MlpWeights* __restrict__ wg, const float* __restrict__ X,
-                                                    uint64_t n, float* __restrict__ rates) {
-  __shared__ MlpWeights w;
-  for (int i = threadIdx.x; i < (int)(sizeof(MlpWeights) / 4); i += blockDim.x)
-    reinterpret_cast<uint32_t*>(&w)[i] = reinterpret_cast<const uint32_t*>(wg)[i];
-  __syncthreads();
-  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t r0 = warp * 16; r0 < n; r0 += nwarps * 16) {
-    uint32_t ax[4];
-    Tile64 h1, h2;
-    float z[4];
-    forward_tile(w, X, r0, n, g, t, ax, h1, h2, z);
-    if (t < 2) {
+// ---- inference on the 5th-generation tensor cores (tcgen05, TMEM accumulators)
+// A CTA of 128 threads runs 128 samples per tile: each layer is one
+// tcgen05.mma (K = 16 per instruction, so 1 + 4 + 4 instructions) issued by one
+// thread, with the operands in shared memory in the canonical K-major layout
+// without swizzling (8 x 16-byte core matrices: 128 B each, K-neighbours 128 B
+// apart, 8-row groups K/8 x 128 B apart) and the FP32 accumulator in TMEM
+// (lane = sample, column = unit).  Completion is signalled by tcgen05.commit on
+// an mbarrier; each warp reads its 32 lanes back with tcgen05.ld, adds the bias,
+// applies ReLU and writes the BF16 activations as the next layer's A operand.
+// Same rounding points as the training pass (BF16 inputs, weights and
+// activations, FP32 accumulation and bias).
+constexpr int TC_M = 128;
+constexpr uint32_t TC_COLS = 128;  // TMEM columns: 0..63 layers 1-2, 64..79 layer 3
+
+struct alignas(1024) TcSmem {
+  __nv_bfloat16 x[TC_M * NIN];  // A, layer 1 (K = 16)
+  __nv_bfloat16 h[TC_M * NH];   // A, layers 2 and 3 (K = 64)
+  __nv_bfloat16 w1[NH * NIN];   // B, layer 1 (N = 64, K = 16)
+  __nv_bfloat16 w2[NH * NH];    // B, layer 2 (N = 64, K = 64)
+  __nv_bfloat16 w3[16 * NH];    // B, layer 3 (N = 16; rows 4..15 zero)
+  float b1[NH], b2[NH], b3[16];
+  uint64_t mbar;
+  uint32_t tmem;
+};
+
+// byte offset of element (row, k) of a K-major matrix with K columns
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k, int K) {
+  return (uint32_t)((row >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// shared-memory matrix descriptor: start, leading (K) byte offset, stride (8-row
+// group) byte offset, descriptor version 1, no swizzling
+__device__ __forceinline__ uint64_t sm_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);
+}
+// instruction descriptor, kind::f16: FP32 D, BF16 A and B, both K-major, M = 128
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// waits for phase `ph` of the mbarrier, at most about a second of SM clocks
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t ph) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(ph)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > (1ll << 31)) return false;
+  }
+}
+// 16 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const uint64_t r = r0 + g + 8 * (e >> 1);
-        if (r < n) rates[r * NOUT + 2 * t + (e & 1)] = expf(z[e]);
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+// this thread's row of a 64-unit layer: bias, ReLU, BF16 into h (K-major, K = 64)
+__device__ __forceinline__ void tc_hidden(TcSmem& S, uint32_t taddr, const float* b, int row) {
+  uint8_t* hb = reinterpret_cast<uint8_t*>(S.h);
+#pragma unroll
+  for (int c0 = 0; c0 < NH; c0 += 16) {
+    float v[16];
+    tmem_ld16(taddr + (uint32_t)c0, v);
+#pragma unroll
+    for (int q = 0; q < 16; q += 8) {
+      uint4 pk;
+      pk.x = pack_bf16(fmaxf(v[q] + b[c0 + q], 0.f), fmaxf(v[q + 1] + b[c0 + q + 1], 0.f));
+      pk.y = pack_bf16(fmaxf(v[q + 2] + b[c0 + q + 2], 0.f), fmaxf(v[q + 3] + b[c0 + q + 3], 0.f));
+      pk.z = pack_bf16(fmaxf(v[q + 4] + b[c0 + q + 4], 0.f), fmaxf(v[q + 5] + b[c0 + q + 5], 0.f));
+      pk.w = pack_bf16(fmaxf(v[q + 6] + b[c0 + q + 6], 0.f), fmaxf(v[q + 7] + b[c0 + q + 7], 0.f));
+      *reinterpret_cast<uint4*>(hb + kmajor_off(row, c0 + q, NH)) = pk;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(TC_M, 1) k_mlp_infer_tc(const MlpWeights* __restrict__ wg,
+                                                          const float* __restrict__ X, uint64_t n,
+                                                          float* __restrict__ rates, uint32_t* __restrict__ err) {
+  __shared__ TcSmem S;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // weights into the K-major layouts, biases; the mbarrier; TMEM
+  for (int i = tid; i < NH * NIN; i += TC_M) {
+    const int o = i / NIN, k = i % NIN;
+    *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<uint8_t*>(S.w1) + kmajor_off(o, k, NIN)) = wg->w1[i];
+  }
+  for (int i = tid; i < NH * NH; i += TC_M) {
+    const int o = i / NH, k = i % NH;
+    *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<uint8_t*>(S.w2) + kmajor_off(o, k, NH)) = wg->w2[i];
+  }
+  for (int i = tid; i < 16 * NH; i += TC_M) {
+    const int o = i / NH, k = i % NH;
+    *reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<uint8_t*>(S.w3) + kmajor_off(o, k, NH)) =
+        o < 8 ? wg->w3[i] : __float2bfloat16_rn(0.f);
+  }
+  for (int i = tid; i < NH; i += TC_M) {
+    S.b1[i] = wg->b1[i];
+    S.b2[i] = wg->b2[i];
+  }
+  if (tid < 16) S.b3[tid] = tid < 8 ? wg->b3[tid] : 0.f;
+  const uint32_t mbar = smem_u32(&S.mbar);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem)),
+                 "r"(TC_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem;
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;  // this warp's TMEM lanes
+  const uint32_t ax = smem_u32(S.x), ah = smem_u32(S.h);
+  const uint32_t bw1 = smem_u32(S.w1), bw2 = smem_u32(S.w2), bw3 = smem_u32(S.w3);
+  uint32_t ph = 0;
+  bool bad = false;
+  for (uint64_t r0 = (uint64_t)blockIdx.x * TC_M; r0 < n && !bad; r0 += (uint64_t)gridDim.x * TC_M) {
+    // this thread's sample: row tid of the tile
+    {
+      const uint64_t r = r0 + (uint64_t)tid;
+      uint8_t* xb = reinterpret_cast<uint8_t*>(S.x);
+#pragma unroll
+      for (int q = 0; q < NIN; q += 8) {
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) v[e] = r < n ? X[r * NIN + q + e] : 0.f;
+        uint4 pk;
+        pk.x = pack_bf16(v[0], v[1]);
+        pk.y = pack_bf16(v[2], v[3]);
+        pk.z = pack_bf16(v[4], v[5]);
+        pk.w = pack_bf16(v[6], v[7]);
+        *reinterpret_cast<uint4*>(xb + kmajor_off(tid, q, NIN)) = pk;
       }
     }
+    for (int layer = 0; layer < 3; layer++) {
+      fence_async_smem();
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      if (tid == 0) {
+        if (layer == 0) {
+          tc_mma(tmem, sm_desc(ax, 128, 256), sm_desc(bw1, 128, 256), tc_idesc(64), 0u);
+        } else {
+#pragma unroll
+          for (int s = 0; s < NH / 16; s++)
+            tc_mma(tmem + (layer == 2 ? 64u : 0u), sm_desc(ah + 256u * s, 128, 1024),
+                   sm_desc((layer == 1 ? bw2 : bw3) + 256u * s, 128, 1024), tc_idesc(layer == 1 ? 64 : 16),
+                   s ? 1u : 0u);
+        }
+        tc_commit(mbar);
+      }
+      const bool ok = mbar_wait(mbar, ph);
+      ph ^= 1u;
+      if (__syncthreads_or(!ok)) {
+        bad = true;
+        break;
+      }
+      tc_fence_after();
+      if (layer < 2) {
+        tc_hidden(S, tmem + lane_base, layer == 0 ? S.b1 : S.b2, tid);
+      } else {
+        float v[16];
+        tmem_ld16(tmem + lane_base + 64u, v);
+        const uint64_t r = r0 + (uint64_t)tid;
+        if (r < n) {
+#pragma unroll
+          for (int o = 0; o < NOUT; o++) rates[r * NOUT + o] = expf(v[o] + S.b3[o]);
+        }
+      }
+    }
+  }
+  if (bad && tid == 0) atomicOr(err, 1u);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_COLS) : "memory");
   }
 }
 
@@ -384,6 +567,7 @@ struct MlpState {
   float* part = nullptr;
   double* loss_part = nullptr;
   uint32_t* idx = nullptr;
+  uint32_t* err = nullptr;  // k_mlp_infer_tc: an mbarrier wait gave up
 };
 
 void mlp_free(dem_ctx* c) {
@@ -391,7 +575,7 @@ void mlp_free(dem_ctx* c) {
   if (!s) return;
   for (void* p : {(void*)s->master, (void*)s->m, (void*)s->v, (void*)s->grad, (void*)s->w, (void*)s->xb,
                   (void*)s->h1b, (void*)s->h2b, (void*)s->dh1b, (void*)s->dh2b, (void*)s->dzf, (void*)s->part,
-                  (void*)s->loss_part, (void*)s->idx})
+                  (void*)s->loss_part, (void*)s->idx, (void*)s->err})
     cudaFree(p);
   delete s;
   c->mlp = nullptr;
@@ -406,6 +590,8 @@ static int mlp_alloc(dem_ctx* c) {
   DEM_CUDA_TRY(c, cudaMalloc(&s->v, NPARAM * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&s->grad, NPARAM * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&s->w, sizeof(MlpWeights)));
+  DEM_CUDA_TRY(c, cudaMalloc(&s->err, 4));
+  DEM_CUDA_TRY(c, cudaMemsetAsync(s->err, 0, 4, c->stream));
   return DEM_OK;
 }
 
@@ -446,9 +632,20 @@ bool mlp_ready(const dem_ctx* c) { return c->mlp && c->mlp->ready; }
 int mlp_rates(dem_ctx* c, const float* dev_x, uint64_t n, float* dev_rates) {
   if (!c->mlp || !c->mlp->ready) return c->fail(DEM_ERR_STATE, "the MLP has no weights (dem_mlp_init / set_params)");
   if (!n) return DEM_OK;
-  const unsigned blocks = (unsigned)std::min<uint64_t>((n + 63) / 64, (uint64_t)c->num_sms * 16);
-  k_mlp_infer<<<blocks, 128, 0, c->stream>>>(c->mlp->w, dev_x, n, dev_rates);
+  // four CTAs of 128 TMEM columns fill an SM's 512
+  const unsigned blocks = (unsigned)std::min<uint64_t>((n + TC_M - 1) / TC_M, (uint64_t)c->num_sms * 4);
+  k_mlp_infer_tc<<<blocks, TC_M, 0, c->stream>>>(c->mlp->w, dev_x, n, dev_rates, c->mlp->err);
   DEM_CUDA_TRY(c, cudaGetLastError());
+  return DEM_OK;
+}
+
+// whether a tensor-core pass gave up waiting (reads the flag: synchronises the stream)
+int mlp_check(dem_ctx* c) {
+  if (!c->mlp) return DEM_OK;
+  uint32_t e = 0;
+  DEM_CUDA_TRY(c, cudaMemcpyAsync(&e, c->mlp->err, 4, cudaMemcpyDeviceToHost, c->stream));
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (e) return c->fail(DEM_ERR_CUDA, "tensor-core MLP pass: an mbarrier wait timed out");
   return DEM_OK;
 }
 
@@ -547,8 +744,7 @@ int dem_mlp_forward(dem_ctx* c, const float* dev_x, uint64_t n, float* dev_rates
   if (!c || (n && (!dev_x || !dev_rates))) return DEM_ERR_INVALID_ARG;
   int rc = mlp_rates(c, dev_x, n, dev_rates);
   if (rc) return rc;
-  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
-  return DEM_OK;
+  return mlp_check(c);
 }
 
 int dem_mlp_loss_grad(dem_ctx* c, const float* dev_x, const uint8_t* dev_y, uint64_t n, float* host_grad,

@@ -2211,7 +2211,7 @@ int launch_learned_sizing(dem_ctx* c, uint64_t nu) {
   uint32_t total = 0;
   DEM_CUDA_TRY(c, cudaMemcpyAsync(bins, d_bins, sizeof(bins), cudaMemcpyDeviceToHost, c->stream));
   DEM_CUDA_TRY(c, cudaMemcpyAsync(&total, c->u_slotoff + nu, 4, cudaMemcpyDeviceToHost, c->stream));
-  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if ((rc = mlp_check(c))) return rc;  // synchronises the stream
   if (total > c->slot_cap) {
     cudaFree(c->u_slots);
     c->u_slots = nullptr;
