@@ -316,8 +316,9 @@ void free_poly(dem_ctx* c) {
     cudaFree(c->vtx[d]);
     cudaFree(c->bvtx[d]);
     cudaFree(c->vrf[d]);
+    cudaFree(c->vwf[d]);
     c->vtx[d] = c->bvtx[d] = nullptr;
-    c->vrf[d] = nullptr;
+    c->vrf[d] = c->vwf[d] = nullptr;
   }
   cudaFree(c->pobb);
   cudaFree(c->pfbox);
@@ -344,6 +345,7 @@ int alloc_poly(dem_ctx* c) {
     DEM_CUDA_TRY(c, cudaMalloc(&c->vtx[d], need * 8));
     DEM_CUDA_TRY(c, cudaMalloc(&c->bvtx[d], need * 8));
     DEM_CUDA_TRY(c, cudaMalloc(&c->vrf[d], need * 4));
+    DEM_CUDA_TRY(c, cudaMalloc(&c->vwf[d], need * 4));
   }
   DEM_CUDA_TRY(c, cudaMalloc(&c->pobb, std::max<uint64_t>(c->pcap, 1) * 15 * 8));
   DEM_CUDA_TRY(c, cudaMalloc(&c->pfbox, std::max<uint64_t>(c->pcap, 1) * 32 * 4));

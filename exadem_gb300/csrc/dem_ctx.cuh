@@ -176,6 +176,7 @@ struct dem_ctx {
   double* bvtx[3] = {};               // vertices at the last rebuild
   double* pobb = nullptr;             // world OBB per particle (15 doubles)
   float* vrf[3] = {};                 // FP32 vertices relative to the particle centre (rebuild time)
+  float* vwf[3] = {};                 // FP32 roundings of the world vertices (every vertex computation)
   float* pfbox = nullptr;             // FP32 gate OBB + vertex slabs per particle (rebuild time)
   float4* pqb = nullptr;              // FP32 orientation backup (w, x, y, z) at the last rebuild
   uint32_t* vneed = nullptr;          // 1 for particles whose vertices the interaction list uses (n+1)

@@ -49,6 +49,9 @@ struct PolyArgs {
   float* fz;
   float* fbox;  // FBOX_STRIDE per particle: FP32 gate OBB and vertex slabs (rebuild time)
   float4* qb;   // FP32 orientation at the last rebuild
+  float* wx;    // FP32 roundings of the world vertices (written with vx, vy, vz)
+  float* wy;
+  float* wz;
   double rV;
 };
 
@@ -68,6 +71,9 @@ __global__ void k_poly_vertices(PolyArgs a, double thr2, unsigned long long* fla
       a.vx[idx] = v.x;
       a.vy[idx] = v.y;
       a.vz[idx] = v.z;
+      a.wx[idx] = (float)v.x;
+      a.wy[idx] = (float)v.y;
+      a.wz[idx] = (float)v.z;
       if (Displ) {
         const V3 dr = v - mk(a.bx[idx], a.by[idx], a.bz[idx]);
         over |= dot(dr, dr) >= thr2;
@@ -200,6 +206,9 @@ __global__ void k_poly_vertices_listed(PolyArgs a, const uint32_t* __restrict__ 
   a.vx[idx] = v.x;
   a.vy[idx] = v.y;
   a.vz[idx] = v.z;
+  a.wx[idx] = (float)v.x;
+  a.wy[idx] = (float)v.y;
+  a.wz[idx] = (float)v.z;
 }
 
 // marks the particles whose vertices the interaction list uses: both sides of the
@@ -1668,6 +1677,10 @@ struct PCArgs {
   const double* vx;
   const double* vy;
   const double* vz;
+  const float* wx;  // FP32 roundings of the world vertices (contact screen)
+  const float* wy;
+  const float* wz;
+  int screen;       // FP32 contact screen of the particle pairs (fused step, no cohesion, no analysis)
   dem_contact_params cp, cpd;
   double dt;
   int cohesive;
@@ -1784,7 +1797,27 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
       const ShapeDev& sj = a.shapes[a.P.type[R.jp]];
       const double rim = si.r * a.P.f[HOM][R.ip], rjm = sj.r * a.P.f[HOM][R.jp];
       const VView vi = pview(a, R.ip), vj = pview(a, R.jp);
-      switch (type) {
+      bool apart = false;
+      if (a.screen) {  // FP32 screen: a pair provably apart skips the FP64 detection
+        const uint64_t oi = (uint64_t)R.ip * a.MV, oj = (uint64_t)R.jp * a.MV;
+        auto wi = [&](int q) { return f3(a.wx[oi + q], a.wy[oi + q], a.wz[oi + q]); };
+        auto wj = [&](int q) { return f3(a.wx[oj + q], a.wy[oj + q], a.wz[oj + q]); };
+        const float Rf = (float)(rim + rjm) * 1.000001f;
+        if (type == DEM_ITYPE_VERTEX_VERTEX) {
+          apart = apart_vv(wi(R.sub_i), wj(R.sub_j), Rf);
+        } else if (type == DEM_ITYPE_VERTEX_EDGE) {
+          apart = apart_ve(wi(R.sub_i), wj(sj.e[2 * R.sub_j]), wj(sj.e[2 * R.sub_j + 1]), Rf);
+        } else if (type == DEM_ITYPE_VERTEX_FACE) {
+          const int b = sj.fo[R.sub_j], e = sj.fo[R.sub_j + 1];
+          apart = apart_vf(wi(R.sub_i), wj(sj.fv[b]), wj(sj.fv[b + 1]), wj(sj.fv[e - 1]), Rf);
+        } else {
+          apart = apart_ee(wi(si.e[2 * R.sub_i]), wi(si.e[2 * R.sub_i + 1]), wj(sj.e[2 * R.sub_j]),
+                           wj(sj.e[2 * R.sub_j + 1]), Rf);
+        }
+      }
+      switch (apart ? ~0u : type) {
+        case ~0u:  // no contact: det_none
+          break;
         case DEM_ITYPE_VERTEX_VERTEX:
           d = detect_vv(vi[R.sub_i], rim, vj[R.sub_j], rjm);
           break;
@@ -1953,6 +1986,9 @@ PolyArgs make_pargs(dem_ctx* c) {
   a.fz = c->vrf[2];
   a.fbox = c->pfbox;
   a.qb = c->pqb;
+  a.wx = c->vwf[0];
+  a.wy = c->vwf[1];
+  a.wz = c->vwf[2];
   a.rV = c->prm.rcut_inc;
   return a;
 }
@@ -2269,11 +2305,15 @@ int launch_contact_poly(dem_ctx* c) {
   a.vx = c->vtx[0];
   a.vy = c->vtx[1];
   a.vz = c->vtx[2];
+  a.wx = c->vwf[0];
+  a.wy = c->vwf[1];
+  a.wz = c->vwf[2];
   a.cp = c->prm.config;
   a.cpd = c->prm.config_driver;
   a.dt = c->prm.dt;
   a.cohesive = c->prm.law == DEM_LAW_HOOKE_COHESIVE;
   a.dmt = c->prm.law == DEM_LAW_HOOKE_DMT;
+  a.screen = c->prm.fused_step && c->prm.fp32_contact_screen && !a.cohesive && !a.dmt && !c->cs.dn;
   a.pt = c->ptable();
   a.cs = c->cs;
   a.mesh = c->mesh_dev;

@@ -401,4 +401,69 @@ __device__ inline int decide_ee(F3 vfi, F3 vsi, F3 vfj, F3 vsj, float R, float S
   return cn < 0 ? DEC_TRUE : (cn > 0 ? DEC_FALSE : DEC_UNDECIDED);
 }
 
+// ---- contact screen of the polyhedron contact law (k_pdetect)
+// Inputs are FP32 roundings of the FP64 world vertices (error u |x| per
+// coordinate).  With W a bound of every |coordinate| involved, a difference of
+// two inputs carries at most 3 u W per coordinate, so its norm at most
+// ETA = 6 u W.  Each test returns true only when the FP64 detection
+// (shape_detection_core.hpp: detection_vertex_vertex / _edge / _face,
+// detection_edge_edge) provably finds no contact: a lower bound of the distance
+// that a contact needs below R (the sum of the Minkowski radii) exceeds R by
+// 8x its error bound.  Otherwise the FP64 detection runs.
+__device__ __forceinline__ float fmaxabs(F3 a) { return fmaxf(fabsf(a.x), fmaxf(fabsf(a.y), fabsf(a.z))); }
+
+// vertex-vertex: a contact needs |pi - pj| < R
+__device__ inline bool apart_vv(F3 a, F3 b, float R) {
+  const float eta = 6.f * F32_U * fmaxf(fmaxabs(a), fmaxabs(b));
+  const float d = flen(a - b);
+  return d > R + 8.f * (eta + 4.f * F32_U * (d + R));
+}
+// vertex-edge: a contact needs the projection parameter in (0, 1) and the
+// distance to the line at most R, so the point-segment distance at most R.  The
+// clamped distance min_t |w - e t| moves by at most |dw| + |de| under input
+// errors; the FP32 projection parameter is off the minimiser by at most
+// 8u (|w| + |e|) / |e|, which adds at most 8u (|w| + |e|)
+__device__ inline bool apart_ve(F3 p, F3 a, F3 b, float R) {
+  const float eta = 6.f * F32_U * fmaxf(fmaxabs(p), fmaxf(fmaxabs(a), fmaxabs(b)));
+  const F3 e = b - a, w = p - a;
+  const float ee = fdot(e, e);
+  if (!(ee > 0.f)) return false;
+  const float t = fminf(fmaxf(fdot(w, e) / ee, 0.f), 1.f);
+  const float d = flen(w - e * t);
+  const float err = 2.f * eta + 8.f * F32_U * (flen(w) + sqrtf(ee)) + 4.f * F32_U * (d + R);
+  return d > R + 8.f * err;
+}
+// vertex-face: a contact needs the distance to the plane through va with normal
+// (vb - va) x (vc - va) (vf_core's frame: first, second and last face vertex)
+// at most R.  The unit normal's error is at most 4 ETA L / |c| (L the longer of
+// the two edges, c their cross product); faces with |c| <= 1e-3 L^2 are not
+// screened
+__device__ inline bool apart_vf(F3 p, F3 va, F3 vb, F3 vc, float R) {
+  const float eta = 6.f * F32_U * fmaxf(fmaxf(fmaxabs(p), fmaxabs(va)), fmaxf(fmaxabs(vb), fmaxabs(vc)));
+  const F3 e1 = vb - va, e2 = vc - va, w = p - va;
+  const F3 c = fcross(e1, e2);
+  const float cl = flen(c), L = fmaxf(flen(e1), flen(e2));
+  if (!(cl > 1e-3f * L * L)) return false;
+  const float dist = fabsf(fdot(c, w)) / cl;
+  const float W = flen(w);
+  const float err = 4.f * eta * L * W / cl + eta + 8.f * F32_U * (W + dist + R);
+  return dist > R + 8.f * err;
+}
+// edge-edge: a contact needs non-parallel edges, the closest points of the two
+// lines inside both edges and their distance at most R, so the distance of the
+// two lines, |v . c| / |c| with c = Ei x Ej, at most R.  Pairs with
+// |c| <= 0.05 |Ei| |Ej| are not screened
+__device__ inline bool apart_ee(F3 a0, F3 a1, F3 b0, F3 b1, float R) {
+  const float eta =
+      6.f * F32_U * fmaxf(fmaxf(fmaxabs(a0), fmaxabs(a1)), fmaxf(fmaxabs(b0), fmaxabs(b1)));
+  const F3 Ei = a1 - a0, Ej = b1 - b0, v = a0 - b0;
+  const F3 c = fcross(Ei, Ej);
+  const float Li = flen(Ei), Lj = flen(Ej), cl = flen(c), V = flen(v);
+  if (!(cl > 0.05f * Li * Lj)) return false;
+  const float D = fabsf(fdot(v, c)) / cl;
+  const float dc = eta * (Li + Lj) + 4.f * F32_U * Li * Lj;  // bound of |c - c_exact|
+  const float err = eta + (V + D) * dc / cl + 8.f * F32_U * (V + D + R);
+  return D > R + 8.f * err;
+}
+
 }  // namespace dem
