@@ -203,7 +203,8 @@ struct dem_ctx {
   uint64_t nu_last = 0;               // units of the last polyhedron rebuild
   bool labels_valid = false;          // u_types holds the last rebuild's exact counts
   uint32_t* u_rec = nullptr;          // flattened enumeration: 16 words (masks, dR, S, R) per unit (ucap)
-  uint32_t* t_cnt = nullptr;          // tests per (segment, unit), segment-major (6 ucap + 1)
+  uint32_t* t_cnt = nullptr;          // tests per (segment, unit), segment-major (6 ucap + 1); then kept tests
+  uint32_t t_ntests = 0;              // tests of the last flattened count pass
   uint32_t* t_off = nullptr;          // their offsets (6 ucap + 1)
   uint32_t* t_keep = nullptr;         // kept bit per test (t_keepcap words)
   uint64_t t_keepcap = 0;

@@ -1371,10 +1371,12 @@ __global__ void __launch_bounds__(PT, 8) k_feat_test(FeatArgs a, const UnitRec* 
   }
 }
 
+// Fill = false: counts per unit (fcnt, utypes) and per (segment, unit) group (kc);
+// Fill = true: the driver units' features (the pairs' come from k_feat_fill_flat)
 template <bool Fill>
 __global__ void __launch_bounds__(PT) k_feat_collect(FeatArgs a, const UnitRec* __restrict__ rec,
                                                      const uint32_t* __restrict__ toff,
-                                                     const uint32_t* __restrict__ keep) {
+                                                     const uint32_t* __restrict__ keep, uint32_t* __restrict__ kc) {
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
   const uint64_t warp = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5;
@@ -1395,6 +1397,7 @@ __global__ void __launch_bounds__(PT) k_feat_collect(FeatArgs a, const UnitRec* 
       if (!Fill && lane == 0) a.utypes[u] = 0u;
       continue;
     }
+    if (Fill) continue;  // pair units: k_feat_fill_flat
     const UnitRec q = rec[u];
     const uint32_t B = a.u_partner[u];
     const uint64_t pid = a.u_pid[u];
@@ -1455,6 +1458,7 @@ __global__ void __launch_bounds__(PT) k_feat_collect(FeatArgs a, const UnitRec* 
           }
         }
         n = __reduce_add_sync(0xffffffffu, c);
+        if (lane == 0) kc[g] = n;
       }
       count += n;
       ty[(seg + 1) >> 1] += n;
@@ -1464,6 +1468,47 @@ __global__ void __launch_bounds__(PT) k_feat_collect(FeatArgs a, const UnitRec* 
       auto sat = [](uint32_t v) { return v > 255u ? 255u : v; };
       a.utypes[u] = sat(ty[0]) | (sat(ty[1]) << 8) | (sat(ty[2]) << 16) | (sat(ty[3]) << 24);
     }
+  }
+}
+
+// The fill of the pair units: one thread per test, 32 tests per warp; a kept
+// test goes to foff[u] + the kept tests of u's earlier segments + the kept
+// tests before it in its (segment, unit) group, which is k_feat's order.
+__global__ void __launch_bounds__(PT) k_feat_fill_flat(FeatArgs a, const UnitRec* __restrict__ rec,
+                                                       const uint32_t* __restrict__ toff, uint32_t ntests,
+                                                       const uint32_t* __restrict__ keep,
+                                                       const uint32_t* __restrict__ kc) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t ng = (uint32_t)(6 * a.nu);
+  const uint32_t nu = (uint32_t)a.nu;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * PT) >> 5;
+  for (uint64_t w = ((uint64_t)blockIdx.x * PT + threadIdx.x) >> 5; w * 32 < ntests; w += nwarps) {
+    const uint32_t bits = keep[w];
+    if (!bits) continue;
+    const uint32_t T = (uint32_t)(w * 32) + (uint32_t)lane;
+    if (!((bits >> lane) & 1u)) continue;
+    const uint32_t g = group_of(toff, 0u, ng - 1u, T);
+    const int seg = (int)(g / nu);
+    const uint32_t u = g - (uint32_t)seg * nu;
+    const uint32_t b = toff[g];
+    // kept tests of the group before T
+    uint32_t before = 0;
+    for (uint32_t wd = b >> 5; wd <= (T >> 5); wd++) {
+      uint32_t m = keep[wd];
+      const uint32_t lo = wd << 5;
+      if (b > lo) m &= ~0u << (b - lo);
+      if (T - lo < 32u) m &= (1u << (T - lo)) - 1u;
+      before += __popc(m);
+    }
+    uint32_t pos = a.foff[u] + before;
+    for (int s2 = 0; s2 < seg; s2++) pos += kc[(uint64_t)s2 * a.nu + u];
+    const UnitRec q = rec[u];
+    uint64_t rows, cols;
+    seg_masks(q, seg, rows, cols);
+    const uint32_t nc = (uint32_t)__popcll(cols);
+    const uint32_t loc = T - b, r = loc / nc;
+    write_feature(a, pos, a.u_owner[u], a.u_partner[u], a.u_pid[u], seg_type(seg), seg_swap(seg),
+                  nth_bit64(rows, (int)r), nth_bit64(cols, (int)(loc - r * nc)));
   }
 }
 
@@ -2171,7 +2216,8 @@ int launch_poly_feature_count(dem_ctx* c, uint64_t nu, uint32_t* total) {
       const unsigned tb = (unsigned)std::min<uint64_t>((words * 32 + PT - 1) / PT, (uint64_t)c->num_sms * 32);
       k_feat_test<<<tb, PT, 0, c->stream>>>(a, rec, c->t_off, nt, c->t_keep);
     }
-    k_feat_collect<false><<<blocks, PT, 0, c->stream>>>(a, rec, c->t_off, c->t_keep);
+    k_feat_collect<false><<<blocks, PT, 0, c->stream>>>(a, rec, c->t_off, c->t_keep, c->t_cnt);
+    c->t_ntests = nt;
     if (mesh) k_mesh_units<false, true><<<blocks, PT, 0, c->stream>>>(a);
   } else {
     ProfScope ps(c, K_BROAD_COUNT, nu ? (mesh ? 2 : 1) : 0);
@@ -2206,9 +2252,15 @@ int launch_poly_feature_fill(dem_ctx* c, uint64_t nu) {
   const unsigned blocks = (unsigned)std::min<uint64_t>((nu * 32 + PT - 1) / PT + 1, (uint64_t)c->num_sms * 16);
   const bool mesh = !c->meshes.empty();
   ProfScope ps(c, K_BROAD_FILL, mesh ? 4 : 2);
-  if (nu && c->t_flat)
-    k_feat_collect<true><<<blocks, PT, 0, c->stream>>>(a, reinterpret_cast<const UnitRec*>(c->u_rec), c->t_off,
-                                                      c->t_keep);
+  if (nu && c->t_flat) {
+    const UnitRec* rec = reinterpret_cast<const UnitRec*>(c->u_rec);
+    if (c->ndrv) k_feat_collect<true><<<blocks, PT, 0, c->stream>>>(a, rec, c->t_off, c->t_keep, nullptr);
+    const uint32_t nt = c->t_ntests;
+    if (nt) {
+      const unsigned tb = (unsigned)std::min<uint64_t>(((uint64_t)nt + PT - 1) / PT, (uint64_t)c->num_sms * 32);
+      k_feat_fill_flat<<<tb, PT, 0, c->stream>>>(a, rec, c->t_off, nt, c->t_keep, c->t_cnt);
+    }
+  }
   else if (nu && c->prm.fp32_broad_phase)
     k_feat_dec<true><<<blocks, PT, 0, c->stream>>>(a);
   else if (nu)
