@@ -327,6 +327,8 @@ void free_poly(dem_ctx* c) {
   cudaFree(c->vneed_off);
   cudaFree(c->vlist);
   cudaFree(c->u_off);
+  cudaFree(c->urec);
+  c->urec = nullptr;
   c->pobb = nullptr;
   c->pfbox = nullptr;
   c->pqb = nullptr;
@@ -348,6 +350,7 @@ int alloc_poly(dem_ctx* c) {
     DEM_CUDA_TRY(c, cudaMalloc(&c->vwf[d], need * 4));
   }
   DEM_CUDA_TRY(c, cudaMalloc(&c->pobb, std::max<uint64_t>(c->pcap, 1) * 15 * 8));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->urec, std::max<uint64_t>(c->pcap, 1) * 16 * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->pfbox, std::max<uint64_t>(c->pcap, 1) * 32 * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->pqb, std::max<uint64_t>(c->pcap, 1) * sizeof(float4)));
   DEM_CUDA_TRY(c, cudaMalloc(&c->vneed, (std::max<uint64_t>(c->pcap, 1) + 1) * 4));

@@ -185,6 +185,7 @@ struct dem_ctx {
   uint64_t nvlist = 0;
   uint64_t vcap = 0;
   uint32_t* u_off = nullptr;          // n+1 unit offsets per owner
+  uint32_t* urec = nullptr;           // 16 units per owner recorded by the unit count pass
   uint32_t* u_owner = nullptr;        // unit arrays (ucap each)
   uint32_t* u_partner = nullptr;
   uint64_t* u_pid = nullptr;

@@ -261,7 +261,11 @@ struct UnitArgs {
   const uint32_t* b_first;
   const uint32_t* b_cnt;
   const uint64_t* b_idj;
+  // the count pass's units of each particle (UREC per particle: kind << 31 |
+  // partner), read by the fill when they fit
+  uint32_t* urec;
 };
+constexpr uint32_t UREC = 16;
 
 __device__ __forceinline__ bool bonded_to(const UnitArgs& a, uint32_t s, uint64_t id) {
   if (!a.b_cnt) return false;
@@ -378,7 +382,11 @@ __global__ void k_unit_count(UnitArgs a, uint32_t* __restrict__ cnt) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
   uint32_t m = 0;
-  for_each_unit(a, (uint32_t)s, [&](uint32_t, uint32_t, uint64_t) { m++; });
+  uint32_t* rec = a.urec + s * UREC;
+  for_each_unit(a, (uint32_t)s, [&](uint32_t kind, uint32_t partner, uint64_t) {
+    if (m < UREC) rec[m] = (kind << 31) | partner;
+    m++;
+  });
   cnt[s] = m;
 }
 
@@ -388,16 +396,27 @@ __global__ void k_unit_fill(UnitArgs a, const uint32_t* __restrict__ off, uint32
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= a.n) return;
   const uint32_t b = off[s], e = off[s + 1];
-  uint32_t w = b;
-  for_each_unit(a, (uint32_t)s, [&](uint32_t kind, uint32_t partner, uint64_t pid) {
-    if (w < e) {
-      u_owner[w] = (uint32_t)s;
-      u_partner[w] = partner;
-      u_pid[w] = pid;
-      u_kind[w] = kind;
+  if (e - b <= UREC) {  // the count pass recorded them
+    const uint32_t* rec = a.urec + s * UREC;
+    for (uint32_t x = b; x < e; x++) {
+      const uint32_t r = rec[x - b], kind = r >> 31, partner = r & 0x7fffffffu;
+      u_owner[x] = (uint32_t)s;
+      u_partner[x] = partner;
+      u_pid[x] = kind ? (uint64_t)partner : a.P.id[partner];
+      u_kind[x] = kind;
     }
-    w++;
-  });
+  } else {
+    uint32_t w = b;
+    for_each_unit(a, (uint32_t)s, [&](uint32_t kind, uint32_t partner, uint64_t pid) {
+      if (w < e) {
+        u_owner[w] = (uint32_t)s;
+        u_partner[w] = partner;
+        u_pid[w] = pid;
+        u_kind[w] = kind;
+      }
+      w++;
+    });
+  }
   // (partner id, kind): particle features (types 0-3) before driver features (types 4-5)
   for (uint32_t x = b + 1; x < e; x++) {
     const uint64_t pk = u_pid[x];
@@ -2125,6 +2144,7 @@ int launch_poly_units(dem_ctx* c, uint64_t* nu_out, int (*grow_units)(dem_ctx*, 
   a.b_first = c->nb ? c->b_own_first : nullptr;
   a.b_cnt = c->nb ? c->b_own_cnt : nullptr;
   a.b_idj = c->nb ? c->B[c->bcur].id_j : nullptr;
+  a.urec = c->urec;
   {
     ProfScope ps(c, K_BROAD_COUNT, 1);
     k_unit_count<<<grid_for(c->n, PT), PT, 0, c->stream>>>(a, c->pcnt);
