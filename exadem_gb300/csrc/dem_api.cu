@@ -76,6 +76,7 @@ int alloc_particles(dem_ctx* c, uint64_t n) {
   cudaFree(c->cell_tmp);
   cudaFree(c->perm);
   cudaFree(c->pcnt);
+  cudaFree(c->srec);
   cudaFree(c->rev_off);
   cudaFree(c->rev_cnt);
   cudaFree(c->own_off[0]);
@@ -84,6 +85,7 @@ int alloc_particles(dem_ctx* c, uint64_t n) {
   DEM_CUDA_TRY(c, cudaMalloc(&c->cell_tmp, cap * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->perm, cap * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->pcnt, (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->srec, cap * 16 * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->rev_off, (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->rev_cnt, (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->own_off[0], (cap + 1) * 4));
@@ -664,6 +666,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   cudaFree(c->cell_of);
   cudaFree(c->cell_tmp);
   cudaFree(c->perm);
+  cudaFree(c->srec);
   cudaFree(c->pcnt);
   for (int q = 0; q < 4; q++) cudaFree(c->crel[q]);
   cudaFree(c->rot_list);

@@ -116,6 +116,7 @@ struct dem_ctx {
   uint32_t* cell_tmp = nullptr;    // n, cell of each particle in the old order
   uint32_t* perm = nullptr;        // n, new slot -> old slot
   uint32_t* pcnt = nullptr;        // n+1 candidate counts (then offsets)
+  uint32_t* srec = nullptr;        // spheres: 8 (partner, meta) candidates per particle from the count pass
   float* crel[4] = {};             // n each: cell-relative x, y, z and radius in FP32 (broad phase)
 
   // interactions (double-buffered for the history carry-over)

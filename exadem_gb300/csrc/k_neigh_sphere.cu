@@ -46,6 +46,9 @@ struct BPArgs {
   const float* rf;
   float skin_f;
   uint64_t cap;  // interaction buffer capacity (graph step): a fill beyond it writes nothing
+  // FP32 path: the count pass's candidates of each particle (SREC per particle:
+  // partner, meta), read by the fill when they fit
+  uint32_t* srec;
   // per-pair damping damp_rate 2 sqrt(kn meff), in the operation order of the
   // contact law: (damp_rate * 2) * sqrt(kn * meff), meff = (m_i m_j)/(m_i + m_j)
   // for particle pairs, m_i for drivers; the pair's parameter set
@@ -293,6 +296,8 @@ __global__ void k_mesh_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays 
   mesh_phase<F32, true>(a, s, (threadIdx.x & 31) == 0 && trig, b, e, dst);
 }
 
+constexpr uint32_t SREC = 8;
+
 template <bool F32>
 __global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ old_off) {
   const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -301,8 +306,16 @@ __global__ void k_count(BPArgs a, uint32_t* __restrict__ cnt, const uint32_t* __
     cnt[s] = old_off[s + 1] - old_off[s];
     return;
   }
-  uint32_t m = a.has_mesh ? a.mcnt[s] : 0u;
-  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t, uint64_t, uint32_t, uint32_t) { m++; });
+  const uint32_t m0 = a.has_mesh ? a.mcnt[s] : 0u;
+  uint32_t m = m0;
+  uint32_t* rec = F32 ? a.srec + s * (2 * SREC) : nullptr;
+  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t, uint32_t meta, uint32_t) {
+    if (F32 && m - m0 < SREC) {
+      rec[2 * (m - m0)] = q;
+      rec[2 * (m - m0) + 1] = meta;
+    }
+    m++;
+  });
   cnt[s] = m;
 }
 
@@ -407,15 +420,26 @@ __global__ void k_fill(BPArgs a, const uint32_t* __restrict__ off, IArrays dst, 
     return;
   }
   uint32_t w = b + (a.has_mesh ? a.mcnt[s] : 0u);  // mesh items first (k_mesh_fill)
-  for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta, uint32_t sub) {
-    if (w < e) {
-      dst.partner[w] = q;
-      dst.pid[w] = pid;
-      dst.meta[w] = meta;
-      dst.sub[w] = sub;
+  if (F32 && e - w <= SREC) {  // the count pass recorded the drivers and particles
+    const uint32_t* rec = a.srec + s * (2 * SREC);
+    for (uint32_t x = w; x < e; x++) {
+      const uint32_t q = rec[2 * (x - w)], meta = rec[2 * (x - w) + 1];
+      dst.partner[x] = q;
+      dst.pid[x] = meta_type(meta) == DEM_ITYPE_VERTEX_VERTEX ? a.P.id[q] : (uint64_t)q;
+      dst.meta[x] = meta;
+      dst.sub[x] = 0u;
     }
-    w++;
-  });
+  } else {
+    for_each_candidate<F32>(a, (uint32_t)s, [&](uint32_t q, uint64_t pid, uint32_t meta, uint32_t sub) {
+      if (w < e) {
+        dst.partner[w] = q;
+        dst.pid[w] = pid;
+        dst.meta[w] = meta;
+        dst.sub[w] = sub;
+      }
+      w++;
+    });
+  }
   finish_owner(a, (uint32_t)s, b, e, dst, old, old_off, perm, have_old, reuse_damp);
 }
 
@@ -790,6 +814,7 @@ BPArgs make_args(dem_ctx* c) {
   a.rf = c->crel[3];
   a.skin_f = (float)c->prm.rcut_inc;
   a.cap = c->capturing ? c->gcap : ~0ull;
+  a.srec = c->srec;
   a.cp = c->prm.config;
   a.cpd = c->prm.config_driver;
   a.pt = c->ptable();
