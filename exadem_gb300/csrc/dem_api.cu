@@ -79,6 +79,7 @@ int alloc_particles(dem_ctx* c, uint64_t n) {
   cudaFree(c->srec);
   cudaFree(c->rev_off);
   cudaFree(c->rev_cnt);
+  cudaFree(c->rev_nlong);
   cudaFree(c->own_off[0]);
   cudaFree(c->own_off[1]);
   DEM_CUDA_TRY(c, cudaMalloc(&c->cell_of, cap * 4));
@@ -88,6 +89,7 @@ int alloc_particles(dem_ctx* c, uint64_t n) {
   DEM_CUDA_TRY(c, cudaMalloc(&c->srec, cap * 16 * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->rev_off, (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->rev_cnt, (cap + 1) * 4));
+  DEM_CUDA_TRY(c, cudaMalloc(&c->rev_nlong, sizeof(unsigned int)));
   DEM_CUDA_TRY(c, cudaMalloc(&c->own_off[0], (cap + 1) * 4));
   DEM_CUDA_TRY(c, cudaMalloc(&c->own_off[1], (cap + 1) * 4));
   for (int q = 0; q < 4; q++) {
@@ -660,6 +662,7 @@ int dem_ctx_destroy(dem_ctx* c) {
   free_bonds(c);
   cudaFree(c->shapes_dev);
   cudaFree(c->rev_off);
+  cudaFree(c->rev_nlong);
   cudaFree(c->rev_cnt);
   cudaFree(c->cell_cnt);
   cudaFree(c->cell_start);

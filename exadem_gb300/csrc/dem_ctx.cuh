@@ -131,6 +131,7 @@ struct dem_ctx {
   dem::Records R{};
   uint32_t* rev_off = nullptr;  // n+1
   uint32_t* rev_cnt = nullptr;  // n+1
+  unsigned int* rev_nlong = nullptr;  // reverse lists too long for a thread (k_rev_short -> k_rev_rank)
   uint32_t* rev_idx = nullptr;  // rcap
   // compacted contact passes (rcap each): work lists and detection results
   uint32_t* L1 = nullptr;

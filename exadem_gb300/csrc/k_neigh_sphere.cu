@@ -755,18 +755,48 @@ __global__ void k_rev_fill(IArrays I, uint64_t ni, const unsigned long long* ni_
   }
 }
 // order of the partner-side contributions: InteractionPair order = (owner id, index).
-// One warp per particle: the entries of its reverse list, filled in any order
-// into `unsorted`, go to idx at their rank, the number of entries of the list
-// with a smaller (owner id, index) key (keys are distinct: the index is).
-// Lanes hold 32 entries at a time and count against every chunk of 32 of the
-// list broadcast by shuffles.
-__global__ void __launch_bounds__(256) k_rev_rank(uint64_t n, const uint32_t* __restrict__ off,
+// A list of at most REV_SHORT entries (spheres: a few) is copied from `unsorted`
+// and insertion-sorted by its particle's thread; a longer one (polyhedra: tens)
+// is queued in `longs` for k_rev_rank.
+constexpr uint32_t REV_SHORT = 12;
+__global__ void k_rev_short(uint64_t n, const uint32_t* __restrict__ off, const uint32_t* __restrict__ owner,
+                            const uint64_t* __restrict__ id, const uint32_t* __restrict__ unsorted,
+                            uint32_t* __restrict__ idx, uint32_t* __restrict__ longs, unsigned int* __restrict__ nlong) {
+  const uint64_t s = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= n) return;
+  const uint32_t b = off[s], e = off[s + 1];
+  if (e - b > REV_SHORT) {
+    longs[atomicAdd(nlong, 1u)] = (uint32_t)s;
+    return;
+  }
+  for (uint32_t x = b; x < e; x++) {
+    const uint32_t k = unsorted[x];
+    const uint64_t ok = id[owner[k]];
+    uint32_t y = x;
+    while (y > b) {
+      const uint32_t kp = idx[y - 1];
+      const uint64_t op = id[owner[kp]];
+      if (op < ok || (op == ok && kp < k)) break;
+      idx[y] = kp;
+      y--;
+    }
+    idx[y] = k;
+  }
+}
+// One warp per queued particle: the entries of its reverse list go to idx at
+// their rank, the number of entries of the list with a smaller (owner id,
+// index) key (keys are distinct: the index is).  Lanes hold 32 entries at a time
+// and count against every chunk of 32 of the list broadcast by shuffles.
+__global__ void __launch_bounds__(256) k_rev_rank(const unsigned int* __restrict__ nlong,
+                                                  const uint32_t* __restrict__ longs, const uint32_t* __restrict__ off,
                                                   const uint32_t* __restrict__ owner,
                                                   const uint64_t* __restrict__ id,
                                                   const uint32_t* __restrict__ unsorted, uint32_t* __restrict__ idx) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint64_t nw = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t s = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < n; s += nw) {
+  const uint64_t nl = *nlong;
+  for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nl; t += nw) {
+    const uint32_t s = longs[t];
     const uint32_t b = off[s], m = off[s + 1] - b;
     for (uint32_t i0 = 0; i0 < m; i0 += 32) {
       const bool have = i0 + lane < m;
@@ -910,15 +940,19 @@ int launch_reverse_lists(dem_ctx* c) {
   }
   int rc = scan_exclusive_u32(c, c->rev_cnt, c->rev_off, n);
   if (rc) return rc;
-  ProfScope ps(c, K_REVERSE, 1 + (go ? 1 : 0) + (n ? 1 : 0));
+  ProfScope ps(c, K_REVERSE, 1 + (go ? 1 : 0) + (n ? 2 : 0));
   // the contact work list L1 (capacity rcap, like rev_idx) holds the unsorted
   // lists: the step's contact phase, after the rebuild, refills it
   uint32_t* unsorted = c->L1;
   k_zero_u32<<<grid_for(n + 1, 256), 256, 0, st>>>(c->rev_cnt, n + 1);
   if (go) k_rev_fill<<<gi, 256, 0, st>>>(I, ni, nd, c->rev_off, c->rev_cnt, unsorted);
   if (n) {
-    const unsigned gr = (unsigned)std::min<uint64_t>((n * 32 + 255) / 256, (uint64_t)c->num_sms * 16);
-    k_rev_rank<<<gr, 256, 0, st>>>(n, c->rev_off, I.owner, c->P[c->pcur].id, unsorted, c->rev_idx);
+    // rev_cnt (the fill's cursors) is free again: the queue of long lists
+    DEM_CUDA_TRY(c, cudaMemsetAsync(c->rev_nlong, 0, sizeof(unsigned int), st));
+    k_rev_short<<<grid_for(n, 256), 256, 0, st>>>(n, c->rev_off, I.owner, c->P[c->pcur].id, unsorted, c->rev_idx,
+                                                  c->rev_cnt, c->rev_nlong);
+    k_rev_rank<<<(unsigned)c->num_sms * 16u, 256, 0, st>>>(c->rev_nlong, c->rev_cnt, c->rev_off, I.owner,
+                                                           c->P[c->pcur].id, unsorted, c->rev_idx);
   }
   DEM_CUDA_TRY(c, cudaGetLastError());
   return DEM_OK;
