@@ -186,12 +186,16 @@ __global__ void k_gather(PArrays P, Records R, uint64_t n, const uint32_t* __res
   if (s >= n) return;
   V3 f = ldv(P, FX, (uint32_t)s);
   V3 m = ldv(P, MX, (uint32_t)s);
+  // a record whose live flag is 0 is zero (+0 or -0 components); the sums start
+  // at +0 or a nonzero value and never become -0, so skipping it keeps every bit
   for (uint32_t k = own_off[s]; k < own_off[s + 1]; k++) {
+    if (!R.live[k]) continue;
     f = f + mk(R.f[0][k], R.f[1][k], R.f[2][k]);
     m = m + mk(R.ti[0][k], R.ti[1][k], R.ti[2][k]);
   }
   for (uint32_t q = rev_off[s]; q < rev_off[s + 1]; q++) {
     const uint32_t k = rev_idx[q];
+    if (!R.live[k]) continue;
     f = f + (-mk(R.f[0][k], R.f[1][k], R.f[2][k]));
     m = m + mk(R.tj[0][k], R.tj[1][k], R.tj[2][k]);
   }

@@ -1904,9 +1904,13 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
     if (a.cohesive) contact = (contact || d.dn <= dncut);
     if (!contact) {
       const V3 z = mk(0, 0, 0);
-      pwrite(a, k, z, z, z, z, z);
-      a.cs.write(k, 0.0, d.cp, z, z);  // item.reset(), dn = 0, the detector's contact point
+      if (a.R.live[k]) {  // item.reset(): history and record zeroed once, then skipped by the gathers
+        pwrite(a, k, z, z, z, z, z);
+        a.R.live[k] = 0;
+      }
+      a.cs.write(k, 0.0, d.cp, z, z);  // dn = 0, the detector's contact point
     } else if (a.cohesive && d.dn >= 0 && !is_mesh) {
+      a.R.live[k] = 1;
       const dem_contact_params& hkp = *hp;
       const double fn_value = (hkp.fc / hkp.dncut) * d.dn - hkp.fc;
       const V3 f = mk(0, 0, 0) + fn_value * d.n;
@@ -1921,6 +1925,7 @@ __global__ void __launch_bounds__(PT) k_pdetect(PCArgs a) {
       }
     } else {
       heavy = true;
+      a.R.live[k] = 1;  // k_phooke writes the record
     }
   }
   const uint32_t pos = warp_append2(heavy, a.cnt + 1);
