@@ -14,8 +14,8 @@
 //
 // Split precision (fp32_contact_screen): a pair whose FP32 distance test
 // proves dn > max(0, dncut) (the proof margin covers the FP32 rounding of the
-// squared distance, see DESIGN) takes the no-contact branch (history reset)
-// without any FP64 work; every other pair runs the full FP64 law.
+// squared distance) takes the no-contact branch (history reset) without any
+// FP64 work; every other pair runs the full FP64 law.
 #include "contact_core.cuh"
 #include "mesh_core.cuh"
 

@@ -88,11 +88,14 @@ typedef struct dem_params {
   int32_t law;             /* DEM_LAW_* */
   dem_contact_params config;        /* contact_sphere slot "config"        */
   dem_contact_params config_driver; /* contact_sphere slot "config_driver" */
-  /* Split-precision switches (no effect on results, see DESIGN):
+  /* Split-precision switches (no effect on results):
    * fp32_broad_phase: FP32 cell-relative broad phase with a proven superset bound,
    *                   then an exact FP64 decision in the rounding band;
-   * fp32_contact_screen: FP32 test that skips the FP64 contact law for pairs
-   *                   that are provably apart.                            */
+   *                   polyhedra: FP32 feature tests with error bounds, FP64
+   *                   where undecided;
+   * fp32_contact_screen: FP32 test that skips the FP64 contact law (spheres)
+   *                   or detection (polyhedra, fused step) for pairs that are
+   *                   provably apart.                                      */
   int32_t fp32_broad_phase;
   int32_t fp32_contact_screen;
   /* fused_step: dem_step runs the fused kernels (prolog + displacement test,
