@@ -72,6 +72,16 @@ __device__ Case run_case(uint64_t seed, uint64_t t) {
       OBBd o;
       o.c = pB + g.vec(0.5 * sc);
       frame(g, o.e1, o.e2, o.e3);
+      if (g.next() & 1) {  // axes along the world axes up to a rotation of 1e-17 .. 1e-6 (cube covariance OBBs)
+        const double tilt = pow(10.0, g.uni(-17.0, -6.0));
+        V3 a = mk(1.0, tilt * g.uni(-1.0, 1.0), tilt * g.uni(-1.0, 1.0));
+        a = a / vnorm(a);
+        V3 b = cross(mk(tilt * g.uni(-1.0, 1.0), tilt * g.uni(-1.0, 1.0), 1.0), a);
+        b = b / vnorm(b);
+        o.e1 = a;
+        o.e2 = b;
+        o.e3 = cross(a, b);
+      }
       o.ext = mk(g.uni(0.1, 1.0) * sc, g.uni(0.1, 1.0) * sc, g.uni(0.1, 1.0) * sc);
       const double rv = g.uni(0.0, 0.05) * sc;
       // a point near the enlarged box surface (face, edge or corner region)

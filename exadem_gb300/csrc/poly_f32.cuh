@@ -191,6 +191,12 @@ __device__ __forceinline__ int cmp_gt(float x, float thr, float e) {
 // obb centre and extents are FP32 roundings of the FP64 values (u T), axes
 // u per component, p carries ETA; every |t_L| and radius sum is a sum of at most
 // 6 products of magnitude <= 2T with |factor| <= 1 + tol.  Bound: 2^-17 T.
+// A cross axis A_k x W_l weighs t by the two entries R[k1][l], R[k2][l]: the
+// error of its projection is at most (2^-17 T + 4u T)(|R[k1][l]| + |R[k2][l]|)
+// (each t within 2^-17 T, each entry an FP32 rounding), that of its radius sum
+// at most 8u of it.  When A_k is nearly a world axis (the covariance OBB of a
+// cube is the world-aligned one) both entries vanish and this bound, far below
+// 2^-17 T, still decides the axis.
 __device__ __forceinline__ int decide_gate(const OBBf& o, F3 p, float rv, float S) {
   const float tol = 1.1920929e-07f;
   const F3 tt = o.c - p;
@@ -232,7 +238,9 @@ __device__ __forceinline__ int decide_gate(const OBBf& o, F3 p, float rv, float 
       const int l1 = (l + 1) % 3, l2 = (l + 2) % 3;
       const float ra = o.ext[k1] * Ab[k2][l] + o.ext[k2] * Ab[k1][l];
       const float rb = rv * (Ab[k][l2] + Ab[k][l1]);
-      const int c = cmp_gt(fabsf(t[k2] * R[k1][l] - t[k1] * R[k2][l]), ra + rb, e);
+      const float lhs = fabsf(t[k2] * R[k1][l] - t[k1] * R[k2][l]), rhs = ra + rb;
+      const float ex = (e + 4.f * F32_U * T) * (fabsf(R[k1][l]) + fabsf(R[k2][l])) + 8.f * F32_U * (lhs + rhs);
+      const int c = cmp_gt(lhs, rhs, fminf(e, ex));
       if (c > 0) return DEC_FALSE;
       undecided |= c == 0;
     }
