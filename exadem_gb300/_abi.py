@@ -237,6 +237,7 @@ def declare_library(lib) -> None:
     _sig(lib, "dem_stick_polyhedra", [_CTX, PU64, PD, C.c_uint64, D, PU64])
     _sig(lib, "dem_bond_count", [_CTX, PU64])
     _sig(lib, "dem_get_bonds", [_CTX, C.POINTER(BondList)])
+    _sig(lib, "dem_get_bond_state", [_CTX, C.c_uint64, PU64, PD, PD, PD])
     _sig(lib, "dem_set_bonds", [_CTX, C.POINTER(BondList)])
     _sig(lib, "dem_broken_interface_count", [_CTX, PU64])
     _sig(lib, "dem_inner_bond_polyhedron", [_CTX])
@@ -267,7 +268,7 @@ EXPORTED = ["dem_ctx_create", "dem_ctx_destroy", "dem_last_error", "dem_ctx_stre
             "dem_mlp_train", "dem_learned_stats", "dem_set_inner_bond_params", "dem_stick_polyhedra",
             "dem_bond_count", "dem_get_bonds", "dem_set_bonds", "dem_broken_interface_count",
             "dem_inner_bond_polyhedron", "dem_apply_interface_fracture_criterion", "dem_set_contact_int_share",
-            "dem_set_sphere_cell_broad_phase"]
+            "dem_set_sphere_cell_broad_phase", "dem_get_bond_state"]
 
 _LIB = None
 

@@ -4,12 +4,15 @@ the library keeps while analysis is on (System.set_analysis).
 
 Per particle pair (the contact law's particles i = pi_, j = pj_) the network
 holds the number of interactions with a non-zero force |fn + ft| and the
-sums of their fn and ft.  Particle-particle types only (0-3); the reference
-adds inner bonds, which this build does not have.  The reference skips
-interactions whose partner is a ghost (filter_duplicates): here those are
-the periodic images, found as pairs whose raw centre distance exceeds their
-interaction range.  Its std::map orders pairs by grid cell; here they come in
-(id_i, id_j) order.  The files are the reference's VTK PolyData text: one
+sums of their fn and ft: the particle-particle contacts (types 0-3), then the
+inner bonds (dump_contact_network.cpp:69-88 adds both, in that order; a bond's
+state is inner_bond_law's fn = f_i - friction and friction, read with
+System.bond_state).  The reference skips interactions whose partner is a
+ghost (filter_duplicates): here those are the periodic images, found as pairs
+whose raw centre offset is longer than half the period along a periodic axis
+(a periodic axis has at least three cells of the interaction reach, so a pair
+in reach directly is never that far apart).  Its std::map orders pairs by grid
+cell; here they come in (id_i, id_j) order.  The files are the reference's VTK PolyData text: one
 `.vtp` per rank in `basename/`, indexed by `basename.pvtp`, values printed
 like a C++ stream's default format (6 significant digits)."""
 from __future__ import annotations
@@ -29,22 +32,30 @@ def contact_network(system) -> dict:
     fn = cs["fn"].reshape(-1, 3)
     ft = cs["ft"].reshape(-1, 3)
     prm = system.params
-    reach_extra = prm.rcut_inc + max(prm.config.dncut, 0.0)
+    period = np.array([prm.bounds_hi[d] - prm.bounds_lo[d] for d in range(3)])
+    periodic = np.array([bool(prm.periodic[d]) for d in range(3)])
     net = {}
-    for k in np.flatnonzero(it["type"] <= 3):
-        f = fn[k] + ft[k]
+
+    def add(i, j, fnk, ftk):
+        f = fnk + ftk
         if not np.sqrt(f @ f) != 0.0:
-            continue
-        a, b = int(it["owner_id"][k]), int(it["partner_id"][k])
-        i, j = (b, a) if it["swap"][k] else (a, b)  # the law's particles pi_, pj_
-        ri, rj = r[row[i]], r[row[j]]
-        d = rj - ri
-        if np.sqrt(d @ d) > p["radius"][row[i]] + p["radius"][row[j]] + reach_extra:
-            continue  # a periodic image partner: the reference's PartnerGhost
+            return
+        d = r[row[j]] - r[row[i]]
+        if np.any(periodic & (np.abs(d) > 0.5 * period)):
+            return  # a periodic image partner: the reference's PartnerGhost
         e = net.setdefault((i, j), [0, np.zeros(3), np.zeros(3)])
         e[0] += 1
-        e[1] = e[1] + fn[k]
-        e[2] = e[2] + ft[k]
+        e[1] = e[1] + fnk
+        e[2] = e[2] + ftk
+
+    for k in np.flatnonzero(it["type"] <= 3):
+        a, b = int(it["owner_id"][k]), int(it["partner_id"][k])
+        i, j = (b, a) if it["swap"][k] else (a, b)  # the law's particles pi_, pj_
+        add(i, j, fn[k], ft[k])
+    if system.bond_count():
+        bl, bs = system.bonds(), system.bond_state()
+        for k in range(len(bl["id_i"])):
+            add(int(bl["id_i"][k]), int(bl["id_j"][k]), bs["fn"][k], bs["ft"][k])
     keys = sorted(net)
     return {"pairs": np.asarray(keys, dtype=np.uint64).reshape(-1, 2),
             "n": np.asarray([net[q][0] for q in keys], dtype=np.int64),

@@ -999,6 +999,29 @@ int dem_get_bonds(dem_ctx* c, dem_bond_list* l) {
   return DEM_OK;
 }
 
+int dem_get_bond_state(dem_ctx* c, uint64_t capacity, uint64_t* count, double* dn, double* fn, double* ft) {
+  if (!c) return DEM_ERR_INVALID_ARG;
+  const uint64_t m = c->nb;
+  if (count) *count = m;
+  if (capacity < m) return c->fail(DEM_ERR_INVALID_ARG, "bond state capacity too small");
+  if (!m) return DEM_OK;
+  const BondArrays& B = c->B[c->bcur];
+  DEM_CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (dn) DEM_CUDA_TRY(c, cudaMemcpy(dn, B.dn, m * 8, cudaMemcpyDeviceToHost));
+  std::vector<double> t(m);
+  for (int q = 0; q < 3; q++) {
+    if (fn) {
+      DEM_CUDA_TRY(c, cudaMemcpy(t.data(), B.fn[q], m * 8, cudaMemcpyDeviceToHost));
+      for (uint64_t k = 0; k < m; k++) fn[3 * k + q] = t[k];
+    }
+    if (ft) {
+      DEM_CUDA_TRY(c, cudaMemcpy(t.data(), B.ft[q], m * 8, cudaMemcpyDeviceToHost));
+      for (uint64_t k = 0; k < m; k++) ft[3 * k + q] = t[k];
+    }
+  }
+  return DEM_OK;
+}
+
 int dem_set_bonds(dem_ctx* c, const dem_bond_list* l) {
   if (!c || !l) return DEM_ERR_INVALID_ARG;
   if (!c->poly) return c->fail(DEM_ERR_STATE, "bonds need polyhedron shapes (dem_set_shapes)");

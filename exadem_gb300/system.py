@@ -430,6 +430,18 @@ class System:
         out["friction"] = out["friction"].reshape(-1, 3)
         return out
 
+    def bond_state(self) -> dict:
+        """dem_get_bond_state: dn, fn (= f_i - friction) and the friction of each bond
+        after the last bond pass, in the rows of bonds()."""
+        m = self.bond_count()
+        out = {"dn": np.zeros(m), "fn": np.zeros(3 * m), "ft": np.zeros(3 * m)}
+        cnt = C.c_uint64()
+        self._check(self.b.get_bond_state(self.h, m, C.byref(cnt), A.ptr(out["dn"]), A.ptr(out["fn"]),
+                                          A.ptr(out["ft"])), "get_bond_state")
+        out["fn"] = out["fn"].reshape(-1, 3)
+        out["ft"] = out["ft"].reshape(-1, 3)
+        return out
+
     def set_bonds(self, bonds: dict) -> None:
         """read_dump_particle_fragmentation's restore (a dict as bonds() returns)."""
         m = len(bonds["id_i"])

@@ -562,6 +562,13 @@ int dem_get_bonds(dem_ctx* ctx, dem_bond_list* out);
 /* read_dump_particle_fragmentation: installs a saved bond list (rows as
  * dem_get_bonds writes them) for the particles currently set, by id.     */
 int dem_set_bonds(dem_ctx* ctx, const dem_bond_list* list);
+/* Contact state of the inner bonds, as inner_bond_law returns it for the
+ * analysis (src/polyhedron/include/exaDEM/polyhedron/inner_bond.hpp:167-184):
+ * per bond of the last bond pass, dn, fn = f_i - friction and the friction, in
+ * the rows of dem_get_bonds.  capacity: rows the arrays hold (count written to
+ * *count); fn and ft hold 3 per row; a null array is skipped.  Zero before the
+ * first bond pass.  dump_contact_network adds these to the network. */
+int dem_get_bond_state(dem_ctx* ctx, uint64_t capacity, uint64_t* count, double* dn, double* fn, double* ft);
 /* Interfaces broken since the context was made (the sum of the
  * apply_interface_fracture_criterion results). */
 int dem_broken_interface_count(dem_ctx* ctx, uint64_t* out);

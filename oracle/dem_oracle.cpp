@@ -2282,6 +2282,25 @@ int oracle_bond_count(void* h, uint64_t* out) {
   *out = ((Oracle*)h)->bonds.size();
   return DEM_OK;
 }
+// dem_get_bond_state: dn, fn = f_i - friction, friction of the last bond pass
+// (inner_bond.hpp:167-184), in bond order
+int oracle_get_bond_state(void* h, uint64_t capacity, uint64_t* count, double* dn, double* fn, double* ft) {
+  Oracle& o = *(Oracle*)h;
+  const uint64_t m = o.bonds.size();
+  if (count) *count = m;
+  if (capacity < m) return DEM_ERR_INVALID_ARG;
+  for (uint64_t k = 0; k < m; k++) {
+    const BondRec r = k < o.brec.size() ? o.brec[k] : BondRec{};
+    const Bond& b = o.bonds[k];
+    if (dn) dn[k] = r.dn;
+    const double n3[3] = {r.fn.x, r.fn.y, r.fn.z}, f3[3] = {b.friction.x, b.friction.y, b.friction.z};
+    for (int d = 0; d < 3; d++) {
+      if (fn) fn[3 * k + d] = n3[d];
+      if (ft) ft[3 * k + d] = f3[d];
+    }
+  }
+  return DEM_OK;
+}
 int oracle_get_bonds(void* h, dem_bond_list* l) {
   Oracle& o = *(Oracle*)h;
   l->count = o.bonds.size();

@@ -58,6 +58,7 @@ def load(rebuild: bool = True):
         sig("oracle_stick_polyhedra", [_CTX, A.PU64, A.PD, C.c_uint64, C.c_double, A.PU64])
         sig("oracle_bond_count", [_CTX, A.PU64])
         sig("oracle_get_bonds", [_CTX, C.POINTER(A.BondList)])
+        sig("oracle_get_bond_state", [_CTX, C.c_uint64, A.PU64, A.PD, A.PD, A.PD])
         sig("oracle_set_bonds", [_CTX, C.POINTER(A.BondList)])
         sig("oracle_broken_interface_count", [_CTX, A.PU64])
         sig("oracle_inner_bond_polyhedron", [_CTX])
@@ -85,6 +86,7 @@ class OracleBackend:
             "stress_tensor": "oracle_stress_tensor", "set_inner_bond_params": "oracle_set_inner_bond_params",
             "stick_polyhedra": "oracle_stick_polyhedra", "bond_count": "oracle_bond_count",
             "get_bonds": "oracle_get_bonds", "set_bonds": "oracle_set_bonds",
+            "get_bond_state": "oracle_get_bond_state",
             "broken_interface_count": "oracle_broken_interface_count",
             "inner_bond_polyhedron": "oracle_inner_bond_polyhedron",
             "apply_interface_fracture_criterion": "oracle_apply_interface_fracture_criterion"}

@@ -29,6 +29,9 @@ def assert_same_bonds(g, o):
     assert len(bg["id_i"]) == len(bo["id_i"])
     for k in bg:
         assert same_bits(bg[k], bo[k]), k
+    sg, so = g.bond_state(), o.bond_state()  # the analysis state of the last bond pass
+    for k in sg:
+        assert same_bits(sg[k], so[k]), k
 
 
 def assert_same_particles(g, o):
