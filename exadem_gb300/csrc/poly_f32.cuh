@@ -213,6 +213,10 @@ __device__ __forceinline__ int decide_gate(const OBBf& o, F3 p, float rv, float 
     for (int l = 0; l < 3; l++) Ab[k][l] = fabsf(R[k][l]) + tol;
   }
   const float t[3] = {fdot(tt, o.e[0]), fdot(tt, o.e[1]), fdot(tt, o.e[2])};
+  // p inside the OBB (beyond the bound): the two boxes share p, so no axis
+  // separates them (every projection of t stays below the OBB's radius on it)
+  const float in = F32_SAFE * e;
+  if (fabsf(t[0]) < o.ext[0] - in && fabsf(t[1]) < o.ext[1] - in && fabsf(t[2]) < o.ext[2] - in) return DEC_TRUE;
   bool undecided = false;
   // A's axes
 #pragma unroll
