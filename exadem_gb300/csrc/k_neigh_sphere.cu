@@ -178,12 +178,23 @@ __device__ inline void for_each_particle(const BPArgs& a, uint32_t s, int sys, E
           sx = 1;
         }
         const uint32_t cc = coff + (uint32_t)x + (uint32_t)d0 * ((uint32_t)y + (uint32_t)d1 * (uint32_t)z);
-        const uint32_t qb = a.cell_start[cc], qe = a.cell_start[cc + 1];
+        uint32_t qb = a.cell_start[cc];
+        const uint32_t qe = a.cell_start[cc + 1];
         const bool ghost = (sx | sy | sz) != 0;
         const float oxf = (float)dx * csx, oyf = (float)dy * csy, ozf = (float)dz * csz;
+        if (!ghost) {  // a cell's particles are in id order: the owner rule keeps the suffix above idi
+          uint32_t hi = qe;
+          while (qb < hi) {
+            const uint32_t mid = (qb + hi) >> 1;
+            if (id[mid] <= idi)
+              qb = mid + 1;
+            else
+              hi = mid;
+          }
+        }
         for (uint32_t q = qb; q < qe; q++) {
           const uint64_t idj = id[q];
-          if (!ghost && idi >= idj) continue;  // owner rule first (integer test)
+          if (!ghost && idi >= idj) continue;  // owner rule (kept: the suffix already satisfies it)
           int keep = -1;
           if (F32) {
             const float xj = a.xr[q], yj = a.yr[q], zj = a.zr[q];

@@ -353,9 +353,18 @@ __device__ inline void for_each_unit(const UnitArgs& a, uint32_t s, Emit&& emit)
         if (x < 0 || x >= d0) continue;
         const uint32_t cc = (uint32_t)x + (uint32_t)d0 * ((uint32_t)y + (uint32_t)d1 * (uint32_t)z);
         const float oxf = (float)dx * a.csz[0], oyf = (float)dy * a.csz[1], ozf = (float)dz * a.csz[2];
-        for (uint32_t q = a.cell_start[cc]; q < a.cell_start[cc + 1]; q++) {
+        // a cell's particles are in id order (k_cell_sort): the owner rule keeps
+        // the suffix of ids above idi, found by bisection
+        uint32_t q0 = a.cell_start[cc], q1 = a.cell_start[cc + 1];
+        while (q0 < q1) {
+          const uint32_t mid = (q0 + q1) >> 1;
+          if (a.P.id[mid] <= idi)
+            q0 = mid + 1;
+          else
+            q1 = mid;
+        }
+        for (uint32_t q = q0; q < a.cell_start[cc + 1]; q++) {
           const uint64_t idj = a.P.id[q];
-          if (idi >= idj) continue;
           int keep = -1;
           if (a.f32) {
             const float xj = a.xr[q], yj = a.yr[q], zj = a.zr[q];
